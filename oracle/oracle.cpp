@@ -1,0 +1,1318 @@
+// ORACLE — test infrastructure only. Never linked into, loaded by, or called from the
+// product library (researchuv_gb300 / libruv). Only tests/, __graft_entry__.smoke() and
+// bench.py's cpu_baseline / reference legs use it, and only as the checker.
+//
+// A CPU restatement of ResearchUV's per-chart LSCM unfold path, written from the
+// reference's Rust source semantics (paths relative to crates/, `researchuv-` dropped):
+//   weld                 unwrap/src/weld.rs:19-57
+//   segment / charts     unwrap/src/segment.rs:61-331
+//   eig3                 unwrap/src/lscm_eig.rs:13-66
+//   tangent_frame        unwrap/src/lscm.rs:152-183
+//   rect_point           unwrap/src/lscm.rs:187-204
+//   anchor_ids           unwrap/src/lscm.rs:210-247
+//   edge_weights         unwrap/src/lscm.rs:252-274
+//   border_targets       unwrap/src/lscm.rs:280-413
+//   unfold_chart driver  unwrap/src/lscm.rs:512-727 (default path: KeepMetric = false)
+//   Sparse + LU          unwrap/src/sparse.rs:19-265
+//   meshgen fixtures     unwrap/src/meshgen.rs:12-198
+//   chart_distortion     unwrap/src/metrics.rs:41-141
+//   vector arithmetic    math/src/vec.rs:100-124
+//
+// Arithmetic follows the Rust evaluation order (left-to-right sums, no FMA contraction:
+// compile with -ffp-contract=off) so that results are bit-identical to the reference on
+// the same host libm.  Parity pinning: the reference (pure Rust) cannot be built in this
+// environment, so this restatement is pinned against the known answers of the reference's
+// own tests (unwrap/tests/parity.rs, unwrap/src/sparse.rs tests, lscm_eig.rs tests,
+// meshgen.rs tests, segment.rs tests, weld.rs tests), transcribed with citations into
+// tests/golden/reference_known_answers.json.
+//
+// Interface: a "bag" of named f64 / i64 arrays behind an opaque handle (ctypes-friendly).
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <set>
+#include <string>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- vec.rs arithmetic
+struct V3 {
+  double x, y, z;
+};
+struct V2 {
+  double u, v;
+};
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 divs(V3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross_v(V3 a, V3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline double len3(V3 a) { return std::sqrt(dot(a, a)); }
+// Vec3::cross(a, b, c) = (a - b) x (c - b)   (math/src/vec.rs:100-102)
+inline V3 cross3(V3 a, V3 b, V3 c) { return cross_v(sub(a, b), sub(c, b)); }
+inline V2 sub2(V2 a, V2 b) { return {a.u - b.u, a.v - b.v}; }
+
+// Rust f64::max / f64::min (NaN-ignoring maxNum/minNum).
+inline double rmax(double a, double b) {
+  if (std::isnan(a)) return b;
+  if (std::isnan(b)) return a;
+  return a > b ? a : b;
+}
+inline double rmin(double a, double b) {
+  if (std::isnan(a)) return b;
+  if (std::isnan(b)) return a;
+  return a < b ? a : b;
+}
+// Rust f64::total_cmp as a strict-weak "less".
+inline int64_t total_key(double a) {
+  int64_t i;
+  std::memcpy(&i, &a, 8);
+  i ^= (int64_t)(((uint64_t)(i >> 63)) >> 1);
+  return i;
+}
+// Rust `x as i64` (saturating, NaN -> 0).
+inline int64_t sat_i64(double x) {
+  if (std::isnan(x)) return 0;
+  if (x >= 9.2233720368547758e18) return std::numeric_limits<int64_t>::max();
+  if (x <= -9.2233720368547758e18) return std::numeric_limits<int64_t>::min();
+  return (int64_t)x;
+}
+
+constexpr double EPS_DEGENERATE = 1.1754943508222875e-38;  // lscm.rs:36
+constexpr double PI = 3.14159265358979323846;
+
+// ---------------------------------------------------------------- meshes
+struct Mesh {
+  std::vector<V3> pos;
+  std::vector<std::array<uint32_t, 3>> faces;
+};
+
+// weld.rs:19-57 — rounding-grid weld, first occurrence is canonical, collapsed faces dropped.
+Mesh weld(const Mesh& in, double tol) {
+  if (tol <= 0.0) return in;
+  struct KeyHash {
+    size_t operator()(const std::tuple<int64_t, int64_t, int64_t>& k) const {
+      uint64_t h = (uint64_t)std::get<0>(k) * 0x9E3779B97F4A7C15ull;
+      h ^= (uint64_t)std::get<1>(k) + 0x7F4A7C159E3779B9ull + (h << 6) + (h >> 2);
+      h ^= (uint64_t)std::get<2>(k) + 0x94D049BB133111EBull + (h << 6) + (h >> 2);
+      return (size_t)h;
+    }
+  };
+  double inv = 1.0 / tol;
+  std::unordered_map<std::tuple<int64_t, int64_t, int64_t>, uint32_t, KeyHash> canon;
+  canon.reserve(in.pos.size() * 2);
+  std::vector<uint32_t> remap(in.pos.size());
+  Mesh out;
+  for (size_t i = 0; i < in.pos.size(); ++i) {
+    V3 p = in.pos[i];
+    auto key = std::make_tuple(sat_i64(std::round(p.x * inv)), sat_i64(std::round(p.y * inv)),
+                               sat_i64(std::round(p.z * inv)));
+    auto it = canon.find(key);
+    uint32_t c;
+    if (it == canon.end()) {
+      c = (uint32_t)out.pos.size();
+      canon.emplace(key, c);
+      out.pos.push_back(p);
+    } else {
+      c = it->second;
+    }
+    remap[i] = c;
+  }
+  for (auto& f : in.faces) {
+    std::array<uint32_t, 3> g{remap[f[0]], remap[f[1]], remap[f[2]]};
+    if (g[0] != g[1] && g[1] != g[2] && g[0] != g[2]) out.faces.push_back(g);
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------- segment.rs
+using EdgeKey = std::pair<uint32_t, uint32_t>;
+inline EdgeKey edge_key(uint32_t a, uint32_t b) { return a < b ? EdgeKey{a, b} : EdgeKey{b, a}; }
+
+struct Chart {
+  std::vector<size_t> face_ids;
+  std::vector<uint32_t> vertex_ids;
+  std::vector<std::array<uint32_t, 3>> tris;
+  std::vector<uint32_t> border;
+  std::vector<std::vector<uint32_t>> border_loops;
+  double area3d = 0.0;
+  long local_of(uint32_t v) const {
+    auto it = std::lower_bound(vertex_ids.begin(), vertex_ids.end(), v);
+    if (it != vertex_ids.end() && *it == v) return (long)(it - vertex_ids.begin());
+    return -1;
+  }
+};
+
+std::vector<double> face_areas3d(const Mesh& m) {  // segment.rs:61-70
+  std::vector<double> a(m.faces.size());
+  for (size_t f = 0; f < m.faces.size(); ++f) {
+    V3 e1 = sub(m.pos[m.faces[f][1]], m.pos[m.faces[f][0]]);
+    V3 e2 = sub(m.pos[m.faces[f][2]], m.pos[m.faces[f][0]]);
+    a[f] = 0.5 * len3(cross_v(e1, e2));
+  }
+  return a;
+}
+
+std::map<EdgeKey, std::vector<size_t>> edge_faces(const Mesh& m) {  // segment.rs:73-81
+  std::map<EdgeKey, std::vector<size_t>> ef;
+  for (size_t fi = 0; fi < m.faces.size(); ++fi) {
+    auto& f = m.faces[fi];
+    uint32_t a = f[0], b = f[1], c = f[2];
+    ef[edge_key(a, b)].push_back(fi);
+    ef[edge_key(b, c)].push_back(fi);
+    ef[edge_key(c, a)].push_back(fi);
+  }
+  return ef;
+}
+
+V3 face_normal_unit(const Mesh& m, size_t fi) {  // segment.rs:104-117
+  auto& f = m.faces[fi];
+  V3 n = cross3(m.pos[f[0]], m.pos[f[1]], m.pos[f[2]]);
+  double l = len3(n);
+  if (l < 1e-30) return {0.0, 0.0, 1.0};
+  return divs(n, l);
+}
+
+std::vector<std::vector<uint32_t>> chart_border_loops(const Mesh& mesh,
+                                                      const std::vector<size_t>& comp,
+                                                      const std::set<EdgeKey>& cut,
+                                                      const std::set<EdgeKey>& mbnd,
+                                                      const std::map<uint32_t, uint32_t>& vid) {
+  // segment.rs:227-331 — keep-going-straight boundary walk.
+  std::set<EdgeKey> bnd_edges;
+  for (size_t f : comp) {
+    auto& t = mesh.faces[f];
+    uint32_t pr[3][2] = {{t[0], t[1]}, {t[1], t[2]}, {t[2], t[0]}};
+    for (auto& e : pr) {
+      EdgeKey k = edge_key(e[0], e[1]);
+      if (cut.count(k) || mbnd.count(k)) bnd_edges.insert(k);
+    }
+  }
+  std::vector<std::vector<uint32_t>> loops;
+  if (bnd_edges.empty()) return loops;
+  std::map<uint32_t, std::vector<uint32_t>> adj;
+  for (auto& e : bnd_edges) {
+    if (vid.count(e.first) && vid.count(e.second)) {
+      adj[e.first].push_back(e.second);
+      adj[e.second].push_back(e.first);
+    }
+  }
+  std::set<EdgeKey> used;
+  std::vector<uint32_t> starts;
+  for (auto& kv : adj) starts.push_back(kv.first);
+  for (uint32_t start : starts) {
+    bool has_unused = false;
+    for (uint32_t n : adj[start])
+      if (!used.count(edge_key(start, n))) {
+        has_unused = true;
+        break;
+      }
+    if (!has_unused) continue;
+    std::vector<uint32_t> loop_v{start};
+    uint32_t cur = start;
+    std::vector<uint32_t> cands = adj[start];
+    std::sort(cands.begin(), cands.end());
+    if (cands.empty()) continue;
+    uint32_t first = cands[0];
+    used.insert(edge_key(cur, first));
+    uint32_t prev = cur;
+    cur = first;
+    loop_v.push_back(cur);
+    for (;;) {
+      std::vector<uint32_t> nxts;
+      auto it = adj.find(cur);
+      if (it != adj.end())
+        for (uint32_t n : it->second)
+          if (n != prev && !used.count(edge_key(cur, n))) nxts.push_back(n);
+      if (nxts.empty()) break;
+      V3 d_in = sub(mesh.pos[cur], mesh.pos[prev]);
+      double ln = len3(d_in);
+      uint32_t next;
+      if (ln < 1e-30) {
+        next = nxts[0];
+      } else {
+        V3 din = divs(d_in, ln);
+        bool have = false;
+        double bd = 0.0;
+        uint32_t bn = nxts[0];
+        for (uint32_t n : nxts) {
+          double dt = dot(sub(mesh.pos[n], mesh.pos[cur]), din);
+          if (have && dt <= bd) continue;
+          have = true;
+          bd = dt;
+          bn = n;
+        }
+        next = bn;
+      }
+      used.insert(edge_key(cur, next));
+      prev = cur;
+      cur = next;
+      loop_v.push_back(cur);
+      if (cur == start) break;
+    }
+    if (loop_v.size() >= 4) loops.push_back(std::move(loop_v));
+  }
+  return loops;
+}
+
+std::vector<Chart> segment(const Mesh& mesh, double angle_min_deg, size_t* n_cut_out) {
+  // segment.rs:85-102 (dihedrals), :130-140 (segment), :143-223 (build_charts)
+  double th = angle_min_deg * (PI / 180.0);
+  auto ef = edge_faces(mesh);
+  std::set<EdgeKey> cut, mbnd;
+  for (auto& kv : ef) {
+    double ang;
+    if (kv.second.size() == 1) {
+      ang = 0.0;
+      mbnd.insert(kv.first);
+    } else if (kv.second.size() == 2) {
+      V3 n1 = face_normal_unit(mesh, kv.second[0]);
+      V3 n2 = face_normal_unit(mesh, kv.second[1]);
+      double d = dot(n1, n2);
+      if (d < -1.0) d = -1.0;
+      if (d > 1.0) d = 1.0;
+      ang = std::acos(d);
+    } else {
+      ang = PI;
+    }
+    if (ang > th) cut.insert(kv.first);
+  }
+  if (n_cut_out) *n_cut_out = cut.size();
+  auto areas = face_areas3d(mesh);
+  size_t nf = mesh.faces.size();
+  std::vector<char> seen(nf, 0);
+  std::vector<Chart> charts;
+  for (size_t fi = 0; fi < nf; ++fi) {
+    if (seen[fi]) continue;
+    std::vector<size_t> stack{fi};
+    seen[fi] = 1;
+    std::vector<size_t> comp;
+    while (!stack.empty()) {
+      size_t f = stack.back();
+      stack.pop_back();
+      comp.push_back(f);
+      auto& t = mesh.faces[f];
+      uint32_t pr[3][2] = {{t[0], t[1]}, {t[1], t[2]}, {t[2], t[0]}};
+      for (auto& e : pr) {
+        EdgeKey k = edge_key(e[0], e[1]);
+        if (cut.count(k)) continue;
+        auto it = ef.find(k);
+        if (it == ef.end()) continue;
+        for (size_t g : it->second)
+          if (!seen[g]) {
+            seen[g] = 1;
+            stack.push_back(g);
+          }
+      }
+    }
+    Chart ch;
+    std::set<uint32_t> vset;
+    for (size_t f : comp)
+      for (uint32_t v : mesh.faces[f]) vset.insert(v);
+    ch.vertex_ids.assign(vset.begin(), vset.end());
+    std::map<uint32_t, uint32_t> vid;
+    for (size_t i = 0; i < ch.vertex_ids.size(); ++i) vid[ch.vertex_ids[i]] = (uint32_t)i;
+    for (size_t f : comp) {
+      auto& t = mesh.faces[f];
+      ch.tris.push_back({vid[t[0]], vid[t[1]], vid[t[2]]});
+    }
+    std::set<uint32_t> bnd;
+    for (size_t f : comp) {
+      auto& t = mesh.faces[f];
+      uint32_t pr[3][2] = {{t[0], t[1]}, {t[1], t[2]}, {t[2], t[0]}};
+      for (auto& e : pr) {
+        EdgeKey k = edge_key(e[0], e[1]);
+        if (cut.count(k) || mbnd.count(k)) {
+          bnd.insert(e[0]);
+          bnd.insert(e[1]);
+        }
+      }
+    }
+    ch.border.assign(bnd.begin(), bnd.end());
+    ch.border_loops = chart_border_loops(mesh, comp, cut, mbnd, vid);
+    double a = 0.0;
+    for (size_t f : comp) a += areas[f];
+    ch.area3d = a;
+    ch.face_ids = std::move(comp);
+    charts.push_back(std::move(ch));
+  }
+  return charts;
+}
+
+// ---------------------------------------------------------------- lscm_eig.rs:13-66
+void eig3(const double m[3][3], double w[3], double v[3][3]) {
+  double a[3][3];
+  std::memcpy(a, m, sizeof(a));
+  double vv[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    int p = 0, q = 1;
+    double max_off = std::fabs(a[0][1]);
+    int pairs[2][2] = {{0, 2}, {1, 2}};
+    for (auto& pq : pairs) {
+      double x = std::fabs(a[pq[0]][pq[1]]);
+      if (x > max_off) {
+        max_off = x;
+        p = pq[0];
+        q = pq[1];
+      }
+    }
+    if (max_off <= 1e-300) break;
+    double apq = a[p][q], app = a[p][p], aqq = a[q][q];
+    double theta = 0.5 * std::atan2(2.0 * apq, app - aqq);
+    double c = std::cos(theta), s = std::sin(theta);
+    for (int r = 0; r < 3; ++r) {
+      if (r == p || r == q) continue;
+      double ar_p = c * a[r][p] + s * a[r][q];
+      double ar_q = -s * a[r][p] + c * a[r][q];
+      a[r][p] = ar_p;
+      a[p][r] = ar_p;
+      a[r][q] = ar_q;
+      a[q][r] = ar_q;
+    }
+    a[p][p] = c * c * app + 2.0 * s * c * apq + s * s * aqq;
+    a[q][q] = s * s * app - 2.0 * s * c * apq + c * c * aqq;
+    a[p][q] = 0.0;
+    a[q][p] = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      double vp = vv[p][k], vq = vv[q][k];
+      vv[p][k] = c * vp - s * vq;
+      vv[q][k] = s * vp + c * vq;
+    }
+  }
+  w[0] = a[0][0];
+  w[1] = a[1][1];
+  w[2] = a[2][2];
+  std::memcpy(v, vv, sizeof(vv));
+}
+
+// lscm.rs:152-183
+std::vector<V2> tangent_frame(const std::vector<V3>& p3) {
+  size_t n = p3.size();
+  std::vector<V2> out;
+  if (n == 0) return out;
+  V3 c{0.0, 0.0, 0.0};
+  for (auto& p : p3) c = add(c, p);
+  c = divs(c, (double)n);
+  std::vector<V3> d(n);
+  for (size_t i = 0; i < n; ++i) d[i] = sub(p3[i], c);
+  double cm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (auto& v : d) {
+    double vi[3] = {v.x, v.y, v.z};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) cm[i][j] += vi[i] * vi[j];
+  }
+  double w[3], vv[3][3];
+  eig3(cm, w, vv);
+  int idx[3] = {0, 1, 2};
+  std::stable_sort(idx, idx + 3, [&](int a, int b) { return total_key(w[b]) < total_key(w[a]); });
+  V3 e1{vv[0][idx[0]], vv[1][idx[0]], vv[2][idx[0]]};
+  V3 e2{vv[0][idx[1]], vv[1][idx[1]], vv[2][idx[1]]};
+  out.resize(n);
+  for (size_t i = 0; i < n; ++i) out[i] = {dot(d[i], e1), dot(d[i], e2)};
+  return out;
+}
+
+// lscm.rs:187-204
+V2 rect_point(double f, double a, double b) {
+  double p2 = 2.0 * (a + b);
+  double t = std::fmod(f, 1.0) * p2;
+  double x0 = a / 2.0, y0 = -b / 2.0;
+  if (t < a) return {x0 - t, y0};
+  t -= a;
+  if (t < b) return {-a / 2.0, y0 + t};
+  t -= b;
+  if (t < a) return {-a / 2.0 + t, b / 2.0};
+  t -= a;
+  return {a / 2.0, b / 2.0 - t};
+}
+
+// lscm.rs:210-247
+std::vector<size_t> anchor_ids(const std::vector<V3>& p3, size_t n) {
+  size_t n3 = p3.size();
+  std::vector<size_t> chosen;
+  if (n3 <= n) {
+    for (size_t i = 0; i < n3; ++i) chosen.push_back(i);
+    return chosen;
+  }
+  double min_x = std::numeric_limits<double>::max();
+  for (auto& q : p3) min_x = rmin(min_x, q.x);
+  size_t start = 0;
+  for (size_t i = 0; i < n3; ++i)
+    if (p3[i].x == min_x) {
+      start = i;
+      break;
+    }
+  chosen.push_back(start);
+  while (chosen.size() < n) {
+    std::vector<double> d(n3);
+    for (size_t i = 0; i < n3; ++i) {
+      double m = std::numeric_limits<double>::max();
+      for (size_t c : chosen) m = rmin(m, len3(sub(p3[i], p3[c])));
+      d[i] = m;
+    }
+    for (size_t c : chosen) d[c] = -1.0;
+    size_t bi = 0;
+    double bd = std::numeric_limits<double>::lowest();
+    for (size_t i = 0; i < n3; ++i)
+      if (d[i] > bd) {
+        bi = i;
+        bd = d[i];
+      }
+    chosen.push_back(bi);
+  }
+  std::sort(chosen.begin(), chosen.end());
+  return chosen;
+}
+
+// lscm.rs:252-274
+std::map<std::pair<size_t, size_t>, double> edge_weights(const std::vector<V3>& p3,
+                                                         const std::vector<std::array<uint32_t, 3>>& tris) {
+  std::map<std::pair<size_t, size_t>, double> ew;
+  for (auto& t : tris) {
+    size_t i = t[0], j = t[1], k = t[2];
+    size_t cs[3][3] = {{i, j, k}, {j, k, i}, {k, i, j}};
+    for (auto& c : cs) {
+      size_t e0 = c[0], e1 = c[1], o = c[2];
+      V3 a1 = sub(p3[e1], p3[o]);
+      V3 a2 = sub(p3[e0], p3[o]);
+      double la = len3(a1), lb = len3(a2);
+      if (la <= EPS_DEGENERATE || lb <= EPS_DEGENERATE) continue;
+      double s = len3(cross_v(a1, a2)) / (la * lb);
+      if (s <= EPS_DEGENERATE) continue;
+      double cot = rmax((dot(a1, a2) / (la * lb)) / s, 0.0);
+      auto key = std::make_pair(std::min(e0, e1), std::max(e0, e1));
+      auto it = ew.find(key);
+      if (it == ew.end()) it = ew.emplace(key, 0.0).first;
+      it->second += cot;
+    }
+  }
+  return ew;
+}
+
+// lscm.rs:280-413
+std::map<uint32_t, V2> border_targets(const Mesh& mesh, const Chart& chart,
+                                      const std::vector<std::vector<uint32_t>>& loops) {
+  double area3d = chart.area3d;
+  std::vector<std::vector<double>> fracs;
+  std::vector<double> perims;
+  for (auto& l : loops) {
+    std::vector<double> segs;
+    for (size_t w = 0; w + 1 < l.size(); ++w) segs.push_back(len3(sub(mesh.pos[l[w + 1]], mesh.pos[l[w]])));
+    double total = 0.0;
+    for (double s : segs) total += s;
+    total = rmax(total, 1e-30);
+    std::vector<double> fr{0.0};
+    for (double s : segs) fr.push_back(fr.back() + s);
+    for (double& f : fr) f /= total;
+    fracs.push_back(fr);
+    double per = 0.0;
+    for (double s : segs) per += s;
+    perims.push_back(per);
+  }
+  size_t n = loops.size();
+  std::map<uint32_t, V2> pins;
+  if (n == 2) {
+    double pm = 0.0;
+    for (double p : perims) pm = rmax(pm, p);
+    if (std::fabs(perims[0] - perims[1]) <= 0.25 * pm) {
+      double w = 0.5 * (perims[0] + perims[1]);
+      double h = area3d / rmax(w, 1e-30);
+      auto strip = [](const std::vector<uint32_t>& l) {
+        if (l.size() > 1 && l.front() == l.back()) return std::vector<uint32_t>(l.begin(), l.end() - 1);
+        return l;
+      };
+      auto l0u = strip(loops[0]);
+      auto l1u = strip(loops[1]);
+      size_t f0n = std::min(l0u.size(), fracs[0].size());
+      for (size_t k = 0; k < l0u.size(); ++k) pins[l0u[k]] = {-w / 2.0 + w * fracs[0][k], h / 2.0};
+      (void)f0n;
+      for (uint32_t v1 : l1u) {
+        V3 p1 = mesh.pos[v1];
+        size_t best = 0;
+        double best_d = std::numeric_limits<double>::infinity();
+        for (size_t k0 = 0; k0 < l0u.size(); ++k0) {
+          double d = len3(sub(mesh.pos[l0u[k0]], p1));
+          if (d < best_d) {
+            best_d = d;
+            best = k0;
+          }
+        }
+        pins[v1] = {-w / 2.0 + w * fracs[0][best], -h / 2.0};
+      }
+      return pins;
+    }
+  }
+  std::vector<std::pair<double, double>> sides;
+  if (n == 1) {
+    double p = perims[0], a = area3d;
+    if (p * p >= 16.0 * a) {
+      double s_ = p / 2.0;
+      double d = std::sqrt(rmax(s_ * s_ - 4.0 * a, 0.0));
+      sides.push_back({(s_ + d) / 2.0, (s_ - d) / 2.0});
+    } else {
+      double s = std::sqrt(a);
+      sides.push_back({s, s});
+    }
+  } else {
+    V3 c{0, 0, 0};
+    size_t nv = chart.vertex_ids.size();
+    for (uint32_t v : chart.vertex_ids) c = add(c, mesh.pos[v]);
+    c = divs(c, (double)std::max<size_t>(nv, 1));
+    std::vector<double> dists;
+    for (auto& l : loops) {
+      double s = 0.0;
+      for (uint32_t v : l) s += len3(sub(mesh.pos[v], c));
+      dists.push_back(s / (double)std::max<size_t>(l.size(), 1));
+    }
+    std::vector<size_t> order(n);
+    for (size_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return total_key(dists[a]) < total_key(dists[b]); });
+    double denom = 0.0;
+    for (size_t k = 0; k < n; ++k) {
+      double sign = ((n - 1 - k) % 2 == 0) ? 1.0 : -1.0;
+      denom += sign * perims[order[k]] * perims[order[k]];
+    }
+    double s = 4.0 * std::sqrt(area3d / rmax(std::fabs(denom), 1e-30));
+    sides.assign(n, {0.0, 0.0});
+    for (size_t li : order) {
+      double side = s * perims[li] / 4.0;
+      sides[li] = {side, side};
+    }
+  }
+  for (size_t li = 0; li < n; ++li) {
+    auto& l = loops[li];
+    double a = sides[li].first, b = sides[li].second;
+    auto& fr = fracs[li];
+    bool closed = l.size() > 1 && l.front() == l.back();
+    size_t nverts = closed ? l.size() - 1 : l.size();
+    std::vector<V3> lp;
+    for (uint32_t v : l) lp.push_back(mesh.pos[v]);
+    auto p2loop = tangent_frame(lp);
+    double sa3 = 0.0;
+    for (size_t i = 0; i < p2loop.size(); ++i) {
+      size_t j = (i + 1) % p2loop.size();
+      sa3 += p2loop[i].u * p2loop[j].v - p2loop[i].v * p2loop[j].u;
+    }
+    sa3 *= 0.5;
+    for (size_t k = 0; k < nverts; ++k) {
+      double f = sa3 > 0.0 ? std::fmod(1.0 - fr[k], 1.0) : fr[k];
+      pins[l[k]] = rect_point(f, a, b);
+    }
+  }
+  return pins;
+}
+
+// ---------------------------------------------------------------- sparse.rs:19-265
+struct Sparse {
+  size_t n;
+  std::vector<std::map<size_t, double>> rows;
+  explicit Sparse(size_t n_) : n(n_), rows(n_) {}
+  void add(size_t r, size_t c, double v) {  // sparse.rs:47-52
+    if (v != 0.0) rows[r][c] += v;
+  }
+};
+
+struct LU {
+  std::vector<size_t> perm;
+  std::vector<std::pair<size_t, size_t>> swaps;
+  std::map<std::pair<size_t, size_t>, double> lu;
+};
+
+// sparse.rs:91-95, :120-214. Same arithmetic and visit order as the reference; the scans
+// over all rows / all of `lu` are replaced by indexed lookups that visit the same entries
+// in the same (ascending) order.
+LU factorize(const Sparse& S) {
+  size_t n = S.n;
+  LU F;
+  F.perm.resize(n);
+  for (size_t i = 0; i < n; ++i) F.perm[i] = i;
+  std::stable_sort(F.perm.begin(), F.perm.end(), [&](size_t a, size_t b) {
+    return std::make_pair(S.rows[a].size(), a) < std::make_pair(S.rows[b].size(), b);
+  });
+  std::vector<size_t> inv(n);
+  for (size_t i = 0; i < n; ++i) inv[F.perm[i]] = i;
+  std::vector<std::map<size_t, double>> a(n);
+  std::vector<std::set<size_t>> colrows(n);  // rows r that hold a key at column c
+  for (size_t i = 0; i < n; ++i)
+    for (auto& kv : S.rows[F.perm[i]]) {
+      a[i][inv[kv.first]] = kv.second;
+      colrows[inv[kv.first]].insert(i);
+    }
+  for (size_t k = 0; k < n; ++k) {
+    size_t piv = k;
+    double piv_val = 0.0;
+    for (auto it = colrows[k].lower_bound(k); it != colrows[k].end(); ++it) {
+      size_t r = *it;
+      auto f = a[r].find(k);
+      double v = std::fabs(f == a[r].end() ? 0.0 : f->second);
+      if (v > piv_val) {
+        piv_val = v;
+        piv = r;
+      }
+    }
+    if (piv_val < 1e-300) continue;
+    if (piv != k) {
+      F.swaps.push_back({k, piv});
+      for (auto& kv : a[k]) colrows[kv.first].erase(k);
+      for (auto& kv : a[piv]) colrows[kv.first].erase(piv);
+      std::swap(a[k], a[piv]);
+      for (auto& kv : a[k]) colrows[kv.first].insert(k);
+      for (auto& kv : a[piv]) colrows[kv.first].insert(piv);
+      // swap the L history (entries with column < k) of rows k and piv
+      std::vector<std::pair<std::pair<size_t, size_t>, double>> moved;
+      for (size_t r : {k, piv}) {
+        auto lo = F.lu.lower_bound({r, 0});
+        auto hi = F.lu.lower_bound({r, k});
+        for (auto it = lo; it != hi; ++it) moved.push_back(*it);
+        F.lu.erase(lo, hi);
+      }
+      for (auto& mv : moved) {
+        size_t r2 = mv.first.first == k ? piv : k;
+        F.lu[{r2, mv.first.second}] = mv.second;
+      }
+    }
+    double pivot;
+    {
+      auto f = a[k].find(k);
+      pivot = f == a[k].end() ? 0.0 : f->second;
+    }
+    F.lu[{k, k}] = pivot;
+    std::vector<std::pair<size_t, double>> u_part;
+    for (auto it = a[k].upper_bound(k); it != a[k].end(); ++it) u_part.push_back(*it);
+    for (auto& cv : u_part)
+      if (cv.second != 0.0) F.lu[{k, cv.first}] = cv.second;
+    std::vector<size_t> rlist;
+    for (auto it = colrows[k].upper_bound(k); it != colrows[k].end(); ++it) rlist.push_back(*it);
+    for (size_t r : rlist) {
+      auto f = a[r].find(k);
+      if (f == a[r].end() || f->second == 0.0) continue;
+      double a_rk = f->second;
+      double factor = a_rk / pivot;
+      F.lu[{r, k}] = factor;
+      f->second = 0.0;
+      for (auto& cv : u_part) {
+        size_t c = cv.first;
+        double vk = cv.second;
+        auto g = a[r].find(c);
+        double cur = g == a[r].end() ? 0.0 : g->second;
+        double nv = cur - factor * vk;
+        if (nv == 0.0) {
+          if (g != a[r].end()) {
+            a[r].erase(g);
+            colrows[c].erase(r);
+          }
+        } else {
+          if (g != a[r].end())
+            g->second = nv;
+          else {
+            a[r].emplace(c, nv);
+            colrows[c].insert(r);
+          }
+        }
+      }
+    }
+  }
+  return F;
+}
+
+// sparse.rs:219-265. Returns false for a singular / non-finite solve.
+bool lu_solve(const LU& F, size_t n, const std::vector<double>& b, std::vector<double>& xo) {
+  std::vector<double> bp(n);
+  for (size_t i = 0; i < n; ++i) bp[i] = b[F.perm[i]];
+  for (auto& sw : F.swaps) std::swap(bp[sw.first], bp[sw.second]);
+  std::vector<double> y(n, 0.0);
+  for (size_t i = 0; i < n; ++i) {
+    double s = bp[i];
+    auto lo = F.lu.lower_bound({i, 0});
+    auto hi = F.lu.lower_bound({i, i});
+    for (auto it = lo; it != hi; ++it) s -= it->second * y[it->first.second];
+    y[i] = s;
+  }
+  std::vector<double> x(n, 0.0);
+  for (size_t ii = n; ii-- > 0;) {
+    auto d = F.lu.find({ii, ii});
+    double diag = d == F.lu.end() ? 0.0 : d->second;
+    if (std::fabs(diag) < 1e-300) return false;
+    double s = y[ii];
+    auto lo = F.lu.upper_bound({ii, ii});
+    auto hi = F.lu.lower_bound({ii + 1, 0});
+    for (auto it = lo; it != hi; ++it) s -= it->second * x[it->first.second];
+    x[ii] = s / diag;
+  }
+  for (double v : x)
+    if (!std::isfinite(v)) return false;
+  xo.assign(n, 0.0);
+  for (size_t i = 0; i < n; ++i) xo[F.perm[i]] = x[i];
+  return true;
+}
+
+// ---------------------------------------------------------------- bag of named arrays
+struct Bag {
+  std::map<std::string, std::vector<double>> f;
+  std::map<std::string, std::vector<int64_t>> i;
+  std::string err;
+};
+
+std::string key(int c, const char* name) { return "c" + std::to_string(c) + "." + name; }
+
+// The per-chart system of the default unfold path (lscm.rs:512-676), as the interleaved
+// CSR the GPU boundary receives (Sparse::to_csr(2 nf), sparse.rs:69-84) and the full
+// Sparse for the CPU LU.
+struct ChartSystem {
+  std::vector<V2> p2;
+  std::vector<size_t> pin_ids;
+  std::vector<V2> pin_uv;
+  std::vector<long> free_pos;
+  std::vector<size_t> free_ids;
+  size_t nfree = 0;
+  Sparse M{0};
+  std::vector<double> rhs;
+};
+
+ChartSystem build_system(const Mesh& mesh, const Chart& ch, double angle_mix, double mix_w) {
+  ChartSystem S;
+  std::vector<V3> p3;
+  for (uint32_t v : ch.vertex_ids) p3.push_back(mesh.pos[v]);
+  size_t nv = p3.size();
+  S.p2 = tangent_frame(p3);
+  std::map<uint32_t, V2> pin_source;
+  if (ch.border_loops.empty()) {
+    auto anchors = anchor_ids(p3, 4);
+    for (size_t i : anchors) pin_source[ch.vertex_ids[i]] = S.p2[i];
+  } else {
+    pin_source = border_targets(mesh, ch, ch.border_loops);
+  }
+  for (auto& kv : pin_source) {
+    long li = ch.local_of(kv.first);
+    if (li >= 0 && std::find(S.pin_ids.begin(), S.pin_ids.end(), (size_t)li) == S.pin_ids.end()) {
+      S.pin_ids.push_back((size_t)li);
+      S.pin_uv.push_back(kv.second);
+    }
+  }
+  auto ew = edge_weights(p3, ch.tris);
+  std::vector<char> is_free(nv, 1);
+  for (size_t pi : S.pin_ids) is_free[pi] = 0;
+  std::map<size_t, V2> pin_lookup;
+  for (size_t k = 0; k < S.pin_ids.size(); ++k) pin_lookup[S.pin_ids[k]] = S.pin_uv[k];
+  S.free_pos.assign(nv, -1);
+  for (size_t i = 0; i < nv; ++i)
+    if (is_free[i]) {
+      S.free_pos[i] = (long)S.free_ids.size();
+      S.free_ids.push_back(i);
+    }
+  S.nfree = S.free_ids.size();
+  size_t nvar = 2 * S.nfree + 1, aux = 2 * S.nfree;
+  double mix_b = 1.0 - angle_mix;
+  S.rhs.assign(nvar, 0.0);
+  S.M = Sparse(nvar);
+  const size_t NONE = (size_t)-1;
+  for (auto& kv : ew) {
+    size_t i = kv.first.first, j = kv.first.second;
+    double w = kv.second;
+    if (w <= EPS_DEGENERATE) continue;
+    V3 d3 = sub(p3[j], p3[i]);
+    double c = w / rmax(dot(d3, d3), EPS_DEGENERATE);
+    V2 d = sub2(S.p2[j], S.p2[i]);
+    struct Dir {
+      size_t aa, bb;
+      V2 dv;
+    } dirs[2] = {{i, j, d}, {j, i, {-d.u, -d.v}}};
+    for (auto& dr : dirs) {
+      if (!is_free[dr.aa]) continue;
+      size_t ra = 2 * (size_t)S.free_pos[dr.aa];
+      size_t bbx = NONE, bby = NONE;
+      if (is_free[dr.bb]) {
+        bbx = 2 * (size_t)S.free_pos[dr.bb];
+        bby = bbx + 1;
+      }
+      S.M.add(ra, ra, c);
+      S.M.add(ra + 1, ra + 1, c);
+      if (bbx != NONE) S.M.add(ra, bbx, -c);
+      if (bby != NONE) S.M.add(ra + 1, bby, -c);
+      if (is_free[dr.bb]) {
+        S.rhs[ra] += mix_b * c * dr.dv.u;
+        S.rhs[ra + 1] += mix_b * c * dr.dv.v;
+      } else {
+        V2 pin = pin_lookup[dr.bb];
+        S.rhs[ra] += mix_b * c * dr.dv.u + c * pin.u;
+        S.rhs[ra + 1] += mix_b * c * dr.dv.v + c * pin.v;
+      }
+    }
+  }
+  S.M.add(aux, aux, mix_w);
+  S.rhs[aux] = mix_w;
+  return S;
+}
+
+// Damped driver loop (lscm.rs:570-719). The default path's system does not change between
+// iterations (assembly depends only on positions, the tangent frame and the pins), so a
+// deterministic solver returns the same solution every iteration: the loop is a function
+// of (p2, pinned targets, solution).
+void driver_loop(const ChartSystem& S, const std::vector<double>& sol, int max_iter, std::vector<V2>& uv,
+                 int64_t* iters_out, double* err_accum_out) {
+  size_t nv = S.p2.size();
+  uv = S.p2;
+  std::vector<V2> new_uv(nv);
+  double err_accum = 1.0, step = 1.0, prev_err = std::numeric_limits<double>::infinity();
+  int64_t iters_done = 0;
+  if (max_iter <= 0) max_iter = 100;
+  for (int it = 0; it < max_iter; ++it) {
+    iters_done = it + 1;
+    new_uv = uv;
+    for (size_t i : S.free_ids) {
+      size_t pos = (size_t)S.free_pos[i];
+      new_uv[i] = {sol[2 * pos], sol[2 * pos + 1]};
+    }
+    for (size_t k = 0; k < S.pin_ids.size(); ++k) new_uv[S.pin_ids[k]] = S.pin_uv[k];
+    std::vector<V2> dv(nv);
+    for (size_t i = 0; i < nv; ++i) dv[i] = sub2(new_uv[i], uv[i]);
+    double ndv = 0.0, nuv = 0.0;
+    for (auto& d : dv) ndv += d.u * d.u + d.v * d.v;
+    for (auto& u : uv) nuv += u.u * u.u + u.v * u.v;
+    double err = std::sqrt(ndv) / rmax(std::sqrt(nuv), 1e-30);
+    double applied = err * step;
+    if (prev_err > 1e-30 && err > 2.0 * prev_err)
+      step = rmax(step * 0.5, 0.05);
+    else if (it > 3)
+      step = rmin(step * 1.2, 1.0);
+    if (applied < 1e-8 || (prev_err > 1e-30 && it != 0 && applied / prev_err <= 0.01)) break;
+    for (size_t i = 0; i < nv; ++i) uv[i] = {uv[i].u + dv[i].u * step, uv[i].v + dv[i].v * step};
+    prev_err = applied;
+    err_accum += err;
+    if (max_iter * 10 < it) break;
+  }
+  *iters_out = iters_done;
+  *err_accum_out = err_accum;
+}
+
+// metrics.rs:59-70
+void svd2(const double m[2][2], double* s1, double* s2) {
+  double a = m[0][0] * m[0][0] + m[1][0] * m[1][0];
+  double b = m[0][0] * m[0][1] + m[1][0] * m[1][1];
+  double c = m[0][1] * m[0][1] + m[1][1] * m[1][1];
+  double tr = a + c;
+  double d = 0.5 * (a - c);
+  double disc = std::sqrt(rmax(d * d + b * b, 0.0));
+  double l1 = 0.5 * tr + disc;
+  double l2 = rmax(0.5 * tr - disc, 0.0);
+  *s1 = std::sqrt(rmax(l1, 0.0));
+  *s2 = std::sqrt(l2);
+}
+
+// metrics.rs:73-141 (conformal / area ratio per triangle; folds per metrics.rs:41-56)
+void chart_distortion(const Mesh& mesh, const Chart& ch, const std::vector<V2>& uv, double out[5]) {
+  std::vector<double> conf, ar;
+  int64_t flips = 0;
+  for (size_t t = 0; t < ch.tris.size(); ++t) {
+    auto& f = mesh.faces[ch.face_ids[t]];
+    V3 a3 = mesh.pos[f[0]], b3 = mesh.pos[f[1]], c3 = mesh.pos[f[2]];
+    V2 u0 = uv[ch.tris[t][0]], u1 = uv[ch.tris[t][1]], u2 = uv[ch.tris[t][2]];
+    V3 e1 = sub(b3, a3), e2 = sub(c3, a3);
+    V3 nrm = cross_v(e1, e2);
+    double ln = len3(nrm);
+    if (ln < 1e-30) continue;
+    V3 n = divs(nrm, ln);
+    V3 t1 = divs(e1, rmax(len3(e1), 1e-30));
+    V3 t2 = cross_v(n, t1);
+    double e1t1 = dot(e1, t1), e2t1 = dot(e2, t1), e1t2 = dot(e1, t2), e2t2 = dot(e2, t2);
+    double det = e1t1 * e2t2 - e2t1 * e1t2;
+    if (std::fabs(det) < 1e-30) {
+      flips++;
+      continue;
+    }
+    double i00 = e2t2 / det, i01 = -e2t1 / det, i10 = -e1t2 / det, i11 = e1t1 / det;
+    V2 du1 = sub2(u1, u0), du2 = sub2(u2, u0);
+    double F[2][2] = {{du1.u * i00 + du2.u * i10, du1.u * i01 + du2.u * i11},
+                      {du1.v * i00 + du2.v * i10, du1.v * i01 + du2.v * i11}};
+    double s1, s2;
+    svd2(F, &s1, &s2);
+    conf.push_back(s1 / rmax(s2, 1e-30));
+    double uva = 0.5 * std::fabs(du1.u * du2.v - du2.u * du1.v);
+    ar.push_back(uva / (0.5 * ln));
+  }
+  double cs = 0.0, cm = 0.0, as = 0.0;
+  for (double x : conf) cs += x;
+  for (double x : conf) cm = rmax(cm, x);
+  for (double x : ar) as += x;
+  // winding_flips (metrics.rs:41-56)
+  int64_t folds = 0;
+  if (!ch.tris.empty()) {
+    auto sgn = [&](size_t t) {
+      V2 a = uv[ch.tris[t][0]], b = uv[ch.tris[t][1]], c = uv[ch.tris[t][2]];
+      return (b.u - a.u) * (c.v - a.v) - (c.u - a.u) * (b.v - a.v);
+    };
+    double sum = 0.0;
+    for (size_t t = 0; t < ch.tris.size(); ++t) sum += sgn(t);
+    double dom = sum < 0.0 ? -1.0 : 1.0;
+    for (size_t t = 0; t < ch.tris.size(); ++t)
+      if (sgn(t) * dom <= 0.0) folds++;
+  }
+  out[0] = cs / (double)std::max<size_t>(conf.size(), 1);
+  out[1] = cm;
+  out[2] = as / (double)std::max<size_t>(ar.size(), 1);
+  out[3] = (double)flips;
+  out[4] = (double)folds;
+}
+
+}  // namespace
+
+// ================================================================= extern "C" interface
+extern "C" {
+
+void* orc_bag_new() { return new Bag(); }
+void orc_bag_free(void* h) { delete static_cast<Bag*>(h); }
+
+int64_t orc_len(void* h, const char* name) {
+  Bag* b = static_cast<Bag*>(h);
+  auto f = b->f.find(name);
+  if (f != b->f.end()) return (int64_t)f->second.size();
+  auto i = b->i.find(name);
+  if (i != b->i.end()) return (int64_t)i->second.size();
+  return -1;
+}
+int orc_get_f64(void* h, const char* name, double* out) {
+  Bag* b = static_cast<Bag*>(h);
+  auto f = b->f.find(name);
+  if (f == b->f.end()) return -1;
+  std::memcpy(out, f->second.data(), f->second.size() * 8);
+  return 0;
+}
+int orc_get_i64(void* h, const char* name, int64_t* out) {
+  Bag* b = static_cast<Bag*>(h);
+  auto i = b->i.find(name);
+  if (i == b->i.end()) return -1;
+  std::memcpy(out, i->second.data(), i->second.size() * 8);
+  return 0;
+}
+void orc_put_f64(void* h, const char* name, const double* v, int64_t n) {
+  static_cast<Bag*>(h)->f[name].assign(v, v + n);
+}
+void orc_put_i64(void* h, const char* name, const int64_t* v, int64_t n) {
+  static_cast<Bag*>(h)->i[name].assign(v, v + n);
+}
+
+// meshgen.rs fixtures -> bag {"pos" (3*nv), "faces" (3*nf)}
+void orc_meshgen(void* h, const char* name, int64_t n, double r_major, double r_minor, int64_t nu, int64_t nv_) {
+  Bag* b = static_cast<Bag*>(h);
+  std::vector<V3> p;
+  std::vector<std::array<uint32_t, 3>> f;
+  std::string nm(name);
+  if (nm == "cube") {  // meshgen.rs:12-54
+    int fd[6][4] = {{2, 0, 0, 1}, {2, 1, 0, 1}, {0, 0, 1, 2}, {0, 1, 1, 2}, {1, 0, 0, 2}, {1, 1, 0, 2}};
+    for (auto& d : fd) {
+      uint32_t base = (uint32_t)p.size();
+      for (int64_t i = 0; i <= n; ++i)
+        for (int64_t j = 0; j <= n; ++j) {
+          double pt[3];
+          for (int k = 0; k < 3; ++k) {
+            if (k == d[0])
+              pt[k] = (double)d[1];
+            else if (k == d[2])
+              pt[k] = (double)i / (double)n;
+            else if (k == d[3])
+              pt[k] = (double)j / (double)n;
+            else
+              pt[k] = 0.0;
+          }
+          p.push_back({pt[0], pt[1], pt[2]});
+        }
+      for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = 0; j < n; ++j) {
+          uint32_t a = base + (uint32_t)i * ((uint32_t)n + 1) + (uint32_t)j;
+          uint32_t bb = a + 1, c = a + ((uint32_t)n + 1), dd = c + 1;
+          f.push_back({a, bb, dd});
+          f.push_back({a, dd, c});
+        }
+    }
+  } else if (nm == "sphere") {  // meshgen.rs:60-87 (nu x nv_)
+    double du = 2.0 * PI / (double)(nu - 1);
+    double dv = PI / (double)(nv_ - 1);
+    for (int64_t j = 0; j < nv_; ++j) {
+      double v = dv * (double)j;
+      for (int64_t i = 0; i < nu; ++i) {
+        double u = du * (double)i;
+        p.push_back({std::sin(v) * std::cos(u), std::sin(v) * std::sin(u), std::cos(v)});
+      }
+    }
+    for (int64_t i = 0; i < nu; ++i)
+      for (int64_t j = 0; j < nv_ - 1; ++j) {
+        uint32_t a = (uint32_t)(j * nu + i), bb = (uint32_t)(j * nu + (i + 1) % nu);
+        uint32_t c = a + (uint32_t)nu, d = bb + (uint32_t)nu;
+        f.push_back({a, c, d});
+        f.push_back({a, d, bb});
+      }
+  } else if (nm == "torus" || nm == "annulus") {  // meshgen.rs:92-131
+    for (int64_t j = 0; j < nv_; ++j) {
+      double v = 2.0 * PI * (double)j / (double)nv_;
+      for (int64_t i = 0; i < nu; ++i) {
+        double u = 2.0 * PI * (double)i / (double)nu;
+        double cr = r_major + r_minor * std::cos(v);
+        p.push_back({cr * std::cos(u), cr * std::sin(u), r_minor * std::sin(v)});
+      }
+    }
+    int64_t jc = nv_ / 2, k = 0;
+    for (int64_t i = 0; i < nu; ++i)
+      for (int64_t j = 0; j < nv_; ++j) {
+        uint32_t a = (uint32_t)(j * nu + i), bb = (uint32_t)(j * nu + (i + 1) % nu);
+        int64_t jn = (j + 1) % nv_;
+        uint32_t c = (uint32_t)(jn * nu + i), d = (uint32_t)(jn * nu + (i + 1) % nu);
+        bool keep = nm == "torus" || ((k / 2) % nv_ != jc);
+        if (keep) f.push_back({a, bb, d});
+        ++k;
+        keep = nm == "torus" || ((k / 2) % nv_ != jc);
+        if (keep) f.push_back({a, d, c});
+        ++k;
+      }
+  } else if (nm == "grid") {  // meshgen.rs:135-155 (nu x nv_ quads)
+    int64_t w = nu, hh = nv_;
+    for (int64_t j = 0; j <= hh; ++j)
+      for (int64_t i = 0; i <= w; ++i) p.push_back({(double)i, (double)j, 0.0});
+    uint32_t stride = (uint32_t)(w + 1);
+    for (int64_t j = 0; j < hh; ++j)
+      for (int64_t i = 0; i < w; ++i) {
+        uint32_t a = (uint32_t)j * stride + (uint32_t)i, bb = a + 1, c = a + stride, d = c + 1;
+        f.push_back({a, bb, d});
+        f.push_back({a, d, c});
+      }
+  } else if (nm == "cylinder") {  // meshgen.rs:160-182 (r = r_major, height = r_minor)
+    double r = r_major, height = r_minor;
+    for (int64_t j = 0; j <= nv_; ++j) {
+      double z = height * (double)j / (double)std::max<int64_t>(nv_, 1);
+      for (int64_t i = 0; i <= nu; ++i) {
+        double t = 2.0 * PI * (double)i / (double)std::max<int64_t>(nu, 1);
+        p.push_back({r * std::cos(t), r * std::sin(t), z});
+      }
+    }
+    uint32_t stride = (uint32_t)(nu + 1);
+    for (int64_t j = 0; j < nv_; ++j)
+      for (int64_t i = 0; i < nu; ++i) {
+        uint32_t a = (uint32_t)j * stride + (uint32_t)i, bb = a + 1, c = a + stride, d = c + 1;
+        f.push_back({a, bb, d});
+        f.push_back({a, d, c});
+      }
+  }
+  auto& P = b->f["pos"];
+  P.clear();
+  for (auto& q : p) {
+    P.push_back(q.x);
+    P.push_back(q.y);
+    P.push_back(q.z);
+  }
+  auto& F = b->i["faces"];
+  F.clear();
+  for (auto& t : f)
+    for (uint32_t v : t) F.push_back(v);
+}
+
+// eig3 (lscm_eig.rs:13-66): m row-major 9 -> w[3], v[9] (v[i*3+k] = component i of vector k)
+void orc_eig3(const double* m, double* w, double* v) {
+  double mm[3][3], vv[3][3];
+  for (int i = 0; i < 9; ++i) mm[i / 3][i % 3] = m[i];
+  eig3(mm, w, vv);
+  for (int i = 0; i < 9; ++i) v[i] = vv[i / 3][i % 3];
+}
+
+// Sparse::solve on COO triples (sparse.rs:47-52 add semantics, :219-265 solve).
+int orc_sparse_solve(int64_t n, int64_t nnz, const int64_t* r, const int64_t* c, const double* v,
+                     const double* b, double* x) {
+  Sparse S((size_t)n);
+  for (int64_t k = 0; k < nnz; ++k) S.add((size_t)r[k], (size_t)c[k], v[k]);
+  LU F = factorize(S);
+  std::vector<double> bb(b, b + n), xo;
+  if (!lu_solve(F, (size_t)n, bb, xo)) return -1;
+  std::memcpy(x, xo.data(), (size_t)n * 8);
+  return 0;
+}
+
+// The unfold pipeline's chart stages for a raw triangle soup.
+// in: bag with "pos" (3*nv), "faces" (3*nf).
+// out (same bag): "mesh.pos", "mesh.faces", "n_charts", "n_cut", per chart c:
+//   c.face_ids, c.vertex_ids, c.tris, c.border, c.loop_off, c.loop_ids, c.area3d,
+//   c.p2 (2*nv), c.pin_ids (local), c.pin_uv (2*npins), c.free_pos (nv, -1 = pinned),
+//   c.csr_ptr, c.csr_cols, c.csr_vals (interleaved, Sparse::to_csr(2 nf)), c.rhs (2nf+1)
+//   and, when solve_limit >= 2nf+1: c.sol (LU solution), c.uv, c.iters, c.err_accum,
+//   c.metrics (conformal mean/max, area ratio mean, flips, folds).
+int orc_pipeline(void* h, double weld_tol, double angle_deg, double angle_mix, double mix_w,
+                 int64_t solve_limit, int64_t max_iter) {
+  Bag* b = static_cast<Bag*>(h);
+  Mesh raw;
+  auto& P = b->f["pos"];
+  auto& F = b->i["faces"];
+  for (size_t k = 0; k + 2 < P.size(); k += 3) raw.pos.push_back({P[k], P[k + 1], P[k + 2]});
+  for (size_t k = 0; k + 2 < F.size(); k += 3)
+    raw.faces.push_back({(uint32_t)F[k], (uint32_t)F[k + 1], (uint32_t)F[k + 2]});
+  Mesh mesh = weld(raw, weld_tol);
+  {
+    auto& mp = b->f["mesh.pos"];
+    mp.clear();
+    for (auto& q : mesh.pos) {
+      mp.push_back(q.x);
+      mp.push_back(q.y);
+      mp.push_back(q.z);
+    }
+    auto& mf = b->i["mesh.faces"];
+    mf.clear();
+    for (auto& t : mesh.faces)
+      for (uint32_t v : t) mf.push_back(v);
+  }
+  size_t n_cut = 0;
+  auto charts = segment(mesh, angle_deg, &n_cut);
+  b->i["n_charts"] = {(int64_t)charts.size()};
+  b->i["n_cut"] = {(int64_t)n_cut};
+  for (size_t ci = 0; ci < charts.size(); ++ci) {
+    auto& ch = charts[ci];
+    int c = (int)ci;
+    auto& fi = b->i[key(c, "face_ids")];
+    fi.assign(ch.face_ids.begin(), ch.face_ids.end());
+    auto& vi = b->i[key(c, "vertex_ids")];
+    vi.assign(ch.vertex_ids.begin(), ch.vertex_ids.end());
+    auto& tr = b->i[key(c, "tris")];
+    tr.clear();
+    for (auto& t : ch.tris)
+      for (uint32_t v : t) tr.push_back(v);
+    auto& bd = b->i[key(c, "border")];
+    bd.assign(ch.border.begin(), ch.border.end());
+    auto& lo = b->i[key(c, "loop_off")];
+    auto& li = b->i[key(c, "loop_ids")];
+    lo = {0};
+    li.clear();
+    for (auto& l : ch.border_loops) {
+      for (uint32_t v : l) li.push_back(v);
+      lo.push_back((int64_t)li.size());
+    }
+    b->f[key(c, "area3d")] = {ch.area3d};
+    ChartSystem S = build_system(mesh, ch, angle_mix, mix_w);
+    auto& p2 = b->f[key(c, "p2")];
+    p2.clear();
+    for (auto& q : S.p2) {
+      p2.push_back(q.u);
+      p2.push_back(q.v);
+    }
+    auto& pid = b->i[key(c, "pin_ids")];
+    pid.assign(S.pin_ids.begin(), S.pin_ids.end());
+    auto& puv = b->f[key(c, "pin_uv")];
+    puv.clear();
+    for (auto& q : S.pin_uv) {
+      puv.push_back(q.u);
+      puv.push_back(q.v);
+    }
+    auto& fp = b->i[key(c, "free_pos")];
+    fp.assign(S.free_pos.begin(), S.free_pos.end());
+    // Sparse::to_csr(2 nf)  (sparse.rs:69-84)
+    size_t limit = 2 * S.nfree;
+    auto& cp = b->i[key(c, "csr_ptr")];
+    auto& cc = b->i[key(c, "csr_cols")];
+    auto& cv = b->f[key(c, "csr_vals")];
+    cp = {0};
+    cc.clear();
+    cv.clear();
+    for (size_t r = 0; r < limit; ++r) {
+      for (auto& kv : S.M.rows[r])
+        if (kv.first < limit) {
+          cc.push_back((int64_t)kv.first);
+          cv.push_back(kv.second);
+        }
+      cp.push_back((int64_t)cv.size());
+    }
+    b->f[key(c, "rhs")] = S.rhs;
+    if ((int64_t)(2 * S.nfree + 1) <= solve_limit) {
+      LU Fc = factorize(S.M);
+      std::vector<double> sol;
+      bool ok = lu_solve(Fc, S.M.n, S.rhs, sol);
+      if (ok) {
+        b->f[key(c, "sol")] = sol;
+        std::vector<V2> uv;
+        int64_t iters;
+        double ea;
+        driver_loop(S, sol, (int)max_iter, uv, &iters, &ea);
+        auto& u = b->f[key(c, "uv")];
+        u.clear();
+        for (auto& q : uv) {
+          u.push_back(q.u);
+          u.push_back(q.v);
+        }
+        b->i[key(c, "iters")] = {iters};
+        b->f[key(c, "err_accum")] = {ea};
+        double met[5];
+        chart_distortion(mesh, ch, uv, met);
+        b->f[key(c, "metrics")] = std::vector<double>(met, met + 5);
+      } else {
+        b->i[key(c, "iters")] = {0};
+      }
+    }
+  }
+  return 0;
+}
+
+// Driver loop with an externally supplied solution (e.g. a SuperLU solve of the exported
+// CSR): in-bag c.sol must hold 2nf+1 values.  Writes c.uv, c.iters, c.err_accum, c.metrics.
+int orc_driver_from_solution(void* h, int64_t chart, int64_t max_iter) {
+  Bag* b = static_cast<Bag*>(h);
+  int c = (int)chart;
+  auto& p2 = b->f[key(c, "p2")];
+  auto& pid = b->i[key(c, "pin_ids")];
+  auto& puv = b->f[key(c, "pin_uv")];
+  auto& fp = b->i[key(c, "free_pos")];
+  auto& sol = b->f[key(c, "sol")];
+  ChartSystem S;
+  size_t nv = p2.size() / 2;
+  for (size_t i = 0; i < nv; ++i) S.p2.push_back({p2[2 * i], p2[2 * i + 1]});
+  for (size_t k = 0; k < pid.size(); ++k) {
+    S.pin_ids.push_back((size_t)pid[k]);
+    S.pin_uv.push_back({puv[2 * k], puv[2 * k + 1]});
+  }
+  S.free_pos.assign(fp.begin(), fp.end());
+  for (size_t i = 0; i < nv; ++i)
+    if (fp[i] >= 0) S.free_ids.push_back(i);
+  S.nfree = S.free_ids.size();
+  if (sol.size() < 2 * S.nfree) return -1;
+  std::vector<V2> uv;
+  int64_t iters;
+  double ea;
+  driver_loop(S, sol, (int)max_iter, uv, &iters, &ea);
+  auto& u = b->f[key(c, "uv")];
+  u.clear();
+  for (auto& q : uv) {
+    u.push_back(q.u);
+    u.push_back(q.v);
+  }
+  b->i[key(c, "iters")] = {iters};
+  b->f[key(c, "err_accum")] = {ea};
+  return 0;
+}
+
+// chart_distortion on given UVs for chart c of the last orc_pipeline (needs mesh.* and c.*).
+int orc_chart_metrics(void* h, int64_t chart, const double* uv, double* out5) {
+  Bag* b = static_cast<Bag*>(h);
+  int c = (int)chart;
+  Mesh mesh;
+  auto& mp = b->f["mesh.pos"];
+  auto& mf = b->i["mesh.faces"];
+  for (size_t k = 0; k + 2 < mp.size(); k += 3) mesh.pos.push_back({mp[k], mp[k + 1], mp[k + 2]});
+  for (size_t k = 0; k + 2 < mf.size(); k += 3)
+    mesh.faces.push_back({(uint32_t)mf[k], (uint32_t)mf[k + 1], (uint32_t)mf[k + 2]});
+  Chart ch;
+  auto& fi = b->i[key(c, "face_ids")];
+  auto& tr = b->i[key(c, "tris")];
+  ch.face_ids.assign(fi.begin(), fi.end());
+  for (size_t k = 0; k + 2 < tr.size(); k += 3)
+    ch.tris.push_back({(uint32_t)tr[k], (uint32_t)tr[k + 1], (uint32_t)tr[k + 2]});
+  size_t nv = b->i[key(c, "vertex_ids")].size();
+  std::vector<V2> u(nv);
+  for (size_t i = 0; i < nv; ++i) u[i] = {uv[2 * i], uv[2 * i + 1]};
+  chart_distortion(mesh, ch, u, out5);
+  return 0;
+}
+
+}  // extern "C"

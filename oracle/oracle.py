@@ -1,0 +1,259 @@
+"""ORACLE — test infrastructure only (the checker, never the thing measured or shipped).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline / reference
+legs may import this module.  It wraps ``oracle.cpp`` — a CPU restatement of ResearchUV's
+per-chart LSCM unfold path (unwrap/src/{weld,segment,lscm,lscm_eig,sparse,metrics,meshgen}.rs)
+— and adds the FP64 sparse-LU oracle for systems too large for the reference's Θ(n²)
+BTreeMap LU (``scipy.sparse.linalg.splu``, SuperLU, on the scalar Laplacian with the u and v
+right-hand sides).
+
+Parity pinning: the reference is pure Rust and cannot be built here; the restatement is
+pinned against the known answers of the reference's own tests
+(``tests/golden/reference_known_answers.json``, each item citing its file:line).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "oracle.cpp")
+_LIB = os.path.join(_HERE, "_build", "liboracle.so")
+_CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement into oracle/_build/liboracle.so (plain g++, no build system)."""
+    os.makedirs(os.path.dirname(_LIB), exist_ok=True)
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
+        tmp = _LIB + ".tmp"
+        subprocess.check_call(["g++", *_CXXFLAGS, "-o", tmp, _SRC])
+        os.replace(tmp, _LIB)
+    return _LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(build())
+        vp, i64, f64, cp = ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_char_p
+        P = ctypes.POINTER
+        L.orc_bag_new.restype = vp
+        L.orc_bag_free.argtypes = [vp]
+        L.orc_len.argtypes = [vp, cp]
+        L.orc_len.restype = i64
+        L.orc_get_f64.argtypes = [vp, cp, P(f64)]
+        L.orc_get_i64.argtypes = [vp, cp, P(i64)]
+        L.orc_put_f64.argtypes = [vp, cp, P(f64), i64]
+        L.orc_put_i64.argtypes = [vp, cp, P(i64), i64]
+        L.orc_meshgen.argtypes = [vp, cp, i64, f64, f64, i64, i64]
+        L.orc_eig3.argtypes = [P(f64), P(f64), P(f64)]
+        L.orc_sparse_solve.argtypes = [i64, i64, P(i64), P(i64), P(f64), P(f64), P(f64)]
+        L.orc_sparse_solve.restype = ctypes.c_int
+        L.orc_pipeline.argtypes = [vp, f64, f64, f64, f64, i64, i64]
+        L.orc_driver_from_solution.argtypes = [vp, i64, i64]
+        L.orc_chart_metrics.argtypes = [vp, i64, P(f64), P(f64)]
+        _lib = L
+    return _lib
+
+
+def _f64p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _i64p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+class Bag:
+    """Owner of one oracle result set (named f64 / i64 arrays)."""
+
+    def __init__(self):
+        self.h = lib().orc_bag_new()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_bag_free(self.h)
+            self.h = None
+
+    def has(self, name: str) -> bool:
+        return lib().orc_len(self.h, name.encode()) >= 0
+
+    def f64(self, name: str) -> np.ndarray:
+        n = lib().orc_len(self.h, name.encode())
+        if n < 0:
+            raise KeyError(name)
+        out = np.empty(n, np.float64)
+        if lib().orc_get_f64(self.h, name.encode(), _f64p(out)) != 0:
+            raise KeyError(name)
+        return out
+
+    def i64(self, name: str) -> np.ndarray:
+        n = lib().orc_len(self.h, name.encode())
+        if n < 0:
+            raise KeyError(name)
+        out = np.empty(n, np.int64)
+        if lib().orc_get_i64(self.h, name.encode(), _i64p(out)) != 0:
+            raise KeyError(name)
+        return out
+
+    def put_f64(self, name, a):
+        a = np.ascontiguousarray(a, np.float64).ravel()
+        lib().orc_put_f64(self.h, name.encode(), _f64p(a), a.size)
+
+    def put_i64(self, name, a):
+        a = np.ascontiguousarray(a, np.int64).ravel()
+        lib().orc_put_i64(self.h, name.encode(), _i64p(a), a.size)
+
+
+# ------------------------------------------------------------------ meshgen.rs fixtures
+def meshgen(name: str, n: int = 0, *, r_major=0.0, r_minor=0.0, nu=0, nv=0):
+    """Restated fixtures (unwrap/src/meshgen.rs:12-198). Returns (pos (V,3) f64, faces (F,3) i64)."""
+    b = Bag()
+    lib().orc_meshgen(b.h, name.encode(), n, r_major, r_minor, nu, nv)
+    return b.f64("pos").reshape(-1, 3), b.i64("faces").reshape(-1, 3)
+
+
+def cube(n):
+    return meshgen("cube", n)
+
+
+def uv_sphere(nu, nv):
+    return meshgen("sphere", nu=nu, nv=nv)
+
+
+def torus(r_major, r_minor, nu, nvt):
+    return meshgen("torus", r_major=r_major, r_minor=r_minor, nu=nu, nv=nvt)
+
+
+def torus_annulus(r_major, r_minor, nu, nvt):
+    return meshgen("annulus", r_major=r_major, r_minor=r_minor, nu=nu, nv=nvt)
+
+
+def grid(w, h):
+    return meshgen("grid", nu=w, nv=h)
+
+
+def cylinder(r, height, nu, nv):
+    return meshgen("cylinder", r_major=r, r_minor=height, nu=nu, nv=nv)
+
+
+def eig3(m):
+    m = np.ascontiguousarray(m, np.float64).reshape(9)
+    w = np.empty(3)
+    v = np.empty(9)
+    lib().orc_eig3(_f64p(m), _f64p(w), _f64p(v))
+    return w, v.reshape(3, 3)
+
+
+def sparse_solve(n, rows, cols, vals, b):
+    """Sparse::add over the COO triples then Sparse::solve (unwrap/src/sparse.rs). None if singular."""
+    r = np.ascontiguousarray(rows, np.int64)
+    c = np.ascontiguousarray(cols, np.int64)
+    v = np.ascontiguousarray(vals, np.float64)
+    bb = np.ascontiguousarray(b, np.float64)
+    x = np.empty(n)
+    rc = lib().orc_sparse_solve(n, r.size, _i64p(r), _i64p(c), _f64p(v), _f64p(bb), _f64p(x))
+    return None if rc != 0 else x
+
+
+# ------------------------------------------------------------------ the unfold path
+class Pipeline:
+    """weld -> segment -> per-chart system (and, for small charts, the reference LU solve +
+    damped driver) for one raw triangle soup.
+
+    ``lu_limit``: charts whose system has at most this many unknowns (2 nf + 1) are solved by
+    the restated reference LU; larger ones can be solved with :meth:`superlu_uv`.
+    """
+
+    def __init__(self, pos, faces, weld_tol=1e-12, angle_deg=30.0, angle_mix=1.0, mix_w=1.0,
+                 lu_limit=4000, max_iter=100):
+        self.bag = Bag()
+        self.bag.put_f64("pos", np.asarray(pos, np.float64))
+        self.bag.put_i64("faces", np.asarray(faces, np.int64))
+        self.max_iter = max_iter
+        lib().orc_pipeline(self.bag.h, weld_tol, angle_deg, angle_mix, mix_w, lu_limit, max_iter)
+        self.n_charts = int(self.bag.i64("n_charts")[0])
+        self.n_cut = int(self.bag.i64("n_cut")[0])
+
+    def mesh(self):
+        return self.bag.f64("mesh.pos").reshape(-1, 3), self.bag.i64("mesh.faces").reshape(-1, 3)
+
+    def chart(self, c: int) -> dict:
+        b = self.bag
+        k = f"c{c}."
+        d = {
+            "face_ids": b.i64(k + "face_ids"),
+            "vertex_ids": b.i64(k + "vertex_ids"),
+            "tris": b.i64(k + "tris").reshape(-1, 3),
+            "border": b.i64(k + "border"),
+            "area3d": float(b.f64(k + "area3d")[0]),
+            "p2": b.f64(k + "p2").reshape(-1, 2),
+            "pin_ids": b.i64(k + "pin_ids"),
+            "pin_uv": b.f64(k + "pin_uv").reshape(-1, 2),
+            "free_pos": b.i64(k + "free_pos"),
+            "csr_ptr": b.i64(k + "csr_ptr"),
+            "csr_cols": b.i64(k + "csr_cols"),
+            "csr_vals": b.f64(k + "csr_vals"),
+            "rhs": b.f64(k + "rhs"),
+        }
+        off = b.i64(k + "loop_off")
+        ids = b.i64(k + "loop_ids")
+        d["border_loops"] = [ids[off[i]:off[i + 1]] for i in range(len(off) - 1)]
+        if b.has(k + "uv"):
+            d["uv"] = b.f64(k + "uv").reshape(-1, 2)
+            d["iters"] = int(b.i64(k + "iters")[0])
+            d["err_accum"] = float(b.f64(k + "err_accum")[0])
+        if b.has(k + "sol"):
+            d["sol"] = b.f64(k + "sol")
+        if b.has(k + "metrics"):
+            d["metrics"] = b.f64(k + "metrics")
+        return d
+
+    def superlu_uv(self, c: int):
+        """FP64 sparse-LU oracle for chart ``c``: SuperLU (scipy) on the scalar block of the
+        exported interleaved CSR (the reference's A = L (x) I2 structure), both coordinate
+        right-hand sides, then the reference's damped driver update.  Returns the chart UVs."""
+        import scipy.sparse as sp
+        import scipy.sparse.linalg as spla
+
+        ch = self.chart(c)
+        n2 = len(ch["csr_ptr"]) - 1
+        A = sp.csr_matrix((ch["csr_vals"], ch["csr_cols"], ch["csr_ptr"]), shape=(n2, n2))
+        rhs = ch["rhs"]
+        if n2 == 0:
+            sol = np.array([1.0])
+        else:
+            L = A[0::2, 0::2].tocsc()
+            lu = spla.splu(L, permc_spec="COLAMD")
+            B = np.stack([rhs[0:n2:2], rhs[1:n2:2]], axis=1)
+            X = lu.solve(B)
+            sol = np.empty(n2 + 1)
+            sol[0:n2:2] = X[:, 0]
+            sol[1:n2:2] = X[:, 1]
+            sol[n2] = 1.0
+        self.bag.put_f64(f"c{c}.sol", sol)
+        lib().orc_driver_from_solution(self.bag.h, c, self.max_iter)
+        return self.bag.f64(f"c{c}.uv").reshape(-1, 2)
+
+    def metrics(self, c: int, uv):
+        uv = np.ascontiguousarray(uv, np.float64).reshape(-1)
+        out = np.empty(5)
+        lib().orc_chart_metrics(self.bag.h, c, _f64p(uv), _f64p(out))
+        return out
+
+
+def uv_error(uv_test, uv_ref) -> float:
+    """The reference's GPU/CPU parity measure (unwrap/src/lscm.rs:749-758):
+    max_i |uv_test_i - uv_ref_i| / max_i |uv_ref_i| (Euclidean per vertex)."""
+    a = np.asarray(uv_test, np.float64).reshape(-1, 2)
+    b = np.asarray(uv_ref, np.float64).reshape(-1, 2)
+    diff = np.sqrt(((a - b) ** 2).sum(1)).max(initial=0.0)
+    scale = max(np.sqrt((b ** 2).sum(1)).max(initial=0.0), 1e-30)
+    return float(diff / scale)
