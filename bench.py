@@ -1,0 +1,376 @@
+#!/usr/bin/env python
+"""Benchmark of the batched LSCM solve (one JSON line on rank 0).
+
+Workload (default): 4096 disk charts, triangle counts log-uniform in [50, 50 000] (seeded
+synthetic meshes, researchuv_gb300/workloads.py), one chart per disk, Dirichlet border pins
+(the reference's border-rectangle pass).  A step = one batched unfold of every chart: GPU
+assembly of the cotangent systems with the pins eliminated, one batched mixed-precision
+Jacobi-PCG over the packed block-diagonal operator to rel-res 1e-12 per chart, and the damped
+driver update.
+
+* value  — unknowns/s (sum over charts of 2 * free vertices per step time), inputs resident
+           in HBM (ruv_lscm_upload once), step time = device time of the three phases
+           (CUDA events on the library's stream).  Inputs (~1 GB operator) exceed L2.
+* e2e    — the same metric through ruv_lscm_solve_batch with host buffers: H2D of the
+           batch and D2H of the UVs inside the timed region (wall clock; the call is
+           synchronous).
+* roofline — the batched SpMV kernel (the dominant kernel) timed alone with CUDA events on
+           the same operator: algorithmic bytes per launch / mean launch time vs the
+           measured HBM copy bandwidth.
+* cpu_baseline — the reference CPU algorithm (the oracle port of unfold_chart + the BTreeMap
+           sparse LU) on a bounded sample of the same charts, 1 core; its UVs also give the
+           UV error of the GPU result on those charts (plus FP64 SuperLU on a few large charts).
+
+--impl reference times that CPU port on all host cores (process pool over charts, like the
+reference's par_map) as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "batched LSCM unknowns/s at <=1e-6 UV err vs FP64 LU"
+UNIT = "unknowns/s"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="disks4096", choices=["disks4096", "hf1024", "hf2048", "disks256"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        tdist.init_process_group("gloo", rank=rank, world_size=world)
+        pg = tdist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_workload(name):
+    import researchuv_gb300 as R
+    from researchuv_gb300 import workloads as W
+
+    t0 = time.time()
+    if name.startswith("disks"):
+        n = int(name[5:])
+        vo, to, p3, tr = W.disks(n, 50, 50_000, seed=3)
+        gen = time.time() - t0
+        charts = R.prepare_patches(vo, to, p3, tr)
+        cfg = {"workload": f"{n} displaced polar-disk charts, triangles log-uniform [50, 50000], seed 3",
+               "charts": n, "triangles": int(to[-1]), "vertices": int(vo[-1])}
+        src = ("patches", vo, to, p3, tr)
+    else:
+        n, ns, amp = (1024, 8, 0.15) if name == "hf1024" else (2048, 16, 0.3)
+        p, f = W.height_field(n, ns, amp, seed=2)
+        gen = time.time() - t0
+        charts = R.prepare_mesh(p, f)
+        cfg = {"workload": f"{n}x{n} height field, {ns} sines, amplitude {amp}, seed 2",
+               "charts": charts.n_charts, "triangles": int(f.shape[0]), "vertices": int(p.shape[0])}
+        src = ("mesh", p, f)
+    cfg["host_prep_s"] = round(time.time() - t0 - gen, 3)
+    return charts, cfg, src
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU (oracle) legs
+def _oracle_chart(args):
+    """One chart through the reference CPU algorithm (oracle port): weld(0) + segment +
+    unfold_chart with the BTreeMap LU.  Returns (uv, unknowns, seconds)."""
+    p, f = args
+    from oracle import oracle as O
+
+    t0 = time.perf_counter()
+    P = O.Pipeline(p, f, weld_tol=0.0, lu_limit=1 << 40)
+    dt = time.perf_counter() - t0
+    ch = P.chart(0)
+    return ch.get("uv"), 2 * int((ch["free_pos"] >= 0).sum()), dt, P.n_charts
+
+
+def _sample(src, budget_unknowns_cap=3000, n_max=400, seed=7):
+    """Chart ids of a bounded sample: charts whose reference LU is feasible (2 nf + 1 <= cap),
+    random order (seeded) so the sample spans the feasible part of the size distribution."""
+    _, vo, to, _, _ = src
+    nv = np.diff(vo)
+    ok = np.nonzero(nv <= budget_unknowns_cap // 2)[0]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rng.shuffle(ok)
+    return ok[:n_max]
+
+
+def cpu_baseline(src, uv_gpu, budget_s):
+    """1-core timing of the oracle port on a bounded sample + UV error of the GPU result."""
+    from oracle import oracle as O
+
+    kind, vo, to, p3, tr = src
+    ids = _sample(src)
+    t_total, unk, errs, used = 0.0, 0, [], 0
+    for c in ids:
+        if t_total > budget_s:
+            break
+        uv, u, dt, nch = _oracle_chart((p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]]))
+        t_total += dt
+        unk += u
+        used += 1
+        if uv is not None and nch == 1:
+            errs.append(O.uv_error(uv_gpu[vo[c]:vo[c + 1]], uv))
+    # a few of the largest charts against the FP64 SuperLU oracle
+    big = np.argsort(-np.diff(vo))[:6]
+    for c in big:
+        P = O.Pipeline(p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]], weld_tol=0.0, lu_limit=0)
+        if P.n_charts == 1:
+            errs.append(O.uv_error(uv_gpu[vo[c]:vo[c + 1]], P.superlu_uv(0)))
+    return {"value": unk / max(t_total, 1e-9), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{used} charts with 2nf+1 <= 3000 (reference LU feasible), {unk} unknowns, "
+                      f"{t_total:.1f} s on 1 core; weld+segment+unfold_chart+BTreeMap LU per chart"}, \
+        (max(errs) if errs else None), len(errs)
+
+
+def run_reference(args, rank):
+    """Reference arm: the reference CPU algorithm (oracle port) on all host cores."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    _, cfg, src = make_workload(args.workload)
+    if src[0] != "patches":
+        print(json.dumps({"impl": "reference", "metric": METRIC, "value": None, "unit": UNIT,
+                          "unavailable": "the reference LU is Theta(n^2) per chart: a single 1M-vertex chart is "
+                                         "infeasible (extrapolated hours); run the disks workload"}))
+        return
+    kind, vo, to, p3, tr = src
+    ids = _sample(src, n_max=100000)
+    cores = os.cpu_count() or 1
+    # size one step to ~8 s of all-core work: calibrate on the first charts
+    tasks = [(p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]]) for c in ids]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        probe = pool.map(_oracle_chart, tasks[:cores * 4])
+        per = (time.perf_counter() - t0) / max(len(probe), 1)
+        n_step = max(cores, min(len(tasks), int(8.0 / max(per, 1e-6))))
+        step_tasks = tasks[:n_step]
+        for _ in range(args.warmup):
+            pool.map(_oracle_chart, step_tasks[: max(cores, n_step // 4)])
+        times, unks = [], 0
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            out = pool.map(_oracle_chart, step_tasks)
+            times.append(time.perf_counter() - t0)
+            unks = sum(o[1] for o in out)
+    ms = 1000.0 * statistics.mean(times)
+    value = unks / (ms / 1000.0)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {**cfg, "sample": f"{len(step_tasks)} charts per step (2nf+1 <= 3000)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{len(step_tasks)} charts/step, {unks} unknowns, process pool over charts"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU arm
+def main():
+    args = parse()
+    rank, world, local, pg = dist()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        barrier(pg)
+        return
+    import ctypes
+
+    import researchuv_gb300 as R
+
+    charts, cfg, src = make_workload(args.workload)
+    ctx = R.Context(local)
+    L = R.lib()
+    batch = charts.batch()
+    vo = charts.i64("chart.vert_off")
+    nv = int(vo[-1])
+    prec = R.Precision.MIXED if args.precision == "mixed" else R.Precision.FP64
+    opts = R.UnfoldOptions(precision=prec, precond=R.Precond.JACOBI)
+    copts = opts.to_c()
+    stats = (R.RuvChartStat * max(batch.n_charts, 1))()
+
+    # warm-up (also the first e2e solve: allocates the workspace)
+    for _ in range(max(args.warmup, 1)):
+        uv, st, status = R.solve_batch(ctx, batch, opts, nv)
+    n_free = np.array([s.n_free for s in st])
+    unknowns = int(2 * n_free.sum())
+    statuses = np.array([s.status for s in st])
+    cg_iters = np.array([s.cg_iters for s in st])
+
+    # device-resident timed region
+    ctx.check(L.ruv_lscm_upload(ctx.h, ctypes.byref(batch)), "upload")
+    ctx.check(L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(copts), stats), "solve")  # warm
+    clk = Clocks(local)
+    barrier(pg)
+    clk.start()
+    l0 = L.ruv_kernel_launches(ctx.h)
+    dev_ms = []
+    phases = np.zeros(3)
+    for _ in range(args.steps):
+        ctx.check(L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(copts), stats), "solve")
+        t = R.last_timings(ctx)
+        phases += np.array(t)
+        dev_ms.append(sum(t))
+    launches = (L.ruv_kernel_launches(ctx.h) - l0) // max(args.steps, 1)
+    barrier(pg)
+    # end-to-end through the host-buffer call
+    e2e_ms = []
+    uv = np.empty((nv, 2))
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st_ = L.ruv_lscm_solve_batch(ctx.h, ctypes.byref(batch), ctypes.byref(copts),
+                                     uv.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), stats)
+        e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+        ctx.check(st_, "e2e")
+    barrier(pg)
+    clock_info = clk.stop()
+    ms = allmax(pg, statistics.mean(dev_ms))
+    ems = allmax(pg, statistics.mean(e2e_ms))
+    phases /= max(args.steps, 1)
+
+    # dominant kernel (batched SpMV) timed alone on the same operator
+    spmv_ms, spmv_bytes = R.bench_spmv(ctx, prec, reps=30, n_buffers=2)
+    peak, peak_src = peaks()
+    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9 if spmv_ms > 0 else 0.0
+
+    h2d = sum(int(x) for x in [
+        8 * (batch.n_charts + 1) * 2, 3 * 8 * nv, 3 * 4 * int(charts.i64("chart.tri_off")[-1]), nv, 2 * 8 * nv,
+        2 * 8 * nv])
+    d2h = 2 * 8 * nv
+
+    line = {
+        "metric": METRIC, "value": world * unknowns / (ms / 1000.0), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if prec == R.Precision.MIXED else "f64",
+        "data": "synthetic",
+        "config": {**cfg, "unknowns": unknowns, "precision": args.precision, "precond": "jacobi",
+                   "tol": 1e-12, "l2": "inputs larger than L2 (operator + vectors ~1 GB)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "phase_ms": {"assembly": round(phases[0], 3), "pcg": round(phases[1], 3),
+                                "driver": round(phases[2], 3)},
+                   "cg_iters_max": int(cg_iters.max()), "cg_iters_mean": float(cg_iters.mean()),
+                   "charts_not_ok": int((statuses != 0).sum())},
+        "e2e": {"value": world * unknowns / (ems / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": ems},
+        "roofline": {"bound": "hbm", "kernel": "k_spmv_pq (batched CSR-vector SpMV + p.q)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "traffic": None, "ms_per_launch": spmv_ms,
+                     "algorithmic_bytes": spmv_bytes},
+        "gpu_launches": int(launches),
+        "clocks": clock_info,
+    }
+    if rank == 0 and not args.no_cpu_baseline and src[0] == "patches":
+        base, err, n_err = cpu_baseline(src, uv, args.cpu_budget)
+        line["cpu_baseline"] = base
+        line["uv_err_max_vs_lu"] = err
+        line["uv_err_charts_checked"] = n_err
+    if rank == 0:
+        print(json.dumps(line))
+    barrier(pg)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,199 @@
+/* ruv.h — C ABI of the GB300 (sm_103a) LSCM solve path.
+ *
+ * Drop-in boundary for ResearchUV's CUDA solve (paths relative to the reference's crates/,
+ * `researchuv-` prefix dropped):
+ *   GpuSolver::global / GpuSolver::new      gpu/src/solver.rs:104-113, :122-201  -> ruv_ctx_create
+ *   GpuSolver::cg_solve_precond            gpu/src/solver.rs:284-565            -> ruv_cg_solve
+ *   GpuSolver::cg_solve                    gpu/src/solver.rs:274-277            -> ruv_cg_solve(PRECOND_NONE)
+ *   GpuSolver::apply_ic0_for_test          gpu/src/solver.rs:205-270            -> ruv_apply_ic0
+ *   Precond {None, Jacobi, Ic0, Ic0Color, Amg, AmgSa}  gpu/src/precond.rs:20-47 -> ruv_precond
+ *   unfold_chart with SolverBackend::Gpu   unwrap/src/lscm.rs:471-506, :512-727 -> ruv_lscm_solve_batch
+ *   weld + segment + border pass (the chart stages of pipeline::run)
+ *                                          unwrap/src/pipeline.rs:146-150, lscm.rs:512-592
+ *                                                                               -> ruv_prepare_mesh / ruv_prepare_patches
+ *
+ * Conventions: every entry returns a ruv_status (the reference's Option::None maps to any
+ * non-OK status; the caller decides about a CPU fallback, the library never falls back).
+ * Host buffers are caller-owned; device buffers are owned by the context and reused across
+ * calls.  No exceptions cross the ABI.  A context is not thread-safe: use one per thread
+ * (each holds its own CUDA stream) or serialise calls.
+ */
+#ifndef RUV_H
+#define RUV_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RUV_ABI_VERSION 1
+
+typedef enum ruv_status {
+  RUV_OK = 0,
+  RUV_ERR_NO_DEVICE = 1,     /* no CUDA device / wrong architecture            */
+  RUV_ERR_BAD_INPUT = 2,     /* malformed sizes, indices or options            */
+  RUV_ERR_OOM = 3,           /* device allocation failed                       */
+  RUV_ERR_NOT_CONVERGED = 4, /* max_iter reached above tolerance (any chart)   */
+  RUV_ERR_BREAKDOWN = 5,     /* |p.Ap| <= 1e-300, non-finite, or zero diagonal */
+  RUV_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up             */
+  RUV_ERR_LAUNCH = 7,        /* a CUDA launch / runtime call failed            */
+  RUV_ERR_INTERNAL = 8
+} ruv_status;
+
+/* gpu/src/precond.rs:20-47 */
+typedef enum ruv_precond {
+  RUV_PRECOND_NONE = 0,
+  RUV_PRECOND_JACOBI = 1,
+  RUV_PRECOND_IC0 = 2,
+  RUV_PRECOND_IC0_COLOR = 3,
+  RUV_PRECOND_AMG = 4,
+  RUV_PRECOND_AMG_SA = 5
+} ruv_precond;
+
+/* Arithmetic of the inner Krylov loop. */
+typedef enum ruv_precision {
+  RUV_PREC_FP64 = 0,  /* FP64 PCG throughout                                        */
+  RUV_PREC_MIXED = 1  /* FP32 SpMV / preconditioner / CG, FP64 true residual r = b - Ax
+                         and FP64 solution accumulation (reliable-update refinement)   */
+} ruv_precision;
+
+typedef struct ruv_ctx ruv_ctx;
+
+int32_t ruv_abi_version(void);
+const char* ruv_status_str(ruv_status s);
+
+/* GpuSolver::new (gpu/src/solver.rs:122-201): device init, kernels resident (no JIT). */
+ruv_status ruv_ctx_create(ruv_ctx** out, int32_t device);
+void ruv_ctx_destroy(ruv_ctx* ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char* ruv_last_error(const ruv_ctx* ctx);
+
+/* GpuSolver::cg_solve_precond (gpu/src/solver.rs:284-565).
+ * A: n x n SPD CSR (row_ptr[n+1], cols[nnz], vals[nnz]); b[n]; x_out[n] (written on OK).
+ * Stops when ||r|| <= tol * ||b|| (tol absolute when ||b|| <= 1e-300), x0 = 0.
+ * iters_out (may be NULL) receives the iteration count.  NOT_CONVERGED after max_iter;
+ * BREAKDOWN on |p.Ap| <= 1e-300 or a non-finite iterate (solver.rs:505-508, :561-563);
+ * BAD_INPUT on size mismatches (solver.rs:297-299) or a zero diagonal under Jacobi
+ * (precond.rs:595-611). */
+ruv_status ruv_cg_solve(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols,
+                        const double* vals, const double* b, double* x_out, int64_t max_iter,
+                        double tol, ruv_precond pc, int64_t* iters_out);
+
+/* GpuSolver::apply_ic0_for_test (gpu/src/solver.rs:205-270): z = (L L^T)^-1 r with the
+ * IC(0) factor of A (natural order, pivot floor 1e-12 |a_ii|, precond.rs:145-219). */
+ruv_status ruv_apply_ic0(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols,
+                         const double* vals, const double* r, double* z_out);
+
+/* ------------------------------------------------------------------ batched LSCM solve */
+
+/* All charts of a mesh, packed.  Chart c owns packed vertices [vert_off[c], vert_off[c+1])
+ * in chart-local order (ascending source id) and triangles [tri_off[c], tri_off[c+1]) whose
+ * indices are chart-local.  This is the data unfold_chart consumes (lscm.rs:512-592):
+ * positions, triangles in chart order, Dirichlet pins with their targets, and the
+ * tangent-frame projection p2 that seeds the driver. */
+typedef struct ruv_lscm_batch {
+  int64_t n_charts;
+  const int64_t* vert_off; /* n_charts + 1 */
+  const int64_t* tri_off;  /* n_charts + 1 */
+  const double* p3;        /* 3 * n_verts */
+  const int32_t* tris;     /* 3 * n_tris (chart-local) */
+  const uint8_t* pinned;   /* n_verts, 1 = pinned */
+  const double* pin_uv;    /* 2 * n_verts, target of pinned vertices (others ignored) */
+  const double* p2;        /* 2 * n_verts */
+} ruv_lscm_batch;
+
+/* UnfoldOptions (lscm.rs:76-101) plus the solver controls of gpu_solve (lscm.rs:471-506). */
+typedef struct ruv_unfold_opts {
+  double angle_mix;        /* #AngleDistanceMix, default 1.0 (mix_b = 1 - angle_mix)  */
+  double mix_w;            /* slack weight, default 1.0 (must be > 0)                 */
+  int32_t max_iter;        /* driver iterations, default 100                          */
+  ruv_precond precond;     /* default JACOBI (lscm.rs:498)                            */
+  ruv_precision precision; /* default MIXED                                           */
+  double tol;              /* relative residual per chart, default 1e-12 (lscm.rs:501) */
+  int64_t max_cg_iter;     /* default max(max_iter, 1024) * 16 (lscm.rs:501)         */
+} ruv_unfold_opts;
+
+void ruv_unfold_opts_default(ruv_unfold_opts* o);
+
+/* Per-chart outcome (UnfoldResult, lscm.rs:105-116, plus solver statistics). */
+typedef struct ruv_chart_stat {
+  int32_t status;       /* ruv_status of this chart's solve                    */
+  int32_t driver_iters; /* UnfoldResult::iters                                  */
+  int32_t cg_iters;     /* Krylov iterations                                    */
+  int32_t n_free;       /* free (unpinned) vertices; unknowns = 2 * n_free      */
+  double rel_res;       /* final ||b - Ax|| / ||b|| in FP64                     */
+  double err_accum;     /* UnfoldResult::err_accum                              */
+} ruv_chart_stat;
+
+/* One batched unfold of every chart: GPU assembly of the cotangent system with pins
+ * eliminated, one batched PCG over the packed block-diagonal operator with per-chart
+ * convergence, and the damped driver update.  uv_out: 2 * n_verts (chart-local order, as
+ * UnfoldResult::uv).  stats: n_charts entries (may be NULL).  Returns the worst chart
+ * status (OK when every chart converged). */
+ruv_status ruv_lscm_solve_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, const ruv_unfold_opts* opts,
+                                double* uv_out, ruv_chart_stat* stats);
+
+/* Device-resident variant of ruv_lscm_solve_batch, split in three: upload a batch into the
+ * context, solve it (assembly + batched PCG + driver, results stay in device memory), and
+ * download the UVs.  ruv_lscm_solve_batch is exactly these three calls. */
+ruv_status ruv_lscm_upload(ruv_ctx* ctx, const ruv_lscm_batch* in);
+ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ruv_chart_stat* stats);
+ruv_status ruv_lscm_download_uv(ruv_ctx* ctx, double* uv_out);
+
+/* Device time (ms, CUDA events on the context stream) of the phases of the last
+ * ruv_lscm_solve_resident: [0] assembly, [1] batched PCG, [2] driver update.
+ * Returns the number of values written (<= n). */
+int32_t ruv_last_timings(const ruv_ctx* ctx, double* ms, int32_t n);
+
+/* Number of kernels this context has enqueued so far (each node of a replayed CUDA graph
+ * counts once per replay). */
+int64_t ruv_kernel_launches(const ruv_ctx* ctx);
+
+/* Kernel benchmark on the last assembled batch: `reps` launches of the batched SpMV kernel
+ * (q = A p over every row, FP32 values when precision is MIXED, FP64 otherwise), rotating
+ * between `n_buffers` vector sets so the timed launches read their vectors from HBM.
+ * Writes the mean device time per launch (ms, CUDA events) and the algorithmic bytes of
+ * one launch (values + columns + row pointers + p read once + q written). */
+ruv_status ruv_bench_spmv(ruv_ctx* ctx, ruv_precision precision, int32_t reps, int32_t n_buffers,
+                          double* ms_per_launch, double* bytes_per_launch);
+
+/* ------------------------------------------------------------------ host chart stages */
+
+typedef struct ruv_prepared ruv_prepared;
+
+/* weld (weld.rs:19-57) + segment (segment.rs:130-331) of a raw triangle soup, then per
+ * chart the tangent frame (lscm.rs:152-183) and the pins: border rectangle
+ * (lscm.rs:280-413) or 4 anchors for closed charts (lscm.rs:210-247, :524-542). */
+ruv_status ruv_prepare_mesh(const double* pos, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                            double weld_tol, double angle_min_deg, int32_t threads, ruv_prepared** out);
+/* Charts given directly (one chart per patch, no weld / segmentation): patch c owns
+ * vertices [vert_off[c], vert_off[c+1]) and triangles [tri_off[c], tri_off[c+1]) with
+ * patch-local indices.  Border loops are walked over each patch's boundary edges. */
+ruv_status ruv_prepare_patches(int64_t n_patches, const int64_t* vert_off, const int64_t* tri_off,
+                               const double* p3, const int32_t* tris, int32_t threads, ruv_prepared** out);
+void ruv_prepared_free(ruv_prepared* p);
+/* Read-only view of the prepared charts as the batched-solve input (valid while p lives). */
+ruv_status ruv_prepared_batch(const ruv_prepared* p, ruv_lscm_batch* view);
+
+/* Structure queries for parity checks.  `what` selects an int64 array:
+ *   "chart.vert_off" (n_charts+1)  "chart.tri_off" (n_charts+1)  "chart.vertex_ids" (source id
+ *   per packed vertex)  "chart.face_ids" (source face per packed triangle)  "chart.border_off"
+ *   "chart.border"  "chart.loop_off" (per chart, into loop_seg)  "chart.loop_seg" (per loop,
+ *   into loop_ids)  "chart.loop_ids"  "mesh.faces"  "chart.pinned"
+ * or a double array: "chart.area3d"  "mesh.pos"  "chart.pin_uv"  "chart.p2"  "chart.p3".
+ * Returns the element count (copies when out != NULL), or -1 for an unknown name. */
+int64_t ruv_prepared_get_i64(const ruv_prepared* p, const char* what, int64_t* out);
+int64_t ruv_prepared_get_f64(const ruv_prepared* p, const char* what, double* out);
+
+/* Assembled system of one chart of the last ruv_lscm_solve_batch on ctx, exported as the
+ * interleaved CSR the reference hands its GPU solver (Sparse::to_csr(2 nf), sparse.rs:69-84):
+ * row_ptr[2nf+1], cols[nnz], vals[nnz], rhs[2nf].  Call with NULL buffers to get nnz and nf. */
+ruv_status ruv_export_chart_system(ruv_ctx* ctx, int64_t chart, int64_t* nf_out, int64_t* nnz_out,
+                                   int32_t* row_ptr, int32_t* cols, double* vals, double* rhs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RUV_H */

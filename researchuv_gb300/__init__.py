@@ -1,0 +1,445 @@
+"""researchuv_gb300 — GB300 (sm_103a) LSCM solve path behind ResearchUV's GPU-solver boundary.
+
+Python mirror of the reference's interface for this path (names and argument meaning as in
+the reference; paths relative to its crates/, ``researchuv-`` dropped):
+
+* :class:`CsrMatrix`, :class:`Precond`, :class:`GpuSolver` — ``gpu/src/solver.rs:14-44``,
+  ``gpu/src/precond.rs:20-47``, ``GpuSolver::{global,new,cg_solve,cg_solve_precond,
+  apply_ic0_for_test}`` (``solver.rs:104-565``).  Failures return ``None`` as the reference's
+  ``Option`` does; the reason is in :attr:`GpuSolver.last_error`.
+* :class:`UnfoldOptions`, :class:`UnfoldResult`, :class:`SolverBackend` —
+  ``unwrap/src/lscm.rs:56-116``.
+* :func:`prepare_mesh` / :func:`prepare_patches` + :func:`unfold_charts` — the chart stages
+  and the per-chart unfold of ``unwrap/src/pipeline.rs:146-194``, all charts in one batched
+  GPU solve.
+
+Everything runs through ``libruv.so`` (C ABI in ``include/ruv.h``).  There is no CPU
+fallback: importing works without a GPU, but every solve raises or returns ``None`` when
+no sm_103a device is present, and a missing library raises at first use.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import enum
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libruv.so")
+
+_P = ctypes.POINTER
+_i32, _i64, _f64, _u8, _vp, _cp = (ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_uint8,
+                                   ctypes.c_void_p, ctypes.c_char_p)
+
+
+class RuvBatch(ctypes.Structure):
+    _fields_ = [("n_charts", _i64), ("vert_off", _P(_i64)), ("tri_off", _P(_i64)), ("p3", _P(_f64)),
+                ("tris", _P(_i32)), ("pinned", _P(_u8)), ("pin_uv", _P(_f64)), ("p2", _P(_f64))]
+
+
+class RuvUnfoldOpts(ctypes.Structure):
+    _fields_ = [("angle_mix", _f64), ("mix_w", _f64), ("max_iter", _i32), ("precond", ctypes.c_int),
+                ("precision", ctypes.c_int), ("tol", _f64), ("max_cg_iter", _i64)]
+
+
+class RuvChartStat(ctypes.Structure):
+    _fields_ = [("status", _i32), ("driver_iters", _i32), ("cg_iters", _i32), ("n_free", _i32),
+                ("rel_res", _f64), ("err_accum", _f64)]
+
+
+# every symbol include/ruv.h declares, with its ctypes signature
+SIGNATURES = {
+    "ruv_abi_version": (_i32, []),
+    "ruv_status_str": (_cp, [ctypes.c_int]),
+    "ruv_ctx_create": (ctypes.c_int, [_P(_vp), _i32]),
+    "ruv_ctx_destroy": (None, [_vp]),
+    "ruv_last_error": (_cp, [_vp]),
+    "ruv_cg_solve": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _P(_f64), _P(_f64), _i64, _f64,
+                                    ctypes.c_int, _P(_i64)]),
+    "ruv_apply_ic0": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _P(_f64), _P(_f64)]),
+    "ruv_unfold_opts_default": (None, [_P(RuvUnfoldOpts)]),
+    "ruv_lscm_solve_batch": (ctypes.c_int, [_vp, _P(RuvBatch), _P(RuvUnfoldOpts), _P(_f64), _P(RuvChartStat)]),
+    "ruv_prepare_mesh": (ctypes.c_int, [_P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _i32, _P(_vp)]),
+    "ruv_prepare_patches": (ctypes.c_int, [_i64, _P(_i64), _P(_i64), _P(_f64), _P(_i32), _i32, _P(_vp)]),
+    "ruv_prepared_free": (None, [_vp]),
+    "ruv_prepared_batch": (ctypes.c_int, [_vp, _P(RuvBatch)]),
+    "ruv_prepared_get_i64": (_i64, [_vp, _cp, _P(_i64)]),
+    "ruv_prepared_get_f64": (_i64, [_vp, _cp, _P(_f64)]),
+    "ruv_export_chart_system": (ctypes.c_int, [_vp, _i64, _P(_i64), _P(_i64), _P(_i32), _P(_i32), _P(_f64),
+                                               _P(_f64)]),
+    "ruv_lscm_upload": (ctypes.c_int, [_vp, _P(RuvBatch)]),
+    "ruv_lscm_solve_resident": (ctypes.c_int, [_vp, _P(RuvUnfoldOpts), _P(RuvChartStat)]),
+    "ruv_lscm_download_uv": (ctypes.c_int, [_vp, _P(_f64)]),
+    "ruv_last_timings": (_i32, [_vp, _P(_f64), _i32]),
+    "ruv_kernel_launches": (_i64, [_vp]),
+    "ruv_bench_spmv": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _i32, _P(_f64), _P(_f64)]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded libruv.so (built by :func:`researchuv_gb300.build.build`).  Raises if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libruv.so not built ({LIB_PATH}); run researchuv_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class Status(enum.IntEnum):
+    OK = 0
+    NO_DEVICE = 1
+    BAD_INPUT = 2
+    OOM = 3
+    NOT_CONVERGED = 4
+    BREAKDOWN = 5
+    TIMEOUT = 6
+    LAUNCH = 7
+    INTERNAL = 8
+
+
+class RuvError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = Status(status)
+        super().__init__(f"{self.status.name}: {msg}")
+
+
+class Precond(enum.IntEnum):
+    """gpu/src/precond.rs:20-47 (``None`` is spelled NONE)."""
+    NONE = 0
+    JACOBI = 1
+    IC0 = 2
+    IC0_COLOR = 3
+    AMG = 4
+    AMG_SA = 5
+
+    @classmethod
+    def from_env(cls) -> "Precond":
+        """RESEARCHUV_GPU_PRECOND, as unwrap/src/lscm.rs:492-499 reads it (default Jacobi)."""
+        return {"amgsa": cls.AMG_SA, "amg": cls.AMG, "ic0color": cls.IC0_COLOR, "ic0": cls.IC0,
+                "none": cls.NONE}.get(os.environ.get("RESEARCHUV_GPU_PRECOND", ""), cls.JACOBI)
+
+
+class Precision(enum.IntEnum):
+    FP64 = 0
+    MIXED = 1
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(_P(ct)) if a is not None else None
+
+
+# ------------------------------------------------------------------ GpuSolver boundary
+@dataclasses.dataclass
+class CsrMatrix:
+    """gpu/src/solver.rs:14-44."""
+    vals: np.ndarray
+    cols: np.ndarray
+    row_ptr: np.ndarray
+
+    def __post_init__(self):
+        self.vals = np.ascontiguousarray(self.vals, np.float64)
+        self.cols = np.ascontiguousarray(self.cols, np.int32)
+        self.row_ptr = np.ascontiguousarray(self.row_ptr, np.int32)
+
+    def rows(self) -> int:
+        return max(len(self.row_ptr) - 1, 0)
+
+    def row(self, i):
+        lo, hi = self.row_ptr[i], self.row_ptr[i + 1]
+        return list(zip(self.cols[lo:hi].tolist(), self.vals[lo:hi].tolist()))
+
+    def row_get(self, i, j) -> float:
+        for c, v in self.row(i):
+            if c == j:
+                return v
+        return 0.0
+
+
+class Context:
+    """One device context (stream + reusable device workspace).  Not thread-safe."""
+
+    def __init__(self, device: int = 0):
+        h = _vp()
+        st = lib().ruv_ctx_create(ctypes.byref(h), device)
+        if st != 0:
+            raise RuvError(st, "ruv_ctx_create(device=%d)" % device)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ruv_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self) -> str:
+        return lib().ruv_last_error(self.h).decode()
+
+    def check(self, st, what=""):
+        if st != 0:
+            raise RuvError(st, f"{what}: {self.last_error()}")
+
+
+class GpuSolver:
+    """gpu/src/solver.rs:49-565 — FP64 (P)CG on one SPD CSR system."""
+
+    _global: Optional["GpuSolver"] = None
+    _global_tried = False
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.last_error = ""
+
+    @classmethod
+    def new(cls, device: int = 0) -> Optional["GpuSolver"]:
+        try:
+            return cls(Context(device))
+        except RuvError:
+            return None
+
+    @classmethod
+    def global_(cls) -> Optional["GpuSolver"]:
+        """GpuSolver::global (solver.rs:104-113): initialised once; None without a device."""
+        if not cls._global_tried:
+            cls._global_tried = True
+            cls._global = cls.new()
+        return cls._global
+
+    def cg_solve_precond(self, a: CsrMatrix, b: Sequence[float], max_iter: int, tol: float,
+                         precond: Precond = Precond.NONE):
+        """solver.rs:284-565.  Returns (x, iters) or None."""
+        b = np.ascontiguousarray(b, np.float64)
+        n = a.rows()
+        if n == 0 or b.size != n or a.cols.size != a.vals.size or a.row_ptr.size != n + 1:
+            self.last_error = "dimension mismatch"
+            return None
+        x = np.empty(n, np.float64)
+        iters = _i64(0)
+        st = lib().ruv_cg_solve(self.ctx.h, n, _ptr(a.row_ptr, _i32), _ptr(a.cols, _i32), _ptr(a.vals, _f64),
+                                _ptr(b, _f64), _ptr(x, _f64), int(max_iter), float(tol), int(precond),
+                                ctypes.byref(iters))
+        if st != 0:
+            self.last_error = f"{Status(st).name}: {self.ctx.last_error()}"
+            return None
+        return x, int(iters.value)
+
+    def cg_solve(self, a: CsrMatrix, b, max_iter: int, tol: float):
+        r = self.cg_solve_precond(a, b, max_iter, tol, Precond.NONE)
+        return None if r is None else r[0]
+
+    def apply_ic0_for_test(self, a: CsrMatrix, r):
+        r = np.ascontiguousarray(r, np.float64)
+        if r.size != a.rows():
+            return None
+        z = np.empty_like(r)
+        st = lib().ruv_apply_ic0(self.ctx.h, a.rows(), _ptr(a.row_ptr, _i32), _ptr(a.cols, _i32),
+                                 _ptr(a.vals, _f64), _ptr(r, _f64), _ptr(z, _f64))
+        if st != 0:
+            self.last_error = f"{Status(st).name}: {self.ctx.last_error()}"
+            return None
+        return z
+
+
+# ------------------------------------------------------------------ unfold driver
+class SolverBackend(enum.Enum):
+    """unwrap/src/lscm.rs:56-72.  This library implements the GPU backend only."""
+    CPU = "cpu"
+    GPU = "gpu"
+
+
+@dataclasses.dataclass
+class UnfoldOptions:
+    """unwrap/src/lscm.rs:74-101 plus the GPU solve controls (lscm.rs:471-506)."""
+    max_iter: int = 100
+    angle_mix: float = 1.0
+    keep_metric: bool = False
+    target_area: float = 0.0
+    mix_w: float = 1.0
+    solver: SolverBackend = SolverBackend.GPU
+    precond: Precond = dataclasses.field(default_factory=Precond.from_env)
+    precision: Precision = Precision.MIXED
+    tol: float = 1e-12
+    max_cg_iter: int = 0  # 0 = max(max_iter, 1024) * 16 (lscm.rs:501)
+
+    def to_c(self) -> RuvUnfoldOpts:
+        if self.keep_metric:
+            raise RuvError(Status.BAD_INPUT, "KeepMetric's non-symmetric area row is not on the GPU path "
+                                             "(lscm.rs:677)")
+        if self.solver != SolverBackend.GPU:
+            raise RuvError(Status.BAD_INPUT, "this library implements SolverBackend::Gpu only")
+        o = RuvUnfoldOpts()
+        lib().ruv_unfold_opts_default(ctypes.byref(o))
+        o.angle_mix = self.angle_mix
+        o.mix_w = self.mix_w
+        o.max_iter = self.max_iter
+        o.precond = int(self.precond)
+        o.precision = int(self.precision)
+        o.tol = self.tol
+        o.max_cg_iter = self.max_cg_iter if self.max_cg_iter > 0 else max(self.max_iter, 1024) * 16
+        return o
+
+
+@dataclasses.dataclass
+class UnfoldResult:
+    """unwrap/src/lscm.rs:103-116 plus solver statistics."""
+    uv: np.ndarray
+    iters: int
+    err_accum: float
+    target: float
+    area3d: float
+    status: Status = Status.OK
+    cg_iters: int = 0
+    n_free: int = 0
+    rel_res: float = 0.0
+
+
+class Charts:
+    """Charts prepared on the host (weld + segment + tangent frames + pins), packed."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ruv_prepared_free(self.h)
+            self.h = None
+
+    def i64(self, what: str) -> np.ndarray:
+        n = lib().ruv_prepared_get_i64(self.h, what.encode(), None)
+        if n < 0:
+            raise KeyError(what)
+        out = np.empty(n, np.int64)
+        lib().ruv_prepared_get_i64(self.h, what.encode(), _ptr(out, _i64))
+        return out
+
+    def f64(self, what: str) -> np.ndarray:
+        n = lib().ruv_prepared_get_f64(self.h, what.encode(), None)
+        if n < 0:
+            raise KeyError(what)
+        out = np.empty(n, np.float64)
+        lib().ruv_prepared_get_f64(self.h, what.encode(), _ptr(out, _f64))
+        return out
+
+    @property
+    def n_charts(self) -> int:
+        return len(self.i64("chart.vert_off")) - 1
+
+    def batch(self) -> RuvBatch:
+        v = RuvBatch()
+        st = lib().ruv_prepared_batch(self.h, ctypes.byref(v))
+        if st != 0:
+            raise RuvError(st, "ruv_prepared_batch")
+        return v
+
+    def chart(self, c: int) -> dict:
+        vo, to, bo = self.i64("chart.vert_off"), self.i64("chart.tri_off"), self.i64("chart.border_off")
+        lo, ls, li = self.i64("chart.loop_off"), self.i64("chart.loop_seg"), self.i64("chart.loop_ids")
+        v0, v1, t0, t1 = vo[c], vo[c + 1], to[c], to[c + 1]
+        return {
+            "vertex_ids": self.i64("chart.vertex_ids")[v0:v1],
+            "face_ids": self.i64("chart.face_ids")[t0:t1],
+            "tris": self.i64("chart.tris").reshape(-1, 3)[t0:t1],
+            "border": self.i64("chart.border")[bo[c]:bo[c + 1]],
+            "border_loops": [li[ls[k]:ls[k + 1]] for k in range(lo[c], lo[c + 1])],
+            "area3d": float(self.f64("chart.area3d")[c]),
+            "p2": self.f64("chart.p2").reshape(-1, 2)[v0:v1],
+            "pinned": self.i64("chart.pinned")[v0:v1].astype(bool),
+            "pin_uv": self.f64("chart.pin_uv").reshape(-1, 2)[v0:v1],
+        }
+
+
+def prepare_mesh(positions, faces, weld_tol: float = 1e-12, angle_min_deg: float = 30.0,
+                 threads: int = 0) -> Charts:
+    """weld (weld.rs:19-57) + segment (segment.rs:130-331) + per-chart frames and pins."""
+    p = np.ascontiguousarray(positions, np.float64).reshape(-1, 3)
+    f = np.ascontiguousarray(faces, np.int32).reshape(-1, 3)
+    h = _vp()
+    st = lib().ruv_prepare_mesh(_ptr(p, _f64), p.shape[0], _ptr(f, _i32), f.shape[0], weld_tol, angle_min_deg,
+                                threads, ctypes.byref(h))
+    if st != 0:
+        raise RuvError(st, "ruv_prepare_mesh")
+    return Charts(h)
+
+
+def prepare_patches(vert_off, tri_off, p3, tris, threads: int = 0) -> Charts:
+    """One chart per given patch (no weld / segmentation)."""
+    vo = np.ascontiguousarray(vert_off, np.int64)
+    to = np.ascontiguousarray(tri_off, np.int64)
+    p = np.ascontiguousarray(p3, np.float64).reshape(-1)
+    t = np.ascontiguousarray(tris, np.int32).reshape(-1)
+    h = _vp()
+    st = lib().ruv_prepare_patches(len(vo) - 1, _ptr(vo, _i64), _ptr(to, _i64), _ptr(p, _f64), _ptr(t, _i32),
+                                   threads, ctypes.byref(h))
+    if st != 0:
+        raise RuvError(st, "ruv_prepare_patches")
+    return Charts(h)
+
+
+def solve_batch(ctx: Context, batch: RuvBatch, opts: UnfoldOptions, n_verts: int, check: bool = True):
+    """ruv_lscm_solve_batch on a packed batch.  Returns (uv (n_verts, 2), stats list, status)."""
+    o = opts.to_c()
+    uv = np.empty((n_verts, 2), np.float64)
+    stats = (RuvChartStat * max(batch.n_charts, 1))()
+    st = lib().ruv_lscm_solve_batch(ctx.h, ctypes.byref(batch), ctypes.byref(o), _ptr(uv, _f64), stats)
+    if check and st not in (0, Status.NOT_CONVERGED):
+        ctx.check(st, "ruv_lscm_solve_batch")
+    return uv, [stats[i] for i in range(batch.n_charts)], Status(st)
+
+
+def unfold_charts(ctx: Context, charts: Charts, opts: Optional[UnfoldOptions] = None) -> List[UnfoldResult]:
+    """unfold_chart (lscm.rs:512-727) for every chart, in one batched GPU solve."""
+    opts = opts or UnfoldOptions()
+    vo = charts.i64("chart.vert_off")
+    area = charts.f64("chart.area3d")
+    uv, stats, _ = solve_batch(ctx, charts.batch(), opts, int(vo[-1]))
+    out = []
+    for c, s in enumerate(stats):
+        out.append(UnfoldResult(uv=uv[vo[c]:vo[c + 1]].copy(), iters=s.driver_iters, err_accum=s.err_accum,
+                                target=opts.target_area if opts.target_area > 0 else float(area[c]),
+                                area3d=float(area[c]), status=Status(s.status), cg_iters=s.cg_iters,
+                                n_free=s.n_free, rel_res=s.rel_res))
+    return out
+
+
+def export_chart_system(ctx: Context, chart: int):
+    """Interleaved CSR (Sparse::to_csr(2 nf), sparse.rs:69-84) + rhs of a chart of the last batch."""
+    nf, nnz = _i64(0), _i64(0)
+    ctx.check(lib().ruv_export_chart_system(ctx.h, chart, ctypes.byref(nf), ctypes.byref(nnz), None, None, None,
+                                            None), "export")
+    rp = np.empty(2 * nf.value + 1, np.int32)
+    cols = np.empty(nnz.value, np.int32)
+    vals = np.empty(nnz.value, np.float64)
+    rhs = np.empty(2 * nf.value, np.float64)
+    ctx.check(lib().ruv_export_chart_system(ctx.h, chart, ctypes.byref(nf), ctypes.byref(nnz), _ptr(rp, _i32),
+                                            _ptr(cols, _i32), _ptr(vals, _f64), _ptr(rhs, _f64)), "export")
+    return rp, cols, vals, rhs
+
+
+def last_timings(ctx: Context):
+    """Device ms of [assembly, batched PCG, driver] of the last resident solve."""
+    out = (_f64 * 3)()
+    n = lib().ruv_last_timings(ctx.h, out, 3)
+    return [out[i] for i in range(n)]
+
+
+def bench_spmv(ctx: Context, precision: Precision = Precision.MIXED, reps: int = 20, n_buffers: int = 2):
+    """(ms per launch, algorithmic bytes per launch) of the batched SpMV on the last assembled batch."""
+    ms, by = _f64(0), _f64(0)
+    ctx.check(lib().ruv_bench_spmv(ctx.h, int(precision), reps, n_buffers, ctypes.byref(ms), ctypes.byref(by)),
+              "ruv_bench_spmv")
+    return ms.value, by.value

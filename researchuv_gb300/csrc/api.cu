@@ -1,0 +1,500 @@
+// C ABI (include/ruv.h): the drop-in for the reference's GpuSolver boundary
+// (gpu/src/solver.rs:104-565) and the batched unfold_chart solve (unwrap/src/lscm.rs:471-727).
+// Every entry point catches internally and reports a ruv_status; no exception crosses.
+#include <cstring>
+#include <memory>
+#include <new>
+
+#include "system.cuh"
+
+using namespace ruv;
+
+struct ruv_ctx {
+  Ctx c;
+};
+
+struct ruv_prepared {
+  Prepared p;
+};
+
+namespace {
+
+ruv_status fail(ruv_ctx* ctx, ruv_status s, const std::string& msg) {
+  if (ctx) ctx->c.last_error = msg;
+  return s;
+}
+
+template <class F>
+ruv_status guarded(ruv_ctx* ctx, F&& body) {
+  struct CounterScope {
+    explicit CounterScope(ruv_ctx* c) { g_launch_counter = c ? &c->c.launches : nullptr; }
+    ~CounterScope() { g_launch_counter = nullptr; }
+  } scope(ctx);
+  try {
+    if (ctx) {
+      ctx->c.last_error.clear();
+      cudaError_t e = cudaSetDevice(ctx->c.device);
+      if (e != cudaSuccess) return fail(ctx, RUV_ERR_NO_DEVICE, cudaGetErrorString(e));
+    }
+    return body();
+  } catch (const Error& e) {
+    if (ctx) cudaStreamSynchronize(ctx->c.stream);
+    cudaGetLastError();
+    return fail(ctx, e.status, e.msg);
+  } catch (const std::bad_alloc&) {
+    return fail(ctx, RUV_ERR_OOM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(ctx, RUV_ERR_INTERNAL, e.what());
+  } catch (...) {
+    return fail(ctx, RUV_ERR_INTERNAL, "unknown error");
+  }
+}
+
+template <class T>
+T* upload(Ctx& c, const std::string& name, const T* host, int64_t n) {
+  T* d = c.ws.get<T>(name, n);
+  if (n > 0) RUV_CUDA(cudaMemcpyAsync(d, host, sizeof(T) * n, cudaMemcpyHostToDevice, c.stream));
+  return d;
+}
+
+int worst(int a, int b) {
+  // NOT_CONVERGED < BREAKDOWN in severity; any non-OK beats OK
+  if (a == RUV_OK) return b;
+  if (b == RUV_OK) return a;
+  return a > b ? a : b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t ruv_abi_version(void) { return RUV_ABI_VERSION; }
+
+const char* ruv_status_str(ruv_status s) {
+  switch (s) {
+    case RUV_OK: return "ok";
+    case RUV_ERR_NO_DEVICE: return "no usable CUDA device";
+    case RUV_ERR_BAD_INPUT: return "bad input";
+    case RUV_ERR_OOM: return "out of device memory";
+    case RUV_ERR_NOT_CONVERGED: return "not converged";
+    case RUV_ERR_BREAKDOWN: return "breakdown";
+    case RUV_ERR_TIMEOUT: return "device wait timed out";
+    case RUV_ERR_LAUNCH: return "CUDA launch/runtime failure";
+    default: return "internal error";
+  }
+}
+
+ruv_status ruv_ctx_create(ruv_ctx** out, int32_t device) {
+  if (!out) return RUV_ERR_BAD_INPUT;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return RUV_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return RUV_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return RUV_ERR_NO_DEVICE;
+  // the kernels are built for sm_103a only
+  if (!(prop.major == 10 && prop.minor == 3)) return RUV_ERR_NO_DEVICE;
+  std::unique_ptr<ruv_ctx> ctx(new (std::nothrow) ruv_ctx());
+  if (!ctx) return RUV_ERR_OOM;
+  ctx->c.device = device;
+  ctx->c.sm_count = prop.multiProcessorCount;
+  if (cudaSetDevice(device) != cudaSuccess) return RUV_ERR_NO_DEVICE;
+  if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) return RUV_ERR_LAUNCH;
+  *out = ctx.release();
+  return RUV_OK;
+}
+
+void ruv_ctx_destroy(ruv_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->c.device);
+  cudaStreamSynchronize(ctx->c.stream);
+  ctx->c.ws.release();
+  cudaStreamDestroy(ctx->c.stream);
+  delete ctx;
+}
+
+const char* ruv_last_error(const ruv_ctx* ctx) { return ctx ? ctx->c.last_error.c_str() : ""; }
+
+void ruv_unfold_opts_default(ruv_unfold_opts* o) {
+  if (!o) return;
+  o->angle_mix = 1.0;
+  o->mix_w = 1.0;
+  o->max_iter = 100;
+  o->precond = RUV_PRECOND_JACOBI;
+  o->precision = RUV_PREC_MIXED;
+  o->tol = 1e-12;
+  o->max_cg_iter = 1024 * 16;
+}
+
+ruv_status ruv_cg_solve(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                        const double* b, double* x_out, int64_t max_iter, double tol, ruv_precond pc,
+                        int64_t* iters_out) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    // solver.rs:296-299: a malformed system is rejected
+    if (n <= 0 || !row_ptr || !cols || !vals || !b || !x_out) return fail(ctx, RUV_ERR_BAD_INPUT, "empty system or null buffer");
+    if (row_ptr[0] != 0) return fail(ctx, RUV_ERR_BAD_INPUT, "row_ptr[0] != 0");
+    for (int32_t i = 0; i < n; ++i)
+      if (row_ptr[i + 1] < row_ptr[i]) return fail(ctx, RUV_ERR_BAD_INPUT, "row_ptr not monotone");
+    const int64_t nnz = row_ptr[n];
+    std::vector<double> diag(n, 0.0);
+    for (int32_t i = 0; i < n; ++i) {
+      bool found = false;
+      for (int32_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+        if (cols[k] < 0 || cols[k] >= n) return fail(ctx, RUV_ERR_BAD_INPUT, "column index out of range");
+        if (cols[k] == i && !found) {  // CsrMatrix::row_get returns the first match
+          diag[i] = vals[k];
+          found = true;
+        }
+      }
+    }
+    if (pc == RUV_PRECOND_JACOBI)
+      for (int32_t i = 0; i < n; ++i)
+        if (std::fabs(diag[i]) < 1e-300) return fail(ctx, RUV_ERR_BAD_INPUT, "Jacobi: zero diagonal");
+    if (pc != RUV_PRECOND_NONE && pc != RUV_PRECOND_JACOBI)
+      return fail(ctx, RUV_ERR_BAD_INPUT, "preconditioner not available in this build");
+    Ctx& c = ctx->c;
+    DevSystem sys;
+    sys.n_charts = 1;
+    sys.n_rows = n;
+    sys.nnz = nnz;
+    sys.nrhs = 1;
+    sys.h_chart_row = {0, (int64_t)n};
+    sys.chart_row = upload(c, "cg.chart_row", sys.h_chart_row.data(), 2);
+    sys.row_ptr = upload(c, "cg.row_ptr", row_ptr, (int64_t)n + 1);
+    sys.cols = upload(c, "cg.cols", cols, nnz);
+    sys.vals = upload(c, "cg.vals", vals, nnz);
+    std::vector<float> v32(vals, vals + nnz);
+    sys.vals32 = upload(c, "cg.vals32", v32.data(), nnz);
+    sys.diag = upload(c, "cg.diag", diag.data(), n);
+    sys.b = upload(c, "cg.b", b, n);
+    double* x = c.ws.get<double>("cg.x", n);
+    SolveOpts o;
+    o.precond = pc;
+    o.precision = RUV_PREC_FP64;
+    o.tol = tol;
+    o.max_iter = max_iter;
+    auto res = pcg_solve(c, sys, x, o);
+    if (iters_out) *iters_out = res[0].iters;
+    if (res[0].status != RUV_OK) return fail(ctx, (ruv_status)res[0].status, "CG did not converge / broke down");
+    RUV_CUDA(cudaMemcpyAsync(x_out, x, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+    RUV_CUDA(cudaStreamSynchronize(c.stream));
+    for (int32_t i = 0; i < n; ++i)
+      if (!std::isfinite(x_out[i])) return fail(ctx, RUV_ERR_BREAKDOWN, "non-finite solution");  // solver.rs:561-563
+    return RUV_OK;
+  });
+}
+
+ruv_status ruv_apply_ic0(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                         const double* r, double* z_out) {
+  (void)n;
+  (void)row_ptr;
+  (void)cols;
+  (void)vals;
+  (void)r;
+  (void)z_out;
+  return fail(ctx, RUV_ERR_BAD_INPUT, "IC(0) is not available in this build");
+}
+
+ruv_status ruv_lscm_upload(ruv_ctx* ctx, const ruv_lscm_batch* in) {
+  if (!ctx || !in) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    const int64_t NC = in->n_charts;
+    if (NC < 0 || !in->vert_off || !in->tri_off) return fail(ctx, RUV_ERR_BAD_INPUT, "null offsets");
+    if (in->vert_off[0] != 0 || in->tri_off[0] != 0) return fail(ctx, RUV_ERR_BAD_INPUT, "offsets must start at 0");
+    for (int64_t c = 0; c < NC; ++c)
+      if (in->vert_off[c + 1] < in->vert_off[c] || in->tri_off[c + 1] < in->tri_off[c])
+        return fail(ctx, RUV_ERR_BAD_INPUT, "offsets must be non-decreasing");
+    const int64_t NV = in->vert_off[NC], NT = in->tri_off[NC];
+    if ((NV > 0 && (!in->p3 || !in->pinned || !in->pin_uv || !in->p2)) || (NT > 0 && !in->tris))
+      return fail(ctx, RUV_ERR_BAD_INPUT, "null array");
+    Ctx& c = ctx->c;
+    c.have_batch = false;
+    c.have_uv = false;
+    DevBatch& bt = c.resident;
+    bt = DevBatch();
+    bt.n_charts = NC;
+    bt.n_verts = NV;
+    bt.n_tris = NT;
+    bt.h_vert_off.assign(in->vert_off, in->vert_off + NC + 1);
+    bt.vert_off = upload(c, "in.vert_off", in->vert_off, NC + 1);
+    bt.tri_off = upload(c, "in.tri_off", in->tri_off, NC + 1);
+    bt.p3 = upload(c, "in.p3", in->p3, 3 * NV);
+    bt.tris = upload(c, "in.tris", in->tris, 3 * NT);
+    bt.pinned = upload(c, "in.pinned", in->pinned, NV);
+    bt.pin_uv = upload(c, "in.pin_uv", in->pin_uv, 2 * NV);
+    bt.p2 = upload(c, "in.p2", in->p2, 2 * NV);
+    c.have_batch = true;
+    return RUV_OK;
+  });
+}
+
+ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ruv_chart_stat* stats) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    if (!c.have_batch) return fail(ctx, RUV_ERR_BAD_INPUT, "no batch uploaded on this context");
+    ruv_unfold_opts o;
+    ruv_unfold_opts_default(&o);
+    if (opts) o = *opts;
+    if (!(o.mix_w > 0.0)) return fail(ctx, RUV_ERR_BAD_INPUT, "mix_w must be > 0 (lscm.rs:479)");
+    if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI)
+      return fail(ctx, RUV_ERR_BAD_INPUT, "preconditioner not available in this build");
+    DevBatch& bt = c.resident;
+    const int64_t NC = bt.n_charts, NV = bt.n_verts;
+    if (NC == 0) {
+      c.have_uv = true;
+      c.timings[0] = c.timings[1] = c.timings[2] = 0.0;
+      return RUV_OK;
+    }
+    cudaEvent_t ev[4];
+    for (auto& e : ev) RUV_CUDA(cudaEventCreate(&e));
+    struct EvGuard {
+      cudaEvent_t* e;
+      ~EvGuard() {
+        for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]);
+      }
+    } guard{ev};
+    DevSystem& sys = c.last_sys;
+    c.have_last = false;
+    c.have_uv = false;
+    RUV_CUDA(cudaEventRecord(ev[0], c.stream));
+    assemble_lscm(c, bt, sys, o.angle_mix);
+    c.have_last = true;
+    RUV_CUDA(cudaEventRecord(ev[1], c.stream));
+    double* x = c.ws.get<double>("lscm.x", 2 * sys.n_rows);
+    SolveOpts so;
+    so.precond = o.precond;
+    so.precision = o.precision;
+    so.tol = o.tol;
+    so.max_iter = o.max_cg_iter > 0 ? o.max_cg_iter : 16384;
+    auto res = pcg_solve(c, sys, x, so);
+    RUV_CUDA(cudaEventRecord(ev[2], c.stream));
+    double* uv = c.ws.get<double>("lscm.uv", 2 * NV);
+    std::vector<int32_t> iters;
+    std::vector<double> err_accum;
+    driver_update(c, bt, sys, x, o.max_iter, uv, iters, err_accum);
+    RUV_CUDA(cudaEventRecord(ev[3], c.stream));
+    RUV_CUDA(cudaEventSynchronize(ev[3]));
+    for (int k = 0; k < 3; ++k) {
+      float ms = 0.f;
+      RUV_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+      c.timings[k] = ms;
+    }
+    c.have_uv = true;
+    int w = RUV_OK;
+    for (int64_t k = 0; k < NC; ++k) {
+      w = worst(w, res[k].status);
+      if (stats) {
+        stats[k].status = res[k].status;
+        stats[k].driver_iters = iters[k];
+        stats[k].cg_iters = res[k].iters;
+        stats[k].n_free = (int32_t)(sys.h_chart_row[k + 1] - sys.h_chart_row[k]);
+        stats[k].rel_res = res[k].rel_res;
+        stats[k].err_accum = err_accum[k];
+      }
+    }
+    if (w != RUV_OK) return fail(ctx, (ruv_status)w, "at least one chart did not converge");
+    return RUV_OK;
+  });
+}
+
+ruv_status ruv_lscm_download_uv(ruv_ctx* ctx, double* uv_out) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    if (!c.have_uv) return fail(ctx, RUV_ERR_BAD_INPUT, "no solved batch on this context");
+    const int64_t NV = c.resident.n_verts;
+    if (NV > 0 && !uv_out) return fail(ctx, RUV_ERR_BAD_INPUT, "null uv_out");
+    double* uv = c.ws.get<double>("lscm.uv", 2 * NV);
+    if (NV > 0) RUV_CUDA(cudaMemcpyAsync(uv_out, uv, sizeof(double) * 2 * NV, cudaMemcpyDeviceToHost, c.stream));
+    RUV_CUDA(cudaStreamSynchronize(c.stream));
+    return RUV_OK;
+  });
+}
+
+ruv_status ruv_lscm_solve_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, const ruv_unfold_opts* opts, double* uv_out,
+                                ruv_chart_stat* stats) {
+  ruv_status s = ruv_lscm_upload(ctx, in);
+  if (s != RUV_OK) return s;
+  if (in->vert_off[in->n_charts] > 0 && !uv_out) return fail(ctx, RUV_ERR_BAD_INPUT, "null uv_out");
+  ruv_status solved = ruv_lscm_solve_resident(ctx, opts, stats);
+  if (solved != RUV_OK && solved != RUV_ERR_NOT_CONVERGED && solved != RUV_ERR_BREAKDOWN) return solved;
+  std::string msg = ctx->c.last_error;
+  if (!ctx->c.have_uv) return solved;
+  s = ruv_lscm_download_uv(ctx, uv_out);
+  if (s != RUV_OK) return s;
+  ctx->c.last_error = msg;
+  return solved;
+}
+
+int64_t ruv_kernel_launches(const ruv_ctx* ctx) { return ctx ? ctx->c.launches : 0; }
+
+int32_t ruv_last_timings(const ruv_ctx* ctx, double* ms, int32_t n) {
+  if (!ctx || !ms) return 0;
+  int32_t k = n < 3 ? n : 3;
+  for (int32_t i = 0; i < k; ++i) ms[i] = ctx->c.timings[i];
+  return k;
+}
+
+ruv_status ruv_bench_spmv(ruv_ctx* ctx, ruv_precision precision, int32_t reps, int32_t n_buffers, double* ms_per_launch,
+                          double* bytes_per_launch) {
+  if (!ctx || reps <= 0 || n_buffers <= 0) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    if (!c.have_last) return fail(ctx, RUV_ERR_BAD_INPUT, "no assembled batch on this context");
+    double bytes = 0.0;
+    double ms = bench_spmv(c, c.last_sys, precision == RUV_PREC_MIXED, reps, n_buffers, &bytes);
+    if (ms_per_launch) *ms_per_launch = ms;
+    if (bytes_per_launch) *bytes_per_launch = bytes;
+    return RUV_OK;
+  });
+}
+
+ruv_status ruv_export_chart_system(ruv_ctx* ctx, int64_t chart, int64_t* nf_out, int64_t* nnz_out, int32_t* row_ptr,
+                                   int32_t* cols, double* vals, double* rhs) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    if (!c.have_last) return fail(ctx, RUV_ERR_BAD_INPUT, "no assembled batch on this context");
+    DevSystem& sys = c.last_sys;
+    if (chart < 0 || chart >= sys.n_charts) return fail(ctx, RUV_ERR_BAD_INPUT, "chart out of range");
+    const int64_t r0 = sys.h_chart_row[chart], r1 = sys.h_chart_row[chart + 1], nf = r1 - r0;
+    std::vector<int32_t> rp(nf + 1);
+    RUV_CUDA(cudaMemcpyAsync(rp.data(), sys.row_ptr + r0, sizeof(int32_t) * (nf + 1), cudaMemcpyDeviceToHost, c.stream));
+    RUV_CUDA(cudaStreamSynchronize(c.stream));
+    const int64_t e0 = rp[0], ne = rp[nf] - rp[0];
+    if (nf_out) *nf_out = nf;
+    if (nnz_out) *nnz_out = 2 * ne;
+    if (!row_ptr && !cols && !vals && !rhs) return RUV_OK;
+    std::vector<int32_t> sc(ne);
+    std::vector<double> sv(ne), sb(2 * nf);
+    if (ne > 0) {
+      RUV_CUDA(cudaMemcpyAsync(sc.data(), sys.cols + e0, sizeof(int32_t) * ne, cudaMemcpyDeviceToHost, c.stream));
+      RUV_CUDA(cudaMemcpyAsync(sv.data(), sys.vals + e0, sizeof(double) * ne, cudaMemcpyDeviceToHost, c.stream));
+    }
+    if (nf > 0)
+      RUV_CUDA(cudaMemcpyAsync(sb.data(), sys.b + 2 * r0, sizeof(double) * 2 * nf, cudaMemcpyDeviceToHost, c.stream));
+    RUV_CUDA(cudaStreamSynchronize(c.stream));
+    // A = L (x) I2: scalar row r -> interleaved rows 2r (u) and 2r + 1 (v)
+    int64_t at = 0;
+    if (row_ptr) row_ptr[0] = 0;
+    for (int64_t r = 0; r < nf; ++r)
+      for (int comp = 0; comp < 2; ++comp) {
+        for (int64_t k = rp[r] - e0; k < rp[r + 1] - e0; ++k) {
+          if (cols) cols[at] = (int32_t)(2 * (sc[k] - r0) + comp);
+          if (vals) vals[at] = sv[k];
+          ++at;
+        }
+        if (row_ptr) row_ptr[2 * r + comp + 1] = (int32_t)at;
+      }
+    if (rhs)
+      for (int64_t i = 0; i < 2 * nf; ++i) rhs[i] = sb[i];
+    return RUV_OK;
+  });
+}
+
+// ------------------------------------------------------------------ host chart stages
+ruv_status ruv_prepare_mesh(const double* pos, int64_t n_verts, const int32_t* faces, int64_t n_faces, double weld_tol,
+                            double angle_min_deg, int32_t threads, ruv_prepared** out) {
+  if (!out || n_verts < 0 || n_faces < 0 || (n_verts > 0 && !pos) || (n_faces > 0 && !faces)) return RUV_ERR_BAD_INPUT;
+  if (n_verts >= (int64_t)INT32_MAX) return RUV_ERR_BAD_INPUT;
+  *out = nullptr;
+  try {
+    std::unique_ptr<ruv_prepared> p(new ruv_prepared());
+    std::string err;
+    ruv_status s = prepare_mesh(pos, n_verts, faces, n_faces, weld_tol, angle_min_deg, threads, p->p, err);
+    if (s != RUV_OK) return s;
+    *out = p.release();
+    return RUV_OK;
+  } catch (const std::bad_alloc&) {
+    return RUV_ERR_OOM;
+  } catch (...) {
+    return RUV_ERR_INTERNAL;
+  }
+}
+
+ruv_status ruv_prepare_patches(int64_t n_patches, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
+                               const int32_t* tris, int32_t threads, ruv_prepared** out) {
+  if (!out || n_patches < 0 || !vert_off || !tri_off) return RUV_ERR_BAD_INPUT;
+  if ((vert_off[n_patches] > 0 && !p3) || (tri_off[n_patches] > 0 && !tris)) return RUV_ERR_BAD_INPUT;
+  if (vert_off[n_patches] >= (int64_t)INT32_MAX) return RUV_ERR_BAD_INPUT;
+  *out = nullptr;
+  try {
+    std::unique_ptr<ruv_prepared> p(new ruv_prepared());
+    std::string err;
+    ruv_status s = prepare_patches(n_patches, vert_off, tri_off, p3, tris, threads, p->p, err);
+    if (s != RUV_OK) return s;
+    *out = p.release();
+    return RUV_OK;
+  } catch (const std::bad_alloc&) {
+    return RUV_ERR_OOM;
+  } catch (...) {
+    return RUV_ERR_INTERNAL;
+  }
+}
+
+void ruv_prepared_free(ruv_prepared* p) { delete p; }
+
+ruv_status ruv_prepared_batch(const ruv_prepared* p, ruv_lscm_batch* v) {
+  if (!p || !v) return RUV_ERR_BAD_INPUT;
+  const Prepared& P = p->p;
+  v->n_charts = (int64_t)P.vert_off.size() - 1;
+  v->vert_off = P.vert_off.data();
+  v->tri_off = P.tri_off.data();
+  v->p3 = P.p3.data();
+  v->tris = P.tris.data();
+  v->pinned = P.pinned.data();
+  v->pin_uv = P.pin_uv.data();
+  v->p2 = P.p2.data();
+  return RUV_OK;
+}
+
+int64_t ruv_prepared_get_i64(const ruv_prepared* p, const char* what, int64_t* out) {
+  if (!p || !what) return -1;
+  const Prepared& P = p->p;
+  std::string w(what);
+  auto emit = [&](const auto& vec) -> int64_t {
+    if (out)
+      for (size_t i = 0; i < vec.size(); ++i) out[i] = (int64_t)vec[i];
+    return (int64_t)vec.size();
+  };
+  if (w == "chart.vert_off") return emit(P.vert_off);
+  if (w == "chart.tri_off") return emit(P.tri_off);
+  if (w == "chart.vertex_ids") return emit(P.vertex_ids);
+  if (w == "chart.face_ids") return emit(P.face_ids);
+  if (w == "chart.tris") return emit(P.tris);
+  if (w == "chart.border_off") return emit(P.border_off);
+  if (w == "chart.border") return emit(P.border);
+  if (w == "chart.loop_off") return emit(P.loop_off);
+  if (w == "chart.loop_seg") return emit(P.loop_seg);
+  if (w == "chart.loop_ids") return emit(P.loop_ids);
+  if (w == "chart.pinned") return emit(P.pinned);
+  if (w == "mesh.faces") return emit(P.mesh_faces);
+  if (w == "mesh.n_cut_slots") {
+    if (out) out[0] = P.n_cut_slots;
+    return 1;
+  }
+  return -1;
+}
+
+int64_t ruv_prepared_get_f64(const ruv_prepared* p, const char* what, double* out) {
+  if (!p || !what) return -1;
+  const Prepared& P = p->p;
+  std::string w(what);
+  auto emit = [&](const std::vector<double>& vec) -> int64_t {
+    if (out && !vec.empty()) std::memcpy(out, vec.data(), sizeof(double) * vec.size());
+    return (int64_t)vec.size();
+  };
+  if (w == "chart.area3d") return emit(P.area3d);
+  if (w == "mesh.pos") return emit(P.mesh_pos);
+  if (w == "chart.pin_uv") return emit(P.pin_uv);
+  if (w == "chart.p2") return emit(P.p2);
+  if (w == "chart.p3") return emit(P.p3);
+  return -1;
+}
+
+}  // extern "C"

@@ -1,0 +1,537 @@
+// GPU assembly of the per-chart LSCM systems with the pins eliminated, and the damped
+// driver update — unfold_chart's numeric core (unwrap/src/lscm.rs:252-274 edge_weights,
+// :594-676 assembly, :686-719 driver), for every chart of a batch at once.
+//
+// Layout: vertices and triangles of all charts are packed chart after chart.  A row is a
+// free vertex; rows are numbered by an exclusive scan of the free flags, so each chart's
+// rows are contiguous and ascend with the chart-local vertex id, exactly like the
+// reference's free_pos map (lscm.rs:582-592).
+//
+// Bit-exactness: every floating operation uses the explicit round-to-nearest intrinsics
+// (__dadd_rn, __dmul_rn, __ddiv_rn, __dsqrt_rn: never contracted into FMAs) in the
+// reference's evaluation order, and every sum runs in the reference's order (edge weight:
+// triangle order; diagonal and right-hand side: ascending neighbour id), so the CSR
+// pattern, values and right-hand side are bit-identical to the reference's
+// Sparse::to_csr(2 nf) (sparse.rs:69-84) of the same chart.
+#include "system.cuh"
+
+namespace ruv {
+namespace {
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+struct P3 {
+  double x, y, z;
+};
+__device__ __forceinline__ P3 ld3(const double* p, int64_t i) { return {p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
+__device__ __forceinline__ P3 psub(P3 a, P3 b) { return {dsub(a.x, b.x), dsub(a.y, b.y), dsub(a.z, b.z)}; }
+__device__ __forceinline__ double pdot(P3 a, P3 b) { return dadd(dadd(dmul(a.x, b.x), dmul(a.y, b.y)), dmul(a.z, b.z)); }
+__device__ __forceinline__ P3 pcross(P3 a, P3 b) {
+  return {dsub(dmul(a.y, b.z), dmul(a.z, b.y)), dsub(dmul(a.z, b.x), dmul(a.x, b.z)), dsub(dmul(a.x, b.y), dmul(a.y, b.x))};
+}
+__device__ __forceinline__ double plen(P3 a) { return __dsqrt_rn(pdot(a, a)); }
+__device__ __forceinline__ double rs_max(double a, double b) {  // Rust f64::max
+  if (a != a) return b;
+  if (b != b) return a;
+  return a > b ? a : b;
+}
+
+__device__ __forceinline__ int64_t find_chart(const int64_t* off, int64_t n_charts, int64_t i) {
+  int64_t lo = 0, hi = n_charts;  // largest c with off[c] <= i
+  while (hi - lo > 1) {
+    int64_t mid = (lo + hi) >> 1;
+    if (off[mid] <= i) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// chart-local triangle indices -> packed vertex ids (validated)
+__global__ void k_globalize(const int32_t* __restrict__ tris, const int64_t* __restrict__ tri_off,
+                            const int64_t* __restrict__ vert_off, int64_t n_charts, int64_t n_tris,
+                            int32_t* __restrict__ tri_g, int* __restrict__ bad) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tris) return;
+  int64_t c = find_chart(tri_off, n_charts, t);
+  int64_t v0 = vert_off[c], nv = vert_off[c + 1] - v0;
+  int32_t a = tris[3 * t], b = tris[3 * t + 1], d = tris[3 * t + 2];
+  if (a < 0 || b < 0 || d < 0 || a >= nv || b >= nv || d >= nv || a == b || b == d || a == d) {
+    atomicExch(bad, 1);
+    a = b = d = 0;
+  }
+  tri_g[3 * t] = (int32_t)(v0 + a);
+  tri_g[3 * t + 1] = (int32_t)(v0 + b);
+  tri_g[3 * t + 2] = (int32_t)(v0 + d);
+}
+
+// Clamped cotangent at each triangle corner m (angle at t[m], opposite edge t[m+1]-t[m+2]),
+// lscm.rs:256-268; 0.0 where the reference skips the corner (degenerate guard).
+__global__ void k_corner_cot(const double* __restrict__ p3, const int32_t* __restrict__ tri_g, int64_t n_tris,
+                             double* __restrict__ cot) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tris) return;
+  int32_t v[3] = {tri_g[3 * t], tri_g[3 * t + 1], tri_g[3 * t + 2]};
+  P3 p[3] = {ld3(p3, v[0]), ld3(p3, v[1]), ld3(p3, v[2])};
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    P3 a1 = psub(p[(m + 2) % 3], p[m]);  // e1 - o
+    P3 a2 = psub(p[(m + 1) % 3], p[m]);  // e0 - o
+    double la = plen(a1), lb = plen(a2);
+    double c = 0.0;
+    if (!(la <= kEpsDegenerate || lb <= kEpsDegenerate)) {
+      double lab = dmul(la, lb);
+      double s = ddiv(plen(pcross(a1, a2)), lab);
+      if (!(s <= kEpsDegenerate)) c = rs_max(ddiv(ddiv(pdot(a1, a2), lab), s), 0.0);
+    }
+    cot[3 * t + m] = c;
+  }
+}
+
+__global__ void k_free_flags(const uint8_t* __restrict__ pinned, int64_t n, uint8_t* __restrict__ fr) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) fr[i] = pinned[i] ? 0 : 1;
+}
+
+__global__ void k_chart_rows(const int64_t* __restrict__ vert_off, const int64_t* __restrict__ row_of,
+                             int64_t n_charts, int64_t* __restrict__ chart_row) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c <= n_charts) chart_row[c] = row_of[vert_off[c]];
+}
+
+// Two incidence records per (triangle, corner) for free vertices: (neighbour, corner index
+// of the cotangent opposite that edge).
+__global__ void k_count_records(const int32_t* __restrict__ tri_g, const uint8_t* __restrict__ pinned,
+                                int64_t n_tris, int32_t* __restrict__ deg) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tris) return;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int32_t v = tri_g[3 * t + m];
+    if (!pinned[v]) atomicAdd(&deg[v], 2);
+  }
+}
+
+__global__ void k_scatter_records(const int32_t* __restrict__ tri_g, const uint8_t* __restrict__ pinned,
+                                  int64_t n_tris, const int64_t* __restrict__ rec_off, int32_t* __restrict__ cursor,
+                                  int2* __restrict__ rec) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tris) return;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int32_t v = tri_g[3 * t + m];
+    if (pinned[v]) continue;
+    int64_t at = rec_off[v] + atomicAdd(&cursor[v], 2);
+    rec[at] = make_int2(tri_g[3 * t + (m + 1) % 3], (int32_t)(3 * t + (m + 2) % 3));
+    rec[at + 1] = make_int2(tri_g[3 * t + (m + 2) % 3], (int32_t)(3 * t + (m + 1) % 3));
+  }
+}
+
+__device__ __forceinline__ bool rec_less(int2 a, int2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
+
+// One row (free vertex v).  MODE 0: sort the bucket and count entries; MODE 1: fill.
+template <int MODE>
+__global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, const int64_t* __restrict__ row_of,
+                       const int64_t* __restrict__ rec_off, int2* __restrict__ rec, const double* __restrict__ cot,
+                       const double* __restrict__ p3, const double* __restrict__ p2, const double* __restrict__ pin_uv,
+                       double mix_b, int32_t* __restrict__ row_len, const int64_t* __restrict__ row_ptr,
+                       int32_t* __restrict__ cols, double* __restrict__ vals, float* __restrict__ vals32,
+                       double* __restrict__ diag_out, double* __restrict__ b, int32_t* __restrict__ row_vert) {
+  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n_verts || pinned[v]) return;
+  const int64_t r0 = rec_off[v], r1 = rec_off[v + 1];
+  if (MODE == 0) {  // insertion sort by (neighbour, corner) — buckets hold ~2x valence records
+    for (int64_t i = r0 + 1; i < r1; ++i) {
+      int2 key = rec[i];
+      int64_t j = i - 1;
+      while (j >= r0 && rec_less(key, rec[j])) {
+        rec[j + 1] = rec[j];
+        --j;
+      }
+      rec[j + 1] = key;
+    }
+  }
+  const P3 pv = ld3(p3, v);
+  const int64_t row = row_of[v];
+  // pass A: diagonal (sum of c over kept edges, ascending neighbour) and entry count
+  double dg = 0.0;
+  bool has_diag = false;
+  int32_t n_off = 0;
+  for (int64_t i = r0; i < r1;) {
+    int32_t nb = rec[i].x;
+    double w = 0.0;
+    int64_t j = i;
+    for (; j < r1 && rec[j].x == nb; ++j) w = dadd(w, cot[rec[j].y]);
+    i = j;
+    if (w <= kEpsDegenerate) continue;  // lscm.rs:606
+    P3 d3 = psub(ld3(p3, nb), pv);
+    double c = ddiv(w, rs_max(pdot(d3, d3), kEpsDegenerate));
+    if (c != 0.0) {  // Sparse::add skips zeros (sparse.rs:47-52)
+      dg = dadd(dg, c);
+      has_diag = true;
+      if (!pinned[nb]) ++n_off;
+    }
+  }
+  if (MODE == 0) {
+    row_len[row] = n_off + (has_diag ? 1 : 0);
+    return;
+  }
+  // pass B: entries in column order (diagonal between the lower and upper neighbours) and
+  // the right-hand side (pinned neighbours eliminated; mix_b pull term, lscm.rs:630-638)
+  int64_t at = row_ptr[row];
+  bool diag_done = !has_diag;
+  double bu = 0.0, bv = 0.0;
+  const double p2u = p2[2 * v], p2v = p2[2 * v + 1];
+  for (int64_t i = r0; i < r1;) {
+    int32_t nb = rec[i].x;
+    double w = 0.0;
+    int64_t j = i;
+    for (; j < r1 && rec[j].x == nb; ++j) w = dadd(w, cot[rec[j].y]);
+    i = j;
+    if (w <= kEpsDegenerate) continue;
+    P3 d3 = psub(ld3(p3, nb), pv);
+    double c = ddiv(w, rs_max(pdot(d3, d3), kEpsDegenerate));
+    // dv as the reference forms it: d = p2[hi] - p2[lo], negated for the higher endpoint
+    double du, dw;
+    if (v < nb) {
+      du = dsub(p2[2 * nb], p2u);
+      dw = dsub(p2[2 * nb + 1], p2v);
+    } else {
+      du = -dsub(p2u, p2[2 * nb]);
+      dw = -dsub(p2v, p2[2 * nb + 1]);
+    }
+    double mc = dmul(mix_b, c);
+    if (!pinned[nb]) {
+      bu = dadd(bu, dmul(mc, du));
+      bv = dadd(bv, dmul(mc, dw));
+      if (c != 0.0) {
+        if (!diag_done && nb > v) {
+          cols[at] = (int32_t)row;
+          vals[at] = dg;
+          vals32[at] = (float)dg;
+          ++at;
+          diag_done = true;
+        }
+        cols[at] = (int32_t)row_of[nb];
+        vals[at] = -c;
+        vals32[at] = (float)(-c);
+        ++at;
+      }
+    } else {
+      bu = dadd(bu, dadd(dmul(mc, du), dmul(c, pin_uv[2 * nb])));
+      bv = dadd(bv, dadd(dmul(mc, dw), dmul(c, pin_uv[2 * nb + 1])));
+    }
+  }
+  if (!diag_done) {
+    cols[at] = (int32_t)row;
+    vals[at] = dg;
+    vals32[at] = (float)dg;
+  }
+  diag_out[row] = dg;
+  b[2 * row] = bu;
+  b[2 * row + 1] = bv;
+  row_vert[row] = (int32_t)v;
+}
+
+__global__ void k_i64_to_i32(const int64_t* __restrict__ a, int64_t n, int32_t* __restrict__ o) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) o[i] = (int32_t)a[i];
+}
+
+// ---------------------------------------------------------------- driver (lscm.rs:570-719)
+struct DriverState {
+  double step, prev_err, err_accum;
+  int32_t iters, active, broke;
+};
+
+__global__ void k_driver_init(const double* __restrict__ p2, int64_t n, double* __restrict__ uv) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 2 * n) uv[i] = p2[i];
+}
+
+__global__ void k_driver_state_init(DriverState* st, int64_t n_charts) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n_charts) st[c] = DriverState{1.0, __longlong_as_double(0x7ff0000000000000ll), 1.0, 0, 1, 0};
+}
+
+__device__ __forceinline__ void new_uv_of(int64_t v, const uint8_t* pinned, const double* pin_uv, const int64_t* row_of,
+                                          const double* x, double& u, double& w) {
+  if (pinned[v]) {
+    u = pin_uv[2 * v];
+    w = pin_uv[2 * v + 1];
+  } else {
+    int64_t r = row_of[v];
+    u = x[2 * r];
+    w = x[2 * r + 1];
+  }
+}
+
+// per vertex-tile partial sums of |new_uv - uv|^2 and |uv|^2 for active charts
+__global__ void k_driver_partials(const int64_t* __restrict__ tile_beg, const int32_t* __restrict__ tile_chart,
+                                  int64_t n_tiles, const DriverState* __restrict__ st, const uint8_t* __restrict__ pinned,
+                                  const double* __restrict__ pin_uv, const int64_t* __restrict__ row_of,
+                                  const double* __restrict__ x, const double* __restrict__ uv,
+                                  double* __restrict__ part) {
+  __shared__ double sh[64];
+  int64_t t = blockIdx.x;
+  int c = tile_chart[t];
+  if (!st[c].active) return;
+  double s[2] = {0.0, 0.0};
+  for (int64_t v = tile_beg[2 * t] + threadIdx.x; v < tile_beg[2 * t + 1]; v += blockDim.x) {
+    double nu, nw;
+    new_uv_of(v, pinned, pin_uv, row_of, x, nu, nw);
+    double du = nu - uv[2 * v], dw = nw - uv[2 * v + 1];
+    s[0] += du * du + dw * dw;
+    s[1] += uv[2 * v] * uv[2 * v] + uv[2 * v + 1] * uv[2 * v + 1];
+  }
+  block_sum<2>(s, sh);
+  if (threadIdx.x == 0) {
+    part[2 * t] = s[0];
+    part[2 * t + 1] = s[1];
+  }
+}
+
+__global__ void k_driver_decide(const int64_t* __restrict__ chart_tile, int64_t n_charts, DriverState* __restrict__ st,
+                                const double* __restrict__ part, int it, int max_iter, int* __restrict__ n_active) {
+  __shared__ double sh[64];
+  int64_t c = blockIdx.x;
+  if (!st[c].active) return;
+  double s[2] = {0.0, 0.0};
+  for (int64_t t = chart_tile[c] + threadIdx.x; t < chart_tile[c + 1]; t += blockDim.x) {
+    s[0] += part[2 * t];
+    s[1] += part[2 * t + 1];
+  }
+  block_sum<2>(s, sh);
+  if (threadIdx.x != 0) return;
+  DriverState d = st[c];
+  d.iters = it + 1;
+  double err = sqrt(s[0]) / rs_max(sqrt(s[1]), 1e-30);
+  double applied = err * d.step;
+  if (d.prev_err > 1e-30 && err > 2.0 * d.prev_err)
+    d.step = rs_max(d.step * 0.5, 0.05);
+  else if (it > 3)
+    d.step = fmin(d.step * 1.2, 1.0);
+  if (applied < 1e-8 || (d.prev_err > 1e-30 && it != 0 && applied / d.prev_err <= 0.01)) {
+    d.active = 0;  // converged / stagnation: uv stays as is
+    d.broke = 1;
+  } else {
+    d.prev_err = applied;
+    d.err_accum += err;
+    if (max_iter * 10 < it || it + 1 >= max_iter) d.active = 2;  // apply this update, then stop
+  }
+  st[c] = d;
+  if (d.active != 1) atomicSub(n_active, 1);
+}
+
+__global__ void k_driver_apply(const int64_t* __restrict__ tile_beg, const int32_t* __restrict__ tile_chart,
+                               int64_t n_tiles, DriverState* __restrict__ st, const uint8_t* __restrict__ pinned,
+                               const double* __restrict__ pin_uv, const int64_t* __restrict__ row_of,
+                               const double* __restrict__ x, double* __restrict__ uv) {
+  int64_t t = blockIdx.x;
+  int c = tile_chart[t];
+  int a = st[c].active;
+  if (a == 0) return;
+  double step = st[c].step;
+  for (int64_t v = tile_beg[2 * t] + threadIdx.x; v < tile_beg[2 * t + 1]; v += blockDim.x) {
+    double nu, nw;
+    new_uv_of(v, pinned, pin_uv, row_of, x, nu, nw);
+    double du = dsub(nu, uv[2 * v]), dw = dsub(nw, uv[2 * v + 1]);
+    uv[2 * v] = dadd(uv[2 * v], dmul(du, step));
+    uv[2 * v + 1] = dadd(uv[2 * v + 1], dmul(dw, step));
+  }
+}
+
+__global__ void k_driver_retire(DriverState* st, int64_t n_charts) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n_charts && st[c].active == 2) st[c].active = 0;
+}
+
+}  // namespace
+
+void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
+  cudaStream_t s = ctx.stream;
+  Workspace& ws = ctx.ws;
+  const int64_t NV = bt.n_verts, NT = bt.n_tris, NC = bt.n_charts;
+  const int B = 256;
+  if (NT * 6 >= (int64_t)INT32_MAX || NV >= (int64_t)INT32_MAX)
+    throw Error{RUV_ERR_BAD_INPUT, "batch too large for 32-bit record indices"};
+  int* bad = ws.get<int>("asm.bad", 1);
+  RUV_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  int32_t* tri_g = ws.get<int32_t>("asm.tri_g", 3 * NT);
+  double* cot = ws.get<double>("asm.cot", 3 * NT);
+  if (NT > 0) {
+    k_globalize<<<div_up(NT, B), B, 0, s>>>(bt.tris, bt.tri_off, bt.vert_off, NC, NT, tri_g, bad);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+    k_corner_cot<<<div_up(NT, B), B, 0, s>>>(bt.p3, tri_g, NT, cot);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
+  // free-row numbering
+  uint8_t* fr = ws.get<uint8_t>("asm.free", NV);
+  bt.row_of = ws.get<int64_t>("asm.row_of", NV + 1);
+  if (NV > 0) {
+    k_free_flags<<<div_up(NV, B), B, 0, s>>>(bt.pinned, NV, fr);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
+  exclusive_scan_u8(fr, bt.row_of, NV, ws, s, "asm.rows");
+  sys.chart_row = ws.get<int64_t>("sys.chart_row", NC + 1);
+  k_chart_rows<<<div_up(NC + 1, B), B, 0, s>>>(bt.vert_off, bt.row_of, NC, sys.chart_row);
+  count_launches(1);
+  RUV_LAUNCH_CHECK();
+  // incidence buckets
+  int32_t* deg = ws.get<int32_t>("asm.deg", NV);
+  RUV_CUDA(cudaMemsetAsync(deg, 0, sizeof(int32_t) * (NV > 0 ? NV : 1), s));
+  if (NT > 0) {
+    k_count_records<<<div_up(NT, B), B, 0, s>>>(tri_g, bt.pinned, NT, deg);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
+  int64_t* rec_off = ws.get<int64_t>("asm.rec_off", NV + 1);
+  exclusive_scan(deg, rec_off, NV, ws, s, "asm.rec");
+  // host reads: totals and per-chart row offsets (one small sync)
+  int64_t* hp = static_cast<int64_t*>(ctx.pinned.get(sizeof(int64_t) * (NC + 4)));
+  RUV_CUDA(cudaMemcpyAsync(hp, bt.row_of + NV, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaMemcpyAsync(hp + 1, rec_off + NV, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaMemcpyAsync(hp + 2, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  const int64_t NR = hp[0], NREC = hp[1];
+  int bad_flag = (int)(reinterpret_cast<int*>(hp + 2)[0]);
+  if (bad_flag) throw Error{RUV_ERR_BAD_INPUT, "triangle index out of range or repeated within a triangle"};
+  int32_t* cursor = ws.get<int32_t>("asm.cursor", NV);
+  RUV_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (NV > 0 ? NV : 1), s));
+  int2* rec = ws.get<int2>("asm.rec", NREC);
+  if (NT > 0) {
+    k_scatter_records<<<div_up(NT, B), B, 0, s>>>(tri_g, bt.pinned, NT, rec_off, cursor, rec);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
+  const double mix_b = 1.0 - angle_mix;
+  int32_t* row_len = ws.get<int32_t>("asm.row_len", NR);
+  if (NV > 0) {
+    k_rows<0><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, bt.p3, bt.p2, bt.pin_uv, mix_b,
+                                             row_len, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    count_launches(1);
+  }
+  RUV_LAUNCH_CHECK();
+  int64_t* rp64 = ws.get<int64_t>("asm.rp64", NR + 1);
+  exclusive_scan(row_len, rp64, NR, ws, s, "asm.rp");
+  RUV_CUDA(cudaMemcpyAsync(hp + 3, rp64 + NR, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  const int64_t NNZ = hp[3];
+  if (NNZ >= (int64_t)INT32_MAX) throw Error{RUV_ERR_BAD_INPUT, "operator too large for 32-bit CSR offsets"};
+  sys.n_charts = NC;
+  sys.n_rows = NR;
+  sys.nnz = NNZ;
+  sys.nrhs = 2;
+  sys.row_ptr = ws.get<int32_t>("sys.row_ptr", NR + 1);
+  sys.cols = ws.get<int32_t>("sys.cols", NNZ);
+  sys.vals = ws.get<double>("sys.vals", NNZ);
+  sys.vals32 = ws.get<float>("sys.vals32", NNZ);
+  sys.diag = ws.get<double>("sys.diag", NR);
+  sys.b = ws.get<double>("sys.b", 2 * NR);
+  bt.row_vert = ws.get<int32_t>("sys.row_vert", NR);
+  k_i64_to_i32<<<div_up(NR + 1, B), B, 0, s>>>(rp64, NR + 1, sys.row_ptr);
+  count_launches(1);
+  RUV_LAUNCH_CHECK();
+  if (NV > 0) {
+    k_rows<1><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, bt.p3, bt.p2, bt.pin_uv, mix_b,
+                                             nullptr, rp64, sys.cols, sys.vals, sys.vals32, sys.diag, sys.b,
+                                             bt.row_vert);
+    count_launches(1);
+  }
+  RUV_LAUNCH_CHECK();
+  sys.h_chart_row.resize(NC + 1);
+  RUV_CUDA(cudaMemcpyAsync(sys.h_chart_row.data(), sys.chart_row, sizeof(int64_t) * (NC + 1), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+}
+
+// Tiles over a packed per-chart range (vertices or rows): no tile spans two charts.
+static void build_tiles(const std::vector<int64_t>& off, int64_t tile, std::vector<int64_t>& beg, std::vector<int32_t>& chart,
+                        std::vector<int64_t>& chart_tile) {
+  int64_t nc = (int64_t)off.size() - 1;
+  beg.clear();
+  chart.clear();
+  chart_tile.assign(nc + 1, 0);
+  for (int64_t c = 0; c < nc; ++c) {
+    chart_tile[c] = (int64_t)chart.size();
+    for (int64_t a = off[c]; a < off[c + 1]; a += tile) {
+      beg.push_back(a);
+      chart.push_back((int32_t)c);
+    }
+  }
+  chart_tile[nc] = (int64_t)chart.size();
+  beg.push_back(off[nc]);
+}
+
+void driver_update(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x, int max_iter, double* uv,
+                   std::vector<int32_t>& iters, std::vector<double>& err_accum) {
+  cudaStream_t s = ctx.stream;
+  Workspace& ws = ctx.ws;
+  const int64_t NC = bt.n_charts, NV = bt.n_verts;
+  if (max_iter <= 0) max_iter = 100;
+  // vertex tiles of <= 2048 that never span two charts: table of [begin, end) pairs
+  std::vector<int64_t> beg, chart_tile;
+  std::vector<int32_t> tchart;
+  build_tiles(bt.h_vert_off, 2048, beg, tchart, chart_tile);
+  const int64_t NTL = (int64_t)tchart.size();
+  std::vector<int64_t> tab(2 * NTL);
+  for (int64_t t = 0; t < NTL; ++t) {
+    tab[2 * t] = beg[t];
+    tab[2 * t + 1] = std::min(beg[t] + 2048, bt.h_vert_off[tchart[t] + 1]);
+  }
+  int64_t* d_tab = ws.get<int64_t>("drv.tab", 2 * NTL);
+  int32_t* d_tchart = ws.get<int32_t>("drv.tchart", NTL);
+  int64_t* d_ctile = ws.get<int64_t>("drv.ctile", NC + 1);
+  DriverState* st = ws.get<DriverState>("drv.state", NC);
+  double* part = ws.get<double>("drv.part", 2 * NTL);
+  int* n_active = ws.get<int>("drv.nactive", 1);
+  RUV_CUDA(cudaMemcpyAsync(d_tab, tab.data(), sizeof(int64_t) * 2 * NTL, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_tchart, tchart.data(), sizeof(int32_t) * NTL, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_ctile, chart_tile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
+  int h_nc = (int)NC;
+  RUV_CUDA(cudaMemcpyAsync(n_active, &h_nc, sizeof(int), cudaMemcpyHostToDevice, s));
+  if (NV > 0) {
+    k_driver_init<<<div_up(2 * NV, 256), 256, 0, s>>>(bt.p2, NV, uv);
+    count_launches(1);
+  }
+  k_driver_state_init<<<div_up(NC, 256), 256, 0, s>>>(st, NC);
+  count_launches(1);
+  RUV_LAUNCH_CHECK();
+  int* h_active = static_cast<int*>(ctx.pinned.get(sizeof(int)));
+  for (int it = 0; it < max_iter; ++it) {
+    if (NTL > 0) {
+      k_driver_partials<<<(unsigned)NTL, 256, 0, s>>>(d_tab, d_tchart, NTL, st, bt.pinned, bt.pin_uv, bt.row_of, x, uv,
+                                                      part);
+      count_launches(1);
+      RUV_LAUNCH_CHECK();
+    }
+    k_driver_decide<<<(unsigned)NC, 128, 0, s>>>(d_ctile, NC, st, part, it, max_iter, n_active);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+    if (NTL > 0) {
+      k_driver_apply<<<(unsigned)NTL, 256, 0, s>>>(d_tab, d_tchart, NTL, st, bt.pinned, bt.pin_uv, bt.row_of, x, uv);
+      count_launches(1);
+      RUV_LAUNCH_CHECK();
+    }
+    k_driver_retire<<<div_up(NC, 256), 256, 0, s>>>(st, NC);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+    RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RUV_CUDA(cudaStreamSynchronize(s));
+    if (*h_active <= 0) break;
+  }
+  std::vector<DriverState> hs(NC);
+  RUV_CUDA(cudaMemcpyAsync(hs.data(), st, sizeof(DriverState) * NC, cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  iters.resize(NC);
+  err_accum.resize(NC);
+  for (int64_t c = 0; c < NC; ++c) {
+    iters[c] = hs[c].iters;
+    err_accum[c] = hs[c].err_accum;
+  }
+}
+
+}  // namespace ruv

@@ -1,0 +1,155 @@
+// Device-side building blocks shared by the LSCM kernels: status handling, the device
+// workspace, warp/block reductions with a fixed (deterministic) combine order, and a
+// device-wide exclusive scan.  Everything runs on the context's own stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "ruv_internal.h"
+
+namespace ruv {
+
+constexpr int kWarp = 32;
+constexpr double kEpsDegenerate = 1.1754943508222875e-38;  // unwrap/src/lscm.rs:36
+
+// ------------------------------------------------------------------ errors
+struct Error {
+  ruv_status status;
+  std::string msg;
+};
+
+#define RUV_CUDA(call)                                                                      \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      throw ::ruv::Error{e_ == cudaErrorMemoryAllocation ? RUV_ERR_OOM : RUV_ERR_LAUNCH,     \
+                         std::string(#call) + ": " + cudaGetErrorString(e_)};               \
+  } while (0)
+
+#define RUV_LAUNCH_CHECK() RUV_CUDA(cudaGetLastError())
+
+inline unsigned div_up(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// Kernel-launch accounting: the calling context points this at its counter for the duration
+// of an API call; every launch site adds the kernels it enqueues (graph replays add their
+// node count).
+inline thread_local int64_t* g_launch_counter = nullptr;
+inline void count_launches(int64_t n) {
+  if (g_launch_counter) *g_launch_counter += n;
+}
+
+// ------------------------------------------------------------------ workspace
+// Named device buffers owned by a context, grown on demand and reused across calls, so a
+// steady stream of same-shaped solves allocates nothing after the first.
+class Workspace {
+ public:
+  ~Workspace() { release(); }
+  void* get(const std::string& name, size_t bytes) {
+    auto& b = bufs_[name];
+    if (b.bytes < bytes) {
+      if (b.ptr) cudaFree(b.ptr);
+      b.ptr = nullptr;
+      b.bytes = 0;
+      size_t want = bytes + bytes / 8 + 256;
+      cudaError_t e = cudaMalloc(&b.ptr, want);
+      if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        cudaGetLastError();
+        throw Error{RUV_ERR_OOM, "cudaMalloc(" + std::to_string(want) + ") for " + name + ": " +
+                                     cudaGetErrorString(e)};
+      }
+      b.bytes = want;
+    }
+    return b.ptr;
+  }
+  template <class T>
+  T* get(const std::string& name, int64_t count) {
+    return static_cast<T*>(get(name, (size_t)(count > 0 ? count : 1) * sizeof(T)));
+  }
+  void release() {
+    for (auto& kv : bufs_)
+      if (kv.second.ptr) cudaFree(kv.second.ptr);
+    bufs_.clear();
+  }
+  size_t bytes() const {
+    size_t s = 0;
+    for (auto& kv : bufs_) s += kv.second.bytes;
+    return s;
+  }
+
+ private:
+  struct Buf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+  };
+  std::map<std::string, Buf> bufs_;
+};
+
+// Pinned host staging (for the small per-iteration control reads).
+class PinnedHost {
+ public:
+  ~PinnedHost() {
+    if (p_) cudaFreeHost(p_);
+  }
+  void* get(size_t bytes) {
+    if (bytes > n_) {
+      if (p_) cudaFreeHost(p_);
+      p_ = nullptr;
+      n_ = 0;
+      RUV_CUDA(cudaMallocHost(&p_, bytes));
+      n_ = bytes;
+    }
+    return p_;
+  }
+
+ private:
+  void* p_ = nullptr;
+  size_t n_ = 0;
+};
+
+// ------------------------------------------------------------------ reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sum of up to NV values per thread; every thread gets the totals.  `sh` must hold
+// NV * 32 doubles.  Fixed combine order => bitwise reproducible for a fixed launch shape.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[k * 32 + wid] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double t = lane < nw ? sh[k * 32 + lane] : 0.0;
+    v[k] = warp_sum(t);
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ scan
+// Exclusive scan of int32 counts into int64 offsets (out has n + 1 entries; out[n] = total).
+void exclusive_scan(const int32_t* in, int64_t* out, int64_t n, Workspace& ws, cudaStream_t s,
+                    const std::string& tag);
+// Same for uint8 flags.
+void exclusive_scan_u8(const uint8_t* in, int64_t* out, int64_t n, Workspace& ws, cudaStream_t s,
+                       const std::string& tag);
+
+}  // namespace ruv

@@ -1,0 +1,691 @@
+// Batched preconditioned conjugate gradients over the packed block-diagonal operator
+// (every chart of a mesh in one launch sequence, each chart with its own scalars,
+// convergence test and status) — the sm_103a replacement for the reference's host-driven
+// single-system loop (gpu/src/solver.rs:284-565) and its kernels (gpu/src/kernels.cu:7-75).
+//
+// Work decomposition: rows are cut into tiles that never span two charts; one CTA owns a
+// tile.  A tile-level kernel writes one partial per reduction; a chart-level kernel (one
+// CTA per chart) combines its chart's partials in tile order, so every reduction is
+// deterministic and no host round trip happens inside an iteration.  Charts that are done
+// exit at the top of every kernel.  One iteration is captured once as a CUDA graph and
+// replayed; the host reads the count of active charts every `kCheckEvery` iterations.
+//
+// SpMV: CSR-vector with `LPR` lanes per row (sub-warp per row, chosen from the row-length
+// profile), coalesced 32-bit value/column loads across the lanes, (u, v) pairs moved as one
+// 64-bit (FP32) / 128-bit (FP64) vector, shuffle reduction inside the sub-warp, and the
+// p.q product fused into the same pass.
+//
+// Precision: RUV_PREC_FP64 runs the reference's recurrence in FP64.  RUV_PREC_MIXED runs
+// the SpMV, preconditioner and CG recurrence in FP32 and keeps FP64 for the solution
+// accumulator and the true residual r = b - A x (FP64 values), recomputed per chart
+// whenever the FP32 residual has dropped by `kDelta` since the last true residual
+// ("reliable updates"); convergence is judged on the FP64 true residual only.
+#include "system.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace ruv {
+namespace {
+
+constexpr int kTileThreads = 256;
+constexpr int kChartThreads = 128;
+constexpr int kCheckEvery = 16;
+constexpr double kDelta = 0.1;
+
+enum : int32_t { kActive = 0, kDone = 1 };
+
+struct ChartState {
+  double rz;       // r.z of the current iterate
+  double alpha;
+  double beta;
+  double tol_abs;  // tol * ||b|| (tol when ||b|| <= 1e-300), solver.rs:465-466
+  double r_ref;    // ||r|| at the last true-residual (mixed)
+  double rr;       // last ||r||^2 (FP64 true residual for mixed)
+  double bnorm;
+  int32_t iters;
+  int32_t status;
+  int32_t state;
+  int32_t refresh;  // mixed: a true-residual refresh is due
+  int32_t refinements;
+  int32_t pad;
+};
+
+template <class S, int NR>
+struct V {
+  S c[NR];
+};
+template <class S, int NR>
+__device__ __forceinline__ V<S, NR> ldv(const S* p, int64_t i) {
+  V<S, NR> r;
+  if constexpr (NR == 2 && sizeof(S) == 8) {
+    double2 t = reinterpret_cast<const double2*>(p)[i];
+    r.c[0] = t.x;
+    r.c[1] = t.y;
+  } else if constexpr (NR == 2 && sizeof(S) == 4) {
+    float2 t = reinterpret_cast<const float2*>(p)[i];
+    r.c[0] = t.x;
+    r.c[1] = t.y;
+  } else {
+    r.c[0] = p[i];
+  }
+  return r;
+}
+template <class S, int NR>
+__device__ __forceinline__ void stv(S* p, int64_t i, const V<S, NR>& v) {
+  if constexpr (NR == 2 && sizeof(S) == 8) {
+    reinterpret_cast<double2*>(p)[i] = make_double2(v.c[0], v.c[1]);
+  } else if constexpr (NR == 2 && sizeof(S) == 4) {
+    reinterpret_cast<float2*>(p)[i] = make_float2(v.c[0], v.c[1]);
+  } else {
+    p[i] = v.c[0];
+  }
+}
+
+struct Tiles {
+  const int64_t* tab;      // [begin, end) pairs
+  const int32_t* chart;    // chart of each tile
+  const int64_t* chart_tile;
+  int64_t n;
+};
+
+// ---------------------------------------------------------------- tile kernels
+// Initial state: x = 0, r = b, z = M^-1 r, p = z.  Partials: b.b, r.z, #zero diagonals.
+template <class S, int NR>
+__global__ void __launch_bounds__(kTileThreads) k_init(Tiles T, const double* __restrict__ b, const double* __restrict__ diag,
+                                                       int use_jacobi, double* __restrict__ x64, S* __restrict__ xs,
+                                                       S* __restrict__ r, S* __restrict__ z, S* __restrict__ p,
+                                                       double* __restrict__ part) {
+  __shared__ double sh[3 * 32];
+  int64_t t = blockIdx.x;
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
+    V<double, NR> bv = ldv<double, NR>(b, i);
+    V<S, NR> rv, zv, zero;
+    double d = diag[i];
+    if (d == 0.0) acc[2] += 1.0;
+    S dinv = use_jacobi ? (S)(1.0 / d) : (S)1.0;
+#pragma unroll
+    for (int k = 0; k < NR; ++k) {
+      rv.c[k] = (S)bv.c[k];
+      zv.c[k] = rv.c[k] * dinv;
+      zero.c[k] = (S)0;
+      acc[0] += bv.c[k] * bv.c[k];
+      acc[1] += (double)rv.c[k] * (double)zv.c[k];
+    }
+    V<double, NR> z64;
+#pragma unroll
+    for (int k = 0; k < NR; ++k) z64.c[k] = 0.0;
+    stv<double, NR>(x64, i, z64);
+    if (xs) stv<S, NR>(xs, i, zero);
+    stv<S, NR>(r, i, rv);
+    stv<S, NR>(z, i, zv);
+    stv<S, NR>(p, i, zv);
+  }
+  block_sum<3>(acc, sh);
+  if (threadIdx.x == 0) {
+    part[3 * t] = acc[0];
+    part[3 * t + 1] = acc[1];
+    part[3 * t + 2] = acc[2];
+  }
+}
+
+// q = A p on the tile's rows (LPR lanes per row) fused with the partial p.q.
+template <class S, int NR, int LPR>
+__global__ void __launch_bounds__(kTileThreads) k_spmv_pq(Tiles T, const ChartState* __restrict__ st,
+                                                          const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
+                                                          const S* __restrict__ vals, const S* __restrict__ p,
+                                                          S* __restrict__ q, double* __restrict__ part) {
+  __shared__ double sh[32];
+  int64_t t = blockIdx.x;
+  if (st[T.chart[t]].state != kActive) return;
+  const int sub = threadIdx.x % LPR;
+  double acc[1] = {0.0};
+  const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
+  // block-uniform trip count: every lane takes part in the sub-warp shuffles
+  for (int64_t base = beg; base < end; base += blockDim.x / LPR) {
+    const int64_t i = base + threadIdx.x / LPR;
+    const bool valid = i < end;
+    const int lo = valid ? row_ptr[i] : 0, hi = valid ? row_ptr[i + 1] : 0;
+    V<S, NR> s;
+#pragma unroll
+    for (int k = 0; k < NR; ++k) s.c[k] = (S)0;
+    for (int e = lo + sub; e < hi; e += LPR) {
+      const S a = vals[e];
+      const V<S, NR> pv = ldv<S, NR>(p, cols[e]);
+#pragma unroll
+      for (int k = 0; k < NR; ++k) s.c[k] += a * pv.c[k];
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < NR; ++k) s.c[k] += __shfl_xor_sync(0xffffffffu, s.c[k], o, LPR);
+    if (valid && sub == 0) {
+      stv<S, NR>(q, i, s);
+      const V<S, NR> pi = ldv<S, NR>(p, i);
+#pragma unroll
+      for (int k = 0; k < NR; ++k) acc[0] += (double)pi.c[k] * (double)s.c[k];
+    }
+  }
+  block_sum<1>(acc, sh);
+  if (threadIdx.x == 0) part[t] = acc[0];
+}
+
+// x += alpha p; r -= alpha q; z = M^-1 r.  Partials: r.r, r.z.
+template <class S, int NR>
+__global__ void __launch_bounds__(kTileThreads) k_update(Tiles T, const ChartState* __restrict__ st,
+                                                         const double* __restrict__ diag, int use_jacobi,
+                                                         S* __restrict__ x, S* __restrict__ r, S* __restrict__ z,
+                                                         const S* __restrict__ p, const S* __restrict__ q,
+                                                         double* __restrict__ part) {
+  __shared__ double sh[2 * 32];
+  int64_t t = blockIdx.x;
+  const ChartState& cs = st[T.chart[t]];
+  if (cs.state != kActive) return;
+  const S alpha = (S)cs.alpha;
+  double acc[2] = {0.0, 0.0};
+  for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
+    V<S, NR> xv = ldv<S, NR>(x, i), rv = ldv<S, NR>(r, i), pv = ldv<S, NR>(p, i), qv = ldv<S, NR>(q, i), zv;
+    const S dinv = use_jacobi ? (S)(1.0 / diag[i]) : (S)1;
+#pragma unroll
+    for (int k = 0; k < NR; ++k) {
+      xv.c[k] += alpha * pv.c[k];
+      rv.c[k] -= alpha * qv.c[k];
+      zv.c[k] = rv.c[k] * dinv;
+      acc[0] += (double)rv.c[k] * (double)rv.c[k];
+      acc[1] += (double)rv.c[k] * (double)zv.c[k];
+    }
+    stv<S, NR>(x, i, xv);
+    stv<S, NR>(r, i, rv);
+    stv<S, NR>(z, i, zv);
+  }
+  block_sum<2>(acc, sh);
+  if (threadIdx.x == 0) {
+    part[2 * t] = acc[0];
+    part[2 * t + 1] = acc[1];
+  }
+}
+
+// p = z + beta p
+template <class S, int NR>
+__global__ void __launch_bounds__(kTileThreads) k_direction(Tiles T, const ChartState* __restrict__ st,
+                                                            const S* __restrict__ z, S* __restrict__ p) {
+  int64_t t = blockIdx.x;
+  const ChartState& cs = st[T.chart[t]];
+  if (cs.state != kActive) return;
+  const S beta = (S)cs.beta;
+  for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
+    V<S, NR> zv = ldv<S, NR>(z, i), pv = ldv<S, NR>(p, i);
+#pragma unroll
+    for (int k = 0; k < NR; ++k) pv.c[k] = zv.c[k] + beta * pv.c[k];
+    stv<S, NR>(p, i, pv);
+  }
+}
+
+// Mixed precision, refresh step 1 (charts that asked for a refresh, or every chart when
+// `all`): fold the FP32 increment into the FP64 solution, xs = 0.  A separate launch from
+// the true residual, which reads x64 of neighbouring rows in other tiles.
+template <int NR>
+__global__ void __launch_bounds__(kTileThreads) k_fold(Tiles T, const ChartState* __restrict__ st, int all,
+                                                       double* __restrict__ x64, float* __restrict__ xs) {
+  int64_t t = blockIdx.x;
+  const ChartState& cs = st[T.chart[t]];
+  if (!all && (cs.state != kActive || !cs.refresh)) return;
+  for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
+    V<double, NR> xv = ldv<double, NR>(x64, i);
+    V<float, NR> dv = ldv<float, NR>(xs, i), zero;
+#pragma unroll
+    for (int k = 0; k < NR; ++k) {
+      xv.c[k] += (double)dv.c[k];
+      zero.c[k] = 0.f;
+    }
+    stv<double, NR>(x64, i, xv);
+    stv<float, NR>(xs, i, zero);
+  }
+}
+
+// Mixed precision, refresh step 2: r = b - A x64 in FP64; r32 = r; z = M^-1 r.
+// Partials: r.r (FP64), r.z.
+template <int NR, int LPR>
+__global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const ChartState* __restrict__ st,
+                                                                const int32_t* __restrict__ row_ptr,
+                                                                const int32_t* __restrict__ cols,
+                                                                const double* __restrict__ vals, const double* __restrict__ b,
+                                                                const double* __restrict__ diag, int use_jacobi,
+                                                                const double* __restrict__ x64, float* __restrict__ r,
+                                                                float* __restrict__ z, double* __restrict__ part) {
+  __shared__ double sh[2 * 32];
+  int64_t t = blockIdx.x;
+  const ChartState& cs = st[T.chart[t]];
+  if (cs.state != kActive || !cs.refresh) return;
+  const int sub = threadIdx.x % LPR;
+  double acc[2] = {0.0, 0.0};
+  const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
+  for (int64_t base = beg; base < end; base += blockDim.x / LPR) {
+    const int64_t i = base + threadIdx.x / LPR;
+    const bool valid = i < end;
+    const int lo = valid ? row_ptr[i] : 0, hi = valid ? row_ptr[i + 1] : 0;
+    V<double, NR> s;
+#pragma unroll
+    for (int k = 0; k < NR; ++k) s.c[k] = 0.0;
+    for (int e = lo + sub; e < hi; e += LPR) {
+      const double a = vals[e];
+      const V<double, NR> xv = ldv<double, NR>(x64, cols[e]);
+#pragma unroll
+      for (int k = 0; k < NR; ++k) s.c[k] += a * xv.c[k];
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < NR; ++k) s.c[k] += __shfl_xor_sync(0xffffffffu, s.c[k], o, LPR);
+    if (valid && sub == 0) {
+      const V<double, NR> bv = ldv<double, NR>(b, i);
+      const double dinv = use_jacobi ? 1.0 / diag[i] : 1.0;
+      V<float, NR> rv, zv;
+#pragma unroll
+      for (int k = 0; k < NR; ++k) {
+        double res = bv.c[k] - s.c[k];
+        acc[0] += res * res;
+        rv.c[k] = (float)res;
+        zv.c[k] = rv.c[k] * (float)dinv;
+        acc[1] += (double)rv.c[k] * (double)zv.c[k];
+      }
+      stv<float, NR>(r, i, rv);
+      stv<float, NR>(z, i, zv);
+    }
+  }
+  block_sum<2>(acc, sh);
+  if (threadIdx.x == 0) {
+    part[2 * t] = acc[0];
+    part[2 * t + 1] = acc[1];
+  }
+}
+
+// ---------------------------------------------------------------- chart kernels
+template <int NV>
+__device__ __forceinline__ void chart_reduce(const Tiles& T, int64_t c, const double* part, int stride, double (&v)[NV],
+                                             double* sh) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = 0.0;
+  for (int64_t t = T.chart_tile[c] + threadIdx.x; t < T.chart_tile[c + 1]; t += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] += part[stride * t + k];
+  block_sum<NV>(v, sh);
+}
+
+__global__ void __launch_bounds__(kChartThreads) k_chart_init(Tiles T, ChartState* __restrict__ st, const double* __restrict__ part,
+                                                              double tol, int precond_none, int* __restrict__ n_active) {
+  __shared__ double sh[3 * 32];
+  int64_t c = blockIdx.x;
+  double v[3];
+  chart_reduce<3>(T, c, part, 3, v, sh);
+  if (threadIdx.x != 0) return;
+  ChartState s{};
+  s.bnorm = sqrt(v[0]);
+  s.tol_abs = s.bnorm <= 1e-300 ? tol : tol * s.bnorm;
+  s.rr = v[0];
+  s.r_ref = s.bnorm;
+  s.rz = precond_none ? v[0] : v[1];
+  s.iters = 0;
+  s.refinements = 0;
+  s.refresh = 0;
+  if (v[2] > 0.0 && !precond_none) {
+    s.status = RUV_ERR_BREAKDOWN;  // Jacobi with a zero diagonal (precond.rs:595-611)
+    s.state = kDone;
+  } else if (sqrt(v[0]) <= s.tol_abs) {
+    s.status = RUV_OK;
+    s.state = kDone;
+  } else {
+    s.status = RUV_ERR_NOT_CONVERGED;
+    s.state = kActive;
+    atomicAdd(n_active, 1);
+  }
+  st[c] = s;
+}
+
+__global__ void __launch_bounds__(kChartThreads) k_chart_alpha(Tiles T, ChartState* __restrict__ st, const double* __restrict__ part,
+                                                               int* __restrict__ n_active) {
+  __shared__ double sh[32];
+  int64_t c = blockIdx.x;
+  if (st[c].state != kActive) return;
+  double v[1];
+  chart_reduce<1>(T, c, part, 1, v, sh);
+  if (threadIdx.x != 0) return;
+  ChartState& s = st[c];
+  double pap = v[0];
+  if (fabs(pap) <= 1e-300 || !isfinite(pap)) {  // solver.rs:505-508
+    s.status = RUV_ERR_BREAKDOWN;
+    s.state = kDone;
+    atomicSub(n_active, 1);
+    return;
+  }
+  s.alpha = s.rz / pap;
+}
+
+// FP64 path: convergence on the recurrence residual (solver.rs:518-522), then beta.
+__global__ void __launch_bounds__(kChartThreads) k_chart_beta(Tiles T, ChartState* __restrict__ st, const double* __restrict__ part,
+                                                              int precond_none, int64_t max_iter, int* __restrict__ n_active) {
+  __shared__ double sh[2 * 32];
+  int64_t c = blockIdx.x;
+  if (st[c].state != kActive) return;
+  double v[2];
+  chart_reduce<2>(T, c, part, 2, v, sh);
+  if (threadIdx.x != 0) return;
+  ChartState& s = st[c];
+  s.iters += 1;
+  s.rr = v[0];
+  if (sqrt(v[0]) <= s.tol_abs) {
+    s.status = RUV_OK;
+    s.state = kDone;
+    atomicSub(n_active, 1);
+    return;
+  }
+  if (s.iters >= max_iter) {
+    s.status = RUV_ERR_NOT_CONVERGED;
+    s.state = kDone;
+    atomicSub(n_active, 1);
+    return;
+  }
+  double rznew = precond_none ? v[0] : v[1];
+  s.beta = rznew / s.rz;
+  s.rz = rznew;
+}
+
+// Mixed path: the FP32 residual only schedules true-residual refreshes.
+__global__ void __launch_bounds__(kChartThreads) k_chart_beta_mixed(Tiles T, ChartState* __restrict__ st,
+                                                                    const double* __restrict__ part, int precond_none,
+                                                                    int64_t max_iter, int* __restrict__ n_active) {
+  __shared__ double sh[2 * 32];
+  int64_t c = blockIdx.x;
+  if (st[c].state != kActive) return;
+  double v[2];
+  chart_reduce<2>(T, c, part, 2, v, sh);
+  if (threadIdx.x != 0) return;
+  ChartState& s = st[c];
+  s.iters += 1;
+  double rn = sqrt(v[0]);
+  double rznew = precond_none ? v[0] : v[1];
+  if (rn <= kDelta * s.r_ref || rn <= s.tol_abs || !isfinite(rn) || s.iters >= max_iter) {
+    s.refresh = 1;  // beta is formed after the refresh, from the true residual
+  } else {
+    s.refresh = 0;
+    s.beta = rznew / s.rz;
+    s.rz = rznew;
+  }
+  (void)n_active;
+}
+
+__global__ void __launch_bounds__(kChartThreads) k_chart_after_refresh(Tiles T, ChartState* __restrict__ st,
+                                                                       const double* __restrict__ part, int precond_none,
+                                                                       int64_t max_iter, int* __restrict__ n_active) {
+  __shared__ double sh[2 * 32];
+  int64_t c = blockIdx.x;
+  if (st[c].state != kActive || !st[c].refresh) return;
+  double v[2];
+  chart_reduce<2>(T, c, part, 2, v, sh);
+  if (threadIdx.x != 0) return;
+  ChartState& s = st[c];
+  s.refinements += 1;
+  s.rr = v[0];
+  double rn = sqrt(v[0]);
+  if (rn <= s.tol_abs) {
+    s.status = RUV_OK;
+    s.state = kDone;
+    atomicSub(n_active, 1);
+    return;
+  }
+  if (!isfinite(rn)) {
+    s.status = RUV_ERR_BREAKDOWN;
+    s.state = kDone;
+    atomicSub(n_active, 1);
+    return;
+  }
+  if (s.iters >= max_iter) {
+    s.status = RUV_ERR_NOT_CONVERGED;
+    s.state = kDone;
+    atomicSub(n_active, 1);
+    return;
+  }
+  s.r_ref = rn;
+  double rznew = precond_none ? v[0] : v[1];
+  s.beta = rznew / s.rz;
+  s.rz = rznew;
+  s.refresh = 0;
+}
+
+// ---------------------------------------------------------------- host driver
+struct TileTable {
+  std::vector<int64_t> tab, chart_tile;
+  std::vector<int32_t> chart;
+};
+
+TileTable make_tiles(const std::vector<int64_t>& chart_row, int64_t tile_rows) {
+  TileTable T;
+  int64_t nc = (int64_t)chart_row.size() - 1;
+  T.chart_tile.assign(nc + 1, 0);
+  for (int64_t c = 0; c < nc; ++c) {
+    T.chart_tile[c] = (int64_t)T.chart.size();
+    for (int64_t a = chart_row[c]; a < chart_row[c + 1]; a += tile_rows) {
+      T.tab.push_back(a);
+      T.tab.push_back(std::min(a + tile_rows, chart_row[c + 1]));
+      T.chart.push_back((int32_t)c);
+    }
+  }
+  T.chart_tile[nc] = (int64_t)T.chart.size();
+  return T;
+}
+
+template <class S, int NR, int LPR>
+void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st, int* n_active,
+             std::vector<ChartState>& out) {
+  cudaStream_t s = ctx.stream;
+  Workspace& ws = ctx.ws;
+  const bool mixed = std::is_same<S, float>::value;
+  const int64_t NR_ = sys.n_rows, NC = sys.n_charts, NTL = T.n;
+  const int jac = o.precond == RUV_PRECOND_JACOBI ? 1 : 0;
+  const int none = o.precond == RUV_PRECOND_NONE ? 1 : 0;
+  S* xs = mixed ? ws.get<S>("pcg.xs", NR * NR_) : nullptr;
+  S* r = ws.get<S>("pcg.r", NR * NR_);
+  S* z = ws.get<S>("pcg.z", NR * NR_);
+  S* p = ws.get<S>("pcg.p", NR * NR_);
+  S* q = ws.get<S>("pcg.q", NR * NR_);
+  double* part = ws.get<double>("pcg.part", 3 * NTL);
+  const S* vals = mixed ? reinterpret_cast<const S*>(sys.vals32) : reinterpret_cast<const S*>(sys.vals);
+  RUV_CUDA(cudaMemsetAsync(n_active, 0, sizeof(int), s));
+  if (NTL > 0) {
+    k_init<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, sys.b, sys.diag, jac, x64, xs, r, z, p, part);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
+  k_chart_init<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, o.tol, none, n_active);
+  count_launches(1);
+  RUV_LAUNCH_CHECK();
+  int* h_active = static_cast<int*>(ctx.pinned.get(sizeof(int)));
+  RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  if (*h_active > 0 && NTL > 0) {
+    // capture one iteration as a graph, replay it
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    RUV_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int rep = 0; rep < kCheckEvery; ++rep) {
+      k_spmv_pq<S, NR, LPR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, p, q, part);
+      k_chart_alpha<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, n_active);
+      k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.diag, jac, mixed ? xs : reinterpret_cast<S*>(x64),
+                                                             r, z, p, q, part);
+      if (!mixed) {
+        k_chart_beta<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
+      } else {
+        k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
+        k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, x64, reinterpret_cast<float*>(xs));
+        k_true_residual<NR, LPR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, sys.vals, sys.b,
+                                                                       sys.diag, jac, x64, reinterpret_cast<float*>(r),
+                                                                       reinterpret_cast<float*>(z), part);
+        k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
+      }
+      k_direction<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
+    }
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess) throw Error{RUV_ERR_LAUNCH, std::string("graph capture: ") + cudaGetErrorString(ce)};
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    if (ce != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      throw Error{RUV_ERR_LAUNCH, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+    }
+    int64_t launched = 0;
+    try {
+      while (launched < o.max_iter + kCheckEvery) {
+        RUV_CUDA(cudaGraphLaunch(exec, s));
+        count_launches((int64_t)kCheckEvery * (mixed ? 8 : 5));
+        launched += kCheckEvery;
+        RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+        RUV_CUDA(cudaStreamSynchronize(s));
+        if (*h_active <= 0) break;
+      }
+    } catch (...) {
+      cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(graph);
+      throw;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+  }
+  if (mixed && NTL > 0) {
+    // fold any FP32 increment still pending (charts that stopped between refreshes)
+    k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 1, x64, reinterpret_cast<float*>(xs));
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
+  out.resize(NC);
+  RUV_CUDA(cudaMemcpyAsync(out.data(), st, sizeof(ChartState) * NC, cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+}
+
+template <class S, int NR>
+void dispatch_lpr(int lpr, Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st,
+                  int* n_active, std::vector<ChartState>& out) {
+  switch (lpr) {
+    case 2: return run_pcg<S, NR, 2>(ctx, sys, x64, o, T, st, n_active, out);
+    case 4: return run_pcg<S, NR, 4>(ctx, sys, x64, o, T, st, n_active, out);
+    case 8: return run_pcg<S, NR, 8>(ctx, sys, x64, o, T, st, n_active, out);
+    case 16: return run_pcg<S, NR, 16>(ctx, sys, x64, o, T, st, n_active, out);
+    default: return run_pcg<S, NR, 32>(ctx, sys, x64, o, T, st, n_active, out);
+  }
+}
+
+Tiles upload_tiles(Ctx& ctx, const DevSystem& sys, const std::string& tag) {
+  cudaStream_t s = ctx.stream;
+  TileTable TT = make_tiles(sys.h_chart_row, ctx.tile_rows);
+  const int64_t NTL = (int64_t)TT.chart.size(), NC = sys.n_charts;
+  int64_t* d_tab = ctx.ws.get<int64_t>(tag + ".tab", 2 * NTL);
+  int32_t* d_chart = ctx.ws.get<int32_t>(tag + ".tchart", NTL);
+  int64_t* d_ctile = ctx.ws.get<int64_t>(tag + ".ctile", NC + 1);
+  if (NTL > 0) {
+    RUV_CUDA(cudaMemcpyAsync(d_tab, TT.tab.data(), sizeof(int64_t) * 2 * NTL, cudaMemcpyHostToDevice, s));
+    RUV_CUDA(cudaMemcpyAsync(d_chart, TT.chart.data(), sizeof(int32_t) * NTL, cudaMemcpyHostToDevice, s));
+  }
+  RUV_CUDA(cudaMemcpyAsync(d_ctile, TT.chart_tile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
+  // the host tables go out of scope: make sure the copies have been consumed
+  RUV_CUDA(cudaStreamSynchronize(s));
+  return Tiles{d_tab, d_chart, d_ctile, NTL};
+}
+
+// Lanes per row from the average row length: enough lanes to cover a typical row once.
+int pick_lpr(const Ctx& ctx, const DevSystem& sys) {
+  if (ctx.lanes_per_row > 0) return ctx.lanes_per_row;
+  double avg = sys.n_rows > 0 ? (double)sys.nnz / (double)sys.n_rows : 1.0;
+  return avg <= 3 ? 2 : avg <= 6 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32;
+}
+
+template <class S, int NR, int LPR>
+double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
+  cudaStream_t s = ctx.stream;
+  const int64_t N = sys.n_rows, NC = sys.n_charts;
+  ChartState* st = ctx.ws.get<ChartState>("bench.state", NC);
+  RUV_CUDA(cudaMemsetAsync(st, 0, sizeof(ChartState) * NC, s));  // every chart active
+  double* part = ctx.ws.get<double>("bench.part", T.n);
+  std::vector<S*> ps(nbuf), qs(nbuf);
+  for (int k = 0; k < nbuf; ++k) {
+    ps[k] = ctx.ws.get<S>("bench.p" + std::to_string(k), NR * N);
+    qs[k] = ctx.ws.get<S>("bench.q" + std::to_string(k), NR * N);
+    RUV_CUDA(cudaMemsetAsync(ps[k], 0, sizeof(S) * NR * N, s));
+  }
+  const S* vals = std::is_same<S, float>::value ? reinterpret_cast<const S*>(sys.vals32) : reinterpret_cast<const S*>(sys.vals);
+  auto launch = [&](int k) {
+    k_spmv_pq<S, NR, LPR><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, ps[k % nbuf],
+                                                                qs[k % nbuf], part);
+    count_launches(1);
+  };
+  for (int k = 0; k < 3; ++k) launch(k);
+  RUV_LAUNCH_CHECK();
+  cudaEvent_t e0, e1;
+  RUV_CUDA(cudaEventCreate(&e0));
+  RUV_CUDA(cudaEventCreate(&e1));
+  RUV_CUDA(cudaEventRecord(e0, s));
+  for (int k = 0; k < reps; ++k) launch(k);
+  RUV_CUDA(cudaEventRecord(e1, s));
+  RUV_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  RUV_LAUNCH_CHECK();
+  return (double)ms / reps;
+}
+
+template <class S, int NR>
+double time_spmv_lpr(int lpr, Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
+  switch (lpr) {
+    case 2: return time_spmv<S, NR, 2>(ctx, sys, T, reps, nbuf);
+    case 4: return time_spmv<S, NR, 4>(ctx, sys, T, reps, nbuf);
+    case 8: return time_spmv<S, NR, 8>(ctx, sys, T, reps, nbuf);
+    case 16: return time_spmv<S, NR, 16>(ctx, sys, T, reps, nbuf);
+    default: return time_spmv<S, NR, 32>(ctx, sys, T, reps, nbuf);
+  }
+}
+
+}  // namespace
+
+double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes) {
+  Tiles T = upload_tiles(ctx, sys, "bench");
+  const int lpr = pick_lpr(ctx, sys);
+  const double N = (double)sys.n_rows, NNZ = (double)sys.nnz, nr = (double)sys.nrhs;
+  const double vb = mixed ? 4.0 : 8.0;
+  if (bytes) *bytes = NNZ * (vb + 4.0) + (N + 1.0) * 4.0 + 2.0 * N * nr * vb;
+  if (T.n == 0) return 0.0;
+  if (sys.nrhs == 2)
+    return mixed ? time_spmv_lpr<float, 2>(lpr, ctx, sys, T, reps, n_buffers)
+                 : time_spmv_lpr<double, 2>(lpr, ctx, sys, T, reps, n_buffers);
+  return mixed ? time_spmv_lpr<float, 1>(lpr, ctx, sys, T, reps, n_buffers)
+               : time_spmv_lpr<double, 1>(lpr, ctx, sys, T, reps, n_buffers);
+}
+
+std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o) {
+  if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI)
+    throw Error{RUV_ERR_BAD_INPUT, "preconditioner not available in this build"};
+  const int64_t NC = sys.n_charts;
+  Tiles T = upload_tiles(ctx, sys, "pcg");
+  ChartState* st = ctx.ws.get<ChartState>("pcg.state", NC);
+  int* n_active = ctx.ws.get<int>("pcg.nactive", 1);
+  const int lpr = pick_lpr(ctx, sys);
+  std::vector<ChartState> out;
+  const bool mixed = o.precision == RUV_PREC_MIXED;
+  if (sys.nrhs == 2) {
+    if (mixed) dispatch_lpr<float, 2>(lpr, ctx, sys, x, o, T, st, n_active, out);
+    else dispatch_lpr<double, 2>(lpr, ctx, sys, x, o, T, st, n_active, out);
+  } else {
+    if (mixed) dispatch_lpr<float, 1>(lpr, ctx, sys, x, o, T, st, n_active, out);
+    else dispatch_lpr<double, 1>(lpr, ctx, sys, x, o, T, st, n_active, out);
+  }
+  std::vector<ChartResult> res(NC);
+  for (int64_t c = 0; c < NC; ++c) {
+    const ChartState& cs = out[c];
+    res[c].status = cs.status;
+    res[c].iters = cs.iters;
+    res[c].refinements = cs.refinements;
+    res[c].rel_res = cs.bnorm > 1e-300 ? std::sqrt(cs.rr) / cs.bnorm : std::sqrt(cs.rr);
+  }
+  return res;
+}
+
+}  // namespace ruv

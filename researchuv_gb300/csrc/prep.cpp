@@ -1,0 +1,856 @@
+// Host chart stages of the LSCM path: weld, sharp-edge segmentation, border loops, tangent
+// frames and Dirichlet pins — everything unfold_chart computes before it assembles
+// (reference: unwrap/src/weld.rs:19-57, unwrap/src/segment.rs:61-331,
+// unwrap/src/lscm.rs:152-247, :280-413, :512-592).
+//
+// These stages are O(V + F) integer/topology work with a little libm (acos, atan2, sin,
+// cos) and stay on the host; they run on the calling thread plus a pool over charts.  The
+// data structures are flat arrays (vertex->face CSR, sorted edge tables, per-chart scratch)
+// instead of the reference's BTreeMaps, but every visit order that decides a result — DFS
+// stack pops, ascending-neighbour walks, left-to-right floating sums — is the reference's,
+// so the partition, loops, pins and frames are bit-identical on the same host libm.
+// Compiled with -ffp-contract=off (no FMA contraction).
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ruv_internal.h"
+
+namespace ruv {
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+struct D3 {
+  double x, y, z;
+};
+inline D3 operator-(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline D3 operator+(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline D3 operator/(D3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+inline double dot3(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 cross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double norm3(D3 a) { return std::sqrt(dot3(a, a)); }
+
+inline double fmax_rs(double a, double b) {  // Rust f64::max
+  if (a != a) return b;
+  if (b != b) return a;
+  return a > b ? a : b;
+}
+inline double fmin_rs(double a, double b) {  // Rust f64::min
+  if (a != a) return b;
+  if (b != b) return a;
+  return a < b ? a : b;
+}
+inline int64_t total_order_key(double a) {  // Rust f64::total_cmp
+  int64_t i;
+  std::memcpy(&i, &a, 8);
+  return i ^ (int64_t)(((uint64_t)(i >> 63)) >> 1);
+}
+inline int64_t round_to_i64(double x) {  // (x).round() as i64, saturating
+  double r = std::round(x);
+  if (r != r) return 0;
+  if (r >= 9.2233720368547758e18) return INT64_MAX;
+  if (r <= -9.2233720368547758e18) return INT64_MIN;
+  return (int64_t)r;
+}
+
+template <class F>
+void parallel_for(int64_t n, int threads, F&& body) {
+  if (n <= 0) return;
+  int nt = threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency());
+  nt = (int)std::min<int64_t>(nt, n);
+  if (nt <= 1) {
+    for (int64_t i = 0; i < n; ++i) body(i);
+    return;
+  }
+  std::atomic<int64_t> next{0};
+  std::vector<std::thread> pool;
+  pool.reserve(nt);
+  for (int t = 0; t < nt; ++t)
+    pool.emplace_back([&] {
+      for (;;) {
+        int64_t i = next.fetch_add(1);
+        if (i >= n) break;
+        body(i);
+      }
+    });
+  for (auto& th : pool) th.join();
+}
+
+// ------------------------------------------------------------------ weld (weld.rs:19-57)
+// Open-addressing table on the rounded integer key; the first vertex with a key becomes
+// the canonical id (the reference's HashMap-first-occurrence rule).
+void weld(const double* pos, int64_t nv, const int32_t* faces, int64_t nf, double tol,
+          std::vector<D3>& out_pos, std::vector<int32_t>& out_faces) {
+  out_pos.clear();
+  out_faces.clear();
+  if (tol <= 0.0) {
+    out_pos.resize(nv);
+    for (int64_t i = 0; i < nv; ++i) out_pos[i] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    out_faces.assign(faces, faces + 3 * nf);
+    return;
+  }
+  double inv = 1.0 / tol;
+  uint64_t cap = 16;
+  while (cap < (uint64_t)nv * 2 + 16) cap <<= 1;
+  struct Slot {
+    int64_t k[3];
+    int32_t id;
+  };
+  std::vector<Slot> table(cap, Slot{{0, 0, 0}, -1});
+  std::vector<int32_t> remap(nv);
+  for (int64_t i = 0; i < nv; ++i) {
+    int64_t k0 = round_to_i64(pos[3 * i] * inv), k1 = round_to_i64(pos[3 * i + 1] * inv),
+            k2 = round_to_i64(pos[3 * i + 2] * inv);
+    uint64_t h = (uint64_t)k0 * 0xff51afd7ed558ccdull ^ ((uint64_t)k1 + 0x9e3779b97f4a7c15ull) * 0xc4ceb9fe1a85ec53ull ^
+                 ((uint64_t)k2 + 0x632be59bd9b4e019ull) * 0x94d049bb133111ebull;
+    h ^= h >> 29;
+    uint64_t s = h & (cap - 1);
+    for (;;) {
+      Slot& sl = table[s];
+      if (sl.id < 0) {
+        sl.k[0] = k0;
+        sl.k[1] = k1;
+        sl.k[2] = k2;
+        sl.id = (int32_t)out_pos.size();
+        out_pos.push_back({pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]});
+        remap[i] = sl.id;
+        break;
+      }
+      if (sl.k[0] == k0 && sl.k[1] == k1 && sl.k[2] == k2) {
+        remap[i] = sl.id;
+        break;
+      }
+      s = (s + 1) & (cap - 1);
+    }
+  }
+  out_faces.reserve(3 * nf);
+  for (int64_t f = 0; f < nf; ++f) {
+    int32_t a = remap[faces[3 * f]], b = remap[faces[3 * f + 1]], c = remap[faces[3 * f + 2]];
+    if (a != b && b != c && a != c) {
+      out_faces.push_back(a);
+      out_faces.push_back(b);
+      out_faces.push_back(c);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ face adjacency
+// For every face slot (f, k) — edge (t[k], t[k+1]) — the list of faces carrying that edge in
+// ascending face order (segment.rs:73-81 edge_faces), via a vertex->faces CSR.
+struct EdgeFaces {
+  std::vector<int64_t> off;  // 3F + 1
+  std::vector<int32_t> faces;
+};
+
+void build_vertex_faces(int64_t nv, const std::vector<int32_t>& F, std::vector<int64_t>& vf_off,
+                        std::vector<int32_t>& vf) {
+  int64_t nf = (int64_t)F.size() / 3;
+  vf_off.assign(nv + 1, 0);
+  for (int64_t i = 0; i < 3 * nf; ++i) vf_off[F[i] + 1]++;
+  for (int64_t v = 0; v < nv; ++v) vf_off[v + 1] += vf_off[v];
+  vf.resize(3 * nf);
+  std::vector<int64_t> cur(vf_off.begin(), vf_off.end() - 1);
+  for (int64_t f = 0; f < nf; ++f)
+    for (int k = 0; k < 3; ++k) vf[cur[F[3 * f + k]]++] = (int32_t)f;
+  // a face with a repeated vertex cannot occur after weld; faces per vertex stay ascending
+}
+
+EdgeFaces build_edge_faces(int64_t nv, const std::vector<int32_t>& F, int threads) {
+  int64_t nf = (int64_t)F.size() / 3;
+  std::vector<int64_t> vf_off;
+  std::vector<int32_t> vf;
+  build_vertex_faces(nv, F, vf_off, vf);
+  EdgeFaces ef;
+  std::vector<int32_t> cnt(3 * nf);
+  auto contains = [&](int32_t g, int32_t y) { return F[3 * g] == y || F[3 * g + 1] == y || F[3 * g + 2] == y; };
+  parallel_for((nf + 4095) / 4096, threads, [&](int64_t blk) {
+    int64_t f1 = std::min(nf, (blk + 1) * 4096);
+    for (int64_t f = blk * 4096; f < f1; ++f)
+      for (int k = 0; k < 3; ++k) {
+        int32_t x = F[3 * f + k], y = F[3 * f + (k + 1) % 3];
+        int32_t a = std::min(x, y), b = std::max(x, y);
+        int32_t c = 0;
+        for (int64_t q = vf_off[a]; q < vf_off[a + 1]; ++q)
+          if (contains(vf[q], b)) ++c;
+        cnt[3 * f + k] = c;
+      }
+  });
+  ef.off.assign(3 * nf + 1, 0);
+  for (int64_t i = 0; i < 3 * nf; ++i) ef.off[i + 1] = ef.off[i] + cnt[i];
+  ef.faces.resize(ef.off[3 * nf]);
+  parallel_for((nf + 4095) / 4096, threads, [&](int64_t blk) {
+    int64_t f1 = std::min(nf, (blk + 1) * 4096);
+    for (int64_t f = blk * 4096; f < f1; ++f)
+      for (int k = 0; k < 3; ++k) {
+        int32_t x = F[3 * f + k], y = F[3 * f + (k + 1) % 3];
+        int32_t a = std::min(x, y), b = std::max(x, y);
+        int64_t o = ef.off[3 * f + k];
+        for (int64_t q = vf_off[a]; q < vf_off[a + 1]; ++q)
+          if (contains(vf[q], b)) ef.faces[o++] = vf[q];
+      }
+  });
+  (void)nv;
+  return ef;
+}
+
+// ------------------------------------------------------------------ eig3 / tangent frame
+// lscm_eig.rs:13-66 — cyclic-by-largest Jacobi rotations on the 3x3 covariance.
+void jacobi_eig3(double a[3][3], double w[3], double v[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) v[i][j] = i == j ? 1.0 : 0.0;
+  for (int it = 0; it < 64; ++it) {
+    int p = 0, q = 1;
+    double off = std::fabs(a[0][1]);
+    if (std::fabs(a[0][2]) > off) {
+      off = std::fabs(a[0][2]);
+      p = 0;
+      q = 2;
+    }
+    if (std::fabs(a[1][2]) > off) {
+      off = std::fabs(a[1][2]);
+      p = 1;
+      q = 2;
+    }
+    if (off <= 1e-300) break;
+    double apq = a[p][q], app = a[p][p], aqq = a[q][q];
+    double th = 0.5 * std::atan2(2.0 * apq, app - aqq);
+    double c = std::cos(th), s = std::sin(th);
+    int r = 3 - p - q;  // the one index that is neither p nor q
+    double arp = c * a[r][p] + s * a[r][q];
+    double arq = -s * a[r][p] + c * a[r][q];
+    a[r][p] = a[p][r] = arp;
+    a[r][q] = a[q][r] = arq;
+    a[p][p] = c * c * app + 2.0 * s * c * apq + s * s * aqq;
+    a[q][q] = s * s * app - 2.0 * s * c * apq + c * c * aqq;
+    a[p][q] = a[q][p] = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      double vp = v[p][k], vq = v[q][k];
+      v[p][k] = c * vp - s * vq;
+      v[q][k] = s * vp + c * vq;
+    }
+  }
+  w[0] = a[0][0];
+  w[1] = a[1][1];
+  w[2] = a[2][2];
+}
+
+// lscm.rs:152-183 — projection on the two dominant principal directions.
+template <class Get>
+void pca_project(int64_t n, Get get, double* out_uv) {
+  if (n == 0) return;
+  D3 c{0.0, 0.0, 0.0};
+  for (int64_t i = 0; i < n; ++i) c = c + get(i);
+  c = c / (double)n;
+  double cm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int64_t i = 0; i < n; ++i) {
+    D3 d = get(i) - c;
+    double e[3] = {d.x, d.y, d.z};
+    for (int r = 0; r < 3; ++r)
+      for (int s = 0; s < 3; ++s) cm[r][s] += e[r] * e[s];
+  }
+  double w[3], v[3][3];
+  jacobi_eig3(cm, w, v);
+  int idx[3] = {0, 1, 2};
+  std::stable_sort(idx, idx + 3, [&](int a, int b) { return total_order_key(w[b]) < total_order_key(w[a]); });
+  D3 e1{v[0][idx[0]], v[1][idx[0]], v[2][idx[0]]};
+  D3 e2{v[0][idx[1]], v[1][idx[1]], v[2][idx[1]]};
+  for (int64_t i = 0; i < n; ++i) {
+    D3 d = get(i) - c;
+    out_uv[2 * i] = dot3(d, e1);
+    out_uv[2 * i + 1] = dot3(d, e2);
+  }
+}
+
+// lscm.rs:187-204 — clockwise perimeter point of a centred a x b rectangle.
+inline void rect_point(double f, double a, double b, double* uv) {
+  double per = 2.0 * (a + b);
+  double t = std::fmod(f, 1.0) * per;
+  if (t < a) {
+    uv[0] = a / 2.0 - t;
+    uv[1] = -b / 2.0;
+    return;
+  }
+  t -= a;
+  if (t < b) {
+    uv[0] = -a / 2.0;
+    uv[1] = -b / 2.0 + t;
+    return;
+  }
+  t -= b;
+  if (t < a) {
+    uv[0] = -a / 2.0 + t;
+    uv[1] = b / 2.0;
+    return;
+  }
+  t -= a;
+  uv[0] = a / 2.0;
+  uv[1] = b / 2.0 - t;
+}
+
+// ------------------------------------------------------------------ one chart
+struct ChartOut {
+  std::vector<int32_t> faces;      // source face ids, chart order
+  std::vector<int32_t> verts;      // sorted source vertex ids
+  std::vector<int32_t> tris;       // local
+  std::vector<int32_t> border;     // sorted source ids
+  std::vector<int64_t> loop_len;   // per loop
+  std::vector<int32_t> loop_ids;   // concatenated loops (source ids)
+  double area3d = 0.0;
+  std::vector<double> p3, p2, pin_uv;
+  std::vector<uint8_t> pinned;
+};
+
+struct MeshView {
+  const std::vector<D3>& pos;
+  const std::vector<int32_t>& F;
+  const EdgeFaces& ef;
+  const std::vector<uint8_t>& cut;   // per face slot
+  const std::vector<double>& farea;  // per face
+};
+
+inline bool slot_is_border(const MeshView& m, int64_t slot) {
+  return m.cut[slot] || (m.ef.off[slot + 1] - m.ef.off[slot]) == 1;
+}
+
+void build_chart(const MeshView& m, ChartOut& ch) {
+  const auto& F = m.F;
+  // vertex set (segment.rs:177-196)
+  ch.verts.clear();
+  ch.verts.reserve(ch.faces.size() * 3);
+  for (int32_t f : ch.faces)
+    for (int k = 0; k < 3; ++k) ch.verts.push_back(F[3 * f + k]);
+  std::sort(ch.verts.begin(), ch.verts.end());
+  ch.verts.erase(std::unique(ch.verts.begin(), ch.verts.end()), ch.verts.end());
+  auto local = [&](int32_t v) -> int32_t {
+    return (int32_t)(std::lower_bound(ch.verts.begin(), ch.verts.end(), v) - ch.verts.begin());
+  };
+  ch.tris.resize(ch.faces.size() * 3);
+  for (size_t t = 0; t < ch.faces.size(); ++t)
+    for (int k = 0; k < 3; ++k) ch.tris[3 * t + k] = local(F[3 * ch.faces[t] + k]);
+  // border vertices and boundary edge set (segment.rs:198-209, :235-244)
+  std::vector<uint64_t> bedges;
+  ch.border.clear();
+  for (int32_t f : ch.faces)
+    for (int k = 0; k < 3; ++k)
+      if (slot_is_border(m, 3 * (int64_t)f + k)) {
+        uint32_t x = (uint32_t)F[3 * f + k], y = (uint32_t)F[3 * f + (k + 1) % 3];
+        ch.border.push_back((int32_t)x);
+        ch.border.push_back((int32_t)y);
+        uint32_t a = std::min(x, y), b = std::max(x, y);
+        bedges.push_back(((uint64_t)a << 32) | b);
+      }
+  std::sort(ch.border.begin(), ch.border.end());
+  ch.border.erase(std::unique(ch.border.begin(), ch.border.end()), ch.border.end());
+  std::sort(bedges.begin(), bedges.end());
+  bedges.erase(std::unique(bedges.begin(), bedges.end()), bedges.end());
+  // area (segment.rs:212): sum in chart face order
+  double area = 0.0;
+  for (int32_t f : ch.faces) area += m.farea[f];
+  ch.area3d = area;
+  // border loops: keep-going-straight walk (segment.rs:245-330)
+  ch.loop_len.clear();
+  ch.loop_ids.clear();
+  if (!bedges.empty()) {
+    // adjacency over boundary vertices; neighbour lists come out ascending because the
+    // sorted edge list is scanned in order (segment.rs:249-255)
+    std::vector<int32_t> bv(ch.border);  // every endpoint of a boundary edge is a border vertex
+    auto bidx = [&](uint32_t v) { return (int64_t)(std::lower_bound(bv.begin(), bv.end(), (int32_t)v) - bv.begin()); };
+    std::vector<int64_t> aoff(bv.size() + 1, 0);
+    for (uint64_t e : bedges) {
+      aoff[bidx((uint32_t)(e >> 32)) + 1]++;
+      aoff[bidx((uint32_t)e) + 1]++;
+    }
+    for (size_t i = 0; i < bv.size(); ++i) aoff[i + 1] += aoff[i];
+    std::vector<int32_t> adj(aoff.back());
+    std::vector<int64_t> cur(aoff.begin(), aoff.end() - 1);
+    for (uint64_t e : bedges) {
+      uint32_t a = (uint32_t)(e >> 32), b = (uint32_t)e;
+      adj[cur[bidx(a)]++] = (int32_t)b;
+      adj[cur[bidx(b)]++] = (int32_t)a;
+    }
+    std::vector<uint8_t> used(bedges.size(), 0);
+    auto eidx = [&](uint32_t x, uint32_t y) {
+      uint32_t a = std::min(x, y), b = std::max(x, y);
+      uint64_t key = ((uint64_t)a << 32) | b;
+      return (int64_t)(std::lower_bound(bedges.begin(), bedges.end(), key) - bedges.begin());
+    };
+    std::vector<int32_t> walk, nxts;
+    for (size_t si = 0; si < bv.size(); ++si) {
+      uint32_t start = (uint32_t)bv[si];
+      if (aoff[si + 1] == aoff[si]) continue;
+      bool any_unused = false;
+      for (int64_t q = aoff[si]; q < aoff[si + 1]; ++q)
+        if (!used[eidx(start, (uint32_t)adj[q])]) any_unused = true;
+      if (!any_unused) continue;
+      walk.clear();
+      walk.push_back((int32_t)start);
+      uint32_t first = (uint32_t)adj[aoff[si]];  // smallest neighbour (lists are ascending)
+      for (int64_t q = aoff[si]; q < aoff[si + 1]; ++q) first = std::min(first, (uint32_t)adj[q]);
+      used[eidx(start, first)] = 1;
+      uint32_t prev = start, now = first;
+      walk.push_back((int32_t)now);
+      for (;;) {
+        int64_t ni = bidx(now);
+        nxts.clear();
+        for (int64_t q = aoff[ni]; q < aoff[ni + 1]; ++q) {
+          uint32_t n = (uint32_t)adj[q];
+          if (n != prev && !used[eidx(now, n)]) nxts.push_back((int32_t)n);
+        }
+        if (nxts.empty()) break;
+        D3 din = m.pos[now] - m.pos[prev];
+        double ln = norm3(din);
+        uint32_t next = (uint32_t)nxts[0];
+        if (!(ln < 1e-30)) {
+          din = din / ln;
+          bool have = false;
+          double best = 0.0;
+          for (int32_t n : nxts) {
+            double d = dot3(m.pos[n] - m.pos[now], din);
+            if (!have || !(d <= best)) {  // the first maximum wins (segment.rs:307-310)
+              have = true;
+              best = d;
+              next = (uint32_t)n;
+            }
+          }
+        }
+        used[eidx(now, next)] = 1;
+        prev = now;
+        now = next;
+        walk.push_back((int32_t)now);
+        if (now == start) break;
+      }
+      if (walk.size() >= 4) {
+        ch.loop_len.push_back((int64_t)walk.size());
+        ch.loop_ids.insert(ch.loop_ids.end(), walk.begin(), walk.end());
+      }
+    }
+  }
+  // positions and tangent frame (lscm.rs:513-516)
+  int64_t nv = (int64_t)ch.verts.size();
+  ch.p3.resize(3 * nv);
+  for (int64_t i = 0; i < nv; ++i) {
+    D3 p = m.pos[ch.verts[i]];
+    ch.p3[3 * i] = p.x;
+    ch.p3[3 * i + 1] = p.y;
+    ch.p3[3 * i + 2] = p.z;
+  }
+  ch.p2.resize(2 * nv);
+  pca_project(nv, [&](int64_t i) { return m.pos[ch.verts[i]]; }, ch.p2.data());
+  // pins (lscm.rs:524-542)
+  ch.pinned.assign(nv, 0);
+  ch.pin_uv.assign(2 * nv, 0.0);
+  if (ch.loop_len.empty()) {
+    // closed chart: 4 greedy farthest-point anchors pinned to their p2 (lscm.rs:210-247)
+    std::vector<int64_t> chosen;
+    if (nv <= 4) {
+      for (int64_t i = 0; i < nv; ++i) chosen.push_back(i);
+    } else {
+      double min_x = std::numeric_limits<double>::max();
+      for (int64_t i = 0; i < nv; ++i) min_x = fmin_rs(min_x, ch.p3[3 * i]);
+      int64_t s0 = 0;
+      for (int64_t i = 0; i < nv; ++i)
+        if (ch.p3[3 * i] == min_x) {
+          s0 = i;
+          break;
+        }
+      chosen.push_back(s0);
+      std::vector<double> dmin(nv, std::numeric_limits<double>::max());
+      while (chosen.size() < 4) {
+        int64_t c = chosen.back();
+        D3 pc{ch.p3[3 * c], ch.p3[3 * c + 1], ch.p3[3 * c + 2]};
+        for (int64_t i = 0; i < nv; ++i) {
+          D3 pi{ch.p3[3 * i], ch.p3[3 * i + 1], ch.p3[3 * i + 2]};
+          dmin[i] = fmin_rs(dmin[i], norm3(pi - pc));
+        }
+        int64_t best = 0;
+        double bd = std::numeric_limits<double>::lowest();
+        for (int64_t i = 0; i < nv; ++i) {
+          bool taken = std::find(chosen.begin(), chosen.end(), i) != chosen.end();
+          double d = taken ? -1.0 : dmin[i];
+          if (d > bd) {
+            bd = d;
+            best = i;
+          }
+        }
+        chosen.push_back(best);
+      }
+    }
+    for (int64_t i : chosen) {
+      ch.pinned[i] = 1;
+      ch.pin_uv[2 * i] = ch.p2[2 * i];
+      ch.pin_uv[2 * i + 1] = ch.p2[2 * i + 1];
+    }
+    return;
+  }
+  // border rectangle pass (lscm.rs:280-413); "last loop wins" for a vertex on two loops
+  size_t nl = ch.loop_len.size();
+  std::vector<int64_t> loff(nl + 1, 0);
+  for (size_t l = 0; l < nl; ++l) loff[l + 1] = loff[l] + ch.loop_len[l];
+  std::vector<std::vector<double>> fracs(nl);
+  std::vector<double> perim(nl);
+  for (size_t l = 0; l < nl; ++l) {
+    const int32_t* L = ch.loop_ids.data() + loff[l];
+    int64_t len = ch.loop_len[l];
+    std::vector<double> seg(len > 0 ? len - 1 : 0);
+    for (int64_t w = 0; w + 1 < len; ++w) seg[w] = norm3(m.pos[L[w + 1]] - m.pos[L[w]]);
+    double total = 0.0;
+    for (double s : seg) total += s;
+    perim[l] = total;
+    total = fmax_rs(total, 1e-30);
+    auto& fr = fracs[l];
+    fr.assign(1, 0.0);
+    for (double s : seg) fr.push_back(fr.back() + s);
+    for (double& x : fr) x /= total;
+  }
+  auto set_pin = [&](int32_t src, double u, double v) {
+    int32_t li = local(src);
+    ch.pinned[li] = 1;
+    ch.pin_uv[2 * li] = u;
+    ch.pin_uv[2 * li + 1] = v;
+  };
+  if (nl == 2) {
+    double pm = fmax_rs(fmax_rs(0.0, perim[0]), perim[1]);
+    if (std::fabs(perim[0] - perim[1]) <= 0.25 * pm) {
+      // cylinder strip (lscm.rs:305-338)
+      double w = 0.5 * (perim[0] + perim[1]);
+      double h = ch.area3d / fmax_rs(w, 1e-30);
+      auto strip_len = [&](size_t l) {
+        const int32_t* L = ch.loop_ids.data() + loff[l];
+        int64_t len = ch.loop_len[l];
+        return (len > 1 && L[0] == L[len - 1]) ? len - 1 : len;
+      };
+      int64_t n0 = strip_len(0), n1 = strip_len(1);
+      const int32_t* L0 = ch.loop_ids.data() + loff[0];
+      const int32_t* L1 = ch.loop_ids.data() + loff[1];
+      // pins is a map (later inserts overwrite): emulate by writing in reference order
+      for (int64_t k = 0; k < n0; ++k) set_pin(L0[k], -w / 2.0 + w * fracs[0][k], h / 2.0);
+      for (int64_t k1 = 0; k1 < n1; ++k1) {
+        D3 p1 = m.pos[L1[k1]];
+        int64_t best = 0;
+        double bd = std::numeric_limits<double>::infinity();
+        for (int64_t k0 = 0; k0 < n0; ++k0) {
+          double d = norm3(m.pos[L0[k0]] - p1);
+          if (d < bd) {
+            bd = d;
+            best = k0;
+          }
+        }
+        set_pin(L1[k1], -w / 2.0 + w * fracs[0][best], -h / 2.0);
+      }
+      return;
+    }
+  }
+  std::vector<double> sa(nl), sb(nl);
+  if (nl == 1) {
+    double p = perim[0], a = ch.area3d;
+    if (p * p >= 16.0 * a) {
+      double hs = p / 2.0;
+      double d = std::sqrt(fmax_rs(hs * hs - 4.0 * a, 0.0));
+      sa[0] = (hs + d) / 2.0;
+      sb[0] = (hs - d) / 2.0;
+    } else {
+      sa[0] = sb[0] = std::sqrt(a);
+    }
+  } else {
+    // multi-loop similarity scale (lscm.rs:351-384)
+    D3 c{0.0, 0.0, 0.0};
+    for (int32_t v : ch.verts) c = c + m.pos[v];
+    c = c / (double)std::max<int64_t>(nv, 1);
+    std::vector<double> dist(nl);
+    for (size_t l = 0; l < nl; ++l) {
+      double s = 0.0;
+      for (int64_t k = 0; k < ch.loop_len[l]; ++k) s += norm3(m.pos[ch.loop_ids[loff[l] + k]] - c);
+      dist[l] = s / (double)std::max<int64_t>(ch.loop_len[l], 1);
+    }
+    std::vector<size_t> order(nl);
+    for (size_t l = 0; l < nl; ++l) order[l] = l;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return total_order_key(dist[a]) < total_order_key(dist[b]); });
+    double denom = 0.0;
+    for (size_t k = 0; k < nl; ++k) {
+      double sign = ((nl - 1 - k) % 2 == 0) ? 1.0 : -1.0;
+      denom += sign * perim[order[k]] * perim[order[k]];
+    }
+    double s = 4.0 * std::sqrt(ch.area3d / fmax_rs(std::fabs(denom), 1e-30));
+    for (size_t l : order) sa[l] = sb[l] = s * perim[l] / 4.0;
+  }
+  std::vector<double> lp2;
+  for (size_t l = 0; l < nl; ++l) {
+    const int32_t* L = ch.loop_ids.data() + loff[l];
+    int64_t len = ch.loop_len[l];
+    bool closed = len > 1 && L[0] == L[len - 1];
+    int64_t nverts = closed ? len - 1 : len;
+    // winding of the 3-D walk in its own tangent frame (lscm.rs:394-406)
+    lp2.assign(2 * len, 0.0);
+    pca_project(len, [&](int64_t i) { return m.pos[L[i]]; }, lp2.data());
+    double sa3 = 0.0;
+    for (int64_t i = 0; i < len; ++i) {
+      int64_t j = (i + 1) % len;
+      sa3 += lp2[2 * i] * lp2[2 * j + 1] - lp2[2 * i + 1] * lp2[2 * j];
+    }
+    sa3 *= 0.5;
+    for (int64_t k = 0; k < nverts; ++k) {
+      double f = sa3 > 0.0 ? std::fmod(1.0 - fracs[l][k], 1.0) : fracs[l][k];
+      double uv[2];
+      rect_point(f, sa[l], sb[l], uv);
+      set_pin(L[k], uv[0], uv[1]);
+    }
+  }
+}
+
+void pack_charts(std::vector<ChartOut>& charts, Prepared& P) {
+  int64_t nc = (int64_t)charts.size();
+  P.vert_off.assign(nc + 1, 0);
+  P.tri_off.assign(nc + 1, 0);
+  P.border_off.assign(nc + 1, 0);
+  P.loop_off.assign(nc + 1, 0);
+  int64_t nloops = 0;
+  for (int64_t c = 0; c < nc; ++c) {
+    P.vert_off[c + 1] = P.vert_off[c] + (int64_t)charts[c].verts.size();
+    P.tri_off[c + 1] = P.tri_off[c] + (int64_t)charts[c].faces.size();
+    P.border_off[c + 1] = P.border_off[c] + (int64_t)charts[c].border.size();
+    nloops += (int64_t)charts[c].loop_len.size();
+    P.loop_off[c + 1] = nloops;
+  }
+  int64_t NV = P.vert_off[nc], NT = P.tri_off[nc];
+  P.vertex_ids.resize(NV);
+  P.face_ids.resize(NT);
+  P.tris.resize(3 * NT);
+  P.p3.resize(3 * NV);
+  P.p2.resize(2 * NV);
+  P.pin_uv.resize(2 * NV);
+  P.pinned.resize(NV);
+  P.border.resize(P.border_off[nc]);
+  P.area3d.resize(nc);
+  P.loop_seg.assign(nloops + 1, 0);
+  {
+    int64_t li = 0;
+    for (int64_t c = 0; c < nc; ++c)
+      for (int64_t len : charts[c].loop_len) {
+        P.loop_seg[li + 1] = P.loop_seg[li] + len;
+        ++li;
+      }
+  }
+  P.loop_ids.resize(P.loop_seg[nloops]);
+  parallel_for(nc, 0, [&](int64_t c) {
+    ChartOut& ch = charts[c];
+    int64_t v0 = P.vert_off[c], t0 = P.tri_off[c];
+    std::copy(ch.verts.begin(), ch.verts.end(), P.vertex_ids.begin() + v0);
+    std::copy(ch.faces.begin(), ch.faces.end(), P.face_ids.begin() + t0);
+    std::copy(ch.tris.begin(), ch.tris.end(), P.tris.begin() + 3 * t0);
+    std::copy(ch.p3.begin(), ch.p3.end(), P.p3.begin() + 3 * v0);
+    std::copy(ch.p2.begin(), ch.p2.end(), P.p2.begin() + 2 * v0);
+    std::copy(ch.pin_uv.begin(), ch.pin_uv.end(), P.pin_uv.begin() + 2 * v0);
+    std::copy(ch.pinned.begin(), ch.pinned.end(), P.pinned.begin() + v0);
+    std::copy(ch.border.begin(), ch.border.end(), P.border.begin() + P.border_off[c]);
+    if (!ch.loop_ids.empty()) std::copy(ch.loop_ids.begin(), ch.loop_ids.end(), P.loop_ids.begin() + P.loop_seg[P.loop_off[c]]);
+    P.area3d[c] = ch.area3d;
+    ChartOut().faces.swap(ch.faces);  // release per-chart memory early
+  });
+}
+
+std::vector<double> face_areas(const std::vector<D3>& pos, const std::vector<int32_t>& F, int threads) {
+  int64_t nf = (int64_t)F.size() / 3;
+  std::vector<double> a(nf);
+  parallel_for((nf + 8191) / 8192, threads, [&](int64_t blk) {
+    int64_t f1 = std::min(nf, (blk + 1) * 8192);
+    for (int64_t f = blk * 8192; f < f1; ++f) {
+      D3 e1 = pos[F[3 * f + 1]] - pos[F[3 * f]];
+      D3 e2 = pos[F[3 * f + 2]] - pos[F[3 * f]];
+      a[f] = 0.5 * norm3(cross(e1, e2));
+    }
+  });
+  return a;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ entry points
+ruv_status prepare_mesh(const double* pos, int64_t nv, const int32_t* faces, int64_t nf, double weld_tol,
+                        double angle_min_deg, int threads, Prepared& P, std::string& err) {
+  for (int64_t i = 0; i < 3 * nf; ++i)
+    if (faces[i] < 0 || faces[i] >= nv) {
+      err = "face index out of range";
+      return RUV_ERR_BAD_INPUT;
+    }
+  std::vector<D3> wpos;
+  std::vector<int32_t> F;
+  weld(pos, nv, faces, nf, weld_tol, wpos, F);
+  int64_t wnv = (int64_t)wpos.size(), wnf = (int64_t)F.size() / 3;
+  for (int64_t f = 0; f < wnf; ++f)
+    if (F[3 * f] == F[3 * f + 1] || F[3 * f + 1] == F[3 * f + 2] || F[3 * f] == F[3 * f + 2]) {
+      err = "degenerate face with a repeated vertex";  // only possible without welding
+      return RUV_ERR_BAD_INPUT;
+    }
+  P.mesh_pos.resize(3 * wnv);
+  for (int64_t i = 0; i < wnv; ++i) {
+    P.mesh_pos[3 * i] = wpos[i].x;
+    P.mesh_pos[3 * i + 1] = wpos[i].y;
+    P.mesh_pos[3 * i + 2] = wpos[i].z;
+  }
+  P.mesh_faces.assign(F.begin(), F.end());
+  EdgeFaces ef = build_edge_faces(wnv, F, threads);
+  // unit normals per face (segment.rs:104-117) and the cut flag per face slot
+  std::vector<D3> nrm(wnf);
+  parallel_for((wnf + 8191) / 8192, threads, [&](int64_t blk) {
+    int64_t f1 = std::min(wnf, (blk + 1) * 8192);
+    for (int64_t f = blk * 8192; f < f1; ++f) {
+      D3 a = wpos[F[3 * f]], b = wpos[F[3 * f + 1]], c = wpos[F[3 * f + 2]];
+      D3 n = cross(a - b, c - b);
+      double l = norm3(n);
+      nrm[f] = l < 1e-30 ? D3{0.0, 0.0, 1.0} : n / l;
+    }
+  });
+  double th = angle_min_deg * (kPi / 180.0);
+  std::vector<uint8_t> cut(3 * wnf, 0);
+  parallel_for((wnf + 8191) / 8192, threads, [&](int64_t blk) {
+    int64_t f1 = std::min(wnf, (blk + 1) * 8192);
+    for (int64_t s = blk * 8192 * 3; s < f1 * 3; ++s) {
+      int64_t cnt = ef.off[s + 1] - ef.off[s];
+      double ang;
+      if (cnt == 1)
+        ang = 0.0;
+      else if (cnt == 2) {
+        double d = dot3(nrm[ef.faces[ef.off[s]]], nrm[ef.faces[ef.off[s] + 1]]);
+        d = d < -1.0 ? -1.0 : (d > 1.0 ? 1.0 : d);
+        ang = std::acos(d);
+      } else
+        ang = kPi;
+      cut[s] = ang > th ? 1 : 0;
+    }
+  });
+  P.n_cut_slots = 0;
+  for (uint8_t c : cut) P.n_cut_slots += c;
+  // face components over non-cut edges, DFS stack order (segment.rs:150-175)
+  std::vector<uint8_t> seen(wnf, 0);
+  std::vector<ChartOut> charts;
+  std::vector<int32_t> stack;
+  for (int64_t f0 = 0; f0 < wnf; ++f0) {
+    if (seen[f0]) continue;
+    charts.emplace_back();
+    auto& comp = charts.back().faces;
+    stack.assign(1, (int32_t)f0);
+    seen[f0] = 1;
+    while (!stack.empty()) {
+      int32_t f = stack.back();
+      stack.pop_back();
+      comp.push_back(f);
+      for (int k = 0; k < 3; ++k) {
+        int64_t s = 3 * (int64_t)f + k;
+        if (cut[s]) continue;
+        for (int64_t q = ef.off[s]; q < ef.off[s + 1]; ++q) {
+          int32_t g = ef.faces[q];
+          if (!seen[g]) {
+            seen[g] = 1;
+            stack.push_back(g);
+          }
+        }
+      }
+    }
+  }
+  std::vector<double> farea = face_areas(wpos, F, threads);
+  MeshView mv{wpos, F, ef, cut, farea};
+  // biggest charts first for load balance; results land in their own slots
+  std::vector<int64_t> order(charts.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int64_t)i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t a, int64_t b) { return charts[a].faces.size() > charts[b].faces.size(); });
+  parallel_for((int64_t)charts.size(), threads, [&](int64_t i) { build_chart(mv, charts[order[i]]); });
+  pack_charts(charts, P);
+  (void)err;
+  return RUV_OK;
+}
+
+ruv_status prepare_patches(int64_t np, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
+                           const int32_t* tris, int threads, Prepared& P, std::string& err) {
+  if (np < 0 || vert_off[0] != 0 || tri_off[0] != 0) {
+    err = "offsets must start at 0";
+    return RUV_ERR_BAD_INPUT;
+  }
+  for (int64_t c = 0; c < np; ++c)
+    if (vert_off[c + 1] < vert_off[c] || tri_off[c + 1] < tri_off[c]) {
+      err = "offsets must be non-decreasing";
+      return RUV_ERR_BAD_INPUT;
+    }
+  int64_t NV = vert_off[np], NT = tri_off[np];
+  std::vector<D3> pos(NV);
+  for (int64_t i = 0; i < NV; ++i) pos[i] = {p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]};
+  std::vector<int32_t> F(3 * NT);
+  for (int64_t c = 0; c < np; ++c) {
+    int64_t nvc = vert_off[c + 1] - vert_off[c];
+    for (int64_t t = tri_off[c]; t < tri_off[c + 1]; ++t)
+      for (int k = 0; k < 3; ++k) {
+        int32_t v = tris[3 * t + k];
+        if (v < 0 || v >= nvc) {
+          err = "patch triangle index out of range";
+          return RUV_ERR_BAD_INPUT;
+        }
+        F[3 * t + k] = (int32_t)(vert_off[c] + v);
+      }
+    for (int64_t t = tri_off[c]; t < tri_off[c + 1]; ++t)
+      if (F[3 * t] == F[3 * t + 1] || F[3 * t + 1] == F[3 * t + 2] || F[3 * t] == F[3 * t + 2]) {
+        err = "degenerate patch triangle";
+        return RUV_ERR_BAD_INPUT;
+      }
+  }
+  P.mesh_pos.assign(p3, p3 + 3 * NV);
+  P.mesh_faces.assign(F.begin(), F.end());
+  EdgeFaces ef = build_edge_faces(NV, F, threads);
+  std::vector<uint8_t> cut(3 * NT, 0);  // no segmentation: only mesh-boundary edges are border
+  P.n_cut_slots = 0;
+  // faces of each patch in the reference's DFS pop order (segment.rs:150-175), so a
+  // connected patch gets exactly the chart the segmentation of that patch would produce
+  std::vector<ChartOut> charts(np);
+  std::vector<uint8_t> seen(NT, 0);
+  parallel_for(np, threads, [&](int64_t c) {
+    auto& comp = charts[c].faces;
+    comp.reserve(tri_off[c + 1] - tri_off[c]);
+    std::vector<int32_t> stack;
+    for (int64_t f0 = tri_off[c]; f0 < tri_off[c + 1]; ++f0) {
+      if (seen[f0]) continue;
+      stack.assign(1, (int32_t)f0);
+      seen[f0] = 1;
+      while (!stack.empty()) {
+        int32_t f = stack.back();
+        stack.pop_back();
+        comp.push_back(f);
+        for (int k = 0; k < 3; ++k) {
+          int64_t s = 3 * (int64_t)f + k;
+          for (int64_t q = ef.off[s]; q < ef.off[s + 1]; ++q) {
+            int32_t g = ef.faces[q];
+            if (!seen[g]) {
+              seen[g] = 1;
+              stack.push_back(g);
+            }
+          }
+        }
+      }
+    }
+  });
+  std::vector<double> farea = face_areas(pos, F, threads);
+  MeshView mv{pos, F, ef, cut, farea};
+  std::vector<int64_t> order(np);
+  for (int64_t i = 0; i < np; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t a, int64_t b) { return charts[a].faces.size() > charts[b].faces.size(); });
+  parallel_for(np, threads, [&](int64_t i) { build_chart(mv, charts[order[i]]); });
+  pack_charts(charts, P);
+  // a patch's vertices that no triangle uses would be dropped by the vertex set; require
+  // every patch vertex to be used so the packed layout equals the caller's
+  for (int64_t c = 0; c < np; ++c)
+    if (P.vert_off[c + 1] - P.vert_off[c] != vert_off[c + 1] - vert_off[c]) {
+      err = "patch " + std::to_string(c) + " has vertices no triangle uses";
+      return RUV_ERR_BAD_INPUT;
+    }
+  return RUV_OK;
+}
+
+}  // namespace ruv

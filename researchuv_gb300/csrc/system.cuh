@@ -1,0 +1,94 @@
+// The packed block-diagonal operator the batched solver works on, and the stages that
+// produce and consume it.
+#pragma once
+
+#include "common.cuh"
+
+namespace ruv {
+
+// One SPD block per chart, rows packed chart after chart (chart c owns rows
+// [chart_row[c], chart_row[c+1])).  For the LSCM path a row is a free vertex and the block is
+// the scalar cotangent Laplacian L of the chart: the reference's interleaved system is
+// A = L (x) I2 (u and v rows carry identical values), so the solver stores L once and
+// carries (u, v) as one 2-wide right-hand side.  For the generic drop-in (ruv_cg_solve) a
+// row is a scalar unknown and nrhs = 1.
+struct DevSystem {
+  int64_t n_charts = 0, n_rows = 0, nnz = 0;
+  int nrhs = 2;
+  int64_t* chart_row = nullptr;  // n_charts + 1 (device)
+  std::vector<int64_t> h_chart_row;
+  int32_t* row_ptr = nullptr;    // n_rows + 1
+  int32_t* cols = nullptr;       // nnz (global row ids)
+  double* vals = nullptr;        // nnz, FP64
+  float* vals32 = nullptr;       // nnz, FP32 copy for the mixed-precision inner loop
+  double* diag = nullptr;        // n_rows
+  double* b = nullptr;           // nrhs * n_rows
+};
+
+// Solver controls and per-chart outcome.
+struct SolveOpts {
+  ruv_precond precond = RUV_PRECOND_JACOBI;
+  ruv_precision precision = RUV_PREC_FP64;
+  double tol = 1e-12;
+  int64_t max_iter = 16384;
+};
+
+struct ChartResult {
+  int32_t status;
+  int32_t iters;
+  int32_t refinements;
+  double rel_res;
+};
+
+struct Ctx;
+
+// x (nrhs * n_rows, device) <- A^-1 b per chart.  Returns per-chart results (host).
+std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o);
+
+// Assembly of the LSCM systems of a batch on the device (see assemble.cu).
+struct DevBatch {
+  int64_t n_charts = 0, n_verts = 0, n_tris = 0;
+  int64_t* vert_off = nullptr;  // n_charts + 1
+  int64_t* tri_off = nullptr;
+  double* p3 = nullptr;         // 3 * n_verts
+  int32_t* tris = nullptr;      // 3 * n_tris, chart-local
+  uint8_t* pinned = nullptr;
+  double* pin_uv = nullptr;     // 2 * n_verts
+  double* p2 = nullptr;         // 2 * n_verts
+  // produced by assembly
+  int64_t* row_of = nullptr;    // n_verts + 1: exclusive count of free vertices (row id if free)
+  int32_t* row_vert = nullptr;  // n_rows: packed vertex of each row
+  std::vector<int64_t> h_vert_off;
+};
+
+void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix);
+
+// Damped driver update (unfold_chart's loop, lscm.rs:570-719) on the device: writes uv
+// (2 * n_verts) and per-chart driver iterations / err_accum.
+void driver_update(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x, int max_iter, double* uv,
+                   std::vector<int32_t>& iters, std::vector<double>& err_accum);
+
+struct Ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  Workspace ws;
+  PinnedHost pinned;
+  std::string last_error;
+  // the last batch's assembled system (for ruv_export_chart_system)
+  DevSystem last_sys;
+  bool have_last = false;
+  int lanes_per_row = 0;   // SpMV sub-warp width (0 = from the row-length profile)
+  int tile_rows = 256;     // rows per CTA tile
+  // the batch resident on the device (ruv_lscm_upload)
+  DevBatch resident;
+  bool have_batch = false;
+  bool have_uv = false;
+  double timings[3] = {0.0, 0.0, 0.0};
+  int64_t launches = 0;  // kernels enqueued by this context so far
+};
+
+// Standalone timing of the batched SpMV kernel on an assembled system (see ruv_bench_spmv).
+double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes);
+
+}  // namespace ruv

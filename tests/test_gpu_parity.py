@@ -1,0 +1,210 @@
+"""GPU parity: the sm_103a path against the oracle, through the C ABI (libruv.so).
+
+Bars (from the reference and the workload definitions):
+* CSR pattern, values and right-hand side of every chart: bit-identical to the reference's
+  Sparse::to_csr(2 nf) (unwrap/src/sparse.rs:69-84) as the oracle restates it.
+* UVs: FP64 PCG <= 1e-10 normalised max-abs vs the CPU LU (the small cube workload);
+  mixed precision <= 1e-6 vs FP64 LU; normalisation of unwrap/src/lscm.rs:749-758.
+* Driver iterations and err_accum as the reference driver computes them.
+* GpuSolver::cg_solve known answers (gpu/src/solver.rs:767-1109).
+"""
+import numpy as np
+import pytest
+
+import researchuv_gb300 as R
+from oracle import oracle as O
+from researchuv_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10   # FP64 PCG vs CPU LU (cube workload)
+MIXED_TOL = 1e-6   # FP32 inner CG + FP64 refinement vs FP64 LU
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return R.Context(0)
+
+
+def _solve_mesh(ctx, p, f, precision, weld_tol=1e-12, angle=30.0, lu_limit=6000):
+    P = O.Pipeline(p, f, weld_tol=weld_tol, angle_deg=angle, lu_limit=lu_limit)
+    C = R.prepare_mesh(p, f, weld_tol=weld_tol, angle_min_deg=angle)
+    assert C.n_charts == P.n_charts
+    res = R.unfold_charts(ctx, C, R.UnfoldOptions(precision=precision, precond=R.Precond.JACOBI))
+    return P, C, res
+
+
+def _check_system(ctx, P, c):
+    ref = P.chart(c)
+    rp, cols, vals, rhs = R.export_chart_system(ctx, c)
+    assert np.array_equal(rp, ref["csr_ptr"]), "CSR row pointers differ"
+    assert np.array_equal(cols, ref["csr_cols"]), "CSR pattern differs"
+    assert np.array_equal(vals.view(np.uint64), ref["csr_vals"].view(np.uint64)), "CSR values differ (bitwise)"
+    n2 = len(rp) - 1
+    assert np.array_equal(rhs, ref["rhs"][:n2]), "right-hand side differs"
+
+
+def test_cube_fp64_matches_cpu_lu(ctx):
+    p, f = O.cube(6)
+    P, C, res = _solve_mesh(ctx, p, f, R.Precision.FP64)
+    for c in range(P.n_charts):
+        _check_system(ctx, P, c)
+        ref = P.chart(c)
+        assert res[c].status == R.Status.OK
+        assert O.uv_error(res[c].uv, ref["uv"]) <= FP64_TOL
+        assert res[c].iters == ref["iters"] == 2
+        assert abs(res[c].err_accum - ref["err_accum"]) <= 1e-9 * abs(ref["err_accum"])
+
+
+@pytest.mark.parametrize("precision", [R.Precision.FP64, R.Precision.MIXED])
+def test_fixtures_match_cpu_lu(ctx, precision):
+    tol = FP64_TOL if precision == R.Precision.FP64 else MIXED_TOL
+    for name, (p, f) in [("grid32", O.grid(32, 32)), ("sphere", O.uv_sphere(48, 24)),
+                         ("annulus", O.torus_annulus(2.0, 0.7, 64, 40)), ("cylinder", O.cylinder(1.0, 2.0, 32, 16))]:
+        P, C, res = _solve_mesh(ctx, p, f, precision)
+        for c in range(P.n_charts):
+            _check_system(ctx, P, c)
+            ref = P.chart(c)
+            err = O.uv_error(res[c].uv, ref["uv"])
+            # sphere: closed chart, 4 anchors -> conditioning ~1e7; FP64 CG to 1e-12 rel-res
+            bound = tol if name != "sphere" else max(tol, 1e-6)
+            assert err <= bound, f"{name} chart {c}: uv error {err:.3e} > {bound:.1e}"
+            assert res[c].iters == ref["iters"]
+
+
+def test_reference_gpu_parity_grid32(ctx, known):
+    """unwrap/src/lscm.rs:733-760: GPU unfold of grid(32,32) within 1e-6 of the CPU solve."""
+    p, f = O.grid(32, 32)
+    P, C, res = _solve_mesh(ctx, p, f, R.Precision.MIXED)
+    assert O.uv_error(res[0].uv, P.chart(0)["uv"]) < known["gpu_parity"]["grid32x32"]["rel_max_abs_lt"]
+
+
+def test_batched_disks_match_fp64_lu(ctx):
+    vo, to, p3, tr = W.disks(48, t_min=50, t_max=5000, seed=11)
+    C = R.prepare_patches(vo, to, p3, tr)
+    res = R.unfold_charts(ctx, C, R.UnfoldOptions(precision=R.Precision.MIXED))
+    for c in range(len(vo) - 1):
+        P = O.Pipeline(p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]], weld_tol=0.0, lu_limit=0)
+        assert P.n_charts == 1
+        rp, cols, vals, rhs = R.export_chart_system(ctx, c)
+        ref = P.chart(0)
+        assert np.array_equal(cols, ref["csr_cols"]) and np.array_equal(vals, ref["csr_vals"])
+        uv_lu = P.superlu_uv(0)
+        assert res[c].status == R.Status.OK
+        assert O.uv_error(res[c].uv, uv_lu) <= MIXED_TOL
+
+
+def test_empty_and_fully_pinned_charts(ctx):
+    """A chart whose vertices are all pinned (a lone triangle) has nf = 0: UVs are the pins."""
+    p = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
+    f = np.array([[0, 1, 2]])
+    P = O.Pipeline(p, f)
+    C = R.prepare_mesh(p, f)
+    res = R.unfold_charts(ctx, C, R.UnfoldOptions())
+    assert res[0].status == R.Status.OK and res[0].n_free == 0
+    assert O.uv_error(res[0].uv, P.chart(0)["uv"]) == 0.0
+
+
+def test_repeatable_bitwise(ctx):
+    """Same batch twice -> bitwise identical UVs (deterministic reductions)."""
+    vo, to, p3, tr = W.disks(16, t_min=200, t_max=3000, seed=5)
+    C = R.prepare_patches(vo, to, p3, tr)
+    a = R.unfold_charts(ctx, C)
+    b = R.unfold_charts(ctx, C)
+    for x, y in zip(a, b):
+        assert np.array_equal(x.uv, y.uv)
+
+
+# ------------------------------------------------------------------ GpuSolver known answers
+def _lap1d(n):
+    vals, cols, rp = [], [], [0]
+    for i in range(n):
+        if i > 0:
+            vals.append(-1.0)
+            cols.append(i - 1)
+        vals.append(2.0)
+        cols.append(i)
+        if i + 1 < n:
+            vals.append(-1.0)
+            cols.append(i + 1)
+        rp.append(len(vals))
+    b = np.zeros(n)
+    b[0] = b[-1] = 1.0
+    return R.CsrMatrix(np.array(vals), np.array(cols), np.array(rp)), b
+
+
+def test_cg_laplacian_1d(known):
+    k = known["gpu_cg"]["laplacian_1d_4096"]
+    g = R.GpuSolver.global_()
+    a, b = _lap1d(k["n"])
+    x = g.cg_solve(a, b, k["max_iter"], k["tol"])
+    assert x is not None, g.last_error
+    assert np.abs(x - 1.0).max() < k["x_tol"]
+
+
+def test_cg_banded_500k(known):
+    k = known["gpu_cg"]["banded_500k"]
+    n, band = k["n"], k["band"]
+    i = np.arange(n)
+    rows, cols, vals = [], [], []
+    for d in range(band, 0, -1):
+        m = i >= d
+        rows.append(i[m]); cols.append(i[m] - d); vals.append(np.full(m.sum(), -0.25 / d))
+    rows.append(i); cols.append(i); vals.append(np.full(n, 4.0))
+    for d in range(1, band + 1):
+        m = i + d < n
+        rows.append(i[m]); cols.append(i[m] + d); vals.append(np.full(m.sum(), -0.25 / d))
+    r = np.concatenate(rows); c = np.concatenate(cols); v = np.concatenate(vals)
+    order = np.lexsort((c, r))
+    r, c, v = r[order], c[order], v[order]
+    rp = np.concatenate([[0], np.cumsum(np.bincount(r, minlength=n))])
+    a = R.CsrMatrix(v, c, rp)
+    b = (i % 97) * 0.01 + 1.0
+    x = R.GpuSolver.global_().cg_solve(a, b, k["max_iter"], k["tol"])
+    assert x is not None
+    for row in [0, n // 2, n - 1]:
+        s = sum(a.vals[q] * x[a.cols[q]] for q in range(a.row_ptr[row], a.row_ptr[row + 1]))
+        assert abs(s - b[row]) < k["row_check_tol"]
+
+
+def _poisson(side):
+    n = side * side
+    rows, cols, vals = [], [], []
+    for rr in range(side):
+        for cc in range(side):
+            i = rr * side + cc
+            for r2, c2 in [(rr - 1, cc), (rr, cc - 1)]:
+                if r2 >= 0 and c2 >= 0:
+                    rows.append(i); cols.append(r2 * side + c2); vals.append(-1.0)
+            rows.append(i); cols.append(i); vals.append(4.05 if i % 11 == 0 else 4.0)
+            for r2, c2 in [(rr + 1, cc), (rr, cc + 1)]:
+                if r2 < side and c2 < side:
+                    rows.append(i); cols.append(r2 * side + c2); vals.append(-1.0)
+    rp = np.concatenate([[0], np.cumsum(np.bincount(np.array(rows), minlength=n))])
+    return R.CsrMatrix(np.array(vals), np.array(cols), rp), (np.arange(n) % 97) * 0.01 + 1.0
+
+
+def test_cg_poisson_preconditioning(known):
+    k = known["gpu_cg"]["poisson_400"]
+    a, b = _poisson(400)
+    g = R.GpuSolver.global_()
+    x_none, it_none = g.cg_solve_precond(a, b, 100_000, k["tol"], R.Precond.NONE)
+    x_j, it_j = g.cg_solve_precond(a, b, 100_000, k["tol"], R.Precond.JACOBI)
+    n = a.rows()
+    for i in [0, n // 2, n - 1]:
+        assert abs(x_j[i] - x_none[i]) < k["x_agree_tol"]
+    assert it_j <= it_none
+
+
+def test_cg_mismatched_dimensions():
+    a, b = _lap1d(8)
+    assert R.GpuSolver.global_().cg_solve(a, b[:4], 10, 1e-10) is None
+
+
+def test_cg_not_converged_and_breakdown():
+    a, b = _lap1d(4096)
+    g = R.GpuSolver.global_()
+    assert g.cg_solve(a, b, 3, 1e-12) is None and "NOT_CONVERGED" in g.last_error
+    z = R.CsrMatrix(np.array([0.0, 0.0]), np.array([0, 1]), np.array([0, 1, 2]))
+    assert g.cg_solve(z, np.array([1.0, 1.0]), 10, 1e-12) is None and "BREAKDOWN" in g.last_error
+    assert g.cg_solve_precond(z, np.array([1.0, 1.0]), 10, 1e-12, R.Precond.JACOBI) is None
