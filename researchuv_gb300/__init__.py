@@ -75,6 +75,7 @@ SIGNATURES = {
     "ruv_lscm_download_uv": (ctypes.c_int, [_vp, _P(_f64)]),
     "ruv_last_timings": (_i32, [_vp, _P(_f64), _i32]),
     "ruv_kernel_launches": (_i64, [_vp]),
+    "ruv_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _P(_i32), _P(_i32), _P(_i32), _P(_f64)]),
     "ruv_bench_spmv": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _i32, _P(_f64), _P(_f64)]),
 }
 
@@ -443,3 +444,12 @@ def bench_spmv(ctx: Context, precision: Precision = Precision.MIXED, reps: int =
     ctx.check(lib().ruv_bench_spmv(ctx.h, int(precision), reps, n_buffers, ctypes.byref(ms), ctypes.byref(by)),
               "ruv_bench_spmv")
     return ms.value, by.value
+
+
+def autotune(ctx: Context, precision: Precision = Precision.MIXED, reps: int = 10):
+    """Pick the fastest SpMV launch shape on the last assembled batch; returns
+    (lanes_per_row, rows_in_flight, tile_rows, ms_per_launch)."""
+    l, u, t, ms = _i32(0), _i32(0), _i32(0), _f64(0)
+    ctx.check(lib().ruv_autotune(ctx.h, int(precision), reps, ctypes.byref(l), ctypes.byref(u), ctypes.byref(t),
+                                 ctypes.byref(ms)), "ruv_autotune")
+    return l.value, u.value, t.value, ms.value

@@ -1,6 +1,8 @@
 // C ABI (include/ruv.h): the drop-in for the reference's GpuSolver boundary
 // (gpu/src/solver.rs:104-565) and the batched unfold_chart solve (unwrap/src/lscm.rs:471-727).
 // Every entry point catches internally and reports a ruv_status; no exception crosses.
+#include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -101,6 +103,10 @@ ruv_status ruv_ctx_create(ruv_ctx** out, int32_t device) {
   if (!ctx) return RUV_ERR_OOM;
   ctx->c.device = device;
   ctx->c.sm_count = prop.multiProcessorCount;
+  // launch-shape overrides for the tuner (RUV_LPR, RUV_UNROLL, RUV_TILE_ROWS)
+  if (const char* e = std::getenv("RUV_LPR")) ctx->c.lanes_per_row = std::atoi(e);
+  if (const char* e = std::getenv("RUV_UNROLL")) ctx->c.unroll = std::atoi(e);
+  if (const char* e = std::getenv("RUV_TILE_ROWS")) ctx->c.tile_rows = std::max(32, std::atoi(e));
   if (cudaSetDevice(device) != cudaSuccess) return RUV_ERR_NO_DEVICE;
   if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) return RUV_ERR_LAUNCH;
   *out = ctx.release();
@@ -350,6 +356,21 @@ ruv_status ruv_bench_spmv(ruv_ctx* ctx, ruv_precision precision, int32_t reps, i
     double ms = bench_spmv(c, c.last_sys, precision == RUV_PREC_MIXED, reps, n_buffers, &bytes);
     if (ms_per_launch) *ms_per_launch = ms;
     if (bytes_per_launch) *bytes_per_launch = bytes;
+    return RUV_OK;
+  });
+}
+
+ruv_status ruv_autotune(ruv_ctx* ctx, ruv_precision precision, int32_t reps, int32_t* lanes_per_row,
+                        int32_t* rows_in_flight, int32_t* tile_rows, double* ms_per_launch) {
+  if (!ctx || reps <= 0) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    if (!c.have_last) return fail(ctx, RUV_ERR_BAD_INPUT, "no assembled batch on this context");
+    TuneResult t = autotune_spmv(c, c.last_sys, precision == RUV_PREC_MIXED, reps);
+    if (lanes_per_row) *lanes_per_row = t.lpr;
+    if (rows_in_flight) *rows_in_flight = t.unroll;
+    if (tile_rows) *tile_rows = t.tile_rows;
+    if (ms_per_launch) *ms_per_launch = t.ms;
     return RUV_OK;
   });
 }

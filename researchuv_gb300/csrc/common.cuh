@@ -125,7 +125,27 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // Block sum of up to NV values per thread; every thread gets the totals.  `sh` must hold
-// NV * 32 doubles.  Fixed combine order => bitwise reproducible for a fixed launch shape.
+// NV * 32 values.  Fixed combine order => bitwise reproducible for a fixed launch shape.
+// (GB300 runs FP64 at a small fraction of the FP32 rate: the per-element loops of the
+// FP32 solver reduce in float and widen once per tile.)
+template <int NV, class A>
+__device__ __forceinline__ void block_sum_t(A (&v)[NV], A* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[k * 32 + wid] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    A t = lane < nw ? sh[k * 32 + lane] : A(0);
+    v[k] = warp_sum(t);
+  }
+  __syncthreads();
+}
+
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;

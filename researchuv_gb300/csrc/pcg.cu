@@ -90,25 +90,37 @@ struct Tiles {
 };
 
 // ---------------------------------------------------------------- tile kernels
-// Initial state: x = 0, r = b, z = M^-1 r, p = z.  Partials: b.b, r.z, #zero diagonals.
+// Accumulator type of the per-element loops: float in the FP32 solver (GB300's FP64 pipe is
+// a small fraction of its FP32 rate, so FP64 appears only per tile and per chart), double in
+// the FP64 solver.
+
+// Inverse diagonal (Jacobi) once per solve: dinv in the solver's precision; zero diagonals
+// are counted so the chart can report a breakdown (precond.rs:595-611).
+template <class S>
+__global__ void __launch_bounds__(kTileThreads) k_dinv(int64_t n, const double* __restrict__ diag, S* __restrict__ dinv) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dinv[i] = diag[i] == 0.0 ? S(0) : S(1) / (S)diag[i];
+}
+
+// Initial state: x = 0, r = b, z = M^-1 r, p = z.  Partials (FP64, once per solve): b.b, r.z,
+// #zero diagonals.
 template <class S, int NR>
 __global__ void __launch_bounds__(kTileThreads) k_init(Tiles T, const double* __restrict__ b, const double* __restrict__ diag,
-                                                       int use_jacobi, double* __restrict__ x64, S* __restrict__ xs,
-                                                       S* __restrict__ r, S* __restrict__ z, S* __restrict__ p,
-                                                       double* __restrict__ part) {
+                                                       const S* __restrict__ dinv, int use_jacobi, double* __restrict__ x64,
+                                                       S* __restrict__ xs, S* __restrict__ r, S* __restrict__ z,
+                                                       S* __restrict__ p, double* __restrict__ part) {
   __shared__ double sh[3 * 32];
   int64_t t = blockIdx.x;
   double acc[3] = {0.0, 0.0, 0.0};
   for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
     V<double, NR> bv = ldv<double, NR>(b, i);
     V<S, NR> rv, zv, zero;
-    double d = diag[i];
-    if (d == 0.0) acc[2] += 1.0;
-    S dinv = use_jacobi ? (S)(1.0 / d) : (S)1.0;
+    if (diag[i] == 0.0) acc[2] += 1.0;
+    const S di = use_jacobi ? dinv[i] : S(1);
 #pragma unroll
     for (int k = 0; k < NR; ++k) {
       rv.c[k] = (S)bv.c[k];
-      zv.c[k] = rv.c[k] * dinv;
+      zv.c[k] = rv.c[k] * di;
       zero.c[k] = (S)0;
       acc[0] += bv.c[k] * bv.c[k];
       acc[1] += (double)rv.c[k] * (double)zv.c[k];
@@ -130,79 +142,118 @@ __global__ void __launch_bounds__(kTileThreads) k_init(Tiles T, const double* __
   }
 }
 
-// q = A p on the tile's rows (LPR lanes per row) fused with the partial p.q.
-template <class S, int NR, int LPR>
+// q = A p on the tile's rows fused with the partial p.q.  CSR-vector: LPR lanes per row,
+// each lane covering K = ceil(8 / LPR) entries in one unrolled sweep (rows of a mesh
+// Laplacian hold <= 8 entries almost always; longer rows finish in a remainder loop), U rows
+// per sub-warp in flight so a warp keeps U * K independent value/column loads and U * K
+// gathers outstanding.  Block-uniform trip counts keep every lane in the shuffles.
+template <class S, int NR, int LPR, int U>
 __global__ void __launch_bounds__(kTileThreads) k_spmv_pq(Tiles T, const ChartState* __restrict__ st,
                                                           const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
                                                           const S* __restrict__ vals, const S* __restrict__ p,
                                                           S* __restrict__ q, double* __restrict__ part) {
-  __shared__ double sh[32];
-  int64_t t = blockIdx.x;
+  constexpr int K = (8 + LPR - 1) / LPR;
+  __shared__ S sh[32];
+  const int64_t t = blockIdx.x;
   if (st[T.chart[t]].state != kActive) return;
   const int sub = threadIdx.x % LPR;
-  double acc[1] = {0.0};
+  const int rpp = kTileThreads / LPR;
+  S acc[1] = {S(0)};
   const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
-  // block-uniform trip count: every lane takes part in the sub-warp shuffles
-  for (int64_t base = beg; base < end; base += blockDim.x / LPR) {
-    const int64_t i = base + threadIdx.x / LPR;
-    const bool valid = i < end;
-    const int lo = valid ? row_ptr[i] : 0, hi = valid ? row_ptr[i + 1] : 0;
-    V<S, NR> s;
+  for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
+    int lo[U], hi[U];
 #pragma unroll
-    for (int k = 0; k < NR; ++k) s.c[k] = (S)0;
-    for (int e = lo + sub; e < hi; e += LPR) {
-      const S a = vals[e];
-      const V<S, NR> pv = ldv<S, NR>(p, cols[e]);
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      const bool valid = i < end;
+      lo[u] = valid ? row_ptr[i] : 0;
+      hi[u] = valid ? row_ptr[i + 1] : 0;
+    }
+    S av[U][K];
+    int cv[U][K];
 #pragma unroll
-      for (int k = 0; k < NR; ++k) s.c[k] += a * pv.c[k];
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int e = lo[u] + sub + k * LPR;
+        const bool in = e < hi[u];
+        av[u][k] = in ? vals[e] : S(0);
+        cv[u][k] = in ? cols[e] : -1;
+      }
+    V<S, NR> s[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int c = 0; c < NR; ++c) s[u].c[c] = S(0);
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (cv[u][k] >= 0) {
+          const V<S, NR> pv = ldv<S, NR>(p, cv[u][k]);
+#pragma unroll
+          for (int c = 0; c < NR; ++c) s[u].c[c] += av[u][k] * pv.c[c];
+        }
+      for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {  // rows longer than K * LPR
+        const S a = vals[e];
+        const V<S, NR> pv = ldv<S, NR>(p, cols[e]);
+#pragma unroll
+        for (int c = 0; c < NR; ++c) s[u].c[c] += a * pv.c[c];
+      }
     }
 #pragma unroll
-    for (int o = LPR / 2; o > 0; o >>= 1)
+    for (int u = 0; u < U; ++u)
 #pragma unroll
-      for (int k = 0; k < NR; ++k) s.c[k] += __shfl_xor_sync(0xffffffffu, s.c[k], o, LPR);
-    if (valid && sub == 0) {
-      stv<S, NR>(q, i, s);
-      const V<S, NR> pi = ldv<S, NR>(p, i);
+      for (int o = LPR / 2; o > 0; o >>= 1)
 #pragma unroll
-      for (int k = 0; k < NR; ++k) acc[0] += (double)pi.c[k] * (double)s.c[k];
+        for (int c = 0; c < NR; ++c) s[u].c[c] += __shfl_xor_sync(0xffffffffu, s[u].c[c], o, LPR);
+    if (sub == 0) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+        if (i < end) {
+          stv<S, NR>(q, i, s[u]);
+          const V<S, NR> pi = ldv<S, NR>(p, i);
+#pragma unroll
+          for (int c = 0; c < NR; ++c) acc[0] += pi.c[c] * s[u].c[c];
+        }
+      }
     }
   }
-  block_sum<1>(acc, sh);
-  if (threadIdx.x == 0) part[t] = acc[0];
+  block_sum_t<1, S>(acc, sh);
+  if (threadIdx.x == 0) part[t] = (double)acc[0];
 }
 
 // x += alpha p; r -= alpha q; z = M^-1 r.  Partials: r.r, r.z.
 template <class S, int NR>
 __global__ void __launch_bounds__(kTileThreads) k_update(Tiles T, const ChartState* __restrict__ st,
-                                                         const double* __restrict__ diag, int use_jacobi,
+                                                         const S* __restrict__ dinv, int use_jacobi,
                                                          S* __restrict__ x, S* __restrict__ r, S* __restrict__ z,
                                                          const S* __restrict__ p, const S* __restrict__ q,
                                                          double* __restrict__ part) {
-  __shared__ double sh[2 * 32];
+  __shared__ S sh[2 * 32];
   int64_t t = blockIdx.x;
   const ChartState& cs = st[T.chart[t]];
   if (cs.state != kActive) return;
   const S alpha = (S)cs.alpha;
-  double acc[2] = {0.0, 0.0};
+  S acc[2] = {S(0), S(0)};
   for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
     V<S, NR> xv = ldv<S, NR>(x, i), rv = ldv<S, NR>(r, i), pv = ldv<S, NR>(p, i), qv = ldv<S, NR>(q, i), zv;
-    const S dinv = use_jacobi ? (S)(1.0 / diag[i]) : (S)1;
+    const S di = use_jacobi ? dinv[i] : S(1);
 #pragma unroll
     for (int k = 0; k < NR; ++k) {
       xv.c[k] += alpha * pv.c[k];
       rv.c[k] -= alpha * qv.c[k];
-      zv.c[k] = rv.c[k] * dinv;
-      acc[0] += (double)rv.c[k] * (double)rv.c[k];
-      acc[1] += (double)rv.c[k] * (double)zv.c[k];
+      zv.c[k] = rv.c[k] * di;
+      acc[0] += rv.c[k] * rv.c[k];
+      acc[1] += rv.c[k] * zv.c[k];
     }
     stv<S, NR>(x, i, xv);
     stv<S, NR>(r, i, rv);
     stv<S, NR>(z, i, zv);
   }
-  block_sum<2>(acc, sh);
+  block_sum_t<2, S>(acc, sh);
   if (threadIdx.x == 0) {
-    part[2 * t] = acc[0];
-    part[2 * t + 1] = acc[1];
+    part[2 * t] = (double)acc[0];
+    part[2 * t + 1] = (double)acc[1];
   }
 }
 
@@ -251,7 +302,7 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
                                                                 const int32_t* __restrict__ row_ptr,
                                                                 const int32_t* __restrict__ cols,
                                                                 const double* __restrict__ vals, const double* __restrict__ b,
-                                                                const double* __restrict__ diag, int use_jacobi,
+                                                                const float* __restrict__ dinv, int use_jacobi,
                                                                 const double* __restrict__ x64, float* __restrict__ r,
                                                                 float* __restrict__ z, double* __restrict__ part) {
   __shared__ double sh[2 * 32];
@@ -280,15 +331,15 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
       for (int k = 0; k < NR; ++k) s.c[k] += __shfl_xor_sync(0xffffffffu, s.c[k], o, LPR);
     if (valid && sub == 0) {
       const V<double, NR> bv = ldv<double, NR>(b, i);
-      const double dinv = use_jacobi ? 1.0 / diag[i] : 1.0;
+      const float di = use_jacobi ? dinv[i] : 1.0f;
       V<float, NR> rv, zv;
 #pragma unroll
       for (int k = 0; k < NR; ++k) {
         double res = bv.c[k] - s.c[k];
         acc[0] += res * res;
         rv.c[k] = (float)res;
-        zv.c[k] = rv.c[k] * (float)dinv;
-        acc[1] += (double)rv.c[k] * (double)zv.c[k];
+        zv.c[k] = rv.c[k] * di;
+        acc[1] += (double)(rv.c[k] * zv.c[k]);
       }
       stv<float, NR>(r, i, rv);
       stv<float, NR>(z, i, zv);
@@ -459,23 +510,7 @@ struct TileTable {
   std::vector<int32_t> chart;
 };
 
-TileTable make_tiles(const std::vector<int64_t>& chart_row, int64_t tile_rows) {
-  TileTable T;
-  int64_t nc = (int64_t)chart_row.size() - 1;
-  T.chart_tile.assign(nc + 1, 0);
-  for (int64_t c = 0; c < nc; ++c) {
-    T.chart_tile[c] = (int64_t)T.chart.size();
-    for (int64_t a = chart_row[c]; a < chart_row[c + 1]; a += tile_rows) {
-      T.tab.push_back(a);
-      T.tab.push_back(std::min(a + tile_rows, chart_row[c + 1]));
-      T.chart.push_back((int32_t)c);
-    }
-  }
-  T.chart_tile[nc] = (int64_t)T.chart.size();
-  return T;
-}
-
-template <class S, int NR, int LPR>
+template <class S, int NR, int LPR, int U>
 void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st, int* n_active,
              std::vector<ChartState>& out) {
   cudaStream_t s = ctx.stream;
@@ -489,11 +524,18 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
   S* z = ws.get<S>("pcg.z", NR * NR_);
   S* p = ws.get<S>("pcg.p", NR * NR_);
   S* q = ws.get<S>("pcg.q", NR * NR_);
+  S* dinv = ws.get<S>("pcg.dinv", NR_);
+  float* dinv32 = mixed ? reinterpret_cast<float*>(dinv) : nullptr;
   double* part = ws.get<double>("pcg.part", 3 * NTL);
   const S* vals = mixed ? reinterpret_cast<const S*>(sys.vals32) : reinterpret_cast<const S*>(sys.vals);
   RUV_CUDA(cudaMemsetAsync(n_active, 0, sizeof(int), s));
+  if (NR_ > 0) {
+    k_dinv<S><<<div_up(NR_, kTileThreads), kTileThreads, 0, s>>>(NR_, sys.diag, dinv);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
   if (NTL > 0) {
-    k_init<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, sys.b, sys.diag, jac, x64, xs, r, z, p, part);
+    k_init<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, sys.b, sys.diag, dinv, jac, x64, xs, r, z, p, part);
     count_launches(1);
     RUV_LAUNCH_CHECK();
   }
@@ -504,23 +546,23 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
   RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   RUV_CUDA(cudaStreamSynchronize(s));
   if (*h_active > 0 && NTL > 0) {
-    // capture one iteration as a graph, replay it
+    // capture kCheckEvery iterations as one graph, replay it
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     RUV_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int rep = 0; rep < kCheckEvery; ++rep) {
-      k_spmv_pq<S, NR, LPR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, p, q, part);
+      k_spmv_pq<S, NR, LPR, U><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, p, q, part);
       k_chart_alpha<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, n_active);
-      k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.diag, jac, mixed ? xs : reinterpret_cast<S*>(x64),
-                                                             r, z, p, q, part);
+      k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, dinv, jac, mixed ? xs : reinterpret_cast<S*>(x64), r,
+                                                             z, p, q, part);
       if (!mixed) {
         k_chart_beta<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
       } else {
         k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
         k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, x64, reinterpret_cast<float*>(xs));
-        k_true_residual<NR, LPR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, sys.vals, sys.b,
-                                                                       sys.diag, jac, x64, reinterpret_cast<float*>(r),
-                                                                       reinterpret_cast<float*>(z), part);
+        k_true_residual<NR, 8><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, sys.vals, sys.b, dinv32,
+                                                                     jac, x64, reinterpret_cast<float*>(r),
+                                                                     reinterpret_cast<float*>(z), part);
         k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
       }
       k_direction<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
@@ -561,17 +603,25 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
   RUV_CUDA(cudaStreamSynchronize(s));
 }
 
+// The SpMV shape: lanes per row (LPR) and rows in flight per sub-warp (U).  Instantiated
+// for the shapes the tuner explores; see pick_shape.
+struct Shape {
+  int lpr, unroll;
+};
+
+#define RUV_SHAPES(X) X(2, 2) X(2, 4) X(4, 1) X(4, 2) X(4, 4) X(8, 1) X(8, 2) X(8, 4) X(16, 1) X(32, 1)
+
 template <class S, int NR>
-void dispatch_lpr(int lpr, Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st,
+void dispatch_pcg(Shape sh, Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st,
                   int* n_active, std::vector<ChartState>& out) {
-  switch (lpr) {
-    case 2: return run_pcg<S, NR, 2>(ctx, sys, x64, o, T, st, n_active, out);
-    case 4: return run_pcg<S, NR, 4>(ctx, sys, x64, o, T, st, n_active, out);
-    case 8: return run_pcg<S, NR, 8>(ctx, sys, x64, o, T, st, n_active, out);
-    case 16: return run_pcg<S, NR, 16>(ctx, sys, x64, o, T, st, n_active, out);
-    default: return run_pcg<S, NR, 32>(ctx, sys, x64, o, T, st, n_active, out);
-  }
+#define RUV_CASE(L, UU) \
+  if (sh.lpr == L && sh.unroll == UU) return run_pcg<S, NR, L, UU>(ctx, sys, x64, o, T, st, n_active, out);
+  RUV_SHAPES(RUV_CASE)
+#undef RUV_CASE
+  throw Error{RUV_ERR_BAD_INPUT, "unsupported SpMV shape"};
 }
+
+TileTable make_tiles(const std::vector<int64_t>& chart_row, int64_t tile_rows);
 
 Tiles upload_tiles(Ctx& ctx, const DevSystem& sys, const std::string& tag) {
   cudaStream_t s = ctx.stream;
@@ -585,19 +635,21 @@ Tiles upload_tiles(Ctx& ctx, const DevSystem& sys, const std::string& tag) {
     RUV_CUDA(cudaMemcpyAsync(d_chart, TT.chart.data(), sizeof(int32_t) * NTL, cudaMemcpyHostToDevice, s));
   }
   RUV_CUDA(cudaMemcpyAsync(d_ctile, TT.chart_tile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
-  // the host tables go out of scope: make sure the copies have been consumed
-  RUV_CUDA(cudaStreamSynchronize(s));
+  RUV_CUDA(cudaStreamSynchronize(s));  // the host tables go out of scope
   return Tiles{d_tab, d_chart, d_ctile, NTL};
 }
 
-// Lanes per row from the average row length: enough lanes to cover a typical row once.
-int pick_lpr(const Ctx& ctx, const DevSystem& sys) {
-  if (ctx.lanes_per_row > 0) return ctx.lanes_per_row;
+// SpMV shape: explicit (RUV_LPR / RUV_UNROLL via the context) or from the row-length
+// profile: enough lanes to cover a typical row once, then as many rows in flight as keep
+// 8 independent loads per lane.
+Shape pick_shape(const Ctx& ctx, const DevSystem& sys) {
   double avg = sys.n_rows > 0 ? (double)sys.nnz / (double)sys.n_rows : 1.0;
-  return avg <= 3 ? 2 : avg <= 6 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32;
+  int lpr = ctx.lanes_per_row > 0 ? ctx.lanes_per_row : (avg <= 5 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32);
+  int u = ctx.unroll > 0 ? ctx.unroll : (lpr <= 4 ? 2 : lpr == 8 ? 4 : 1);
+  return Shape{lpr, u};
 }
 
-template <class S, int NR, int LPR>
+template <class S, int NR, int LPR, int U>
 double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
   cudaStream_t s = ctx.stream;
   const int64_t N = sys.n_rows, NC = sys.n_charts;
@@ -612,8 +664,8 @@ double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
   }
   const S* vals = std::is_same<S, float>::value ? reinterpret_cast<const S*>(sys.vals32) : reinterpret_cast<const S*>(sys.vals);
   auto launch = [&](int k) {
-    k_spmv_pq<S, NR, LPR><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, ps[k % nbuf],
-                                                                qs[k % nbuf], part);
+    k_spmv_pq<S, NR, LPR, U><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, ps[k % nbuf],
+                                                                    qs[k % nbuf], part);
     count_launches(1);
   };
   for (int k = 0; k < 3; ++k) launch(k);
@@ -634,30 +686,75 @@ double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
 }
 
 template <class S, int NR>
-double time_spmv_lpr(int lpr, Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
-  switch (lpr) {
-    case 2: return time_spmv<S, NR, 2>(ctx, sys, T, reps, nbuf);
-    case 4: return time_spmv<S, NR, 4>(ctx, sys, T, reps, nbuf);
-    case 8: return time_spmv<S, NR, 8>(ctx, sys, T, reps, nbuf);
-    case 16: return time_spmv<S, NR, 16>(ctx, sys, T, reps, nbuf);
-    default: return time_spmv<S, NR, 32>(ctx, sys, T, reps, nbuf);
+double dispatch_time(Shape sh, Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
+#define RUV_CASE(L, UU) \
+  if (sh.lpr == L && sh.unroll == UU) return time_spmv<S, NR, L, UU>(ctx, sys, T, reps, nbuf);
+  RUV_SHAPES(RUV_CASE)
+#undef RUV_CASE
+  throw Error{RUV_ERR_BAD_INPUT, "unsupported SpMV shape"};
+}
+
+TileTable make_tiles(const std::vector<int64_t>& chart_row, int64_t tile_rows) {
+  TileTable T;
+  int64_t nc = (int64_t)chart_row.size() - 1;
+  T.chart_tile.assign(nc + 1, 0);
+  for (int64_t c = 0; c < nc; ++c) {
+    T.chart_tile[c] = (int64_t)T.chart.size();
+    for (int64_t a = chart_row[c]; a < chart_row[c + 1]; a += tile_rows) {
+      T.tab.push_back(a);
+      T.tab.push_back(std::min(a + tile_rows, chart_row[c + 1]));
+      T.chart.push_back((int32_t)c);
+    }
   }
+  T.chart_tile[nc] = (int64_t)T.chart.size();
+  return T;
 }
 
 }  // namespace
 
 double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes) {
   Tiles T = upload_tiles(ctx, sys, "bench");
-  const int lpr = pick_lpr(ctx, sys);
+  const Shape sh = pick_shape(ctx, sys);
   const double N = (double)sys.n_rows, NNZ = (double)sys.nnz, nr = (double)sys.nrhs;
   const double vb = mixed ? 4.0 : 8.0;
   if (bytes) *bytes = NNZ * (vb + 4.0) + (N + 1.0) * 4.0 + 2.0 * N * nr * vb;
   if (T.n == 0) return 0.0;
   if (sys.nrhs == 2)
-    return mixed ? time_spmv_lpr<float, 2>(lpr, ctx, sys, T, reps, n_buffers)
-                 : time_spmv_lpr<double, 2>(lpr, ctx, sys, T, reps, n_buffers);
-  return mixed ? time_spmv_lpr<float, 1>(lpr, ctx, sys, T, reps, n_buffers)
-               : time_spmv_lpr<double, 1>(lpr, ctx, sys, T, reps, n_buffers);
+    return mixed ? dispatch_time<float, 2>(sh, ctx, sys, T, reps, n_buffers)
+                 : dispatch_time<double, 2>(sh, ctx, sys, T, reps, n_buffers);
+  return dispatch_time<double, 1>(sh, ctx, sys, T, reps, n_buffers);
+}
+
+// Autotuner: time the batched SpMV for every instantiated (lanes per row, rows in flight)
+// shape and tile height on the assembled operator; keep the fastest in the context.
+TuneResult autotune_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps) {
+  TuneResult best{0, 0, 0, 1e30};
+  const int tiles[] = {128, 256, 512, 1024};
+  const Shape shapes[] = {
+#define RUV_SH(L, UU) Shape{L, UU},
+      RUV_SHAPES(RUV_SH)
+#undef RUV_SH
+  };
+  const int saved_tile = ctx.tile_rows;
+  for (int tr : tiles) {
+    ctx.tile_rows = tr;
+    Tiles T = upload_tiles(ctx, sys, "tune");
+    if (T.n == 0) break;
+    for (const Shape& sh : shapes) {
+      double ms = sys.nrhs == 2 ? (mixed ? dispatch_time<float, 2>(sh, ctx, sys, T, reps, 2)
+                                         : dispatch_time<double, 2>(sh, ctx, sys, T, reps, 2))
+                                : dispatch_time<double, 1>(sh, ctx, sys, T, reps, 2);
+      if (ms < best.ms) best = TuneResult{sh.lpr, sh.unroll, tr, ms};
+    }
+  }
+  if (best.lpr > 0) {
+    ctx.lanes_per_row = best.lpr;
+    ctx.unroll = best.unroll;
+    ctx.tile_rows = best.tile_rows;
+  } else {
+    ctx.tile_rows = saved_tile;
+  }
+  return best;
 }
 
 std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o) {
@@ -667,15 +764,15 @@ std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const So
   Tiles T = upload_tiles(ctx, sys, "pcg");
   ChartState* st = ctx.ws.get<ChartState>("pcg.state", NC);
   int* n_active = ctx.ws.get<int>("pcg.nactive", 1);
-  const int lpr = pick_lpr(ctx, sys);
+  const Shape sh = pick_shape(ctx, sys);
   std::vector<ChartState> out;
   const bool mixed = o.precision == RUV_PREC_MIXED;
   if (sys.nrhs == 2) {
-    if (mixed) dispatch_lpr<float, 2>(lpr, ctx, sys, x, o, T, st, n_active, out);
-    else dispatch_lpr<double, 2>(lpr, ctx, sys, x, o, T, st, n_active, out);
+    if (mixed) dispatch_pcg<float, 2>(sh, ctx, sys, x, o, T, st, n_active, out);
+    else dispatch_pcg<double, 2>(sh, ctx, sys, x, o, T, st, n_active, out);
   } else {
-    if (mixed) dispatch_lpr<float, 1>(lpr, ctx, sys, x, o, T, st, n_active, out);
-    else dispatch_lpr<double, 1>(lpr, ctx, sys, x, o, T, st, n_active, out);
+    // the generic drop-in (one scalar right-hand side) runs in FP64 as the reference does
+    dispatch_pcg<double, 1>(sh, ctx, sys, x, o, T, st, n_active, out);
   }
   std::vector<ChartResult> res(NC);
   for (int64_t c = 0; c < NC; ++c) {

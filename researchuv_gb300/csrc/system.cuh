@@ -79,6 +79,7 @@ struct Ctx {
   DevSystem last_sys;
   bool have_last = false;
   int lanes_per_row = 0;   // SpMV sub-warp width (0 = from the row-length profile)
+  int unroll = 0;          // SpMV rows in flight per sub-warp (0 = from the shape)
   int tile_rows = 256;     // rows per CTA tile
   // the batch resident on the device (ruv_lscm_upload)
   DevBatch resident;
@@ -90,5 +91,11 @@ struct Ctx {
 
 // Standalone timing of the batched SpMV kernel on an assembled system (see ruv_bench_spmv).
 double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes);
+
+struct TuneResult {
+  int lpr, unroll, tile_rows;
+  double ms;
+};
+TuneResult autotune_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps);
 
 }  // namespace ruv
