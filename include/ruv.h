@@ -85,6 +85,29 @@ ruv_status ruv_cg_solve(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const i
 ruv_status ruv_apply_ic0(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols,
                          const double* vals, const double* r, double* z_out);
 
+/* Variant of ruv_cg_solve that allocates nothing, for callers that cannot call cudaMalloc:
+ * code running inside a host application that owns all device memory through its own
+ * allocator or memory pool (a renderer, a game engine, a plugin host with a fixed budget),
+ * or code that must not trigger an allocation (and its implicit synchronisation) mid-frame.
+ * It has no counterpart in the reference.
+ *
+ * The caller passes DEVICE pointers for the system (row_ptr[n+1], cols[nnz], vals[nnz]),
+ * the right-hand side b[n] and the solution x[n]; the solver's own scratch (CG vectors,
+ * inverse diagonal, partial sums, solver state) lives in one fixed array compiled into the
+ * library, about 12.6 MB, which every GPU that loads the library holds until exit.  Systems
+ * with n > RUV_NOALLOC_MAX_ROWS are rejected with BAD_INPUT.  PRECOND_NONE or _JACOBI.
+ * Same stopping rule and statuses as ruv_cg_solve; work is enqueued on `stream` (a
+ * cudaStream_t, NULL = the legacy default stream) and the call returns after it finished.
+ * The first call on each device resolves the array's device address for that device: make
+ * that first call before any stream capture.  All calls share the one array, so calls that
+ * overlap on the GPU (other threads or streams at the same time) race and must be
+ * serialised by the caller.  An explanation of a non-OK status is written to msg
+ * (msg_len bytes, may be NULL). */
+#define RUV_NOALLOC_MAX_ROWS 262144
+ruv_status ruv_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                                const double* b, double* x, int64_t max_iter, double tol, ruv_precond pc,
+                                int64_t* iters_out, void* stream, char* msg, int32_t msg_len);
+
 /* ------------------------------------------------------------------ batched LSCM solve */
 
 /* All charts of a mesh, packed.  Chart c owns packed vertices [vert_off[c], vert_off[c+1])

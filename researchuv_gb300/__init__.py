@@ -75,6 +75,8 @@ SIGNATURES = {
     "ruv_lscm_download_uv": (ctypes.c_int, [_vp, _P(_f64)]),
     "ruv_last_timings": (_i32, [_vp, _P(_f64), _i32]),
     "ruv_kernel_launches": (_i64, [_vp]),
+    "ruv_cg_solve_noalloc": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _i64, _f64, ctypes.c_int, _P(_i64), _vp,
+                                            ctypes.c_char_p, _i32]),
     "ruv_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _P(_i32), _P(_i32), _P(_i32), _P(_f64)]),
     "ruv_bench_spmv": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _i32, _P(_f64), _P(_f64)]),
 }

@@ -24,6 +24,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <mutex>
 
 namespace ruv {
 namespace {
@@ -785,4 +787,210 @@ std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const So
   return res;
 }
 
+
+// ===================================================================== no-alloc CG
+// A variant of the FP64 PCG behind ruv_cg_solve for callers that cannot allocate device
+// memory: its scratch (the CG vectors, the inverse diagonal, tile partials, tile table and
+// solver state) lives in one file-scope __device__ array of fixed size instead of the
+// context workspace, the caller's device buffers hold the system and the solution, and
+// the host loop issues plain launches (no CUDA graph, no pinned staging).
+namespace {
+
+constexpr int64_t kNoAllocMaxRows = RUV_NOALLOC_MAX_ROWS;
+constexpr int kNoAllocTile = 256;
+constexpr int64_t kNoAllocMaxTiles = (kNoAllocMaxRows + kNoAllocTile - 1) / kNoAllocTile;
+
+struct NoAllocScratch {
+  double r[kNoAllocMaxRows], z[kNoAllocMaxRows], p[kNoAllocMaxRows], q[kNoAllocMaxRows];
+  double dinv[kNoAllocMaxRows], diag[kNoAllocMaxRows];
+  double part[3 * kNoAllocMaxTiles];
+  int64_t tab[2 * kNoAllocMaxTiles];
+  int64_t chart_tile[2];
+  int32_t tchart[kNoAllocMaxTiles];
+  ChartState st;
+  int32_t n_active;
+  int32_t bad;
+  int32_t nonfinite;
+};
+
+// Every GPU that loads the library holds this array (about 12.6 MB) until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+// Device addresses of g_noalloc_scratch, resolved once per device (host code may not use
+// the symbol's name as a device pointer).
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+__global__ void k_na_check_ptr(int32_t n, const int32_t* __restrict__ row_ptr, int32_t* __restrict__ bad) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && row_ptr[0] != 0) atomicExch(bad, 1);
+  if (i < n && row_ptr[i + 1] < row_ptr[i]) atomicExch(bad, 1);
+}
+
+// Column check, diagonal extraction (first entry on the diagonal, as CsrMatrix::row_get)
+// and the single-chart tile table.
+__global__ void k_na_setup(int32_t n, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
+                           const double* __restrict__ vals, NoAllocScratch* __restrict__ S) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    double d = 0.0;
+    bool found = false;
+    for (int32_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+      const int32_t c = cols[k];
+      if (c < 0 || c >= n) atomicExch(&S->bad, 2);
+      if (c == i && !found) {
+        d = vals[k];
+        found = true;
+      }
+    }
+    S->diag[i] = d;
+  }
+  const int64_t n_tiles = (n + kNoAllocTile - 1) / kNoAllocTile;
+  if (i < n_tiles) {
+    S->tab[2 * i] = i * kNoAllocTile;
+    S->tab[2 * i + 1] = min((int64_t)n, (i + 1) * kNoAllocTile);
+    S->tchart[i] = 0;
+  }
+  if (i == 0) {
+    S->chart_tile[0] = 0;
+    S->chart_tile[1] = n_tiles;
+  }
+}
+
+__global__ void k_na_nonfinite(int32_t n, const double* __restrict__ x, int32_t* __restrict__ flag) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && !isfinite(x[i])) atomicExch(flag, 1);
+}
+
+void na_message(char* msg, int32_t len, const char* text) {
+  if (msg && len > 0) {
+    std::snprintf(msg, (size_t)len, "%s", text);
+  }
+}
+
+template <int LPR, int U>
+void na_iterations(cudaStream_t s, NoAllocScratch* S, Tiles T, const int32_t* row_ptr, const int32_t* cols,
+                   const double* vals, double* x, int jac, int none, int64_t max_iter) {
+  k_spmv_pq<double, 1, LPR, U><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, &S->st, row_ptr, cols, vals, S->p, S->q,
+                                                                     S->part);
+  k_chart_alpha<<<1, kChartThreads, 0, s>>>(T, &S->st, S->part, &S->n_active);
+  k_update<double, 1><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, &S->st, S->dinv, jac, x, S->r, S->z, S->p, S->q, S->part);
+  k_chart_beta<<<1, kChartThreads, 0, s>>>(T, &S->st, S->part, none, max_iter, &S->n_active);
+  k_direction<double, 1><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, &S->st, S->z, S->p);
+}
+
+}  // namespace
 }  // namespace ruv
+
+extern "C" ruv_status ruv_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                                           const double* b, double* x, int64_t max_iter, double tol, ruv_precond pc,
+                                           int64_t* iters_out, void* stream, char* msg, int32_t msg_len) {
+  using namespace ruv;
+  if (n <= 0 || !row_ptr || !cols || !vals || !b || !x) {
+    na_message(msg, msg_len, "empty system or null device pointer");
+    return RUV_ERR_BAD_INPUT;
+  }
+  if ((int64_t)n > kNoAllocMaxRows) {
+    char buf[160];
+    std::snprintf(buf, sizeof(buf), "n = %d exceeds the no-alloc scratch maximum of %lld rows (RUV_NOALLOC_MAX_ROWS)",
+                  (int)n, (long long)kNoAllocMaxRows);
+    na_message(msg, msg_len, buf);
+    return RUV_ERR_BAD_INPUT;
+  }
+  if (pc != RUV_PRECOND_NONE && pc != RUV_PRECOND_JACOBI) {
+    na_message(msg, msg_len, "the no-alloc solve supports PRECOND_NONE and PRECOND_JACOBI");
+    return RUV_ERR_BAD_INPUT;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    cudaGetLastError();
+    na_message(msg, msg_len, "no current CUDA device");
+    return RUV_ERR_NO_DEVICE;
+  }
+  NoAllocScratch* S = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess || !ptr) {
+        cudaGetLastError();
+        na_message(msg, msg_len, "cudaGetSymbolAddress of the no-alloc scratch failed");
+        return RUV_ERR_NO_DEVICE;
+      }
+      g_noalloc_addr[dev] = ptr;
+    }
+    S = static_cast<NoAllocScratch*>(g_noalloc_addr[dev]);
+  }
+  auto launch_fail = [&](const char* what) {
+    cudaGetLastError();
+    na_message(msg, msg_len, what);
+    return RUV_ERR_LAUNCH;
+  };
+  // flags that must start at zero on every call (the scratch keeps the last call's contents)
+  if (cudaMemsetAsync(&S->n_active, 0, 3 * sizeof(int32_t), s) != cudaSuccess) return launch_fail("memset");
+  const unsigned grid_n = div_up((int64_t)n + 1, 256);
+  k_na_check_ptr<<<grid_n, 256, 0, s>>>(n, row_ptr, &S->bad);
+  int32_t flags[3] = {0, 0, 0};
+  if (cudaMemcpyAsync(flags, &S->n_active, sizeof(flags), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return launch_fail("row pointer check failed to run");
+  if (flags[1]) {
+    na_message(msg, msg_len, "row_ptr[0] != 0 or row_ptr not monotone");
+    return RUV_ERR_BAD_INPUT;
+  }
+  k_na_setup<<<grid_n, 256, 0, s>>>(n, row_ptr, cols, vals, S);
+  int32_t nnz = 0;
+  if (cudaMemcpyAsync(flags, &S->n_active, sizeof(flags), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(&nnz, row_ptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return launch_fail("set-up kernel failed");
+  if (flags[1]) {
+    na_message(msg, msg_len, "column index out of range");
+    return RUV_ERR_BAD_INPUT;
+  }
+  const int jac = pc == RUV_PRECOND_JACOBI ? 1 : 0, none = pc == RUV_PRECOND_NONE ? 1 : 0;
+  const int64_t n_tiles = (n + kNoAllocTile - 1) / kNoAllocTile;
+  Tiles T{S->tab, S->tchart, S->chart_tile, n_tiles};
+  k_dinv<double><<<div_up(n, kTileThreads), kTileThreads, 0, s>>>(n, S->diag, S->dinv);
+  k_init<double, 1><<<(unsigned)n_tiles, kTileThreads, 0, s>>>(T, b, S->diag, S->dinv, jac, x, nullptr, S->r, S->z, S->p,
+                                                               S->part);
+  k_chart_init<<<1, kChartThreads, 0, s>>>(T, &S->st, S->part, tol, none, &S->n_active);
+  const double avg = (double)nnz / (double)n;
+  const int lpr = avg <= 5 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32;
+  int64_t launched = 0;
+  for (;;) {
+    int32_t active = 0;
+    if (cudaMemcpyAsync(&active, &S->n_active, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return launch_fail("CG iteration failed");
+    if (active <= 0 || launched >= max_iter + kCheckEvery) break;
+    for (int k = 0; k < kCheckEvery; ++k) {
+      if (lpr == 4) na_iterations<4, 2>(s, S, T, row_ptr, cols, vals, x, jac, none, max_iter);
+      else if (lpr == 8) na_iterations<8, 4>(s, S, T, row_ptr, cols, vals, x, jac, none, max_iter);
+      else if (lpr == 16) na_iterations<16, 1>(s, S, T, row_ptr, cols, vals, x, jac, none, max_iter);
+      else na_iterations<32, 1>(s, S, T, row_ptr, cols, vals, x, jac, none, max_iter);
+    }
+    if (cudaGetLastError() != cudaSuccess) return launch_fail("CG kernel launch failed");
+    launched += kCheckEvery;
+  }
+  ChartState st;
+  k_na_nonfinite<<<div_up(n, 256), 256, 0, s>>>(n, x, &S->nonfinite);
+  if (cudaMemcpyAsync(&st, &S->st, sizeof(st), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(flags, &S->n_active, sizeof(flags), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return launch_fail("reading the solver state failed");
+  if (iters_out) *iters_out = st.iters;
+  if (st.status != RUV_OK) {
+    na_message(msg, msg_len, st.status == RUV_ERR_NOT_CONVERGED ? "CG did not converge within max_iter" : "CG breakdown");
+    return (ruv_status)st.status;
+  }
+  if (flags[2]) {
+    na_message(msg, msg_len, "non-finite solution");
+    return RUV_ERR_BREAKDOWN;
+  }
+  na_message(msg, msg_len, "");
+  return RUV_OK;
+}
