@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-single-chart", action="store_true")
+    ap.add_argument("--single-chart-sample", type=int, default=192)
     return ap.parse_args()
 
 
@@ -270,6 +272,44 @@ def run_reference(args, rank):
     print(json.dumps(line))
 
 
+def single_chart_baseline(ctx, vo, unknowns, batched_ms, n_sample):
+    """The measuring stick of the batched solve: plain single-chart FP64 GPU PCG, i.e. one
+    GpuSolver::cg_solve_precond call (FP64, Jacobi, tol 1e-12, the reference's defaults,
+    lscm.rs:492-501) per chart on that chart's interleaved CSR, sequentially, as the
+    reference's per-chart unfold would.  Timed on a size-stratified sample of charts and
+    scaled to the whole workload by unknowns (larger charts need more iterations per
+    unknown, so the scaling understates the full sequential time)."""
+    import researchuv_gb300 as R
+
+    sizes = np.diff(vo)
+    order = np.argsort(sizes)
+    idx = order[np.linspace(0, len(order) - 1, min(n_sample, len(order))).astype(int)]
+    systems = []
+    for c in idx:
+        rp, cols, vals, rhs = R.export_chart_system(ctx, int(c))
+        if len(rp) > 1:
+            systems.append((R.CsrMatrix(vals, cols, rp), rhs))
+    solver = R.GpuSolver.new()
+    for a, rhs in systems[:4]:  # warm-up
+        solver.cg_solve_precond(a, rhs, 16384, 1e-12, R.Precond.JACOBI)
+    t0 = time.perf_counter()
+    unk, iters, fails = 0, 0, 0
+    for a, rhs in systems:
+        r = solver.cg_solve_precond(a, rhs, 16384, 1e-12, R.Precond.JACOBI)
+        unk += a.rows()
+        if r is None:
+            fails += 1
+        else:
+            iters += r[1]
+    dt = time.perf_counter() - t0
+    full_ms = 1000.0 * dt * unknowns / max(unk, 1)
+    return {"ms_per_step_extrapolated": full_ms, "sample_charts": len(systems), "sample_unknowns": unk,
+            "sample_s": round(dt, 3), "sample_iters": iters, "failed": fails,
+            "batched_speedup": full_ms / batched_ms,
+            "what": "sequential ruv_cg_solve per chart (FP64 Jacobi PCG, host CSR in / x out), "
+                    "size-stratified sample scaled by unknowns"}
+
+
 # ------------------------------------------------------------------ GPU arm
 def main():
     args = parse()
@@ -367,6 +407,8 @@ def main():
         "gpu_launches": int(launches),
         "clocks": clock_info,
     }
+    if rank == 0 and not args.no_single_chart:
+        line["single_chart_fp64_pcg"] = single_chart_baseline(ctx, vo, unknowns, ms, args.single_chart_sample)
     if rank == 0 and not args.no_cpu_baseline and src[0] == "patches":
         base, err, n_err = cpu_baseline(src, uv, args.cpu_budget)
         line["cpu_baseline"] = base

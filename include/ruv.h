@@ -165,7 +165,8 @@ ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ru
 ruv_status ruv_lscm_download_uv(ruv_ctx* ctx, double* uv_out);
 
 /* Device time (ms, CUDA events on the context stream) of the phases of the last
- * ruv_lscm_solve_resident: [0] assembly, [1] batched PCG, [2] driver update.
+ * ruv_lscm_solve_resident: [0] assembly, [1] batched PCG, [2] driver update, [3] the
+ * preconditioner set-up inside [1] (AMG hierarchy; 0 otherwise).
  * Returns the number of values written (<= n). */
 int32_t ruv_last_timings(const ruv_ctx* ctx, double* ms, int32_t n);
 

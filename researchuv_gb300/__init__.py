@@ -434,9 +434,10 @@ def export_chart_system(ctx: Context, chart: int):
 
 
 def last_timings(ctx: Context):
-    """Device ms of [assembly, batched PCG, driver] of the last resident solve."""
-    out = (_f64 * 3)()
-    n = lib().ruv_last_timings(ctx.h, out, 3)
+    """Device ms of [assembly, batched PCG, driver, preconditioner set-up within PCG] of the
+    last resident solve."""
+    out = (_f64 * 4)()
+    n = lib().ruv_last_timings(ctx.h, out, 4)
     return [out[i] for i in range(n)]
 
 

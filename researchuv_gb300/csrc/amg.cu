@@ -1,0 +1,1206 @@
+// Aggregation AMG preconditioner for the batched solver, set up on the GPU
+// (the sm_103a counterpart of gpu/src/amg.rs:127-773 and precond.rs:439-498).
+//
+// Hierarchy.  Every level is one packed block-diagonal CSR over all charts (chart rows stay
+// contiguous, so aggregates never cross charts).  Per level and for every chart that is
+// still coarsening:
+//   * aggregation: two rounds of pairwise matching on |A| (each unmatched row proposes to
+//     its strongest unmatched neighbour, ties to the smaller index; mutual proposals pair
+//     up), first on rows, then on the pairs -> aggregates of <= 4 rows (the reference's
+//     size-4 target, amg.rs:245, with a parallel matching in place of its sequential scan);
+//   * prolongator: tentative (one 1 per row, Precond::Amg) or smoothed
+//     P = (I - omega D^-1 A) P_tent, omega = 2/3 (Precond::AmgSa, amg.rs:299-362);
+//   * Galerkin operator A_c = R (A P), R = P^T (amg.rs:384-429), each product row formed by
+//     a bounded, order-fixed accumulation (deterministic: no float atomics anywhere).
+// A chart stops coarsening once it has <= kDirect rows (or its aggregation stalls); its
+// last operator is factored densely (Cholesky, FP64 pivots, FP32 factor) by one CTA per
+// chart, the batched counterpart of the reference's exact coarse factor (amg.rs:46-50).
+//
+// Apply (one V(1,1) cycle, z = M^-1 r, FP32): down: x = w D^-1 b, t = b - A x (one fused
+// pass), b_c = R t; direct solves of every chart at its own last level (one CTA per chart);
+// up: x += P x_c, x' = x + w D^-1 (b - A x).  Charts whose CG has converged are skipped.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <memory>
+
+#include "system.cuh"
+
+namespace ruv {
+namespace {
+
+constexpr int kAmgThreads = 256;
+constexpr int kDirect = 64;       // rows at which a chart is solved directly
+constexpr int kMaxLevels = 16;
+constexpr float kOmega = 2.0f / 3.0f;
+constexpr int kPairRounds = 4;
+constexpr int kAccCap = 48;       // distinct keys per accumulated strength row (a heuristic)
+constexpr int kGalCap = 96;       // distinct keys per Galerkin product row (exact)
+constexpr int kPMaxRow = 8;       // smoothed prolongator row cap (own aggregate always kept)
+constexpr int64_t kLevelTile = 1024;  // rows per CTA tile in the V-cycle kernels
+
+__device__ __forceinline__ int64_t find_chart64(const int64_t* off, int64_t n_charts, int64_t i) {
+  int64_t lo = 0, hi = n_charts;
+  while (hi - lo > 1) {
+    int64_t mid = (lo + hi) >> 1;
+    if (off[mid] <= i) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Bounded accumulation of (key, value) products in arrival order; keys sorted at the end.
+template <int CAP>
+struct Acc {
+  int key[CAP];
+  float val[CAP];
+  int n = 0;
+  bool overflow = false;
+  __device__ __forceinline__ void add(int k, float v) {
+    for (int t = 0; t < n; ++t)
+      if (key[t] == k) {
+        val[t] += v;
+        return;
+      }
+    if (n < CAP) {
+      key[n] = k;
+      val[n] = v;
+      ++n;
+    } else {
+      overflow = true;
+    }
+  }
+  __device__ __forceinline__ void sort() {
+    for (int i = 1; i < n; ++i) {
+      int k = key[i];
+      float v = val[i];
+      int j = i - 1;
+      while (j >= 0 && key[j] > k) {
+        key[j + 1] = key[j];
+        val[j + 1] = val[j];
+        --j;
+      }
+      key[j + 1] = k;
+      val[j + 1] = v;
+    }
+  }
+};
+
+// ---------------------------------------------------------------- setup kernels
+// Row -> chart and whether the chart keeps coarsening at this level.
+__global__ void k_row_chart(int64_t n, const int64_t* __restrict__ chart_row, int64_t n_charts,
+                            const int32_t* __restrict__ cont, int32_t* __restrict__ row_chart,
+                            uint8_t* __restrict__ active) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int64_t c = find_chart64(chart_row, n_charts, i);
+  row_chart[i] = (int32_t)c;
+  active[i] = cont[c] ? 1 : 0;
+}
+
+// Pairwise matching, proposal: strongest unmatched neighbour (|a_ij|, ties to smaller j).
+__global__ void k_propose(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                          const float* __restrict__ vals, const uint8_t* __restrict__ active,
+                          const int32_t* __restrict__ mate, int32_t* __restrict__ prop) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int32_t best = -1;
+  if (active[i] && mate[i] < 0) {
+    float bs = -1.0f;
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+      int32_t j = cols[e];
+      if (j == i || mate[j] >= 0) continue;
+      float s = fabsf(vals[e]);
+      if (s > bs || (s == bs && j < best)) {
+        bs = s;
+        best = j;
+      }
+    }
+  }
+  prop[i] = best;
+}
+
+__global__ void k_accept(int64_t n, const int32_t* __restrict__ prop, int32_t* __restrict__ mate) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int32_t j = prop[i];
+  if (j > i && prop[j] == (int32_t)i) {
+    mate[i] = j;
+    mate[j] = (int32_t)i;
+  }
+}
+
+// Lead row of each active row after pairing: its pair's smaller row; an unmatched row joins
+// the pair of its strongest matched neighbour (|a_ij|, ties to the smaller j), or stays
+// alone when it has none.  Every row ends in a group, so coarsening cannot stall.
+__global__ void k_row_lead(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                           const float* __restrict__ vals, const uint8_t* __restrict__ active,
+                           const int32_t* __restrict__ mate, int32_t* __restrict__ lead_row, uint8_t* __restrict__ lead) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!active[i]) {
+    lead[i] = 0;
+    return;
+  }
+  int32_t L;
+  if (mate[i] >= 0) {
+    L = min((int32_t)i, mate[i]);
+  } else {
+    int32_t best = -1;
+    float bs = -1.0f;
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+      const int32_t j = cols[e];
+      if (j == i || mate[j] < 0) continue;
+      const float sj = fabsf(vals[e]);
+      if (sj > bs || (sj == bs && j < best)) {
+        bs = sj;
+        best = j;
+      }
+    }
+    L = best >= 0 ? min(best, mate[best]) : (int32_t)i;
+  }
+  lead_row[i] = L;
+  lead[i] = L == (int32_t)i ? 1 : 0;
+}
+
+__global__ void k_group_of(int64_t n, const uint8_t* __restrict__ active, const int32_t* __restrict__ lead_row,
+                           const int64_t* __restrict__ gid, int32_t* __restrict__ grp_of, int32_t* __restrict__ gcnt) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !active[i]) return;
+  const int32_t g = (int32_t)gid[lead_row[i]];
+  grp_of[i] = g;
+  atomicAdd(&gcnt[g], 1);
+}
+
+__global__ void k_group_scatter(int64_t n, const uint8_t* __restrict__ active, const int32_t* __restrict__ grp_of,
+                                const int64_t* __restrict__ goff, int32_t* __restrict__ cursor, int32_t* __restrict__ mem) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !active[i]) return;
+  const int32_t g = grp_of[i];
+  mem[goff[g] + atomicAdd(&cursor[g], 1)] = (int32_t)i;
+}
+
+__global__ void k_sort_members(int64_t ng, const int64_t* __restrict__ goff, int32_t* __restrict__ mem) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  for (int64_t a = goff[g] + 1; a < goff[g + 1]; ++a) {
+    int32_t k = mem[a];
+    int64_t j = a - 1;
+    while (j >= goff[g] && mem[j] > k) {
+      mem[j + 1] = mem[j];
+      --j;
+    }
+    mem[j + 1] = k;
+  }
+}
+
+// Strengths from group g to its neighbour groups (sum of |a| between members), in member
+// and entry order.  Only groups passing `want(h)` are accumulated.
+template <class Want>
+__device__ __forceinline__ void group_strengths(int64_t g, const int64_t* goff, const int32_t* mem, const int32_t* rp,
+                                                const int32_t* cols, const float* vals, const int32_t* grp_of,
+                                                Acc<kAccCap>& acc, Want want) {
+  for (int64_t a = goff[g]; a < goff[g + 1]; ++a) {
+    const int32_t i = mem[a];
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+      const int32_t h = grp_of[cols[e]];
+      if (h == (int32_t)g || !want(h)) continue;
+      acc.add(h, fabsf(vals[e]));
+    }
+  }
+}
+
+// Second matching level, on groups: propose to the strongest unmatched neighbour group.
+__global__ void k_propose2(int64_t ng, const int64_t* __restrict__ goff, const int32_t* __restrict__ mem,
+                           const int32_t* __restrict__ rp, const int32_t* __restrict__ cols, const float* __restrict__ vals,
+                           const int32_t* __restrict__ grp_of, const int32_t* __restrict__ gmate,
+                           int32_t* __restrict__ prop, int* __restrict__ stats) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  int32_t best = -1;
+  if (gmate[g] < 0) {
+    Acc<kAccCap> acc;
+    group_strengths(g, goff, mem, rp, cols, vals, grp_of, acc, [&](int32_t h) { return gmate[h] < 0; });
+    atomicMax(stats + 2, acc.n);
+    float bs = -1.0f;
+    for (int t = 0; t < acc.n; ++t)
+      if (acc.val[t] > bs || (acc.val[t] == bs && acc.key[t] < best)) {
+        bs = acc.val[t];
+        best = acc.key[t];
+      }
+  }
+  prop[g] = best;
+}
+
+// Lead group of each group after pairing groups (unmatched groups join the pair of their
+// strongest matched neighbour group).
+__global__ void k_group_lead(int64_t ng, const int64_t* __restrict__ goff, const int32_t* __restrict__ mem,
+                             const int32_t* __restrict__ rp, const int32_t* __restrict__ cols, const float* __restrict__ vals,
+                             const int32_t* __restrict__ grp_of, const int32_t* __restrict__ gmate,
+                             int32_t* __restrict__ glead_of, uint8_t* __restrict__ glead) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  int32_t L;
+  if (gmate[g] >= 0) {
+    L = min((int32_t)g, gmate[g]);
+  } else {
+    Acc<kAccCap> acc;
+    group_strengths(g, goff, mem, rp, cols, vals, grp_of, acc, [&](int32_t h) { return gmate[h] >= 0; });
+    int32_t best = -1;
+    float bs = -1.0f;
+    for (int t = 0; t < acc.n; ++t)
+      if (acc.val[t] > bs || (acc.val[t] == bs && acc.key[t] < best)) {
+        bs = acc.val[t];
+        best = acc.key[t];
+      }
+    L = best >= 0 ? min(best, gmate[best]) : (int32_t)g;
+  }
+  glead_of[g] = L;
+  glead[g] = L == (int32_t)g ? 1 : 0;
+}
+
+// agg[i] = coarse row of row i (aggregates numbered in lead-group order).
+__global__ void k_agg(int64_t n, const uint8_t* __restrict__ active, const int32_t* __restrict__ grp_of,
+                      const int32_t* __restrict__ glead_of, const int64_t* __restrict__ aid, int32_t* __restrict__ agg) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  agg[i] = active[i] ? (int32_t)aid[glead_of[grp_of[i]]] : -1;
+}
+
+// Prolongator rows.  MODE 0: count, MODE 1: fill.  Tentative: one 1 at agg[i].  Smoothed:
+// row i = e_agg[i] - w/d_i * sum_j a_ij e_agg[j] (amg.rs:308-362), truncated to its kPMaxRow
+// largest entries with the own aggregate always kept (amg.rs:331-356), keys ascending.
+template <int MODE>
+__global__ void k_prolong(int64_t n, const uint8_t* __restrict__ active, const int32_t* __restrict__ rp,
+                          const int32_t* __restrict__ cols, const float* __restrict__ vals,
+                          const float* __restrict__ dinv, const int32_t* __restrict__ agg, int smooth,
+                          int32_t* __restrict__ cnt, const int64_t* __restrict__ off, int32_t* __restrict__ pc,
+                          float* __restrict__ pv, int* __restrict__ overflow) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!active[i]) {
+    if (MODE == 0) cnt[i] = 0;
+    return;
+  }
+  Acc<kAccCap> acc;
+  acc.add(agg[i], 1.0f);
+  if (smooth) {
+    const float wd = kOmega * dinv[i];
+    for (int e = rp[i]; e < rp[i + 1]; ++e) acc.add(agg[cols[e]], -wd * vals[e]);
+    if (acc.n > kPMaxRow) {
+      // keep the own aggregate (slot 0) and the kPMaxRow - 1 largest magnitudes (ties to the
+      // smaller column): selection by repeated maximum, then compaction
+      bool keep[kAccCap];
+      for (int t = 0; t < acc.n; ++t) keep[t] = t == 0;
+      for (int k = 1; k < kPMaxRow; ++k) {
+        int bt = -1;
+        for (int t = 1; t < acc.n; ++t) {
+          if (keep[t]) continue;
+          if (bt < 0 || fabsf(acc.val[t]) > fabsf(acc.val[bt]) ||
+              (fabsf(acc.val[t]) == fabsf(acc.val[bt]) && acc.key[t] < acc.key[bt]))
+            bt = t;
+        }
+        keep[bt] = true;
+      }
+      int m = 0;
+      for (int t = 0; t < acc.n; ++t)
+        if (keep[t]) {
+          acc.key[m] = acc.key[t];
+          acc.val[m] = acc.val[t];
+          ++m;
+        }
+      acc.n = m;
+    }
+    acc.sort();
+  }
+  if (acc.overflow) atomicExch(overflow, 1);
+  atomicMax(overflow + 3, acc.n);
+  if (MODE == 0) {
+    cnt[i] = acc.n;
+  } else {
+    int64_t at = off[i];
+    for (int t = 0; t < acc.n; ++t) {
+      pc[at + t] = acc.key[t];
+      pv[at + t] = acc.val[t];
+    }
+  }
+}
+
+// Transpose (R = P^T): counts per coarse row, then a stable scatter by fine row order.
+__global__ void k_count_cols(int64_t nnz, const int32_t* __restrict__ pc, int32_t* __restrict__ cnt) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nnz) atomicAdd(&cnt[pc[e]], 1);
+}
+
+__global__ void k_scatter_t(int64_t n, const int64_t* __restrict__ poff, const int32_t* __restrict__ pc,
+                            const float* __restrict__ pv, const int64_t* __restrict__ roff,
+                            int32_t* __restrict__ cursor, int32_t* __restrict__ rc, float* __restrict__ rv) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int64_t e = poff[i]; e < poff[i + 1]; ++e) {
+    int32_t c = pc[e];
+    int64_t at = roff[c] + atomicAdd(&cursor[c], 1);
+    rc[at] = (int32_t)i;
+    rv[at] = pv[e];
+  }
+}
+
+// Sort each row of R by fine row (deterministic order after the atomic scatter).
+__global__ void k_sort_rows(int64_t n, const int64_t* __restrict__ off, int32_t* __restrict__ c, float* __restrict__ v) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  for (int64_t i = off[r] + 1; i < off[r + 1]; ++i) {
+    int32_t k = c[i];
+    float x = v[i];
+    int64_t j = i - 1;
+    while (j >= off[r] && c[j] > k) {
+      c[j + 1] = c[j];
+      v[j + 1] = v[j];
+      --j;
+    }
+    c[j + 1] = k;
+    v[j + 1] = x;
+  }
+}
+
+// W = A P (rows of active fine rows).  MODE 0 count / 1 fill.
+template <int MODE>
+__global__ void k_ap(int64_t n, const uint8_t* __restrict__ active, const int32_t* __restrict__ rp,
+                     const int32_t* __restrict__ cols, const float* __restrict__ vals, const int64_t* __restrict__ poff,
+                     const int32_t* __restrict__ pc, const float* __restrict__ pv, int32_t* __restrict__ cnt,
+                     const int64_t* __restrict__ woff, int32_t* __restrict__ wc, float* __restrict__ wv,
+                     int* __restrict__ overflow) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!active[i]) {
+    if (MODE == 0) cnt[i] = 0;
+    return;
+  }
+  Acc<kGalCap> acc;
+  for (int e = rp[i]; e < rp[i + 1]; ++e) {
+    const int32_t j = cols[e];
+    const float a = vals[e];
+    for (int64_t q = poff[j]; q < poff[j + 1]; ++q) acc.add(pc[q], a * pv[q]);
+  }
+  if (acc.overflow) atomicExch(overflow, 1);
+  atomicMax(overflow + 4, acc.n);
+  acc.sort();
+  if (MODE == 0) {
+    cnt[i] = acc.n;
+  } else {
+    int64_t at = woff[i];
+    for (int t = 0; t < acc.n; ++t) {
+      wc[at + t] = acc.key[t];
+      wv[at + t] = acc.val[t];
+    }
+  }
+}
+
+// A_c = R W (coarse rows).  MODE 0 count / 1 fill (also the coarse diagonal inverse).
+template <int MODE>
+__global__ void k_rw(int64_t nc, const int64_t* __restrict__ roff, const int32_t* __restrict__ rc,
+                     const float* __restrict__ rv, const int64_t* __restrict__ woff, const int32_t* __restrict__ wc,
+                     const float* __restrict__ wv, int32_t* __restrict__ cnt, const int64_t* __restrict__ aoff,
+                     int32_t* __restrict__ ac, float* __restrict__ av, float* __restrict__ adinv,
+                     int* __restrict__ overflow) {
+  int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= nc) return;
+  Acc<kGalCap> acc;
+  for (int64_t q = roff[I]; q < roff[I + 1]; ++q) {
+    const int32_t i = rc[q];
+    const float r = rv[q];
+    for (int64_t e = woff[i]; e < woff[i + 1]; ++e) acc.add(wc[e], r * wv[e]);
+  }
+  if (acc.overflow) atomicExch(overflow, 1);
+  atomicMax(overflow + 5, acc.n);
+  acc.sort();
+  if (MODE == 0) {
+    cnt[I] = acc.n;
+  } else {
+    int64_t at = aoff[I];
+    float d = 0.0f;
+    for (int t = 0; t < acc.n; ++t) {
+      ac[at + t] = acc.key[t];
+      av[at + t] = acc.val[t];
+      if (acc.key[t] == (int32_t)I) d = acc.val[t];
+    }
+    adinv[I] = d > 0.0f ? 1.0f / d : 0.0f;
+  }
+}
+
+__global__ void k_i64_i32(int64_t n, const int64_t* __restrict__ a, int32_t* __restrict__ b) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (int32_t)a[i];
+}
+
+__global__ void k_f64_f32_inv(int64_t n, const double* __restrict__ d, float* __restrict__ inv) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) inv[i] = d[i] != 0.0 ? (float)(1.0 / d[i]) : 0.0f;
+}
+
+// Coarse chart offsets: chart_row_c[c] = aid at the chart's first row (aggregates are
+// numbered in row order, per chart contiguous).
+__global__ void k_coarse_chart_rows(int64_t n_charts, const int64_t* __restrict__ chart_row,
+                                    const int64_t* __restrict__ lead_scan_rows, int64_t* __restrict__ out) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c <= n_charts) out[c] = lead_scan_rows[chart_row[c]];
+}
+
+// Row i heads an aggregate iff it leads its group and that group leads its aggregate
+// (`lead` is 0 for inactive rows, so grp_of is only read for active ones).
+__global__ void k_agg_lead_rows(int64_t n, const uint8_t* __restrict__ lead, const uint8_t* __restrict__ glead,
+                                const int32_t* __restrict__ grp_of, uint8_t* __restrict__ arow) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) arow[i] = (lead[i] && glead[grp_of[i]]) ? 1 : 0;
+}
+
+// Dense Cholesky of each final chart block (<= kDirect rows) in shared memory, FP64
+// pivots; the factor is stored as FP32 lower-triangular rows.
+__global__ void __launch_bounds__(128) k_direct_factor(const int32_t* __restrict__ final_lvl,
+                                                       const int64_t* const* __restrict__ lvl_chart_row,
+                                                       const int32_t* const* __restrict__ lvl_rp,
+                                                       const int32_t* const* __restrict__ lvl_cols,
+                                                       const float* const* __restrict__ lvl_vals,
+                                                       const int64_t* __restrict__ fac_off, float* __restrict__ fac,
+                                                       int* __restrict__ bad) {
+  __shared__ double M[kDirect * kDirect];
+  const int c = blockIdx.x;
+  const int f = final_lvl[c];
+  if (f < 0) return;
+  const int64_t r0 = lvl_chart_row[f][c];
+  const int m = (int)(lvl_chart_row[f][c + 1] - r0);
+  if (m <= 0 || m > kDirect) return;
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) M[t] = 0.0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < m; r += blockDim.x) {
+    const int64_t row = r0 + r;
+    for (int e = lvl_rp[f][row]; e < lvl_rp[f][row + 1]; ++e) {
+      int64_t col = lvl_cols[f][e] - r0;
+      if (col >= 0 && col < m) M[r * m + col] = (double)lvl_vals[f][e];
+    }
+  }
+  __syncthreads();
+  for (int j = 0; j < m; ++j) {
+    if (threadIdx.x == 0) {
+      double d = M[j * m + j];
+      for (int k = 0; k < j; ++k) d -= M[j * m + k] * M[j * m + k];
+      if (!(d > 0.0)) {
+        atomicExch(bad, 1);
+        d = 1e-30;
+      }
+      M[j * m + j] = sqrt(d);
+    }
+    __syncthreads();
+    const double piv = M[j * m + j];
+    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+      double s = M[i * m + j];
+      for (int k = 0; k < j; ++k) s -= M[i * m + k] * M[j * m + k];
+      M[i * m + j] = s / piv;
+    }
+    __syncthreads();
+  }
+  float* L = fac + fac_off[c];
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+    int i = t / m, k = t % m;
+    L[t] = k <= i ? (float)M[t] : 0.0f;
+  }
+}
+
+// ---------------------------------------------------------------- apply kernels
+template <int NR>
+struct F {
+  float c[NR];
+};
+template <int NR>
+__device__ __forceinline__ F<NR> ldf(const float* p, int64_t i) {
+  F<NR> r;
+  if constexpr (NR == 2) {
+    float2 t = reinterpret_cast<const float2*>(p)[i];
+    r.c[0] = t.x;
+    r.c[1] = t.y;
+  } else {
+    r.c[0] = p[i];
+  }
+  return r;
+}
+template <int NR>
+__device__ __forceinline__ void stf(float* p, int64_t i, const F<NR>& v) {
+  if constexpr (NR == 2) reinterpret_cast<float2*>(p)[i] = make_float2(v.c[0], v.c[1]);
+  else p[i] = v.c[0];
+}
+
+// rows of level-k charts that continue below k (and whose CG is still running)
+__device__ __forceinline__ bool row_live(int32_t c, int lvl, const int32_t* final_lvl, const int32_t* done) {
+  return final_lvl[c] > lvl && !done[c];
+}
+
+// The level kernels run over chart-aligned row tiles (one CTA per tile, one chart-state
+// check per CTA) as CSR-vector: LPR lanes per row, each lane covering ceil(8/LPR) entries in
+// one unrolled sweep, U rows in flight per sub-warp, block-uniform trip counts (every lane
+// takes part in the shuffles).  One generic row loop, four row operations.
+struct LvlTiles {
+  const int64_t* tab;    // [begin, end) pairs
+  const int32_t* chart;  // chart of each tile
+  int64_t n;
+};
+
+template <int NR>
+struct RowIn {
+  int lo, hi;
+};
+
+// Generic: for each row i of the tile, s = sum_e w(e) * g(col(e)); then fin(i, s).
+template <int NR, int LPR, int U, class W, class G, class Fin>
+__device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_t* ptr64, const int32_t* ptr32,
+                                          const int32_t* __restrict__ cols, W w, G g, Fin fin) {
+  constexpr int K = (8 + LPR - 1) / LPR;
+  const int sub = threadIdx.x % LPR;
+  const int rpp = kAmgThreads / LPR;
+  for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
+    int64_t lo[U], hi[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      const bool valid = i < end;
+      lo[u] = valid ? (ptr64 ? ptr64[i] : (int64_t)ptr32[i]) : 0;
+      hi[u] = valid ? (ptr64 ? ptr64[i + 1] : (int64_t)ptr32[i + 1]) : 0;
+    }
+    float av[U][K];
+    int cv[U][K];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int64_t e = lo[u] + sub + k * LPR;
+        const bool in = e < hi[u];
+        av[u][k] = in ? w(e) : 0.0f;
+        cv[u][k] = in ? cols[e] : -1;
+      }
+    F<NR> s[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int c = 0; c < NR; ++c) s[u].c[c] = 0.0f;
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (cv[u][k] >= 0) {
+          const F<NR> v = g(cv[u][k]);
+#pragma unroll
+          for (int c = 0; c < NR; ++c) s[u].c[c] += av[u][k] * v.c[c];
+        }
+      for (int64_t e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {
+        const float a = w(e);
+        const F<NR> v = g(cols[e]);
+#pragma unroll
+        for (int c = 0; c < NR; ++c) s[u].c[c] += a * v.c[c];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int o = LPR / 2; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < NR; ++c) s[u].c[c] += __shfl_xor_sync(0xffffffffu, s[u].c[c], o, LPR);
+      const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      if (sub == 0 && i < end) fin(i, s[u]);
+    }
+  }
+}
+
+// Down 1: x = w D^-1 b;  t = b - A x  (x of neighbours formed on the fly).
+template <int NR, int LPR, int U>
+__global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const int32_t* __restrict__ done,
+                                                             const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                                             const float* __restrict__ vals, const float* __restrict__ dinv,
+                                                             const float* __restrict__ b, float* __restrict__ x,
+                                                             float* __restrict__ t) {
+  const int64_t tl = blockIdx.x;
+  if (done[T.chart[tl]]) return;
+  tile_rows<NR, LPR, U>(
+      T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, cols, [&](int64_t e) { return vals[e]; },
+      [&](int32_t j) {
+        F<NR> v = ldf<NR>(b, j);
+        const float wd = kOmega * dinv[j];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) v.c[c] *= wd;
+        return v;
+      },
+      [&](int64_t i, const F<NR>& s) {
+        const F<NR> bi = ldf<NR>(b, i);
+        F<NR> xi, ti;
+        const float wd = kOmega * dinv[i];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+          xi.c[c] = wd * bi.c[c];
+          ti.c[c] = bi.c[c] - s.c[c];
+        }
+        stf<NR>(x, i, xi);
+        stf<NR>(t, i, ti);
+      });
+}
+
+// Restrict: b_c = R t over the coarse rows (tiles of the coarse level).
+template <int NR, int LPR, int U>
+__global__ void __launch_bounds__(kAmgThreads) k_restrict(LvlTiles T, const int32_t* __restrict__ done,
+                                                          const int64_t* __restrict__ roff, const int32_t* __restrict__ rc,
+                                                          const float* __restrict__ rv, const float* __restrict__ t,
+                                                          float* __restrict__ bc) {
+  const int64_t tl = blockIdx.x;
+  if (done[T.chart[tl]]) return;
+  tile_rows<NR, LPR, U>(
+      T.tab[2 * tl], T.tab[2 * tl + 1], roff, nullptr, rc, [&](int64_t e) { return rv[e]; },
+      [&](int32_t j) { return ldf<NR>(t, j); }, [&](int64_t I, const F<NR>& s) { stf<NR>(bc, I, s); });
+}
+
+// Up 1: y = x + alpha_c P x_c (alpha_c = 1: plain; > 1: over-correction of an unsmoothed
+// (piecewise-constant) coarse space, which underestimates the smooth error).
+template <int NR, int LPR, int U>
+__global__ void __launch_bounds__(kAmgThreads) k_prolong_add(LvlTiles T, const int32_t* __restrict__ done,
+                                                             const int64_t* __restrict__ poff, const int32_t* __restrict__ pc,
+                                                             const float* __restrict__ pv, const float* __restrict__ xc,
+                                                             const float* __restrict__ x, float* __restrict__ y, float alpha_c) {
+  const int64_t tl = blockIdx.x;
+  if (done[T.chart[tl]]) return;
+  tile_rows<NR, LPR, U>(
+      T.tab[2 * tl], T.tab[2 * tl + 1], poff, nullptr, pc, [&](int64_t e) { return alpha_c * pv[e]; },
+      [&](int32_t j) { return ldf<NR>(xc, j); },
+      [&](int64_t i, const F<NR>& s) {
+        F<NR> xi = ldf<NR>(x, i);
+#pragma unroll
+        for (int c = 0; c < NR; ++c) xi.c[c] += s.c[c];
+        stf<NR>(y, i, xi);
+      });
+}
+
+// Up 2: x = y + w D^-1 (b - A y).
+template <int NR, int LPR, int U>
+__global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int32_t* __restrict__ done,
+                                                           const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                                           const float* __restrict__ vals, const float* __restrict__ dinv,
+                                                           const float* __restrict__ b, const float* __restrict__ y,
+                                                           float* __restrict__ x) {
+  const int64_t tl = blockIdx.x;
+  if (done[T.chart[tl]]) return;
+  tile_rows<NR, LPR, U>(
+      T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, cols, [&](int64_t e) { return vals[e]; },
+      [&](int32_t j) { return ldf<NR>(y, j); },
+      [&](int64_t i, const F<NR>& s) {
+        const F<NR> bi = ldf<NR>(b, i), yi = ldf<NR>(y, i);
+        F<NR> xi;
+        const float wd = kOmega * dinv[i];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) xi.c[c] = yi.c[c] + wd * (bi.c[c] - s.c[c]);
+        stf<NR>(x, i, xi);
+      });
+}
+
+// Direct solve of every chart at its last level: L L^T x = b (one warp per chart).
+template <int NR>
+__global__ void __launch_bounds__(32) k_direct_solve(const int32_t* __restrict__ final_lvl, const int32_t* __restrict__ done,
+                                                     const int64_t* const* __restrict__ lvl_chart_row,
+                                                     float* const* __restrict__ lvl_b, float* const* __restrict__ lvl_x,
+                                                     const float* const* __restrict__ lvl_dinv,
+                                                     const int64_t* __restrict__ fac_off, const float* __restrict__ fac) {
+  __shared__ float y[NR][kDirect];
+  const int c = blockIdx.x;
+  const int f = final_lvl[c];
+  if (f < 0 || done[c]) return;
+  const int64_t r0 = lvl_chart_row[f][c];
+  const int m = (int)(lvl_chart_row[f][c + 1] - r0);
+  if (m <= 0) return;
+  const float* b = lvl_b[f];
+  float* x = lvl_x[f];
+  const int lane = threadIdx.x;
+  if (m > kDirect) {  // aggregation stalled above the dense limit: x = D^-1 b
+    const float* dv = lvl_dinv[f];
+    for (int i = lane; i < m; i += 32)
+#pragma unroll
+      for (int k = 0; k < NR; ++k) x[NR * (r0 + i) + k] = dv[r0 + i] * b[NR * (r0 + i) + k];
+    return;
+  }
+  const float* L = fac + fac_off[c];
+  for (int i = lane; i < m; i += 32)
+#pragma unroll
+    for (int k = 0; k < NR; ++k) y[k][i] = b[NR * (r0 + i) + k];
+  __syncwarp();
+  // forward: L y = b
+  for (int i = 0; i < m; ++i) {
+    float s[NR];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) s[k] = 0.0f;
+    for (int j = lane; j < i; j += 32)
+#pragma unroll
+      for (int k = 0; k < NR; ++k) s[k] += L[i * m + j] * y[k][j];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) s[k] = warp_sum(s[k]);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < NR; ++k) y[k][i] = (y[k][i] - s[k]) / L[i * m + i];
+    __syncwarp();
+  }
+  // backward: L^T x = y
+  for (int i = m - 1; i >= 0; --i) {
+    float s[NR];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) s[k] = 0.0f;
+    for (int j = i + 1 + lane; j < m; j += 32)
+#pragma unroll
+      for (int k = 0; k < NR; ++k) s[k] += L[j * m + i] * y[k][j];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) s[k] = warp_sum(s[k]);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < NR; ++k) y[k][i] = (y[k][i] - s[k]) / L[i * m + i];
+    __syncwarp();
+  }
+  for (int i = lane; i < m; i += 32)
+#pragma unroll
+    for (int k = 0; k < NR; ++k) x[NR * (r0 + i) + k] = y[k][i];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+struct AmgLevelDev {
+  int64_t n = 0, nnz = 0, n_next = 0, n_pnnz = 0;
+  std::vector<int64_t> h_chart_row;
+  int64_t* chart_row = nullptr;
+  int32_t* row_chart = nullptr;
+  int32_t *rp = nullptr, *cols = nullptr;
+  float *vals = nullptr, *dinv = nullptr;
+  // transfer to the next level (rows of charts that continue below this level)
+  int64_t* poff = nullptr;
+  int32_t* pc = nullptr;
+  float* pv = nullptr;
+  int64_t* roff = nullptr;
+  int32_t* rc = nullptr;
+  float* rv = nullptr;
+  float *b = nullptr, *x = nullptr, *y = nullptr, *t = nullptr;
+  LvlTiles cont{nullptr, nullptr, 0};  // tiles over rows whose chart continues below this level
+  LvlTiles all{nullptr, nullptr, 0};   // tiles over every row of this level
+};
+
+struct AmgHierarchy {
+  int nrhs = 2;
+  int64_t n_charts = 0;
+  std::vector<AmgLevelDev> lv;
+  int32_t* final_lvl = nullptr;
+  int64_t* fac_off = nullptr;
+  float* fac = nullptr;
+  const int64_t** d_lvl_chart_row = nullptr;
+  float** d_lvl_b = nullptr;
+  float** d_lvl_x = nullptr;
+  const float** d_lvl_dinv = nullptr;
+  std::vector<int32_t> h_final;
+  int64_t total_rows = 0, total_nnz = 0;
+  float alpha_c = 1.0f;
+};
+
+namespace {
+
+int64_t read_i64(Ctx& ctx, const int64_t* d) {
+  int64_t* h = static_cast<int64_t*>(ctx.pinned.get(sizeof(int64_t)));
+  RUV_CUDA(cudaMemcpyAsync(h, d, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx.stream));
+  RUV_CUDA(cudaStreamSynchronize(ctx.stream));
+  return *h;
+}
+
+// Two-pass row build from a count kernel: counts -> offsets (int64, n + 1) and the total.
+int64_t offsets_from_counts(Ctx& ctx, const int32_t* cnt, int64_t n, int64_t* off, const std::string& tag) {
+  exclusive_scan(cnt, off, n, ctx.ws, ctx.stream, tag);
+  return read_i64(ctx, off + n);
+}
+
+}  // namespace
+
+AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string& info) {
+  cudaStream_t s = ctx.stream;
+  const int B = kAmgThreads;
+  const int64_t NC = sys.n_charts;
+  std::unique_ptr<AmgHierarchy> H(new AmgHierarchy());
+  H->nrhs = sys.nrhs;
+  H->n_charts = NC;
+  H->alpha_c = smooth ? 1.0f : 1.5f;  // over-correct the piecewise-constant coarse space
+  if (const char* e = std::getenv("RUV_AMG_ALPHA")) H->alpha_c = (float)std::atof(e);
+  cudaEvent_t t_setup0;
+  RUV_CUDA(cudaEventCreate(&t_setup0));
+  RUV_CUDA(cudaEventRecord(t_setup0, s));
+  int* ovf = ctx.ws.get<int>("amg.overflow", 8);
+  RUV_CUDA(cudaMemsetAsync(ovf, 0, 8 * sizeof(int), s));
+  const bool debug = std::getenv("RUV_AMG_DEBUG") != nullptr;
+  {
+    AmgLevelDev L0;
+    L0.n = sys.n_rows;
+    L0.nnz = sys.nnz;
+    L0.h_chart_row = sys.h_chart_row;
+    L0.chart_row = sys.chart_row;
+    L0.rp = sys.row_ptr;
+    L0.cols = sys.cols;
+    L0.vals = sys.vals32;
+    L0.dinv = ctx.ws.get<float>("amg.l0.dinv", L0.n);
+    if (L0.n > 0) {
+      k_f64_f32_inv<<<div_up(L0.n, B), B, 0, s>>>(L0.n, sys.diag, L0.dinv);
+      count_launches(1);
+    }
+    H->lv.push_back(L0);
+  }
+  H->h_final.assign(NC, -1);
+  std::vector<int32_t> cont(NC, 0);
+  for (int lvl = 0; lvl < kMaxLevels; ++lvl) {
+    const std::string tag = "amg.l" + std::to_string(lvl);
+    AmgLevelDev& L = H->lv[lvl];
+    int64_t n_cont = 0;
+    for (int64_t c = 0; c < NC; ++c) {
+      if (H->h_final[c] >= 0) {
+        cont[c] = 0;
+        continue;
+      }
+      const int64_t m = L.h_chart_row[c + 1] - L.h_chart_row[c];
+      bool stalled = false;
+      if (lvl > 0) {
+        const AmgLevelDev& P = H->lv[lvl - 1];
+        const int64_t mf = P.h_chart_row[c + 1] - P.h_chart_row[c];
+        stalled = (double)m > 0.85 * (double)mf;
+      }
+      if (m <= kDirect || lvl == kMaxLevels - 1 || stalled) {
+        H->h_final[c] = lvl;
+        cont[c] = 0;
+      } else {
+        cont[c] = 1;
+        ++n_cont;
+      }
+    }
+    int32_t* d_cont = ctx.ws.get<int32_t>(tag + ".cont", NC);
+    RUV_CUDA(cudaMemcpyAsync(d_cont, cont.data(), sizeof(int32_t) * NC, cudaMemcpyHostToDevice, s));
+    L.row_chart = ctx.ws.get<int32_t>(tag + ".row_chart", L.n);
+    uint8_t* active = ctx.ws.get<uint8_t>(tag + ".active", L.n);
+    if (L.n > 0) {
+      k_row_chart<<<div_up(L.n, B), B, 0, s>>>(L.n, L.chart_row, NC, d_cont, L.row_chart, active);
+      count_launches(1);
+    }
+    RUV_CUDA(cudaStreamSynchronize(s));  // `cont` is reused by the next level
+    if (n_cont == 0) break;
+    // ---- aggregation: pairs of rows, then pairs of pairs
+    int32_t* mate = ctx.ws.get<int32_t>(tag + ".mate", L.n);
+    int32_t* prop = ctx.ws.get<int32_t>(tag + ".prop", L.n);
+    RUV_CUDA(cudaMemsetAsync(mate, 0xff, sizeof(int32_t) * L.n, s));
+    for (int r = 0; r < kPairRounds; ++r) {
+      k_propose<<<div_up(L.n, B), B, 0, s>>>(L.n, L.rp, L.cols, L.vals, active, mate, prop);
+      k_accept<<<div_up(L.n, B), B, 0, s>>>(L.n, prop, mate);
+      count_launches(2);
+    }
+    uint8_t* lead = ctx.ws.get<uint8_t>(tag + ".lead", L.n);
+    int32_t* lead_row = ctx.ws.get<int32_t>(tag + ".lead_row", L.n);
+    k_row_lead<<<div_up(L.n, B), B, 0, s>>>(L.n, L.rp, L.cols, L.vals, active, mate, lead_row, lead);
+    count_launches(1);
+    int64_t* gid = ctx.ws.get<int64_t>(tag + ".gid", L.n + 1);
+    exclusive_scan_u8(lead, gid, L.n, ctx.ws, s, tag + ".gs");
+    const int64_t NG = read_i64(ctx, gid + L.n);
+    int32_t* grp_of = ctx.ws.get<int32_t>(tag + ".grp_of", L.n);
+    int32_t* gcnt = ctx.ws.get<int32_t>(tag + ".gcnt", NG);
+    RUV_CUDA(cudaMemsetAsync(gcnt, 0, sizeof(int32_t) * std::max<int64_t>(NG, 1), s));
+    k_group_of<<<div_up(L.n, B), B, 0, s>>>(L.n, active, lead_row, gid, grp_of, gcnt);
+    count_launches(1);
+    int64_t* goff = ctx.ws.get<int64_t>(tag + ".goff", NG + 1);
+    exclusive_scan(gcnt, goff, NG, ctx.ws, s, tag + ".go");
+    int32_t* gcur = ctx.ws.get<int32_t>(tag + ".gcur", NG);
+    RUV_CUDA(cudaMemsetAsync(gcur, 0, sizeof(int32_t) * std::max<int64_t>(NG, 1), s));
+    int32_t* mem = ctx.ws.get<int32_t>(tag + ".mem", L.n);
+    k_group_scatter<<<div_up(L.n, B), B, 0, s>>>(L.n, active, grp_of, goff, gcur, mem);
+    count_launches(1);
+    int32_t* gmate = ctx.ws.get<int32_t>(tag + ".gmate", NG);
+    int32_t* gprop = ctx.ws.get<int32_t>(tag + ".gprop", NG);
+    int32_t* glead_of = ctx.ws.get<int32_t>(tag + ".glead_of", NG);
+    uint8_t* glead = ctx.ws.get<uint8_t>(tag + ".glead", NG);
+    RUV_CUDA(cudaMemsetAsync(gmate, 0xff, sizeof(int32_t) * std::max<int64_t>(NG, 1), s));
+    if (NG > 0) {
+      k_sort_members<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem);
+      count_launches(1);
+      for (int r = 0; r < kPairRounds; ++r) {
+        k_propose2<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, L.cols, L.vals, grp_of, gmate, gprop, ovf);
+        k_accept<<<div_up(NG, B), B, 0, s>>>(NG, gprop, gmate);
+        count_launches(2);
+      }
+      k_group_lead<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, L.cols, L.vals, grp_of, gmate, glead_of, glead);
+      count_launches(1);
+    }
+    int64_t* aid = ctx.ws.get<int64_t>(tag + ".aid", NG + 1);
+    exclusive_scan_u8(glead, aid, NG, ctx.ws, s, tag + ".as");
+    const int64_t NA = read_i64(ctx, aid + NG);
+    int32_t* agg = ctx.ws.get<int32_t>(tag + ".agg", L.n);
+    k_agg<<<div_up(L.n, B), B, 0, s>>>(L.n, active, grp_of, glead_of, aid, agg);
+    // coarse chart offsets: aggregates are numbered in lead-row order, so chart c's
+    // aggregates start at the count of aggregate-leading rows before its first row
+    uint8_t* arow = ctx.ws.get<uint8_t>(tag + ".arow", L.n);
+    k_agg_lead_rows<<<div_up(L.n, B), B, 0, s>>>(L.n, lead, glead, grp_of, arow);
+    count_launches(2);
+    int64_t* ascan = ctx.ws.get<int64_t>(tag + ".ascan", L.n + 1);
+    exclusive_scan_u8(arow, ascan, L.n, ctx.ws, s, tag + ".ar");
+    const std::string ntag = "amg.l" + std::to_string(lvl + 1);
+    AmgLevelDev C;
+    C.n = NA;
+    C.chart_row = ctx.ws.get<int64_t>(ntag + ".chart_row", NC + 1);
+    k_coarse_chart_rows<<<div_up(NC + 1, B), B, 0, s>>>(NC, L.chart_row, ascan, C.chart_row);
+    count_launches(1);
+    // ---- prolongator P (fine rows of continuing charts)
+    int32_t* cnt = ctx.ws.get<int32_t>(tag + ".pcnt", L.n);
+    L.poff = ctx.ws.get<int64_t>(tag + ".poff", L.n + 1);
+    k_prolong<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, smooth ? 1 : 0, cnt,
+                                              nullptr, nullptr, nullptr, ovf);
+    count_launches(1);
+    const int64_t PN = offsets_from_counts(ctx, cnt, L.n, L.poff, tag + ".po");
+    L.n_pnnz = PN;
+    L.pc = ctx.ws.get<int32_t>(tag + ".pc", PN);
+    L.pv = ctx.ws.get<float>(tag + ".pv", PN);
+    k_prolong<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, smooth ? 1 : 0, cnt,
+                                              L.poff, L.pc, L.pv, ovf);
+    count_launches(1);
+    // ---- R = P^T
+    int32_t* rcnt = ctx.ws.get<int32_t>(tag + ".rcnt", NA);
+    RUV_CUDA(cudaMemsetAsync(rcnt, 0, sizeof(int32_t) * std::max<int64_t>(NA, 1), s));
+    if (PN > 0) {
+      k_count_cols<<<div_up(PN, B), B, 0, s>>>(PN, L.pc, rcnt);
+      count_launches(1);
+    }
+    L.roff = ctx.ws.get<int64_t>(tag + ".roff", NA + 1);
+    exclusive_scan(rcnt, L.roff, NA, ctx.ws, s, tag + ".ro");
+    int32_t* cursor = ctx.ws.get<int32_t>(tag + ".rcur", NA);
+    RUV_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * std::max<int64_t>(NA, 1), s));
+    L.rc = ctx.ws.get<int32_t>(tag + ".rc", PN);
+    L.rv = ctx.ws.get<float>(tag + ".rv", PN);
+    k_scatter_t<<<div_up(L.n, B), B, 0, s>>>(L.n, L.poff, L.pc, L.pv, L.roff, cursor, L.rc, L.rv);
+    k_sort_rows<<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv);
+    count_launches(2);
+    // ---- W = A P, then A_c = R W
+    int32_t* wcnt = ctx.ws.get<int32_t>(tag + ".wcnt", L.n);
+    int64_t* woff = ctx.ws.get<int64_t>(tag + ".woff", L.n + 1);
+    k_ap<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, nullptr, nullptr,
+                                         nullptr, ovf);
+    count_launches(1);
+    const int64_t WN = offsets_from_counts(ctx, wcnt, L.n, woff, tag + ".wo");
+    int32_t* wc = ctx.ws.get<int32_t>(tag + ".wc", WN);
+    float* wv = ctx.ws.get<float>(tag + ".wv", WN);
+    k_ap<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, woff, wc, wv, ovf);
+    count_launches(1);
+    int32_t* acnt = ctx.ws.get<int32_t>(ntag + ".acnt", NA);
+    int64_t* aoff = ctx.ws.get<int64_t>(ntag + ".aoff", NA + 1);
+    if (NA > 0) {
+      k_rw<0><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv, woff, wc, wv, acnt, nullptr, nullptr, nullptr, nullptr,
+                                          ovf);
+      count_launches(1);
+    }
+    const int64_t AN = offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao");
+    if (AN >= (int64_t)INT32_MAX) throw Error{RUV_ERR_BAD_INPUT, "coarse operator too large"};
+    C.rp = ctx.ws.get<int32_t>(ntag + ".rp", NA + 1);
+    C.cols = ctx.ws.get<int32_t>(ntag + ".cols", AN);
+    C.vals = ctx.ws.get<float>(ntag + ".vals", AN);
+    C.dinv = ctx.ws.get<float>(ntag + ".dinv", NA);
+    C.nnz = AN;
+    if (NA > 0) {
+      k_rw<1><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv, woff, wc, wv, acnt, aoff, C.cols, C.vals, C.dinv, ovf);
+      k_i64_i32<<<div_up(NA + 1, B), B, 0, s>>>(NA + 1, aoff, C.rp);
+      count_launches(2);
+    }
+    L.n_next = NA;
+    if (debug) {
+      int hv[8];
+      RUV_CUDA(cudaMemcpyAsync(hv, ovf, sizeof(hv), cudaMemcpyDeviceToHost, s));
+      RUV_CUDA(cudaStreamSynchronize(s));
+      std::fprintf(stderr, "amg level %d: n=%lld nnz=%lld groups=%lld aggregates=%lld P=%lld W=%lld Ac=%lld "
+                   "max keys propose2=%d P=%d W=%d Ac=%d overflow=%d\n", lvl, (long long)L.n, (long long)L.nnz,
+                   (long long)NG, (long long)NA, (long long)PN, (long long)WN, (long long)AN, hv[2], hv[3], hv[4], hv[5],
+                   hv[0]);
+      RUV_CUDA(cudaMemsetAsync(ovf + 2, 0, 4 * sizeof(int), s));
+    }
+    C.h_chart_row.resize(NC + 1);
+    RUV_CUDA(cudaMemcpyAsync(C.h_chart_row.data(), C.chart_row, sizeof(int64_t) * (NC + 1), cudaMemcpyDeviceToHost, s));
+    RUV_CUDA(cudaStreamSynchronize(s));
+    H->lv.push_back(C);
+  }
+  int h_ovf[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  RUV_CUDA(cudaMemcpyAsync(h_ovf, ovf, sizeof(h_ovf), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  if (h_ovf[0]) throw Error{RUV_ERR_INTERNAL, "AMG setup: a product row exceeded its accumulation bound"};
+  // ---- per-level vectors, tile tables, pointer tables, dense factors
+  const int NR = sys.nrhs;
+  const int K = (int)H->lv.size();
+  for (int k = 0; k < K; ++k) {
+    AmgLevelDev& L = H->lv[k];
+    const std::string tag = "amg.v" + std::to_string(k);
+    for (int which = 0; which < 2; ++which) {
+      std::vector<int64_t> tab;
+      std::vector<int32_t> tch;
+      for (int64_t c = 0; c < NC; ++c) {
+        if (which == 0 && !(H->h_final[c] > k)) continue;
+        for (int64_t a0 = L.h_chart_row[c]; a0 < L.h_chart_row[c + 1]; a0 += kLevelTile) {
+          tab.push_back(a0);
+          tab.push_back(std::min(a0 + kLevelTile, L.h_chart_row[c + 1]));
+          tch.push_back((int32_t)c);
+        }
+      }
+      const int64_t nt = (int64_t)tch.size();
+      int64_t* dtab = ctx.ws.get<int64_t>(tag + (which ? ".atab" : ".ctab"), 2 * nt);
+      int32_t* dch = ctx.ws.get<int32_t>(tag + (which ? ".ach" : ".cch"), nt);
+      if (nt > 0) {
+        RUV_CUDA(cudaMemcpyAsync(dtab, tab.data(), sizeof(int64_t) * 2 * nt, cudaMemcpyHostToDevice, s));
+        RUV_CUDA(cudaMemcpyAsync(dch, tch.data(), sizeof(int32_t) * nt, cudaMemcpyHostToDevice, s));
+        RUV_CUDA(cudaStreamSynchronize(s));
+      }
+      (which ? L.all : L.cont) = LvlTiles{dtab, dch, nt};
+    }
+    L.b = k == 0 ? nullptr : ctx.ws.get<float>(tag + ".b", NR * L.n);
+    L.x = k == 0 ? nullptr : ctx.ws.get<float>(tag + ".x", NR * L.n);
+    L.y = ctx.ws.get<float>(tag + ".y", NR * L.n);
+    L.t = ctx.ws.get<float>(tag + ".t", NR * L.n);
+    H->total_rows += L.n;
+    H->total_nnz += L.nnz;
+  }
+  H->final_lvl = ctx.ws.get<int32_t>("amg.final", NC);
+  RUV_CUDA(cudaMemcpyAsync(H->final_lvl, H->h_final.data(), sizeof(int32_t) * NC, cudaMemcpyHostToDevice, s));
+  std::vector<int64_t> foff(NC + 1, 0);
+  for (int64_t c = 0; c < NC; ++c) {
+    const int f = H->h_final[c];
+    const int64_t m = f >= 0 ? H->lv[f].h_chart_row[c + 1] - H->lv[f].h_chart_row[c] : 0;
+    foff[c + 1] = foff[c] + (m <= kDirect ? m * m : 0);
+  }
+  H->fac_off = ctx.ws.get<int64_t>("amg.fac_off", NC + 1);
+  H->fac = ctx.ws.get<float>("amg.fac", foff[NC]);
+  RUV_CUDA(cudaMemcpyAsync(H->fac_off, foff.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
+  std::vector<const int64_t*> cr(K);
+  std::vector<const int32_t*> rps(K), cls(K);
+  std::vector<const float*> vls(K), dvs(K);
+  for (int k = 0; k < K; ++k) {
+    cr[k] = H->lv[k].chart_row;
+    rps[k] = H->lv[k].rp;
+    cls[k] = H->lv[k].cols;
+    vls[k] = H->lv[k].vals;
+    dvs[k] = H->lv[k].dinv;
+  }
+  H->d_lvl_chart_row = ctx.ws.get<const int64_t*>("amg.p_cr", K);
+  const int32_t** d_rp = ctx.ws.get<const int32_t*>("amg.p_rp", K);
+  const int32_t** d_cols = ctx.ws.get<const int32_t*>("amg.p_cols", K);
+  const float** d_vals = ctx.ws.get<const float*>("amg.p_vals", K);
+  H->d_lvl_dinv = ctx.ws.get<const float*>("amg.p_dinv", K);
+  RUV_CUDA(cudaMemcpyAsync(H->d_lvl_chart_row, cr.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_rp, rps.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_cols, cls.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_vals, vls.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(H->d_lvl_dinv, dvs.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, s));
+  int* bad = ovf + 1;
+  if (NC > 0) {
+    k_direct_factor<<<(unsigned)NC, 128, 0, s>>>(H->final_lvl, H->d_lvl_chart_row, d_rp, d_cols, d_vals, H->fac_off,
+                                                 H->fac, bad);
+    count_launches(1);
+  }
+  H->d_lvl_b = ctx.ws.get<float*>("amg.p_b", K);
+  H->d_lvl_x = ctx.ws.get<float*>("amg.p_x", K);
+  RUV_CUDA(cudaMemcpyAsync(h_ovf, ovf, sizeof(h_ovf), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));  // host pointer tables above go out of scope
+  if (h_ovf[1]) throw Error{RUV_ERR_BREAKDOWN, "AMG setup: a coarse block is not positive definite"};
+  info = "levels=" + std::to_string(K) + " rows=" + std::to_string(H->total_rows) + " nnz=" + std::to_string(H->total_nnz);
+  {
+    cudaEvent_t t1;
+    RUV_CUDA(cudaEventCreate(&t1));
+    RUV_CUDA(cudaEventRecord(t1, s));
+    RUV_CUDA(cudaEventSynchronize(t1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t_setup0, t1);
+    cudaEventDestroy(t1);
+    ctx.timings[3] = ms;
+    if (debug) std::fprintf(stderr, "amg setup %.2f ms, %s, operator complexity %.2f\n", ms, info.c_str(),
+                            sys.nnz > 0 ? (double)H->total_nnz / (double)sys.nnz : 0.0);
+  }
+  cudaEventDestroy(t_setup0);
+  return H.release();
+}
+
+void amg_free(AmgHierarchy* H) { delete H; }
+
+int amg_levels(const AmgHierarchy* H) { return (int)H->lv.size(); }
+
+// Bind the level-0 right-hand side / output vectors (the CG's r and z) before capture.
+void amg_bind(Ctx& ctx, AmgHierarchy* H, float* r0, float* z0) {
+  const int K = (int)H->lv.size();
+  H->lv[0].b = r0;
+  H->lv[0].x = z0;
+  std::vector<float*> bs(K), xs(K);
+  for (int k = 0; k < K; ++k) {
+    bs[k] = H->lv[k].b;
+    xs[k] = H->lv[k].x;
+  }
+  RUV_CUDA(cudaMemcpyAsync(H->d_lvl_b, bs.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, ctx.stream));
+  RUV_CUDA(cudaMemcpyAsync(H->d_lvl_x, xs.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, ctx.stream));
+  RUV_CUDA(cudaStreamSynchronize(ctx.stream));
+}
+
+namespace {
+
+int lanes_for(double avg) { return avg <= 5 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32; }
+
+#define RUV_LPR_SWITCH(lpr, CALL) \
+  switch (lpr) {                   \
+    case 4: CALL(4, 2); break;     \
+    case 8: CALL(8, 2); break;     \
+    case 16: CALL(16, 1); break;   \
+    default: CALL(32, 1); break;   \
+  }
+
+template <int NR>
+int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
+  cudaStream_t s = ctx.stream;
+  const int K = (int)H->lv.size();
+  const int B = kAmgThreads;
+  int launches = 0;
+  for (int k = 0; k + 1 < K; ++k) {
+    AmgLevelDev& L = H->lv[k];
+    AmgLevelDev& C = H->lv[k + 1];
+    if (L.cont.n == 0) continue;
+    const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
+#define CALL(X, UU)                                                                                              \
+  k_smooth_down<NR, X, UU><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.x, \
+                                                            L.t)
+    RUV_LPR_SWITCH(la, CALL)
+#undef CALL
+    ++launches;
+    if (C.all.n == 0) continue;
+    const int lr = lanes_for(C.n ? (double)L.n_pnnz / (double)C.n : 1.0);
+#define CALL(X, UU) k_restrict<NR, X, UU><<<(unsigned)C.all.n, B, 0, s>>>(C.all, done, L.roff, L.rc, L.rv, L.t, C.b)
+    RUV_LPR_SWITCH(lr, CALL)
+#undef CALL
+    ++launches;
+  }
+  if (NR == 2)
+    k_direct_solve<2><<<(unsigned)H->n_charts, 32, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b, H->d_lvl_x,
+                                                           H->d_lvl_dinv, H->fac_off, H->fac);
+  else
+    k_direct_solve<1><<<(unsigned)H->n_charts, 32, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b, H->d_lvl_x,
+                                                           H->d_lvl_dinv, H->fac_off, H->fac);
+  ++launches;
+  for (int k = K - 2; k >= 0; --k) {
+    AmgLevelDev& L = H->lv[k];
+    AmgLevelDev& C = H->lv[k + 1];
+    if (L.cont.n == 0) continue;
+    const int lp = lanes_for(L.n ? (double)L.n_pnnz / (double)L.n : 1.0);
+#define CALL(X, UU)                                                                                                  \
+  k_prolong_add<NR, X, UU><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.poff, L.pc, L.pv, C.x, L.x, L.y, \
+                                                            H->alpha_c)
+    RUV_LPR_SWITCH(lp, CALL)
+#undef CALL
+    const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
+#define CALL(X, UU) \
+  k_smooth_up<NR, X, UU><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.y, L.x)
+    RUV_LPR_SWITCH(la, CALL)
+#undef CALL
+    launches += 2;
+  }
+  return launches;
+}
+
+}  // namespace
+
+// One V(1,1) cycle: z0 = M^-1 r0 for every chart not marked done (launches only; capturable).
+int amg_apply(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
+  return H->nrhs == 2 ? apply_impl<2>(ctx, H, done) : apply_impl<1>(ctx, H, done);
+}
+
+}  // namespace ruv

@@ -160,7 +160,7 @@ ruv_status ruv_cg_solve(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const i
     if (pc == RUV_PRECOND_JACOBI)
       for (int32_t i = 0; i < n; ++i)
         if (std::fabs(diag[i]) < 1e-300) return fail(ctx, RUV_ERR_BAD_INPUT, "Jacobi: zero diagonal");
-    if (pc != RUV_PRECOND_NONE && pc != RUV_PRECOND_JACOBI)
+    if (pc != RUV_PRECOND_NONE && pc != RUV_PRECOND_JACOBI && pc != RUV_PRECOND_AMG && pc != RUV_PRECOND_AMG_SA)
       return fail(ctx, RUV_ERR_BAD_INPUT, "preconditioner not available in this build");
     Ctx& c = ctx->c;
     DevSystem sys;
@@ -247,13 +247,14 @@ ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ru
     ruv_unfold_opts_default(&o);
     if (opts) o = *opts;
     if (!(o.mix_w > 0.0)) return fail(ctx, RUV_ERR_BAD_INPUT, "mix_w must be > 0 (lscm.rs:479)");
-    if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI)
+    if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI && o.precond != RUV_PRECOND_AMG &&
+        o.precond != RUV_PRECOND_AMG_SA)
       return fail(ctx, RUV_ERR_BAD_INPUT, "preconditioner not available in this build");
     DevBatch& bt = c.resident;
     const int64_t NC = bt.n_charts, NV = bt.n_verts;
     if (NC == 0) {
       c.have_uv = true;
-      c.timings[0] = c.timings[1] = c.timings[2] = 0.0;
+      c.timings[0] = c.timings[1] = c.timings[2] = c.timings[3] = 0.0;
       return RUV_OK;
     }
     cudaEvent_t ev[4];
@@ -290,6 +291,7 @@ ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ru
       RUV_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
       c.timings[k] = ms;
     }
+    if (o.precond != RUV_PRECOND_AMG && o.precond != RUV_PRECOND_AMG_SA) c.timings[3] = 0.0;
     c.have_uv = true;
     int w = RUV_OK;
     for (int64_t k = 0; k < NC; ++k) {
@@ -341,7 +343,7 @@ int64_t ruv_kernel_launches(const ruv_ctx* ctx) { return ctx ? ctx->c.launches :
 
 int32_t ruv_last_timings(const ruv_ctx* ctx, double* ms, int32_t n) {
   if (!ctx || !ms) return 0;
-  int32_t k = n < 3 ? n : 3;
+  int32_t k = n < 4 ? n : 4;
   for (int32_t i = 0; i < k; ++i) ms[i] = ctx->c.timings[i];
   return k;
 }

@@ -18,7 +18,7 @@
 // Precision: RUV_PREC_FP64 runs the reference's recurrence in FP64.  RUV_PREC_MIXED runs
 // the SpMV, preconditioner and CG recurrence in FP32 and keeps FP64 for the solution
 // accumulator and the true residual r = b - A x (FP64 values), recomputed per chart
-// whenever the FP32 residual has dropped by `kDelta` since the last true residual
+// whenever the FP32 residual has dropped by `kDelta` (100x) since the last true residual
 // ("reliable updates"); convergence is judged on the FP64 true residual only.
 #include "system.cuh"
 
@@ -33,7 +33,7 @@ namespace {
 constexpr int kTileThreads = 256;
 constexpr int kChartThreads = 128;
 constexpr int kCheckEvery = 16;
-constexpr double kDelta = 0.1;
+constexpr double kDelta = 0.01;  // refresh after a 100x drop of the FP32 residual
 
 enum : int32_t { kActive = 0, kDone = 1 };
 
@@ -50,6 +50,8 @@ struct ChartState {
   int32_t state;
   int32_t refresh;  // mixed: a true-residual refresh is due
   int32_t refinements;
+  float alpha32;  // alpha / beta rounded once per chart for the FP32 tile kernels
+  float beta32;
   int32_t pad;
 };
 
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(kTileThreads) k_update(Tiles T, const ChartSta
   int64_t t = blockIdx.x;
   const ChartState& cs = st[T.chart[t]];
   if (cs.state != kActive) return;
-  const S alpha = (S)cs.alpha;
+  const S alpha = std::is_same<S, float>::value ? (S)cs.alpha32 : (S)cs.alpha;
   S acc[2] = {S(0), S(0)};
   for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
     V<S, NR> xv = ldv<S, NR>(x, i), rv = ldv<S, NR>(r, i), pv = ldv<S, NR>(p, i), qv = ldv<S, NR>(q, i), zv;
@@ -266,7 +268,7 @@ __global__ void __launch_bounds__(kTileThreads) k_direction(Tiles T, const Chart
   int64_t t = blockIdx.x;
   const ChartState& cs = st[T.chart[t]];
   if (cs.state != kActive) return;
-  const S beta = (S)cs.beta;
+  const S beta = std::is_same<S, float>::value ? (S)cs.beta32 : (S)cs.beta;
   for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
     V<S, NR> zv = ldv<S, NR>(z, i), pv = ldv<S, NR>(p, i);
 #pragma unroll
@@ -413,6 +415,7 @@ __global__ void __launch_bounds__(kChartThreads) k_chart_alpha(Tiles T, ChartSta
     return;
   }
   s.alpha = s.rz / pap;
+  s.alpha32 = (float)s.alpha;
 }
 
 // FP64 path: convergence on the recurrence residual (solver.rs:518-522), then beta.
@@ -441,13 +444,15 @@ __global__ void __launch_bounds__(kChartThreads) k_chart_beta(Tiles T, ChartStat
   }
   double rznew = precond_none ? v[0] : v[1];
   s.beta = rznew / s.rz;
+  s.beta32 = (float)s.beta;
   s.rz = rznew;
 }
 
 // Mixed path: the FP32 residual only schedules true-residual refreshes.
 __global__ void __launch_bounds__(kChartThreads) k_chart_beta_mixed(Tiles T, ChartState* __restrict__ st,
                                                                     const double* __restrict__ part, int precond_none,
-                                                                    int64_t max_iter, int* __restrict__ n_active) {
+                                                                    int64_t max_iter, int* __restrict__ n_active,
+                                                                    int separate_precond) {
   __shared__ double sh[2 * 32];
   int64_t c = blockIdx.x;
   if (st[c].state != kActive) return;
@@ -462,15 +467,19 @@ __global__ void __launch_bounds__(kChartThreads) k_chart_beta_mixed(Tiles T, Cha
     s.refresh = 1;  // beta is formed after the refresh, from the true residual
   } else {
     s.refresh = 0;
-    s.beta = rznew / s.rz;
-    s.rz = rznew;
+    if (!separate_precond) {  // (a separate preconditioner forms beta after its apply)
+      s.beta = rznew / s.rz;
+      s.beta32 = (float)s.beta;
+      s.rz = rznew;
+    }
   }
   (void)n_active;
 }
 
 __global__ void __launch_bounds__(kChartThreads) k_chart_after_refresh(Tiles T, ChartState* __restrict__ st,
                                                                        const double* __restrict__ part, int precond_none,
-                                                                       int64_t max_iter, int* __restrict__ n_active) {
+                                                                       int64_t max_iter, int* __restrict__ n_active,
+                                                                       int separate_precond) {
   __shared__ double sh[2 * 32];
   int64_t c = blockIdx.x;
   if (st[c].state != kActive || !st[c].refresh) return;
@@ -500,8 +509,118 @@ __global__ void __launch_bounds__(kChartThreads) k_chart_after_refresh(Tiles T, 
     return;
   }
   s.r_ref = rn;
+  if (separate_precond) {
+    s.refresh = 2;  // refreshed: the beta kernel uses the plain Fletcher-Reeves ratio
+    return;
+  }
   double rznew = precond_none ? v[0] : v[1];
   s.beta = rznew / s.rz;
+  s.beta32 = (float)s.beta;
+  s.rz = rznew;
+  s.refresh = 0;
+}
+
+// ---------------------------------------------------------------- separate preconditioner
+// (AMG) support: done mask, r.z / z.q partials, chart-level beta.
+__global__ void k_mark_done(const ChartState* __restrict__ st, int64_t n, int32_t* __restrict__ done) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) done[c] = st[c].state != kActive ? 1 : 0;
+}
+
+template <class S, int NR>
+__global__ void __launch_bounds__(kTileThreads) k_dots_rz(Tiles T, const ChartState* __restrict__ st, const S* __restrict__ r,
+                                                          const S* __restrict__ z, const S* __restrict__ q,
+                                                          double* __restrict__ part) {
+  __shared__ S sh[2 * 32];
+  int64_t t = blockIdx.x;
+  if (st[T.chart[t]].state != kActive) return;
+  S acc[2] = {S(0), S(0)};
+  for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
+    const V<S, NR> rv = ldv<S, NR>(r, i), zv = ldv<S, NR>(z, i), qv = ldv<S, NR>(q, i);
+#pragma unroll
+    for (int k = 0; k < NR; ++k) {
+      acc[0] += rv.c[k] * zv.c[k];
+      acc[1] += zv.c[k] * qv.c[k];
+    }
+  }
+  block_sum_t<2, S>(acc, sh);
+  if (threadIdx.x == 0) {
+    part[2 * t] = (double)acc[0];
+    part[2 * t + 1] = (double)acc[1];
+  }
+}
+
+template <class S, int NR>
+__global__ void __launch_bounds__(kTileThreads) k_copy_dir(Tiles T, const ChartState* __restrict__ st, const S* __restrict__ z,
+                                                           S* __restrict__ p) {
+  int64_t t = blockIdx.x;
+  if (st[T.chart[t]].state != kActive) return;
+  for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) stv<S, NR>(p, i, ldv<S, NR>(z, i));
+}
+
+// FP64 outer loop with a separate preconditioner: convergence on the recurrence residual
+// (solver.rs:518-522); beta comes after the apply.
+__global__ void __launch_bounds__(kChartThreads) k_chart_check64(Tiles T, ChartState* __restrict__ st,
+                                                                 const double* __restrict__ part, int64_t max_iter,
+                                                                 int* __restrict__ n_active) {
+  __shared__ double sh[2 * 32];
+  int64_t c = blockIdx.x;
+  if (st[c].state != kActive) return;
+  double v[2];
+  chart_reduce<2>(T, c, part, 2, v, sh);
+  if (threadIdx.x != 0) return;
+  ChartState& s = st[c];
+  s.iters += 1;
+  s.rr = v[0];
+  if (sqrt(v[0]) <= s.tol_abs) {
+    s.status = RUV_OK;
+    s.state = kDone;
+    atomicSub(n_active, 1);
+  } else if (!isfinite(v[0])) {
+    s.status = RUV_ERR_BREAKDOWN;
+    s.state = kDone;
+    atomicSub(n_active, 1);
+  } else if (s.iters >= max_iter) {
+    s.status = RUV_ERR_NOT_CONVERGED;
+    s.state = kDone;
+    atomicSub(n_active, 1);
+  }
+}
+
+// FP64 <-> FP32 copies of the preconditioner's input / output (FP64 outer loop).
+template <class A, class Bt>
+__global__ void k_convert(int64_t n, const A* __restrict__ in, Bt* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (Bt)in[i];
+}
+
+// After the first apply: rz = r.z.
+__global__ void __launch_bounds__(kChartThreads) k_chart_rz0(Tiles T, ChartState* __restrict__ st, const double* __restrict__ part) {
+  __shared__ double sh[2 * 32];
+  int64_t c = blockIdx.x;
+  if (st[c].state != kActive) return;
+  double v[2];
+  chart_reduce<2>(T, c, part, 2, v, sh);
+  if (threadIdx.x == 0) st[c].rz = v[0];
+}
+
+// beta after a separate apply: flexible (Polak-Ribiere, as the reference's FCG for AMG,
+// solver.rs:474-481, :526-539) using r_new - r_old = -alpha q, or Fletcher-Reeves right
+// after a true-residual refresh (r jumped).
+__global__ void __launch_bounds__(kChartThreads) k_chart_beta_pc(Tiles T, ChartState* __restrict__ st,
+                                                                 const double* __restrict__ part, int flexible) {
+  __shared__ double sh[2 * 32];
+  int64_t c = blockIdx.x;
+  if (st[c].state != kActive) return;
+  double v[2];
+  chart_reduce<2>(T, c, part, 2, v, sh);
+  if (threadIdx.x != 0) return;
+  ChartState& s = st[c];
+  const double rznew = v[0];
+  double beta = (flexible && s.refresh != 2) ? (-s.alpha * v[1]) / s.rz : rznew / s.rz;
+  if (!isfinite(beta)) beta = 0.0;
+  s.beta = beta;
+  s.beta32 = (float)beta;
   s.rz = rznew;
   s.refresh = 0;
 }
@@ -560,12 +679,12 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
       if (!mixed) {
         k_chart_beta<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
       } else {
-        k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
+        k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0);
         k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, x64, reinterpret_cast<float*>(xs));
         k_true_residual<NR, 8><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, sys.vals, sys.b, dinv32,
                                                                      jac, x64, reinterpret_cast<float*>(r),
                                                                      reinterpret_cast<float*>(z), part);
-        k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
+        k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0);
       }
       k_direction<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
     }
@@ -596,6 +715,139 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
   }
   if (mixed && NTL > 0) {
     // fold any FP32 increment still pending (charts that stopped between refreshes)
+    k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 1, x64, reinterpret_cast<float*>(xs));
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
+  out.resize(NC);
+  RUV_CUDA(cudaMemcpyAsync(out.data(), st, sizeof(ChartState) * NC, cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+}
+
+// Batched PCG with the AMG V-cycle as a separate apply step: FP32 inner loop with FP64
+// true-residual refreshes (the mixed scheme), for any requested precision.
+template <class S, int NR, int LPR, int U>
+void run_pcg_amg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st, int* n_active,
+                 std::vector<ChartState>& out, bool smooth) {
+  constexpr bool mixed = std::is_same<S, float>::value;
+  cudaStream_t s = ctx.stream;
+  Workspace& ws = ctx.ws;
+  const int64_t NR_ = sys.n_rows, NC = sys.n_charts, NTL = T.n;
+  S* xs = mixed ? ws.get<S>("pcg.xs", NR * NR_) : nullptr;
+  S* r = ws.get<S>("pcg.r", NR * NR_);
+  S* z = ws.get<S>("pcg.z", NR * NR_);
+  S* p = ws.get<S>("pcg.p", NR * NR_);
+  S* q = ws.get<S>("pcg.q", NR * NR_);
+  S* dinv = ws.get<S>("pcg.dinv", NR_);
+  float* dinv32 = mixed ? reinterpret_cast<float*>(dinv) : nullptr;
+  // the V-cycle works in FP32: the FP64 loop hands it FP32 copies of r and takes z back
+  float* r32 = mixed ? reinterpret_cast<float*>(r) : ws.get<float>("pcg.r32", NR * NR_);
+  float* z32 = mixed ? reinterpret_cast<float*>(z) : ws.get<float>("pcg.z32", NR * NR_);
+  const S* vals = mixed ? reinterpret_cast<const S*>(sys.vals32) : reinterpret_cast<const S*>(sys.vals);
+  S* xiter = mixed ? xs : reinterpret_cast<S*>(x64);
+  double* part = ws.get<double>("pcg.part", 3 * NTL);
+  double* part2 = ws.get<double>("pcg.part2", 2 * NTL);
+  int32_t* done = ws.get<int32_t>("pcg.done", NC);
+  std::string info;
+  AmgHierarchy* H = amg_setup(ctx, sys, smooth, info);
+  struct Free {
+    AmgHierarchy* h;
+    ~Free() { amg_free(h); }
+  } free_h{H};
+  amg_bind(ctx, H, r32, z32);
+  const unsigned gv = div_up(NR * NR_, 256);
+  auto to32 = [&]() {
+    if (!mixed) k_convert<S, float><<<gv, 256, 0, s>>>(NR * NR_, r, r32);
+  };
+  auto to64 = [&]() {
+    if (!mixed) k_convert<float, S><<<gv, 256, 0, s>>>(NR * NR_, z32, z);
+  };
+  const int conv = mixed ? 0 : 2;
+  RUV_CUDA(cudaMemsetAsync(n_active, 0, sizeof(int), s));
+  if (NR_ > 0) {
+    k_dinv<S><<<div_up(NR_, kTileThreads), kTileThreads, 0, s>>>(NR_, sys.diag, dinv);
+    count_launches(1);
+  }
+  if (NTL > 0) {
+    k_init<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, sys.b, sys.diag, dinv, 1, x64, xs, r, z, p, part);
+    count_launches(1);
+  }
+  k_chart_init<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, o.tol, 0, n_active);  // (rz replaced below)
+  count_launches(1);
+  RUV_LAUNCH_CHECK();
+  int* h_active = static_cast<int*>(ctx.pinned.get(sizeof(int)));
+  RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  if (*h_active > 0 && NTL > 0) {
+    // z0 = M^-1 r0, rz = r.z, p = z
+    k_mark_done<<<div_up(NC, 256), 256, 0, s>>>(st, NC, done);
+    to32();
+    count_launches(1 + conv + amg_apply(ctx, H, done));
+    to64();
+    k_dots_rz<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, r, z, q, part2);
+    k_chart_rz0<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part2);
+    k_copy_dir<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
+    count_launches(3);
+    RUV_LAUNCH_CHECK();
+    constexpr int kRep = 8;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int per_iter = 0;
+    RUV_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int rep = 0; rep < kRep; ++rep) {
+      int l = 0;
+      k_spmv_pq<S, NR, LPR, U><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, p, q, part);
+      k_chart_alpha<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, n_active);
+      k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, dinv, 0, xiter, r, z, p, q, part);
+      if (mixed) {
+        k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1);
+        k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, x64, reinterpret_cast<float*>(xs));
+        k_true_residual<NR, 8><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, sys.vals, sys.b,
+                                                                     dinv32, 0, x64, reinterpret_cast<float*>(r),
+                                                                     reinterpret_cast<float*>(z), part);
+        k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1);
+        l += 4;
+      } else {
+        k_chart_check64<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, o.max_iter, n_active);
+        l += 1;
+      }
+      k_mark_done<<<div_up(NC, 256), 256, 0, s>>>(st, NC, done);
+      to32();
+      l += 4 + conv;
+      l += amg_apply(ctx, H, done);
+      to64();
+      k_dots_rz<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, r, z, q, part2);
+      k_chart_beta_pc<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part2, 1);
+      k_direction<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
+      l += 3;
+      per_iter = l;
+    }
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess) throw Error{RUV_ERR_LAUNCH, std::string("graph capture: ") + cudaGetErrorString(ce)};
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    if (ce != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      throw Error{RUV_ERR_LAUNCH, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+    }
+    int64_t launched = 0;
+    try {
+      while (launched < o.max_iter + kRep) {
+        RUV_CUDA(cudaGraphLaunch(exec, s));
+        count_launches((int64_t)kRep * per_iter);
+        launched += kRep;
+        RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+        RUV_CUDA(cudaStreamSynchronize(s));
+        if (*h_active <= 0) break;
+      }
+    } catch (...) {
+      cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(graph);
+      throw;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+  }
+  if (mixed && NTL > 0) {
     k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 1, x64, reinterpret_cast<float*>(xs));
     count_launches(1);
     RUV_LAUNCH_CHECK();
@@ -688,6 +940,16 @@ double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
 }
 
 template <class S, int NR>
+void dispatch_pcg_amg(Shape sh, Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st,
+                      int* n_active, std::vector<ChartState>& out, bool smooth) {
+#define RUV_CASE(L, UU) \
+  if (sh.lpr == L && sh.unroll == UU) return run_pcg_amg<S, NR, L, UU>(ctx, sys, x64, o, T, st, n_active, out, smooth);
+  RUV_SHAPES(RUV_CASE)
+#undef RUV_CASE
+  throw Error{RUV_ERR_BAD_INPUT, "unsupported SpMV shape"};
+}
+
+template <class S, int NR>
 double dispatch_time(Shape sh, Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
 #define RUV_CASE(L, UU) \
   if (sh.lpr == L && sh.unroll == UU) return time_spmv<S, NR, L, UU>(ctx, sys, T, reps, nbuf);
@@ -760,7 +1022,8 @@ TuneResult autotune_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps) {
 }
 
 std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o) {
-  if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI)
+  const bool amg = o.precond == RUV_PRECOND_AMG || o.precond == RUV_PRECOND_AMG_SA;
+  if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI && !amg)
     throw Error{RUV_ERR_BAD_INPUT, "preconditioner not available in this build"};
   const int64_t NC = sys.n_charts;
   Tiles T = upload_tiles(ctx, sys, "pcg");
@@ -769,7 +1032,18 @@ std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const So
   const Shape sh = pick_shape(ctx, sys);
   std::vector<ChartState> out;
   const bool mixed = o.precision == RUV_PREC_MIXED;
-  if (sys.nrhs == 2) {
+  if (amg) {
+    // the V-cycle runs in FP32 under either loop: the mixed loop (FP32 recurrences, FP64
+    // true-residual refreshes) or the FP64 loop (FP64 recurrences, FP32 copies in and out)
+    const bool smooth = o.precond == RUV_PRECOND_AMG_SA;
+    if (sys.nrhs == 2) {
+      if (mixed) dispatch_pcg_amg<float, 2>(sh, ctx, sys, x, o, T, st, n_active, out, smooth);
+      else dispatch_pcg_amg<double, 2>(sh, ctx, sys, x, o, T, st, n_active, out, smooth);
+    } else {
+      if (mixed) dispatch_pcg_amg<float, 1>(sh, ctx, sys, x, o, T, st, n_active, out, smooth);
+      else dispatch_pcg_amg<double, 1>(sh, ctx, sys, x, o, T, st, n_active, out, smooth);
+    }
+  } else if (sys.nrhs == 2) {
     if (mixed) dispatch_pcg<float, 2>(sh, ctx, sys, x, o, T, st, n_active, out);
     else dispatch_pcg<double, 2>(sh, ctx, sys, x, o, T, st, n_active, out);
   } else {

@@ -42,6 +42,15 @@ struct ChartResult {
 
 struct Ctx;
 
+// Batched aggregation AMG (amg.cu): set up on the device from an assembled system, bound to
+// the CG's level-0 vectors, applied as one V-cycle (launches only, capturable).
+struct AmgHierarchy;
+AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string& info);
+void amg_free(AmgHierarchy* H);
+int amg_levels(const AmgHierarchy* H);
+void amg_bind(Ctx& ctx, AmgHierarchy* H, float* r0, float* z0);
+int amg_apply(Ctx& ctx, AmgHierarchy* H, const int32_t* done);
+
 // x (nrhs * n_rows, device) <- A^-1 b per chart.  Returns per-chart results (host).
 std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o);
 
@@ -85,7 +94,7 @@ struct Ctx {
   DevBatch resident;
   bool have_batch = false;
   bool have_uv = false;
-  double timings[3] = {0.0, 0.0, 0.0};
+  double timings[4] = {0.0, 0.0, 0.0, 0.0};  // assembly, PCG, driver, preconditioner setup (in PCG)
   int64_t launches = 0;  // kernels enqueued by this context so far
 };
 

@@ -208,3 +208,44 @@ def test_cg_not_converged_and_breakdown():
     z = R.CsrMatrix(np.array([0.0, 0.0]), np.array([0, 1]), np.array([0, 1, 2]))
     assert g.cg_solve(z, np.array([1.0, 1.0]), 10, 1e-12) is None and "BREAKDOWN" in g.last_error
     assert g.cg_solve_precond(z, np.array([1.0, 1.0]), 10, 1e-12, R.Precond.JACOBI) is None
+
+
+# ------------------------------------------------------------------ AMG preconditioners
+@pytest.mark.parametrize("pc", [R.Precond.AMG, R.Precond.AMG_SA])
+def test_batched_disks_amg_match_fp64_lu(ctx, pc):
+    vo, to, p3, tr = W.disks(40, t_min=50, t_max=20000, seed=21)
+    C = R.prepare_patches(vo, to, p3, tr)
+    jac = R.unfold_charts(ctx, C, R.UnfoldOptions(precond=R.Precond.JACOBI))
+    res = R.unfold_charts(ctx, C, R.UnfoldOptions(precond=pc))
+    big = max(range(len(res)), key=lambda c: res[c].n_free)
+    for c in range(len(vo) - 1):
+        assert res[c].status == R.Status.OK, (c, res[c].status)
+        P = O.Pipeline(p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]], weld_tol=0.0, lu_limit=0)
+        assert O.uv_error(res[c].uv, P.superlu_uv(0)) <= MIXED_TOL
+    # the multigrid cycle needs far fewer Krylov iterations than Jacobi on the largest chart
+    assert res[big].cg_iters * 3 < jac[big].cg_iters, (res[big].cg_iters, jac[big].cg_iters)
+
+
+def test_cg_amg_poisson_and_elongated(known):
+    """gpu/src/solver.rs:912-935, :1032-1102: AMG/AMG-SA converge to the plain-CG solution
+    with fewer iterations on the 2-D Poisson and the elongated 1-D systems."""
+    g = R.GpuSolver.global_()
+    a, b = _poisson(400)
+    x_none, it_none = g.cg_solve_precond(a, b, 100_000, 1e-10, R.Precond.NONE)
+    for pc in (R.Precond.AMG, R.Precond.AMG_SA):
+        r = g.cg_solve_precond(a, b, 100_000, 1e-10, pc)
+        assert r is not None, g.last_error
+        x, it = r
+        n = a.rows()
+        for i in [0, n // 2, n - 1]:
+            assert abs(x[i] - x_none[i]) < 1e-4
+        assert it < it_none, (pc, it, it_none)
+    # kappa ~ 1e10: at equal residual the FP32 V-cycle leaves more low-mode error than plain
+    # FP64 CG, so the multigrid solve runs one decade tighter to meet the 1e-5 agreement
+    a, b = _lap1d(200_000)
+    x_none, it_none = g.cg_solve_precond(a, b, 200_000, 1e-10, R.Precond.NONE)
+    r = g.cg_solve_precond(a, b, 200_000, 1e-11, R.Precond.AMG_SA)
+    assert r is not None, g.last_error
+    for i in [0, 100_000, 199_999]:
+        assert abs(r[0][i] - x_none[i]) < 1e-5
+    assert r[1] < it_none
