@@ -454,16 +454,23 @@ __global__ void k_agg_lead_rows(int64_t n, const uint8_t* __restrict__ lead, con
   if (i < n) arow[i] = (lead[i] && glead[grp_of[i]]) ? 1 : 0;
 }
 
-// Dense Cholesky of each final chart block (<= kDirect rows) in shared memory, FP64
-// pivots; the factor is stored as FP32 lower-triangular rows.
-__global__ void __launch_bounds__(128) k_direct_factor(const int32_t* __restrict__ final_lvl,
-                                                       const int64_t* const* __restrict__ lvl_chart_row,
-                                                       const int32_t* const* __restrict__ lvl_rp,
-                                                       const int32_t* const* __restrict__ lvl_cols,
-                                                       const float* const* __restrict__ lvl_vals,
-                                                       const int64_t* __restrict__ fac_off, float* __restrict__ fac,
-                                                       int* __restrict__ bad) {
-  __shared__ double M[kDirect * kDirect];
+// Dense inverse of each final chart block (<= kDirect rows), one CTA per chart, FP64 in
+// shared memory: Cholesky A = L L^T, then Y = L^-1 (one column per thread), then
+// A^-1 = Y^T Y, stored as FP32 (symmetric, row-major m x m).  The V-cycle's coarse solve is
+// then one dense mat-vec per chart instead of two serial triangular sweeps.
+constexpr int kFactorThreads = 128;
+constexpr size_t kFactorSmem = 2 * sizeof(double) * kDirect * kDirect;
+
+__global__ void __launch_bounds__(kFactorThreads) k_direct_factor(const int32_t* __restrict__ final_lvl,
+                                                                  const int64_t* const* __restrict__ lvl_chart_row,
+                                                                  const int32_t* const* __restrict__ lvl_rp,
+                                                                  const int32_t* const* __restrict__ lvl_cols,
+                                                                  const float* const* __restrict__ lvl_vals,
+                                                                  const int64_t* __restrict__ fac_off, float* __restrict__ fac,
+                                                                  int* __restrict__ bad) {
+  extern __shared__ double smem[];
+  double* M = smem;                        // m x m, row-major; L in the lower triangle
+  double* Y = smem + kDirect * kDirect;    // Y[k * m + j] = (L^-1)[k][j]
   const int c = blockIdx.x;
   const int f = final_lvl[c];
   if (f < 0) return;
@@ -499,10 +506,23 @@ __global__ void __launch_bounds__(128) k_direct_factor(const int32_t* __restrict
     }
     __syncthreads();
   }
-  float* L = fac + fac_off[c];
+  // Y = L^-1: column j solves L y = e_j by forward substitution (rows above j are zero).
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    for (int i = 0; i < j; ++i) Y[i * m + j] = 0.0;
+    for (int i = j; i < m; ++i) {
+      double s = i == j ? 1.0 : 0.0;
+      for (int k = j; k < i; ++k) s -= M[i * m + k] * Y[k * m + j];
+      Y[i * m + j] = s / M[i * m + i];
+    }
+  }
+  __syncthreads();
+  // A^-1 = Y^T Y: (A^-1)[i][k] = sum_{j >= max(i,k)} Y[j][i] Y[j][k]
+  float* Ainv = fac + fac_off[c];
   for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
-    int i = t / m, k = t % m;
-    L[t] = k <= i ? (float)M[t] : 0.0f;
+    const int i = t / m, k = t % m;
+    double s = 0.0;
+    for (int j = i > k ? i : k; j < m; ++j) s += Y[j * m + i] * Y[j * m + k];
+    Ainv[t] = (float)s;
   }
 }
 
@@ -529,15 +549,11 @@ __device__ __forceinline__ void stf(float* p, int64_t i, const F<NR>& v) {
   else p[i] = v.c[0];
 }
 
-// rows of level-k charts that continue below k (and whose CG is still running)
-__device__ __forceinline__ bool row_live(int32_t c, int lvl, const int32_t* final_lvl, const int32_t* done) {
-  return final_lvl[c] > lvl && !done[c];
-}
-
 // The level kernels run over chart-aligned row tiles (one CTA per tile, one chart-state
-// check per CTA) as CSR-vector: LPR lanes per row, each lane covering ceil(8/LPR) entries in
-// one unrolled sweep, U rows in flight per sub-warp, block-uniform trip counts (every lane
-// takes part in the shuffles).  One generic row loop, four row operations.
+// check per CTA) as CSR-vector: LPR lanes per row, each lane covering K entries in one
+// unrolled sweep (longer rows finish in a remainder loop), U rows in flight per sub-warp,
+// block-uniform trip counts (every lane takes part in the shuffles).  One generic row loop,
+// four row operations; the shape per operator comes from its mean row length.
 struct LvlTiles {
   const int64_t* tab;    // [begin, end) pairs
   const int32_t* chart;  // chart of each tile
@@ -550,10 +566,9 @@ struct RowIn {
 };
 
 // Generic: for each row i of the tile, s = sum_e w(e) * g(col(e)); then fin(i, s).
-template <int NR, int LPR, int U, class W, class G, class Fin>
+template <int NR, int LPR, int U, int K, class W, class G, class Fin>
 __device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_t* ptr64, const int32_t* ptr32,
                                           const int32_t* __restrict__ cols, W w, G g, Fin fin) {
-  constexpr int K = (8 + LPR - 1) / LPR;
   const int sub = threadIdx.x % LPR;
   const int rpp = kAmgThreads / LPR;
   for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
@@ -608,7 +623,7 @@ __device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_
 }
 
 // Down 1: x = w D^-1 b;  t = b - A x  (x of neighbours formed on the fly).
-template <int NR, int LPR, int U>
+template <int NR, int LPR, int U, int K>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const int32_t* __restrict__ done,
                                                              const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                                                              const float* __restrict__ vals, const float* __restrict__ dinv,
@@ -616,7 +631,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const i
                                                              float* __restrict__ t) {
   const int64_t tl = blockIdx.x;
   if (done[T.chart[tl]]) return;
-  tile_rows<NR, LPR, U>(
+  tile_rows<NR, LPR, U, K>(
       T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, cols, [&](int64_t e) { return vals[e]; },
       [&](int32_t j) {
         F<NR> v = ldf<NR>(b, j);
@@ -640,28 +655,28 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const i
 }
 
 // Restrict: b_c = R t over the coarse rows (tiles of the coarse level).
-template <int NR, int LPR, int U>
+template <int NR, int LPR, int U, int K>
 __global__ void __launch_bounds__(kAmgThreads) k_restrict(LvlTiles T, const int32_t* __restrict__ done,
                                                           const int64_t* __restrict__ roff, const int32_t* __restrict__ rc,
                                                           const float* __restrict__ rv, const float* __restrict__ t,
                                                           float* __restrict__ bc) {
   const int64_t tl = blockIdx.x;
   if (done[T.chart[tl]]) return;
-  tile_rows<NR, LPR, U>(
+  tile_rows<NR, LPR, U, K>(
       T.tab[2 * tl], T.tab[2 * tl + 1], roff, nullptr, rc, [&](int64_t e) { return rv[e]; },
       [&](int32_t j) { return ldf<NR>(t, j); }, [&](int64_t I, const F<NR>& s) { stf<NR>(bc, I, s); });
 }
 
 // Up 1: y = x + alpha_c P x_c (alpha_c = 1: plain; > 1: over-correction of an unsmoothed
 // (piecewise-constant) coarse space, which underestimates the smooth error).
-template <int NR, int LPR, int U>
+template <int NR, int LPR, int U, int K>
 __global__ void __launch_bounds__(kAmgThreads) k_prolong_add(LvlTiles T, const int32_t* __restrict__ done,
                                                              const int64_t* __restrict__ poff, const int32_t* __restrict__ pc,
                                                              const float* __restrict__ pv, const float* __restrict__ xc,
                                                              const float* __restrict__ x, float* __restrict__ y, float alpha_c) {
   const int64_t tl = blockIdx.x;
   if (done[T.chart[tl]]) return;
-  tile_rows<NR, LPR, U>(
+  tile_rows<NR, LPR, U, K>(
       T.tab[2 * tl], T.tab[2 * tl + 1], poff, nullptr, pc, [&](int64_t e) { return alpha_c * pv[e]; },
       [&](int32_t j) { return ldf<NR>(xc, j); },
       [&](int64_t i, const F<NR>& s) {
@@ -673,7 +688,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_prolong_add(LvlTiles T, const i
 }
 
 // Up 2: x = y + w D^-1 (b - A y).
-template <int NR, int LPR, int U>
+template <int NR, int LPR, int U, int K>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int32_t* __restrict__ done,
                                                            const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                                                            const float* __restrict__ vals, const float* __restrict__ dinv,
@@ -681,7 +696,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int
                                                            float* __restrict__ x) {
   const int64_t tl = blockIdx.x;
   if (done[T.chart[tl]]) return;
-  tile_rows<NR, LPR, U>(
+  tile_rows<NR, LPR, U, K>(
       T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, cols, [&](int64_t e) { return vals[e]; },
       [&](int32_t j) { return ldf<NR>(y, j); },
       [&](int64_t i, const F<NR>& s) {
@@ -694,14 +709,16 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int
       });
 }
 
-// Direct solve of every chart at its last level: L L^T x = b (one warp per chart).
+// Direct solve of every chart at its last level: x = A^-1 b with the dense inverse (one CTA
+// of kDirect threads per chart, thread i forms row i; A^-1 is symmetric, so row i is read as
+// column i and the loads coalesce across threads).
 template <int NR>
-__global__ void __launch_bounds__(32) k_direct_solve(const int32_t* __restrict__ final_lvl, const int32_t* __restrict__ done,
-                                                     const int64_t* const* __restrict__ lvl_chart_row,
-                                                     float* const* __restrict__ lvl_b, float* const* __restrict__ lvl_x,
-                                                     const float* const* __restrict__ lvl_dinv,
-                                                     const int64_t* __restrict__ fac_off, const float* __restrict__ fac) {
-  __shared__ float y[NR][kDirect];
+__global__ void __launch_bounds__(kDirect) k_direct_solve(const int32_t* __restrict__ final_lvl, const int32_t* __restrict__ done,
+                                                          const int64_t* const* __restrict__ lvl_chart_row,
+                                                          float* const* __restrict__ lvl_b, float* const* __restrict__ lvl_x,
+                                                          const float* const* __restrict__ lvl_dinv,
+                                                          const int64_t* __restrict__ fac_off, const float* __restrict__ fac) {
+  __shared__ float bs[NR][kDirect];
   const int c = blockIdx.x;
   const int f = final_lvl[c];
   if (f < 0 || done[c]) return;
@@ -710,52 +727,30 @@ __global__ void __launch_bounds__(32) k_direct_solve(const int32_t* __restrict__
   if (m <= 0) return;
   const float* b = lvl_b[f];
   float* x = lvl_x[f];
-  const int lane = threadIdx.x;
+  const int i = threadIdx.x;
   if (m > kDirect) {  // aggregation stalled above the dense limit: x = D^-1 b
     const float* dv = lvl_dinv[f];
-    for (int i = lane; i < m; i += 32)
+    for (int r = i; r < m; r += blockDim.x)
 #pragma unroll
-      for (int k = 0; k < NR; ++k) x[NR * (r0 + i) + k] = dv[r0 + i] * b[NR * (r0 + i) + k];
+      for (int k = 0; k < NR; ++k) x[NR * (r0 + r) + k] = dv[r0 + r] * b[NR * (r0 + r) + k];
     return;
   }
-  const float* L = fac + fac_off[c];
-  for (int i = lane; i < m; i += 32)
+  if (i < m)
 #pragma unroll
-    for (int k = 0; k < NR; ++k) y[k][i] = b[NR * (r0 + i) + k];
-  __syncwarp();
-  // forward: L y = b
-  for (int i = 0; i < m; ++i) {
-    float s[NR];
+    for (int k = 0; k < NR; ++k) bs[k][i] = b[NR * (r0 + i) + k];
+  __syncthreads();
+  if (i >= m) return;
+  const float* Ainv = fac + fac_off[c];
+  float s[NR];
 #pragma unroll
-    for (int k = 0; k < NR; ++k) s[k] = 0.0f;
-    for (int j = lane; j < i; j += 32)
+  for (int k = 0; k < NR; ++k) s[k] = 0.0f;
+  for (int j = 0; j < m; ++j) {
+    const float a = Ainv[j * m + i];
 #pragma unroll
-      for (int k = 0; k < NR; ++k) s[k] += L[i * m + j] * y[k][j];
-#pragma unroll
-    for (int k = 0; k < NR; ++k) s[k] = warp_sum(s[k]);
-    if (lane == 0)
-#pragma unroll
-      for (int k = 0; k < NR; ++k) y[k][i] = (y[k][i] - s[k]) / L[i * m + i];
-    __syncwarp();
+    for (int k = 0; k < NR; ++k) s[k] += a * bs[k][j];
   }
-  // backward: L^T x = y
-  for (int i = m - 1; i >= 0; --i) {
-    float s[NR];
 #pragma unroll
-    for (int k = 0; k < NR; ++k) s[k] = 0.0f;
-    for (int j = i + 1 + lane; j < m; j += 32)
-#pragma unroll
-      for (int k = 0; k < NR; ++k) s[k] += L[j * m + i] * y[k][j];
-#pragma unroll
-    for (int k = 0; k < NR; ++k) s[k] = warp_sum(s[k]);
-    if (lane == 0)
-#pragma unroll
-      for (int k = 0; k < NR; ++k) y[k][i] = (y[k][i] - s[k]) / L[i * m + i];
-    __syncwarp();
-  }
-  for (int i = lane; i < m; i += 32)
-#pragma unroll
-    for (int k = 0; k < NR; ++k) x[NR * (r0 + i) + k] = y[k][i];
+  for (int k = 0; k < NR; ++k) x[NR * (r0 + i) + k] = s[k];
 }
 
 }  // namespace
@@ -1088,7 +1083,8 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   RUV_CUDA(cudaMemcpyAsync(H->d_lvl_dinv, dvs.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, s));
   int* bad = ovf + 1;
   if (NC > 0) {
-    k_direct_factor<<<(unsigned)NC, 128, 0, s>>>(H->final_lvl, H->d_lvl_chart_row, d_rp, d_cols, d_vals, H->fac_off,
+    RUV_CUDA(cudaFuncSetAttribute(k_direct_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFactorSmem));
+    k_direct_factor<<<(unsigned)NC, kFactorThreads, kFactorSmem, s>>>(H->final_lvl, H->d_lvl_chart_row, d_rp, d_cols, d_vals, H->fac_off,
                                                  H->fac, bad);
     count_launches(1);
   }
@@ -1135,14 +1131,18 @@ void amg_bind(Ctx& ctx, AmgHierarchy* H, float* r0, float* z0) {
 
 namespace {
 
-int lanes_for(double avg) { return avg <= 5 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32; }
+// Lanes per row from the operator's mean row length: one lane per row for the tentative
+// prolongator (one entry per row), then enough lanes that K = 4 slots per lane cover a
+// typical row in one sweep with two rows in flight (8 independent gathers per lane).
+int lanes_for(double avg) { return avg <= 1.5 ? 1 : avg <= 8 ? 2 : avg <= 16 ? 4 : avg <= 32 ? 8 : 16; }
 
 #define RUV_LPR_SWITCH(lpr, CALL) \
   switch (lpr) {                   \
-    case 4: CALL(4, 2); break;     \
-    case 8: CALL(8, 2); break;     \
-    case 16: CALL(16, 1); break;   \
-    default: CALL(32, 1); break;   \
+    case 1: CALL(1, 4, 2); break;  \
+    case 2: CALL(2, 2, 4); break;  \
+    case 4: CALL(4, 2, 4); break;  \
+    case 8: CALL(8, 2, 4); break;  \
+    default: CALL(16, 1, 4); break; \
   }
 
 template <int NR>
@@ -1156,24 +1156,24 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
-#define CALL(X, UU)                                                                                              \
-  k_smooth_down<NR, X, UU><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.x, \
+#define CALL(X, UU, KK)                                                                                              \
+  k_smooth_down<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.x, \
                                                             L.t)
     RUV_LPR_SWITCH(la, CALL)
 #undef CALL
     ++launches;
     if (C.all.n == 0) continue;
     const int lr = lanes_for(C.n ? (double)L.n_pnnz / (double)C.n : 1.0);
-#define CALL(X, UU) k_restrict<NR, X, UU><<<(unsigned)C.all.n, B, 0, s>>>(C.all, done, L.roff, L.rc, L.rv, L.t, C.b)
+#define CALL(X, UU, KK) k_restrict<NR, X, UU, KK><<<(unsigned)C.all.n, B, 0, s>>>(C.all, done, L.roff, L.rc, L.rv, L.t, C.b)
     RUV_LPR_SWITCH(lr, CALL)
 #undef CALL
     ++launches;
   }
   if (NR == 2)
-    k_direct_solve<2><<<(unsigned)H->n_charts, 32, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b, H->d_lvl_x,
+    k_direct_solve<2><<<(unsigned)H->n_charts, kDirect, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b, H->d_lvl_x,
                                                            H->d_lvl_dinv, H->fac_off, H->fac);
   else
-    k_direct_solve<1><<<(unsigned)H->n_charts, 32, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b, H->d_lvl_x,
+    k_direct_solve<1><<<(unsigned)H->n_charts, kDirect, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b, H->d_lvl_x,
                                                            H->d_lvl_dinv, H->fac_off, H->fac);
   ++launches;
   for (int k = K - 2; k >= 0; --k) {
@@ -1181,14 +1181,14 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
     const int lp = lanes_for(L.n ? (double)L.n_pnnz / (double)L.n : 1.0);
-#define CALL(X, UU)                                                                                                  \
-  k_prolong_add<NR, X, UU><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.poff, L.pc, L.pv, C.x, L.x, L.y, \
+#define CALL(X, UU, KK)                                                                                                  \
+  k_prolong_add<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.poff, L.pc, L.pv, C.x, L.x, L.y, \
                                                             H->alpha_c)
     RUV_LPR_SWITCH(lp, CALL)
 #undef CALL
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
-#define CALL(X, UU) \
-  k_smooth_up<NR, X, UU><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.y, L.x)
+#define CALL(X, UU, KK) \
+  k_smooth_up<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.y, L.x)
     RUV_LPR_SWITCH(la, CALL)
 #undef CALL
     launches += 2;

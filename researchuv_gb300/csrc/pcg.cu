@@ -16,10 +16,16 @@
 // p.q product fused into the same pass.
 //
 // Precision: RUV_PREC_FP64 runs the reference's recurrence in FP64.  RUV_PREC_MIXED runs
-// the SpMV, preconditioner and CG recurrence in FP32 and keeps FP64 for the solution
-// accumulator and the true residual r = b - A x (FP64 values), recomputed per chart
-// whenever the FP32 residual has dropped by `kDelta` (100x) since the last true residual
-// ("reliable updates"); convergence is judged on the FP64 true residual only.
+// the SpMV, preconditioner and CG recurrence in FP32 and keeps an extended-precision
+// solution accumulator and true residual r = b - A x, recomputed per chart whenever the
+// FP32 residual has dropped by `kDelta` (100x) since the last true residual ("reliable
+// updates"); convergence is judged on the true residual only.  The extended precision is
+// double-float (a value is an unevaluated FP32 pair hi + lo, ~48 significant bits, FP32
+// instructions only: GB300's FP64 pipe is a small fraction of its FP32 rate).  The true
+// residual is formed as r_i = b_i - rs_i x_i - sum_j a_ij (x_j - x_i), rs_i the FP64 row
+// sum: for a Laplacian with eliminated pins rs_i is zero away from the pins, so the
+// products are of the small differences x_j - x_i rather than of x itself and the
+// cancellation in b - A x costs no more than the FP64 product does.
 #include "system.cuh"
 
 #include <algorithm>
@@ -52,7 +58,7 @@ struct ChartState {
   int32_t refinements;
   float alpha32;  // alpha / beta rounded once per chart for the FP32 tile kernels
   float beta32;
-  int32_t pad;
+  float rscale;   // 1 / ||b|| as FP32 (1 when b = 0): FP32 sums of squares of r * rscale stay in range
 };
 
 template <class S, int NR>
@@ -86,6 +92,53 @@ __device__ __forceinline__ void stv(S* p, int64_t i, const V<S, NR>& v) {
   }
 }
 
+// Double-float arithmetic: TwoSum (Knuth) and the FMA TwoProduct carry the rounding error
+// of an FP32 add / multiply exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+// (Sh, Sl) += (ah + al) * (dh + dl), dropping the al * dl term (2^-48 relative).
+__device__ __forceinline__ void df_fma(float ah, float al, float dh, float dl, float& Sh, float& Sl) {
+  const float p = ah * dh;
+  const float t = fmaf(ah, dl, fmaf(al, dh, fmaf(ah, dh, -p)));
+  float sh, se;
+  two_sum(Sh, p, sh, se);
+  Sh = sh;
+  Sl += se + t;
+}
+// A row's double-float value: NR hi parts then NR lo parts (one 16- / 8-byte access).
+template <int NR>
+struct DF {
+  float h[NR], l[NR];
+};
+template <int NR>
+__device__ __forceinline__ DF<NR> lddf(const float* p, int64_t i) {
+  DF<NR> r;
+  if constexpr (NR == 2) {
+    const float4 t = reinterpret_cast<const float4*>(p)[i];
+    r.h[0] = t.x;
+    r.h[1] = t.y;
+    r.l[0] = t.z;
+    r.l[1] = t.w;
+  } else {
+    const float2 t = reinterpret_cast<const float2*>(p)[i];
+    r.h[0] = t.x;
+    r.l[0] = t.y;
+  }
+  return r;
+}
+template <int NR>
+__device__ __forceinline__ void stdf(float* p, int64_t i, const DF<NR>& v) {
+  if constexpr (NR == 2) reinterpret_cast<float4*>(p)[i] = make_float4(v.h[0], v.h[1], v.l[0], v.l[1]);
+  else reinterpret_cast<float2*>(p)[i] = make_float2(v.h[0], v.l[0]);
+}
+__device__ __forceinline__ void split_f64(double v, float& h, float& l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
 struct Tiles {
   const int64_t* tab;      // [begin, end) pairs
   const int32_t* chart;    // chart of each tile
@@ -108,11 +161,13 @@ __global__ void __launch_bounds__(kTileThreads) k_dinv(int64_t n, const double* 
 
 // Initial state: x = 0, r = b, z = M^-1 r, p = z.  Partials (FP64, once per solve): b.b, r.z,
 // #zero diagonals.
+// Mixed precision also: the double-float solution xdf = 0 and right-hand side bdf = b.
 template <class S, int NR>
 __global__ void __launch_bounds__(kTileThreads) k_init(Tiles T, const double* __restrict__ b, const double* __restrict__ diag,
                                                        const S* __restrict__ dinv, int use_jacobi, double* __restrict__ x64,
                                                        S* __restrict__ xs, S* __restrict__ r, S* __restrict__ z,
-                                                       S* __restrict__ p, double* __restrict__ part) {
+                                                       S* __restrict__ p, double* __restrict__ part,
+                                                       float* __restrict__ xdf, float* __restrict__ bdf) {
   __shared__ double sh[3 * 32];
   int64_t t = blockIdx.x;
   double acc[3] = {0.0, 0.0, 0.0};
@@ -134,6 +189,16 @@ __global__ void __launch_bounds__(kTileThreads) k_init(Tiles T, const double* __
     for (int k = 0; k < NR; ++k) z64.c[k] = 0.0;
     stv<double, NR>(x64, i, z64);
     if (xs) stv<S, NR>(xs, i, zero);
+    if (xdf) {
+      DF<NR> xz, bd;
+#pragma unroll
+      for (int k = 0; k < NR; ++k) {
+        xz.h[k] = xz.l[k] = 0.0f;
+        split_f64(bv.c[k], bd.h[k], bd.l[k]);
+      }
+      stdf<NR>(xdf, i, xz);
+      stdf<NR>(bdf, i, bd);
+    }
     stv<S, NR>(r, i, rv);
     stv<S, NR>(z, i, zv);
     stv<S, NR>(p, i, zv);
@@ -226,7 +291,8 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_pq(Tiles T, const ChartSt
   if (threadIdx.x == 0) part[t] = (double)acc[0];
 }
 
-// x += alpha p; r -= alpha q; z = M^-1 r.  Partials: r.r, r.z.
+// x += alpha p; r -= alpha q; z = M^-1 r.  Partials: r.r, r.z.  precond: 0 = none (z = r),
+// 1 = Jacobi, 2 = applied separately afterwards (z is not written).
 template <class S, int NR>
 __global__ void __launch_bounds__(kTileThreads) k_update(Tiles T, const ChartState* __restrict__ st,
                                                          const S* __restrict__ dinv, int use_jacobi,
@@ -241,7 +307,7 @@ __global__ void __launch_bounds__(kTileThreads) k_update(Tiles T, const ChartSta
   S acc[2] = {S(0), S(0)};
   for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
     V<S, NR> xv = ldv<S, NR>(x, i), rv = ldv<S, NR>(r, i), pv = ldv<S, NR>(p, i), qv = ldv<S, NR>(q, i), zv;
-    const S di = use_jacobi ? dinv[i] : S(1);
+    const S di = use_jacobi == 1 ? dinv[i] : S(1);
 #pragma unroll
     for (int k = 0; k < NR; ++k) {
       xv.c[k] += alpha * pv.c[k];
@@ -252,7 +318,7 @@ __global__ void __launch_bounds__(kTileThreads) k_update(Tiles T, const ChartSta
     }
     stv<S, NR>(x, i, xv);
     stv<S, NR>(r, i, rv);
-    stv<S, NR>(z, i, zv);
+    if (use_jacobi != 2) stv<S, NR>(z, i, zv);
   }
   block_sum_t<2, S>(acc, sh);
   if (threadIdx.x == 0) {
@@ -277,82 +343,170 @@ __global__ void __launch_bounds__(kTileThreads) k_direction(Tiles T, const Chart
   }
 }
 
+// Mixed precision, once per solve: the low FP32 halves of the FP64 values (vals32 holds the
+// high halves) and the FP64 row sums as double-float pairs.
+__global__ void k_split_rows(int64_t n, const int32_t* __restrict__ row_ptr, const double* __restrict__ vals,
+                             const float* __restrict__ vals32, float* __restrict__ vals_lo, float2* __restrict__ rsum) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double acc = 0.0;
+  for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
+    const double v = vals[e];
+    vals_lo[e] = (float)(v - (double)vals32[e]);
+    acc += v;
+  }
+  float h, l;
+  split_f64(acc, h, l);
+  rsum[i] = make_float2(h, l);
+}
+
 // Mixed precision, refresh step 1 (charts that asked for a refresh, or every chart when
-// `all`): fold the FP32 increment into the FP64 solution, xs = 0.  A separate launch from
-// the true residual, which reads x64 of neighbouring rows in other tiles.
+// `all`): fold the FP32 increment into the double-float solution, xs = 0.  A separate launch
+// from the true residual, which reads the solution of neighbouring rows in other tiles.
+// With `all` (end of the solve) the FP64 solution x64 = hi + lo is written too.
 template <int NR>
 __global__ void __launch_bounds__(kTileThreads) k_fold(Tiles T, const ChartState* __restrict__ st, int all,
-                                                       double* __restrict__ x64, float* __restrict__ xs) {
+                                                       float* __restrict__ xdf, float* __restrict__ xs,
+                                                       double* __restrict__ x64) {
   int64_t t = blockIdx.x;
   const ChartState& cs = st[T.chart[t]];
   if (!all && (cs.state != kActive || !cs.refresh)) return;
   for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
-    V<double, NR> xv = ldv<double, NR>(x64, i);
+    DF<NR> xv = lddf<NR>(xdf, i);
     V<float, NR> dv = ldv<float, NR>(xs, i), zero;
 #pragma unroll
     for (int k = 0; k < NR; ++k) {
-      xv.c[k] += (double)dv.c[k];
+      float sh, se;
+      two_sum(xv.h[k], dv.c[k], sh, se);
+      se += xv.l[k];
+      xv.h[k] = sh + se;  // renormalise: |lo| <= ulp(hi) / 2
+      xv.l[k] = se - (xv.h[k] - sh);
       zero.c[k] = 0.f;
     }
-    stv<double, NR>(x64, i, xv);
+    stdf<NR>(xdf, i, xv);
     stv<float, NR>(xs, i, zero);
+    if (all) {
+      V<double, NR> x;
+#pragma unroll
+      for (int k = 0; k < NR; ++k) x.c[k] = (double)xv.h[k] + (double)xv.l[k];
+      stv<double, NR>(x64, i, x);
+    }
   }
 }
 
-// Mixed precision, refresh step 2: r = b - A x64 in FP64; r32 = r; z = M^-1 r.
-// Partials: r.r (FP64), r.z.
-template <int NR, int LPR>
+// Mixed precision, refresh step 2: r = b - A x in double-float (see the file comment),
+// r32 = r, z = M^-1 r (precond 0: z = r, 1: Jacobi, 2: applied separately, z not written).
+// Partials: r.r and r.z, summed in FP32 over r * rscale and rescaled per tile.  The CSR-vector
+// shape (LPR lanes, K = ceil(8 / LPR) slots, U rows in flight) is the tuned SpMV's.
+template <int NR, int LPR, int U>
 __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const ChartState* __restrict__ st,
                                                                 const int32_t* __restrict__ row_ptr,
-                                                                const int32_t* __restrict__ cols,
-                                                                const double* __restrict__ vals, const double* __restrict__ b,
-                                                                const float* __restrict__ dinv, int use_jacobi,
-                                                                const double* __restrict__ x64, float* __restrict__ r,
-                                                                float* __restrict__ z, double* __restrict__ part) {
-  __shared__ double sh[2 * 32];
-  int64_t t = blockIdx.x;
+                                                                const int32_t* __restrict__ cols, const float* __restrict__ vh,
+                                                                const float* __restrict__ vl, const float2* __restrict__ rsum,
+                                                                const float* __restrict__ bdf, const float* __restrict__ dinv,
+                                                                int precond, const float* __restrict__ xdf,
+                                                                float* __restrict__ r, float* __restrict__ z,
+                                                                double* __restrict__ part) {
+  constexpr int K = (8 + LPR - 1) / LPR;
+  __shared__ float sh[2 * 32];
+  const int64_t t = blockIdx.x;
   const ChartState& cs = st[T.chart[t]];
   if (cs.state != kActive || !cs.refresh) return;
+  const float rsc = cs.rscale;
   const int sub = threadIdx.x % LPR;
-  double acc[2] = {0.0, 0.0};
+  const int rpp = kTileThreads / LPR;
+  float acc[2] = {0.0f, 0.0f};
   const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
-  for (int64_t base = beg; base < end; base += blockDim.x / LPR) {
-    const int64_t i = base + threadIdx.x / LPR;
-    const bool valid = i < end;
-    const int lo = valid ? row_ptr[i] : 0, hi = valid ? row_ptr[i + 1] : 0;
-    V<double, NR> s;
+  for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
+    int lo[U], hi[U];
+    DF<NR> xi[U];
 #pragma unroll
-    for (int k = 0; k < NR; ++k) s.c[k] = 0.0;
-    for (int e = lo + sub; e < hi; e += LPR) {
-      const double a = vals[e];
-      const V<double, NR> xv = ldv<double, NR>(x64, cols[e]);
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      const bool valid = i < end;
+      lo[u] = valid ? row_ptr[i] : 0;
+      hi[u] = valid ? row_ptr[i + 1] : 0;
+      xi[u] = lddf<NR>(xdf, valid ? i : beg);
+    }
+    float ah[U][K], al[U][K];
+    int cv[U][K];
 #pragma unroll
-      for (int k = 0; k < NR; ++k) s.c[k] += a * xv.c[k];
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int e = lo[u] + sub + k * LPR;
+        const bool in = e < hi[u];
+        ah[u][k] = in ? vh[e] : 0.0f;
+        al[u][k] = in ? vl[e] : 0.0f;
+        cv[u][k] = in ? cols[e] : -1;
+      }
+    float Sh[U][NR], Sl[U][NR];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int c = 0; c < NR; ++c) Sh[u][c] = Sl[u][c] = 0.0f;
+      auto entry = [&](float a_h, float a_l, int j) {
+        const DF<NR> xj = lddf<NR>(xdf, j);
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+          float dh, dl;
+          two_sum(xj.h[c], -xi[u].h[c], dh, dl);
+          dl += xj.l[c] - xi[u].l[c];
+          df_fma(a_h, a_l, dh, dl, Sh[u][c], Sl[u][c]);
+        }
+      };
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (cv[u][k] >= 0) entry(ah[u][k], al[u][k], cv[u][k]);
+      for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) entry(vh[e], vl[e], cols[e]);
     }
 #pragma unroll
-    for (int o = LPR / 2; o > 0; o >>= 1)
+    for (int u = 0; u < U; ++u) {
 #pragma unroll
-      for (int k = 0; k < NR; ++k) s.c[k] += __shfl_xor_sync(0xffffffffu, s.c[k], o, LPR);
-    if (valid && sub == 0) {
-      const V<double, NR> bv = ldv<double, NR>(b, i);
-      const float di = use_jacobi ? dinv[i] : 1.0f;
-      V<float, NR> rv, zv;
+      for (int o = LPR / 2; o > 0; o >>= 1)
 #pragma unroll
-      for (int k = 0; k < NR; ++k) {
-        double res = bv.c[k] - s.c[k];
-        acc[0] += res * res;
-        rv.c[k] = (float)res;
-        zv.c[k] = rv.c[k] * di;
-        acc[1] += (double)(rv.c[k] * zv.c[k]);
+        for (int c = 0; c < NR; ++c) {
+          const float oh = __shfl_xor_sync(0xffffffffu, Sh[u][c], o, LPR);
+          const float ol = __shfl_xor_sync(0xffffffffu, Sl[u][c], o, LPR);
+          float s2, e2;
+          two_sum(Sh[u][c], oh, s2, e2);
+          Sh[u][c] = s2;
+          Sl[u][c] += ol + e2;
+        }
+      const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      if (sub == 0 && i < end) {
+        const float2 rs = rsum[i];
+        const DF<NR> bv = lddf<NR>(bdf, i);
+        const float di = precond == 1 ? dinv[i] : 1.0f;
+        V<float, NR> rv, zv;
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+          // A x = rs * x_i + S
+          float th = 0.0f, tl = 0.0f;
+          df_fma(rs.x, rs.y, xi[u].h[c], xi[u].l[c], th, tl);
+          float ah2, ae2;
+          two_sum(th, Sh[u][c], ah2, ae2);
+          const float axl = tl + Sl[u][c] + ae2;
+          // r = b - A x
+          float uh, ue;
+          two_sum(bv.h[c], -ah2, uh, ue);
+          ue += bv.l[c] - axl;
+          rv.c[c] = uh + ue;
+          zv.c[c] = rv.c[c] * di;
+          const float rs_ = rv.c[c] * rsc;
+          acc[0] += rs_ * rs_;
+          acc[1] += rs_ * (zv.c[c] * rsc);
+        }
+        stv<float, NR>(r, i, rv);
+        if (precond != 2) stv<float, NR>(z, i, zv);
       }
-      stv<float, NR>(r, i, rv);
-      stv<float, NR>(z, i, zv);
     }
   }
-  block_sum<2>(acc, sh);
+  block_sum_t<2, float>(acc, sh);
   if (threadIdx.x == 0) {
-    part[2 * t] = acc[0];
-    part[2 * t + 1] = acc[1];
+    const double inv = 1.0 / ((double)rsc * (double)rsc);
+    part[2 * t] = (double)acc[0] * inv;
+    part[2 * t + 1] = (double)acc[1] * inv;
   }
 }
 
@@ -378,6 +532,7 @@ __global__ void __launch_bounds__(kChartThreads) k_chart_init(Tiles T, ChartStat
   ChartState s{};
   s.bnorm = sqrt(v[0]);
   s.tol_abs = s.bnorm <= 1e-300 ? tol : tol * s.bnorm;
+  s.rscale = s.bnorm > 0.0 ? (float)fmin(fmax(1.0 / s.bnorm, 1e-30), 1e30) : 1.0f;
   s.rr = v[0];
   s.r_ref = s.bnorm;
   s.rz = precond_none ? v[0] : v[1];
@@ -631,6 +786,32 @@ struct TileTable {
   std::vector<int32_t> chart;
 };
 
+// Mixed precision's double-float state: solution and right-hand side (2 * NR floats per
+// row), the low halves of the FP64 values and the FP64 row sums (k_split_rows, launched here).
+struct MixedExtras {
+  float* xdf = nullptr;
+  float* bdf = nullptr;
+  float* vals_lo = nullptr;
+  float2* rsum = nullptr;
+};
+
+MixedExtras mixed_extras(Ctx& ctx, DevSystem& sys, int nr) {
+  MixedExtras m;
+  if (nr == 0) return m;
+  const int64_t N = sys.n_rows;
+  m.xdf = ctx.ws.get<float>("pcg.xdf", 2 * nr * N);
+  m.bdf = ctx.ws.get<float>("pcg.bdf", 2 * nr * N);
+  m.vals_lo = ctx.ws.get<float>("pcg.vals_lo", sys.nnz);
+  m.rsum = ctx.ws.get<float2>("pcg.rsum", N);
+  if (N > 0) {
+    k_split_rows<<<div_up(N, kTileThreads), kTileThreads, 0, ctx.stream>>>(N, sys.row_ptr, sys.vals, sys.vals32, m.vals_lo,
+                                                                           m.rsum);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
+  return m;
+}
+
 template <class S, int NR, int LPR, int U>
 void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st, int* n_active,
              std::vector<ChartState>& out) {
@@ -649,6 +830,7 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
   float* dinv32 = mixed ? reinterpret_cast<float*>(dinv) : nullptr;
   double* part = ws.get<double>("pcg.part", 3 * NTL);
   const S* vals = mixed ? reinterpret_cast<const S*>(sys.vals32) : reinterpret_cast<const S*>(sys.vals);
+  MixedExtras mx = mixed_extras(ctx, sys, mixed ? NR : 0);
   RUV_CUDA(cudaMemsetAsync(n_active, 0, sizeof(int), s));
   if (NR_ > 0) {
     k_dinv<S><<<div_up(NR_, kTileThreads), kTileThreads, 0, s>>>(NR_, sys.diag, dinv);
@@ -656,7 +838,8 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
     RUV_LAUNCH_CHECK();
   }
   if (NTL > 0) {
-    k_init<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, sys.b, sys.diag, dinv, jac, x64, xs, r, z, p, part);
+    k_init<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, sys.b, sys.diag, dinv, jac, x64, xs, r, z, p, part, mx.xdf,
+                                                         mx.bdf);
     count_launches(1);
     RUV_LAUNCH_CHECK();
   }
@@ -680,10 +863,10 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
         k_chart_beta<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
       } else {
         k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0);
-        k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, x64, reinterpret_cast<float*>(xs));
-        k_true_residual<NR, 8><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, sys.vals, sys.b, dinv32,
-                                                                     jac, x64, reinterpret_cast<float*>(r),
-                                                                     reinterpret_cast<float*>(z), part);
+        k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, mx.xdf, reinterpret_cast<float*>(xs), x64);
+        k_true_residual<NR, LPR, U><<<(unsigned)NTL, kTileThreads, 0, s>>>(
+            T, st, sys.row_ptr, sys.cols, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, jac, mx.xdf,
+            reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
         k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0);
       }
       k_direction<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
@@ -714,8 +897,8 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
     cudaGraphDestroy(graph);
   }
   if (mixed && NTL > 0) {
-    // fold any FP32 increment still pending (charts that stopped between refreshes)
-    k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 1, x64, reinterpret_cast<float*>(xs));
+    // fold any FP32 increment still pending (charts that stopped between refreshes); x64 = xdf
+    k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 1, mx.xdf, reinterpret_cast<float*>(xs), x64);
     count_launches(1);
     RUV_LAUNCH_CHECK();
   }
@@ -747,6 +930,7 @@ void run_pcg_amg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
   S* xiter = mixed ? xs : reinterpret_cast<S*>(x64);
   double* part = ws.get<double>("pcg.part", 3 * NTL);
   double* part2 = ws.get<double>("pcg.part2", 2 * NTL);
+  MixedExtras mx = mixed_extras(ctx, sys, mixed ? NR : 0);
   int32_t* done = ws.get<int32_t>("pcg.done", NC);
   std::string info;
   AmgHierarchy* H = amg_setup(ctx, sys, smooth, info);
@@ -769,7 +953,8 @@ void run_pcg_amg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
     count_launches(1);
   }
   if (NTL > 0) {
-    k_init<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, sys.b, sys.diag, dinv, 1, x64, xs, r, z, p, part);
+    k_init<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, sys.b, sys.diag, dinv, 1, x64, xs, r, z, p, part, mx.xdf,
+                                                         mx.bdf);
     count_launches(1);
   }
   k_chart_init<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, o.tol, 0, n_active);  // (rz replaced below)
@@ -798,13 +983,13 @@ void run_pcg_amg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
       int l = 0;
       k_spmv_pq<S, NR, LPR, U><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, p, q, part);
       k_chart_alpha<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, n_active);
-      k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, dinv, 0, xiter, r, z, p, q, part);
+      k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, dinv, 2, xiter, r, z, p, q, part);
       if (mixed) {
         k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1);
-        k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, x64, reinterpret_cast<float*>(xs));
-        k_true_residual<NR, 8><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, sys.vals, sys.b,
-                                                                     dinv32, 0, x64, reinterpret_cast<float*>(r),
-                                                                     reinterpret_cast<float*>(z), part);
+        k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, mx.xdf, reinterpret_cast<float*>(xs), x64);
+        k_true_residual<NR, LPR, U><<<(unsigned)NTL, kTileThreads, 0, s>>>(
+            T, st, sys.row_ptr, sys.cols, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, 2, mx.xdf,
+            reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
         k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1);
         l += 4;
       } else {
@@ -848,7 +1033,7 @@ void run_pcg_amg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
     cudaGraphDestroy(graph);
   }
   if (mixed && NTL > 0) {
-    k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 1, x64, reinterpret_cast<float*>(xs));
+    k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 1, mx.xdf, reinterpret_cast<float*>(xs), x64);
     count_launches(1);
     RUV_LAUNCH_CHECK();
   }
@@ -1230,7 +1415,7 @@ extern "C" ruv_status ruv_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, co
   Tiles T{S->tab, S->tchart, S->chart_tile, n_tiles};
   k_dinv<double><<<div_up(n, kTileThreads), kTileThreads, 0, s>>>(n, S->diag, S->dinv);
   k_init<double, 1><<<(unsigned)n_tiles, kTileThreads, 0, s>>>(T, b, S->diag, S->dinv, jac, x, nullptr, S->r, S->z, S->p,
-                                                               S->part);
+                                                               S->part, nullptr, nullptr);
   k_chart_init<<<1, kChartThreads, 0, s>>>(T, &S->st, S->part, tol, none, &S->n_active);
   const double avg = (double)nnz / (double)n;
   const int lpr = avg <= 5 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32;
