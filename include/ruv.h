@@ -85,6 +85,19 @@ ruv_status ruv_cg_solve(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const i
 ruv_status ruv_apply_ic0(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols,
                          const double* vals, const double* r, double* z_out);
 
+/* The IC(0) factor the preconditioner builds on the device, copied out for inspection: what
+ * factor_ic0 returns to the reference's own tests (gpu/src/precond.rs:145-205; with
+ * `colored`, of the colour-permuted matrix, precond.rs:49-123).  l_ptr[n+1] receives the row
+ * offsets, l_cols / l_vals (capacity `cap`) the rows of L with the diagonal last, to_orig[n]
+ * the position -> original row map (identity without colouring), *nnz_out the factor's
+ * nonzeros, *levels_out the dependency-level count (the larger of the two sweeps),
+ * *colours_out the colour count (0 without colouring).  BAD_INPUT when nnz exceeds cap
+ * (counts are still written); BREAKDOWN where factor_ic0 returns None. */
+ruv_status ruv_ic0_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols,
+                          const double* vals, int32_t colored, int64_t cap, int64_t* l_ptr,
+                          int32_t* l_cols, double* l_vals, int32_t* to_orig, int64_t* nnz_out,
+                          int32_t* levels_out, int32_t* colours_out);
+
 /* Variant of ruv_cg_solve that allocates nothing, for callers that cannot call cudaMalloc:
  * code running inside a host application that owns all device memory through its own
  * allocator or memory pool (a renderer, a game engine, a plugin host with a fixed budget),

@@ -17,6 +17,8 @@
 //   meshgen fixtures     unwrap/src/meshgen.rs:12-198
 //   chart_distortion     unwrap/src/metrics.rs:41-141
 //   vector arithmetic    math/src/vec.rs:100-124
+//   IC(0) + colouring    gpu/src/precond.rs:49-123 (graph_coloring, color_permutation,
+//                        permute_csr), :145-262 (factor_ic0, tri_levels, transpose_lower)
 //
 // Arithmetic follows the Rust evaluation order (left-to-right sums, no FMA contraction:
 // compile with -ffp-contract=off) so that results are bit-identical to the reference on
@@ -965,6 +967,182 @@ void chart_distortion(const Mesh& mesh, const Chart& ch, const std::vector<V2>& 
   out[4] = (double)folds;
 }
 
+
+// ---------------------------------------------------------------- precond.rs IC(0)
+struct Csr {
+  int64_t n = 0;
+  std::vector<int64_t> ptr, cols;
+  std::vector<double> vals;
+};
+
+// factor_ic0 (gpu/src/precond.rs:145-205): IC(0) on the lower pattern, natural order, rows
+// of L with the strictly lower entries ascending and the diagonal last; pivot floor
+// 1e-12 * max(|a_ii|, 1e-30).  false where the reference returns None.
+bool ic0_factor(const Csr& a, Csr& L) {
+  const int64_t n = a.n;
+  std::vector<std::map<int64_t, double>> rows(n);
+  std::vector<double> diag(n, 0.0);
+  L.n = n;
+  L.ptr.assign(1, 0);
+  L.cols.clear();
+  L.vals.clear();
+  for (int64_t i = 0; i < n; ++i) {
+    std::vector<std::pair<int64_t, double>> low;
+    for (int64_t e = a.ptr[i]; e < a.ptr[i + 1]; ++e)
+      if (a.cols[e] < i) low.push_back({a.cols[e], a.vals[e]});
+    std::sort(low.begin(), low.end(), [](const std::pair<int64_t, double>& x, const std::pair<int64_t, double>& y) {
+      return x.first < y.first;
+    });
+    for (auto& kv : low) {
+      const int64_t k = kv.first;
+      double s_ = kv.second;
+      for (auto it = rows[i].begin(); it != rows[i].end() && it->first < k; ++it) {
+        auto f = rows[k].find(it->first);
+        if (f != rows[k].end()) s_ -= it->second * f->second;
+      }
+      const double l_kk = diag[k];
+      if (std::fabs(l_kk) < 1e-300) return false;
+      rows[i][k] = s_ / l_kk;  // a repeated column overwrites, as BTreeMap::insert does
+    }
+    double a_ii = 0.0;  // row_get: the first stored (i, i)
+    for (int64_t e = a.ptr[i]; e < a.ptr[i + 1]; ++e)
+      if (a.cols[e] == i) {
+        a_ii = a.vals[e];
+        break;
+      }
+    if (std::fabs(a_ii) < 1e-300) return false;
+    double sum = a_ii;
+    for (auto& kv : rows[i]) sum -= kv.second * kv.second;
+    const double floor_ = 1e-12 * std::max(std::fabs(a_ii), 1e-30);
+    if (sum < floor_) sum = floor_;
+    diag[i] = std::sqrt(sum);
+    for (auto& kv : rows[i]) {
+      L.cols.push_back(kv.first);
+      L.vals.push_back(kv.second);
+    }
+    L.cols.push_back(i);
+    L.vals.push_back(diag[i]);
+    L.ptr.push_back((int64_t)L.cols.size());
+  }
+  return true;
+}
+
+// transpose_lower (precond.rs:238-262): rows of the transpose, ascending, diagonal last.
+Csr transpose_lower(const Csr& L) {
+  const int64_t n = L.n;
+  std::vector<std::vector<std::pair<int64_t, double>>> t(n);
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t e = L.ptr[i]; e < L.ptr[i + 1]; ++e) {
+      const int64_t j = L.cols[e];
+      t[j == i ? i : j].push_back({i, L.vals[e]});
+    }
+  Csr T;
+  T.n = n;
+  T.ptr.assign(1, 0);
+  for (int64_t i = 0; i < n; ++i) {
+    auto row = t[i];
+    std::stable_sort(row.begin(), row.end(), [](const std::pair<int64_t, double>& x, const std::pair<int64_t, double>& y) {
+      return x.first < y.first;
+    });
+    size_t d = 0;  // the first entry on the diagonal moves to the end
+    while (d < row.size() && row[d].first != i) ++d;
+    const std::pair<int64_t, double> dg = row[d];
+    row.erase(row.begin() + (std::ptrdiff_t)d);
+    for (auto& kv : row) {
+      T.cols.push_back(kv.first);
+      T.vals.push_back(kv.second);
+    }
+    T.cols.push_back(dg.first);
+    T.vals.push_back(dg.second);
+    T.ptr.push_back((int64_t)T.cols.size());
+  }
+  return T;
+}
+
+// tri_levels (precond.rs:214-236): level of each row of a diagonal-last factor.
+std::vector<int64_t> tri_levels(const Csr& F, bool descending) {
+  const int64_t n = F.n;
+  std::vector<int64_t> level(n, 0);
+  for (int64_t t = 0; t < n; ++t) {
+    const int64_t i = descending ? n - 1 - t : t;
+    int64_t lv = 0;
+    for (int64_t e = F.ptr[i]; e < F.ptr[i + 1] - 1; ++e) lv = std::max(lv, level[F.cols[e]] + 1);
+    level[i] = lv;
+  }
+  return level;
+}
+
+// graph_coloring (precond.rs:49-75): greedy, vertices in index order, smallest free colour.
+std::vector<int64_t> graph_coloring(const Csr& a) {
+  const int64_t n = a.n;
+  std::vector<int64_t> color(n, -1);
+  std::vector<int64_t> used;
+  for (int64_t v = 0; v < n; ++v) {
+    used.clear();
+    for (int64_t e = a.ptr[v]; e < a.ptr[v + 1]; ++e) {
+      const int64_t c = a.cols[e];
+      if (c != v && color[c] >= 0) used.push_back(color[c]);
+    }
+    std::sort(used.begin(), used.end());
+    used.erase(std::unique(used.begin(), used.end()), used.end());
+    int64_t k = 0;
+    for (int64_t c : used) {
+      if (c == k) ++k;
+      else break;
+    }
+    color[v] = k;
+  }
+  return color;
+}
+
+// color_permutation + permute_csr (precond.rs:77-123).
+void color_permute(const Csr& a, const std::vector<int64_t>& color, std::vector<int64_t>& to_perm,
+                   std::vector<int64_t>& to_orig, Csr& P) {
+  const int64_t n = a.n;
+  int64_t nc = 0;
+  for (int64_t c : color) nc = std::max(nc, c + 1);
+  std::vector<int64_t> cnt(nc + 1, 0);
+  for (int64_t c : color) cnt[c + 1] += 1;
+  for (int64_t k = 1; k <= nc; ++k) cnt[k] += cnt[k - 1];
+  to_perm.assign(n, 0);
+  to_orig.assign(n, 0);
+  for (int64_t v = 0; v < n; ++v) {
+    const int64_t pos = cnt[color[v]]++;
+    to_perm[v] = pos;
+    to_orig[pos] = v;
+  }
+  P.n = n;
+  P.ptr.assign(1, 0);
+  P.cols.clear();
+  P.vals.clear();
+  for (int64_t pos = 0; pos < n; ++pos) {
+    const int64_t o = to_orig[pos];
+    std::vector<std::pair<int64_t, double>> row;
+    for (int64_t e = a.ptr[o]; e < a.ptr[o + 1]; ++e) row.push_back({to_perm[a.cols[e]], a.vals[e]});
+    std::stable_sort(row.begin(), row.end(), [](const std::pair<int64_t, double>& x, const std::pair<int64_t, double>& y) {
+      return x.first < y.first;
+    });
+    for (auto& kv : row) {
+      P.cols.push_back(kv.first);
+      P.vals.push_back(kv.second);
+    }
+    P.ptr.push_back((int64_t)P.cols.size());
+  }
+}
+
+Csr bag_csr(Bag* b, const std::string& pre) {
+  Csr a;
+  a.ptr = b->i[pre + ".row_ptr"];
+  a.cols = b->i[pre + ".cols"];
+  a.vals = b->f[pre + ".vals"];
+  a.n = (int64_t)a.ptr.size() - 1;
+  return a;
+}
+void put_csr(Bag* b, const std::string& pre, const Csr& a) {
+  b->i[pre + ".ptr"] = a.ptr;
+  b->i[pre + ".cols"] = a.cols;
+  b->f[pre + ".vals"] = a.vals;
+}
 }  // namespace
 
 // ================================================================= extern "C" interface
@@ -1315,4 +1493,61 @@ int orc_chart_metrics(void* h, int64_t chart, const double* uv, double* out5) {
   return 0;
 }
 
+
+// IC(0) of bag {"a.row_ptr", "a.cols", "a.vals"} -> {"l.*", "lt.*" (ptr, cols, vals),
+// "fwd.level", "bwd.level"}; with `colored`, of the colour-permuted matrix, adding
+// {"color", "to_perm", "to_orig", "p.ptr", "p.cols", "p.vals"}.  0, or -1 where the
+// reference's factor_ic0 returns None.
+int orc_ic0(void* h, int colored) {
+  Bag* b = static_cast<Bag*>(h);
+  Csr a = bag_csr(b, "a");
+  if (colored) {
+    std::vector<int64_t> color = graph_coloring(a), tp, to;
+    Csr P;
+    color_permute(a, color, tp, to, P);
+    b->i["color"] = color;
+    b->i["to_perm"] = tp;
+    b->i["to_orig"] = to;
+    put_csr(b, "p", P);
+    a = P;
+  }
+  Csr L;
+  if (!ic0_factor(a, L)) return -1;
+  Csr T = transpose_lower(L);
+  put_csr(b, "l", L);
+  put_csr(b, "lt", T);
+  b->i["fwd.level"] = tri_levels(L, false);
+  b->i["bwd.level"] = tri_levels(T, true);
+  return 0;
+}
+
+// z = (L L^T)^-1 r with the factor in the bag (the reference test's host sweeps,
+// precond.rs:932-950: forward over L, backward over L^T, diagonal read from each row).
+void orc_ic0_apply(void* h, const double* r, double* z) {
+  Bag* b = static_cast<Bag*>(h);
+  const auto& lp = b->i["l.ptr"];
+  const auto& lc = b->i["l.cols"];
+  const auto& lv = b->f["l.vals"];
+  const auto& tp = b->i["lt.ptr"];
+  const auto& tc = b->i["lt.cols"];
+  const auto& tv = b->f["lt.vals"];
+  const int64_t n = (int64_t)lp.size() - 1;
+  auto get = [](const std::vector<int64_t>& p, const std::vector<int64_t>& c, const std::vector<double>& v, int64_t i,
+                int64_t j) {
+    for (int64_t k = p[i]; k < p[i + 1]; ++k)
+      if (c[k] == j) return v[k];
+    return 0.0;
+  };
+  std::vector<double> y(n, 0.0);
+  for (int64_t i = 0; i < n; ++i) {
+    double s_ = r[i];
+    for (int64_t k = lp[i]; k < lp[i + 1] - 1; ++k) s_ -= lv[k] * y[lc[k]];
+    y[i] = s_ / get(lp, lc, lv, i, i);
+  }
+  for (int64_t i = n - 1; i >= 0; --i) {
+    double s_ = y[i];
+    for (int64_t k = tp[i]; k < tp[i + 1] - 1; ++k) s_ -= tv[k] * z[tc[k]];
+    z[i] = s_ / get(tp, tc, tv, i, i);
+  }
+}
 }  // extern "C"

@@ -59,6 +59,9 @@ def lib():
         L.orc_pipeline.argtypes = [vp, f64, f64, f64, f64, i64, i64]
         L.orc_driver_from_solution.argtypes = [vp, i64, i64]
         L.orc_chart_metrics.argtypes = [vp, i64, P(f64), P(f64)]
+        L.orc_ic0.argtypes = [vp, ctypes.c_int]
+        L.orc_ic0.restype = ctypes.c_int
+        L.orc_ic0_apply.argtypes = [vp, P(f64), P(f64)]
         _lib = L
     return _lib
 
@@ -257,3 +260,37 @@ def uv_error(uv_test, uv_ref) -> float:
     diff = np.sqrt(((a - b) ** 2).sum(1)).max(initial=0.0)
     scale = max(np.sqrt((b ** 2).sum(1)).max(initial=0.0), 1e-30)
     return float(diff / scale)
+
+
+class Ic0:
+    """IC(0) factor of a CSR matrix as the reference builds it (gpu/src/precond.rs:145-262):
+    ``l_*`` (lower, diagonal last), ``lt_*`` (transpose, diagonal last), ``fwd_level`` /
+    ``bwd_level`` per row; with ``colored``, of the colour-permuted matrix
+    (precond.rs:49-123), with ``color``, ``to_perm``, ``to_orig`` and the permuted CSR ``p_*``.
+    ``ok`` is False where the reference's factor_ic0 returns None."""
+
+    def __init__(self, row_ptr, cols, vals, colored: bool = False):
+        self.bag = Bag()
+        self.bag.put_i64("a.row_ptr", np.asarray(row_ptr, dtype=np.int64))
+        self.bag.put_i64("a.cols", np.asarray(cols, dtype=np.int64))
+        self.bag.put_f64("a.vals", np.asarray(vals, dtype=np.float64))
+        self.ok = lib().orc_ic0(self.bag.h, 1 if colored else 0) == 0
+        if not self.ok:
+            return
+        for pre in ("l", "lt") + (("p",) if colored else ()):
+            setattr(self, pre + "_ptr", self.bag.i64(pre + ".ptr"))
+            setattr(self, pre + "_cols", self.bag.i64(pre + ".cols"))
+            setattr(self, pre + "_vals", self.bag.f64(pre + ".vals"))
+        self.fwd_level = self.bag.i64("fwd.level")
+        self.bwd_level = self.bag.i64("bwd.level")
+        if colored:
+            self.color = self.bag.i64("color")
+            self.to_perm = self.bag.i64("to_perm")
+            self.to_orig = self.bag.i64("to_orig")
+
+    def apply(self, r):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.zeros_like(r)
+        lib().orc_ic0_apply(self.bag.h, _f64p(r), _f64p(z))
+        return z
+

@@ -60,6 +60,8 @@ SIGNATURES = {
     "ruv_cg_solve": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _P(_f64), _P(_f64), _i64, _f64,
                                     ctypes.c_int, _P(_i64)]),
     "ruv_apply_ic0": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _P(_f64), _P(_f64)]),
+    "ruv_ic0_export": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _i32, _i64, _P(_i64), _P(_i32),
+                                      _P(_f64), _P(_i32), _P(_i64), _P(_i32), _P(_i32)]),
     "ruv_unfold_opts_default": (None, [_P(RuvUnfoldOpts)]),
     "ruv_lscm_solve_batch": (ctypes.c_int, [_vp, _P(RuvBatch), _P(RuvUnfoldOpts), _P(_f64), _P(RuvChartStat)]),
     "ruv_prepare_mesh": (ctypes.c_int, [_P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _i32, _P(_vp)]),
@@ -256,6 +258,24 @@ class GpuSolver:
             self.last_error = f"{Status(st).name}: {self.ctx.last_error()}"
             return None
         return z
+
+    def ic0_factor(self, a: CsrMatrix, colored: bool = False) -> dict:
+        """The device IC(0) factor of ``a`` (natural or colour-permuted order): rows of L with
+        the diagonal last, the position -> original row map, the level and colour counts."""
+        n = a.rows()
+        cap = int(len(a.vals))  # the factor keeps the lower pattern: at most nnz(A) entries
+        ptr = np.zeros(n + 1, np.int64)
+        cols = np.zeros(max(cap, 1), np.int32)
+        vals = np.zeros(max(cap, 1), np.float64)
+        perm = np.zeros(n, np.int32)
+        nnz, lev, col = _i64(0), _i32(0), _i32(0)
+        st = lib().ruv_ic0_export(self.ctx.h, n, _ptr(a.row_ptr, _i32), _ptr(a.cols, _i32), _ptr(a.vals, _f64),
+                                  1 if colored else 0, cap, _ptr(ptr, _i64), _ptr(cols, _i32), _ptr(vals, _f64),
+                                  _ptr(perm, _i32), ctypes.byref(nnz), ctypes.byref(lev), ctypes.byref(col))
+        self.ctx.check(st, "ruv_ic0_export")
+        k = nnz.value
+        return {"ptr": ptr, "cols": cols[:k], "vals": vals[:k], "to_orig": perm, "levels": lev.value,
+                "colours": col.value}
 
 
 # ------------------------------------------------------------------ unfold driver

@@ -1102,7 +1102,6 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     float ms = 0.f;
     cudaEventElapsedTime(&ms, t_setup0, t1);
     cudaEventDestroy(t1);
-    ctx.timings[3] = ms;
     if (debug) std::fprintf(stderr, "amg setup %.2f ms, %s, operator complexity %.2f\n", ms, info.c_str(),
                             sys.nnz > 0 ? (double)H->total_nnz / (double)sys.nnz : 0.0);
   }
@@ -1201,6 +1200,30 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
 // One V(1,1) cycle: z0 = M^-1 r0 for every chart not marked done (launches only; capturable).
 int amg_apply(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
   return H->nrhs == 2 ? apply_impl<2>(ctx, H, done) : apply_impl<1>(ctx, H, done);
+}
+
+namespace {
+// The V-cycle runs in FP32 under either CG loop; it varies slightly between applications
+// (FP32 rounding, the coarse over-correction), so the CG uses the flexible beta.
+class AmgPrecond final : public SepPrecond {
+ public:
+  AmgPrecond(Ctx& ctx, const DevSystem& sys, bool smooth) {
+    std::string info;
+    H_ = amg_setup(ctx, sys, smooth, info);
+  }
+  ~AmgPrecond() override { amg_free(H_); }
+  bool native_fp64() const override { return false; }
+  bool flexible() const override { return true; }
+  void bind(Ctx& ctx, void* r, void* z, bool) override { amg_bind(ctx, H_, static_cast<float*>(r), static_cast<float*>(z)); }
+  int apply(Ctx& ctx, const int32_t* done) override { return amg_apply(ctx, H_, done); }
+
+ private:
+  AmgHierarchy* H_ = nullptr;
+};
+}  // namespace
+
+std::unique_ptr<SepPrecond> make_amg(Ctx& ctx, const DevSystem& sys, bool smooth) {
+  return std::unique_ptr<SepPrecond>(new AmgPrecond(ctx, sys, smooth));
 }
 
 }  // namespace ruv

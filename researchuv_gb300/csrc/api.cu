@@ -135,48 +135,61 @@ void ruv_unfold_opts_default(ruv_unfold_opts* o) {
   o->max_cg_iter = 1024 * 16;
 }
 
+// A host CSR system checked and uploaded as a one-chart DevSystem (nrhs = 1).  Returns a
+// non-OK status (with the context's message set) for a malformed system (solver.rs:296-299).
+static ruv_status host_system(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                              const double* b, DevSystem& sys, std::vector<double>& diag) {
+  if (n <= 0 || !row_ptr || !cols || !vals || !b) return fail(ctx, RUV_ERR_BAD_INPUT, "empty system or null buffer");
+  if (row_ptr[0] != 0) return fail(ctx, RUV_ERR_BAD_INPUT, "row_ptr[0] != 0");
+  for (int32_t i = 0; i < n; ++i)
+    if (row_ptr[i + 1] < row_ptr[i]) return fail(ctx, RUV_ERR_BAD_INPUT, "row_ptr not monotone");
+  const int64_t nnz = row_ptr[n];
+  diag.assign(n, 0.0);
+  for (int32_t i = 0; i < n; ++i) {
+    bool found = false;
+    for (int32_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+      if (cols[k] < 0 || cols[k] >= n) return fail(ctx, RUV_ERR_BAD_INPUT, "column index out of range");
+      if (cols[k] == i && !found) {  // CsrMatrix::row_get returns the first match
+        diag[i] = vals[k];
+        found = true;
+      }
+    }
+  }
+  Ctx& c = ctx->c;
+  sys = DevSystem();
+  sys.n_charts = 1;
+  sys.n_rows = n;
+  sys.nnz = nnz;
+  sys.nrhs = 1;
+  sys.h_chart_row = {0, (int64_t)n};
+  sys.chart_row = upload(c, "cg.chart_row", sys.h_chart_row.data(), 2);
+  sys.row_ptr = upload(c, "cg.row_ptr", row_ptr, (int64_t)n + 1);
+  sys.cols = upload(c, "cg.cols", cols, nnz);
+  sys.vals = upload(c, "cg.vals", vals, nnz);
+  std::vector<float> v32(vals, vals + nnz);
+  sys.vals32 = upload(c, "cg.vals32", v32.data(), nnz);
+  sys.diag = upload(c, "cg.diag", diag.data(), n);
+  sys.b = upload(c, "cg.b", b, n);
+  return RUV_OK;
+}
+
+static bool known_precond(int pc) { return pc >= RUV_PRECOND_NONE && pc <= RUV_PRECOND_AMG_SA; }
+
 ruv_status ruv_cg_solve(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols, const double* vals,
                         const double* b, double* x_out, int64_t max_iter, double tol, ruv_precond pc,
                         int64_t* iters_out) {
   if (!ctx) return RUV_ERR_BAD_INPUT;
   return guarded(ctx, [&]() -> ruv_status {
-    // solver.rs:296-299: a malformed system is rejected
-    if (n <= 0 || !row_ptr || !cols || !vals || !b || !x_out) return fail(ctx, RUV_ERR_BAD_INPUT, "empty system or null buffer");
-    if (row_ptr[0] != 0) return fail(ctx, RUV_ERR_BAD_INPUT, "row_ptr[0] != 0");
-    for (int32_t i = 0; i < n; ++i)
-      if (row_ptr[i + 1] < row_ptr[i]) return fail(ctx, RUV_ERR_BAD_INPUT, "row_ptr not monotone");
-    const int64_t nnz = row_ptr[n];
-    std::vector<double> diag(n, 0.0);
-    for (int32_t i = 0; i < n; ++i) {
-      bool found = false;
-      for (int32_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
-        if (cols[k] < 0 || cols[k] >= n) return fail(ctx, RUV_ERR_BAD_INPUT, "column index out of range");
-        if (cols[k] == i && !found) {  // CsrMatrix::row_get returns the first match
-          diag[i] = vals[k];
-          found = true;
-        }
-      }
-    }
+    if (!x_out) return fail(ctx, RUV_ERR_BAD_INPUT, "null output buffer");
+    if (!known_precond(pc)) return fail(ctx, RUV_ERR_BAD_INPUT, "unknown preconditioner");
+    Ctx& c = ctx->c;
+    DevSystem sys;
+    std::vector<double> diag;
+    const ruv_status hs = host_system(ctx, n, row_ptr, cols, vals, b, sys, diag);
+    if (hs != RUV_OK) return hs;
     if (pc == RUV_PRECOND_JACOBI)
       for (int32_t i = 0; i < n; ++i)
         if (std::fabs(diag[i]) < 1e-300) return fail(ctx, RUV_ERR_BAD_INPUT, "Jacobi: zero diagonal");
-    if (pc != RUV_PRECOND_NONE && pc != RUV_PRECOND_JACOBI && pc != RUV_PRECOND_AMG && pc != RUV_PRECOND_AMG_SA)
-      return fail(ctx, RUV_ERR_BAD_INPUT, "preconditioner not available in this build");
-    Ctx& c = ctx->c;
-    DevSystem sys;
-    sys.n_charts = 1;
-    sys.n_rows = n;
-    sys.nnz = nnz;
-    sys.nrhs = 1;
-    sys.h_chart_row = {0, (int64_t)n};
-    sys.chart_row = upload(c, "cg.chart_row", sys.h_chart_row.data(), 2);
-    sys.row_ptr = upload(c, "cg.row_ptr", row_ptr, (int64_t)n + 1);
-    sys.cols = upload(c, "cg.cols", cols, nnz);
-    sys.vals = upload(c, "cg.vals", vals, nnz);
-    std::vector<float> v32(vals, vals + nnz);
-    sys.vals32 = upload(c, "cg.vals32", v32.data(), nnz);
-    sys.diag = upload(c, "cg.diag", diag.data(), n);
-    sys.b = upload(c, "cg.b", b, n);
     double* x = c.ws.get<double>("cg.x", n);
     SolveOpts o;
     o.precond = pc;
@@ -196,13 +209,49 @@ ruv_status ruv_cg_solve(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const i
 
 ruv_status ruv_apply_ic0(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols, const double* vals,
                          const double* r, double* z_out) {
-  (void)n;
-  (void)row_ptr;
-  (void)cols;
-  (void)vals;
-  (void)r;
-  (void)z_out;
-  return fail(ctx, RUV_ERR_BAD_INPUT, "IC(0) is not available in this build");
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    if (!z_out) return fail(ctx, RUV_ERR_BAD_INPUT, "null output buffer");
+    Ctx& c = ctx->c;
+    DevSystem sys;
+    std::vector<double> diag;
+    const ruv_status hs = host_system(ctx, n, row_ptr, cols, vals, r, sys, diag);  // b carries r
+    if (hs != RUV_OK) return hs;
+    double* z = c.ws.get<double>("ic0.z", n);
+    ic0_apply_once(c, sys, sys.b, z, nullptr);
+    RUV_CUDA(cudaMemcpyAsync(z_out, z, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+    RUV_CUDA(cudaStreamSynchronize(c.stream));
+    return RUV_OK;
+  });
+}
+
+ruv_status ruv_ic0_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                          int32_t colored, int64_t cap, int64_t* l_ptr, int32_t* l_cols, double* l_vals,
+                          int32_t* to_orig, int64_t* nnz_out, int32_t* levels_out, int32_t* colours_out) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    if (!l_ptr || !to_orig || !nnz_out || !levels_out || !colours_out || (cap > 0 && (!l_cols || !l_vals)))
+      return fail(ctx, RUV_ERR_BAD_INPUT, "null output buffer");
+    Ctx& c = ctx->c;
+    DevSystem sys;
+    std::vector<double> diag, zero(n > 0 ? n : 0, 0.0);
+    const ruv_status hs = host_system(ctx, n, row_ptr, cols, vals, zero.data(), sys, diag);
+    if (hs != RUV_OK) return hs;
+    std::vector<int64_t> p;
+    std::vector<int32_t> lc, perm;
+    std::vector<double> lv;
+    int levels = 0, colours = 0;
+    ic0_export(c, sys, colored != 0, p, lc, lv, perm, levels, colours);
+    *nnz_out = (int64_t)lc.size();
+    *levels_out = levels;
+    *colours_out = colours;
+    std::copy(p.begin(), p.end(), l_ptr);
+    std::copy(perm.begin(), perm.end(), to_orig);
+    if ((int64_t)lc.size() > cap) return fail(ctx, RUV_ERR_BAD_INPUT, "factor larger than the output capacity");
+    std::copy(lc.begin(), lc.end(), l_cols);
+    std::copy(lv.begin(), lv.end(), l_vals);
+    return RUV_OK;
+  });
 }
 
 ruv_status ruv_lscm_upload(ruv_ctx* ctx, const ruv_lscm_batch* in) {
@@ -247,9 +296,7 @@ ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ru
     ruv_unfold_opts_default(&o);
     if (opts) o = *opts;
     if (!(o.mix_w > 0.0)) return fail(ctx, RUV_ERR_BAD_INPUT, "mix_w must be > 0 (lscm.rs:479)");
-    if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI && o.precond != RUV_PRECOND_AMG &&
-        o.precond != RUV_PRECOND_AMG_SA)
-      return fail(ctx, RUV_ERR_BAD_INPUT, "preconditioner not available in this build");
+    if (!known_precond(o.precond)) return fail(ctx, RUV_ERR_BAD_INPUT, "unknown preconditioner");
     DevBatch& bt = c.resident;
     const int64_t NC = bt.n_charts, NV = bt.n_verts;
     if (NC == 0) {
@@ -291,7 +338,7 @@ ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ru
       RUV_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
       c.timings[k] = ms;
     }
-    if (o.precond != RUV_PRECOND_AMG && o.precond != RUV_PRECOND_AMG_SA) c.timings[3] = 0.0;
+
     c.have_uv = true;
     int w = RUV_OK;
     for (int64_t k = 0; k < NC; ++k) {

@@ -74,11 +74,16 @@ __global__ void k_corner_cot(const double* __restrict__ p3, const int32_t* __res
   if (t >= n_tris) return;
   int32_t v[3] = {tri_g[3 * t], tri_g[3 * t + 1], tri_g[3 * t + 2]};
   P3 p[3] = {ld3(p3, v[0]), ld3(p3, v[1]), ld3(p3, v[2])};
+  // |p[k+1] - p[k]|, each edge once: a - b is exactly -(b - a) in IEEE arithmetic and the
+  // squares are equal, so both corners at an edge see the same length bit for bit
+  double len[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) len[k] = plen(psub(p[(k + 1) % 3], p[k]));
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
     P3 a1 = psub(p[(m + 2) % 3], p[m]);  // e1 - o
     P3 a2 = psub(p[(m + 1) % 3], p[m]);  // e0 - o
-    double la = plen(a1), lb = plen(a2);
+    double la = len[(m + 2) % 3], lb = len[m];
     double c = 0.0;
     if (!(la <= kEpsDegenerate || lb <= kEpsDegenerate)) {
       double lab = dmul(la, lb);
@@ -130,14 +135,17 @@ __global__ void k_scatter_records(const int32_t* __restrict__ tri_g, const uint8
 
 __device__ __forceinline__ bool rec_less(int2 a, int2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
 
-// One row (free vertex v).  MODE 0: sort the bucket and count entries; MODE 1: fill.
+// One row (free vertex v).  MODE 0: sort the bucket, form each kept edge's coefficient
+// c = w / max(|p_nb - p_v|^2, EPS) once (stored at the neighbour's first record; -1 marks a
+// dropped edge) and count entries; MODE 1: fill from the stored coefficients.
 template <int MODE>
 __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, const int64_t* __restrict__ row_of,
                        const int64_t* __restrict__ rec_off, int2* __restrict__ rec, const double* __restrict__ cot,
                        const double* __restrict__ p3, const double* __restrict__ p2, const double* __restrict__ pin_uv,
                        double mix_b, int32_t* __restrict__ row_len, const int64_t* __restrict__ row_ptr,
                        int32_t* __restrict__ cols, double* __restrict__ vals, float* __restrict__ vals32,
-                       double* __restrict__ diag_out, double* __restrict__ b, int32_t* __restrict__ row_vert) {
+                       double* __restrict__ diag_out, double* __restrict__ b, int32_t* __restrict__ row_vert,
+                       double* __restrict__ coef) {
   int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n_verts || pinned[v]) return;
   const int64_t r0 = rec_off[v], r1 = rec_off[v + 1];
@@ -154,19 +162,34 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
   }
   const P3 pv = ld3(p3, v);
   const int64_t row = row_of[v];
+  // the coefficient of the neighbour group starting at record i (its end returned in j)
+  auto group = [&](int64_t i, int64_t& j) -> double {
+    const int32_t nb = rec[i].x;
+    j = i;
+    if (MODE == 1) {
+      while (j < r1 && rec[j].x == nb) ++j;
+      return coef[i];
+    }
+    double w = 0.0;
+    for (; j < r1 && rec[j].x == nb; ++j) w = dadd(w, cot[rec[j].y]);
+    double c = -1.0;
+    if (!(w <= kEpsDegenerate)) {  // lscm.rs:606
+      P3 d3 = psub(ld3(p3, nb), pv);
+      c = ddiv(w, rs_max(pdot(d3, d3), kEpsDegenerate));
+    }
+    coef[i] = c;
+    return c;
+  };
   // pass A: diagonal (sum of c over kept edges, ascending neighbour) and entry count
   double dg = 0.0;
   bool has_diag = false;
   int32_t n_off = 0;
   for (int64_t i = r0; i < r1;) {
     int32_t nb = rec[i].x;
-    double w = 0.0;
-    int64_t j = i;
-    for (; j < r1 && rec[j].x == nb; ++j) w = dadd(w, cot[rec[j].y]);
+    int64_t j;
+    const double c = group(i, j);
     i = j;
-    if (w <= kEpsDegenerate) continue;  // lscm.rs:606
-    P3 d3 = psub(ld3(p3, nb), pv);
-    double c = ddiv(w, rs_max(pdot(d3, d3), kEpsDegenerate));
+    if (c < 0.0) continue;  // dropped: w <= EPS
     if (c != 0.0) {  // Sparse::add skips zeros (sparse.rs:47-52)
       dg = dadd(dg, c);
       has_diag = true;
@@ -185,13 +208,10 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
   const double p2u = p2[2 * v], p2v = p2[2 * v + 1];
   for (int64_t i = r0; i < r1;) {
     int32_t nb = rec[i].x;
-    double w = 0.0;
-    int64_t j = i;
-    for (; j < r1 && rec[j].x == nb; ++j) w = dadd(w, cot[rec[j].y]);
+    int64_t j;
+    const double c = group(i, j);
     i = j;
-    if (w <= kEpsDegenerate) continue;
-    P3 d3 = psub(ld3(p3, nb), pv);
-    double c = ddiv(w, rs_max(pdot(d3, d3), kEpsDegenerate));
+    if (c < 0.0) continue;
     // dv as the reference forms it: d = p2[hi] - p2[lo], negated for the higher endpoint
     double du, dw;
     if (v < nb) {
@@ -403,6 +423,7 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   int32_t* cursor = ws.get<int32_t>("asm.cursor", NV);
   RUV_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (NV > 0 ? NV : 1), s));
   int2* rec = ws.get<int2>("asm.rec", NREC);
+  double* coef = ws.get<double>("asm.coef", NREC);
   if (NT > 0) {
     k_scatter_records<<<div_up(NT, B), B, 0, s>>>(tri_g, bt.pinned, NT, rec_off, cursor, rec);
     count_launches(1);
@@ -412,7 +433,7 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   int32_t* row_len = ws.get<int32_t>("asm.row_len", NR);
   if (NV > 0) {
     k_rows<0><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, bt.p3, bt.p2, bt.pin_uv, mix_b,
-                                             row_len, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+                                             row_len, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, coef);
     count_launches(1);
   }
   RUV_LAUNCH_CHECK();
@@ -439,7 +460,7 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   if (NV > 0) {
     k_rows<1><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, bt.p3, bt.p2, bt.pin_uv, mix_b,
                                              nullptr, rp64, sys.cols, sys.vals, sys.vals32, sys.diag, sys.b,
-                                             bt.row_vert);
+                                             bt.row_vert, coef);
     count_launches(1);
   }
   RUV_LAUNCH_CHECK();

@@ -907,11 +907,12 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
   RUV_CUDA(cudaStreamSynchronize(s));
 }
 
-// Batched PCG with the AMG V-cycle as a separate apply step: FP32 inner loop with FP64
-// true-residual refreshes (the mixed scheme), for any requested precision.
+// Batched PCG with a separately applied preconditioner (AMG V-cycle, IC(0) sweeps): the
+// mixed loop (FP32 recurrences, double-float true-residual refreshes) or the FP64 loop.
+// A preconditioner that has no FP64 form gets FP32 copies of r and z under the FP64 loop.
 template <class S, int NR, int LPR, int U>
-void run_pcg_amg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st, int* n_active,
-                 std::vector<ChartState>& out, bool smooth) {
+void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st, int* n_active,
+                 std::vector<ChartState>& out, SepPrecond& P) {
   constexpr bool mixed = std::is_same<S, float>::value;
   cudaStream_t s = ctx.stream;
   Workspace& ws = ctx.ws;
@@ -923,30 +924,26 @@ void run_pcg_amg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
   S* q = ws.get<S>("pcg.q", NR * NR_);
   S* dinv = ws.get<S>("pcg.dinv", NR_);
   float* dinv32 = mixed ? reinterpret_cast<float*>(dinv) : nullptr;
-  // the V-cycle works in FP32: the FP64 loop hands it FP32 copies of r and takes z back
-  float* r32 = mixed ? reinterpret_cast<float*>(r) : ws.get<float>("pcg.r32", NR * NR_);
-  float* z32 = mixed ? reinterpret_cast<float*>(z) : ws.get<float>("pcg.z32", NR * NR_);
+  const bool copies = !mixed && !P.native_fp64();
+  float* r32 = copies ? ws.get<float>("pcg.r32", NR * NR_) : reinterpret_cast<float*>(r);
+  float* z32 = copies ? ws.get<float>("pcg.z32", NR * NR_) : reinterpret_cast<float*>(z);
   const S* vals = mixed ? reinterpret_cast<const S*>(sys.vals32) : reinterpret_cast<const S*>(sys.vals);
   S* xiter = mixed ? xs : reinterpret_cast<S*>(x64);
   double* part = ws.get<double>("pcg.part", 3 * NTL);
   double* part2 = ws.get<double>("pcg.part2", 2 * NTL);
   MixedExtras mx = mixed_extras(ctx, sys, mixed ? NR : 0);
   int32_t* done = ws.get<int32_t>("pcg.done", NC);
-  std::string info;
-  AmgHierarchy* H = amg_setup(ctx, sys, smooth, info);
-  struct Free {
-    AmgHierarchy* h;
-    ~Free() { amg_free(h); }
-  } free_h{H};
-  amg_bind(ctx, H, r32, z32);
+  if (copies) P.bind(ctx, r32, z32, false);
+  else P.bind(ctx, r, z, !mixed);
+  const int flex = P.flexible() ? 1 : 0;
   const unsigned gv = div_up(NR * NR_, 256);
   auto to32 = [&]() {
-    if (!mixed) k_convert<S, float><<<gv, 256, 0, s>>>(NR * NR_, r, r32);
+    if (copies) k_convert<S, float><<<gv, 256, 0, s>>>(NR * NR_, r, r32);
   };
   auto to64 = [&]() {
-    if (!mixed) k_convert<float, S><<<gv, 256, 0, s>>>(NR * NR_, z32, z);
+    if (copies) k_convert<float, S><<<gv, 256, 0, s>>>(NR * NR_, z32, z);
   };
-  const int conv = mixed ? 0 : 2;
+  const int conv = copies ? 2 : 0;
   RUV_CUDA(cudaMemsetAsync(n_active, 0, sizeof(int), s));
   if (NR_ > 0) {
     k_dinv<S><<<div_up(NR_, kTileThreads), kTileThreads, 0, s>>>(NR_, sys.diag, dinv);
@@ -967,7 +964,7 @@ void run_pcg_amg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
     // z0 = M^-1 r0, rz = r.z, p = z
     k_mark_done<<<div_up(NC, 256), 256, 0, s>>>(st, NC, done);
     to32();
-    count_launches(1 + conv + amg_apply(ctx, H, done));
+    count_launches(1 + conv + P.apply(ctx, done));
     to64();
     k_dots_rz<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, r, z, q, part2);
     k_chart_rz0<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part2);
@@ -999,10 +996,10 @@ void run_pcg_amg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
       k_mark_done<<<div_up(NC, 256), 256, 0, s>>>(st, NC, done);
       to32();
       l += 4 + conv;
-      l += amg_apply(ctx, H, done);
+      l += P.apply(ctx, done);
       to64();
       k_dots_rz<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, r, z, q, part2);
-      k_chart_beta_pc<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part2, 1);
+      k_chart_beta_pc<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part2, flex);
       k_direction<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
       l += 3;
       per_iter = l;
@@ -1125,10 +1122,10 @@ double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
 }
 
 template <class S, int NR>
-void dispatch_pcg_amg(Shape sh, Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st,
-                      int* n_active, std::vector<ChartState>& out, bool smooth) {
+void dispatch_pcg_sep(Shape sh, Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st,
+                      int* n_active, std::vector<ChartState>& out, SepPrecond& P) {
 #define RUV_CASE(L, UU) \
-  if (sh.lpr == L && sh.unroll == UU) return run_pcg_amg<S, NR, L, UU>(ctx, sys, x64, o, T, st, n_active, out, smooth);
+  if (sh.lpr == L && sh.unroll == UU) return run_pcg_sep<S, NR, L, UU>(ctx, sys, x64, o, T, st, n_active, out, P);
   RUV_SHAPES(RUV_CASE)
 #undef RUV_CASE
   throw Error{RUV_ERR_BAD_INPUT, "unsupported SpMV shape"};
@@ -1207,9 +1204,10 @@ TuneResult autotune_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps) {
 }
 
 std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o) {
-  const bool amg = o.precond == RUV_PRECOND_AMG || o.precond == RUV_PRECOND_AMG_SA;
-  if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI && !amg)
-    throw Error{RUV_ERR_BAD_INPUT, "preconditioner not available in this build"};
+  const bool sep = o.precond == RUV_PRECOND_AMG || o.precond == RUV_PRECOND_AMG_SA || o.precond == RUV_PRECOND_IC0 ||
+                   o.precond == RUV_PRECOND_IC0_COLOR;
+  if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI && !sep)
+    throw Error{RUV_ERR_BAD_INPUT, "unknown preconditioner"};
   const int64_t NC = sys.n_charts;
   Tiles T = upload_tiles(ctx, sys, "pcg");
   ChartState* st = ctx.ws.get<ChartState>("pcg.state", NC);
@@ -1217,16 +1215,34 @@ std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const So
   const Shape sh = pick_shape(ctx, sys);
   std::vector<ChartState> out;
   const bool mixed = o.precision == RUV_PREC_MIXED;
-  if (amg) {
-    // the V-cycle runs in FP32 under either loop: the mixed loop (FP32 recurrences, FP64
-    // true-residual refreshes) or the FP64 loop (FP64 recurrences, FP32 copies in and out)
-    const bool smooth = o.precond == RUV_PRECOND_AMG_SA;
+  ctx.timings[3] = 0.0;
+  if (sep) {
+    // preconditioner set-up, timed on the stream
+    cudaEvent_t e[2];
+    RUV_CUDA(cudaEventCreate(&e[0]));
+    RUV_CUDA(cudaEventCreate(&e[1]));
+    struct EvGuard {
+      cudaEvent_t* e;
+      ~EvGuard() {
+        cudaEventDestroy(e[0]);
+        cudaEventDestroy(e[1]);
+      }
+    } guard{e};
+    RUV_CUDA(cudaEventRecord(e[0], ctx.stream));
+    std::unique_ptr<SepPrecond> P = (o.precond == RUV_PRECOND_AMG || o.precond == RUV_PRECOND_AMG_SA)
+                                        ? make_amg(ctx, sys, o.precond == RUV_PRECOND_AMG_SA)
+                                        : make_ic0(ctx, sys, o.precond == RUV_PRECOND_IC0_COLOR);
+    RUV_CUDA(cudaEventRecord(e[1], ctx.stream));
+    RUV_CUDA(cudaEventSynchronize(e[1]));
+    float ms = 0.f;
+    RUV_CUDA(cudaEventElapsedTime(&ms, e[0], e[1]));
+    ctx.timings[3] = ms;
     if (sys.nrhs == 2) {
-      if (mixed) dispatch_pcg_amg<float, 2>(sh, ctx, sys, x, o, T, st, n_active, out, smooth);
-      else dispatch_pcg_amg<double, 2>(sh, ctx, sys, x, o, T, st, n_active, out, smooth);
+      if (mixed) dispatch_pcg_sep<float, 2>(sh, ctx, sys, x, o, T, st, n_active, out, *P);
+      else dispatch_pcg_sep<double, 2>(sh, ctx, sys, x, o, T, st, n_active, out, *P);
     } else {
-      if (mixed) dispatch_pcg_amg<float, 1>(sh, ctx, sys, x, o, T, st, n_active, out, smooth);
-      else dispatch_pcg_amg<double, 1>(sh, ctx, sys, x, o, T, st, n_active, out, smooth);
+      if (mixed) dispatch_pcg_sep<float, 1>(sh, ctx, sys, x, o, T, st, n_active, out, *P);
+      else dispatch_pcg_sep<double, 1>(sh, ctx, sys, x, o, T, st, n_active, out, *P);
     }
   } else if (sys.nrhs == 2) {
     if (mixed) dispatch_pcg<float, 2>(sh, ctx, sys, x, o, T, st, n_active, out);

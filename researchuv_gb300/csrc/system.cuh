@@ -2,6 +2,8 @@
 // produce and consume it.
 #pragma once
 
+#include <memory>
+
 #include "common.cuh"
 
 namespace ruv {
@@ -42,14 +44,34 @@ struct ChartResult {
 
 struct Ctx;
 
-// Batched aggregation AMG (amg.cu): set up on the device from an assembled system, bound to
-// the CG's level-0 vectors, applied as one V-cycle (launches only, capturable).
+// A preconditioner applied as its own launch sequence between the CG's update and direction
+// steps: z = M^-1 r for every chart whose CG is still running.  Set up from an assembled
+// system on construction; bound once to the CG's r and z; apply() only enqueues launches
+// (capturable in a CUDA graph) and returns how many.
+struct SepPrecond {
+  virtual ~SepPrecond() = default;
+  virtual bool native_fp64() const = 0;  // applies in FP64 under the FP64 loop (else FP32 copies)
+  virtual bool flexible() const = 0;     // varies between applications: flexible-CG beta
+  virtual void bind(Ctx& ctx, void* r, void* z, bool fp64) = 0;
+  virtual int apply(Ctx& ctx, const int32_t* done) = 0;
+};
+
+// Batched aggregation AMG (amg.cu): hierarchy built on the device, one V(1,1) cycle per apply.
 struct AmgHierarchy;
 AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string& info);
 void amg_free(AmgHierarchy* H);
 int amg_levels(const AmgHierarchy* H);
 void amg_bind(Ctx& ctx, AmgHierarchy* H, float* r0, float* z0);
 int amg_apply(Ctx& ctx, AmgHierarchy* H, const int32_t* done);
+std::unique_ptr<SepPrecond> make_amg(Ctx& ctx, const DevSystem& sys, bool smooth);
+
+// Batched IC(0), natural or multi-colour ordering (ic0.cu): factor on the device, two
+// level-scheduled triangular sweeps per apply.
+std::unique_ptr<SepPrecond> make_ic0(Ctx& ctx, const DevSystem& sys, bool colored);
+// One FP64 application z = (L L^T)^-1 r on device vectors (factor built and dropped).
+void ic0_apply_once(Ctx& ctx, const DevSystem& sys, const double* d_r, double* d_z, int* fwd_levels);
+void ic0_export(Ctx& ctx, const DevSystem& sys, bool colored, std::vector<int64_t>& ptr, std::vector<int32_t>& cols,
+                std::vector<double>& vals, std::vector<int32_t>& to_orig, int& levels, int& colours);
 
 // x (nrhs * n_rows, device) <- A^-1 b per chart.  Returns per-chart results (host).
 std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o);

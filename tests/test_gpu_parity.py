@@ -14,6 +14,7 @@ import pytest
 import researchuv_gb300 as R
 from oracle import oracle as O
 from researchuv_gb300 import workloads as W
+from systems import lap1d as _lap1d, poisson as _poisson
 
 pytestmark = pytest.mark.gpu
 
@@ -116,23 +117,6 @@ def test_repeatable_bitwise(ctx):
 
 
 # ------------------------------------------------------------------ GpuSolver known answers
-def _lap1d(n):
-    vals, cols, rp = [], [], [0]
-    for i in range(n):
-        if i > 0:
-            vals.append(-1.0)
-            cols.append(i - 1)
-        vals.append(2.0)
-        cols.append(i)
-        if i + 1 < n:
-            vals.append(-1.0)
-            cols.append(i + 1)
-        rp.append(len(vals))
-    b = np.zeros(n)
-    b[0] = b[-1] = 1.0
-    return R.CsrMatrix(np.array(vals), np.array(cols), np.array(rp)), b
-
-
 def test_cg_laplacian_1d(known):
     k = known["gpu_cg"]["laplacian_1d_4096"]
     g = R.GpuSolver.global_()
@@ -165,23 +149,6 @@ def test_cg_banded_500k(known):
     for row in [0, n // 2, n - 1]:
         s = sum(a.vals[q] * x[a.cols[q]] for q in range(a.row_ptr[row], a.row_ptr[row + 1]))
         assert abs(s - b[row]) < k["row_check_tol"]
-
-
-def _poisson(side):
-    n = side * side
-    rows, cols, vals = [], [], []
-    for rr in range(side):
-        for cc in range(side):
-            i = rr * side + cc
-            for r2, c2 in [(rr - 1, cc), (rr, cc - 1)]:
-                if r2 >= 0 and c2 >= 0:
-                    rows.append(i); cols.append(r2 * side + c2); vals.append(-1.0)
-            rows.append(i); cols.append(i); vals.append(4.05 if i % 11 == 0 else 4.0)
-            for r2, c2 in [(rr + 1, cc), (rr, cc + 1)]:
-                if r2 < side and c2 < side:
-                    rows.append(i); cols.append(r2 * side + c2); vals.append(-1.0)
-    rp = np.concatenate([[0], np.cumsum(np.bincount(np.array(rows), minlength=n))])
-    return R.CsrMatrix(np.array(vals), np.array(cols), rp), (np.arange(n) % 97) * 0.01 + 1.0
 
 
 def test_cg_poisson_preconditioning(known):
