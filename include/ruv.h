@@ -177,6 +177,36 @@ ruv_status ruv_lscm_upload(ruv_ctx* ctx, const ruv_lscm_batch* in);
 ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ruv_chart_stat* stats);
 ruv_status ruv_lscm_download_uv(ruv_ctx* ctx, double* uv_out);
 
+/* Differentiation (the forward / backward pair a torch.autograd.Function would wrap).
+ * No counterpart in the reference's API: its unfold is not differentiable.
+ *
+ * ruv_lscm_forward: the forward solve, exactly ruv_lscm_solve_batch; the batch and the
+ * solution stay on the context for the backward call.
+ *
+ * ruv_lscm_backward: given dL/duv (2 * n_verts, chart-local vertex order as uv_out), writes
+ * dL/dp3 (3 * n_verts) of the last forward solve, the pins held at their targets.  The
+ * assembly is recomputed; one adjoint solve A lam = dL/duv (free rows) runs with the same
+ * operator, preconditioner and precision as `opts` asks; the reverse pass of the assembly
+ * (edge coefficients, cotangents) maps lam to the positions.  stats (may be NULL) report the
+ * adjoint solve per chart.  dL/duv of pinned vertices is ignored (their UVs are constants). */
+ruv_status ruv_lscm_forward(ruv_ctx* ctx, const ruv_lscm_batch* in, const ruv_unfold_opts* opts,
+                            double* uv_out, ruv_chart_stat* stats);
+ruv_status ruv_lscm_backward(ruv_ctx* ctx, const ruv_unfold_opts* opts, const double* dl_duv,
+                             double* dl_dp3, ruv_chart_stat* stats);
+
+/* Distortion loss of a UV layout of the resident batch: per chart
+ * sum_t area_t (s1/s2 - 1)^2, area_t the 3-D triangle area and s1 >= s2 the singular values
+ * of the UV Jacobian as unwrap/src/metrics.rs:73-128 forms them (triangles that metric skips
+ * add nothing).  loss_out: n_charts; dl_duv (2 * n_verts) and dl_dp3 (3 * n_verts) receive
+ * its gradients when non-NULL. */
+ruv_status ruv_distortion_loss(ruv_ctx* ctx, const double* uv, double* loss_out, double* dl_duv,
+                               double* dl_dp3);
+
+/* chart_distortion (unwrap/src/metrics.rs:73-141) of a UV layout of the resident batch: per
+ * chart [conformal mean, conformal max, area-ratio mean, flips, folds] (metrics_out:
+ * 5 * n_charts). */
+ruv_status ruv_chart_distortion(ruv_ctx* ctx, const double* uv, double* metrics_out);
+
 /* Device time (ms, CUDA events on the context stream) of the phases of the last
  * ruv_lscm_solve_resident: [0] assembly, [1] batched PCG, [2] driver update, [3] the
  * preconditioner set-up inside [1] (AMG hierarchy; 0 otherwise).

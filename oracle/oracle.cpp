@@ -19,6 +19,9 @@
 //   vector arithmetic    math/src/vec.rs:100-124
 //   IC(0) + colouring    gpu/src/precond.rs:49-123 (graph_coloring, color_permutation,
 //                        permute_csr), :145-262 (factor_ic0, tri_levels, transpose_lower)
+//   fixed-pin system     lscm.rs:594-676 with the pins given (the map the adjoint
+//                        differentiates), its reverse pass and the metrics.rs:73-128
+//                        distortion loss with its gradient (forward-mode duals, 15 seeds)
 //
 // Arithmetic follows the Rust evaluation order (left-to-right sums, no FMA contraction:
 // compile with -ffp-contract=off) so that results are bit-identical to the reference on
@@ -1130,6 +1133,121 @@ void color_permute(const Csr& a, const std::vector<int64_t>& color, std::vector<
   }
 }
 
+
+// ---------------------------------------------------------------- fixed-pin system + adjoint
+// Forward-mode dual numbers (value + N partials), CPU.
+template <int N>
+struct Dn {
+  double v = 0.0;
+  std::array<double, N> d{};
+  Dn() = default;
+  Dn(double x) : v(x) {}
+};
+template <int N> Dn<N> operator+(const Dn<N>& a, const Dn<N>& b) { Dn<N> r(a.v + b.v); for (int k = 0; k < N; ++k) r.d[k] = a.d[k] + b.d[k]; return r; }
+template <int N> Dn<N> operator-(const Dn<N>& a, const Dn<N>& b) { Dn<N> r(a.v - b.v); for (int k = 0; k < N; ++k) r.d[k] = a.d[k] - b.d[k]; return r; }
+template <int N> Dn<N> operator-(const Dn<N>& a) { Dn<N> r(-a.v); for (int k = 0; k < N; ++k) r.d[k] = -a.d[k]; return r; }
+template <int N> Dn<N> operator*(const Dn<N>& a, const Dn<N>& b) { Dn<N> r(a.v * b.v); for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k]; return r; }
+template <int N> Dn<N> operator/(const Dn<N>& a, const Dn<N>& b) { Dn<N> r(a.v / b.v); for (int k = 0; k < N; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v); return r; }
+template <int N> Dn<N> dnsqrt(const Dn<N>& a) { Dn<N> r(std::sqrt(a.v)); for (int k = 0; k < N; ++k) r.d[k] = r.v > 0.0 ? a.d[k] / (2.0 * r.v) : 0.0; return r; }
+template <int N> Dn<N> dnmax(const Dn<N>& a, double c) { return a.v > c ? a : Dn<N>(c); }
+
+struct FixedSystem {
+  size_t n = 0, nf = 0;
+  std::vector<V3> p3;
+  std::vector<std::array<uint32_t, 3>> tris;
+  std::vector<char> pinned;
+  std::vector<V2> pin_uv;
+  std::vector<long> row_of;
+  std::vector<std::map<size_t, double>> rows;  // scalar L over free vertices
+  std::vector<double> b;                       // 2 nf
+};
+
+FixedSystem fixed_system(Bag* bg) {
+  FixedSystem S;
+  const auto& P = bg->f["p3"];
+  const auto& T = bg->i["tris"];
+  const auto& pin = bg->i["pinned"];
+  const auto& pu = bg->f["pin_uv"];
+  S.n = pin.size();
+  for (size_t i = 0; i < S.n; ++i) {
+    S.p3.push_back({P[3 * i], P[3 * i + 1], P[3 * i + 2]});
+    S.pinned.push_back(pin[i] ? 1 : 0);
+    S.pin_uv.push_back({pu[2 * i], pu[2 * i + 1]});
+  }
+  for (size_t t = 0; t + 2 < T.size(); t += 3) S.tris.push_back({(uint32_t)T[t], (uint32_t)T[t + 1], (uint32_t)T[t + 2]});
+  S.row_of.assign(S.n, -1);
+  for (size_t i = 0; i < S.n; ++i)
+    if (!S.pinned[i]) S.row_of[i] = (long)S.nf++;
+  S.rows.assign(S.nf, {});
+  S.b.assign(2 * S.nf, 0.0);
+  auto ew = edge_weights(S.p3, S.tris);
+  for (auto& kv : ew) {  // lscm.rs:594-676 with mix_b = 0 (angle_mix = 1, the default)
+    size_t i = kv.first.first, j = kv.first.second;
+    double w = kv.second;
+    if (w <= EPS_DEGENERATE) continue;
+    V3 d3 = sub(S.p3[j], S.p3[i]);
+    double c = w / rmax(dot(d3, d3), EPS_DEGENERATE);
+    size_t ab[2][2] = {{i, j}, {j, i}};
+    for (auto& e : ab) {
+      if (S.pinned[e[0]]) continue;
+      size_t r = (size_t)S.row_of[e[0]];
+      if (c != 0.0) S.rows[r][r] += c;  // Sparse::add skips zeros
+      if (!S.pinned[e[1]]) {
+        if (c != 0.0) S.rows[r][(size_t)S.row_of[e[1]]] += -c;
+      } else {
+        S.b[2 * r] += c * S.pin_uv[e[1]].u;
+        S.b[2 * r + 1] += c * S.pin_uv[e[1]].v;
+      }
+    }
+  }
+  return S;
+}
+
+// The distortion term of one triangle as metrics.rs:95-128 forms it: 0.5 |n| (s1/s2 - 1)^2.
+template <class T>
+bool tri_distortion_cpu(const T (&p)[9], const T (&u)[6], T& out) {
+  T e1x = p[3] - p[0], e1y = p[4] - p[1], e1z = p[5] - p[2];
+  T e2x = p[6] - p[0], e2y = p[7] - p[1], e2z = p[8] - p[2];
+  T nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+  T ln = dnsqrt(nx * nx + ny * ny + nz * nz);
+  if (ln.v < 1e-30) return false;
+  T ux = nx / ln, uy = ny / ln, uz = nz / ln;
+  T l1 = dnmax(dnsqrt(e1x * e1x + e1y * e1y + e1z * e1z), 1e-30);
+  T t1x = e1x / l1, t1y = e1y / l1, t1z = e1z / l1;
+  T t2x = uy * t1z - uz * t1y, t2y = uz * t1x - ux * t1z, t2z = ux * t1y - uy * t1x;
+  T e1t1 = e1x * t1x + e1y * t1y + e1z * t1z, e2t1 = e2x * t1x + e2y * t1y + e2z * t1z;
+  T e1t2 = e1x * t2x + e1y * t2y + e1z * t2z, e2t2 = e2x * t2x + e2y * t2y + e2z * t2z;
+  T det = e1t1 * e2t2 - e2t1 * e1t2;
+  if (std::fabs(det.v) < 1e-30) return false;
+  T i00 = e2t2 / det, i01 = -e2t1 / det, i10 = -e1t2 / det, i11 = e1t1 / det;
+  T d1u = u[2] - u[0], d1v = u[3] - u[1], d2u = u[4] - u[0], d2v = u[5] - u[1];
+  T f00 = d1u * i00 + d2u * i10, f01 = d1u * i01 + d2u * i11;
+  T f10 = d1v * i00 + d2v * i10, f11 = d1v * i01 + d2v * i11;
+  T a = f00 * f00 + f10 * f10, bq = f00 * f01 + f10 * f11, c = f01 * f01 + f11 * f11;
+  T tr = a + c, dd = T(0.5) * (a - c);
+  T disc = dnsqrt(dnmax(dd * dd + bq * bq, 0.0));
+  T s1 = dnsqrt(dnmax(T(0.5) * tr + disc, 0.0)), s2 = dnsqrt(dnmax(T(0.5) * tr - disc, 0.0));
+  T r = s1 / dnmax(s2, 1e-30) - T(1.0);
+  out = T(0.5) * ln * r * r;
+  return true;
+}
+
+// Clamped corner cotangent as edge_weights forms it (lscm.rs:256-268); false where skipped.
+template <class T>
+bool corner_cot_cpu(const T (&o)[3], const T (&e1)[3], const T (&e0)[3], T& out) {
+  T a1[3] = {e1[0] - o[0], e1[1] - o[1], e1[2] - o[2]};
+  T a2[3] = {e0[0] - o[0], e0[1] - o[1], e0[2] - o[2]};
+  T la = dnsqrt(a1[0] * a1[0] + a1[1] * a1[1] + a1[2] * a1[2]);
+  T lb = dnsqrt(a2[0] * a2[0] + a2[1] * a2[1] + a2[2] * a2[2]);
+  if (la.v <= EPS_DEGENERATE || lb.v <= EPS_DEGENERATE) return false;
+  T cx = a1[1] * a2[2] - a1[2] * a2[1], cy = a1[2] * a2[0] - a1[0] * a2[2], cz = a1[0] * a2[1] - a1[1] * a2[0];
+  T s_ = dnsqrt(cx * cx + cy * cy + cz * cz) / (la * lb);
+  if (s_.v <= EPS_DEGENERATE) return false;
+  T dt = a1[0] * a2[0] + a1[1] * a2[1] + a1[2] * a2[2];
+  out = dnmax((dt / (la * lb)) / s_, 0.0);
+  return true;
+}
+
 Csr bag_csr(Bag* b, const std::string& pre) {
   Csr a;
   a.ptr = b->i[pre + ".row_ptr"];
@@ -1548,6 +1666,136 @@ void orc_ic0_apply(void* h, const double* r, double* z) {
     double s_ = y[i];
     for (int64_t k = tp[i]; k < tp[i + 1] - 1; ++k) s_ -= tv[k] * z[tc[k]];
     z[i] = s_ / get(tp, tc, tv, i, i);
+  }
+}
+
+// Fixed-pin LSCM system of one chart: bag {"p3" (3n), "tris" (3T, local), "pinned" (n),
+// "pin_uv" (2n)} -> {"row_of" (n, -1 pinned), "csr.ptr", "csr.cols", "csr.vals" (scalar L
+// over free vertices, columns ascending), "b" (2 nf)}.
+void orc_lscm_fixed(void* h) {
+  Bag* b = static_cast<Bag*>(h);
+  FixedSystem S = fixed_system(b);
+  std::vector<int64_t> ptr(1, 0), cols, row_of(S.n);
+  std::vector<double> vals;
+  for (size_t r = 0; r < S.nf; ++r) {
+    for (auto& kv : S.rows[r]) {
+      cols.push_back((int64_t)kv.first);
+      vals.push_back(kv.second);
+    }
+    ptr.push_back((int64_t)cols.size());
+  }
+  for (size_t i = 0; i < S.n; ++i) row_of[i] = S.row_of[i];
+  b->i["row_of"] = row_of;
+  b->i["csr.ptr"] = ptr;
+  b->i["csr.cols"] = cols;
+  b->f["csr.vals"] = vals;
+  b->f["b"] = S.b;
+}
+
+// Distortion loss of a layout (uv: 2n, all vertices) with its gradients: per-triangle terms
+// summed in triangle order into *loss; duv (2n) and dp3 (3n) receive the gradients.
+// Triangles with all three vertices pinned are left out (their UVs come from the pin rule,
+// which can make them collinear).  Also bag "loss_t" (per triangle, 0 where skipped).
+void orc_distortion_loss(void* h, const double* uv, double* loss, double* duv, double* dp3) {
+  Bag* b = static_cast<Bag*>(h);
+  const auto& P = b->f["p3"];
+  const auto& T = b->i["tris"];
+  const auto& pin = b->i["pinned"];
+  const size_t n = P.size() / 3, nt = T.size() / 3;
+  std::fill(duv, duv + 2 * n, 0.0);
+  std::fill(dp3, dp3 + 3 * n, 0.0);
+  std::vector<double> lt(nt, 0.0);
+  double total = 0.0;
+  for (size_t t = 0; t < nt; ++t) {
+    size_t v[3] = {(size_t)T[3 * t], (size_t)T[3 * t + 1], (size_t)T[3 * t + 2]};
+    if (pin[v[0]] && pin[v[1]] && pin[v[2]]) continue;
+    Dn<15> p[9], u[6];
+    for (int k = 0; k < 3; ++k) {
+      for (int j = 0; j < 3; ++j) {
+        p[3 * k + j] = Dn<15>(P[3 * v[k] + j]);
+        p[3 * k + j].d[3 * k + j] = 1.0;
+      }
+      for (int j = 0; j < 2; ++j) {
+        u[2 * k + j] = Dn<15>(uv[2 * v[k] + j]);
+        u[2 * k + j].d[9 + 2 * k + j] = 1.0;
+      }
+    }
+    Dn<15> out;
+    if (!tri_distortion_cpu(p, u, out)) continue;
+    lt[t] = out.v;
+    total += out.v;
+    for (int k = 0; k < 3; ++k) {
+      for (int j = 0; j < 3; ++j) dp3[3 * v[k] + j] += out.d[3 * k + j];
+      for (int j = 0; j < 2; ++j) duv[2 * v[k] + j] += out.d[9 + 2 * k + j];
+    }
+  }
+  b->f["loss_t"] = lt;
+  *loss = total;
+}
+
+// Reverse pass of the fixed-pin assembly: given the solution x and the adjoint lam (2 nf
+// each, free rows), dp3 (3n) = d(lam^T (b - A x)) / dp3, i.e. the position gradient of a
+// loss whose uv-gradient produced lam.
+void orc_lscm_adjoint_positions(void* h, const double* x, const double* lam, double* dp3) {
+  Bag* b = static_cast<Bag*>(h);
+  FixedSystem S = fixed_system(b);
+  std::fill(dp3, dp3 + 3 * S.n, 0.0);
+  auto ew = edge_weights(S.p3, S.tris);
+  std::map<std::pair<size_t, size_t>, double> gw;  // dL/dw per edge
+  for (auto& kv : ew) {
+    size_t i = kv.first.first, j = kv.first.second;
+    double w = kv.second;
+    if (w <= EPS_DEGENERATE) continue;
+    if (S.pinned[i] && S.pinned[j]) continue;
+    auto uvl = [&](size_t v, double& u0, double& u1, double& l0, double& l1) {
+      if (S.pinned[v]) {
+        u0 = S.pin_uv[v].u;
+        u1 = S.pin_uv[v].v;
+        l0 = l1 = 0.0;
+      } else {
+        size_t r = (size_t)S.row_of[v];
+        u0 = x[2 * r];
+        u1 = x[2 * r + 1];
+        l0 = lam[2 * r];
+        l1 = lam[2 * r + 1];
+      }
+    };
+    double ui0, ui1, li0, li1, uj0, uj1, lj0, lj1;
+    uvl(i, ui0, ui1, li0, li1);
+    uvl(j, uj0, uj1, lj0, lj1);
+    const double gc = -((li0 - lj0) * (ui0 - uj0) + (li1 - lj1) * (ui1 - uj1));
+    V3 d3 = sub(S.p3[j], S.p3[i]);
+    const double d2 = dot(d3, d3);
+    if (d2 > EPS_DEGENERATE) {
+      gw[kv.first] = gc / d2;
+      const double gd2 = -gc * w / (d2 * d2);
+      const double g3[3] = {2.0 * gd2 * d3.x, 2.0 * gd2 * d3.y, 2.0 * gd2 * d3.z};
+      for (int k = 0; k < 3; ++k) {
+        dp3[3 * j + k] += g3[k];
+        dp3[3 * i + k] -= g3[k];
+      }
+    } else {
+      gw[kv.first] = gc / EPS_DEGENERATE;
+    }
+  }
+  for (auto& t : S.tris) {  // cotangent partials by duals over the 9 coordinates
+    size_t vs[3] = {t[0], t[1], t[2]};
+    Dn<9> q[3][3];
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j) {
+        q[k][j] = Dn<9>(S.p3[vs[k]].x * (j == 0) + S.p3[vs[k]].y * (j == 1) + S.p3[vs[k]].z * (j == 2));
+        q[k][j].d[3 * k + j] = 1.0;
+      }
+    int cs[3][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}};  // (e0, e1, o) as edge_weights walks them
+    for (auto& c : cs) {
+      size_t e0 = vs[c[0]], e1 = vs[c[1]];
+      auto it = gw.find(std::make_pair(std::min(e0, e1), std::max(e0, e1)));
+      if (it == gw.end() || it->second == 0.0) continue;
+      Dn<9> ct;
+      if (!corner_cot_cpu(q[c[2]], q[c[1]], q[c[0]], ct) || !(ct.v > 0.0)) continue;
+      for (int k = 0; k < 3; ++k)
+        for (int j = 0; j < 3; ++j) dp3[3 * vs[k] + j] += it->second * ct.d[3 * k + j];
+    }
   }
 }
 }  // extern "C"

@@ -62,6 +62,9 @@ def lib():
         L.orc_ic0.argtypes = [vp, ctypes.c_int]
         L.orc_ic0.restype = ctypes.c_int
         L.orc_ic0_apply.argtypes = [vp, P(f64), P(f64)]
+        L.orc_lscm_fixed.argtypes = [vp]
+        L.orc_distortion_loss.argtypes = [vp, P(f64), P(f64), P(f64), P(f64)]
+        L.orc_lscm_adjoint_positions.argtypes = [vp, P(f64), P(f64), P(f64)]
         _lib = L
     return _lib
 
@@ -293,4 +296,123 @@ class Ic0:
         z = np.zeros_like(r)
         lib().orc_ic0_apply(self.bag.h, _f64p(r), _f64p(z))
         return z
+
+
+class FixedPinChart:
+    """One chart's LSCM system with the pins given (unwrap/src/lscm.rs:594-676, mix_b = 0),
+    solved by SuperLU in FP64, with the CPU reference gradient of a loss through the solve:
+    lam = A^-1 dL/duv, then the reverse pass of the assembly (edge coefficients and corner
+    cotangents differentiated by forward-mode duals)."""
+
+    def __init__(self, p3, tris, pinned, pin_uv):
+        self.p3 = np.ascontiguousarray(p3, np.float64).reshape(-1, 3)
+        self.tris = np.ascontiguousarray(tris, np.int64).reshape(-1, 3)
+        self.pinned = np.ascontiguousarray(pinned, np.int64).reshape(-1)
+        self.pin_uv = np.ascontiguousarray(pin_uv, np.float64).reshape(-1, 2)
+        self.bag = Bag()
+        self.bag.put_f64("p3", self.p3.reshape(-1))
+        self.bag.put_i64("tris", self.tris.reshape(-1))
+        self.bag.put_i64("pinned", self.pinned)
+        self.bag.put_f64("pin_uv", self.pin_uv.reshape(-1))
+        lib().orc_lscm_fixed(self.bag.h)
+        import scipy.sparse as sp
+        self.row_of = self.bag.i64("row_of")
+        nf = int((self.row_of >= 0).sum())
+        self.nf = nf
+        self.A = sp.csr_matrix((self.bag.f64("csr.vals"), self.bag.i64("csr.cols"), self.bag.i64("csr.ptr")),
+                               shape=(nf, nf))
+        self.b = self.bag.f64("b").reshape(nf, 2)
+        self._lu = None
+
+    def lu(self):
+        if self._lu is None:
+            import scipy.sparse.linalg as sla
+            self._lu = sla.splu(self.A.tocsc(), permc_spec="MMD_AT_PLUS_A")
+        return self._lu
+
+    def solve(self, rhs=None):
+        return self.lu().solve(self.b if rhs is None else rhs)
+
+    def uv(self, x=None):
+        """All-vertex UVs: the solution on free vertices, the pins elsewhere."""
+        x = self.solve() if x is None else x
+        out = self.pin_uv.copy()
+        free = self.row_of >= 0
+        out[free] = x[self.row_of[free]]
+        return out
+
+    def distortion(self, uv):
+        """(loss, dL/duv (n,2), dL/dp3 (n,3), per-triangle terms)."""
+        uv = np.ascontiguousarray(uv, np.float64).reshape(-1)
+        n = len(self.pinned)
+        loss = ctypes.c_double(0.0)
+        duv = np.zeros(2 * n)
+        dp3 = np.zeros(3 * n)
+        lib().orc_distortion_loss(self.bag.h, _f64p(uv), ctypes.byref(loss), _f64p(duv), _f64p(dp3))
+        return loss.value, duv.reshape(n, 2), dp3.reshape(n, 3), self.bag.f64("loss_t")
+
+    def adjoint_positions(self, x, lam):
+        """dp3 (n,3) of lam^T (b - A x): the position gradient through the solve."""
+        n = len(self.pinned)
+        dp3 = np.zeros(3 * n)
+        lib().orc_lscm_adjoint_positions(self.bag.h, _f64p(np.ascontiguousarray(x, np.float64).reshape(-1)),
+                                         _f64p(np.ascontiguousarray(lam, np.float64).reshape(-1)), _f64p(dp3))
+        return dp3.reshape(n, 3)
+
+
+def config4_loss(chart: "FixedPinChart", x, lam_l2: float, target):
+    """Loss of the differentiation workload for a solution x of `chart`:
+    sum_t area_t (s1/s2 - 1)^2 + lam_l2 * sum_v |uv_v - target_v|^2 over all vertices.
+    Returns (loss, uv, per-triangle distortion terms)."""
+    uv = chart.uv(x)
+    d, _, _, lt = chart.distortion(uv)
+    return d + lam_l2 * float(((uv - target) ** 2).sum()), uv, lt
+
+
+def lu_adjoint_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target):
+    """CPU reference gradient dL/dp3 (n, 3) of config4_loss through the fixed-pin solve:
+    SuperLU solve, lam = A^-1 dL/duv (free rows), reverse pass of the assembly, plus the
+    explicit position gradient of the distortion term."""
+    ch = FixedPinChart(p3, tris, pinned, pin_uv)
+    x = ch.solve()
+    uv = ch.uv(x)
+    _, duv, dp_dist, _ = ch.distortion(uv)
+    g = duv + 2.0 * lam_l2 * (uv - target)
+    free = ch.row_of >= 0
+    gf = np.zeros((ch.nf, 2))
+    gf[ch.row_of[free]] = g[free]
+    lam = ch.solve(gf)
+    return dp_dist + ch.adjoint_positions(x, lam), uv
+
+
+def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float = 1e-6):
+    """Central differences of config4_loss with respect to p3[v, k] for (v, k) in picks,
+    through the fixed-pin solve.  The perturbed solution is formed as x + dx with
+    A' dx = (b' - b) - (A' - A) x (a right-hand side that is exactly zero away from v), and
+    the loss difference term by term, so neither the solve's rounding nor the cancellation
+    of two large loss totals reaches the difference quotient."""
+    p3 = np.ascontiguousarray(p3, np.float64).reshape(-1, 3)
+    base = FixedPinChart(p3, tris, pinned, pin_uv)
+    x = base.solve()
+    uv = base.uv(x)
+    _, _, _, lt = base.distortion(uv)
+    free = base.row_of >= 0
+    out = []
+    for v, k in picks:
+        diffs = []
+        for sgn in (1.0, -1.0):
+            q = p3.copy()
+            q[v, k] += sgn * h
+            ch = FixedPinChart(q, tris, pinned, pin_uv)
+            assert np.array_equal(ch.A.indptr, base.A.indptr) and np.array_equal(ch.A.indices, base.A.indices)
+            dA = ch.A.copy()
+            dA.data = ch.A.data - base.A.data
+            dx = ch.solve((ch.b - base.b) - dA @ x)
+            uv2 = uv.copy()
+            uv2[free] = uv[free] + dx[base.row_of[free]]
+            _, _, _, lt2 = ch.distortion(uv2)
+            du = uv2 - uv
+            diffs.append(float((lt2 - lt).sum()) + lam_l2 * float((du * (uv2 + uv - 2.0 * target)).sum()))
+        out.append((diffs[0] - diffs[1]) / (2.0 * h))
+    return np.array(out)
 

@@ -75,6 +75,10 @@ SIGNATURES = {
     "ruv_lscm_upload": (ctypes.c_int, [_vp, _P(RuvBatch)]),
     "ruv_lscm_solve_resident": (ctypes.c_int, [_vp, _P(RuvUnfoldOpts), _P(RuvChartStat)]),
     "ruv_lscm_download_uv": (ctypes.c_int, [_vp, _P(_f64)]),
+    "ruv_lscm_forward": (ctypes.c_int, [_vp, _P(RuvBatch), _P(RuvUnfoldOpts), _P(_f64), _P(RuvChartStat)]),
+    "ruv_lscm_backward": (ctypes.c_int, [_vp, _P(RuvUnfoldOpts), _P(_f64), _P(_f64), _P(RuvChartStat)]),
+    "ruv_distortion_loss": (ctypes.c_int, [_vp, _P(_f64), _P(_f64), _P(_f64), _P(_f64)]),
+    "ruv_chart_distortion": (ctypes.c_int, [_vp, _P(_f64), _P(_f64)]),
     "ruv_last_timings": (_i32, [_vp, _P(_f64), _i32]),
     "ruv_kernel_launches": (_i64, [_vp]),
     "ruv_cg_solve_noalloc": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _i64, _f64, ctypes.c_int, _P(_i64), _vp,
@@ -437,6 +441,51 @@ def unfold_charts(ctx: Context, charts: Charts, opts: Optional[UnfoldOptions] = 
                                 area3d=float(area[c]), status=Status(s.status), cg_iters=s.cg_iters,
                                 n_free=s.n_free, rel_res=s.rel_res))
     return out
+
+
+# ------------------------------------------------------------------ differentiation
+def lscm_forward(ctx: Context, batch: RuvBatch, opts: UnfoldOptions, n_verts: int):
+    """Forward half of the differentiable unfold (ruv_lscm_forward): the batched solve; the
+    batch and its solution stay on the context.  Returns (uv (n_verts, 2), stats)."""
+    o = opts.to_c()
+    uv = np.empty((n_verts, 2), np.float64)
+    stats = (RuvChartStat * max(batch.n_charts, 1))()
+    ctx.check(lib().ruv_lscm_forward(ctx.h, ctypes.byref(batch), ctypes.byref(o), _ptr(uv, _f64), stats),
+              "ruv_lscm_forward")
+    return uv, [stats[i] for i in range(batch.n_charts)]
+
+
+def lscm_backward(ctx: Context, dl_duv, opts: UnfoldOptions, n_charts: int):
+    """Backward half (ruv_lscm_backward): dL/dp3 (n_verts, 3) of the last forward solve from
+    dL/duv (n_verts, 2), pins held at their targets.  Returns (dL/dp3, adjoint-solve stats)."""
+    g = np.ascontiguousarray(dl_duv, np.float64).reshape(-1, 2)
+    dp = np.empty((g.shape[0], 3), np.float64)
+    o = opts.to_c()
+    stats = (RuvChartStat * max(n_charts, 1))()
+    ctx.check(lib().ruv_lscm_backward(ctx.h, ctypes.byref(o), _ptr(g, _f64), _ptr(dp, _f64), stats),
+              "ruv_lscm_backward")
+    return dp, [stats[i] for i in range(n_charts)]
+
+
+def distortion_loss(ctx: Context, uv, n_charts: int, grad: bool = True):
+    """sum_t area_t (s1/s2 - 1)^2 per chart of the resident batch (ruv_distortion_loss).
+    Returns (loss (n_charts,), dL/duv (n, 2) or None, dL/dp3 (n, 3) or None)."""
+    u = np.ascontiguousarray(uv, np.float64).reshape(-1, 2)
+    loss = np.empty(max(n_charts, 1), np.float64)
+    duv = np.empty_like(u) if grad else None
+    dp = np.empty((u.shape[0], 3), np.float64) if grad else None
+    ctx.check(lib().ruv_distortion_loss(ctx.h, _ptr(u, _f64), _ptr(loss, _f64), _ptr(duv, _f64), _ptr(dp, _f64)),
+              "ruv_distortion_loss")
+    return loss[:n_charts], duv, dp
+
+
+def chart_distortion(ctx: Context, uv, n_charts: int) -> np.ndarray:
+    """chart_distortion (metrics.rs:73-141) per chart of the resident batch: rows of
+    [conformal mean, conformal max, area-ratio mean, flips, folds]."""
+    u = np.ascontiguousarray(uv, np.float64).reshape(-1, 2)
+    out = np.empty((max(n_charts, 1), 5), np.float64)
+    ctx.check(lib().ruv_chart_distortion(ctx.h, _ptr(u, _f64), _ptr(out, _f64)), "ruv_chart_distortion")
+    return out[:n_charts]
 
 
 def export_chart_system(ctx: Context, chart: int):

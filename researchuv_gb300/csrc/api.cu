@@ -275,6 +275,7 @@ ruv_status ruv_lscm_upload(ruv_ctx* ctx, const ruv_lscm_batch* in) {
     bt.n_verts = NV;
     bt.n_tris = NT;
     bt.h_vert_off.assign(in->vert_off, in->vert_off + NC + 1);
+    bt.h_tri_off.assign(in->tri_off, in->tri_off + NC + 1);
     bt.vert_off = upload(c, "in.vert_off", in->vert_off, NC + 1);
     bt.tri_off = upload(c, "in.tri_off", in->tri_off, NC + 1);
     bt.p3 = upload(c, "in.p3", in->p3, 3 * NV);
@@ -384,6 +385,102 @@ ruv_status ruv_lscm_solve_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, const ru
   if (s != RUV_OK) return s;
   ctx->c.last_error = msg;
   return solved;
+}
+
+ruv_status ruv_lscm_forward(ruv_ctx* ctx, const ruv_lscm_batch* in, const ruv_unfold_opts* opts, double* uv_out,
+                            ruv_chart_stat* stats) {
+  return ruv_lscm_solve_batch(ctx, in, opts, uv_out, stats);
+}
+
+ruv_status ruv_lscm_backward(ruv_ctx* ctx, const ruv_unfold_opts* opts, const double* dl_duv, double* dl_dp3,
+                             ruv_chart_stat* stats) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    if (!c.have_uv || !c.have_batch) return fail(ctx, RUV_ERR_BAD_INPUT, "no forward solve on this context");
+    DevBatch& bt = c.resident;
+    const int64_t NV = bt.n_verts, NC = bt.n_charts;
+    if (NV > 0 && (!dl_duv || !dl_dp3)) return fail(ctx, RUV_ERR_BAD_INPUT, "null gradient buffer");
+    ruv_unfold_opts o;
+    ruv_unfold_opts_default(&o);
+    if (opts) o = *opts;
+    if (!known_precond(o.precond)) return fail(ctx, RUV_ERR_BAD_INPUT, "unknown preconditioner");
+    double* x = c.ws.get<double>("lscm.x", 1);  // the forward solution (rows), kept by the solve
+    // the assembly is recomputed (same inputs, bit-identical operator)
+    DevSystem sys;
+    assemble_lscm(c, bt, sys, o.angle_mix);
+    double* gv = upload(c, "adj.gv", dl_duv, 2 * NV);
+    double* dp = c.ws.get<double>("adj.dp3", std::max<int64_t>(3 * NV, 1));
+    SolveOpts so;
+    so.precond = o.precond;
+    so.precision = o.precision;
+    so.tol = o.tol;
+    so.max_iter = o.max_cg_iter > 0 ? o.max_cg_iter : 16384;
+    std::vector<ChartResult> res;
+    lscm_backward(c, bt, sys, x, gv, so, dp, res);
+    if (NV > 0) RUV_CUDA(cudaMemcpyAsync(dl_dp3, dp, sizeof(double) * 3 * NV, cudaMemcpyDeviceToHost, c.stream));
+    RUV_CUDA(cudaStreamSynchronize(c.stream));
+    int w = RUV_OK;
+    for (int64_t k = 0; k < NC; ++k) {
+      w = worst(w, res[k].status);
+      if (stats) {
+        stats[k].status = res[k].status;
+        stats[k].driver_iters = 0;
+        stats[k].cg_iters = res[k].iters;
+        stats[k].n_free = (int32_t)(sys.h_chart_row[k + 1] - sys.h_chart_row[k]);
+        stats[k].rel_res = res[k].rel_res;
+        stats[k].err_accum = 0.0;
+      }
+    }
+    if (w != RUV_OK) return fail(ctx, (ruv_status)w, "adjoint solve: at least one chart did not converge");
+    return RUV_OK;
+  });
+}
+
+ruv_status ruv_distortion_loss(ruv_ctx* ctx, const double* uv, double* loss_out, double* dl_duv, double* dl_dp3) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    if (!c.have_batch) return fail(ctx, RUV_ERR_BAD_INPUT, "no batch uploaded on this context");
+    const DevBatch& bt = c.resident;
+    const int64_t NV = bt.n_verts, NC = bt.n_charts;
+    if (NV > 0 && !uv) return fail(ctx, RUV_ERR_BAD_INPUT, "null uv");
+    if (NC > 0 && !loss_out) return fail(ctx, RUV_ERR_BAD_INPUT, "null loss_out");
+    const double* duv = upload(c, "dist.uv", uv, 2 * NV);
+    double* g_uv = nullptr;
+    double* g_p = nullptr;
+    if (dl_duv) {
+      g_uv = c.ws.get<double>("dist.guv", std::max<int64_t>(2 * NV, 1));
+      RUV_CUDA(cudaMemsetAsync(g_uv, 0, sizeof(double) * std::max<int64_t>(2 * NV, 1), c.stream));
+    }
+    if (dl_dp3) {
+      g_p = c.ws.get<double>("dist.gp", std::max<int64_t>(3 * NV, 1));
+      RUV_CUDA(cudaMemsetAsync(g_p, 0, sizeof(double) * std::max<int64_t>(3 * NV, 1), c.stream));
+    }
+    std::vector<double> loss;
+    distortion_loss(c, bt, duv, g_uv, g_p, loss);
+    std::copy(loss.begin(), loss.end(), loss_out);
+    if (g_uv && NV > 0) RUV_CUDA(cudaMemcpyAsync(dl_duv, g_uv, sizeof(double) * 2 * NV, cudaMemcpyDeviceToHost, c.stream));
+    if (g_p && NV > 0) RUV_CUDA(cudaMemcpyAsync(dl_dp3, g_p, sizeof(double) * 3 * NV, cudaMemcpyDeviceToHost, c.stream));
+    RUV_CUDA(cudaStreamSynchronize(c.stream));
+    return RUV_OK;
+  });
+}
+
+ruv_status ruv_chart_distortion(ruv_ctx* ctx, const double* uv, double* metrics_out) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    if (!c.have_batch) return fail(ctx, RUV_ERR_BAD_INPUT, "no batch uploaded on this context");
+    const DevBatch& bt = c.resident;
+    const int64_t NV = bt.n_verts, NC = bt.n_charts;
+    if ((NV > 0 && !uv) || (NC > 0 && !metrics_out)) return fail(ctx, RUV_ERR_BAD_INPUT, "null buffer");
+    const double* duv = upload(c, "met.uv", uv, 2 * NV);
+    std::vector<double> out;
+    chart_metrics(c, bt, duv, out);
+    std::copy(out.begin(), out.end(), metrics_out);
+    return RUV_OK;
+  });
 }
 
 int64_t ruv_kernel_launches(const ruv_ctx* ctx) { return ctx ? ctx->c.launches : 0; }

@@ -380,6 +380,8 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   RUV_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   int32_t* tri_g = ws.get<int32_t>("asm.tri_g", 3 * NT);
   double* cot = ws.get<double>("asm.cot", 3 * NT);
+  bt.tri_g = tri_g;
+  bt.cot = cot;
   if (NT > 0) {
     k_globalize<<<div_up(NT, B), B, 0, s>>>(bt.tris, bt.tri_off, bt.vert_off, NC, NT, tri_g, bad);
     count_launches(1);
@@ -424,6 +426,9 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   RUV_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (NV > 0 ? NV : 1), s));
   int2* rec = ws.get<int2>("asm.rec", NREC);
   double* coef = ws.get<double>("asm.coef", NREC);
+  bt.rec_off = rec_off;
+  bt.rec = rec;
+  bt.coef = coef;
   if (NT > 0) {
     k_scatter_records<<<div_up(NT, B), B, 0, s>>>(tri_g, bt.pinned, NT, rec_off, cursor, rec);
     count_launches(1);

@@ -312,8 +312,8 @@ __device__ __forceinline__ void stvec(S* p, int64_t i, const Vec<S, NR>& v) {
 // level solves out[i] = (in[i] - sum_{off-diagonal e} v[e] out[col[e]]) / v[diagonal];
 // forward with L, backward with L^T.  `out` is read and written in the same launch (no
 // read-only path); the block barrier between levels publishes each level's results.
-template <class S, int NR>
-__global__ void __launch_bounds__(kIcThreads) k_sweep(const int64_t* __restrict__ chart_row, const int32_t* __restrict__ done,
+template <class S, int NR, int BT>
+__global__ void __launch_bounds__(BT) k_sweep(const int64_t* __restrict__ chart_row, const int32_t* __restrict__ done,
                                                       const int32_t* __restrict__ rows, const int32_t* __restrict__ lev,
                                                       const int32_t* __restrict__ n_lev, const int64_t* __restrict__ ptr,
                                                       const int32_t* __restrict__ col, const S* __restrict__ val,
@@ -342,6 +342,53 @@ __global__ void __launch_bounds__(kIcThreads) k_sweep(const int64_t* __restrict_
   }
 }
 
+// Global levels, for few and wide levels (a colour-ordered factor, a large chart): level l
+// is the union of every chart's level l, solved by one grid-wide launch.
+__global__ void __launch_bounds__(kIcThreads) k_row_level(const int64_t* __restrict__ chart_row,
+                                                          const int32_t* __restrict__ rows, const int32_t* __restrict__ lev,
+                                                          const int32_t* __restrict__ n_lev, int32_t* __restrict__ row_level,
+                                                          int32_t* __restrict__ row_chart) {
+  const int64_t c = blockIdx.x;
+  const int32_t* lvl = lev + chart_row[c] + c;
+  for (int l = 0; l < n_lev[c]; ++l)
+    for (int idx = lvl[l] + threadIdx.x; idx < lvl[l + 1]; idx += blockDim.x) {
+      row_level[rows[idx]] = l;
+      row_chart[rows[idx]] = (int32_t)c;
+    }
+}
+__global__ void k_level_hist(int64_t n, const int32_t* __restrict__ row_level, int32_t* __restrict__ hist) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&hist[row_level[i]], 1);
+}
+__global__ void k_level_scatter(int64_t n, const int32_t* __restrict__ row_level, int32_t* __restrict__ cursor,
+                                int32_t* __restrict__ grows) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) grows[atomicAdd(&cursor[row_level[i]], 1)] = (int32_t)i;
+}
+
+// One global level: out[i] = (in[i] - sum v[e] out[col[e]]) / v[diagonal] for its rows.
+template <class S, int NR>
+__global__ void k_level_rows(const int32_t* __restrict__ lrows, int32_t count, const int32_t* __restrict__ row_chart,
+                             const int32_t* __restrict__ done, const int64_t* __restrict__ ptr,
+                             const int32_t* __restrict__ col, const S* __restrict__ val, const S* __restrict__ in, S* out) {
+  const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int32_t i = lrows[t];
+  if (done && done[row_chart[i]]) return;
+  const int64_t b = ptr[i], d = ptr[i + 1] - 1;
+  Vec<S, NR> s = ldvec<S, NR>(in, i);
+  for (int64_t e = b; e < d; ++e) {
+    const S a = val[e];
+    const Vec<S, NR> o = ldvec<S, NR>(out, col[e]);
+#pragma unroll
+    for (int k = 0; k < NR; ++k) s.c[k] -= a * o.c[k];
+  }
+  const S dg = val[d];
+#pragma unroll
+  for (int k = 0; k < NR; ++k) s.c[k] /= dg;
+  stvec<S, NR>(out, i, s);
+}
+
 // Colour permutation of the sweep's input / output: out[p] = in[to_orig[p]] (gather) or
 // out[to_orig[p]] = in[p] (scatter).
 template <class S, int NR, bool GATHER>
@@ -363,7 +410,16 @@ struct Factor {
   int32_t *frows = nullptr, *flev = nullptr, *fnl = nullptr;
   int32_t *brows = nullptr, *blev = nullptr, *bnl = nullptr;
   int max_levels = 0;
+  int64_t max_chart_rows = 0;
+  // global levels (when chosen): rows by level, host offsets per level
+  int32_t *fgrows = nullptr, *bgrows = nullptr, *row_chart = nullptr;
+  std::vector<int32_t> foff, boff;
 };
+
+// Few, wide levels run as one launch per level over all charts; otherwise one CTA per chart
+// walks its own levels.
+constexpr int kGlobalMaxLevels = 64;
+constexpr int64_t kGlobalMinRows = 32768;
 
 // Pattern, transpose and both level tables of the IC(0) factor of `sys` (values not yet
 // factored).  Buffers are workspace entries under `tag`.
@@ -421,9 +477,40 @@ Factor factor_pattern(Ctx& ctx, const DevSystem& sys, const std::string& tag, in
     RUV_CUDA(cudaMemcpyAsync(fl.data(), F.fnl, sizeof(int32_t) * NC, cudaMemcpyDeviceToHost, s));
     RUV_CUDA(cudaMemcpyAsync(bl.data(), F.bnl, sizeof(int32_t) * NC, cudaMemcpyDeviceToHost, s));
     RUV_CUDA(cudaStreamSynchronize(s));
-    for (int64_t c = 0; c < NC; ++c) F.max_levels = std::max(F.max_levels, std::max(fl[c], bl[c]));
+    for (int64_t c = 0; c < NC; ++c) {
+      F.max_levels = std::max(F.max_levels, std::max(fl[c], bl[c]));
+      F.max_chart_rows = std::max(F.max_chart_rows, sys.h_chart_row[c + 1] - sys.h_chart_row[c]);
+    }
   }
   RUV_LAUNCH_CHECK();
+  if (F.max_levels > 0 && F.max_levels <= kGlobalMaxLevels && F.max_chart_rows >= kGlobalMinRows) {
+    int32_t* row_level = ws.get<int32_t>(tag + ".rlev", N);
+    int32_t* hist = ws.get<int32_t>(tag + ".hist", F.max_levels);
+    F.row_chart = ws.get<int32_t>(tag + ".rchart", N);
+    F.fgrows = ws.get<int32_t>(tag + ".fgrows", N);
+    F.bgrows = ws.get<int32_t>(tag + ".bgrows", N);
+    const int32_t* rows_of[2] = {F.frows, F.brows};
+    const int32_t* lev_of[2] = {F.flev, F.blev};
+    const int32_t* nl_of[2] = {F.fnl, F.bnl};
+    int32_t* grows_of[2] = {F.fgrows, F.bgrows};
+    std::vector<int32_t>* off_of[2] = {&F.foff, &F.boff};
+    for (int k = 0; k < 2; ++k) {
+      k_row_level<<<(unsigned)NC, kIcThreads, 0, s>>>(sys.chart_row, rows_of[k], lev_of[k], nl_of[k], row_level, F.row_chart);
+      RUV_CUDA(cudaMemsetAsync(hist, 0, sizeof(int32_t) * F.max_levels, s));
+      k_level_hist<<<g, kIcThreads, 0, s>>>(N, row_level, hist);
+      std::vector<int32_t> h(F.max_levels);
+      RUV_CUDA(cudaMemcpyAsync(h.data(), hist, sizeof(int32_t) * F.max_levels, cudaMemcpyDeviceToHost, s));
+      RUV_CUDA(cudaStreamSynchronize(s));
+      std::vector<int32_t>& off = *off_of[k];
+      off.assign(F.max_levels + 1, 0);
+      for (int l = 0; l < F.max_levels; ++l) off[l + 1] = off[l] + h[l];
+      RUV_CUDA(cudaMemcpyAsync(hist, off.data(), sizeof(int32_t) * F.max_levels, cudaMemcpyHostToDevice, s));
+      k_level_scatter<<<g, kIcThreads, 0, s>>>(N, row_level, hist, grows_of[k]);
+      RUV_CUDA(cudaStreamSynchronize(s));  // `off` is the host copy the cursor came from
+      count_launches(3);
+    }
+    RUV_LAUNCH_CHECK();
+  }
   return F;
 }
 
@@ -561,11 +648,34 @@ class Ic0Precond final : public SepPrecond {
       k_permute<S, NR, true><<<g, 256, 0, s>>>(n_, to_orig_, r, rin);
       ++launches;
     }
-    k_sweep<S, NR><<<(unsigned)nc_, kIcThreads, 0, s>>>(chart_row_, done, F_.frows, F_.flev, F_.fnl, F_.lptr, F_.lc, lv, rin,
-                                                         y);
-    k_sweep<S, NR><<<(unsigned)nc_, kIcThreads, 0, s>>>(chart_row_, done, F_.brows, F_.blev, F_.bnl, F_.tptr, F_.tc, tv, y,
-                                                         zout);
-    launches += 2;
+    if (F_.fgrows) {
+      for (int l = 0; l + 1 < (int)F_.foff.size(); ++l) {
+        const int32_t cnt = F_.foff[l + 1] - F_.foff[l];
+        if (cnt == 0) continue;
+        k_level_rows<S, NR><<<div_up(cnt, 256), 256, 0, s>>>(F_.fgrows + F_.foff[l], cnt, F_.row_chart, done, F_.lptr, F_.lc,
+                                                             lv, rin, y);
+        ++launches;
+      }
+      for (int l = 0; l + 1 < (int)F_.boff.size(); ++l) {
+        const int32_t cnt = F_.boff[l + 1] - F_.boff[l];
+        if (cnt == 0) continue;
+        k_level_rows<S, NR><<<div_up(cnt, 256), 256, 0, s>>>(F_.bgrows + F_.boff[l], cnt, F_.row_chart, done, F_.tptr, F_.tc,
+                                                             tv, y, zout);
+        ++launches;
+      }
+    } else if (F_.max_chart_rows >= 65536) {  // a large chart: more rows per round of its CTA
+      k_sweep<S, NR, 1024><<<(unsigned)nc_, 1024, 0, s>>>(chart_row_, done, F_.frows, F_.flev, F_.fnl, F_.lptr, F_.lc, lv,
+                                                            rin, y);
+      k_sweep<S, NR, 1024><<<(unsigned)nc_, 1024, 0, s>>>(chart_row_, done, F_.brows, F_.blev, F_.bnl, F_.tptr, F_.tc, tv,
+                                                            y, zout);
+      launches += 2;
+    } else {
+      k_sweep<S, NR, kIcThreads><<<(unsigned)nc_, kIcThreads, 0, s>>>(chart_row_, done, F_.frows, F_.flev, F_.fnl, F_.lptr,
+                                                                      F_.lc, lv, rin, y);
+      k_sweep<S, NR, kIcThreads><<<(unsigned)nc_, kIcThreads, 0, s>>>(chart_row_, done, F_.brows, F_.blev, F_.bnl, F_.tptr,
+                                                                      F_.tc, tv, y, zout);
+      launches += 2;
+    }
     if (to_orig_) {
       k_permute<S, NR, false><<<g, 256, 0, s>>>(n_, to_orig_, zout, z);
       ++launches;

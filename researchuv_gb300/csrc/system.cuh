@@ -89,10 +89,28 @@ struct DevBatch {
   // produced by assembly
   int64_t* row_of = nullptr;    // n_verts + 1: exclusive count of free vertices (row id if free)
   int32_t* row_vert = nullptr;  // n_rows: packed vertex of each row
-  std::vector<int64_t> h_vert_off;
+  int32_t* tri_g = nullptr;     // 3 * n_tris: packed vertex ids
+  double* cot = nullptr;        // 3 * n_tris: clamped corner cotangents (0 where skipped)
+  int64_t* rec_off = nullptr;   // n_verts + 1: incidence records of each free vertex
+  int2* rec = nullptr;          // (neighbour, corner) sorted per vertex
+  double* coef = nullptr;       // edge coefficient at each neighbour's first record (-1: dropped)
+  std::vector<int64_t> h_vert_off, h_tri_off;
 };
 
 void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix);
+
+// Adjoint of the LSCM solve (adjoint.cu): the batch's vertex-position gradient of a loss
+// given its gradient with respect to the free rows' solution (g, 2 per row): lam = A^-1 g
+// with the same operator and preconditioner, then the assembly's reverse pass.
+void lscm_backward(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x, const double* g, const SolveOpts& o,
+                   double* dp3, std::vector<ChartResult>& res);
+// Per-triangle distortion loss sum_t area_t (s1/s2 - 1)^2 of a UV layout and its gradients
+// (accumulated into duv / dp3 when non-null); loss per chart (host).
+void distortion_loss(Ctx& ctx, const DevBatch& bt, const double* uv, double* duv, double* dp3,
+                     std::vector<double>& loss);
+// chart_distortion (unwrap/src/metrics.rs:73-141) per chart: conformal mean / max, area
+// ratio mean, flips, folds.
+void chart_metrics(Ctx& ctx, const DevBatch& bt, const double* uv, std::vector<double>& out5);
 
 // Damped driver update (unfold_chart's loop, lscm.rs:570-719) on the device: writes uv
 // (2 * n_verts) and per-chart driver iterations / err_accum.

@@ -14,6 +14,11 @@ workloads specify ("f32 positions, f64 assembly").
   radially by 0.1 * N(0,1) of the ring spacing and along the normal by 0.1 * N(0,1) of the
   ring spacing, both noise fields smoothed by 3 Laplacian (neighbour-average) steps.  The
   boundary ring stays on the unit circle.  One chart per disk.
+* :func:`sh_sphere` — an n_lat x n_lon latitude-longitude sphere, radius
+  1 + amp * sum of n_sh seeded random-phase real spherical harmonics of degree <= 6, cut at
+  one meridian (no wrap-around between the last and first longitude) and at both poles (the
+  latitudes stop half a step short of each pole): one disk chart whose border is the cut.
+  (512 x 1024, 8 harmonics, 0.05: the differentiation workload.)
 """
 from __future__ import annotations
 
@@ -129,3 +134,50 @@ def disks(n_charts: int = 4096, t_min: int = 50, t_max: int = 50_000, seed: int 
         tri_off.append(tri_off[-1] + len(faces))
     return (np.asarray(vert_off, np.int64), np.asarray(tri_off, np.int64), np.concatenate(P),
             np.concatenate(F).astype(np.int32))
+
+
+def _assoc_legendre(l: int, m: int, x: np.ndarray) -> np.ndarray:
+    """P_l^m(x) for 0 <= m <= l by the standard upward recurrence in l (no Condon-Shortley
+    phase)."""
+    pmm = np.ones_like(x)
+    if m > 0:
+        s = np.sqrt(np.maximum(0.0, 1.0 - x * x))
+        f = 1.0
+        for _ in range(m):
+            pmm = pmm * f * s
+            f += 2.0
+    if l == m:
+        return pmm
+    pm1 = x * (2 * m + 1) * pmm
+    if l == m + 1:
+        return pm1
+    for ll in range(m + 2, l + 1):
+        pll = ((2 * ll - 1) * x * pm1 - (ll + m - 1) * pmm) / (ll - m)
+        pmm, pm1 = pm1, pll
+    return pm1
+
+
+def sh_sphere(n_lat: int = 512, n_lon: int = 1024, n_sh: int = 8, amp: float = 0.05, seed: int = 4):
+    """Returns (positions (n_lat * n_lon, 3), faces): rows are latitudes from north to south,
+    theta_r = pi (r + 1/2) / n_lat, columns longitudes phi_c = 2 pi c / n_lon.  Each harmonic:
+    degree l ~ U{1..6}, order m ~ U{0..l}, phase ~ U(0, 2 pi), orthonormal scaling
+    sqrt((2l+1)/(4 pi) (l-m)!/(l+m)!) (times sqrt 2 for m > 0)."""
+    from math import factorial, pi, sqrt
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ls = rng.integers(1, 7, n_sh)
+    ms = np.array([rng.integers(0, l + 1) for l in ls])
+    ph = rng.uniform(0.0, 2.0 * np.pi, n_sh)
+    theta = np.pi * (np.arange(n_lat) + 0.5) / n_lat
+    phi = 2.0 * np.pi * np.arange(n_lon) / n_lon
+    T, Ph = np.meshgrid(theta, phi, indexing="ij")
+    ct = np.cos(T)
+    r = np.ones_like(T)
+    for k in range(n_sh):
+        l, m = int(ls[k]), int(ms[k])
+        norm = sqrt((2 * l + 1) / (4 * pi) * factorial(l - m) / factorial(l + m)) * (sqrt(2.0) if m > 0 else 1.0)
+        r += amp * norm * _assoc_legendre(l, m, ct) * np.cos(m * Ph + ph[k])
+    st = np.sin(T)
+    pos = np.stack([(r * st * np.cos(Ph)).ravel(), (r * st * np.sin(Ph)).ravel(), (r * ct).ravel()], 1)
+    return pos.astype(np.float32).astype(np.float64), grid_faces(n_lon, n_lat)
+
