@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="disks4096",
-                    help="disks<N> (N disk charts, the default 4096 is the headline), hf1024, hf2048")
+                    help="disks<N> (N disk charts, the default 4096 is the headline), hf1024, hf2048, "
+                         "sphere<L> (the differentiation workload on an L x 2L sphere; sphere512 at full size)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--precond", default="amg", choices=["jacobi", "amg", "amg_sa", "none"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
@@ -312,12 +313,114 @@ def single_chart_baseline(ctx, vo, unknowns, batched_ms, n_sample):
 
 
 # ------------------------------------------------------------------ GPU arm
+def run_adjoint(args, rank, world, local, pg):
+    """Differentiation workload: an n_lat x 2 n_lat spherical-harmonic sphere cut into one disk
+    chart; a step = forward solve + distortion loss with gradients + backward (adjoint solve
+    and the assembly's reverse pass) through the host-buffer API, giving d(loss)/d(positions)
+    for loss = sum_t area_t (s1/s2 - 1)^2 + lam |uv - target|^2.  Checks the gradient
+    against the CPU LU adjoint at full size and against FP64 central differences (h = 1e-6)
+    on 64 random vertices of a 64 x 128 instance."""
+    import researchuv_gb300 as R
+    from oracle import oracle as O
+    from researchuv_gb300 import workloads as W
+
+    n_lat = int(args.workload[6:])
+    t0 = time.time()
+    p, f = W.sh_sphere(n_lat, 2 * n_lat, seed=4)
+    charts = R.prepare_patches(np.array([0, len(p)]), np.array([0, len(f)]), p, f)
+    ch = charts.chart(0)
+    prep = time.time() - t0
+    n = len(p)
+    rng = np.random.Generator(np.random.PCG64(11))
+    target = ch["p2"] + 0.01 * rng.standard_normal(ch["p2"].shape)
+    lam = 1.0 / n
+    ctx = R.Context(local)
+    prec = R.Precision.MIXED if args.precision == "mixed" else R.Precision.FP64
+    pc = {"jacobi": R.Precond.JACOBI, "amg": R.Precond.AMG, "amg_sa": R.Precond.AMG_SA,
+          "none": R.Precond.NONE}[args.precond]
+    opts = R.UnfoldOptions(precision=prec, precond=pc)
+    batch = charts.batch()
+
+    def step():
+        uv, st = R.lscm_forward(ctx, batch, opts, n)
+        loss, duv, dp_dist = R.distortion_loss(ctx, uv, 1)
+        dp_solve, st_b = R.lscm_backward(ctx, duv + 2.0 * lam * (uv - target), opts, 1)
+        total = float(loss[0]) + lam * float(((uv - target) ** 2).sum())
+        return dp_dist + dp_solve, total, st[0], st_b[0]
+
+    for _ in range(max(args.warmup, 1)):
+        grad, total, st_f, st_b = step()
+    L = R.lib()
+    l0 = L.ruv_kernel_launches(ctx.h)
+    clk = Clocks(local)
+    barrier(pg)
+    clk.start()
+    times = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        grad, total, st_f, st_b = step()
+        times.append(1000.0 * (time.perf_counter() - t1))
+    barrier(pg)
+    clock_info = clk.stop()
+    launches = (L.ruv_kernel_launches(ctx.h) - l0) // max(args.steps, 1)
+    ms = allmax(pg, statistics.mean(times))
+    unknowns = int(2 * st_f.n_free)
+    line = {
+        "metric": "LSCM adjoint d(loss)/d(positions): unknowns/s (forward + loss + backward)",
+        "value": world * unknowns / (ms / 1000.0), "unit": "unknowns/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 loss/adjoint, " + args.precision + " solves",
+        "data": "synthetic",
+        "config": {"workload": f"{n_lat}x{2 * n_lat} sphere, radius 1 + 0.05 * 8 seeded real harmonics "
+                               f"(degree <= 6), cut at one meridian and both poles, seed 4",
+                   "vertices": n, "triangles": int(len(f)), "unknowns": unknowns, "host_prep_s": round(prep, 3),
+                   "precond": args.precond, "precision": args.precision, "lam": lam,
+                   "forward_cg_iters": int(st_f.cg_iters), "adjoint_cg_iters": int(st_b.cg_iters),
+                   "timing": "wall clock of the host-buffer calls (H2D/D2H inside)"},
+        "e2e": {"value": world * unknowns / (ms / 1000.0), "unit": "unknowns/s",
+                "h2d_bytes_per_step": int(8 * (3 * n + 2 * n + 2 * n + 2 * n) + 12 * len(f) + n),
+                "d2h_bytes_per_step": int(8 * (2 * n + 2 * n + 3 * n + 3 * n)), "ms_per_step": ms},
+        "gpu_launches": int(launches), "clocks": clock_info, "loss": total,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        t1 = time.time()
+        ref, _ = O.lu_adjoint_gradient(p, ch["tris"], ch["pinned"].astype(np.int64), ch["pin_uv"], lam, target)
+        cpu_s = time.time() - t1
+        line["cpu_baseline"] = {"value": unknowns / cpu_s, "unit": "unknowns/s", "cores": 1, "kind": "port",
+                                "sample": "the whole workload once: oracle fixed-pin assembly, SuperLU factor, "
+                                          "forward + adjoint solves, reverse pass (FP64)"}
+        line["grad_rel_err_vs_lu_adjoint"] = float(np.linalg.norm(grad - ref) / np.linalg.norm(ref))
+        # central differences on a smaller instance of the same family
+        p2, f2 = W.sh_sphere(64, 128, seed=4)
+        C2 = R.prepare_patches(np.array([0, len(p2)]), np.array([0, len(f2)]), p2, f2)
+        c2 = C2.chart(0)
+        tg2 = c2["p2"] + 0.01 * rng.standard_normal(c2["p2"].shape)
+        lam2 = 1.0 / len(p2)
+        uv2, _ = R.lscm_forward(ctx, C2.batch(), opts, len(p2))
+        _, duv2, dpd2 = R.distortion_loss(ctx, uv2, 1)
+        dps2, _ = R.lscm_backward(ctx, duv2 + 2.0 * lam2 * (uv2 - tg2), opts, 1)
+        g2 = dpd2 + dps2
+        picks = [(int(v), k) for v in np.random.Generator(np.random.PCG64(5)).choice(len(p2), 64, replace=False)
+                 for k in range(3)]
+        fd = O.fd_gradient(p2, c2["tris"], c2["pinned"].astype(np.int64), c2["pin_uv"], lam2, tg2, picks, h=1e-6)
+        ad = np.array([g2[v, k] for v, k in picks])
+        line["fd_check"] = {"instance": "64x128 sphere of the same family", "picks": len(picks), "h": 1e-6,
+                            "rel_err_norm": float(np.linalg.norm(ad - fd) / np.linalg.norm(fd)),
+                            "max_abs_err_over_max_abs": float(np.abs(ad - fd).max() / np.abs(fd).max())}
+    if rank == 0:
+        print(json.dumps(line))
+    barrier(pg)
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist()
     if args.impl == "reference":
         run_reference(args, rank)
         barrier(pg)
+        return
+    if args.workload.startswith("sphere"):
+        run_adjoint(args, rank, world, local, pg)
         return
     import ctypes
 

@@ -5,9 +5,10 @@
 // contiguous, so aggregates never cross charts).  Per level and for every chart that is
 // still coarsening:
 //   * aggregation: two rounds of pairwise matching on |A| (each unmatched row proposes to
-//     its strongest unmatched neighbour, ties to the smaller index; mutual proposals pair
-//     up), first on rows, then on the pairs -> aggregates of <= 4 rows (the reference's
-//     size-4 target, amg.rs:245, with a parallel matching in place of its sequential scan);
+//     one of its strongly coupled unmatched neighbours, picked by a symmetric pseudo-random
+//     pair priority; mutual proposals pair up), first on rows, then on the pairs ->
+//     aggregates of about 4 rows (the reference's size-4 target, amg.rs:245, with a parallel
+//     matching in place of its sequential scan);
 //   * prolongator: tentative (one 1 per row, Precond::Amg) or smoothed
 //     P = (I - omega D^-1 A) P_tent, omega = 2/3 (Precond::AmgSa, amg.rs:299-362);
 //   * Galerkin operator A_c = R (A P), R = P^T (amg.rs:384-429), each product row formed by
@@ -98,21 +99,42 @@ __global__ void k_row_chart(int64_t n, const int64_t* __restrict__ chart_row, in
   active[i] = cont[c] ? 1 : 0;
 }
 
-// Pairwise matching, proposal: strongest unmatched neighbour (|a_ij|, ties to smaller j).
+// Symmetric pseudo-random priority of the pair {i, j} (a 64-bit mix of the ordered pair).
+__device__ __forceinline__ uint32_t pair_priority(int32_t i, int32_t j) {
+  uint64_t x = ((uint64_t)(uint32_t)min(i, j) << 32) | (uint32_t)max(i, j);
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return (uint32_t)x;
+}
+
+// Pairwise matching, proposal: among the unmatched neighbours coupled at least kStrong times
+// as strongly as the strongest one, the one of highest pair priority (ties to the smaller j).
+// Choosing by a symmetric random priority rather than by the coupling itself makes mutual
+// proposals likely even where couplings vary monotonically along a row of the mesh (a
+// weight-ordered handshake then chains i -> i-1 -> i-2 ... and pairs almost nothing).
+constexpr float kStrong = 0.85f;
 __global__ void k_propose(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                           const float* __restrict__ vals, const uint8_t* __restrict__ active,
-                          const int32_t* __restrict__ mate, int32_t* __restrict__ prop) {
+                          const int32_t* __restrict__ mate, int32_t* __restrict__ prop, float strong) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int32_t best = -1;
   if (active[i] && mate[i] < 0) {
-    float bs = -1.0f;
+    float mx = 0.0f;
     for (int e = rp[i]; e < rp[i + 1]; ++e) {
-      int32_t j = cols[e];
-      if (j == i || mate[j] >= 0) continue;
-      float s = fabsf(vals[e]);
-      if (s > bs || (s == bs && j < best)) {
-        bs = s;
+      const int32_t j = cols[e];
+      if (j != i && mate[j] < 0) mx = fmaxf(mx, fabsf(vals[e]));
+    }
+    uint32_t bp = 0;
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+      const int32_t j = cols[e];
+      if (j == i || mate[j] >= 0 || !(fabsf(vals[e]) >= strong * mx) || mx == 0.0f) continue;
+      const uint32_t pr = pair_priority((int32_t)i, j);
+      if (best < 0 || pr > bp || (pr == bp && j < best)) {
+        bp = pr;
         best = j;
       }
     }
@@ -210,11 +232,11 @@ __device__ __forceinline__ void group_strengths(int64_t g, const int64_t* goff, 
   }
 }
 
-// Second matching level, on groups: propose to the strongest unmatched neighbour group.
+// Second matching level, on groups: propose to a strongly coupled unmatched neighbour group.
 __global__ void k_propose2(int64_t ng, const int64_t* __restrict__ goff, const int32_t* __restrict__ mem,
                            const int32_t* __restrict__ rp, const int32_t* __restrict__ cols, const float* __restrict__ vals,
                            const int32_t* __restrict__ grp_of, const int32_t* __restrict__ gmate,
-                           int32_t* __restrict__ prop, int* __restrict__ stats) {
+                           int32_t* __restrict__ prop, int* __restrict__ stats, float strong) {
   int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ng) return;
   int32_t best = -1;
@@ -222,12 +244,17 @@ __global__ void k_propose2(int64_t ng, const int64_t* __restrict__ goff, const i
     Acc<kAccCap> acc;
     group_strengths(g, goff, mem, rp, cols, vals, grp_of, acc, [&](int32_t h) { return gmate[h] < 0; });
     atomicMax(stats + 2, acc.n);
-    float bs = -1.0f;
-    for (int t = 0; t < acc.n; ++t)
-      if (acc.val[t] > bs || (acc.val[t] == bs && acc.key[t] < best)) {
-        bs = acc.val[t];
+    float mx = 0.0f;
+    for (int t = 0; t < acc.n; ++t) mx = fmaxf(mx, acc.val[t]);
+    uint32_t bp = 0;
+    for (int t = 0; t < acc.n; ++t) {  // as k_propose, on groups
+      if (!(acc.val[t] >= strong * mx) || mx == 0.0f) continue;
+      const uint32_t pr = pair_priority((int32_t)g, acc.key[t]);
+      if (best < 0 || pr > bp || (pr == bp && acc.key[t] < best)) {
+        bp = pr;
         best = acc.key[t];
       }
+    }
   }
   prop[g] = best;
 }
@@ -369,7 +396,7 @@ __global__ void k_ap(int64_t n, const uint8_t* __restrict__ active, const int32_
                      const int32_t* __restrict__ cols, const float* __restrict__ vals, const int64_t* __restrict__ poff,
                      const int32_t* __restrict__ pc, const float* __restrict__ pv, int32_t* __restrict__ cnt,
                      const int64_t* __restrict__ woff, int32_t* __restrict__ wc, float* __restrict__ wv,
-                     int* __restrict__ overflow) {
+                     int* __restrict__ overflow, int32_t* __restrict__ big, int32_t* __restrict__ big_n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (!active[i]) {
@@ -382,8 +409,14 @@ __global__ void k_ap(int64_t n, const uint8_t* __restrict__ active, const int32_
     const float a = vals[e];
     for (int64_t q = poff[j]; q < poff[j + 1]; ++q) acc.add(pc[q], a * pv[q]);
   }
-  if (acc.overflow) atomicExch(overflow, 1);
   atomicMax(overflow + 4, acc.n);
+  if (acc.overflow) {  // handed to k_gal_big (listed once, in the counting pass)
+    if (MODE == 0) {
+      cnt[i] = 0;
+      big[atomicAdd(big_n, 1)] = (int32_t)i;
+    }
+    return;
+  }
   acc.sort();
   if (MODE == 0) {
     cnt[i] = acc.n;
@@ -402,7 +435,7 @@ __global__ void k_rw(int64_t nc, const int64_t* __restrict__ roff, const int32_t
                      const float* __restrict__ rv, const int64_t* __restrict__ woff, const int32_t* __restrict__ wc,
                      const float* __restrict__ wv, int32_t* __restrict__ cnt, const int64_t* __restrict__ aoff,
                      int32_t* __restrict__ ac, float* __restrict__ av, float* __restrict__ adinv,
-                     int* __restrict__ overflow) {
+                     int* __restrict__ overflow, int32_t* __restrict__ big, int32_t* __restrict__ big_n) {
   int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= nc) return;
   Acc<kGalCap> acc;
@@ -411,8 +444,14 @@ __global__ void k_rw(int64_t nc, const int64_t* __restrict__ roff, const int32_t
     const float r = rv[q];
     for (int64_t e = woff[i]; e < woff[i + 1]; ++e) acc.add(wc[e], r * wv[e]);
   }
-  if (acc.overflow) atomicExch(overflow, 1);
   atomicMax(overflow + 5, acc.n);
+  if (acc.overflow) {
+    if (MODE == 0) {
+      cnt[I] = 0;
+      big[atomicAdd(big_n, 1)] = (int32_t)I;
+    }
+    return;
+  }
   acc.sort();
   if (MODE == 0) {
     cnt[I] = acc.n;
@@ -426,6 +465,69 @@ __global__ void k_rw(int64_t nc, const int64_t* __restrict__ roff, const int32_t
     }
     adinv[I] = d > 0.0f ? 1.0f / d : 0.0f;
   }
+}
+
+// Product rows with more than kGalCap distinct keys (a large aggregate, a dense row): one CTA
+// per listed row; its first thread accumulates into a key-sorted list in shared memory, each
+// key's contributions summed in the same arrival order as Acc, so the row equals what an
+// unbounded Acc would give.  A row above kBigCap keys sets overflow[0].  RW = 0: row i of
+// W = A P (outer: A's row, inner: P's rows); RW = 1: row I of R W (outer: R's row, inner: W's).
+constexpr int kBigCap = 4096;
+template <int MODE, int RW>
+__global__ void __launch_bounds__(32) k_gal_big(const int32_t* __restrict__ list, const int64_t* __restrict__ o_ptr64,
+                                                const int32_t* __restrict__ o_ptr32, const int32_t* __restrict__ o_idx,
+                                                const float* __restrict__ o_val, const int64_t* __restrict__ i_ptr,
+                                                const int32_t* __restrict__ i_idx, const float* __restrict__ i_val,
+                                                int32_t* __restrict__ cnt, const int64_t* __restrict__ off,
+                                                int32_t* __restrict__ oc, float* __restrict__ ov, float* __restrict__ adinv,
+                                                int* __restrict__ overflow) {
+  __shared__ int32_t key[kBigCap];
+  __shared__ float val[kBigCap];
+  if (threadIdx.x != 0) return;
+  const int32_t row = list[blockIdx.x];
+  const int64_t b = o_ptr64 ? o_ptr64[row] : (int64_t)o_ptr32[row];
+  const int64_t e_ = o_ptr64 ? o_ptr64[row + 1] : (int64_t)o_ptr32[row + 1];
+  int n = 0;
+  for (int64_t q = b; q < e_; ++q) {
+    const int32_t j = o_idx[q];
+    const float a = o_val[q];
+    for (int64_t r = i_ptr[j]; r < i_ptr[j + 1]; ++r) {
+      const int32_t k = i_idx[r];
+      const float v = a * i_val[r];
+      int lo = 0, hi = n;  // first position with key >= k
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (key[mid] < k) lo = mid + 1; else hi = mid;
+      }
+      if (lo < n && key[lo] == k) {
+        val[lo] += v;
+      } else if (n < kBigCap) {
+        for (int t = n; t > lo; --t) {
+          key[t] = key[t - 1];
+          val[t] = val[t - 1];
+        }
+        key[lo] = k;
+        val[lo] = v;
+        ++n;
+      } else {
+        atomicExch(overflow, 1);
+        if (MODE == 0) cnt[row] = 0;
+        return;
+      }
+    }
+  }
+  if (MODE == 0) {
+    cnt[row] = n;
+    return;
+  }
+  const int64_t at = off[row];
+  float d = 0.0f;
+  for (int t = 0; t < n; ++t) {
+    oc[at + t] = key[t];
+    ov[at + t] = val[t];
+    if (RW && key[t] == row) d = val[t];
+  }
+  if (RW) adinv[row] = d > 0.0f ? 1.0f / d : 0.0f;
 }
 
 __global__ void k_i64_i32(int64_t n, const int64_t* __restrict__ a, int32_t* __restrict__ b) {
@@ -817,6 +919,8 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   H->n_charts = NC;
   H->alpha_c = smooth ? 1.0f : 1.5f;  // over-correct the piecewise-constant coarse space
   if (const char* e = std::getenv("RUV_AMG_ALPHA")) H->alpha_c = (float)std::atof(e);
+  float strong = kStrong;  // matching candidates: couplings >= strong * the row's strongest
+  if (const char* e = std::getenv("RUV_AMG_STRONG")) strong = (float)std::atof(e);
   cudaEvent_t t_setup0;
   RUV_CUDA(cudaEventCreate(&t_setup0));
   RUV_CUDA(cudaEventRecord(t_setup0, s));
@@ -880,7 +984,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     int32_t* prop = ctx.ws.get<int32_t>(tag + ".prop", L.n);
     RUV_CUDA(cudaMemsetAsync(mate, 0xff, sizeof(int32_t) * L.n, s));
     for (int r = 0; r < kPairRounds; ++r) {
-      k_propose<<<div_up(L.n, B), B, 0, s>>>(L.n, L.rp, L.cols, L.vals, active, mate, prop);
+      k_propose<<<div_up(L.n, B), B, 0, s>>>(L.n, L.rp, L.cols, L.vals, active, mate, prop, strong);
       k_accept<<<div_up(L.n, B), B, 0, s>>>(L.n, prop, mate);
       count_launches(2);
     }
@@ -912,7 +1016,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
       k_sort_members<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem);
       count_launches(1);
       for (int r = 0; r < kPairRounds; ++r) {
-        k_propose2<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, L.cols, L.vals, grp_of, gmate, gprop, ovf);
+        k_propose2<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, L.cols, L.vals, grp_of, gmate, gprop, ovf, strong);
         k_accept<<<div_up(NG, B), B, 0, s>>>(NG, gprop, gmate);
         count_launches(2);
       }
@@ -969,20 +1073,49 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     // ---- W = A P, then A_c = R W
     int32_t* wcnt = ctx.ws.get<int32_t>(tag + ".wcnt", L.n);
     int64_t* woff = ctx.ws.get<int64_t>(tag + ".woff", L.n + 1);
+    int32_t* big = ctx.ws.get<int32_t>("amg.big", std::max<int64_t>(std::max<int64_t>(L.n, NA), 1));
+    int32_t* big_n = ovf + 6;
+    auto n_big = [&]() {
+      int32_t h = 0;
+      RUV_CUDA(cudaMemcpyAsync(&h, big_n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+      RUV_CUDA(cudaStreamSynchronize(s));
+      return h;
+    };
+    RUV_CUDA(cudaMemsetAsync(big_n, 0, sizeof(int32_t), s));
     k_ap<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, nullptr, nullptr,
-                                         nullptr, ovf);
+                                         nullptr, ovf, big, big_n);
     count_launches(1);
+    const int32_t wbig = n_big();
+    if (wbig > 0) {
+      k_gal_big<0, 0><<<(unsigned)wbig, 32, 0, s>>>(big, nullptr, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, nullptr,
+                                                    nullptr, nullptr, nullptr, ovf);
+      count_launches(1);
+    }
     const int64_t WN = offsets_from_counts(ctx, wcnt, L.n, woff, tag + ".wo");
     int32_t* wc = ctx.ws.get<int32_t>(tag + ".wc", WN);
     float* wv = ctx.ws.get<float>(tag + ".wv", WN);
-    k_ap<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, woff, wc, wv, ovf);
+    k_ap<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, woff, wc, wv, ovf,
+                                         big, big_n);
     count_launches(1);
+    if (wbig > 0) {
+      k_gal_big<1, 0><<<(unsigned)wbig, 32, 0, s>>>(big, nullptr, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, woff,
+                                                    wc, wv, nullptr, ovf);
+      count_launches(1);
+    }
     int32_t* acnt = ctx.ws.get<int32_t>(ntag + ".acnt", NA);
     int64_t* aoff = ctx.ws.get<int64_t>(ntag + ".aoff", NA + 1);
+    int32_t abig = 0;
     if (NA > 0) {
+      RUV_CUDA(cudaMemsetAsync(big_n, 0, sizeof(int32_t), s));
       k_rw<0><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv, woff, wc, wv, acnt, nullptr, nullptr, nullptr, nullptr,
-                                          ovf);
+                                          ovf, big, big_n);
       count_launches(1);
+      abig = n_big();
+      if (abig > 0) {
+        k_gal_big<0, 1><<<(unsigned)abig, 32, 0, s>>>(big, L.roff, nullptr, L.rc, L.rv, woff, wc, wv, acnt, nullptr,
+                                                      nullptr, nullptr, nullptr, ovf);
+        count_launches(1);
+      }
     }
     const int64_t AN = offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao");
     if (AN >= (int64_t)INT32_MAX) throw Error{RUV_ERR_BAD_INPUT, "coarse operator too large"};
@@ -992,7 +1125,13 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     C.dinv = ctx.ws.get<float>(ntag + ".dinv", NA);
     C.nnz = AN;
     if (NA > 0) {
-      k_rw<1><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv, woff, wc, wv, acnt, aoff, C.cols, C.vals, C.dinv, ovf);
+      k_rw<1><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv, woff, wc, wv, acnt, aoff, C.cols, C.vals, C.dinv, ovf,
+                                          big, big_n);
+      if (abig > 0) {
+        k_gal_big<1, 1><<<(unsigned)abig, 32, 0, s>>>(big, L.roff, nullptr, L.rc, L.rv, woff, wc, wv, acnt, aoff, C.cols,
+                                                      C.vals, C.dinv, ovf);
+        count_launches(1);
+      }
       k_i64_i32<<<div_up(NA + 1, B), B, 0, s>>>(NA + 1, aoff, C.rp);
       count_launches(2);
     }
@@ -1015,7 +1154,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   int h_ovf[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   RUV_CUDA(cudaMemcpyAsync(h_ovf, ovf, sizeof(h_ovf), cudaMemcpyDeviceToHost, s));
   RUV_CUDA(cudaStreamSynchronize(s));
-  if (h_ovf[0]) throw Error{RUV_ERR_INTERNAL, "AMG setup: a product row exceeded its accumulation bound"};
+  if (h_ovf[0]) throw Error{RUV_ERR_INTERNAL, "AMG setup: a product row exceeded 4096 distinct columns"};
   // ---- per-level vectors, tile tables, pointer tables, dense factors
   const int NR = sys.nrhs;
   const int K = (int)H->lv.size();
