@@ -1203,7 +1203,7 @@ FixedSystem fixed_system(Bag* bg) {
   return S;
 }
 
-// The distortion term of one triangle as metrics.rs:95-128 forms it: 0.5 |n| (s1/s2 - 1)^2.
+// The distortion term of one triangle with the F of metrics.rs:95-128: 0.5 |n| (s1/s2 - 1)^2.
 template <class T>
 bool tri_distortion_cpu(const T (&p)[9], const T (&u)[6], T& out) {
   T e1x = p[3] - p[0], e1y = p[4] - p[1], e1z = p[5] - p[2];
@@ -1223,10 +1223,13 @@ bool tri_distortion_cpu(const T (&p)[9], const T (&u)[6], T& out) {
   T d1u = u[2] - u[0], d1v = u[3] - u[1], d2u = u[4] - u[0], d2v = u[5] - u[1];
   T f00 = d1u * i00 + d2u * i10, f01 = d1u * i01 + d2u * i11;
   T f10 = d1v * i00 + d2v * i10, f11 = d1v * i01 + d2v * i11;
-  T a = f00 * f00 + f10 * f10, bq = f00 * f01 + f10 * f11, c = f01 * f01 + f11 * f11;
-  T tr = a + c, dd = T(0.5) * (a - c);
-  T disc = dnsqrt(dnmax(dd * dd + bq * bq, 0.0));
-  T s1 = dnsqrt(dnmax(T(0.5) * tr + disc, 0.0)), s2 = dnsqrt(dnmax(T(0.5) * tr - disc, 0.0));
+  // singular values without svd2's 0.5 tr - disc cancellation: s1 = (|(f00 + f11, f10 - f01)|
+  // + |(f00 - f11, f10 + f01)|) / 2, s2 = |det F| / s1
+  T p0 = f00 + f11, p1 = f10 - f01, q0 = f00 - f11, q1 = f10 + f01;
+  T s1 = T(0.5) * (dnsqrt(p0 * p0 + p1 * p1) + dnsqrt(q0 * q0 + q1 * q1));
+  T dF = f00 * f11 - f01 * f10;
+  if (dF.v < 0.0) dF = -dF;
+  T s2 = s1.v > 0.0 ? dF / s1 : T(0.0);
   T r = s1 / dnmax(s2, 1e-30) - T(1.0);
   out = T(0.5) * ln * r * r;
   return true;

@@ -385,7 +385,7 @@ def lu_adjoint_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target):
     return dp_dist + ch.adjoint_positions(x, lam), uv
 
 
-def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float = 1e-6):
+def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float = 1e-6, refine: int = 0):
     """Central differences of config4_loss with respect to p3[v, k] for (v, k) in picks,
     through the fixed-pin solve.  The perturbed solution is formed as x + dx with
     A' dx = (b' - b) - (A' - A) x (a right-hand side that is exactly zero away from v), and
@@ -404,10 +404,15 @@ def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float
             q = p3.copy()
             q[v, k] += sgn * h
             ch = FixedPinChart(q, tris, pinned, pin_uv)
-            assert np.array_equal(ch.A.indptr, base.A.indptr) and np.array_equal(ch.A.indices, base.A.indices)
-            dA = ch.A.copy()
-            dA.data = ch.A.data - base.A.data
-            dx = ch.solve((ch.b - base.b) - dA @ x)
+            if np.array_equal(ch.A.indptr, base.A.indptr) and np.array_equal(ch.A.indices, base.A.indices):
+                dA = ch.A.copy()
+                dA.data = ch.A.data - base.A.data
+                rhs = (ch.b - base.b) - dA @ x
+                dx = ch.solve(rhs)
+                for _ in range(refine):  # iterative refinement of the small correction
+                    dx = dx + ch.solve(rhs - ch.A @ dx)
+            else:  # an edge weight crossed the drop threshold (a clamped cotangent at 0)
+                dx = ch.solve() - x
             uv2 = uv.copy()
             uv2[free] = uv[free] + dx[base.row_of[free]]
             _, _, _, lt2 = ch.distortion(uv2)

@@ -16,7 +16,7 @@
 // Position gradients are accumulated with FP64 atomics.
 //
 // The distortion loss sum_t area_t (s1/s2 - 1)^2 (area_t the 3-D area, s1 >= s2 the
-// singular values of the UV Jacobian F = U P^-1 of metrics.rs:95-128) is differentiated per
+// singular values of the UV Jacobian F = U P^-1 of metrics.rs:95-128, formed stably) is differentiated per
 // triangle by forward-mode dual numbers (three seeds per pass, five passes for the 15
 // coordinates of a triangle), FP64.  Triangles whose three vertices are all pinned are left
 // out of the loss: their UVs are set by the pin rule, not by the solve, and the rule can
@@ -131,13 +131,14 @@ __device__ __forceinline__ bool tri_distortion(const T (&p)[9], const T (&u)[6],
   const T d1u = u[2] - u[0], d1v = u[3] - u[1], d2u = u[4] - u[0], d2v = u[5] - u[1];
   const T f00 = d1u * i00 + d2u * i10, f01 = d1u * i01 + d2u * i11;
   const T f10 = d1v * i00 + d2v * i10, f11 = d1v * i01 + d2v * i11;
-  // svd2 (metrics.rs:59-70)
-  const T a = f00 * f00 + f10 * f10, b = f00 * f01 + f10 * f11, c = f01 * f01 + f11 * f11;
-  const T tr = a + c, dd = 0.5 * (a - c);
-  const T disc = dsqrt(dmax(dd * dd + b * b, 0.0));
-  const T lam1 = 0.5 * tr + disc;
-  const T lam2 = dmax(0.5 * tr - disc, 0.0);
-  const T s1 = dsqrt(dmax(lam1, 0.0)), s2 = dsqrt(lam2);
+  // singular values of F: s1 = (|(f00 + f11, f10 - f01)| + |(f00 - f11, f10 + f01)|) / 2 and
+  // s2 = |det F| / s1 -- the same values as svd2 (metrics.rs:59-70), formed without its
+  // 0.5 tr - disc cancellation, which loses (s1/s2)^2 ulps on anisotropic triangles
+  const T p0 = f00 + f11, p1 = f10 - f01, q0 = f00 - f11, q1 = f10 + f01;
+  const T s1 = 0.5 * (dsqrt(p0 * p0 + p1 * p1) + dsqrt(q0 * q0 + q1 * q1));
+  T dF = f00 * f11 - f01 * f10;
+  if (dF.v < 0.0) dF = -dF;
+  const T s2 = s1.v > 0.0 ? dF / s1 : cst<3>(0.0);
   const T r = s1 / dmax(s2, 1e-30) - cst<3>(1.0);
   out = 0.5 * (ln * (r * r));
   return true;

@@ -51,13 +51,13 @@ __device__ __forceinline__ int64_t find_chart64(const int64_t* off, int64_t n_ch
 }
 
 // Bounded accumulation of (key, value) products in arrival order; keys sorted at the end.
-template <int CAP>
+template <int CAP, class T = float>
 struct Acc {
   int key[CAP];
-  float val[CAP];
+  T val[CAP];
   int n = 0;
   bool overflow = false;
-  __device__ __forceinline__ void add(int k, float v) {
+  __device__ __forceinline__ void add(int k, T v) {
     for (int t = 0; t < n; ++t)
       if (key[t] == k) {
         val[t] += v;
@@ -74,7 +74,7 @@ struct Acc {
   __device__ __forceinline__ void sort() {
     for (int i = 1; i < n; ++i) {
       int k = key[i];
-      float v = val[i];
+      T v = val[i];
       int j = i - 1;
       while (j >= 0 && key[j] > k) {
         key[j + 1] = key[j];
@@ -393,9 +393,9 @@ __global__ void k_sort_rows(int64_t n, const int64_t* __restrict__ off, int32_t*
 // W = A P (rows of active fine rows).  MODE 0 count / 1 fill.
 template <int MODE>
 __global__ void k_ap(int64_t n, const uint8_t* __restrict__ active, const int32_t* __restrict__ rp,
-                     const int32_t* __restrict__ cols, const float* __restrict__ vals, const int64_t* __restrict__ poff,
+                     const int32_t* __restrict__ cols, const double* __restrict__ vals, const int64_t* __restrict__ poff,
                      const int32_t* __restrict__ pc, const float* __restrict__ pv, int32_t* __restrict__ cnt,
-                     const int64_t* __restrict__ woff, int32_t* __restrict__ wc, float* __restrict__ wv,
+                     const int64_t* __restrict__ woff, int32_t* __restrict__ wc, double* __restrict__ wv,
                      int* __restrict__ overflow, int32_t* __restrict__ big, int32_t* __restrict__ big_n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -403,11 +403,11 @@ __global__ void k_ap(int64_t n, const uint8_t* __restrict__ active, const int32_
     if (MODE == 0) cnt[i] = 0;
     return;
   }
-  Acc<kGalCap> acc;
+  Acc<kGalCap, double> acc;
   for (int e = rp[i]; e < rp[i + 1]; ++e) {
     const int32_t j = cols[e];
-    const float a = vals[e];
-    for (int64_t q = poff[j]; q < poff[j + 1]; ++q) acc.add(pc[q], a * pv[q]);
+    const double a = vals[e];
+    for (int64_t q = poff[j]; q < poff[j + 1]; ++q) acc.add(pc[q], a * (double)pv[q]);
   }
   atomicMax(overflow + 4, acc.n);
   if (acc.overflow) {  // handed to k_gal_big (listed once, in the counting pass)
@@ -433,15 +433,15 @@ __global__ void k_ap(int64_t n, const uint8_t* __restrict__ active, const int32_
 template <int MODE>
 __global__ void k_rw(int64_t nc, const int64_t* __restrict__ roff, const int32_t* __restrict__ rc,
                      const float* __restrict__ rv, const int64_t* __restrict__ woff, const int32_t* __restrict__ wc,
-                     const float* __restrict__ wv, int32_t* __restrict__ cnt, const int64_t* __restrict__ aoff,
-                     int32_t* __restrict__ ac, float* __restrict__ av, float* __restrict__ adinv,
+                     const double* __restrict__ wv, int32_t* __restrict__ cnt, const int64_t* __restrict__ aoff,
+                     int32_t* __restrict__ ac, double* __restrict__ av, float* __restrict__ adinv,
                      int* __restrict__ overflow, int32_t* __restrict__ big, int32_t* __restrict__ big_n) {
   int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= nc) return;
-  Acc<kGalCap> acc;
+  Acc<kGalCap, double> acc;
   for (int64_t q = roff[I]; q < roff[I + 1]; ++q) {
     const int32_t i = rc[q];
-    const float r = rv[q];
+    const double r = rv[q];
     for (int64_t e = woff[i]; e < woff[i + 1]; ++e) acc.add(wc[e], r * wv[e]);
   }
   atomicMax(overflow + 5, acc.n);
@@ -457,13 +457,13 @@ __global__ void k_rw(int64_t nc, const int64_t* __restrict__ roff, const int32_t
     cnt[I] = acc.n;
   } else {
     int64_t at = aoff[I];
-    float d = 0.0f;
+    double d = 0.0;
     for (int t = 0; t < acc.n; ++t) {
       ac[at + t] = acc.key[t];
       av[at + t] = acc.val[t];
       if (acc.key[t] == (int32_t)I) d = acc.val[t];
     }
-    adinv[I] = d > 0.0f ? 1.0f / d : 0.0f;
+    adinv[I] = d > 0.0 ? (float)(1.0 / d) : 0.0f;
   }
 }
 
@@ -472,17 +472,17 @@ __global__ void k_rw(int64_t nc, const int64_t* __restrict__ roff, const int32_t
 // key's contributions summed in the same arrival order as Acc, so the row equals what an
 // unbounded Acc would give.  A row above kBigCap keys sets overflow[0].  RW = 0: row i of
 // W = A P (outer: A's row, inner: P's rows); RW = 1: row I of R W (outer: R's row, inner: W's).
-constexpr int kBigCap = 4096;
-template <int MODE, int RW>
+constexpr int kBigCap = 3072;  // keys + FP64 values: 36 KB of shared memory
+template <int MODE, int RW, class OV, class IV>
 __global__ void __launch_bounds__(32) k_gal_big(const int32_t* __restrict__ list, const int64_t* __restrict__ o_ptr64,
                                                 const int32_t* __restrict__ o_ptr32, const int32_t* __restrict__ o_idx,
-                                                const float* __restrict__ o_val, const int64_t* __restrict__ i_ptr,
-                                                const int32_t* __restrict__ i_idx, const float* __restrict__ i_val,
+                                                const OV* __restrict__ o_val, const int64_t* __restrict__ i_ptr,
+                                                const int32_t* __restrict__ i_idx, const IV* __restrict__ i_val,
                                                 int32_t* __restrict__ cnt, const int64_t* __restrict__ off,
-                                                int32_t* __restrict__ oc, float* __restrict__ ov, float* __restrict__ adinv,
+                                                int32_t* __restrict__ oc, double* __restrict__ ov, float* __restrict__ adinv,
                                                 int* __restrict__ overflow) {
   __shared__ int32_t key[kBigCap];
-  __shared__ float val[kBigCap];
+  __shared__ double val[kBigCap];
   if (threadIdx.x != 0) return;
   const int32_t row = list[blockIdx.x];
   const int64_t b = o_ptr64 ? o_ptr64[row] : (int64_t)o_ptr32[row];
@@ -490,10 +490,10 @@ __global__ void __launch_bounds__(32) k_gal_big(const int32_t* __restrict__ list
   int n = 0;
   for (int64_t q = b; q < e_; ++q) {
     const int32_t j = o_idx[q];
-    const float a = o_val[q];
+    const double a = (double)o_val[q];
     for (int64_t r = i_ptr[j]; r < i_ptr[j + 1]; ++r) {
       const int32_t k = i_idx[r];
-      const float v = a * i_val[r];
+      const double v = a * (double)i_val[r];
       int lo = 0, hi = n;  // first position with key >= k
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
@@ -521,18 +521,23 @@ __global__ void __launch_bounds__(32) k_gal_big(const int32_t* __restrict__ list
     return;
   }
   const int64_t at = off[row];
-  float d = 0.0f;
+  double d = 0.0;
   for (int t = 0; t < n; ++t) {
     oc[at + t] = key[t];
     ov[at + t] = val[t];
     if (RW && key[t] == row) d = val[t];
   }
-  if (RW) adinv[row] = d > 0.0f ? 1.0f / d : 0.0f;
+  if (RW) adinv[row] = d > 0.0 ? (float)(1.0 / d) : 0.0f;
 }
 
 __global__ void k_i64_i32(int64_t n, const int64_t* __restrict__ a, int32_t* __restrict__ b) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = (int32_t)a[i];
+}
+
+__global__ void k_f64_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
 }
 
 __global__ void k_f64_f32_inv(int64_t n, const double* __restrict__ d, float* __restrict__ inv) {
@@ -567,7 +572,7 @@ __global__ void __launch_bounds__(kFactorThreads) k_direct_factor(const int32_t*
                                                                   const int64_t* const* __restrict__ lvl_chart_row,
                                                                   const int32_t* const* __restrict__ lvl_rp,
                                                                   const int32_t* const* __restrict__ lvl_cols,
-                                                                  const float* const* __restrict__ lvl_vals,
+                                                                  const double* const* __restrict__ lvl_vals,
                                                                   const int64_t* __restrict__ fac_off, float* __restrict__ fac,
                                                                   int* __restrict__ bad) {
   extern __shared__ double smem[];
@@ -585,15 +590,22 @@ __global__ void __launch_bounds__(kFactorThreads) k_direct_factor(const int32_t*
     const int64_t row = r0 + r;
     for (int e = lvl_rp[f][row]; e < lvl_rp[f][row + 1]; ++e) {
       int64_t col = lvl_cols[f][e] - r0;
-      if (col >= 0 && col < m) M[r * m + col] = (double)lvl_vals[f][e];
+      if (col >= 0 && col < m) M[r * m + col] = lvl_vals[f][e];
     }
   }
   __syncthreads();
   for (int j = 0; j < m; ++j) {
     if (threadIdx.x == 0) {
-      double d = M[j * m + j];
+      // pivot floor: the coarse operator comes from FP32 Galerkin products, so on a nearly
+      // singular chart (kappa ~ 1e10: a long chain pinned at its ends) its smallest
+      // eigenvalue is below the rounding of its entries; the floor keeps the factor real
+      // and leaves that one mode to the outer Krylov iteration
+      const double a_jj = M[j * m + j];
+      double d = a_jj;
       for (int k = 0; k < j; ++k) d -= M[j * m + k] * M[j * m + k];
-      if (!(d > 0.0)) {
+      const double fl = 1e-6 * fabs(a_jj);
+      if (!(d > fl)) d = fl;
+      if (!(d > 0.0)) {  // a zero or non-finite diagonal
         atomicExch(bad, 1);
         d = 1e-30;
       }
@@ -865,6 +877,7 @@ struct AmgLevelDev {
   int32_t* row_chart = nullptr;
   int32_t *rp = nullptr, *cols = nullptr;
   float *vals = nullptr, *dinv = nullptr;
+  double* vals64 = nullptr;  // the operator in FP64 (the Galerkin products' input)
   // transfer to the next level (rows of charts that continue below this level)
   int64_t* poff = nullptr;
   int32_t* pc = nullptr;
@@ -936,6 +949,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     L0.rp = sys.row_ptr;
     L0.cols = sys.cols;
     L0.vals = sys.vals32;
+    L0.vals64 = sys.vals;
     L0.dinv = ctx.ws.get<float>("amg.l0.dinv", L0.n);
     if (L0.n > 0) {
       k_f64_f32_inv<<<div_up(L0.n, B), B, 0, s>>>(L0.n, sys.diag, L0.dinv);
@@ -1082,23 +1096,23 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
       return h;
     };
     RUV_CUDA(cudaMemsetAsync(big_n, 0, sizeof(int32_t), s));
-    k_ap<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, nullptr, nullptr,
+    k_ap<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt, nullptr, nullptr,
                                          nullptr, ovf, big, big_n);
     count_launches(1);
     const int32_t wbig = n_big();
     if (wbig > 0) {
-      k_gal_big<0, 0><<<(unsigned)wbig, 32, 0, s>>>(big, nullptr, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, nullptr,
+      k_gal_big<0, 0><<<(unsigned)wbig, 32, 0, s>>>(big, nullptr, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt, nullptr,
                                                     nullptr, nullptr, nullptr, ovf);
       count_launches(1);
     }
     const int64_t WN = offsets_from_counts(ctx, wcnt, L.n, woff, tag + ".wo");
     int32_t* wc = ctx.ws.get<int32_t>(tag + ".wc", WN);
-    float* wv = ctx.ws.get<float>(tag + ".wv", WN);
-    k_ap<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, woff, wc, wv, ovf,
+    double* wv = ctx.ws.get<double>(tag + ".wv", WN);
+    k_ap<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt, woff, wc, wv, ovf,
                                          big, big_n);
     count_launches(1);
     if (wbig > 0) {
-      k_gal_big<1, 0><<<(unsigned)wbig, 32, 0, s>>>(big, nullptr, L.rp, L.cols, L.vals, L.poff, L.pc, L.pv, wcnt, woff,
+      k_gal_big<1, 0><<<(unsigned)wbig, 32, 0, s>>>(big, nullptr, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt, woff,
                                                     wc, wv, nullptr, ovf);
       count_launches(1);
     }
@@ -1122,18 +1136,20 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     C.rp = ctx.ws.get<int32_t>(ntag + ".rp", NA + 1);
     C.cols = ctx.ws.get<int32_t>(ntag + ".cols", AN);
     C.vals = ctx.ws.get<float>(ntag + ".vals", AN);
+    C.vals64 = ctx.ws.get<double>(ntag + ".vals64", AN);
     C.dinv = ctx.ws.get<float>(ntag + ".dinv", NA);
     C.nnz = AN;
     if (NA > 0) {
-      k_rw<1><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv, woff, wc, wv, acnt, aoff, C.cols, C.vals, C.dinv, ovf,
+      k_rw<1><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv, woff, wc, wv, acnt, aoff, C.cols, C.vals64, C.dinv, ovf,
                                           big, big_n);
       if (abig > 0) {
         k_gal_big<1, 1><<<(unsigned)abig, 32, 0, s>>>(big, L.roff, nullptr, L.rc, L.rv, woff, wc, wv, acnt, aoff, C.cols,
-                                                      C.vals, C.dinv, ovf);
+                                                      C.vals64, C.dinv, ovf);
         count_launches(1);
       }
       k_i64_i32<<<div_up(NA + 1, B), B, 0, s>>>(NA + 1, aoff, C.rp);
-      count_launches(2);
+      if (AN > 0) k_f64_f32<<<div_up(AN, B), B, 0, s>>>(AN, C.vals64, C.vals);
+      count_launches(3);
     }
     L.n_next = NA;
     if (debug) {
@@ -1202,18 +1218,19 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   RUV_CUDA(cudaMemcpyAsync(H->fac_off, foff.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
   std::vector<const int64_t*> cr(K);
   std::vector<const int32_t*> rps(K), cls(K);
-  std::vector<const float*> vls(K), dvs(K);
+  std::vector<const double*> vls(K);
+  std::vector<const float*> dvs(K);
   for (int k = 0; k < K; ++k) {
     cr[k] = H->lv[k].chart_row;
     rps[k] = H->lv[k].rp;
     cls[k] = H->lv[k].cols;
-    vls[k] = H->lv[k].vals;
+    vls[k] = H->lv[k].vals64;
     dvs[k] = H->lv[k].dinv;
   }
   H->d_lvl_chart_row = ctx.ws.get<const int64_t*>("amg.p_cr", K);
   const int32_t** d_rp = ctx.ws.get<const int32_t*>("amg.p_rp", K);
   const int32_t** d_cols = ctx.ws.get<const int32_t*>("amg.p_cols", K);
-  const float** d_vals = ctx.ws.get<const float*>("amg.p_vals", K);
+  const double** d_vals = ctx.ws.get<const double*>("amg.p_vals", K);
   H->d_lvl_dinv = ctx.ws.get<const float*>("amg.p_dinv", K);
   RUV_CUDA(cudaMemcpyAsync(H->d_lvl_chart_row, cr.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, s));
   RUV_CUDA(cudaMemcpyAsync(d_rp, rps.data(), sizeof(void*) * K, cudaMemcpyHostToDevice, s));
