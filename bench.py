@@ -44,6 +44,11 @@ import numpy as np  # noqa: E402
 METRIC = "batched LSCM unknowns/s at <=1e-6 UV err vs FP64 LU"
 UNIT = "unknowns/s"
 L2_BYTES = 129 * 1024 * 1024
+# DRAM bytes (read + write) per algorithmic byte of the batched SpMV kernel, from one ncu
+# capture of its first launch on the 1024-disk operator (247.9 MB of traffic for 257 MB of
+# algorithmic bytes; profiles/kernels_disks1024_dram.md).  The disk workloads scale by count,
+# so the traffic of a launch on the 4096-disk operator is this ratio times its algorithmic bytes.
+SPMV_DRAM_PER_ALG_BYTE = 0.965
 
 
 def parse():
@@ -61,6 +66,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-single-chart", action="store_true")
     ap.add_argument("--single-chart-sample", type=int, default=192)
+    ap.add_argument("--ncu-step", action="store_true",
+                    help="for profiler launch lists: upload, one warm-up solve, then one solve of the workload "
+                         "(launch shape from RUV_LPR / RUV_UNROLL / RUV_TILE_ROWS); prints the kernel count "
+                         "before the last solve to stderr and nothing else")
     return ap.parse_args()
 
 
@@ -422,6 +431,26 @@ def main():
     if args.workload.startswith("sphere"):
         run_adjoint(args, rank, world, local, pg)
         return
+    if args.ncu_step:
+        import ctypes
+
+        import researchuv_gb300 as R
+
+        charts, _, _ = make_workload(args.workload)
+        ctx = R.Context(local)
+        L = R.lib()
+        pc = {"jacobi": R.Precond.JACOBI, "amg": R.Precond.AMG, "amg_sa": R.Precond.AMG_SA,
+              "none": R.Precond.NONE}[args.precond]
+        prec = R.Precision.MIXED if args.precision == "mixed" else R.Precision.FP64
+        copts = R.UnfoldOptions(precision=prec, precond=pc).to_c()
+        batch = charts.batch()
+        stats = (R.RuvChartStat * max(batch.n_charts, 1))()
+        ctx.check(L.ruv_lscm_upload(ctx.h, ctypes.byref(batch)), "upload")
+        ctx.check(L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(copts), stats), "solve")
+        sys.stderr.write(f"kernels before the profiled solve: {L.ruv_kernel_launches(ctx.h)}\n")
+        ctx.check(L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(copts), stats), "solve")
+        sys.stderr.write(f"kernels after the profiled solve: {L.ruv_kernel_launches(ctx.h)}\n")
+        return
     import ctypes
 
     import researchuv_gb300 as R
@@ -508,8 +537,11 @@ def main():
                 "d2h_bytes_per_step": d2h, "ms_per_step": ems},
         "roofline": {"bound": "hbm", "kernel": "k_spmv_pq (batched CSR-vector SpMV + p.q)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "traffic": None, "ms_per_launch": spmv_ms,
-                     "algorithmic_bytes": spmv_bytes},
+                     "peak_source": peak_src,
+                     "traffic": (SPMV_DRAM_PER_ALG_BYTE * spmv_bytes if args.workload.startswith("disks") else None),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the "
+                                       "1024-disk operator, scaled by algorithmic bytes",
+                     "ms_per_launch": spmv_ms, "algorithmic_bytes": spmv_bytes},
         "gpu_launches": int(launches),
         "clocks": clock_info,
     }
