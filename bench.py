@@ -4,16 +4,16 @@
 Workload (default): 4096 disk charts, triangle counts log-uniform in [50, 50 000] (seeded
 synthetic meshes, researchuv_gb300/workloads.py), one chart per disk, Dirichlet border pins
 (the reference's border-rectangle pass).  A step = one batched unfold of every chart: GPU
-assembly of the cotangent systems with the pins eliminated, one batched mixed-precision
-Jacobi-PCG over the packed block-diagonal operator to rel-res 1e-12 per chart, and the damped
-driver update.
+assembly of the cotangent systems with the pins eliminated, the AMG hierarchy set-up on the
+GPU, one batched mixed-precision AMG-PCG over the packed block-diagonal operator to rel-res
+1e-12 per chart (double-float refinement), and the damped driver update.
 
 * value  — unknowns/s (sum over charts of 2 * free vertices per step time), inputs resident
            in HBM (ruv_lscm_upload once), step time = device time of the three phases
            (CUDA events on the library's stream).  Inputs (~1 GB operator) exceed L2.
-* e2e    — the same metric through ruv_lscm_solve_batch with host buffers: H2D of the
-           batch and D2H of the UVs inside the timed region (wall clock; the call is
-           synchronous).
+* e2e    — the same metric through ruv_lscm_solve_batch with host buffers (page-locked,
+           ruv_host_alloc): H2D of the batch and D2H of the UVs inside the timed region
+           (wall clock; the call is synchronous).
 * roofline — the batched SpMV kernel (the dominant kernel) timed alone with CUDA events on
            the same operator: algorithmic bytes per launch / mean launch time vs the
            measured HBM copy bandwidth.
@@ -495,12 +495,13 @@ def main():
         dev_ms.append(sum(t[:3]))
     launches = (L.ruv_kernel_launches(ctx.h) - l0) // max(args.steps, 1)
     barrier(pg)
-    # end-to-end through the host-buffer call
+    # end-to-end through the host-buffer call, inputs and outputs in page-locked host memory
     e2e_ms = []
-    uv = np.empty((nv, 2))
+    pbatch, _keep = R.pinned_batch(ctx, charts)
+    uv = R.pinned_empty(ctx, (nv, 2), np.float64)
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        st_ = L.ruv_lscm_solve_batch(ctx.h, ctypes.byref(batch), ctypes.byref(copts),
+        st_ = L.ruv_lscm_solve_batch(ctx.h, ctypes.byref(pbatch), ctypes.byref(copts),
                                      uv.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), stats)
         e2e_ms.append(1000.0 * (time.perf_counter() - t0))
         ctx.check(st_, "e2e")

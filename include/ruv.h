@@ -213,6 +213,11 @@ ruv_status ruv_chart_distortion(ruv_ctx* ctx, const double* uv, double* metrics_
  * Returns the number of values written (<= n). */
 int32_t ruv_last_timings(const ruv_ctx* ctx, double* ms, int32_t n);
 
+/* Page-locked host memory (cudaHostAlloc) for a caller's input and output arrays: copies
+ * between it and the device run at the link's full rate.  Freed with ruv_host_free. */
+ruv_status ruv_host_alloc(ruv_ctx* ctx, int64_t bytes, void** out);
+void ruv_host_free(void* p);
+
 /* Number of kernels this context has enqueued so far (each node of a replayed CUDA graph
  * counts once per replay). */
 int64_t ruv_kernel_launches(const ruv_ctx* ctx);

@@ -79,6 +79,8 @@ SIGNATURES = {
     "ruv_lscm_backward": (ctypes.c_int, [_vp, _P(RuvUnfoldOpts), _P(_f64), _P(_f64), _P(RuvChartStat)]),
     "ruv_distortion_loss": (ctypes.c_int, [_vp, _P(_f64), _P(_f64), _P(_f64), _P(_f64)]),
     "ruv_chart_distortion": (ctypes.c_int, [_vp, _P(_f64), _P(_f64)]),
+    "ruv_host_alloc": (ctypes.c_int, [_vp, _i64, _P(_vp)]),
+    "ruv_host_free": (None, [_vp]),
     "ruv_last_timings": (_i32, [_vp, _P(_f64), _i32]),
     "ruv_kernel_launches": (_i64, [_vp]),
     "ruv_cg_solve_noalloc": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _i64, _f64, ctypes.c_int, _P(_i64), _vp,
@@ -441,6 +443,53 @@ def unfold_charts(ctx: Context, charts: Charts, opts: Optional[UnfoldOptions] = 
                                 area3d=float(area[c]), status=Status(s.status), cg_iters=s.cg_iters,
                                 n_free=s.n_free, rel_res=s.rel_res))
     return out
+
+
+# ------------------------------------------------------------------ page-locked host arrays
+class _PinnedOwner:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        if self.ptr:
+            lib().ruv_host_free(self.ptr)
+            self.ptr = None
+
+
+def pinned_empty(ctx: Context, shape, dtype) -> np.ndarray:
+    """A numpy array in page-locked host memory (ruv_host_alloc); freed with the array."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) if np.ndim(shape) else int(shape)
+    nbytes = max(n * dtype.itemsize, 1)
+    ptr = _vp()
+    ctx.check(lib().ruv_host_alloc(ctx.h, nbytes, ctypes.byref(ptr)), "ruv_host_alloc")
+    buf = (ctypes.c_char * nbytes).from_address(ptr.value)
+    buf._owner = _PinnedOwner(ptr.value)  # the array keeps `buf` (its base), `buf` keeps the memory
+    return np.frombuffer(buf, dtype=dtype, count=n).reshape(shape)
+
+
+def pinned_batch(ctx: Context, charts: "Charts"):
+    """A copy of a prepared batch in page-locked host memory: (RuvBatch, the arrays that own it)."""
+    b = charts.batch()
+    nc = b.n_charts
+    vo = np.ctypeslib.as_array(b.vert_off, shape=(nc + 1,))
+    to = np.ctypeslib.as_array(b.tri_off, shape=(nc + 1,))
+    nv, nt = int(vo[-1]), int(to[-1])
+    srcs = {"vert_off": (vo, _i64), "tri_off": (to, _i64),
+            "p3": (np.ctypeslib.as_array(b.p3, shape=(max(3 * nv, 1),))[:3 * nv], _f64),
+            "tris": (np.ctypeslib.as_array(b.tris, shape=(max(3 * nt, 1),))[:3 * nt], _i32),
+            "pinned": (np.ctypeslib.as_array(b.pinned, shape=(max(nv, 1),))[:nv], _u8),
+            "pin_uv": (np.ctypeslib.as_array(b.pin_uv, shape=(max(2 * nv, 1),))[:2 * nv], _f64),
+            "p2": (np.ctypeslib.as_array(b.p2, shape=(max(2 * nv, 1),))[:2 * nv], _f64)}
+    keep = {}
+    out = RuvBatch()
+    out.n_charts = nc
+    for name, (src, ct) in srcs.items():
+        a = pinned_empty(ctx, src.shape, src.dtype)
+        a[...] = src
+        keep[name] = a
+        setattr(out, name, _ptr(a, ct))
+    return out, keep
 
 
 # ------------------------------------------------------------------ differentiation

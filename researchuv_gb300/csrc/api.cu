@@ -483,6 +483,23 @@ ruv_status ruv_chart_distortion(ruv_ctx* ctx, const double* uv, double* metrics_
   });
 }
 
+ruv_status ruv_host_alloc(ruv_ctx* ctx, int64_t bytes, void** out) {
+  if (!ctx || !out || bytes < 0) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    *out = nullptr;
+    if (cudaHostAlloc(out, (size_t)(bytes > 0 ? bytes : 1), cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      *out = nullptr;
+      return fail(ctx, RUV_ERR_OOM, "page-locked host allocation failed");
+    }
+    return RUV_OK;
+  });
+}
+
+void ruv_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
 int64_t ruv_kernel_launches(const ruv_ctx* ctx) { return ctx ? ctx->c.launches : 0; }
 
 int32_t ruv_last_timings(const ruv_ctx* ctx, double* ms, int32_t n) {
