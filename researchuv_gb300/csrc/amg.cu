@@ -763,7 +763,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const i
           xi.c[c] = wd * bi.c[c];
           ti.c[c] = bi.c[c] - s.c[c];
         }
-        stf<NR>(x, i, xi);
+        if (x) stf<NR>(x, i, xi);  // (the tentative-P cycle forms it again on the way up)
         stf<NR>(t, i, ti);
       });
 }
@@ -815,6 +815,40 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int
       [&](int32_t j) { return ldf<NR>(y, j); },
       [&](int64_t i, const F<NR>& s) {
         const F<NR> bi = ldf<NR>(b, i), yi = ldf<NR>(y, i);
+        F<NR> xi;
+        const float wd = kOmega * dinv[i];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) xi.c[c] = yi.c[c] + wd * (bi.c[c] - s.c[c]);
+        stf<NR>(x, i, xi);
+      });
+}
+
+// Up, tentative prolongator (one 1 per row at agg[i]): the prolongation and the
+// post-smoothing in one pass, x = y + w D^-1 (b - A y) with y_j = w D^-1_j b_j +
+// alpha_c x_c[agg[j]] formed on the fly for every neighbour (the pre-smoothed x is not
+// stored and y is never written).
+template <int NR, int LPR, int U, int K>
+__global__ void __launch_bounds__(kAmgThreads) k_smooth_up_t(LvlTiles T, const int32_t* __restrict__ done,
+                                                             const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                                             const float* __restrict__ vals, const float* __restrict__ dinv,
+                                                             const float* __restrict__ b, const int32_t* __restrict__ agg,
+                                                             const float* __restrict__ xc, float alpha_c,
+                                                             float* __restrict__ x) {
+  const int64_t tl = blockIdx.x;
+  if (done[T.chart[tl]]) return;
+  auto yval = [&](int64_t j) {
+    F<NR> v = ldf<NR>(b, j);
+    const float wd = kOmega * dinv[j];
+    const F<NR> c = ldf<NR>(xc, agg[j]);
+#pragma unroll
+    for (int k = 0; k < NR; ++k) v.c[k] = wd * v.c[k] + alpha_c * c.c[k];
+    return v;
+  };
+  tile_rows<NR, LPR, U, K>(
+      T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, cols, [&](int64_t e) { return vals[e]; },
+      [&](int32_t j) { return yval(j); },
+      [&](int64_t i, const F<NR>& s) {
+        const F<NR> bi = ldf<NR>(b, i), yi = yval(i);
         F<NR> xi;
         const float wd = kOmega * dinv[i];
 #pragma unroll
@@ -886,12 +920,14 @@ struct AmgLevelDev {
   int32_t* rc = nullptr;
   float* rv = nullptr;
   float *b = nullptr, *x = nullptr, *y = nullptr, *t = nullptr;
+  int32_t* agg = nullptr;  // aggregate of each row (the tentative prolongator), -1 if none
   LvlTiles cont{nullptr, nullptr, 0};  // tiles over rows whose chart continues below this level
   LvlTiles all{nullptr, nullptr, 0};   // tiles over every row of this level
 };
 
 struct AmgHierarchy {
   int nrhs = 2;
+  bool smoothed = false;  // smoothed prolongators (AMG-SA); else tentative (one 1 per row)
   int64_t n_charts = 0;
   std::vector<AmgLevelDev> lv;
   int32_t* final_lvl = nullptr;
@@ -929,6 +965,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   const int64_t NC = sys.n_charts;
   std::unique_ptr<AmgHierarchy> H(new AmgHierarchy());
   H->nrhs = sys.nrhs;
+  H->smoothed = smooth;
   H->n_charts = NC;
   H->alpha_c = smooth ? 1.0f : 1.5f;  // over-correct the piecewise-constant coarse space
   if (const char* e = std::getenv("RUV_AMG_ALPHA")) H->alpha_c = (float)std::atof(e);
@@ -1042,6 +1079,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     const int64_t NA = read_i64(ctx, aid + NG);
     int32_t* agg = ctx.ws.get<int32_t>(tag + ".agg", L.n);
     k_agg<<<div_up(L.n, B), B, 0, s>>>(L.n, active, grp_of, glead_of, aid, agg);
+    L.agg = agg;
     // coarse chart offsets: aggregates are numbered in lead-row order, so chart c's
     // aggregates start at the count of aggregate-leading rows before its first row
     uint8_t* arow = ctx.ws.get<uint8_t>(tag + ".arow", L.n);
@@ -1311,8 +1349,9 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
+    float* xpre = H->smoothed ? L.x : nullptr;  // the tentative cycle re-forms it on the way up
 #define CALL(X, UU, KK)                                                                                              \
-  k_smooth_down<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.x, \
+  k_smooth_down<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, xpre, \
                                                             L.t)
     RUV_LPR_SWITCH(la, CALL)
 #undef CALL
@@ -1335,13 +1374,22 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
     AmgLevelDev& L = H->lv[k];
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
+    const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
+    if (!H->smoothed) {
+#define CALL(X, UU, KK)                                                                                                 \
+  k_smooth_up_t<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.agg, \
+                                                              C.x, H->alpha_c, L.x)
+      RUV_LPR_SWITCH(la, CALL)
+#undef CALL
+      ++launches;
+      continue;
+    }
     const int lp = lanes_for(L.n ? (double)L.n_pnnz / (double)L.n : 1.0);
 #define CALL(X, UU, KK)                                                                                                  \
   k_prolong_add<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.poff, L.pc, L.pv, C.x, L.x, L.y, \
                                                             H->alpha_c)
     RUV_LPR_SWITCH(lp, CALL)
 #undef CALL
-    const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
 #define CALL(X, UU, KK) \
   k_smooth_up<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.y, L.x)
     RUV_LPR_SWITCH(la, CALL)

@@ -150,14 +150,30 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
   if (v >= n_verts || pinned[v]) return;
   const int64_t r0 = rec_off[v], r1 = rec_off[v + 1];
   if (MODE == 0) {  // insertion sort by (neighbour, corner) — buckets hold ~2x valence records
-    for (int64_t i = r0 + 1; i < r1; ++i) {
-      int2 key = rec[i];
-      int64_t j = i - 1;
-      while (j >= r0 && rec_less(key, rec[j])) {
-        rec[j + 1] = rec[j];
-        --j;
+    constexpr int kLocal = 48;  // sorted in thread-local memory, written back once
+    const int64_t nrec = r1 - r0;
+    if (nrec <= kLocal) {
+      int2 b[kLocal];
+      for (int64_t i = 0; i < nrec; ++i) {
+        const int2 key = rec[r0 + i];
+        int64_t j = i - 1;
+        while (j >= 0 && rec_less(key, b[j])) {
+          b[j + 1] = b[j];
+          --j;
+        }
+        b[j + 1] = key;
       }
-      rec[j + 1] = key;
+      for (int64_t i = 0; i < nrec; ++i) rec[r0 + i] = b[i];
+    } else {  // a high-valence vertex: in place
+      for (int64_t i = r0 + 1; i < r1; ++i) {
+        int2 key = rec[i];
+        int64_t j = i - 1;
+        while (j >= r0 && rec_less(key, rec[j])) {
+          rec[j + 1] = rec[j];
+          --j;
+        }
+        rec[j + 1] = key;
+      }
     }
   }
   const P3 pv = ld3(p3, v);
