@@ -213,6 +213,16 @@ ruv_status ruv_chart_distortion(ruv_ctx* ctx, const double* uv, double* metrics_
  * Returns the number of values written (<= n). */
 int32_t ruv_last_timings(const ruv_ctx* ctx, double* ms, int32_t n);
 
+/* rectangularize (unwrap/src/metrics.rs:147-227), the post-solve normalisation pipeline::run
+ * applies to every chart (pipeline.rs:171-176), for every chart of the resident batch: the
+ * chart rotated by the angle of the 72-step ladder whose border bounding box scores least,
+ * normalised to [0,1]^2, its border points snapped onto the nearest side.  uv: 2 * n_verts;
+ * border: n_verts flags (the chart's border set); rectified_out: 2 * n_verts; ext_out:
+ * 2 * n_charts (the extents before normalisation).  Bit-identical to the reference on the
+ * same host libm (the angle table is computed on the host). */
+ruv_status ruv_rectangularize(ruv_ctx* ctx, const double* uv, const uint8_t* border,
+                              double* rectified_out, double* ext_out);
+
 /* Page-locked host memory (cudaHostAlloc) for a caller's input and output arrays: copies
  * between it and the device run at the link's full rate.  Freed with ruv_host_free. */
 ruv_status ruv_host_alloc(ruv_ctx* ctx, int64_t bytes, void** out);

@@ -17,6 +17,7 @@
 //   meshgen fixtures     unwrap/src/meshgen.rs:12-198
 //   chart_distortion     unwrap/src/metrics.rs:41-141
 //   vector arithmetic    math/src/vec.rs:100-124
+//   rectangularize       unwrap/src/metrics.rs:147-227
 //   IC(0) + colouring    gpu/src/precond.rs:49-123 (graph_coloring, color_permutation,
 //                        permute_csr), :145-262 (factor_ic0, tri_levels, transpose_lower)
 //   fixed-pin system     lscm.rs:594-676 with the pins given (the map the adjoint
@@ -1614,6 +1615,80 @@ int orc_chart_metrics(void* h, int64_t chart, const double* uv, double* out5) {
   return 0;
 }
 
+
+// rectangularize (metrics.rs:147-227) of one chart: uv (2n), border flags (n) ->
+// q (2n), ext (2).
+void orc_rectangularize(int64_t n, const double* uv, const int64_t* border, double* q, double* ext) {
+  std::vector<size_t> bnd;
+  for (int64_t i = 0; i < n; ++i)
+    if (border[i]) bnd.push_back((size_t)i);
+  if (n == 0) return;
+  if (bnd.empty()) {
+    double mu = uv[0], mv = uv[1], xu = uv[0], xv = uv[1];
+    for (int64_t i = 0; i < n; ++i) {
+      mu = rmin(mu, uv[2 * i]);
+      mv = rmin(mv, uv[2 * i + 1]);
+      xu = rmax(xu, uv[2 * i]);
+      xv = rmax(xv, uv[2 * i + 1]);
+    }
+    ext[0] = xu - mu;
+    ext[1] = xv - mv;
+    for (int64_t i = 0; i < n; ++i) {
+      q[2 * i] = (uv[2 * i] - mu) / rmax(ext[0], 1e-30);
+      q[2 * i + 1] = (uv[2 * i + 1] - mv) / rmax(ext[1], 1e-30);
+    }
+    return;
+  }
+  const int n_steps = 72;
+  bool have = false;
+  double bc = 1.0, bs_ = 0.0, bscore = 0.0;
+  for (int k = 0; k < n_steps; ++k) {
+    const double ang = 3.141592653589793 * (double)k / (double)(n_steps - 1);
+    const double co = std::cos(ang), si = std::sin(ang);
+    double mn = INFINITY, mx = -INFINITY, mnv = INFINITY, mxv = -INFINITY;
+    for (size_t bi : bnd) {
+      const double pu = uv[2 * bi], pv = uv[2 * bi + 1];
+      const double qu = co * pu + si * pv;
+      const double qv = -si * pu + co * pv;
+      mn = rmin(mn, qu);
+      mx = rmax(mx, qu);
+      mnv = rmin(mnv, qv);
+      mxv = rmax(mxv, qv);
+    }
+    const double e0 = mx - mn, e1 = mxv - mnv;
+    const double score = std::sqrt(e0 * (e0 + 1e-30) + e1 * (e1 + 1e-30));
+    if (!(have && score >= bscore)) {
+      have = true;
+      bc = co;
+      bs_ = si;
+      bscore = score;
+    }
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    const double pu = uv[2 * i], pv = uv[2 * i + 1];
+    q[2 * i] = bc * pu + bs_ * pv;
+    q[2 * i + 1] = -bs_ * pu + bc * pv;
+  }
+  double mu = q[0], mv = q[1], xu = q[0], xv = q[1];
+  for (int64_t i = 0; i < n; ++i) {
+    mu = rmin(mu, q[2 * i]);
+    mv = rmin(mv, q[2 * i + 1]);
+    xu = rmax(xu, q[2 * i]);
+    xv = rmax(xv, q[2 * i + 1]);
+  }
+  ext[0] = xu - mu;
+  ext[1] = xv - mv;
+  for (int64_t i = 0; i < n; ++i) {
+    q[2 * i] = (q[2 * i] - mu) / rmax(ext[0], 1e-30);
+    q[2 * i + 1] = (q[2 * i + 1] - mv) / rmax(ext[1], 1e-30);
+  }
+  for (size_t bi : bnd) {
+    const double pu = q[2 * bi], pv = q[2 * bi + 1];
+    const double dx = rmin(pu, 1.0 - pu), dy = rmin(pv, 1.0 - pv);
+    if (dx <= dy) q[2 * bi] = pu < 0.5 ? 0.0 : 1.0;
+    else q[2 * bi + 1] = pv < 0.5 ? 0.0 : 1.0;
+  }
+}
 
 // IC(0) of bag {"a.row_ptr", "a.cols", "a.vals"} -> {"l.*", "lt.*" (ptr, cols, vals),
 // "fwd.level", "bwd.level"}; with `colored`, of the colour-permuted matrix, adding

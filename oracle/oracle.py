@@ -63,6 +63,7 @@ def lib():
         L.orc_ic0.restype = ctypes.c_int
         L.orc_ic0_apply.argtypes = [vp, P(f64), P(f64)]
         L.orc_lscm_fixed.argtypes = [vp]
+        L.orc_rectangularize.argtypes = [i64, P(f64), P(i64), P(f64), P(f64)]
         L.orc_distortion_loss.argtypes = [vp, P(f64), P(f64), P(f64), P(f64)]
         L.orc_lscm_adjoint_positions.argtypes = [vp, P(f64), P(f64), P(f64)]
         _lib = L
@@ -420,4 +421,15 @@ def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float
             diffs.append(float((lt2 - lt).sum()) + lam_l2 * float((du * (uv2 + uv - 2.0 * target)).sum()))
         out.append((diffs[0] - diffs[1]) / (2.0 * h))
     return np.array(out)
+
+
+def rectangularize(uv, border):
+    """rectangularize (metrics.rs:147-227) of one chart: (q (n, 2), ext (2,))."""
+    uv = np.ascontiguousarray(uv, np.float64).reshape(-1)
+    b = np.ascontiguousarray(border, np.int64).reshape(-1)
+    n = len(b)
+    q = np.zeros(2 * n)
+    ext = np.zeros(2)
+    lib().orc_rectangularize(n, _f64p(uv), _i64p(b), _f64p(q), _f64p(ext))
+    return q.reshape(n, 2), ext
 

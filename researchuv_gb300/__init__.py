@@ -79,6 +79,7 @@ SIGNATURES = {
     "ruv_lscm_backward": (ctypes.c_int, [_vp, _P(RuvUnfoldOpts), _P(_f64), _P(_f64), _P(RuvChartStat)]),
     "ruv_distortion_loss": (ctypes.c_int, [_vp, _P(_f64), _P(_f64), _P(_f64), _P(_f64)]),
     "ruv_chart_distortion": (ctypes.c_int, [_vp, _P(_f64), _P(_f64)]),
+    "ruv_rectangularize": (ctypes.c_int, [_vp, _P(_f64), _P(_u8), _P(_f64), _P(_f64)]),
     "ruv_host_alloc": (ctypes.c_int, [_vp, _i64, _P(_vp)]),
     "ruv_host_free": (None, [_vp]),
     "ruv_last_timings": (_i32, [_vp, _P(_f64), _i32]),
@@ -535,6 +536,30 @@ def chart_distortion(ctx: Context, uv, n_charts: int) -> np.ndarray:
     out = np.empty((max(n_charts, 1), 5), np.float64)
     ctx.check(lib().ruv_chart_distortion(ctx.h, _ptr(u, _f64), _ptr(out, _f64)), "ruv_chart_distortion")
     return out[:n_charts]
+
+
+def border_flags(charts: "Charts") -> np.ndarray:
+    """One flag per packed vertex: the vertex is in its chart's border set (segment.rs)."""
+    vo, bo = charts.i64("chart.vert_off"), charts.i64("chart.border_off")
+    vid, bd = charts.i64("chart.vertex_ids"), charts.i64("chart.border")
+    out = np.zeros(int(vo[-1]), np.uint8)
+    for c in range(len(vo) - 1):
+        ids = vid[vo[c]:vo[c + 1]]  # sorted source ids
+        b = bd[bo[c]:bo[c + 1]]
+        out[vo[c] + np.searchsorted(ids, b)] = 1
+    return out
+
+
+def rectangularize(ctx: Context, uv, border, n_charts: int):
+    """rectangularize (metrics.rs:147-227) of every chart of the resident batch.  Returns
+    (rectified UVs (n, 2), extents (n_charts, 2))."""
+    u = np.ascontiguousarray(uv, np.float64).reshape(-1, 2)
+    b = np.ascontiguousarray(border, np.uint8).reshape(-1)
+    q = np.empty_like(u)
+    ext = np.empty((max(n_charts, 1), 2), np.float64)
+    ctx.check(lib().ruv_rectangularize(ctx.h, _ptr(u, _f64), _ptr(b, _u8), _ptr(q, _f64), _ptr(ext, _f64)),
+              "ruv_rectangularize")
+    return q, ext[:n_charts]
 
 
 def export_chart_system(ctx: Context, chart: int):

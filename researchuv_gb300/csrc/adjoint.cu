@@ -324,6 +324,125 @@ __global__ void k_chart_metrics(int64_t n_charts, const int64_t* __restrict__ tr
   out[5 * c + 4] = (double)folds;
 }
 
+// ---------------------------------------------------------------- rectangularize (metrics.rs:147-227)
+constexpr int kRectAngles = 72;
+constexpr int kRectThreads = 256;
+
+__device__ __forceinline__ void warp_minmax4(double (&v)[4]) {  // min, max, min, max
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v[0] = fmin(v[0], __shfl_xor_sync(0xffffffffu, v[0], o));
+    v[1] = fmax(v[1], __shfl_xor_sync(0xffffffffu, v[1], o));
+    v[2] = fmin(v[2], __shfl_xor_sync(0xffffffffu, v[2], o));
+    v[3] = fmax(v[3], __shfl_xor_sync(0xffffffffu, v[3], o));
+  }
+}
+
+// One CTA per chart.  The 72-angle ladder over the border points (each warp a set of
+// angles; min / max are exact in any order), the first angle of least score kept, then the
+// whole chart rotated, normalised to [0,1]^2 and its border points snapped to the nearest
+// rectangle side.  The angle table (cos, sin) comes from the host's libm, as the reference's
+// does; every product and sum is rounded on its own (no FMA), so the result is bit-identical.
+__global__ void __launch_bounds__(kRectThreads) k_rectangularize(const int64_t* __restrict__ vert_off,
+                                                                 const double* __restrict__ uv,
+                                                                 const uint8_t* __restrict__ border,
+                                                                 const double* __restrict__ cs, double* __restrict__ q,
+                                                                 double* __restrict__ ext) {
+  __shared__ double score[kRectAngles];
+  __shared__ double red[4][kRectThreads / 32];
+  __shared__ double rot[2];
+  __shared__ int has_border;
+  const int64_t c = blockIdx.x;
+  const int64_t v0 = vert_off[c], v1 = vert_off[c + 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = kRectThreads / 32;
+  if (v1 <= v0) return;
+  if (threadIdx.x == 0) has_border = 0;
+  __syncthreads();
+  for (int64_t i = v0 + threadIdx.x; i < v1; i += blockDim.x)
+    if (border[i]) has_border = 1;
+  __syncthreads();
+  double cth = 1.0, sth = 0.0;
+  if (has_border) {
+    for (int k = wid; k < kRectAngles; k += nw) {
+      const double co = cs[2 * k], si = cs[2 * k + 1];
+      double v[4] = {INFINITY, -INFINITY, INFINITY, -INFINITY};
+      for (int64_t i = v0 + lane; i < v1; i += 32) {
+        if (!border[i]) continue;
+        const double pu = uv[2 * i], pv = uv[2 * i + 1];
+        const double qu = ad(ml(co, pu), ml(si, pv));
+        const double qv = ad(ml(-si, pu), ml(co, pv));
+        v[0] = fmin(v[0], qu);
+        v[1] = fmax(v[1], qu);
+        v[2] = fmin(v[2], qv);
+        v[3] = fmax(v[3], qv);
+      }
+      warp_minmax4(v);
+      if (lane == 0) {
+        const double e0 = sb(v[1], v[0]), e1 = sb(v[3], v[2]);
+        score[k] = sqrt(ad(ml(e0, ad(e0, 1e-30)), ml(e1, ad(e1, 1e-30))));
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int best = 0;  // the first angle of least score (later ties do not replace it)
+      for (int k = 1; k < kRectAngles; ++k)
+        if (score[k] < score[best]) best = k;
+      rot[0] = cs[2 * best];
+      rot[1] = cs[2 * best + 1];
+    }
+    __syncthreads();
+    cth = rot[0];
+    sth = rot[1];
+  }
+  // rotate and take the bounding box
+  double v[4] = {INFINITY, -INFINITY, INFINITY, -INFINITY};
+  for (int64_t i = v0 + threadIdx.x; i < v1; i += blockDim.x) {
+    const double pu = uv[2 * i], pv = uv[2 * i + 1];
+    double qu = pu, qv = pv;
+    if (has_border) {
+      qu = ad(ml(cth, pu), ml(sth, pv));
+      qv = ad(ml(-sth, pu), ml(cth, pv));
+    }
+    q[2 * i] = qu;
+    q[2 * i + 1] = qv;
+    v[0] = fmin(v[0], qu);
+    v[1] = fmax(v[1], qu);
+    v[2] = fmin(v[2], qv);
+    v[3] = fmax(v[3], qv);
+  }
+  warp_minmax4(v);
+  if (lane == 0)
+    for (int k = 0; k < 4; ++k) red[k][wid] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m[4] = {red[0][0], red[1][0], red[2][0], red[3][0]};
+    for (int w = 1; w < nw; ++w) {
+      m[0] = fmin(m[0], red[0][w]);
+      m[1] = fmax(m[1], red[1][w]);
+      m[2] = fmin(m[2], red[2][w]);
+      m[3] = fmax(m[3], red[3][w]);
+    }
+    red[0][0] = m[0];
+    red[2][0] = m[2];
+    red[1][0] = sb(m[1], m[0]);  // extents
+    red[3][0] = sb(m[3], m[2]);
+    ext[2 * c] = red[1][0];
+    ext[2 * c + 1] = red[3][0];
+  }
+  __syncthreads();
+  const double mu = red[0][0], mv = red[2][0], eu = rmax(red[1][0], 1e-30), ev = rmax(red[3][0], 1e-30);
+  for (int64_t i = v0 + threadIdx.x; i < v1; i += blockDim.x) {
+    double pu = dv(sb(q[2 * i], mu), eu), pv = dv(sb(q[2 * i + 1], mv), ev);
+    if (has_border && border[i]) {  // verticalize: snap onto the nearest side
+      const double dx = fmin(pu, sb(1.0, pu)), dy = fmin(pv, sb(1.0, pv));
+      if (dx <= dy) pu = pu < 0.5 ? 0.0 : 1.0;
+      else pv = pv < 0.5 ? 0.0 : 1.0;
+    }
+    q[2 * i] = pu;
+    q[2 * i + 1] = pv;
+  }
+}
+
 // ---------------------------------------------------------------- reverse pass of the assembly
 // g (vertex-ordered, 2 per vertex) -> per free row.
 __global__ void k_gather_rows(int64_t n_rows, const int32_t* __restrict__ row_vert, const double* __restrict__ gv,
@@ -483,6 +602,25 @@ void distortion_loss(Ctx& ctx, const DevBatch& bt, const double* uv, double* duv
   loss.resize(NC);
   if (NC > 0) RUV_CUDA(cudaMemcpyAsync(loss.data(), lc, sizeof(double) * NC, cudaMemcpyDeviceToHost, s));
   RUV_CUDA(cudaStreamSynchronize(s));
+}
+
+void rectangularize(Ctx& ctx, const DevBatch& bt, const double* uv, const uint8_t* border, double* q, double* ext) {
+  cudaStream_t s = ctx.stream;
+  // the angle ladder of metrics.rs:166-171 with the host's libm (np.linspace(0, pi, 72))
+  std::vector<double> h(2 * kRectAngles);
+  for (int k = 0; k < kRectAngles; ++k) {
+    const double ang = 3.141592653589793 * (double)k / (double)(kRectAngles - 1);
+    h[2 * k] = std::cos(ang);
+    h[2 * k + 1] = std::sin(ang);
+  }
+  double* cs = ctx.ws.get<double>("rect.cs", 2 * kRectAngles);
+  RUV_CUDA(cudaMemcpyAsync(cs, h.data(), sizeof(double) * 2 * kRectAngles, cudaMemcpyHostToDevice, s));
+  if (bt.n_charts > 0) {
+    k_rectangularize<<<(unsigned)bt.n_charts, kRectThreads, 0, s>>>(bt.vert_off, uv, border, cs, q, ext);
+    count_launches(1);
+  }
+  RUV_LAUNCH_CHECK();
+  RUV_CUDA(cudaStreamSynchronize(s));  // `h` goes out of scope
 }
 
 void chart_metrics(Ctx& ctx, const DevBatch& bt, const double* uv, std::vector<double>& out5) {

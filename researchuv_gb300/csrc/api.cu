@@ -483,6 +483,28 @@ ruv_status ruv_chart_distortion(ruv_ctx* ctx, const double* uv, double* metrics_
   });
 }
 
+ruv_status ruv_rectangularize(ruv_ctx* ctx, const double* uv, const uint8_t* border, double* rectified_out,
+                              double* ext_out) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    if (!c.have_batch) return fail(ctx, RUV_ERR_BAD_INPUT, "no batch uploaded on this context");
+    const DevBatch& bt = c.resident;
+    const int64_t NV = bt.n_verts, NC = bt.n_charts;
+    if ((NV > 0 && (!uv || !border || !rectified_out)) || (NC > 0 && !ext_out))
+      return fail(ctx, RUV_ERR_BAD_INPUT, "null buffer");
+    const double* duv = upload(c, "rect.uv", uv, 2 * NV);
+    const uint8_t* db = upload(c, "rect.border", border, NV);
+    double* q = c.ws.get<double>("rect.q", std::max<int64_t>(2 * NV, 1));
+    double* e = c.ws.get<double>("rect.ext", std::max<int64_t>(2 * NC, 1));
+    rectangularize(c, bt, duv, db, q, e);
+    if (NV > 0) RUV_CUDA(cudaMemcpyAsync(rectified_out, q, sizeof(double) * 2 * NV, cudaMemcpyDeviceToHost, c.stream));
+    if (NC > 0) RUV_CUDA(cudaMemcpyAsync(ext_out, e, sizeof(double) * 2 * NC, cudaMemcpyDeviceToHost, c.stream));
+    RUV_CUDA(cudaStreamSynchronize(c.stream));
+    return RUV_OK;
+  });
+}
+
 ruv_status ruv_host_alloc(ruv_ctx* ctx, int64_t bytes, void** out) {
   if (!ctx || !out || bytes < 0) return RUV_ERR_BAD_INPUT;
   return guarded(ctx, [&]() -> ruv_status {

@@ -111,6 +111,9 @@ void distortion_loss(Ctx& ctx, const DevBatch& bt, const double* uv, double* duv
 // chart_distortion (unwrap/src/metrics.rs:73-141) per chart: conformal mean / max, area
 // ratio mean, flips, folds.
 void chart_metrics(Ctx& ctx, const DevBatch& bt, const double* uv, std::vector<double>& out5);
+// rectangularize (unwrap/src/metrics.rs:147-227) per chart: q (2 * n_verts) in [0,1]^2 per
+// chart, ext (2 * n_charts) the extents before normalisation; border: one flag per vertex.
+void rectangularize(Ctx& ctx, const DevBatch& bt, const double* uv, const uint8_t* border, double* q, double* ext);
 
 // Damped driver update (unfold_chart's loop, lscm.rs:570-719) on the device: writes uv
 // (2 * n_verts) and per-chart driver iterations / err_accum.

@@ -101,3 +101,22 @@ def test_batched_adjoint_matches_per_chart_lu():
         ref, _ = O.lu_adjoint_gradient(p3[sl], ch["tris"], ch["pinned"].astype(np.int64), ch["pin_uv"], lam,
                                        target[sl])
         assert _rel(grad[sl], ref) <= 1e-6, (c, _rel(grad[sl], ref))
+
+
+def test_rectangularize_matches_reference():
+    """rectangularize (metrics.rs:147-227) of every chart on the device: bit-identical to the
+    reference restatement (same host libm angle table, no FMA contraction)."""
+    ctx = R.Context(0)
+    cases = [R.prepare_mesh(*O.grid(32, 32)), R.prepare_mesh(*O.cube(6)),
+             R.prepare_mesh(*O.torus_annulus(2.0, 0.7, 64, 40)), R.prepare_mesh(*O.uv_sphere(48, 24)),
+             R.prepare_patches(*W.disks(24, t_min=50, t_max=5000, seed=7))]
+    for C in cases:
+        vo = C.i64("chart.vert_off")
+        uv, _, _ = R.solve_batch(ctx, C.batch(), R.UnfoldOptions(), int(vo[-1]))
+        border = R.border_flags(C)
+        q, ext = R.rectangularize(ctx, uv, border, C.n_charts)
+        for c in range(C.n_charts):
+            sl = slice(vo[c], vo[c + 1])
+            q_ref, e_ref = O.rectangularize(uv[sl], border[sl])
+            assert np.array_equal(q[sl], q_ref), c
+            assert np.array_equal(ext[c], e_ref), c
