@@ -530,6 +530,103 @@ __global__ void __launch_bounds__(32) k_gal_big(const int32_t* __restrict__ list
   if (RW) adinv[row] = d > 0.0 ? (float)(1.0 / d) : 0.0f;
 }
 
+// Tentative prolongator (P = one 1 per row at agg[i]): A_c = R A P straight from A, coarse row
+// I = sum over its member rows i of A's row i with every column j mapped to agg[j] -- no
+// W = A P pass.  MODE 0 count / 1 fill (also the coarse diagonal inverse).  Rows above kGalCap
+// distinct columns go to k_rap_t_big.
+template <int MODE>
+__global__ void k_rap_t(int64_t nc, const int64_t* __restrict__ roff, const int32_t* __restrict__ rc,
+                        const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                        const double* __restrict__ vals, const int32_t* __restrict__ agg, int32_t* __restrict__ cnt,
+                        const int64_t* __restrict__ aoff, int32_t* __restrict__ ac, double* __restrict__ av,
+                        float* __restrict__ adinv, int* __restrict__ overflow, int32_t* __restrict__ big,
+                        int32_t* __restrict__ big_n) {
+  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= nc) return;
+  Acc<kGalCap, double> acc;
+  for (int64_t q = roff[I]; q < roff[I + 1]; ++q) {
+    const int32_t i = rc[q];
+    for (int e = rp[i]; e < rp[i + 1]; ++e) acc.add(agg[cols[e]], vals[e]);
+  }
+  atomicMax(overflow + 5, acc.n);
+  if (acc.overflow) {
+    if (MODE == 0) {
+      cnt[I] = 0;
+      big[atomicAdd(big_n, 1)] = (int32_t)I;
+    }
+    return;
+  }
+  acc.sort();
+  if (MODE == 0) {
+    cnt[I] = acc.n;
+    return;
+  }
+  const int64_t at = aoff[I];
+  double d = 0.0;
+  for (int t = 0; t < acc.n; ++t) {
+    ac[at + t] = acc.key[t];
+    av[at + t] = acc.val[t];
+    if (acc.key[t] == (int32_t)I) d = acc.val[t];
+  }
+  adinv[I] = d > 0.0 ? (float)(1.0 / d) : 0.0f;
+}
+
+// k_rap_t for its listed rows, one CTA per row (its first thread), key-sorted accumulation in
+// shared memory in the same arrival order.
+template <int MODE>
+__global__ void __launch_bounds__(32) k_rap_t_big(const int32_t* __restrict__ list, const int64_t* __restrict__ roff,
+                                                  const int32_t* __restrict__ rc, const int32_t* __restrict__ rp,
+                                                  const int32_t* __restrict__ cols, const double* __restrict__ vals,
+                                                  const int32_t* __restrict__ agg, int32_t* __restrict__ cnt,
+                                                  const int64_t* __restrict__ aoff, int32_t* __restrict__ ac,
+                                                  double* __restrict__ av, float* __restrict__ adinv,
+                                                  int* __restrict__ overflow) {
+  __shared__ int32_t key[kBigCap];
+  __shared__ double val[kBigCap];
+  if (threadIdx.x != 0) return;
+  const int32_t I = list[blockIdx.x];
+  int n = 0;
+  for (int64_t q = roff[I]; q < roff[I + 1]; ++q) {
+    const int32_t i = rc[q];
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+      const int32_t k = agg[cols[e]];
+      const double v = vals[e];
+      int lo = 0, hi = n;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (key[mid] < k) lo = mid + 1; else hi = mid;
+      }
+      if (lo < n && key[lo] == k) {
+        val[lo] += v;
+      } else if (n < kBigCap) {
+        for (int t = n; t > lo; --t) {
+          key[t] = key[t - 1];
+          val[t] = val[t - 1];
+        }
+        key[lo] = k;
+        val[lo] = v;
+        ++n;
+      } else {
+        atomicExch(overflow, 1);
+        if (MODE == 0) cnt[I] = 0;
+        return;
+      }
+    }
+  }
+  if (MODE == 0) {
+    cnt[I] = n;
+    return;
+  }
+  const int64_t at = aoff[I];
+  double d = 0.0;
+  for (int t = 0; t < n; ++t) {
+    ac[at + t] = key[t];
+    av[at + t] = val[t];
+    if (key[t] == I) d = val[t];
+  }
+  adinv[I] = d > 0.0 ? (float)(1.0 / d) : 0.0f;
+}
+
 __global__ void k_i64_i32(int64_t n, const int64_t* __restrict__ a, int32_t* __restrict__ b) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = (int32_t)a[i];
@@ -1122,9 +1219,8 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     k_scatter_t<<<div_up(L.n, B), B, 0, s>>>(L.n, L.poff, L.pc, L.pv, L.roff, cursor, L.rc, L.rv);
     k_sort_rows<<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv);
     count_launches(2);
-    // ---- W = A P, then A_c = R W
-    int32_t* wcnt = ctx.ws.get<int32_t>(tag + ".wcnt", L.n);
-    int64_t* woff = ctx.ws.get<int64_t>(tag + ".woff", L.n + 1);
+    int32_t* acnt = ctx.ws.get<int32_t>(ntag + ".acnt", NA);
+    int64_t* aoff = ctx.ws.get<int64_t>(ntag + ".aoff", NA + 1);
     int32_t* big = ctx.ws.get<int32_t>("amg.big", std::max<int64_t>(std::max<int64_t>(L.n, NA), 1));
     int32_t* big_n = ovf + 6;
     auto n_big = [&]() {
@@ -1133,6 +1229,51 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
       RUV_CUDA(cudaStreamSynchronize(s));
       return h;
     };
+    if (!smooth) {
+      // ---- tentative prolongator: A_c = R A P straight from A
+      int32_t abig = 0;
+      if (NA > 0) {
+        RUV_CUDA(cudaMemsetAsync(big_n, 0, sizeof(int32_t), s));
+        k_rap_t<0><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rp, L.cols, L.vals64, agg, acnt, nullptr, nullptr,
+                                               nullptr, nullptr, ovf, big, big_n);
+        count_launches(1);
+        abig = n_big();
+        if (abig > 0) {
+          k_rap_t_big<0><<<(unsigned)abig, 32, 0, s>>>(big, L.roff, L.rc, L.rp, L.cols, L.vals64, agg, acnt, nullptr,
+                                                       nullptr, nullptr, nullptr, ovf);
+          count_launches(1);
+        }
+      }
+      const int64_t AN = offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao");
+      if (AN >= (int64_t)INT32_MAX) throw Error{RUV_ERR_BAD_INPUT, "coarse operator too large"};
+      C.rp = ctx.ws.get<int32_t>(ntag + ".rp", NA + 1);
+      C.cols = ctx.ws.get<int32_t>(ntag + ".cols", AN);
+      C.vals = ctx.ws.get<float>(ntag + ".vals", AN);
+      C.vals64 = ctx.ws.get<double>(ntag + ".vals64", AN);
+      C.dinv = ctx.ws.get<float>(ntag + ".dinv", NA);
+      C.nnz = AN;
+      if (NA > 0) {
+        k_rap_t<1><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rp, L.cols, L.vals64, agg, acnt, aoff, C.cols,
+                                               C.vals64, C.dinv, ovf, big, big_n);
+        if (abig > 0) {
+          k_rap_t_big<1><<<(unsigned)abig, 32, 0, s>>>(big, L.roff, L.rc, L.rp, L.cols, L.vals64, agg, acnt, aoff,
+                                                       C.cols, C.vals64, C.dinv, ovf);
+          count_launches(1);
+        }
+        k_i64_i32<<<div_up(NA + 1, B), B, 0, s>>>(NA + 1, aoff, C.rp);
+        if (AN > 0) k_f64_f32<<<div_up(AN, B), B, 0, s>>>(AN, C.vals64, C.vals);
+        count_launches(3);
+      }
+      L.n_next = NA;
+      C.h_chart_row.resize(NC + 1);
+      RUV_CUDA(cudaMemcpyAsync(C.h_chart_row.data(), C.chart_row, sizeof(int64_t) * (NC + 1), cudaMemcpyDeviceToHost, s));
+      RUV_CUDA(cudaStreamSynchronize(s));
+      H->lv.push_back(C);
+      continue;
+    }
+    // ---- smoothed prolongator: W = A P, then A_c = R W
+    int32_t* wcnt = ctx.ws.get<int32_t>(tag + ".wcnt", L.n);
+    int64_t* woff = ctx.ws.get<int64_t>(tag + ".woff", L.n + 1);
     RUV_CUDA(cudaMemsetAsync(big_n, 0, sizeof(int32_t), s));
     k_ap<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt, nullptr, nullptr,
                                          nullptr, ovf, big, big_n);
@@ -1154,8 +1295,6 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
                                                     wc, wv, nullptr, ovf);
       count_launches(1);
     }
-    int32_t* acnt = ctx.ws.get<int32_t>(ntag + ".acnt", NA);
-    int64_t* aoff = ctx.ws.get<int64_t>(ntag + ".aoff", NA + 1);
     int32_t abig = 0;
     if (NA > 0) {
       RUV_CUDA(cudaMemsetAsync(big_n, 0, sizeof(int32_t), s));
