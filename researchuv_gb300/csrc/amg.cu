@@ -777,9 +777,9 @@ struct RowIn {
 };
 
 // Generic: for each row i of the tile, s = sum_e w(e) * g(col(e)); then fin(i, s).
-template <int NR, int LPR, int U, int K, class W, class G, class Fin>
-__device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_t* ptr64, const int32_t* ptr32,
-                                          const int32_t* __restrict__ cols, W w, G g, Fin fin) {
+template <int NR, int LPR, int U, int K, class Col, class W, class G, class Fin>
+__device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_t* ptr64, const int32_t* ptr32, Col cols,
+                                          W w, G g, Fin fin) {
   const int sub = threadIdx.x % LPR;
   const int rpp = kAmgThreads / LPR;
   for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
@@ -800,7 +800,7 @@ __device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_
         const int64_t e = lo[u] + sub + k * LPR;
         const bool in = e < hi[u];
         av[u][k] = in ? w(e) : 0.0f;
-        cv[u][k] = in ? cols[e] : -1;
+        cv[u][k] = in ? cols(e) : -1;
       }
     F<NR> s[U];
 #pragma unroll
@@ -816,7 +816,7 @@ __device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_
         }
       for (int64_t e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {
         const float a = w(e);
-        const F<NR> v = g(cols[e]);
+        const F<NR> v = g(cols(e));
 #pragma unroll
         for (int c = 0; c < NR; ++c) s[u].c[c] += a * v.c[c];
       }
@@ -834,16 +834,20 @@ __device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_
 }
 
 // Down 1: x = w D^-1 b;  t = b - A x  (x of neighbours formed on the fly).
-template <int NR, int LPR, int U, int K>
+template <int NR, int LPR, int U, int K, bool NARROW>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const int32_t* __restrict__ done,
                                                              const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                                             const uint16_t* __restrict__ c16,
+                                                             const int32_t* __restrict__ cbase,
                                                              const float* __restrict__ vals, const float* __restrict__ dinv,
                                                              const float* __restrict__ b, float* __restrict__ x,
                                                              float* __restrict__ t) {
   const int64_t tl = blockIdx.x;
-  if (done[T.chart[tl]]) return;
+  const int32_t ch = T.chart[tl];
+  if (done[ch]) return;
+  auto run = [&](auto colf) {
   tile_rows<NR, LPR, U, K>(
-      T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, cols, [&](int64_t e) { return vals[e]; },
+      T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, colf, [&](int64_t e) { return vals[e]; },
       [&](int32_t j) {
         F<NR> v = ldf<NR>(b, j);
         const float wd = kOmega * dinv[j];
@@ -863,6 +867,9 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const i
         if (x) stf<NR>(x, i, xi);  // (the tentative-P cycle forms it again on the way up)
         stf<NR>(t, i, ti);
       });
+  };
+  if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
+  else run(ColsWide{cols});
 }
 
 // Restrict: b_c = R t over the coarse rows (tiles of the coarse level).
@@ -874,7 +881,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_restrict(LvlTiles T, const int3
   const int64_t tl = blockIdx.x;
   if (done[T.chart[tl]]) return;
   tile_rows<NR, LPR, U, K>(
-      T.tab[2 * tl], T.tab[2 * tl + 1], roff, nullptr, rc, [&](int64_t e) { return rv[e]; },
+      T.tab[2 * tl], T.tab[2 * tl + 1], roff, nullptr, ColsWide{rc}, [&](int64_t e) { return rv[e]; },
       [&](int32_t j) { return ldf<NR>(t, j); }, [&](int64_t I, const F<NR>& s) { stf<NR>(bc, I, s); });
 }
 
@@ -888,7 +895,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_prolong_add(LvlTiles T, const i
   const int64_t tl = blockIdx.x;
   if (done[T.chart[tl]]) return;
   tile_rows<NR, LPR, U, K>(
-      T.tab[2 * tl], T.tab[2 * tl + 1], poff, nullptr, pc, [&](int64_t e) { return alpha_c * pv[e]; },
+      T.tab[2 * tl], T.tab[2 * tl + 1], poff, nullptr, ColsWide{pc}, [&](int64_t e) { return alpha_c * pv[e]; },
       [&](int32_t j) { return ldf<NR>(xc, j); },
       [&](int64_t i, const F<NR>& s) {
         F<NR> xi = ldf<NR>(x, i);
@@ -899,16 +906,20 @@ __global__ void __launch_bounds__(kAmgThreads) k_prolong_add(LvlTiles T, const i
 }
 
 // Up 2: x = y + w D^-1 (b - A y).
-template <int NR, int LPR, int U, int K>
+template <int NR, int LPR, int U, int K, bool NARROW>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int32_t* __restrict__ done,
                                                            const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                                           const uint16_t* __restrict__ c16,
+                                                           const int32_t* __restrict__ cbase,
                                                            const float* __restrict__ vals, const float* __restrict__ dinv,
                                                            const float* __restrict__ b, const float* __restrict__ y,
                                                            float* __restrict__ x) {
   const int64_t tl = blockIdx.x;
-  if (done[T.chart[tl]]) return;
+  const int32_t ch = T.chart[tl];
+  if (done[ch]) return;
+  auto run = [&](auto colf) {
   tile_rows<NR, LPR, U, K>(
-      T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, cols, [&](int64_t e) { return vals[e]; },
+      T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, colf, [&](int64_t e) { return vals[e]; },
       [&](int32_t j) { return ldf<NR>(y, j); },
       [&](int64_t i, const F<NR>& s) {
         const F<NR> bi = ldf<NR>(b, i), yi = ldf<NR>(y, i);
@@ -918,21 +929,27 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int
         for (int c = 0; c < NR; ++c) xi.c[c] = yi.c[c] + wd * (bi.c[c] - s.c[c]);
         stf<NR>(x, i, xi);
       });
+  };
+  if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
+  else run(ColsWide{cols});
 }
 
 // Up, tentative prolongator (one 1 per row at agg[i]): the prolongation and the
 // post-smoothing in one pass, x = y + w D^-1 (b - A y) with y_j = w D^-1_j b_j +
 // alpha_c x_c[agg[j]] formed on the fly for every neighbour (the pre-smoothed x is not
 // stored and y is never written).
-template <int NR, int LPR, int U, int K>
+template <int NR, int LPR, int U, int K, bool NARROW>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_up_t(LvlTiles T, const int32_t* __restrict__ done,
                                                              const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                                             const uint16_t* __restrict__ c16,
+                                                             const int32_t* __restrict__ cbase,
                                                              const float* __restrict__ vals, const float* __restrict__ dinv,
                                                              const float* __restrict__ b, const int32_t* __restrict__ agg,
                                                              const float* __restrict__ xc, float alpha_c,
                                                              float* __restrict__ x) {
   const int64_t tl = blockIdx.x;
-  if (done[T.chart[tl]]) return;
+  const int32_t ch = T.chart[tl];
+  if (done[ch]) return;
   auto yval = [&](int64_t j) {
     F<NR> v = ldf<NR>(b, j);
     const float wd = kOmega * dinv[j];
@@ -941,8 +958,9 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up_t(LvlTiles T, const i
     for (int k = 0; k < NR; ++k) v.c[k] = wd * v.c[k] + alpha_c * c.c[k];
     return v;
   };
+  auto run = [&](auto colf) {
   tile_rows<NR, LPR, U, K>(
-      T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, cols, [&](int64_t e) { return vals[e]; },
+      T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, colf, [&](int64_t e) { return vals[e]; },
       [&](int32_t j) { return yval(j); },
       [&](int64_t i, const F<NR>& s) {
         const F<NR> bi = ldf<NR>(b, i), yi = yval(i);
@@ -952,6 +970,9 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up_t(LvlTiles T, const i
         for (int c = 0; c < NR; ++c) xi.c[c] = yi.c[c] + wd * (bi.c[c] - s.c[c]);
         stf<NR>(x, i, xi);
       });
+  };
+  if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
+  else run(ColsWide{cols});
 }
 
 // Direct solve of every chart at its last level: x = A^-1 b with the dense inverse (one CTA
@@ -1018,6 +1039,8 @@ struct AmgLevelDev {
   float* rv = nullptr;
   float *b = nullptr, *x = nullptr, *y = nullptr, *t = nullptr;
   int32_t* agg = nullptr;  // aggregate of each row (the tentative prolongator), -1 if none
+  const uint16_t* c16 = nullptr;  // 16-bit column stream (level 0), see ColsNarrow
+  const int32_t* cbase = nullptr;
   LvlTiles cont{nullptr, nullptr, 0};  // tiles over rows whose chart continues below this level
   LvlTiles all{nullptr, nullptr, 0};   // tiles over every row of this level
 };
@@ -1084,6 +1107,8 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     L0.cols = sys.cols;
     L0.vals = sys.vals32;
     L0.vals64 = sys.vals;
+    L0.c16 = sys.cols16;
+    L0.cbase = sys.cbase;
     L0.dinv = ctx.ws.get<float>("amg.l0.dinv", L0.n);
     if (L0.n > 0) {
       k_f64_f32_inv<<<div_up(L0.n, B), B, 0, s>>>(L0.n, sys.diag, L0.dinv);
@@ -1489,10 +1514,16 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
     if (L.cont.n == 0) continue;
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
     float* xpre = H->smoothed ? L.x : nullptr;  // the tentative cycle re-forms it on the way up
-#define CALL(X, UU, KK)                                                                                              \
-  k_smooth_down<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, xpre, \
-                                                            L.t)
-    RUV_LPR_SWITCH(la, CALL)
+#define CALL(X, UU, KK)                                                                                                \
+  k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
+                                                                    L.dinv, L.b, xpre, L.t)
+    if (L.c16) {
+      constexpr bool NW = true;
+      RUV_LPR_SWITCH(la, CALL)
+    } else {
+      constexpr bool NW = false;
+      RUV_LPR_SWITCH(la, CALL)
+    }
 #undef CALL
     ++launches;
     if (C.all.n == 0) continue;
@@ -1515,10 +1546,16 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
     if (L.cont.n == 0) continue;
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
     if (!H->smoothed) {
-#define CALL(X, UU, KK)                                                                                                 \
-  k_smooth_up_t<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.agg, \
-                                                              C.x, H->alpha_c, L.x)
-      RUV_LPR_SWITCH(la, CALL)
+#define CALL(X, UU, KK)                                                                                                \
+  k_smooth_up_t<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
+                                                                    L.dinv, L.b, L.agg, C.x, H->alpha_c, L.x)
+      if (L.c16) {
+        constexpr bool NW = true;
+        RUV_LPR_SWITCH(la, CALL)
+      } else {
+        constexpr bool NW = false;
+        RUV_LPR_SWITCH(la, CALL)
+      }
 #undef CALL
       ++launches;
       continue;
@@ -1529,9 +1566,16 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
                                                             H->alpha_c)
     RUV_LPR_SWITCH(lp, CALL)
 #undef CALL
-#define CALL(X, UU, KK) \
-  k_smooth_up<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.vals, L.dinv, L.b, L.y, L.x)
-    RUV_LPR_SWITCH(la, CALL)
+#define CALL(X, UU, KK)                                                                                              \
+  k_smooth_up<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
+                                                                  L.dinv, L.b, L.y, L.x)
+    if (L.c16) {
+      constexpr bool NW = true;
+      RUV_LPR_SWITCH(la, CALL)
+    } else {
+      constexpr bool NW = false;
+      RUV_LPR_SWITCH(la, CALL)
+    }
 #undef CALL
     launches += 2;
   }

@@ -128,6 +128,20 @@ __device__ __forceinline__ float warp_sum(float v) {
 // NV * 32 values.  Fixed combine order => bitwise reproducible for a fixed launch shape.
 // (GB300 runs FP64 at a small fraction of the FP32 rate: the per-element loops of the
 // FP32 solver reduce in float and widen once per tile.)
+// Column-index streams of a CSR operator: 32-bit global row ids, or -- for a chart of at most
+// 65536 rows -- 16-bit offsets from the chart's first row, 2 bytes less per non-zero in every
+// pass that streams the operator.  A tile never spans two charts, so a kernel picks the
+// stream once per tile.
+struct ColsWide {
+  const int32_t* c;
+  __device__ __forceinline__ int32_t operator()(int64_t e) const { return c[e]; }
+};
+struct ColsNarrow {
+  const uint16_t* c;
+  int32_t base;
+  __device__ __forceinline__ int32_t operator()(int64_t e) const { return base + (int32_t)c[e]; }
+};
+
 template <int NV, class A>
 __device__ __forceinline__ void block_sum_t(A (&v)[NV], A* sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;

@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 namespace ruv {
@@ -211,24 +212,14 @@ __global__ void __launch_bounds__(kTileThreads) k_init(Tiles T, const double* __
   }
 }
 
-// q = A p on the tile's rows fused with the partial p.q.  CSR-vector: LPR lanes per row,
-// each lane covering K = ceil(8 / LPR) entries in one unrolled sweep (rows of a mesh
-// Laplacian hold <= 8 entries almost always; longer rows finish in a remainder loop), U rows
-// per sub-warp in flight so a warp keeps U * K independent value/column loads and U * K
-// gathers outstanding.  Block-uniform trip counts keep every lane in the shuffles.
-template <class S, int NR, int LPR, int U>
-__global__ void __launch_bounds__(kTileThreads) k_spmv_pq(Tiles T, const ChartState* __restrict__ st,
-                                                          const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
-                                                          const S* __restrict__ vals, const S* __restrict__ p,
-                                                          S* __restrict__ q, double* __restrict__ part) {
+// The row loop of one SpMV tile (see k_spmv_pq); `col` maps an entry to its column.
+template <class S, int NR, int LPR, int U, class Col>
+__device__ __forceinline__ void spmv_pq_tile(int64_t beg, int64_t end, const int32_t* __restrict__ row_ptr, Col col,
+                                             const S* __restrict__ vals, const S* __restrict__ p, S* __restrict__ q,
+                                             S (&acc)[1]) {
   constexpr int K = (8 + LPR - 1) / LPR;
-  __shared__ S sh[32];
-  const int64_t t = blockIdx.x;
-  if (st[T.chart[t]].state != kActive) return;
   const int sub = threadIdx.x % LPR;
   const int rpp = kTileThreads / LPR;
-  S acc[1] = {S(0)};
-  const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
   for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
     int lo[U], hi[U];
 #pragma unroll
@@ -247,7 +238,7 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_pq(Tiles T, const ChartSt
         const int e = lo[u] + sub + k * LPR;
         const bool in = e < hi[u];
         av[u][k] = in ? vals[e] : S(0);
-        cv[u][k] = in ? cols[e] : -1;
+        cv[u][k] = in ? col(e) : -1;
       }
     V<S, NR> s[U];
 #pragma unroll
@@ -263,7 +254,7 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_pq(Tiles T, const ChartSt
         }
       for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {  // rows longer than K * LPR
         const S a = vals[e];
-        const V<S, NR> pv = ldv<S, NR>(p, cols[e]);
+        const V<S, NR> pv = ldv<S, NR>(p, col(e));
 #pragma unroll
         for (int c = 0; c < NR; ++c) s[u].c[c] += a * pv.c[c];
       }
@@ -287,8 +278,42 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_pq(Tiles T, const ChartSt
       }
     }
   }
+}
+
+// q = A p on the tile's rows fused with the partial p.q.  CSR-vector: LPR lanes per row,
+// each lane covering K = ceil(8 / LPR) entries in one unrolled sweep (rows of a mesh
+// Laplacian hold <= 8 entries almost always; longer rows finish in a remainder loop), U rows
+// per sub-warp in flight so a warp keeps U * K independent value/column loads and U * K
+// gathers outstanding.  Block-uniform trip counts keep every lane in the shuffles.  The
+// column stream is 16-bit where the tile's chart has one (cbase >= 0).
+template <class S, int NR, int LPR, int U, bool NARROW>
+__global__ void __launch_bounds__(kTileThreads) k_spmv_pq_k(Tiles T, const ChartState* __restrict__ st,
+                                                            const int32_t* __restrict__ row_ptr,
+                                                            const int32_t* __restrict__ cols,
+                                                            const uint16_t* __restrict__ c16,
+                                                            const int32_t* __restrict__ cbase, const S* __restrict__ vals,
+                                                            const S* __restrict__ p, S* __restrict__ q,
+                                                            double* __restrict__ part) {
+  __shared__ S sh[32];
+  const int64_t t = blockIdx.x;
+  const int32_t ch = T.chart[t];
+  if (st[ch].state != kActive) return;
+  S acc[1] = {S(0)};
+  const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
+  if constexpr (NARROW) spmv_pq_tile<S, NR, LPR, U>(beg, end, row_ptr, ColsNarrow{c16, cbase[ch]}, vals, p, q, acc);
+  else spmv_pq_tile<S, NR, LPR, U>(beg, end, row_ptr, ColsWide{cols}, vals, p, q, acc);
   block_sum_t<1, S>(acc, sh);
   if (threadIdx.x == 0) part[t] = (double)acc[0];
+}
+
+// One launch of the SpMV: the 16-bit column instance when the system has that stream (every
+// chart of at most 65536 rows), the 32-bit one otherwise.
+template <class S, int NR, int LPR, int U>
+void launch_spmv(cudaStream_t s, unsigned grid, Tiles T, const ChartState* st, const int32_t* row_ptr,
+                 const int32_t* cols, const uint16_t* c16, const int32_t* cbase, const S* vals, const S* p, S* q,
+                 double* part) {
+  if (c16) k_spmv_pq_k<S, NR, LPR, U, true><<<grid, kTileThreads, 0, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q, part);
+  else k_spmv_pq_k<S, NR, LPR, U, false><<<grid, kTileThreads, 0, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q, part);
 }
 
 // x += alpha p; r -= alpha q; z = M^-1 r.  Partials: r.r, r.z.  precond: 0 = none (z = r),
@@ -398,10 +423,12 @@ __global__ void __launch_bounds__(kTileThreads) k_fold(Tiles T, const ChartState
 // r32 = r, z = M^-1 r (precond 0: z = r, 1: Jacobi, 2: applied separately, z not written).
 // Partials: r.r and r.z, summed in FP32 over r * rscale and rescaled per tile.  The CSR-vector
 // shape (LPR lanes, K = ceil(8 / LPR) slots, U rows in flight) is the tuned SpMV's.
-template <int NR, int LPR, int U>
+template <int NR, int LPR, int U, bool NARROW>
 __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const ChartState* __restrict__ st,
                                                                 const int32_t* __restrict__ row_ptr,
-                                                                const int32_t* __restrict__ cols, const float* __restrict__ vh,
+                                                                const int32_t* __restrict__ cols,
+                                                                const uint16_t* __restrict__ c16,
+                                                                const int32_t* __restrict__ cbase, const float* __restrict__ vh,
                                                                 const float* __restrict__ vl, const float2* __restrict__ rsum,
                                                                 const float* __restrict__ bdf, const float* __restrict__ dinv,
                                                                 int precond, const float* __restrict__ xdf,
@@ -417,6 +444,7 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
   const int rpp = kTileThreads / LPR;
   float acc[2] = {0.0f, 0.0f};
   const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
+  auto run = [&](auto col) {
   for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
     int lo[U], hi[U];
     DF<NR> xi[U];
@@ -438,7 +466,7 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
         const bool in = e < hi[u];
         ah[u][k] = in ? vh[e] : 0.0f;
         al[u][k] = in ? vl[e] : 0.0f;
-        cv[u][k] = in ? cols[e] : -1;
+        cv[u][k] = in ? col(e) : -1;
       }
     float Sh[U][NR], Sl[U][NR];
 #pragma unroll
@@ -458,7 +486,7 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
 #pragma unroll
       for (int k = 0; k < K; ++k)
         if (cv[u][k] >= 0) entry(ah[u][k], al[u][k], cv[u][k]);
-      for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) entry(vh[e], vl[e], cols[e]);
+      for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) entry(vh[e], vl[e], col(e));
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -502,6 +530,9 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
       }
     }
   }
+  };
+  if constexpr (NARROW) run(ColsNarrow{c16, cbase[T.chart[t]]});
+  else run(ColsWide{cols});
   block_sum_t<2, float>(acc, sh);
   if (threadIdx.x == 0) {
     const double inv = 1.0 / ((double)rsc * (double)rsc);
@@ -855,7 +886,7 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
     cudaGraphExec_t exec = nullptr;
     RUV_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int rep = 0; rep < kCheckEvery; ++rep) {
-      k_spmv_pq<S, NR, LPR, U><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, p, q, part);
+      launch_spmv<S, NR, LPR, U>(s, (unsigned)NTL, T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, vals, p, q, part);
       k_chart_alpha<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, n_active);
       k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, dinv, jac, mixed ? xs : reinterpret_cast<S*>(x64), r,
                                                              z, p, q, part);
@@ -864,9 +895,14 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
       } else {
         k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0);
         k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, mx.xdf, reinterpret_cast<float*>(xs), x64);
-        k_true_residual<NR, LPR, U><<<(unsigned)NTL, kTileThreads, 0, s>>>(
-            T, st, sys.row_ptr, sys.cols, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, jac, mx.xdf,
-            reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
+        if (sys.cols16)
+          k_true_residual<NR, LPR, U, true><<<(unsigned)NTL, kTileThreads, 0, s>>>(
+              T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, jac,
+              mx.xdf, reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
+        else
+          k_true_residual<NR, LPR, U, false><<<(unsigned)NTL, kTileThreads, 0, s>>>(
+              T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, jac,
+              mx.xdf, reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
         k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0);
       }
       k_direction<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
@@ -978,15 +1014,20 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
     RUV_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int rep = 0; rep < kRep; ++rep) {
       int l = 0;
-      k_spmv_pq<S, NR, LPR, U><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, p, q, part);
+      launch_spmv<S, NR, LPR, U>(s, (unsigned)NTL, T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, vals, p, q, part);
       k_chart_alpha<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, n_active);
       k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, dinv, 2, xiter, r, z, p, q, part);
       if (mixed) {
         k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1);
         k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, mx.xdf, reinterpret_cast<float*>(xs), x64);
-        k_true_residual<NR, LPR, U><<<(unsigned)NTL, kTileThreads, 0, s>>>(
-            T, st, sys.row_ptr, sys.cols, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, 2, mx.xdf,
-            reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
+        if (sys.cols16)
+          k_true_residual<NR, LPR, U, true><<<(unsigned)NTL, kTileThreads, 0, s>>>(
+              T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, 2,
+              mx.xdf, reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
+        else
+          k_true_residual<NR, LPR, U, false><<<(unsigned)NTL, kTileThreads, 0, s>>>(
+              T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, 2,
+              mx.xdf, reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
         k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1);
         l += 4;
       } else {
@@ -1100,8 +1141,8 @@ double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
   }
   const S* vals = std::is_same<S, float>::value ? reinterpret_cast<const S*>(sys.vals32) : reinterpret_cast<const S*>(sys.vals);
   auto launch = [&](int k) {
-    k_spmv_pq<S, NR, LPR, U><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, vals, ps[k % nbuf],
-                                                                    qs[k % nbuf], part);
+    launch_spmv<S, NR, LPR, U>(s, (unsigned)T.n, T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, vals, ps[k % nbuf],
+                               qs[k % nbuf], part);
     count_launches(1);
   };
   for (int k = 0; k < 3; ++k) launch(k);
@@ -1156,14 +1197,87 @@ TileTable make_tiles(const std::vector<int64_t>& chart_row, int64_t tile_rows) {
   return T;
 }
 
+// 16-bit column stream: entries of charts of at most 65536 rows as offsets from the chart's
+// first row (one thread per row); cbase = the first row of such a chart, -1 otherwise.
+constexpr int64_t kNarrowRows = 65536;
+__global__ void k_narrow_cols(int64_t n, const int64_t* __restrict__ chart_row, int64_t n_charts,
+                              const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
+                              uint16_t* __restrict__ c16) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int64_t lo = 0, hi = n_charts;  // the chart of row i: largest c with chart_row[c] <= i
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (chart_row[mid] <= i) lo = mid; else hi = mid;
+  }
+  const int64_t r0 = chart_row[lo];
+  if (chart_row[lo + 1] - r0 > kNarrowRows) return;
+  for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) c16[e] = (uint16_t)(cols[e] - r0);
+}
+__global__ void k_chart_entry(int64_t n_charts, const int64_t* __restrict__ chart_row, const int32_t* __restrict__ row_ptr,
+                              int32_t* __restrict__ out) {  // the first entry of every chart (and the end)
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c <= n_charts) out[c] = row_ptr[chart_row[c]];
+}
+__global__ void k_chart_base(int64_t n_charts, const int64_t* __restrict__ chart_row, int32_t* __restrict__ cbase) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n_charts) cbase[c] = chart_row[c + 1] - chart_row[c] <= kNarrowRows ? (int32_t)chart_row[c] : -1;
+}
+
 }  // namespace
 
+// Off unless RUV_NARROW_COLS=1: on the 4096-disk operator the 16-bit stream cuts the SpMV's
+// bytes by 18% and its time by 8% (0.215 -> 0.187 ms), the AMG solve by 1.7%; the kernel then
+// moves fewer bytes at a lower fraction of the HBM bandwidth.
+void narrow_columns(Ctx& ctx, DevSystem& sys) {
+  const char* e = std::getenv("RUV_NARROW_COLS");
+  if (!e || e[0] != '1') {  // 32-bit columns only
+    sys.cols16 = nullptr;
+    sys.cbase = nullptr;
+    return;
+  }
+  cudaStream_t s = ctx.stream;
+  const int64_t N = sys.n_rows, NC = sys.n_charts;
+  for (int64_t c = 0; c < NC; ++c)
+    if (sys.h_chart_row[c + 1] - sys.h_chart_row[c] > kNarrowRows) {  // a large chart: 32-bit columns
+      sys.cols16 = nullptr;
+      sys.cbase = nullptr;
+      return;
+    }
+  sys.cols16 = ctx.ws.get<uint16_t>("sys.cols16", std::max<int64_t>(sys.nnz, 1));
+  sys.cbase = ctx.ws.get<int32_t>("sys.cbase", std::max<int64_t>(NC, 1));
+  if (N > 0) {
+    k_narrow_cols<<<div_up(N, 256), 256, 0, s>>>(N, sys.chart_row, NC, sys.row_ptr, sys.cols, sys.cols16);
+    count_launches(1);
+  }
+  if (NC > 0) {
+    k_chart_base<<<div_up(NC, 256), 256, 0, s>>>(NC, sys.chart_row, sys.cbase);
+    count_launches(1);
+  }
+  RUV_LAUNCH_CHECK();
+}
+
 double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes) {
+  narrow_columns(ctx, sys);
   Tiles T = upload_tiles(ctx, sys, "bench");
   const Shape sh = pick_shape(ctx, sys);
   const double N = (double)sys.n_rows, NNZ = (double)sys.nnz, nr = (double)sys.nrhs;
   const double vb = mixed ? 4.0 : 8.0;
-  if (bytes) *bytes = NNZ * (vb + 4.0) + (N + 1.0) * 4.0 + 2.0 * N * nr * vb;
+  // column bytes per entry: 2 for charts with the 16-bit stream, 4 otherwise
+  double cb = 4.0;
+  if (sys.cols16 && sys.n_charts > 0) {
+    double narrow_nnz = 0.0;
+    std::vector<int32_t> rp(sys.n_charts + 1);
+    int32_t* d_rp = ctx.ws.get<int32_t>("bench.chart_nnz", sys.n_charts + 1);
+    k_chart_entry<<<div_up(sys.n_charts + 1, 256), 256, 0, ctx.stream>>>(sys.n_charts, sys.chart_row, sys.row_ptr, d_rp);
+    count_launches(1);
+    RUV_CUDA(cudaMemcpyAsync(rp.data(), d_rp, sizeof(int32_t) * (sys.n_charts + 1), cudaMemcpyDeviceToHost, ctx.stream));
+    RUV_CUDA(cudaStreamSynchronize(ctx.stream));
+    for (int64_t c = 0; c < sys.n_charts; ++c)
+      if (sys.h_chart_row[c + 1] - sys.h_chart_row[c] <= kNarrowRows) narrow_nnz += (double)(rp[c + 1] - rp[c]);
+    cb = NNZ > 0 ? (2.0 * narrow_nnz + 4.0 * (NNZ - narrow_nnz)) / NNZ : 4.0;
+  }
+  if (bytes) *bytes = NNZ * (vb + cb) + (N + 1.0) * 4.0 + 2.0 * N * nr * vb;
   if (T.n == 0) return 0.0;
   if (sys.nrhs == 2)
     return mixed ? dispatch_time<float, 2>(sh, ctx, sys, T, reps, n_buffers)
@@ -1174,6 +1288,7 @@ double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers,
 // Autotuner: time the batched SpMV for every instantiated (lanes per row, rows in flight)
 // shape and tile height on the assembled operator; keep the fastest in the context.
 TuneResult autotune_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps) {
+  narrow_columns(ctx, sys);
   TuneResult best{0, 0, 0, 1e30};
   const int tiles[] = {128, 256, 512, 1024};
   const Shape shapes[] = {
@@ -1209,6 +1324,7 @@ std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const So
   if (o.precond != RUV_PRECOND_NONE && o.precond != RUV_PRECOND_JACOBI && !sep)
     throw Error{RUV_ERR_BAD_INPUT, "unknown preconditioner"};
   const int64_t NC = sys.n_charts;
+  narrow_columns(ctx, sys);
   Tiles T = upload_tiles(ctx, sys, "pcg");
   ChartState* st = ctx.ws.get<ChartState>("pcg.state", NC);
   int* n_active = ctx.ws.get<int>("pcg.nactive", 1);
@@ -1347,8 +1463,8 @@ void na_message(char* msg, int32_t len, const char* text) {
 template <int LPR, int U>
 void na_iterations(cudaStream_t s, NoAllocScratch* S, Tiles T, const int32_t* row_ptr, const int32_t* cols,
                    const double* vals, double* x, int jac, int none, int64_t max_iter) {
-  k_spmv_pq<double, 1, LPR, U><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, &S->st, row_ptr, cols, vals, S->p, S->q,
-                                                                     S->part);
+  k_spmv_pq_k<double, 1, LPR, U, false><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, &S->st, row_ptr, cols, nullptr, nullptr,
+                                                                              vals, S->p, S->q, S->part);
   k_chart_alpha<<<1, kChartThreads, 0, s>>>(T, &S->st, S->part, &S->n_active);
   k_update<double, 1><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, &S->st, S->dinv, jac, x, S->r, S->z, S->p, S->q, S->part);
   k_chart_beta<<<1, kChartThreads, 0, s>>>(T, &S->st, S->part, none, max_iter, &S->n_active);

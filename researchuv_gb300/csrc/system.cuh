@@ -23,6 +23,8 @@ struct DevSystem {
   int32_t* cols = nullptr;       // nnz (global row ids)
   double* vals = nullptr;        // nnz, FP64
   float* vals32 = nullptr;       // nnz, FP32 copy for the mixed-precision inner loop
+  uint16_t* cols16 = nullptr;    // nnz: column - first row of the chart (charts of <= 65536 rows)
+  int32_t* cbase = nullptr;      // n_charts: first row of a chart with cols16, -1 otherwise
   double* diag = nullptr;        // n_rows
   double* b = nullptr;           // nrhs * n_rows
 };
@@ -72,6 +74,9 @@ std::unique_ptr<SepPrecond> make_ic0(Ctx& ctx, const DevSystem& sys, bool colore
 void ic0_apply_once(Ctx& ctx, const DevSystem& sys, const double* d_r, double* d_z, int* fwd_levels);
 void ic0_export(Ctx& ctx, const DevSystem& sys, bool colored, std::vector<int64_t>& ptr, std::vector<int32_t>& cols,
                 std::vector<double>& vals, std::vector<int32_t>& to_orig, int& levels, int& colours);
+
+// The 16-bit column stream of `sys` (cols16, cbase), built on the device.
+void narrow_columns(Ctx& ctx, DevSystem& sys);
 
 // x (nrhs * n_rows, device) <- A^-1 b per chart.  Returns per-chart results (host).
 std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o);

@@ -216,3 +216,18 @@ def test_cg_amg_poisson_and_elongated(known):
     for i in [0, 100_000, 199_999]:
         assert abs(r[0][i] - x_none[i]) < 1e-5
     assert r[1] < it_none
+
+
+def test_batched_disks_16bit_columns(monkeypatch):
+    """The 16-bit column stream (RUV_NARROW_COLS=1) gives bitwise the same UVs as the 32-bit one."""
+    vo, to, p3, tr = W.disks(16, t_min=200, t_max=6000, seed=17)
+    C = R.prepare_patches(vo, to, p3, tr)
+    ctx = R.Context(0)
+    for pc in (R.Precond.JACOBI, R.Precond.AMG):
+        monkeypatch.delenv("RUV_NARROW_COLS", raising=False)
+        wide = R.unfold_charts(ctx, C, R.UnfoldOptions(precond=pc))
+        monkeypatch.setenv("RUV_NARROW_COLS", "1")
+        narrow = R.unfold_charts(ctx, C, R.UnfoldOptions(precond=pc))
+        for a, b in zip(wide, narrow):
+            assert a.status == b.status == R.Status.OK
+            assert np.array_equal(a.uv, b.uv)
