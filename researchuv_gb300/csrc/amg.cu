@@ -21,6 +21,7 @@
 // pass), b_c = R t; direct solves of every chart at its own last level (one CTA per chart);
 // up: x += P x_c, x' = x + w D^-1 (b - A x).  Charts whose CG has converged are skipped.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -390,241 +391,252 @@ __global__ void k_sort_rows(int64_t n, const int64_t* __restrict__ off, int32_t*
   }
 }
 
-// W = A P (rows of active fine rows).  MODE 0 count / 1 fill.
-template <int MODE>
-__global__ void k_ap(int64_t n, const uint8_t* __restrict__ active, const int32_t* __restrict__ rp,
-                     const int32_t* __restrict__ cols, const double* __restrict__ vals, const int64_t* __restrict__ poff,
-                     const int32_t* __restrict__ pc, const float* __restrict__ pv, int32_t* __restrict__ cnt,
-                     const int64_t* __restrict__ woff, int32_t* __restrict__ wc, double* __restrict__ wv,
-                     int* __restrict__ overflow, int32_t* __restrict__ big, int32_t* __restrict__ big_n) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (!active[i]) {
-    if (MODE == 0) cnt[i] = 0;
-    return;
-  }
-  Acc<kGalCap, double> acc;
-  for (int e = rp[i]; e < rp[i + 1]; ++e) {
-    const int32_t j = cols[e];
-    const double a = vals[e];
-    for (int64_t q = poff[j]; q < poff[j + 1]; ++q) acc.add(pc[q], a * (double)pv[q]);
-  }
-  atomicMax(overflow + 4, acc.n);
-  if (acc.overflow) {  // handed to k_gal_big (listed once, in the counting pass)
-    if (MODE == 0) {
-      cnt[i] = 0;
-      big[atomicAdd(big_n, 1)] = (int32_t)i;
-    }
-    return;
-  }
-  acc.sort();
-  if (MODE == 0) {
-    cnt[i] = acc.n;
-  } else {
-    int64_t at = woff[i];
-    for (int t = 0; t < acc.n; ++t) {
-      wc[at + t] = acc.key[t];
-      wv[at + t] = acc.val[t];
-    }
-  }
-}
+// ---------------------------------------------------------------- sparse products (Galerkin)
+// Row `row` of a two-level product: for each outer entry q of the row (index j, scale s_q, in
+// order) and each inner entry r of row j (in order), the product s_q * v_r under the key
+// key(idx_r); equal keys summed in that arrival order.  W = A P (outer A, inner P),
+// A_c = R W (outer R, inner W), and A_c = R A P_t for the tentative prolongator (outer R,
+// inner A with keys through agg).  Output rows hold their keys ascending with the sums (DIAG:
+// also the inverse of the entry on the diagonal).
+//
+// G lanes per row (32 / G rows per warp).  The lanes take G consecutive products at a time
+// (the owner outer entry of each found by a binary search over the scanned inner lengths,
+// so the inner loads are contiguous), insert the keys into the row's open-addressing table
+// of H slots in shared memory, and the lowest lane of every group of equal keys adds the
+// group's products to the slot in lane order -- the arrival order, so the sums are those of a
+// sequential accumulator and deterministic.  The occupied slots are then compacted and each
+// ranked by counting smaller keys.
+//   MODE 2 (one evaluation): writes the row to a staging area of H/2 entries per row, or, if
+//          it has more distinct keys, lists it (sn = -1) for the large-table kernel;
+//   MODE 0 / 1: counts / writes at off[row] (the large-table kernel, rows from the list).
+struct KeyId {
+  __device__ __forceinline__ int32_t operator()(int32_t k) const { return k; }
+};
+struct KeyAgg {
+  const int32_t* agg;
+  __device__ __forceinline__ int32_t operator()(int32_t k) const { return agg[k]; }
+};
 
-// A_c = R W (coarse rows).  MODE 0 count / 1 fill (also the coarse diagonal inverse).
-template <int MODE>
-__global__ void k_rw(int64_t nc, const int64_t* __restrict__ roff, const int32_t* __restrict__ rc,
-                     const float* __restrict__ rv, const int64_t* __restrict__ woff, const int32_t* __restrict__ wc,
-                     const double* __restrict__ wv, int32_t* __restrict__ cnt, const int64_t* __restrict__ aoff,
-                     int32_t* __restrict__ ac, double* __restrict__ av, float* __restrict__ adinv,
-                     int* __restrict__ overflow, int32_t* __restrict__ big, int32_t* __restrict__ big_n) {
-  int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (I >= nc) return;
-  Acc<kGalCap, double> acc;
-  for (int64_t q = roff[I]; q < roff[I + 1]; ++q) {
-    const int32_t i = rc[q];
-    const double r = rv[q];
-    for (int64_t e = woff[i]; e < woff[i + 1]; ++e) acc.add(wc[e], r * wv[e]);
-  }
-  atomicMax(overflow + 5, acc.n);
-  if (acc.overflow) {
-    if (MODE == 0) {
-      cnt[I] = 0;
-      big[atomicAdd(big_n, 1)] = (int32_t)I;
-    }
-    return;
-  }
-  acc.sort();
-  if (MODE == 0) {
-    cnt[I] = acc.n;
-  } else {
-    int64_t at = aoff[I];
-    double d = 0.0;
-    for (int t = 0; t < acc.n; ++t) {
-      ac[at + t] = acc.key[t];
-      av[at + t] = acc.val[t];
-      if (acc.key[t] == (int32_t)I) d = acc.val[t];
-    }
-    adinv[I] = d > 0.0 ? (float)(1.0 / d) : 0.0f;
-  }
-}
+template <int G, int H>
+struct GalSmem {
+  static constexpr int HS = H / 2;  // distinct keys a row may hold
+  static constexpr size_t bytes = sizeof(double) * (H + G) + sizeof(int32_t) * (H + 2 * HS);
+};
 
-// Product rows with more than kGalCap distinct keys (a large aggregate, a dense row): one CTA
-// per listed row; its first thread accumulates into a key-sorted list in shared memory, each
-// key's contributions summed in the same arrival order as Acc, so the row equals what an
-// unbounded Acc would give.  A row above kBigCap keys sets overflow[0].  RW = 0: row i of
-// W = A P (outer: A's row, inner: P's rows); RW = 1: row I of R W (outer: R's row, inner: W's).
-constexpr int kBigCap = 3072;  // keys + FP64 values: 36 KB of shared memory
-template <int MODE, int RW, class OV, class IV>
-__global__ void __launch_bounds__(32) k_gal_big(const int32_t* __restrict__ list, const int64_t* __restrict__ o_ptr64,
-                                                const int32_t* __restrict__ o_ptr32, const int32_t* __restrict__ o_idx,
-                                                const OV* __restrict__ o_val, const int64_t* __restrict__ i_ptr,
-                                                const int32_t* __restrict__ i_idx, const IV* __restrict__ i_val,
-                                                int32_t* __restrict__ cnt, const int64_t* __restrict__ off,
-                                                int32_t* __restrict__ oc, double* __restrict__ ov, float* __restrict__ adinv,
-                                                int* __restrict__ overflow) {
-  __shared__ int32_t key[kBigCap];
-  __shared__ double val[kBigCap];
-  if (threadIdx.x != 0) return;
-  const int32_t row = list[blockIdx.x];
-  const int64_t b = o_ptr64 ? o_ptr64[row] : (int64_t)o_ptr32[row];
-  const int64_t e_ = o_ptr64 ? o_ptr64[row + 1] : (int64_t)o_ptr32[row + 1];
-  int n = 0;
-  for (int64_t q = b; q < e_; ++q) {
-    const int32_t j = o_idx[q];
-    const double a = (double)o_val[q];
-    for (int64_t r = i_ptr[j]; r < i_ptr[j + 1]; ++r) {
-      const int32_t k = i_idx[r];
-      const double v = a * (double)i_val[r];
-      int lo = 0, hi = n;  // first position with key >= k
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (key[mid] < k) lo = mid + 1; else hi = mid;
+struct GalOut {
+  int32_t* cnt;         // distinct keys per row (MODE 0, 2)
+  int32_t* sn;          // MODE 2: staged count, or -1 when listed
+  int32_t* st_key;      // MODE 2: staging, H/2 entries per row
+  double* st_val;
+  const int64_t* off;   // MODE 1: output offsets
+  int32_t* oc;
+  double* ov;
+  float* adinv;         // DIAG
+  int32_t* next;        // MODE 2: listed rows
+  int32_t* next_n;
+  int* overflow;        // MODE 0: a row above the large table's capacity
+};
+
+template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
+__global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const int32_t* __restrict__ list,
+                                                         const uint8_t* __restrict__ active, const OP* __restrict__ o_ptr,
+                                                         const int32_t* __restrict__ o_idx, const OV* __restrict__ o_val,
+                                                         const IP* __restrict__ i_ptr, const int32_t* __restrict__ i_idx,
+                                                         const IV* __restrict__ i_val, KeyF keyf, GalOut out) {
+  using S = GalSmem<G, H>;
+  constexpr int HS = S::HS;
+  constexpr int SUB = 32 / G;
+  constexpr int LOGH = __builtin_ctz(H);
+  static_assert((H & (H - 1)) == 0 && HS >= G, "table size");
+  extern __shared__ __align__(16) unsigned char gal_smem[];
+  const int lane = threadIdx.x & 31, sl = lane & (G - 1), gb = lane & ~(G - 1);
+  const unsigned smask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gb);
+  const int sw = (threadIdx.x >> 5) * SUB + (lane / G);
+  unsigned char* base = gal_smem + S::bytes * (size_t)sw;
+  double* tval = reinterpret_cast<double*>(base);
+  double* stage = tval + H;
+  int32_t* tkey = reinterpret_cast<int32_t*>(stage + G);
+  int32_t* ckey = tkey + H;
+  int32_t* cslot = ckey + HS;
+  const int64_t nsub = (int64_t)gridDim.x * WARPS * SUB;
+  for (int64_t k0 = (int64_t)blockIdx.x * WARPS * SUB + sw; k0 < nrows; k0 += nsub) {
+    const int64_t row = list ? (int64_t)list[k0] : k0;
+    if (active && !active[row]) {
+      if (sl == 0) {
+        if (MODE != 1) out.cnt[row] = 0;
+        if (MODE == 2) out.sn[row] = 0;
       }
-      if (lo < n && key[lo] == k) {
-        val[lo] += v;
-      } else if (n < kBigCap) {
-        for (int t = n; t > lo; --t) {
-          key[t] = key[t - 1];
-          val[t] = val[t - 1];
+      continue;
+    }
+    for (int t = sl; t < H; t += G) {
+      tkey[t] = -1;
+      if (MODE != 0) tval[t] = 0.0;
+    }
+    __syncwarp(smask);
+    const int64_t ob = (int64_t)o_ptr[row], oe = (int64_t)o_ptr[row + 1];
+    int d = 0;
+    bool over = false;
+    for (int64_t q0 = ob; q0 < oe && !over; q0 += G) {
+      const int64_t q = q0 + sl;
+      int64_t ib = 0;
+      int len = 0;
+      double sc = 0.0;
+      if (q < oe) {
+        const int32_t j = o_idx[q];
+        sc = o_val ? (double)o_val[q] : 1.0;
+        ib = (int64_t)i_ptr[j];
+        len = (int)((int64_t)i_ptr[j + 1] - ib);
+      }
+      int x = len;  // inclusive scan of the inner lengths over the sub-warp
+#pragma unroll
+      for (int o = 1; o < G; o <<= 1) {
+        const int y = __shfl_up_sync(smask, x, o, G);
+        if (sl >= o) x += y;
+      }
+      const int total = __shfl_sync(smask, x, G - 1, G);
+      for (int p0 = 0; p0 < total; p0 += G) {
+        const int pl = p0 + sl;
+        const bool valid = pl < total;
+        int own = 0;  // lanes whose inclusive end is <= pl
+#pragma unroll
+        for (int st = G / 2; st >= 1; st >>= 1) {
+          const int xv = __shfl_sync(smask, x, own + st - 1, G);
+          if (xv <= pl) own += st;
         }
-        key[lo] = k;
-        val[lo] = v;
-        ++n;
-      } else {
-        atomicExch(overflow, 1);
-        if (MODE == 0) cnt[row] = 0;
-        return;
-      }
-    }
-  }
-  if (MODE == 0) {
-    cnt[row] = n;
-    return;
-  }
-  const int64_t at = off[row];
-  double d = 0.0;
-  for (int t = 0; t < n; ++t) {
-    oc[at + t] = key[t];
-    ov[at + t] = val[t];
-    if (RW && key[t] == row) d = val[t];
-  }
-  if (RW) adinv[row] = d > 0.0 ? (float)(1.0 / d) : 0.0f;
-}
-
-// Tentative prolongator (P = one 1 per row at agg[i]): A_c = R A P straight from A, coarse row
-// I = sum over its member rows i of A's row i with every column j mapped to agg[j] -- no
-// W = A P pass.  MODE 0 count / 1 fill (also the coarse diagonal inverse).  Rows above kGalCap
-// distinct columns go to k_rap_t_big.
-template <int MODE>
-__global__ void k_rap_t(int64_t nc, const int64_t* __restrict__ roff, const int32_t* __restrict__ rc,
-                        const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
-                        const double* __restrict__ vals, const int32_t* __restrict__ agg, int32_t* __restrict__ cnt,
-                        const int64_t* __restrict__ aoff, int32_t* __restrict__ ac, double* __restrict__ av,
-                        float* __restrict__ adinv, int* __restrict__ overflow, int32_t* __restrict__ big,
-                        int32_t* __restrict__ big_n) {
-  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (I >= nc) return;
-  Acc<kGalCap, double> acc;
-  for (int64_t q = roff[I]; q < roff[I + 1]; ++q) {
-    const int32_t i = rc[q];
-    for (int e = rp[i]; e < rp[i + 1]; ++e) acc.add(agg[cols[e]], vals[e]);
-  }
-  atomicMax(overflow + 5, acc.n);
-  if (acc.overflow) {
-    if (MODE == 0) {
-      cnt[I] = 0;
-      big[atomicAdd(big_n, 1)] = (int32_t)I;
-    }
-    return;
-  }
-  acc.sort();
-  if (MODE == 0) {
-    cnt[I] = acc.n;
-    return;
-  }
-  const int64_t at = aoff[I];
-  double d = 0.0;
-  for (int t = 0; t < acc.n; ++t) {
-    ac[at + t] = acc.key[t];
-    av[at + t] = acc.val[t];
-    if (acc.key[t] == (int32_t)I) d = acc.val[t];
-  }
-  adinv[I] = d > 0.0 ? (float)(1.0 / d) : 0.0f;
-}
-
-// k_rap_t for its listed rows, one CTA per row (its first thread), key-sorted accumulation in
-// shared memory in the same arrival order.
-template <int MODE>
-__global__ void __launch_bounds__(32) k_rap_t_big(const int32_t* __restrict__ list, const int64_t* __restrict__ roff,
-                                                  const int32_t* __restrict__ rc, const int32_t* __restrict__ rp,
-                                                  const int32_t* __restrict__ cols, const double* __restrict__ vals,
-                                                  const int32_t* __restrict__ agg, int32_t* __restrict__ cnt,
-                                                  const int64_t* __restrict__ aoff, int32_t* __restrict__ ac,
-                                                  double* __restrict__ av, float* __restrict__ adinv,
-                                                  int* __restrict__ overflow) {
-  __shared__ int32_t key[kBigCap];
-  __shared__ double val[kBigCap];
-  if (threadIdx.x != 0) return;
-  const int32_t I = list[blockIdx.x];
-  int n = 0;
-  for (int64_t q = roff[I]; q < roff[I + 1]; ++q) {
-    const int32_t i = rc[q];
-    for (int e = rp[i]; e < rp[i + 1]; ++e) {
-      const int32_t k = agg[cols[e]];
-      const double v = vals[e];
-      int lo = 0, hi = n;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (key[mid] < k) lo = mid + 1; else hi = mid;
-      }
-      if (lo < n && key[lo] == k) {
-        val[lo] += v;
-      } else if (n < kBigCap) {
-        for (int t = n; t > lo; --t) {
-          key[t] = key[t - 1];
-          val[t] = val[t - 1];
+        own = min(own, G - 1);
+        const double sco = __shfl_sync(smask, sc, own, G);
+        const long long ibo = __shfl_sync(smask, (long long)ib, own, G);
+        const int sto = __shfl_sync(smask, x - len, own, G);
+        int32_t key = 0;
+        double v = 0.0;
+        int slot = -1;
+        bool fresh = false;
+        if (valid) {
+          const int64_t e = (int64_t)ibo + (pl - sto);
+          key = keyf(i_idx[e]);
+          if (MODE != 0) v = sco * (double)i_val[e];
+          unsigned h = ((uint32_t)key * 0x9E3779B1u) >> (32 - LOGH);
+          for (int pr = 0; pr < H; ++pr) {
+            const int32_t k = reinterpret_cast<volatile int32_t*>(tkey)[h];
+            if (k == key) {
+              slot = (int)h;
+              break;
+            }
+            if (k == -1) {
+              const int32_t old = atomicCAS(&tkey[h], -1, key);
+              if (old == -1 || old == key) {
+                slot = (int)h;
+                fresh = old == -1;
+                break;
+              }
+            }
+            h = (h + 1) & (H - 1);
+          }
         }
-        key[lo] = k;
-        val[lo] = v;
-        ++n;
-      } else {
-        atomicExch(overflow, 1);
-        if (MODE == 0) cnt[I] = 0;
-        return;
+        d += __popc(__ballot_sync(smask, fresh));
+        if (__ballot_sync(smask, valid && slot < 0) != 0u || d > HS) {
+          over = true;
+          break;
+        }
+        if (MODE != 0) {
+          stage[sl] = v;
+          __syncwarp(smask);
+          const unsigned gm = __match_any_sync(smask, valid ? slot : -1);
+          if (valid && (__ffs(gm) - 1) == lane) {
+            double s = tval[slot];
+            for (unsigned m = gm; m != 0u; m &= m - 1u) s += stage[(__ffs(m) - 1) - gb];
+            tval[slot] = s;
+          }
+        }
+        __syncwarp(smask);
       }
     }
+    if (over) {
+      if (sl == 0) {
+        if (MODE == 2) {
+          out.sn[row] = -1;
+          out.cnt[row] = 0;
+          out.next[atomicAdd(out.next_n, 1)] = (int32_t)row;
+        } else {
+          atomicExch(out.overflow, 1);
+          if (MODE == 0) out.cnt[row] = 0;
+        }
+      }
+      __syncwarp(smask);
+      continue;
+    }
+    if (MODE == 0) {
+      if (sl == 0) out.cnt[row] = d;
+      __syncwarp(smask);
+      continue;
+    }
+    // compact the occupied slots (slot order), then rank each key by counting smaller ones
+    int nb = 0;
+    for (int t0 = 0; t0 < H; t0 += G) {
+      const int t = t0 + sl;
+      const bool occ = tkey[t] != -1;
+      const unsigned m = __ballot_sync(smask, occ) >> gb;
+      if (occ) {
+        const int pos = nb + __popc(m & ((1u << sl) - 1u));
+        ckey[pos] = tkey[t];
+        cslot[pos] = t;
+      }
+      nb += __popc(m);
+    }
+    __syncwarp(smask);
+    int32_t* dk;
+    double* dv;
+    if (MODE == 2) {
+      dk = out.st_key + row * HS;
+      dv = out.st_val + row * HS;
+    } else {
+      dk = out.oc + out.off[row];
+      dv = out.ov + out.off[row];
+    }
+    bool has_d = false;
+    double dval = 0.0;
+    for (int c = sl; c < d; c += G) {
+      const int32_t k = ckey[c];
+      int rank = 0;
+      for (int u = 0; u < d; ++u) rank += ckey[u] < k;
+      const double val = tval[cslot[c]];
+      dk[rank] = k;
+      dv[rank] = val;
+      if (DIAG && k == (int32_t)row) {
+        has_d = true;
+        dval = val;
+      }
+    }
+    if (DIAG) {
+      if (__ballot_sync(smask, has_d) == 0u) {
+        if (sl == 0) out.adinv[row] = 0.0f;
+      } else if (has_d) {
+        out.adinv[row] = dval > 0.0 ? (float)(1.0 / dval) : 0.0f;
+      }
+    }
+    if (sl == 0) {
+      out.cnt[row] = d;
+      if (MODE == 2) out.sn[row] = d;
+    }
+    __syncwarp(smask);
   }
-  if (MODE == 0) {
-    cnt[I] = n;
-    return;
+}
+
+// Staged rows to their place in the product (8 lanes per row); listed rows (sn < 0) are
+// written by the large-table kernel.
+__global__ void k_gal_copy(int64_t nrows, int hs, const int32_t* __restrict__ sn, const int32_t* __restrict__ st_key,
+                           const double* __restrict__ st_val, const int64_t* __restrict__ off, int32_t* __restrict__ oc,
+                           double* __restrict__ ov) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = t >> 3;
+  const int sl = (int)(t & 7);
+  if (row >= nrows) return;
+  const int n = sn[row];
+  const int64_t src = row * hs, dst = off[row];
+  for (int k = sl; k < n; k += 8) {
+    oc[dst + k] = st_key[src + k];
+    ov[dst + k] = st_val[src + k];
   }
-  const int64_t at = aoff[I];
-  double d = 0.0;
-  for (int t = 0; t < n; ++t) {
-    ac[at + t] = key[t];
-    av[at + t] = val[t];
-    if (key[t] == I) d = val[t];
-  }
-  adinv[I] = d > 0.0 ? (float)(1.0 / d) : 0.0f;
 }
 
 __global__ void k_i64_i32(int64_t n, const int64_t* __restrict__ a, int32_t* __restrict__ b) {
@@ -1077,6 +1089,100 @@ int64_t offsets_from_counts(Ctx& ctx, const int32_t* cnt, int64_t n, int64_t* of
   return read_i64(ctx, off + n);
 }
 
+// Work areas of the sparse products: the staging rows, their counts, and the rows listed for
+// the large-table kernel (count at list_n on the device, h1 on the host).
+struct GalWork {
+  int32_t* list = nullptr;
+  int32_t* list_n = nullptr;
+  int* ovf = nullptr;
+  int32_t* sn = nullptr;
+  int32_t* st_key = nullptr;
+  double* st_val = nullptr;
+  float* st_dinv = nullptr;
+  int hs = 0;
+  int32_t h1 = 0;
+  bool debug = false;
+  std::chrono::steady_clock::time_point t0;
+};
+constexpr int kGalWarps = 8;
+constexpr int kGalBigH = 8192;  // large table: 4096 distinct keys, 128 KB of shared memory
+
+template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
+void launch_gal(cudaStream_t s, int64_t nrows, const int32_t* list, const uint8_t* active, const OP* o_ptr,
+                const int32_t* o_idx, const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, KeyF keyf,
+                const GalOut& out) {
+  constexpr int SUB = 32 / G;
+  constexpr size_t smem = GalSmem<G, H>::bytes * WARPS * SUB;
+  auto k = k_gal_hash<MODE, G, H, WARPS, DIAG, OP, OV, IP, IV, KeyF>;
+  if (smem > 48 * 1024) RUV_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k<<<div_up(nrows, (int64_t)WARPS * SUB), 32 * WARPS, smem, s>>>(nrows, list, active, o_ptr, o_idx, o_val, i_ptr, i_idx,
+                                                                 i_val, keyf, out);
+  count_launches(1);
+  RUV_LAUNCH_CHECK();
+}
+
+// First half of a sparse product over `nrows` rows (`avg`: the mean products per row, which
+// picks the lanes per row and the table size): every row evaluated once into the staging
+// area, the rows with more distinct keys counted by the large-table kernel; cnt holds every
+// row's count on return.
+template <bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
+void gal_count(Ctx& ctx, GalWork& g, int64_t nrows, double avg, const uint8_t* active, const OP* o_ptr,
+               const int32_t* o_idx, const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, KeyF keyf,
+               int32_t* cnt) {
+  cudaStream_t s = ctx.stream;
+  g.h1 = 0;
+  if (nrows <= 0) return;
+  if (g.debug) {
+    RUV_CUDA(cudaStreamSynchronize(s));
+    g.t0 = std::chrono::steady_clock::now();
+  }
+  g.hs = avg < 20.0 ? GalSmem<8, 64>::HS : avg < 48.0 ? GalSmem<16, 128>::HS : GalSmem<32, 256>::HS;
+  g.sn = ctx.ws.get<int32_t>("amg.gal_sn", nrows);
+  g.st_key = ctx.ws.get<int32_t>("amg.gal_key", nrows * g.hs);
+  g.st_val = ctx.ws.get<double>("amg.gal_val", nrows * g.hs);
+  g.st_dinv = DIAG ? ctx.ws.get<float>("amg.gal_dinv", nrows) : nullptr;
+  RUV_CUDA(cudaMemsetAsync(g.list_n, 0, sizeof(int32_t), s));
+  GalOut out{cnt, g.sn, g.st_key, g.st_val, nullptr, nullptr, nullptr, g.st_dinv, g.list, g.list_n, g.ovf};
+  if (g.hs == GalSmem<8, 64>::HS)
+    launch_gal<2, 8, 64, kGalWarps, DIAG>(s, nrows, nullptr, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, out);
+  else if (g.hs == GalSmem<16, 128>::HS)
+    launch_gal<2, 16, 128, kGalWarps, DIAG>(s, nrows, nullptr, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, out);
+  else
+    launch_gal<2, 32, 256, kGalWarps, DIAG>(s, nrows, nullptr, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, out);
+  RUV_CUDA(cudaMemcpyAsync(&g.h1, g.list_n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  if (g.h1 > 0) {
+    GalOut o0{cnt, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, g.ovf};
+    launch_gal<0, 32, kGalBigH, 1, DIAG>(s, g.h1, g.list, nullptr, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, o0);
+  }
+}
+
+// Second half: staged rows copied to their offsets, listed rows evaluated again by the
+// large-table kernel straight into place.
+template <bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
+void gal_fill(Ctx& ctx, GalWork& g, int64_t nrows, const OP* o_ptr, const int32_t* o_idx, const OV* o_val,
+              const IP* i_ptr, const int32_t* i_idx, const IV* i_val, KeyF keyf, const int64_t* off, int32_t* oc,
+              double* ov, float* adinv) {
+  cudaStream_t s = ctx.stream;
+  if (nrows <= 0) return;
+  k_gal_copy<<<div_up(nrows * 8, 256), 256, 0, s>>>(nrows, g.hs, g.sn, g.st_key, g.st_val, off, oc, ov);
+  count_launches(1);
+  if (DIAG) {
+    RUV_CUDA(cudaMemcpyAsync(adinv, g.st_dinv, sizeof(float) * nrows, cudaMemcpyDeviceToDevice, s));
+  }
+  RUV_LAUNCH_CHECK();
+  if (g.h1 > 0) {
+    GalOut o1{nullptr, nullptr, nullptr, nullptr, off, oc, ov, adinv, nullptr, nullptr, g.ovf};
+    launch_gal<1, 32, kGalBigH, 1, DIAG>(s, g.h1, g.list, nullptr, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, o1);
+  }
+  if (g.debug) {
+    RUV_CUDA(cudaStreamSynchronize(s));
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - g.t0).count();
+    std::fprintf(stderr, "  product rows %lld: %d lanes per row, large-table rows %d, %.3f ms\n", (long long)nrows,
+                 g.hs == 32 ? 8 : g.hs == 64 ? 16 : 32, g.h1, ms);
+  }
+}
+
 }  // namespace
 
 AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string& info) {
@@ -1246,30 +1352,13 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     count_launches(2);
     int32_t* acnt = ctx.ws.get<int32_t>(ntag + ".acnt", NA);
     int64_t* aoff = ctx.ws.get<int64_t>(ntag + ".aoff", NA + 1);
-    int32_t* big = ctx.ws.get<int32_t>("amg.big", std::max<int64_t>(std::max<int64_t>(L.n, NA), 1));
-    int32_t* big_n = ovf + 6;
-    auto n_big = [&]() {
-      int32_t h = 0;
-      RUV_CUDA(cudaMemcpyAsync(&h, big_n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-      RUV_CUDA(cudaStreamSynchronize(s));
-      return h;
-    };
-    if (!smooth) {
-      // ---- tentative prolongator: A_c = R A P straight from A
-      int32_t abig = 0;
-      if (NA > 0) {
-        RUV_CUDA(cudaMemsetAsync(big_n, 0, sizeof(int32_t), s));
-        k_rap_t<0><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rp, L.cols, L.vals64, agg, acnt, nullptr, nullptr,
-                                               nullptr, nullptr, ovf, big, big_n);
-        count_launches(1);
-        abig = n_big();
-        if (abig > 0) {
-          k_rap_t_big<0><<<(unsigned)abig, 32, 0, s>>>(big, L.roff, L.rc, L.rp, L.cols, L.vals64, agg, acnt, nullptr,
-                                                       nullptr, nullptr, nullptr, ovf);
-          count_launches(1);
-        }
-      }
-      const int64_t AN = offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao");
+    GalWork gw;
+    gw.list = ctx.ws.get<int32_t>("amg.gal_list", std::max<int64_t>(std::max<int64_t>(L.n, NA), 1));
+    gw.list_n = ovf + 6;
+    gw.ovf = ovf;
+    gw.debug = debug;
+    // the coarse operator's storage once its size is known
+    auto alloc_coarse = [&](int64_t AN) {
       if (AN >= (int64_t)INT32_MAX) throw Error{RUV_ERR_BAD_INPUT, "coarse operator too large"};
       C.rp = ctx.ws.get<int32_t>(ntag + ".rp", NA + 1);
       C.cols = ctx.ws.get<int32_t>(ntag + ".cols", AN);
@@ -1277,81 +1366,40 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
       C.vals64 = ctx.ws.get<double>(ntag + ".vals64", AN);
       C.dinv = ctx.ws.get<float>(ntag + ".dinv", NA);
       C.nnz = AN;
+    };
+    auto finish_coarse = [&]() {
       if (NA > 0) {
-        k_rap_t<1><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rp, L.cols, L.vals64, agg, acnt, aoff, C.cols,
-                                               C.vals64, C.dinv, ovf, big, big_n);
-        if (abig > 0) {
-          k_rap_t_big<1><<<(unsigned)abig, 32, 0, s>>>(big, L.roff, L.rc, L.rp, L.cols, L.vals64, agg, acnt, aoff,
-                                                       C.cols, C.vals64, C.dinv, ovf);
-          count_launches(1);
-        }
         k_i64_i32<<<div_up(NA + 1, B), B, 0, s>>>(NA + 1, aoff, C.rp);
-        if (AN > 0) k_f64_f32<<<div_up(AN, B), B, 0, s>>>(AN, C.vals64, C.vals);
-        count_launches(3);
+        if (C.nnz > 0) k_f64_f32<<<div_up(C.nnz, B), B, 0, s>>>(C.nnz, C.vals64, C.vals);
+        count_launches(2);
       }
-      L.n_next = NA;
-      C.h_chart_row.resize(NC + 1);
-      RUV_CUDA(cudaMemcpyAsync(C.h_chart_row.data(), C.chart_row, sizeof(int64_t) * (NC + 1), cudaMemcpyDeviceToHost, s));
-      RUV_CUDA(cudaStreamSynchronize(s));
-      H->lv.push_back(C);
-      continue;
-    }
-    // ---- smoothed prolongator: W = A P, then A_c = R W
-    int32_t* wcnt = ctx.ws.get<int32_t>(tag + ".wcnt", L.n);
-    int64_t* woff = ctx.ws.get<int64_t>(tag + ".woff", L.n + 1);
-    RUV_CUDA(cudaMemsetAsync(big_n, 0, sizeof(int32_t), s));
-    k_ap<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt, nullptr, nullptr,
-                                         nullptr, ovf, big, big_n);
-    count_launches(1);
-    const int32_t wbig = n_big();
-    if (wbig > 0) {
-      k_gal_big<0, 0><<<(unsigned)wbig, 32, 0, s>>>(big, nullptr, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt, nullptr,
-                                                    nullptr, nullptr, nullptr, ovf);
-      count_launches(1);
-    }
-    const int64_t WN = offsets_from_counts(ctx, wcnt, L.n, woff, tag + ".wo");
-    int32_t* wc = ctx.ws.get<int32_t>(tag + ".wc", WN);
-    double* wv = ctx.ws.get<double>(tag + ".wv", WN);
-    k_ap<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt, woff, wc, wv, ovf,
-                                         big, big_n);
-    count_launches(1);
-    if (wbig > 0) {
-      k_gal_big<1, 0><<<(unsigned)wbig, 32, 0, s>>>(big, nullptr, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt, woff,
-                                                    wc, wv, nullptr, ovf);
-      count_launches(1);
-    }
-    int32_t abig = 0;
-    if (NA > 0) {
-      RUV_CUDA(cudaMemsetAsync(big_n, 0, sizeof(int32_t), s));
-      k_rw<0><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv, woff, wc, wv, acnt, nullptr, nullptr, nullptr, nullptr,
-                                          ovf, big, big_n);
-      count_launches(1);
-      abig = n_big();
-      if (abig > 0) {
-        k_gal_big<0, 1><<<(unsigned)abig, 32, 0, s>>>(big, L.roff, nullptr, L.rc, L.rv, woff, wc, wv, acnt, nullptr,
-                                                      nullptr, nullptr, nullptr, ovf);
-        count_launches(1);
-      }
-    }
-    const int64_t AN = offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao");
-    if (AN >= (int64_t)INT32_MAX) throw Error{RUV_ERR_BAD_INPUT, "coarse operator too large"};
-    C.rp = ctx.ws.get<int32_t>(ntag + ".rp", NA + 1);
-    C.cols = ctx.ws.get<int32_t>(ntag + ".cols", AN);
-    C.vals = ctx.ws.get<float>(ntag + ".vals", AN);
-    C.vals64 = ctx.ws.get<double>(ntag + ".vals64", AN);
-    C.dinv = ctx.ws.get<float>(ntag + ".dinv", NA);
-    C.nnz = AN;
-    if (NA > 0) {
-      k_rw<1><<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv, woff, wc, wv, acnt, aoff, C.cols, C.vals64, C.dinv, ovf,
-                                          big, big_n);
-      if (abig > 0) {
-        k_gal_big<1, 1><<<(unsigned)abig, 32, 0, s>>>(big, L.roff, nullptr, L.rc, L.rv, woff, wc, wv, acnt, aoff, C.cols,
-                                                      C.vals64, C.dinv, ovf);
-        count_launches(1);
-      }
-      k_i64_i32<<<div_up(NA + 1, B), B, 0, s>>>(NA + 1, aoff, C.rp);
-      if (AN > 0) k_f64_f32<<<div_up(AN, B), B, 0, s>>>(AN, C.vals64, C.vals);
-      count_launches(3);
+    };
+    auto mean = [](int64_t a, int64_t b) { return b > 0 ? (double)a / (double)b : 0.0; };
+    int64_t WN = 0;
+    if (!smooth) {
+      // ---- tentative prolongator: A_c = R A P straight from A (keys through agg)
+      const double avg = mean(PN, NA) * mean(L.nnz, L.n);
+      gal_count<true>(ctx, gw, NA, avg, nullptr, L.roff, L.rc, (const float*)nullptr, L.rp, L.cols, L.vals64,
+                      KeyAgg{agg}, acnt);
+      alloc_coarse(offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao"));
+      gal_fill<true>(ctx, gw, NA, L.roff, L.rc, (const float*)nullptr, L.rp, L.cols, L.vals64, KeyAgg{agg}, aoff, C.cols,
+                     C.vals64, C.dinv);
+      finish_coarse();
+    } else {
+      // ---- smoothed prolongator: W = A P, then A_c = R W
+      int32_t* wcnt = ctx.ws.get<int32_t>(tag + ".wcnt", L.n);
+      int64_t* woff = ctx.ws.get<int64_t>(tag + ".woff", L.n + 1);
+      gal_count<false>(ctx, gw, L.n, mean(L.nnz, L.n) * mean(PN, L.n), active, L.rp, L.cols, L.vals64, L.poff, L.pc,
+                       L.pv, KeyId{}, wcnt);
+      WN = offsets_from_counts(ctx, wcnt, L.n, woff, tag + ".wo");
+      int32_t* wc = ctx.ws.get<int32_t>(tag + ".wc", WN);
+      double* wv = ctx.ws.get<double>(tag + ".wv", WN);
+      gal_fill<false>(ctx, gw, L.n, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, KeyId{}, woff, wc, wv, nullptr);
+      gal_count<true>(ctx, gw, NA, mean(PN, NA) * mean(WN, L.n), nullptr, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{},
+                      acnt);
+      alloc_coarse(offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao"));
+      gal_fill<true>(ctx, gw, NA, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{}, aoff, C.cols, C.vals64, C.dinv);
+      finish_coarse();
     }
     L.n_next = NA;
     if (debug) {
@@ -1360,7 +1408,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
       RUV_CUDA(cudaStreamSynchronize(s));
       std::fprintf(stderr, "amg level %d: n=%lld nnz=%lld groups=%lld aggregates=%lld P=%lld W=%lld Ac=%lld "
                    "max keys propose2=%d P=%d W=%d Ac=%d overflow=%d\n", lvl, (long long)L.n, (long long)L.nnz,
-                   (long long)NG, (long long)NA, (long long)PN, (long long)WN, (long long)AN, hv[2], hv[3], hv[4], hv[5],
+                   (long long)NG, (long long)NA, (long long)PN, (long long)WN, (long long)C.nnz, hv[2], hv[3], hv[4], hv[5],
                    hv[0]);
       RUV_CUDA(cudaMemsetAsync(ovf + 2, 0, 4 * sizeof(int), s));
     }
