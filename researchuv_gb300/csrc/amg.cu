@@ -37,9 +37,13 @@ constexpr int kDirect = 64;       // rows at which a chart is solved directly
 constexpr int kMaxLevels = 16;
 constexpr float kOmega = 2.0f / 3.0f;
 constexpr int kPairRounds = 4;
-constexpr int kAccCap = 48;       // distinct keys per accumulated strength row (a heuristic)
-constexpr int kGalCap = 96;       // distinct keys per Galerkin product row (exact)
-constexpr int kPMaxRow = 8;       // smoothed prolongator row cap (own aggregate always kept)
+// distinct keys per accumulated strength row: group strengths beyond it (only on dense coarse
+// levels of the smoothed hierarchy) are left out of the matching, deterministically
+constexpr int kAccCap = 48;
+// Smoothed prolongator row cap (own aggregate always kept).  The reference keeps 32
+// (amg.rs:299); on the device the cap sets the density of every coarse operator and so the
+// set-up and V-cycle cost, and 4 gives the shortest whole solve (iterations nearly those of 8)
+constexpr int kPMaxRow = 4;
 constexpr int64_t kLevelTile = 1024;  // rows per CTA tile in the V-cycle kernels
 
 __device__ __forceinline__ int64_t find_chart64(const int64_t* off, int64_t n_charts, int64_t i) {
@@ -301,7 +305,7 @@ __global__ void k_agg(int64_t n, const uint8_t* __restrict__ active, const int32
 template <int MODE>
 __global__ void k_prolong(int64_t n, const uint8_t* __restrict__ active, const int32_t* __restrict__ rp,
                           const int32_t* __restrict__ cols, const float* __restrict__ vals,
-                          const float* __restrict__ dinv, const int32_t* __restrict__ agg, int smooth,
+                          const float* __restrict__ dinv, const int32_t* __restrict__ agg, int smooth, int pmax,
                           int32_t* __restrict__ cnt, const int64_t* __restrict__ off, int32_t* __restrict__ pc,
                           float* __restrict__ pv, int* __restrict__ overflow) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -315,12 +319,12 @@ __global__ void k_prolong(int64_t n, const uint8_t* __restrict__ active, const i
   if (smooth) {
     const float wd = kOmega * dinv[i];
     for (int e = rp[i]; e < rp[i + 1]; ++e) acc.add(agg[cols[e]], -wd * vals[e]);
-    if (acc.n > kPMaxRow) {
-      // keep the own aggregate (slot 0) and the kPMaxRow - 1 largest magnitudes (ties to the
+    if (acc.n > pmax) {
+      // keep the own aggregate (slot 0) and the pmax - 1 largest magnitudes (ties to the
       // smaller column): selection by repeated maximum, then compaction
       bool keep[kAccCap];
       for (int t = 0; t < acc.n; ++t) keep[t] = t == 0;
-      for (int k = 1; k < kPMaxRow; ++k) {
+      for (int k = 1; k < pmax; ++k) {
         int bt = -1;
         for (int t = 1; t < acc.n; ++t) {
           if (keep[t]) continue;
@@ -373,21 +377,28 @@ __global__ void k_scatter_t(int64_t n, const int64_t* __restrict__ poff, const i
   }
 }
 
-// Sort each row of R by fine row (deterministic order after the atomic scatter).
-__global__ void k_sort_rows(int64_t n, const int64_t* __restrict__ off, int32_t* __restrict__ c, float* __restrict__ v) {
-  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Each row of R ordered by fine row (a deterministic order after the atomic scatter): warp
+// per row, every entry placed at the count of smaller keys (the keys of a row are distinct).
+__global__ void k_sort_rows(int64_t n, const int64_t* __restrict__ off, const int32_t* __restrict__ c_in,
+                            const float* __restrict__ v_in, int32_t* __restrict__ c, float* __restrict__ v) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (r >= n) return;
-  for (int64_t i = off[r] + 1; i < off[r + 1]; ++i) {
-    int32_t k = c[i];
-    float x = v[i];
-    int64_t j = i - 1;
-    while (j >= off[r] && c[j] > k) {
-      c[j + 1] = c[j];
-      v[j + 1] = v[j];
-      --j;
+  const int64_t b = off[r], e = off[r + 1];
+  for (int64_t i0 = b; i0 < e; i0 += 32) {
+    const int64_t i = i0 + lane;
+    const int32_t k = i < e ? c_in[i] : INT32_MAX;
+    int rank = 0;
+    for (int64_t u0 = b; u0 < e; u0 += 32) {
+      const int32_t ku = u0 + lane < e ? c_in[u0 + lane] : INT32_MAX;
+      const int m = e - u0 < 32 ? (int)(e - u0) : 32;
+      for (int u = 0; u < m; ++u) rank += __shfl_sync(kFull, ku, u) < k;
     }
-    c[j + 1] = k;
-    v[j + 1] = x;
+    if (i < e) {
+      c[b + rank] = k;
+      v[b + rank] = v_in[i];
+    }
   }
 }
 
@@ -434,7 +445,7 @@ struct GalOut {
   float* adinv;         // DIAG
   int32_t* next;        // MODE 2: listed rows
   int32_t* next_n;
-  int* overflow;        // MODE 0: a row above the large table's capacity
+  int* overflow;        // MODE 0 / 1: a row above the large table's capacity
 };
 
 template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
@@ -459,6 +470,15 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
   int32_t* ckey = tkey + H;
   int32_t* cslot = ckey + HS;
   const int64_t nsub = (int64_t)gridDim.x * WARPS * SUB;
+  // the table starts empty; every row leaves it empty (only its own slots are cleared)
+  auto clear_all = [&]() {
+    for (int t = sl; t < H; t += G) {
+      tkey[t] = -1;
+      tval[t] = 0.0;
+    }
+    __syncwarp(smask);
+  };
+  clear_all();
   for (int64_t k0 = (int64_t)blockIdx.x * WARPS * SUB + sw; k0 < nrows; k0 += nsub) {
     const int64_t row = list ? (int64_t)list[k0] : k0;
     if (active && !active[row]) {
@@ -468,11 +488,6 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
       }
       continue;
     }
-    for (int t = sl; t < H; t += G) {
-      tkey[t] = -1;
-      if (MODE != 0) tval[t] = 0.0;
-    }
-    __syncwarp(smask);
     const int64_t ob = (int64_t)o_ptr[row], oe = (int64_t)o_ptr[row + 1];
     int d = 0;
     bool over = false;
@@ -533,7 +548,15 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
             h = (h + 1) & (H - 1);
           }
         }
-        d += __popc(__ballot_sync(smask, fresh));
+        const unsigned fm = __ballot_sync(smask, fresh);
+        if (fresh) {  // the occupied slots in insertion order
+          const int pos = d + __popc(fm & ((1u << lane) - 1u));
+          if (pos < HS) {
+            ckey[pos] = key;
+            cslot[pos] = slot;
+          }
+        }
+        d += __popc(fm);
         if (__ballot_sync(smask, valid && slot < 0) != 0u || d > HS) {
           over = true;
           break;
@@ -563,27 +586,17 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
         }
       }
       __syncwarp(smask);
+      clear_all();
       continue;
     }
+    __syncwarp(smask);
     if (MODE == 0) {
       if (sl == 0) out.cnt[row] = d;
+      for (int c = sl; c < d; c += G) tkey[cslot[c]] = -1;
       __syncwarp(smask);
       continue;
     }
-    // compact the occupied slots (slot order), then rank each key by counting smaller ones
-    int nb = 0;
-    for (int t0 = 0; t0 < H; t0 += G) {
-      const int t = t0 + sl;
-      const bool occ = tkey[t] != -1;
-      const unsigned m = __ballot_sync(smask, occ) >> gb;
-      if (occ) {
-        const int pos = nb + __popc(m & ((1u << sl) - 1u));
-        ckey[pos] = tkey[t];
-        cslot[pos] = t;
-      }
-      nb += __popc(m);
-    }
-    __syncwarp(smask);
+    // rank each key by counting smaller ones
     int32_t* dk;
     double* dv;
     if (MODE == 2) {
@@ -599,7 +612,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
       const int32_t k = ckey[c];
       int rank = 0;
       for (int u = 0; u < d; ++u) rank += ckey[u] < k;
-      const double val = tval[cslot[c]];
+      const int slot = cslot[c];
+      const double val = tval[slot];
       dk[rank] = k;
       dv[rank] = val;
       if (DIAG && k == (int32_t)row) {
@@ -614,9 +628,15 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
         out.adinv[row] = dval > 0.0 ? (float)(1.0 / dval) : 0.0f;
       }
     }
-    if (sl == 0) {
+    if (MODE == 2 && sl == 0) {  // (MODE 1 leaves the counts alone)
       out.cnt[row] = d;
-      if (MODE == 2) out.sn[row] = d;
+      out.sn[row] = d;
+    }
+    __syncwarp(smask);
+    for (int c = sl; c < d; c += G) {
+      const int slot = cslot[c];
+      tkey[slot] = -1;
+      tval[slot] = 0.0;
     }
     __syncwarp(smask);
   }
@@ -1089,8 +1109,8 @@ int64_t offsets_from_counts(Ctx& ctx, const int32_t* cnt, int64_t n, int64_t* of
   return read_i64(ctx, off + n);
 }
 
-// Work areas of the sparse products: the staging rows, their counts, and the rows listed for
-// the large-table kernel (count at list_n on the device, h1 on the host).
+// Work areas of the sparse products: the staging rows and their counts, and the rows listed
+// for the large-table kernel (count at list_n on the device, h1 on the host).
 struct GalWork {
   int32_t* list = nullptr;
   int32_t* list_n = nullptr;
@@ -1099,7 +1119,8 @@ struct GalWork {
   int32_t* st_key = nullptr;
   double* st_val = nullptr;
   float* st_dinv = nullptr;
-  int hs = 0;
+  int hs = 0;     // staged entries per row
+  int lanes = 0;  // lanes per row of the first pass
   int32_t h1 = 0;
   bool debug = false;
   std::chrono::steady_clock::time_point t0;
@@ -1121,10 +1142,16 @@ void launch_gal(cudaStream_t s, int64_t nrows, const int32_t* list, const uint8_
   RUV_LAUNCH_CHECK();
 }
 
+inline double env_or(const char* name, double dflt) {
+  const char* e = std::getenv(name);
+  return e ? std::atof(e) : dflt;
+}
+
 // First half of a sparse product over `nrows` rows (`avg`: the mean products per row, which
-// picks the lanes per row and the table size): every row evaluated once into the staging
-// area, the rows with more distinct keys counted by the large-table kernel; cnt holds every
-// row's count on return.
+// picks 8, 16 or 32 lanes per row with tables of 64, 128 or 256 slots -- more rows in flight
+// for short rows).  Every row is evaluated once into the staging area; rows with more distinct
+// keys than the table holds are counted by the large-table kernel.  cnt holds every row's
+// count on return.
 template <bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
 void gal_count(Ctx& ctx, GalWork& g, int64_t nrows, double avg, const uint8_t* active, const OP* o_ptr,
                const int32_t* o_idx, const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, KeyF keyf,
@@ -1136,16 +1163,18 @@ void gal_count(Ctx& ctx, GalWork& g, int64_t nrows, double avg, const uint8_t* a
     RUV_CUDA(cudaStreamSynchronize(s));
     g.t0 = std::chrono::steady_clock::now();
   }
-  g.hs = avg < 20.0 ? GalSmem<8, 64>::HS : avg < 48.0 ? GalSmem<16, 128>::HS : GalSmem<32, 256>::HS;
+  const double t8 = env_or("RUV_GAL_T8", 32.0), t16 = env_or("RUV_GAL_T16", 48.0);
+  g.lanes = avg < t8 ? 8 : avg < t16 ? 16 : 32;
+  g.hs = g.lanes == 8 ? GalSmem<8, 64>::HS : g.lanes == 16 ? GalSmem<16, 128>::HS : GalSmem<32, 256>::HS;
   g.sn = ctx.ws.get<int32_t>("amg.gal_sn", nrows);
   g.st_key = ctx.ws.get<int32_t>("amg.gal_key", nrows * g.hs);
   g.st_val = ctx.ws.get<double>("amg.gal_val", nrows * g.hs);
   g.st_dinv = DIAG ? ctx.ws.get<float>("amg.gal_dinv", nrows) : nullptr;
   RUV_CUDA(cudaMemsetAsync(g.list_n, 0, sizeof(int32_t), s));
   GalOut out{cnt, g.sn, g.st_key, g.st_val, nullptr, nullptr, nullptr, g.st_dinv, g.list, g.list_n, g.ovf};
-  if (g.hs == GalSmem<8, 64>::HS)
+  if (g.lanes == 8)
     launch_gal<2, 8, 64, kGalWarps, DIAG>(s, nrows, nullptr, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, out);
-  else if (g.hs == GalSmem<16, 128>::HS)
+  else if (g.lanes == 16)
     launch_gal<2, 16, 128, kGalWarps, DIAG>(s, nrows, nullptr, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, out);
   else
     launch_gal<2, 32, 256, kGalWarps, DIAG>(s, nrows, nullptr, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, out);
@@ -1179,7 +1208,7 @@ void gal_fill(Ctx& ctx, GalWork& g, int64_t nrows, const OP* o_ptr, const int32_
     RUV_CUDA(cudaStreamSynchronize(s));
     const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - g.t0).count();
     std::fprintf(stderr, "  product rows %lld: %d lanes per row, large-table rows %d, %.3f ms\n", (long long)nrows,
-                 g.hs == 32 ? 8 : g.hs == 64 ? 16 : 32, g.h1, ms);
+                 g.lanes, g.h1, ms);
   }
 }
 
@@ -1197,6 +1226,8 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   if (const char* e = std::getenv("RUV_AMG_ALPHA")) H->alpha_c = (float)std::atof(e);
   float strong = kStrong;  // matching candidates: couplings >= strong * the row's strongest
   if (const char* e = std::getenv("RUV_AMG_STRONG")) strong = (float)std::atof(e);
+  int pmax = kPMaxRow;
+  if (const char* e = std::getenv("RUV_AMG_PMAX")) pmax = std::max(1, std::min(kAccCap, std::atoi(e)));
   cudaEvent_t t_setup0;
   RUV_CUDA(cudaEventCreate(&t_setup0));
   RUV_CUDA(cudaEventRecord(t_setup0, s));
@@ -1291,6 +1322,12 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     int32_t* glead_of = ctx.ws.get<int32_t>(tag + ".glead_of", NG);
     uint8_t* glead = ctx.ws.get<uint8_t>(tag + ".glead", NG);
     RUV_CUDA(cudaMemsetAsync(gmate, 0xff, sizeof(int32_t) * std::max<int64_t>(NG, 1), s));
+    GalWork gw;
+    gw.list = ctx.ws.get<int32_t>("amg.gal_list", std::max<int64_t>(L.n, 1));
+    gw.list_n = ovf + 6;
+    gw.ovf = ovf;
+    gw.debug = debug;
+    auto mean = [](int64_t a, int64_t b) { return b > 0 ? (double)a / (double)b : 0.0; };
     if (NG > 0) {
       k_sort_members<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem);
       count_launches(1);
@@ -1324,14 +1361,14 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     // ---- prolongator P (fine rows of continuing charts)
     int32_t* cnt = ctx.ws.get<int32_t>(tag + ".pcnt", L.n);
     L.poff = ctx.ws.get<int64_t>(tag + ".poff", L.n + 1);
-    k_prolong<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, smooth ? 1 : 0, cnt,
+    k_prolong<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, smooth ? 1 : 0, pmax, cnt,
                                               nullptr, nullptr, nullptr, ovf);
     count_launches(1);
     const int64_t PN = offsets_from_counts(ctx, cnt, L.n, L.poff, tag + ".po");
     L.n_pnnz = PN;
     L.pc = ctx.ws.get<int32_t>(tag + ".pc", PN);
     L.pv = ctx.ws.get<float>(tag + ".pv", PN);
-    k_prolong<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, smooth ? 1 : 0, cnt,
+    k_prolong<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, smooth ? 1 : 0, pmax, cnt,
                                               L.poff, L.pc, L.pv, ovf);
     count_launches(1);
     // ---- R = P^T
@@ -1347,16 +1384,13 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     RUV_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * std::max<int64_t>(NA, 1), s));
     L.rc = ctx.ws.get<int32_t>(tag + ".rc", PN);
     L.rv = ctx.ws.get<float>(tag + ".rv", PN);
-    k_scatter_t<<<div_up(L.n, B), B, 0, s>>>(L.n, L.poff, L.pc, L.pv, L.roff, cursor, L.rc, L.rv);
-    k_sort_rows<<<div_up(NA, B), B, 0, s>>>(NA, L.roff, L.rc, L.rv);
+    int32_t* rc_tmp = ctx.ws.get<int32_t>("amg.rc_tmp", PN);
+    float* rv_tmp = ctx.ws.get<float>("amg.rv_tmp", PN);
+    k_scatter_t<<<div_up(L.n, B), B, 0, s>>>(L.n, L.poff, L.pc, L.pv, L.roff, cursor, rc_tmp, rv_tmp);
+    k_sort_rows<<<div_up(NA * 32, B), B, 0, s>>>(NA, L.roff, rc_tmp, rv_tmp, L.rc, L.rv);
     count_launches(2);
     int32_t* acnt = ctx.ws.get<int32_t>(ntag + ".acnt", NA);
     int64_t* aoff = ctx.ws.get<int64_t>(ntag + ".aoff", NA + 1);
-    GalWork gw;
-    gw.list = ctx.ws.get<int32_t>("amg.gal_list", std::max<int64_t>(std::max<int64_t>(L.n, NA), 1));
-    gw.list_n = ovf + 6;
-    gw.ovf = ovf;
-    gw.debug = debug;
     // the coarse operator's storage once its size is known
     auto alloc_coarse = [&](int64_t AN) {
       if (AN >= (int64_t)INT32_MAX) throw Error{RUV_ERR_BAD_INPUT, "coarse operator too large"};
@@ -1374,7 +1408,6 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
         count_launches(2);
       }
     };
-    auto mean = [](int64_t a, int64_t b) { return b > 0 ? (double)a / (double)b : 0.0; };
     int64_t WN = 0;
     if (!smooth) {
       // ---- tentative prolongator: A_c = R A P straight from A (keys through agg)
