@@ -4,9 +4,10 @@
 Workload (default): 4096 disk charts, triangle counts log-uniform in [50, 50 000] (seeded
 synthetic meshes, researchuv_gb300/workloads.py), one chart per disk, Dirichlet border pins
 (the reference's border-rectangle pass).  A step = one batched unfold of every chart: GPU
-assembly of the cotangent systems with the pins eliminated, the AMG hierarchy set-up on the
-GPU, one batched mixed-precision AMG-PCG over the packed block-diagonal operator to rel-res
-1e-12 per chart (double-float refinement), and the damped driver update.
+assembly of the cotangent systems with the pins eliminated, the smoothed-aggregation AMG
+hierarchy set-up on the GPU (--precond amg: tentative prolongators instead), one batched
+mixed-precision AMG-PCG over the packed block-diagonal operator to rel-res 1e-12 per chart
+(double-float refinement), and the damped driver update.
 
 * value  — unknowns/s (sum over charts of 2 * free vertices per step time), inputs resident
            in HBM (ruv_lscm_upload once), step time = device time of the three phases
@@ -61,7 +62,7 @@ def parse():
                     help="disks<N> (N disk charts, the default 4096 is the headline), hf1024, hf2048, "
                          "sphere<L> (the differentiation workload on an L x 2L sphere; sphere512 at full size)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--precond", default="amg", choices=["jacobi", "amg", "amg_sa", "none"])
+    ap.add_argument("--precond", default="amg_sa", choices=["jacobi", "amg", "amg_sa", "none"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-single-chart", action="store_true")
