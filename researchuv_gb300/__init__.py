@@ -82,6 +82,7 @@ SIGNATURES = {
     "ruv_rectangularize": (ctypes.c_int, [_vp, _P(_f64), _P(_u8), _P(_f64), _P(_f64)]),
     "ruv_host_alloc": (ctypes.c_int, [_vp, _i64, _P(_vp)]),
     "ruv_host_free": (None, [_vp]),
+    "ruv_selftest_fp64": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_uint64, _i64, _P(_i64), _P(_f64)]),
     "ruv_last_timings": (_i32, [_vp, _P(_f64), _i32]),
     "ruv_kernel_launches": (_i64, [_vp]),
     "ruv_cg_solve_noalloc": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _i64, _f64, ctypes.c_int, _P(_i64), _vp,
@@ -560,6 +561,17 @@ def rectangularize(ctx: Context, uv, border, n_charts: int):
     ctx.check(lib().ruv_rectangularize(ctx.h, _ptr(u, _f64), _ptr(b, _u8), _ptr(q, _f64), _ptr(ext, _f64)),
               "ruv_rectangularize")
     return q, ext[:n_charts]
+
+
+def selftest_fp64(ctx: Context, mode: int, seed: int, n: int):
+    """Bitwise comparison of the assembly's FP64 division / square root (integer and FP32
+    pipes) with the hardware operations on n seeded inputs of class `mode` (0-5).  Returns
+    (mismatches, (a, b, got, want) of the first)."""
+    bad = _i64(0)
+    first = np.zeros(4, np.float64)
+    ctx.check(lib().ruv_selftest_fp64(ctx.h, int(mode), ctypes.c_uint64(seed), int(n), ctypes.byref(bad),
+                                      _ptr(first, _f64)), "ruv_selftest_fp64")
+    return bad.value, tuple(first)
 
 
 def export_chart_system(ctx: Context, chart: int):

@@ -7,12 +7,14 @@
 // rows are contiguous and ascend with the chart-local vertex id, exactly like the
 // reference's free_pos map (lscm.rs:582-592).
 //
-// Bit-exactness: every floating operation uses the explicit round-to-nearest intrinsics
-// (__dadd_rn, __dmul_rn, __ddiv_rn, __dsqrt_rn: never contracted into FMAs) in the
+// Bit-exactness: every floating operation is an explicit round-to-nearest operation
+// (__dadd_rn, __dmul_rn, and division and square root by div_rn / sqrt_rn, which give the
+// bits of __ddiv_rn / __dsqrt_rn off the FP64 pipe; never contracted into FMAs) in the
 // reference's evaluation order, and every sum runs in the reference's order (edge weight:
 // triangle order; diagonal and right-hand side: ascending neighbour id), so the CSR
 // pattern, values and right-hand side are bit-identical to the reference's
 // Sparse::to_csr(2 nf) (sparse.rs:69-84) of the same chart.
+#include "fp64rn.cuh"
 #include "system.cuh"
 
 namespace ruv {
@@ -21,7 +23,7 @@ namespace {
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return div_rn(a, b); }  // = __ddiv_rn
 
 struct P3 {
   double x, y, z;
@@ -32,7 +34,7 @@ __device__ __forceinline__ double pdot(P3 a, P3 b) { return dadd(dadd(dmul(a.x, 
 __device__ __forceinline__ P3 pcross(P3 a, P3 b) {
   return {dsub(dmul(a.y, b.z), dmul(a.z, b.y)), dsub(dmul(a.z, b.x), dmul(a.x, b.z)), dsub(dmul(a.x, b.y), dmul(a.y, b.x))};
 }
-__device__ __forceinline__ double plen(P3 a) { return __dsqrt_rn(pdot(a, a)); }
+__device__ __forceinline__ double plen(P3 a) { return sqrt_rn(pdot(a, a)); }  // = __dsqrt_rn
 __device__ __forceinline__ double rs_max(double a, double b) {  // Rust f64::max
   if (a != a) return b;
   if (b != b) return a;
@@ -574,6 +576,90 @@ void driver_update(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x
     iters[c] = hs[c].iters;
     err_accum[c] = hs[c].err_accum;
   }
+}
+
+namespace {
+// ---------------------------------------------------------------- self-test of div_rn / sqrt_rn
+// Seeded inputs (splitmix64 of seed + i), compared bit for bit with the hardware operations.
+// mode 0: quotients of random significands, exponents within +-60 of 1, random signs;
+// 1: quotients of arbitrary bit patterns (every class: zeros, subnormals, infinities, NaNs,
+//    quotients leaving the normal range); 2: quotients near a midpoint (a = b q rounded, moved
+//    by -2..2 ulps); 3: square roots, exponents within +-60; 4: square roots of arbitrary bit
+//    patterns; 5: square roots near perfect squares (s^2 exact for s < 2^26, moved by -2..2
+//    ulps, scaled by 4^k).
+__device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double bits_d(uint64_t u) { return __longlong_as_double((long long)u); }
+__device__ __forceinline__ uint64_t d_bits(double d) { return (uint64_t)__double_as_longlong(d); }
+
+__global__ void k_fp64_selftest(int mode, uint64_t seed, int64_t n, unsigned long long* __restrict__ bad,
+                                double* __restrict__ first) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t r0 = splitmix64(seed + 3 * (uint64_t)i), r1 = splitmix64(seed + 3 * (uint64_t)i + 1),
+                 r2 = splitmix64(seed + 3 * (uint64_t)i + 2);
+  double a = 0.0, b = 0.0, got, want;
+  if (mode <= 2) {
+    if (mode == 0) {
+      a = bits_d((r0 & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 60 + (int)(r2 % 121)) << 52));
+      b = bits_d((r1 & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 60 + (int)((r2 >> 8) % 121)) << 52));
+    } else if (mode == 1) {
+      a = bits_d(r0);
+      b = bits_d(r1);
+    } else {
+      b = bits_d((r1 & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 30 + (int)(r2 % 61)) << 52));
+      const double q = bits_d((r0 & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 30 + (int)((r2 >> 8) % 61)) << 52));
+      a = bits_d(d_bits(__dmul_rn(b, q)) + (uint64_t)((int)((r2 >> 16) % 5) - 2));
+    }
+    got = div_rn(a, b);
+    want = __ddiv_rn(a, b);
+  } else {
+    if (mode == 3) {
+      a = bits_d((r0 & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 60 + (int)(r2 % 121)) << 52));
+    } else if (mode == 4) {
+      a = bits_d(r0);
+    } else {
+      const double sq = (double)(r0 & ((1ull << 26) - 1)) + 1.0;
+      const double x = __dmul_rn(sq, sq);  // exact
+      const int k = (int)(r2 % 61) - 30;
+      a = bits_d(d_bits(x) + (uint64_t)((int)((r2 >> 8) % 5) - 2)) * exp2((double)(2 * k));
+    }
+    got = sqrt_rn(a);
+    want = __dsqrt_rn(a);
+  }
+  if (d_bits(got) != d_bits(want)) {
+    if (atomicAdd(bad, 1ull) == 0ull) {
+      first[0] = a;
+      first[1] = b;
+      first[2] = got;
+      first[3] = want;
+    }
+  }
+}
+
+}  // namespace
+
+int64_t fp64_selftest(Ctx& ctx, int mode, uint64_t seed, int64_t n, double* first4) {
+  cudaStream_t s = ctx.stream;
+  unsigned long long* bad = ctx.ws.get<unsigned long long>("selftest.bad", 1);
+  double* first = ctx.ws.get<double>("selftest.first", 4);
+  RUV_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), s));
+  RUV_CUDA(cudaMemsetAsync(first, 0, 4 * sizeof(double), s));
+  if (n > 0) {
+    k_fp64_selftest<<<div_up(n, 256), 256, 0, s>>>(mode, seed, n, bad, first);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+  }
+  unsigned long long h = 0;
+  RUV_CUDA(cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaMemcpyAsync(first4, first, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  return (int64_t)h;
 }
 
 }  // namespace ruv

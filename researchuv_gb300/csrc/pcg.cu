@@ -41,6 +41,10 @@ constexpr int kTileThreads = 256;
 constexpr int kChartThreads = 128;
 constexpr int kCheckEvery = 16;
 constexpr double kDelta = 0.01;  // refresh after a 100x drop of the FP32 residual
+inline double refresh_delta() {
+  const char* e = std::getenv("RUV_REFRESH_DELTA");
+  return e ? std::atof(e) : kDelta;
+}
 
 enum : int32_t { kActive = 0, kDone = 1 };
 
@@ -638,7 +642,7 @@ __global__ void __launch_bounds__(kChartThreads) k_chart_beta(Tiles T, ChartStat
 __global__ void __launch_bounds__(kChartThreads) k_chart_beta_mixed(Tiles T, ChartState* __restrict__ st,
                                                                     const double* __restrict__ part, int precond_none,
                                                                     int64_t max_iter, int* __restrict__ n_active,
-                                                                    int separate_precond) {
+                                                                    int separate_precond, double delta) {
   __shared__ double sh[2 * 32];
   int64_t c = blockIdx.x;
   if (st[c].state != kActive) return;
@@ -649,7 +653,7 @@ __global__ void __launch_bounds__(kChartThreads) k_chart_beta_mixed(Tiles T, Cha
   s.iters += 1;
   double rn = sqrt(v[0]);
   double rznew = precond_none ? v[0] : v[1];
-  if (rn <= kDelta * s.r_ref || rn <= s.tol_abs || !isfinite(rn) || s.iters >= max_iter) {
+  if (rn <= delta * s.r_ref || rn <= s.tol_abs || !isfinite(rn) || s.iters >= max_iter) {
     s.refresh = 1;  // beta is formed after the refresh, from the true residual
   } else {
     s.refresh = 0;
@@ -893,7 +897,8 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
       if (!mixed) {
         k_chart_beta<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active);
       } else {
-        k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0);
+        k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0,
+                                                                  refresh_delta());
         k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, mx.xdf, reinterpret_cast<float*>(xs), x64);
         if (sys.cols16)
           k_true_residual<NR, LPR, U, true><<<(unsigned)NTL, kTileThreads, 0, s>>>(
@@ -1018,7 +1023,8 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
       k_chart_alpha<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, n_active);
       k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, dinv, 2, xiter, r, z, p, q, part);
       if (mixed) {
-        k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1);
+        k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1,
+                                                                  refresh_delta());
         k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, mx.xdf, reinterpret_cast<float*>(xs), x64);
         if (sys.cols16)
           k_true_residual<NR, LPR, U, true><<<(unsigned)NTL, kTileThreads, 0, s>>>(

@@ -119,6 +119,10 @@ void chart_metrics(Ctx& ctx, const DevBatch& bt, const double* uv, std::vector<d
 // rectangularize (unwrap/src/metrics.rs:147-227) per chart: q (2 * n_verts) in [0,1]^2 per
 // chart, ext (2 * n_charts) the extents before normalisation; border: one flag per vertex.
 void rectangularize(Ctx& ctx, const DevBatch& bt, const double* uv, const uint8_t* border, double* q, double* ext);
+// Bitwise comparison of div_rn / sqrt_rn with the hardware operations on n seeded inputs of
+// class `mode` (0-5, see assemble.cu); returns the mismatch count, first4 = (a, b, got, want)
+// of the first mismatch.
+int64_t fp64_selftest(Ctx& ctx, int mode, uint64_t seed, int64_t n, double* first4);
 
 // Damped driver update (unfold_chart's loop, lscm.rs:570-719) on the device: writes uv
 // (2 * n_verts) and per-chart driver iterations / err_accum.
