@@ -35,6 +35,25 @@ __device__ __forceinline__ P3 pcross(P3 a, P3 b) {
   return {dsub(dmul(a.y, b.z), dmul(a.z, b.y)), dsub(dmul(a.z, b.x), dmul(a.x, b.z)), dsub(dmul(a.x, b.y), dmul(a.y, b.x))};
 }
 __device__ __forceinline__ double plen(P3 a) { return sqrt_rn(pdot(a, a)); }  // = __dsqrt_rn
+__device__ __forceinline__ P3 pneg(P3 a) {  // sign flips (integer pipe)
+  constexpr long long kSign = (long long)0x8000000000000000ull;
+  return {__longlong_as_double(__double_as_longlong(a.x) ^ kSign), __longlong_as_double(__double_as_longlong(a.y) ^ kSign),
+          __longlong_as_double(__double_as_longlong(a.z) ^ kSign)};
+}
+__device__ __forceinline__ bool is_nan_bits(long long b) {
+  return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+// x <= c for a positive constant c, on the integer pipe: non-negative doubles order as their
+// bit patterns, negative ones (and -0) read as negative integers, NaN compares false
+__device__ __forceinline__ bool le_pos(double x, double c) {
+  const long long b = __double_as_longlong(x);
+  return !is_nan_bits(b) && b <= __double_as_longlong(c);
+}
+// Rust f64::max(x, 0.0) on the integer pipe: NaN -> 0, positive -> x, zeros and negatives -> +0
+__device__ __forceinline__ double max0(double x) {
+  const long long b = __double_as_longlong(x);
+  return (!is_nan_bits(b) && b > 0) ? x : 0.0;
+}
 __device__ __forceinline__ double rs_max(double a, double b) {  // Rust f64::max
   if (a != a) return b;
   if (b != b) return a;
@@ -76,21 +95,28 @@ __global__ void k_corner_cot(const double* __restrict__ p3, const int32_t* __res
   if (t >= n_tris) return;
   int32_t v[3] = {tri_g[3 * t], tri_g[3 * t + 1], tri_g[3 * t + 2]};
   P3 p[3] = {ld3(p3, v[0]), ld3(p3, v[1]), ld3(p3, v[2])};
-  // |p[k+1] - p[k]|, each edge once: a - b is exactly -(b - a) in IEEE arithmetic and the
-  // squares are equal, so both corners at an edge see the same length bit for bit
+  // edge vectors e_k = p[k+1] - p[k] and their lengths, each once: the corner vectors are
+  // e1 - o = p[m+2] - p[m] = -e_{m+2} (IEEE subtraction is antisymmetric: only the sign of an
+  // exact zero can differ, which no step below turns into a different nonzero value, and the
+  // clamp maps both zeros to +0) and e0 - o = e_m; the squares make the lengths of both
+  // corners at an edge the same bits
+  P3 e[3];
   double len[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) len[k] = plen(psub(p[(k + 1) % 3], p[k]));
+  for (int k = 0; k < 3; ++k) {
+    e[k] = psub(p[(k + 1) % 3], p[k]);
+    len[k] = plen(e[k]);
+  }
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
-    P3 a1 = psub(p[(m + 2) % 3], p[m]);  // e1 - o
-    P3 a2 = psub(p[(m + 1) % 3], p[m]);  // e0 - o
-    double la = len[(m + 2) % 3], lb = len[m];
+    const P3 a1 = pneg(e[(m + 2) % 3]);  // e1 - o
+    const P3 a2 = e[m];                  // e0 - o
+    const double la = len[(m + 2) % 3], lb = len[m];
     double c = 0.0;
-    if (!(la <= kEpsDegenerate || lb <= kEpsDegenerate)) {
-      double lab = dmul(la, lb);
-      double s = ddiv(plen(pcross(a1, a2)), lab);
-      if (!(s <= kEpsDegenerate)) c = rs_max(ddiv(ddiv(pdot(a1, a2), lab), s), 0.0);
+    if (!(le_pos(la, kEpsDegenerate) || le_pos(lb, kEpsDegenerate))) {
+      const double lab = dmul(la, lb);
+      const double sn = ddiv(plen(pcross(a1, a2)), lab);
+      if (!le_pos(sn, kEpsDegenerate)) c = max0(ddiv(ddiv(pdot(a1, a2), lab), sn));
     }
     cot[3 * t + m] = c;
   }

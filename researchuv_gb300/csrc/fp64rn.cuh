@@ -51,9 +51,16 @@ __device__ __forceinline__ I128 i128_sub(I128 r, uint64_t v) {
 }
 // r >= v for a non-negative v below 2^64
 __device__ __forceinline__ bool i128_ge(I128 r, uint64_t v) { return !i128_neg(r) && (r.hi != 0 || r.lo >= v); }
-// float(r / 2^32), for |r| < 2^95
+// float(r / 2^32), for |r| < 2^95, from two 32-bit conversions (64-bit integer <-> float
+// conversions would run on the FP64 pipe); about 2^-23 relative, enough for a correction
 __device__ __forceinline__ float i128_f32_shr32(I128 r) {
-  return __ll2float_rn((long long)((r.hi << 32) | (r.lo >> 32)));
+  const long long v = (long long)((r.hi << 32) | (r.lo >> 32));
+  return __fmaf_rn(__int2float_rn((int)(v >> 32)), 4294967296.0f, __uint2float_rn((unsigned)v));
+}
+// c rounded to an integer multiple of 2^SH, for |c| < 2^(31 + SH), via a 32-bit conversion
+template <int SH>
+__device__ __forceinline__ uint64_t f32_to_step(float c) {
+  return (uint64_t)(long long)__float2int_rn(__fmul_rn(c, 1.0f / (float)(1u << SH))) << SH;
 }
 
 constexpr uint64_t kFp64Frac = (1ull << 52) - 1;
@@ -75,14 +82,13 @@ __device__ __forceinline__ double div_rn(double a, double b) {
   // Q = floor(N / mb), N = ma 2^53 (107 bits), Q in [2^53, 2^54)
   const uint64_t nhi = ma >> 11, nlo = ma << 53;
   const float rb = __frcp_rn(__uint2float_rn((uint32_t)(mb >> 29)));  // ~ 2^29 / mb
-  // seed: (ma 2^-30) (2^29 / mb) ~ (ma / mb) / 2 in [0.5, 1), times 2^54
-  uint64_t q = __float2ull_rz(__fmul_rn(__fmul_rn(__uint2float_rn((uint32_t)(ma >> 30)), rb), 4294967296.0f)) << 22;
+  // seed: (ma 2^-30) (2^29 / mb) ~ (ma / mb) / 2 in [0.5, 1], times 2^54 (error below 2^33)
+  uint64_t q = (uint64_t)__float2uint_rz(__fmul_rn(__fmul_rn(__uint2float_rn((uint32_t)(ma >> 30)), rb), 2147483648.0f))
+               << 23;
   const float rb8 = __fmul_rn(rb, 8.0f);  // (r / 2^32) * rb8 ~ r / mb
-#pragma unroll
-  for (int it = 0; it < 2; ++it) {
-    const I128 r = i128_sub_mul(nhi, nlo, q, mb);
-    q += (uint64_t)__float2ll_rn(__fmul_rn(i128_f32_shr32(r), rb8));
-  }
+  // first correction to a multiple of 2^8 (error then below 2^11), second exact to one unit
+  q += f32_to_step<8>(__fmul_rn(i128_f32_shr32(i128_sub_mul(nhi, nlo, q, mb)), rb8));
+  q += f32_to_step<0>(__fmul_rn(i128_f32_shr32(i128_sub_mul(nhi, nlo, q, mb)), rb8));
   I128 r = i128_sub_mul(nhi, nlo, q, mb);
   for (int k = 0; k < 3 && i128_neg(r); ++k) {
     q -= 1;
@@ -116,13 +122,11 @@ __device__ __forceinline__ double sqrt_rn(double x) {
   // S = floor(sqrt(N)), N = m 2^54 (108 bits), S in [2^53, 2^54); sqrt(x) = S 2^(e/2 - 53)
   const uint64_t nhi = m >> 10, nlo = m << 54;
   const float sf = __fsqrt_rn(__uint2float_rn((uint32_t)(m >> 30)));  // ~ sqrt(m) 2^-15
-  uint64_t s = __float2ull_rz(__fmul_rn(sf, 1048576.0f)) << 22;
-  const float k2s = __fmul_rn(__frcp_rn(__ull2float_rn(s)), 2147483648.0f);  // (r / 2^32) * k2s ~ r / 2S
-#pragma unroll
-  for (int it = 0; it < 2; ++it) {
-    const I128 r = i128_sub_mul(nhi, nlo, s, s);
-    s += (uint64_t)__float2ll_rn(__fmul_rn(i128_f32_shr32(r), k2s));
-  }
+  uint64_t s = (uint64_t)__float2uint_rz(__fmul_rn(sf, 1048576.0f)) << 22;  // error below 2^31
+  // (r / 2^32) * k2s ~ r / 2S: k2s = 2^31 / S ~ 2 / (S >> 30)
+  const float k2s = __fmul_rn(__frcp_rn(__uint2float_rn((uint32_t)(s >> 30))), 2.0f);
+  s += f32_to_step<8>(__fmul_rn(i128_f32_shr32(i128_sub_mul(nhi, nlo, s, s)), k2s));
+  s += f32_to_step<0>(__fmul_rn(i128_f32_shr32(i128_sub_mul(nhi, nlo, s, s)), k2s));
   I128 r = i128_sub_mul(nhi, nlo, s, s);  // floor: 0 <= N - S^2 < 2S + 1
   for (int k = 0; k < 3 && i128_neg(r); ++k) {
     r = i128_add(r, 2 * s - 1);
