@@ -31,10 +31,10 @@ struct P3 {
 __device__ __forceinline__ P3 ld3(const double* p, int64_t i) { return {p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
 __device__ __forceinline__ P3 psub(P3 a, P3 b) { return {dsub(a.x, b.x), dsub(a.y, b.y), dsub(a.z, b.z)}; }
 __device__ __forceinline__ double pdot(P3 a, P3 b) { return dadd(dadd(dmul(a.x, b.x), dmul(a.y, b.y)), dmul(a.z, b.z)); }
+__device__ __forceinline__ double plen(P3 a) { return sqrt_rn(pdot(a, a)); }  // = __dsqrt_rn
 __device__ __forceinline__ P3 pcross(P3 a, P3 b) {
   return {dsub(dmul(a.y, b.z), dmul(a.z, b.y)), dsub(dmul(a.z, b.x), dmul(a.x, b.z)), dsub(dmul(a.x, b.y), dmul(a.y, b.x))};
 }
-__device__ __forceinline__ double plen(P3 a) { return sqrt_rn(pdot(a, a)); }  // = __dsqrt_rn
 __device__ __forceinline__ P3 pneg(P3 a) {  // sign flips (integer pipe)
   constexpr long long kSign = (long long)0x8000000000000000ull;
   return {__longlong_as_double(__double_as_longlong(a.x) ^ kSign), __longlong_as_double(__double_as_longlong(a.y) ^ kSign),
@@ -53,6 +53,34 @@ __device__ __forceinline__ bool le_pos(double x, double c) {
 __device__ __forceinline__ double max0(double x) {
   const long long b = __double_as_longlong(x);
   return (!is_nan_bits(b) && b > 0) ? x : 0.0;
+}
+// x < 0.0 and x != 0.0 on the integer pipe (-0 is not below zero; NaN is unequal to zero)
+__device__ __forceinline__ bool lt0(double x) {
+  const long long b = __double_as_longlong(x);
+  return b < 0 && (b & 0x7fffffffffffffffll) != 0 && !is_nan_bits(b);
+}
+__device__ __forceinline__ double dneg(double x) {  // -x (sign flip on the integer pipe)
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+__device__ __forceinline__ bool ne0(double x) { return (__double_as_longlong(x) & 0x7fffffffffffffffll) != 0; }
+// Rust f64::max(x, c) for a positive constant c, on the integer pipe
+__device__ __forceinline__ double max_pos(double x, double c) {
+  const long long b = __double_as_longlong(x);
+  return (!is_nan_bits(b) && b > __double_as_longlong(c)) ? x : c;
+}
+// (float)x, round to nearest-even, on the integer pipe (double-to-float conversions run on the
+// FP64 pipe); zeros, results outside float's normal range, infinities and NaNs go to the
+// hardware conversion
+__device__ __forceinline__ float f32_rn(double x) {
+  const uint64_t u = (uint64_t)__double_as_longlong(x);
+  const int ef = (int)((u >> 52) & 0x7ff) - 1023 + 127;
+  if (ef <= 0 || ef >= 255) return __double2float_rn(x);
+  uint32_t mf = (uint32_t)((u >> 29) & 0x7fffffu);
+  const uint64_t rest = u & ((1ull << 29) - 1), half = 1ull << 28;
+  if (rest > half || (rest == half && (mf & 1u))) mf += 1;  // a carry moves into the exponent
+  const uint32_t fb = ((uint32_t)ef << 23) + mf;
+  if ((fb >> 23) >= 255u) return __double2float_rn(x);
+  return __uint_as_float(fb | ((uint32_t)(u >> 32) & 0x80000000u));
 }
 __device__ __forceinline__ double rs_max(double a, double b) {  // Rust f64::max
   if (a != a) return b;
@@ -217,9 +245,9 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
     double w = 0.0;
     for (; j < r1 && rec[j].x == nb; ++j) w = dadd(w, cot[rec[j].y]);
     double c = -1.0;
-    if (!(w <= kEpsDegenerate)) {  // lscm.rs:606
+    if (!le_pos(w, kEpsDegenerate)) {  // lscm.rs:606
       P3 d3 = psub(ld3(p3, nb), pv);
-      c = ddiv(w, rs_max(pdot(d3, d3), kEpsDegenerate));
+      c = ddiv(w, max_pos(pdot(d3, d3), kEpsDegenerate));
     }
     coef[i] = c;
     return c;
@@ -233,8 +261,8 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
     int64_t j;
     const double c = group(i, j);
     i = j;
-    if (c < 0.0) continue;  // dropped: w <= EPS
-    if (c != 0.0) {  // Sparse::add skips zeros (sparse.rs:47-52)
+    if (lt0(c)) continue;  // dropped: w <= EPS
+    if (ne0(c)) {  // Sparse::add skips zeros (sparse.rs:47-52)
       dg = dadd(dg, c);
       has_diag = true;
       if (!pinned[nb]) ++n_off;
@@ -255,31 +283,31 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
     int64_t j;
     const double c = group(i, j);
     i = j;
-    if (c < 0.0) continue;
+    if (lt0(c)) continue;
     // dv as the reference forms it: d = p2[hi] - p2[lo], negated for the higher endpoint
     double du, dw;
     if (v < nb) {
       du = dsub(p2[2 * nb], p2u);
       dw = dsub(p2[2 * nb + 1], p2v);
     } else {
-      du = -dsub(p2u, p2[2 * nb]);
-      dw = -dsub(p2v, p2[2 * nb + 1]);
+      du = dneg(dsub(p2u, p2[2 * nb]));
+      dw = dneg(dsub(p2v, p2[2 * nb + 1]));
     }
     double mc = dmul(mix_b, c);
     if (!pinned[nb]) {
       bu = dadd(bu, dmul(mc, du));
       bv = dadd(bv, dmul(mc, dw));
-      if (c != 0.0) {
+      if (ne0(c)) {
         if (!diag_done && nb > v) {
           cols[at] = (int32_t)row;
           vals[at] = dg;
-          vals32[at] = (float)dg;
+          vals32[at] = f32_rn(dg);
           ++at;
           diag_done = true;
         }
         cols[at] = (int32_t)row_of[nb];
-        vals[at] = -c;
-        vals32[at] = (float)(-c);
+        vals[at] = dneg(c);
+        vals32[at] = f32_rn(dneg(c));
         ++at;
       }
     } else {
@@ -290,7 +318,7 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
   if (!diag_done) {
     cols[at] = (int32_t)row;
     vals[at] = dg;
-    vals32[at] = (float)dg;
+    vals32[at] = f32_rn(dg);
   }
   diag_out[row] = dg;
   b[2 * row] = bu;

@@ -3,7 +3,9 @@
 // correctly rounded FP64 division or square root costs the FP64 pipe about ten operations;
 // the assembly's bit-exact cotangents need nine divisions and six square roots per
 // triangle.  These routines give the same bits as the IEEE operations (__ddiv_rn,
-// __dsqrt_rn) for every input.
+// __dsqrt_rn) for every input.  (Additions and multiplications stay on the FP64 pipe: an
+// integer multiplication of two 53-bit significands -- a 64-bit high and low product plus
+// the rounding -- measured no cheaper than the FP64 multiply it would replace.)
 //
 // Method: Newton-Raphson on the integer result with an exact residual, then an exact
 // remainder test for the rounding (the classical scheme for correctly rounded division and
