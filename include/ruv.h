@@ -263,6 +263,16 @@ typedef struct ruv_prepared ruv_prepared;
  * (lscm.rs:280-413) or 4 anchors for closed charts (lscm.rs:210-247, :524-542). */
 ruv_status ruv_prepare_mesh(const double* pos, int64_t n_verts, const int32_t* faces, int64_t n_faces,
                             double weld_tol, double angle_min_deg, int32_t threads, ruv_prepared** out);
+/* ruv_prepare_mesh with its data-parallel stages on the device of ctx: the weld (a device
+ * hash table keeping the reference's first occurrence), the edge-face lists (a stable radix
+ * sort of the edge keys), the face normals and dihedral cut flags (round-to-nearest FP64;
+ * the acos test as a threshold on n1.n2 derived from the host libm) and the per-chart vertex
+ * sets (a radix sort of (chart, vertex) keys).  The DFS component order, border loops,
+ * frames and pins stay on the host.  The result equals ruv_prepare_mesh's bit for bit
+ * (weld.rs:19-57, segment.rs:61-331, lscm.rs:152-413 as there). */
+ruv_status ruv_prepare_mesh_gpu(ruv_ctx* ctx, const double* pos, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                                double weld_tol, double angle_min_deg, int32_t threads, ruv_prepared** out);
+
 /* Charts given directly (one chart per patch, no weld / segmentation): patch c owns
  * vertices [vert_off[c], vert_off[c+1]) and triangles [tri_off[c], tri_off[c+1]) with
  * patch-local indices.  Border loops are walked over each patch's boundary edges. */

@@ -66,6 +66,7 @@ SIGNATURES = {
     "ruv_lscm_solve_batch": (ctypes.c_int, [_vp, _P(RuvBatch), _P(RuvUnfoldOpts), _P(_f64), _P(RuvChartStat)]),
     "ruv_prepare_mesh": (ctypes.c_int, [_P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _i32, _P(_vp)]),
     "ruv_prepare_patches": (ctypes.c_int, [_i64, _P(_i64), _P(_i64), _P(_f64), _P(_i32), _i32, _P(_vp)]),
+    "ruv_prepare_mesh_gpu": (ctypes.c_int, [_vp, _P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _i32, _P(_vp)]),
     "ruv_prepared_free": (None, [_vp]),
     "ruv_prepared_batch": (ctypes.c_int, [_vp, _P(RuvBatch)]),
     "ruv_prepared_get_i64": (_i64, [_vp, _cp, _P(_i64)]),
@@ -395,11 +396,17 @@ class Charts:
 
 
 def prepare_mesh(positions, faces, weld_tol: float = 1e-12, angle_min_deg: float = 30.0,
-                 threads: int = 0) -> Charts:
-    """weld (weld.rs:19-57) + segment (segment.rs:130-331) + per-chart frames and pins."""
+                 threads: int = 0, ctx: Optional["Context"] = None) -> Charts:
+    """weld (weld.rs:19-57) + segment (segment.rs:130-331) + per-chart frames and pins.
+    With a Context, the weld, edge-face lists, cut flags and chart vertex sets run on its
+    device (ruv_prepare_mesh_gpu); the result is the same bit for bit."""
     p = np.ascontiguousarray(positions, np.float64).reshape(-1, 3)
     f = np.ascontiguousarray(faces, np.int32).reshape(-1, 3)
     h = _vp()
+    if ctx is not None:
+        ctx.check(lib().ruv_prepare_mesh_gpu(ctx.h, _ptr(p, _f64), p.shape[0], _ptr(f, _i32), f.shape[0], weld_tol,
+                                             angle_min_deg, threads, ctypes.byref(h)), "ruv_prepare_mesh_gpu")
+        return Charts(h)
     st = lib().ruv_prepare_mesh(_ptr(p, _f64), p.shape[0], _ptr(f, _i32), f.shape[0], weld_tol, angle_min_deg,
                                 threads, ctypes.byref(h))
     if st != 0:

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libruv.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_SOURCES = ["adjoint.cu", "amg.cu", "api.cu", "assemble.cu", "ic0.cu", "pcg.cu", "scan.cu"]
+CU_SOURCES = ["adjoint.cu", "amg.cu", "api.cu", "assemble.cu", "ic0.cu", "pcg.cu", "prep_gpu.cu", "scan.cu"]
 CXX_SOURCES = ["prep.cpp"]
 HEADERS = ["common.cuh", "system.cuh", "ruv_internal.h"]
 

@@ -631,6 +631,22 @@ ruv_status ruv_prepare_mesh(const double* pos, int64_t n_verts, const int32_t* f
   }
 }
 
+ruv_status ruv_prepare_mesh_gpu(ruv_ctx* ctx, const double* pos, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                                double weld_tol, double angle_min_deg, int32_t threads, ruv_prepared** out) {
+  if (!ctx || !out || n_verts < 0 || n_faces < 0 || (n_verts > 0 && !pos) || (n_faces > 0 && !faces))
+    return RUV_ERR_BAD_INPUT;
+  if (n_verts >= (int64_t)INT32_MAX || n_faces >= (int64_t)INT32_MAX / 3) return RUV_ERR_BAD_INPUT;
+  *out = nullptr;
+  return guarded(ctx, [&]() -> ruv_status {
+    std::unique_ptr<ruv_prepared> p(new ruv_prepared());
+    std::string err;
+    ruv_status s = prepare_mesh_gpu(ctx->c, pos, n_verts, faces, n_faces, weld_tol, angle_min_deg, threads, p->p, err);
+    if (s != RUV_OK) return fail(ctx, s, err.empty() ? "mesh preparation failed" : err);
+    *out = p.release();
+    return RUV_OK;
+  });
+}
+
 ruv_status ruv_prepare_patches(int64_t n_patches, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
                                const int32_t* tris, int32_t threads, ruv_prepared** out) {
   if (!out || n_patches < 0 || !vert_off || !tri_off) return RUV_ERR_BAD_INPUT;

@@ -12,6 +12,9 @@
 // Compiled with -ffp-contract=off (no FMA contraction).
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstdio>
+#include <chrono>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -320,21 +323,28 @@ inline bool slot_is_border(const MeshView& m, int64_t slot) {
   return m.cut[slot] || (m.ef.off[slot + 1] - m.ef.off[slot]) == 1;
 }
 
-void build_chart(const MeshView& m, ChartOut& ch) {
+// vertex set (segment.rs:177-196) and chart-local triangles
+void chart_sets(const MeshView& m, ChartOut& ch) {
   const auto& F = m.F;
-  // vertex set (segment.rs:177-196)
   ch.verts.clear();
   ch.verts.reserve(ch.faces.size() * 3);
   for (int32_t f : ch.faces)
     for (int k = 0; k < 3; ++k) ch.verts.push_back(F[3 * f + k]);
   std::sort(ch.verts.begin(), ch.verts.end());
   ch.verts.erase(std::unique(ch.verts.begin(), ch.verts.end()), ch.verts.end());
+  ch.tris.resize(ch.faces.size() * 3);
+  for (size_t t = 0; t < ch.faces.size(); ++t)
+    for (int k = 0; k < 3; ++k)
+      ch.tris[3 * t + k] =
+          (int32_t)(std::lower_bound(ch.verts.begin(), ch.verts.end(), F[3 * ch.faces[t] + k]) - ch.verts.begin());
+}
+
+// everything after the vertex set: border, area, loops, frame, pins
+void chart_finish(const MeshView& m, ChartOut& ch) {
+  const auto& F = m.F;
   auto local = [&](int32_t v) -> int32_t {
     return (int32_t)(std::lower_bound(ch.verts.begin(), ch.verts.end(), v) - ch.verts.begin());
   };
-  ch.tris.resize(ch.faces.size() * 3);
-  for (size_t t = 0; t < ch.faces.size(); ++t)
-    for (int k = 0; k < 3; ++k) ch.tris[3 * t + k] = local(F[3 * ch.faces[t] + k]);
   // border vertices and boundary edge set (segment.rs:198-209, :235-244)
   std::vector<uint64_t> bedges;
   ch.border.clear();
@@ -671,34 +681,24 @@ std::vector<double> face_areas(const std::vector<D3>& pos, const std::vector<int
   return a;
 }
 
-}  // namespace
-
 // ------------------------------------------------------------------ entry points
-ruv_status prepare_mesh(const double* pos, int64_t nv, const int32_t* faces, int64_t nf, double weld_tol,
-                        double angle_min_deg, int threads, Prepared& P, std::string& err) {
-  for (int64_t i = 0; i < 3 * nf; ++i)
-    if (faces[i] < 0 || faces[i] >= nv) {
-      err = "face index out of range";
-      return RUV_ERR_BAD_INPUT;
-    }
-  std::vector<D3> wpos;
-  std::vector<int32_t> F;
-  weld(pos, nv, faces, nf, weld_tol, wpos, F);
-  int64_t wnv = (int64_t)wpos.size(), wnf = (int64_t)F.size() / 3;
-  for (int64_t f = 0; f < wnf; ++f)
-    if (F[3 * f] == F[3 * f + 1] || F[3 * f + 1] == F[3 * f + 2] || F[3 * f] == F[3 * f + 2]) {
-      err = "degenerate face with a repeated vertex";  // only possible without welding
-      return RUV_ERR_BAD_INPUT;
-    }
-  P.mesh_pos.resize(3 * wnv);
-  for (int64_t i = 0; i < wnv; ++i) {
-    P.mesh_pos[3 * i] = wpos[i].x;
-    P.mesh_pos[3 * i + 1] = wpos[i].y;
-    P.mesh_pos[3 * i + 2] = wpos[i].z;
+// Stage timings on stderr when RUV_PREP_TIMING is set.
+struct StageClock {
+  bool on = std::getenv("RUV_PREP_TIMING") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const char* what) {
+    if (!on) return;
+    auto n = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "prep %-22s %9.3f ms\n", what, std::chrono::duration<double, std::milli>(n - t).count());
+    t = n;
   }
-  P.mesh_faces.assign(F.begin(), F.end());
-  EdgeFaces ef = build_edge_faces(wnv, F, threads);
-  // unit normals per face (segment.rs:104-117) and the cut flag per face slot
+};
+
+// face normals and the cut flag per face slot (segment.rs:85-137): an edge carried by one
+// face is never cut, by two faces when acos(n1.n2) > angle, by more always
+std::vector<uint8_t> cut_flags(const std::vector<D3>& wpos, const std::vector<int32_t>& F, const EdgeFaces& ef,
+                               double angle_min_deg, int threads) {
+  const int64_t wnf = (int64_t)F.size() / 3;
   std::vector<D3> nrm(wnf);
   parallel_for((wnf + 8191) / 8192, threads, [&](int64_t blk) {
     int64_t f1 = std::min(wnf, (blk + 1) * 8192);
@@ -727,9 +727,11 @@ ruv_status prepare_mesh(const double* pos, int64_t nv, const int32_t* faces, int
       cut[s] = ang > th ? 1 : 0;
     }
   });
-  P.n_cut_slots = 0;
-  for (uint8_t c : cut) P.n_cut_slots += c;
-  // face components over non-cut edges, DFS stack order (segment.rs:150-175)
+  return cut;
+}
+
+// face components over non-cut edges in the reference's DFS stack order (segment.rs:150-175)
+std::vector<ChartOut> dfs_components(int64_t wnf, const std::vector<uint8_t>& cut, const EdgeFaces& ef) {
   std::vector<uint8_t> seen(wnf, 0);
   std::vector<ChartOut> charts;
   std::vector<int32_t> stack;
@@ -756,6 +758,24 @@ ruv_status prepare_mesh(const double* pos, int64_t nv, const int32_t* faces, int
       }
     }
   }
+  return charts;
+}
+
+// DFS components, chart sets (from `sets`, or on the host), the per-chart finish and packing
+ruv_status finish_mesh(std::vector<D3>& wpos, std::vector<int32_t>& F, EdgeFaces& ef, std::vector<uint8_t>& cut,
+                       int threads, const ChartSetsFn* sets, StageClock& clk, Prepared& P, std::string& err) {
+  const int64_t wnv = (int64_t)wpos.size(), wnf = (int64_t)F.size() / 3;
+  P.mesh_pos.resize(3 * wnv);
+  for (int64_t i = 0; i < wnv; ++i) {
+    P.mesh_pos[3 * i] = wpos[i].x;
+    P.mesh_pos[3 * i + 1] = wpos[i].y;
+    P.mesh_pos[3 * i + 2] = wpos[i].z;
+  }
+  P.mesh_faces.assign(F.begin(), F.end());
+  P.n_cut_slots = 0;
+  for (uint8_t c : cut) P.n_cut_slots += c;
+  std::vector<ChartOut> charts = dfs_components(wnf, cut, ef);
+  clk.mark("components (DFS)");
   std::vector<double> farea = face_areas(wpos, F, threads);
   MeshView mv{wpos, F, ef, cut, farea};
   // biggest charts first for load balance; results land in their own slots
@@ -763,10 +783,104 @@ ruv_status prepare_mesh(const double* pos, int64_t nv, const int32_t* faces, int
   for (size_t i = 0; i < order.size(); ++i) order[i] = (int64_t)i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int64_t a, int64_t b) { return charts[a].faces.size() > charts[b].faces.size(); });
-  parallel_for((int64_t)charts.size(), threads, [&](int64_t i) { build_chart(mv, charts[order[i]]); });
+  if (sets) {
+    const int64_t nc = (int64_t)charts.size();
+    std::vector<int64_t> cf_off(nc + 1, 0);
+    for (int64_t c = 0; c < nc; ++c) cf_off[c + 1] = cf_off[c] + (int64_t)charts[c].faces.size();
+    std::vector<int32_t> cf(cf_off[nc]);
+    for (int64_t c = 0; c < nc; ++c) std::copy(charts[c].faces.begin(), charts[c].faces.end(), cf.begin() + cf_off[c]);
+    ChartSets cs;
+    if (!(*sets)(cf_off, cf, cs, err)) return RUV_ERR_INTERNAL;
+    parallel_for(nc, threads, [&](int64_t c) {
+      ChartOut& ch = charts[c];
+      ch.verts.assign(cs.verts.begin() + cs.vert_off[c], cs.verts.begin() + cs.vert_off[c + 1]);
+      ch.tris.assign(cs.tris.begin() + 3 * cf_off[c], cs.tris.begin() + 3 * cf_off[c + 1]);
+    });
+  } else {
+    parallel_for((int64_t)charts.size(), threads, [&](int64_t i) { chart_sets(mv, charts[order[i]]); });
+  }
+  clk.mark("chart vertex sets");
+  parallel_for((int64_t)charts.size(), threads, [&](int64_t i) { chart_finish(mv, charts[order[i]]); });
+  clk.mark("chart finish");
   pack_charts(charts, P);
-  (void)err;
+  clk.mark("pack");
   return RUV_OK;
+}
+
+}  // namespace
+
+ruv_status prepare_mesh(const double* pos, int64_t nv, const int32_t* faces, int64_t nf, double weld_tol,
+                        double angle_min_deg, int threads, Prepared& P, std::string& err) {
+  for (int64_t i = 0; i < 3 * nf; ++i)
+    if (faces[i] < 0 || faces[i] >= nv) {
+      err = "face index out of range";
+      return RUV_ERR_BAD_INPUT;
+    }
+  StageClock clk;
+  std::vector<D3> wpos;
+  std::vector<int32_t> F;
+  weld(pos, nv, faces, nf, weld_tol, wpos, F);
+  clk.mark("weld");
+  int64_t wnf = (int64_t)F.size() / 3;
+  for (int64_t f = 0; f < wnf; ++f)
+    if (F[3 * f] == F[3 * f + 1] || F[3 * f + 1] == F[3 * f + 2] || F[3 * f] == F[3 * f + 2]) {
+      err = "degenerate face with a repeated vertex";  // only possible without welding
+      return RUV_ERR_BAD_INPUT;
+    }
+  EdgeFaces ef = build_edge_faces((int64_t)wpos.size(), F, threads);
+  clk.mark("edge-faces");
+  std::vector<uint8_t> cut = cut_flags(wpos, F, ef, angle_min_deg, threads);
+  clk.mark("normals+cuts");
+  return finish_mesh(wpos, F, ef, cut, threads, nullptr, clk, P, err);
+}
+
+ruv_status prepare_mesh_topology(std::vector<double>&& wpos3, std::vector<int32_t>&& F, std::vector<int64_t>&& ef_off,
+                                 std::vector<int32_t>&& ef_faces, std::vector<uint8_t>&& cut, int threads,
+                                 const ChartSetsFn* sets, Prepared& P, std::string& err) {
+  StageClock clk;
+  const int64_t wnf = (int64_t)F.size() / 3;
+  for (int64_t f = 0; f < wnf; ++f)
+    if (F[3 * f] == F[3 * f + 1] || F[3 * f + 1] == F[3 * f + 2] || F[3 * f] == F[3 * f + 2]) {
+      err = "degenerate face with a repeated vertex";
+      return RUV_ERR_BAD_INPUT;
+    }
+  std::vector<D3> wpos(wpos3.size() / 3);
+  for (size_t i = 0; i < wpos.size(); ++i) wpos[i] = {wpos3[3 * i], wpos3[3 * i + 1], wpos3[3 * i + 2]};
+  EdgeFaces ef;
+  ef.off = std::move(ef_off);
+  ef.faces = std::move(ef_faces);
+  clk.mark("host copies");
+  return finish_mesh(wpos, F, ef, cut, threads, sets, clk, P, err);
+}
+
+double acos_cut_threshold(double angle_min_deg) {
+  // acos(d) > th  <=>  d < d*: the smallest d in [-1, 1] with acos(d) <= th, by bisection over
+  // the doubles in value order (acos is non-increasing); NaN when no such d exists or when
+  // acos is not monotone near d* (callers then keep the host test)
+  const double th = angle_min_deg * (kPi / 180.0);
+  auto idx_of = [](double d) -> int64_t {  // order-preserving integer index of a double (-0 = +0)
+    uint64_t u;
+    std::memcpy(&u, &d, 8);
+    return (u >> 63) ? -(int64_t)(u & 0x7fffffffffffffffull) : (int64_t)u;
+  };
+  auto dbl_of = [](int64_t k) -> double {
+    uint64_t u = k >= 0 ? (uint64_t)k : (0x8000000000000000ull | (uint64_t)(-k));
+    double d;
+    std::memcpy(&d, &u, 8);
+    return d;
+  };
+  auto cutp = [&](double d) { return std::acos(d) > th; };
+  int64_t lo = idx_of(-1.0), hi = idx_of(1.0);
+  if (!cutp(dbl_of(lo))) return -1.0;                       // nothing is ever cut: d < -1 never holds
+  if (cutp(dbl_of(hi))) return std::nextafter(1.0, 2.0);    // everything is cut
+  while (hi - lo > 1) {  // invariant: cutp(lo), !cutp(hi)
+    int64_t mid = lo + (hi - lo) / 2;
+    if (cutp(dbl_of(mid))) lo = mid; else hi = mid;
+  }
+  for (int64_t k = 1; k <= 256; ++k)
+    if ((lo - k >= idx_of(-1.0) && !cutp(dbl_of(lo - k))) || (hi + k <= idx_of(1.0) && cutp(dbl_of(hi + k))))
+      return std::numeric_limits<double>::quiet_NaN();
+  return dbl_of(hi);
 }
 
 ruv_status prepare_patches(int64_t np, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
@@ -841,7 +955,10 @@ ruv_status prepare_patches(int64_t np, const int64_t* vert_off, const int64_t* t
   for (int64_t i = 0; i < np; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int64_t a, int64_t b) { return charts[a].faces.size() > charts[b].faces.size(); });
-  parallel_for(np, threads, [&](int64_t i) { build_chart(mv, charts[order[i]]); });
+  parallel_for(np, threads, [&](int64_t i) {
+    chart_sets(mv, charts[order[i]]);
+    chart_finish(mv, charts[order[i]]);
+  });
   pack_charts(charts, P);
   // a patch's vertices that no triangle uses would be dropped by the vertex set; require
   // every patch vertex to be used so the packed layout equals the caller's

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -29,5 +30,34 @@ ruv_status prepare_mesh(const double* pos, int64_t nv, const int32_t* faces, int
                         double angle_min_deg, int threads, Prepared& P, std::string& err);
 ruv_status prepare_patches(int64_t np, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
                            const int32_t* tris, int threads, Prepared& P, std::string& err);
+
+// Per-chart vertex sets built elsewhere (on the device): chart c's sorted source vertex ids
+// verts[vert_off[c], vert_off[c + 1]) and its chart-local triangles tris[3 cf_off[c], ...),
+// in the chart's face order cf[cf_off[c], cf_off[c + 1]).
+struct ChartSets {
+  std::vector<int64_t> vert_off;
+  std::vector<int32_t> verts;
+  std::vector<int32_t> tris;
+};
+using ChartSetsFn = std::function<bool(const std::vector<int64_t>& cf_off, const std::vector<int32_t>& cf,
+                                       ChartSets& out, std::string& err)>;
+
+// prepare_mesh from a welded mesh (3 * V positions, 3 * F faces) with its edge-face lists
+// (per face slot, the faces carrying the edge in ascending order) and cut flags: the DFS
+// components, the chart vertex sets (from `sets` when given, else on the host), border
+// loops, frames and pins, and the packing -- the host part of the device path.
+ruv_status prepare_mesh_topology(std::vector<double>&& wpos3, std::vector<int32_t>&& F, std::vector<int64_t>&& ef_off,
+                                 std::vector<int32_t>&& ef_faces, std::vector<uint8_t>&& cut, int threads,
+                                 const ChartSetsFn* sets, Prepared& P, std::string& err);
+
+// The dihedral test acos(n1.n2) > angle of segment.rs:130-137 as d < d*: d* from the host
+// libm's acos (so both sides decide alike); NaN when acos is not monotone around d*.
+double acos_cut_threshold(double angle_min_deg);
+
+// prepare_mesh with the weld, edge-face lists, cut flags and chart vertex sets on the device
+// of `ctx` (prep_gpu.cu): the same Prepared, bit for bit.
+struct Ctx;
+ruv_status prepare_mesh_gpu(Ctx& ctx, const double* pos, int64_t nv, const int32_t* faces, int64_t nf, double weld_tol,
+                            double angle_min_deg, int threads, Prepared& P, std::string& err);
 
 }  // namespace ruv
