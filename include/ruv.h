@@ -177,6 +177,19 @@ ruv_status ruv_lscm_upload(ruv_ctx* ctx, const ruv_lscm_batch* in);
 ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ruv_chart_stat* stats);
 ruv_status ruv_lscm_download_uv(ruv_ctx* ctx, double* uv_out);
 
+/* unfold_chart with KeepMetric (lscm.rs:544-568, :642-676): the slack row becomes the area
+ * row -- the conformal free block K bordered by the slack column flip * area_w (both rows of
+ * a free vertex), the area gradient g(uv) and the corner area(uv) - target, rhs 2 * target.
+ * The reference factors that matrix by its CPU LU every driver iteration (it is not
+ * symmetric; lscm.rs:672-680).  Here only g and area change between iterations, so K is
+ * solved once for two right-hand sides by the batched PCG (y_b = K^-1 b, y_u = K^-1 u) and
+ * every iteration is the Schur complement aux = (2 target - g.y_b) / ((area - target) -
+ * g.y_u), x = y_b - aux y_u, followed by the damped driver step.  target: per chart
+ * (opts.target_area if > 0, else the chart's area3d, lscm.rs:568).  stats: status worst of
+ * the two solves, cg_iters their sum. */
+ruv_status ruv_lscm_solve_batch_keep_metric(ruv_ctx* ctx, const ruv_lscm_batch* in, const ruv_unfold_opts* opts,
+                                            const double* target, double* uv_out, ruv_chart_stat* stats);
+
 /* Differentiation (the forward / backward pair a torch.autograd.Function would wrap).
  * No counterpart in the reference's API: its unfold is not differentiable.
  *

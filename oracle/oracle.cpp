@@ -12,7 +12,8 @@
 //   anchor_ids           unwrap/src/lscm.rs:210-247
 //   edge_weights         unwrap/src/lscm.rs:252-274
 //   border_targets       unwrap/src/lscm.rs:280-413
-//   unfold_chart driver  unwrap/src/lscm.rs:512-727 (default path: KeepMetric = false)
+//   unfold_chart driver  unwrap/src/lscm.rs:512-727 (default path, and KeepMetric's area row
+//                        lscm.rs:120-155, :544-568, :642-676 solved by the LU each iteration)
 //   Sparse + LU          unwrap/src/sparse.rs:19-265
 //   meshgen fixtures     unwrap/src/meshgen.rs:12-198
 //   chart_distortion     unwrap/src/metrics.rs:41-141
@@ -902,6 +903,108 @@ void driver_loop(const ChartSystem& S, const std::vector<double>& sol, int max_i
   *err_accum_out = err_accum;
 }
 
+// KeepMetric's signed UV area and its gradient (lscm.rs:120-155, triangle order).
+double compute_area(const std::vector<V2>& uv, const std::vector<std::array<uint32_t, 3>>& tris) {
+  double a = 0.0;
+  for (auto& t : tris) {
+    V2 p0 = uv[t[0]], p1 = uv[t[1]], p2 = uv[t[2]];
+    a += (p1.u - p0.u) * (p2.v - p0.v) - (p2.u - p0.u) * (p1.v - p0.v);
+  }
+  return a * 0.5;
+}
+std::vector<V2> compute_area_grad(const std::vector<V2>& uv, const std::vector<std::array<uint32_t, 3>>& tris,
+                                  size_t nv) {
+  std::vector<V2> g(nv, V2{0.0, 0.0});
+  for (auto& t : tris) {
+    double x0 = uv[t[0]].u, y0 = uv[t[0]].v, x1 = uv[t[1]].u, y1 = uv[t[1]].v, x2 = uv[t[2]].u, y2 = uv[t[2]].v;
+    double sgd = 0.5 * (x0 * (y2 - y1) + x1 * (y0 - y2) + x2 * (y1 - y0));
+    double sgn = sgd > 0.0 ? 1.0 : -1.0;
+    g[t[0]].u += (y2 - y1) * 0.5 * sgn;
+    g[t[0]].v += (x1 - x2) * 0.5 * sgn;
+    g[t[1]].u += (y0 - y2) * 0.5 * sgn;
+    g[t[1]].v += (x2 - x0) * 0.5 * sgn;
+    g[t[2]].u += (y1 - y0) * 0.5 * sgn;
+    g[t[2]].v += (x0 - x1) * 0.5 * sgn;
+  }
+  return g;
+}
+
+// The KeepMetric unfold (lscm.rs:544-727 with keep_metric): the conformal free block of
+// build_system, bordered by the slack column flip * area_w (both rows of a free vertex), the
+// area-gradient row g(uv) and the corner area(uv) - target, rhs[aux] = 2 target; a sparse LU
+// of that system every driver iteration (the matrix changes with uv), then the damped
+// driver step.  Returns false when an LU fails (the reference breaks out of the loop).
+bool keep_metric_loop(const Mesh& mesh, const Chart& ch, const ChartSystem& S, int max_iter, double target_area,
+                      std::vector<V2>& uv, int64_t* iters_out, double* err_accum_out) {
+  size_t nv = S.p2.size(), nf2 = 2 * S.nfree, aux = nf2;
+  auto areas = face_areas3d(mesh);
+  std::vector<double> area_w(nv, 0.0);
+  for (size_t t = 0; t < ch.tris.size(); ++t)
+    for (uint32_t vv : ch.tris[t]) area_w[vv] += areas[ch.face_ids[t]];
+  double wsum = 0.0;
+  for (double w : area_w) wsum += w;
+  wsum = rmax(wsum, 1e-30);
+  for (double& w : area_w) w /= wsum;
+  uv = S.p2;
+  double flip = compute_area(uv, ch.tris) >= 0.0 ? 1.0 : -1.0;
+  double target = target_area > 0.0 ? target_area : ch.area3d;
+  double err_accum = 1.0, step = 1.0, prev_err = std::numeric_limits<double>::infinity();
+  int64_t iters_done = 0;
+  if (max_iter <= 0) max_iter = 100;
+  bool ok = true;
+  for (int it = 0; it < max_iter; ++it) {
+    iters_done = it + 1;
+    Sparse M(nf2 + 1);
+    for (size_t r = 0; r < nf2; ++r)
+      for (auto& kv : S.M.rows[r])
+        if (kv.first < nf2) M.rows[r][kv.first] = kv.second;
+    std::vector<double> rhs(S.rhs.begin(), S.rhs.begin() + nf2);
+    rhs.push_back(2.0 * target);
+    double area_now = compute_area(uv, ch.tris);
+    auto g = compute_area_grad(uv, ch.tris, nv);
+    for (size_t i = 0; i < nv; ++i)
+      if (S.free_pos[i] >= 0) {
+        size_t ri = 2 * (size_t)S.free_pos[i];
+        M.add(ri, aux, flip * area_w[i]);
+        M.add(ri + 1, aux, flip * area_w[i]);
+        M.add(aux, ri, g[i].u);
+        M.add(aux, ri + 1, g[i].v);
+      }
+    M.add(aux, aux, area_now - target);
+    LU F = factorize(M);
+    std::vector<double> sol;
+    if (!lu_solve(F, M.n, rhs, sol)) {
+      ok = false;
+      break;
+    }
+    std::vector<V2> new_uv = uv;
+    for (size_t i : S.free_ids) {
+      size_t pos = (size_t)S.free_pos[i];
+      new_uv[i] = {sol[2 * pos], sol[2 * pos + 1]};
+    }
+    for (size_t k = 0; k < S.pin_ids.size(); ++k) new_uv[S.pin_ids[k]] = S.pin_uv[k];
+    std::vector<V2> dv(nv);
+    for (size_t i = 0; i < nv; ++i) dv[i] = sub2(new_uv[i], uv[i]);
+    double ndv = 0.0, nuv = 0.0;
+    for (auto& d : dv) ndv += d.u * d.u + d.v * d.v;
+    for (auto& u : uv) nuv += u.u * u.u + u.v * u.v;
+    double err = std::sqrt(ndv) / rmax(std::sqrt(nuv), 1e-30);
+    double applied = err * step;
+    if (prev_err > 1e-30 && err > 2.0 * prev_err)
+      step = rmax(step * 0.5, 0.05);
+    else if (it > 3)
+      step = rmin(step * 1.2, 1.0);
+    if (applied < 1e-8 || (prev_err > 1e-30 && it != 0 && applied / prev_err <= 0.01)) break;
+    for (size_t i = 0; i < nv; ++i) uv[i] = {uv[i].u + dv[i].u * step, uv[i].v + dv[i].v * step};
+    prev_err = applied;
+    err_accum += err;
+    if (max_iter * 10 < it) break;
+  }
+  *iters_out = iters_done;
+  *err_accum_out = err_accum;
+  return ok;
+}
+
 // metrics.rs:59-70
 void svd2(const double m[2][2], double* s1, double* s2) {
   double a = m[0][0] * m[0][0] + m[1][0] * m[1][0];
@@ -1526,7 +1629,23 @@ int orc_pipeline(void* h, double weld_tol, double angle_deg, double angle_mix, d
       cp.push_back((int64_t)cv.size());
     }
     b->f[key(c, "rhs")] = S.rhs;
-    if ((int64_t)(2 * S.nfree + 1) <= solve_limit) {
+    const bool keep_metric = b->f.count("opt.keep_metric") && !b->f["opt.keep_metric"].empty() &&
+                             b->f["opt.keep_metric"][0] != 0.0;
+    if (keep_metric && (int64_t)(2 * S.nfree + 1) <= solve_limit) {
+      const double target_area = b->f.count("opt.target_area") ? b->f["opt.target_area"][0] : 0.0;
+      std::vector<V2> uv;
+      int64_t iters;
+      double ea;
+      keep_metric_loop(mesh, ch, S, (int)max_iter, target_area, uv, &iters, &ea);
+      auto& u = b->f[key(c, "uv")];
+      u.clear();
+      for (auto& q : uv) {
+        u.push_back(q.u);
+        u.push_back(q.v);
+      }
+      b->i[key(c, "iters")] = {iters};
+      b->f[key(c, "err_accum")] = {ea};
+    } else if ((int64_t)(2 * S.nfree + 1) <= solve_limit) {
       LU Fc = factorize(S.M);
       std::vector<double> sol;
       bool ok = lu_solve(Fc, S.M.n, S.rhs, sol);

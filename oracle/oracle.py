@@ -180,10 +180,13 @@ class Pipeline:
     """
 
     def __init__(self, pos, faces, weld_tol=1e-12, angle_deg=30.0, angle_mix=1.0, mix_w=1.0,
-                 lu_limit=4000, max_iter=100):
+                 lu_limit=4000, max_iter=100, keep_metric=False, target_area=0.0):
         self.bag = Bag()
         self.bag.put_f64("pos", np.asarray(pos, np.float64))
         self.bag.put_i64("faces", np.asarray(faces, np.int64))
+        if keep_metric:  # KeepMetric's area row, solved by the reference LU every iteration
+            self.bag.put_f64("opt.keep_metric", np.array([1.0]))
+            self.bag.put_f64("opt.target_area", np.array([float(target_area)]))
         self.max_iter = max_iter
         lib().orc_pipeline(self.bag.h, weld_tol, angle_deg, angle_mix, mix_w, lu_limit, max_iter)
         self.n_charts = int(self.bag.i64("n_charts")[0])

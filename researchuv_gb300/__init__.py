@@ -66,6 +66,8 @@ SIGNATURES = {
     "ruv_lscm_solve_batch": (ctypes.c_int, [_vp, _P(RuvBatch), _P(RuvUnfoldOpts), _P(_f64), _P(RuvChartStat)]),
     "ruv_prepare_mesh": (ctypes.c_int, [_P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _i32, _P(_vp)]),
     "ruv_prepare_patches": (ctypes.c_int, [_i64, _P(_i64), _P(_i64), _P(_f64), _P(_i32), _i32, _P(_vp)]),
+    "ruv_lscm_solve_batch_keep_metric": (ctypes.c_int, [_vp, _P(RuvBatch), _P(RuvUnfoldOpts), _P(_f64), _P(_f64),
+                                                        _P(RuvChartStat)]),
     "ruv_prepare_mesh_gpu": (ctypes.c_int, [_vp, _P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _i32, _P(_vp)]),
     "ruv_prepared_free": (None, [_vp]),
     "ruv_prepared_batch": (ctypes.c_int, [_vp, _P(RuvBatch)]),
@@ -309,9 +311,6 @@ class UnfoldOptions:
     max_cg_iter: int = 0  # 0 = max(max_iter, 1024) * 16 (lscm.rs:501)
 
     def to_c(self) -> RuvUnfoldOpts:
-        if self.keep_metric:
-            raise RuvError(Status.BAD_INPUT, "KeepMetric's non-symmetric area row is not on the GPU path "
-                                             "(lscm.rs:677)")
         if self.solver != SolverBackend.GPU:
             raise RuvError(Status.BAD_INPUT, "this library implements SolverBackend::Gpu only")
         o = RuvUnfoldOpts()
@@ -428,12 +427,25 @@ def prepare_patches(vert_off, tri_off, p3, tris, threads: int = 0) -> Charts:
     return Charts(h)
 
 
-def solve_batch(ctx: Context, batch: RuvBatch, opts: UnfoldOptions, n_verts: int, check: bool = True):
-    """ruv_lscm_solve_batch on a packed batch.  Returns (uv (n_verts, 2), stats list, status)."""
+def solve_batch(ctx: Context, batch: RuvBatch, opts: UnfoldOptions, n_verts: int, check: bool = True,
+                area3d=None):
+    """ruv_lscm_solve_batch on a packed batch.  Returns (uv (n_verts, 2), stats list, status).
+    With opts.keep_metric, ruv_lscm_solve_batch_keep_metric with the per-chart targets
+    (opts.target_area if > 0, else area3d[c])."""
     o = opts.to_c()
     uv = np.empty((n_verts, 2), np.float64)
     stats = (RuvChartStat * max(batch.n_charts, 1))()
-    st = lib().ruv_lscm_solve_batch(ctx.h, ctypes.byref(batch), ctypes.byref(o), _ptr(uv, _f64), stats)
+    if opts.keep_metric:
+        if opts.target_area > 0:
+            target = np.full(batch.n_charts, float(opts.target_area))
+        elif area3d is not None:
+            target = np.ascontiguousarray(area3d, np.float64)
+        else:
+            raise RuvError(Status.BAD_INPUT, "keep_metric needs the charts' area3d (or a target_area)")
+        st = lib().ruv_lscm_solve_batch_keep_metric(ctx.h, ctypes.byref(batch), ctypes.byref(o), _ptr(target, _f64),
+                                                    _ptr(uv, _f64), stats)
+    else:
+        st = lib().ruv_lscm_solve_batch(ctx.h, ctypes.byref(batch), ctypes.byref(o), _ptr(uv, _f64), stats)
     if check and st not in (0, Status.NOT_CONVERGED):
         ctx.check(st, "ruv_lscm_solve_batch")
     return uv, [stats[i] for i in range(batch.n_charts)], Status(st)
@@ -444,7 +456,7 @@ def unfold_charts(ctx: Context, charts: Charts, opts: Optional[UnfoldOptions] = 
     opts = opts or UnfoldOptions()
     vo = charts.i64("chart.vert_off")
     area = charts.f64("chart.area3d")
-    uv, stats, _ = solve_batch(ctx, charts.batch(), opts, int(vo[-1]))
+    uv, stats, _ = solve_batch(ctx, charts.batch(), opts, int(vo[-1]), area3d=area)
     out = []
     for c, s in enumerate(stats):
         out.append(UnfoldResult(uv=uv[vo[c]:vo[c + 1]].copy(), iters=s.driver_iters, err_accum=s.err_accum,

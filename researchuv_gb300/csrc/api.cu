@@ -387,6 +387,77 @@ ruv_status ruv_lscm_solve_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, const ru
   return solved;
 }
 
+ruv_status ruv_lscm_solve_batch_keep_metric(ruv_ctx* ctx, const ruv_lscm_batch* in, const ruv_unfold_opts* opts,
+                                            const double* target, double* uv_out, ruv_chart_stat* stats) {
+  ruv_status up = ruv_lscm_upload(ctx, in);
+  if (up != RUV_OK) return up;
+  const int64_t NC = in->n_charts, NV = in->vert_off[NC];
+  if ((NV > 0 && !uv_out) || (NC > 0 && !target)) return fail(ctx, RUV_ERR_BAD_INPUT, "null buffer");
+  ruv_status solved = guarded(ctx, [&]() -> ruv_status {
+    Ctx& c = ctx->c;
+    ruv_unfold_opts o;
+    ruv_unfold_opts_default(&o);
+    if (opts) o = *opts;
+    if (!known_precond(o.precond)) return fail(ctx, RUV_ERR_BAD_INPUT, "unknown preconditioner");
+    DevBatch& bt = c.resident;
+    c.have_uv = false;
+    c.have_last = false;  // (no backward pass for KeepMetric)
+    if (NC == 0) {
+      c.have_uv = true;
+      return RUV_OK;
+    }
+    DevSystem& sys = c.last_sys;
+    assemble_lscm(c, bt, sys, o.angle_mix);
+    const int64_t NR = sys.n_rows;
+    double* u = c.ws.get<double>("km.u", 2 * std::max<int64_t>(NR, 1));
+    std::vector<double> flip(NC);
+    for (int64_t k = 0; k < NC; ++k)  // (host: the reference's summation order decides the sign)
+      flip[k] = uv_signed_area(in->p2 + 2 * in->vert_off[k], in->tris + 3 * in->tri_off[k],
+                               in->tri_off[k + 1] - in->tri_off[k]) >= 0.0 ? 1.0 : -1.0;
+    keep_metric_rhs(c, bt, sys, upload(c, "km.flip", flip.data(), NC), u);
+    double* yb = c.ws.get<double>("km.yb", 2 * std::max<int64_t>(NR, 1));
+    double* yu = c.ws.get<double>("km.yu", 2 * std::max<int64_t>(NR, 1));
+    SolveOpts so;
+    so.precond = o.precond;
+    so.precision = o.precision;
+    so.tol = o.tol;
+    so.max_iter = o.max_cg_iter > 0 ? o.max_cg_iter : 16384;
+    auto r1 = pcg_solve(c, sys, yb, so);
+    double* b_saved = sys.b;
+    sys.b = u;
+    auto r2 = pcg_solve(c, sys, yu, so);
+    sys.b = b_saved;
+    const double* d_target = upload(c, "km.target", target, NC);
+    double* uv = c.ws.get<double>("lscm.uv", 2 * std::max<int64_t>(NV, 1));
+    std::vector<int32_t> iters;
+    std::vector<double> err_accum;
+    driver_keep_metric(c, bt, sys, yb, yu, d_target, o.max_iter, uv, iters, err_accum);
+    c.have_uv = true;
+    int w = RUV_OK;
+    for (int64_t k = 0; k < NC; ++k) {
+      const int st = worst(r1[k].status, r2[k].status);
+      w = worst(w, st);
+      if (stats) {
+        stats[k].status = st;
+        stats[k].driver_iters = iters[k];
+        stats[k].cg_iters = r1[k].iters + r2[k].iters;
+        stats[k].n_free = (int32_t)(sys.h_chart_row[k + 1] - sys.h_chart_row[k]);
+        stats[k].rel_res = std::max(r1[k].rel_res, r2[k].rel_res);
+        stats[k].err_accum = err_accum[k];
+      }
+    }
+    if (w != RUV_OK) return fail(ctx, (ruv_status)w, "at least one chart did not converge");
+    return RUV_OK;
+  });
+  if (solved != RUV_OK && solved != RUV_ERR_NOT_CONVERGED && solved != RUV_ERR_BREAKDOWN) return solved;
+  std::string msg = ctx->c.last_error;
+  if (!ctx->c.have_uv) return solved;
+  ruv_status s = ruv_lscm_download_uv(ctx, uv_out);
+  if (s != RUV_OK) return s;
+  ctx->c.last_error = msg;
+  return solved;
+}
+
 ruv_status ruv_lscm_forward(ruv_ctx* ctx, const ruv_lscm_batch* in, const ruv_unfold_opts* opts, double* uv_out,
                             ruv_chart_stat* stats) {
   return ruv_lscm_solve_batch(ctx, in, opts, uv_out, stats);

@@ -14,6 +14,8 @@
 // triangle order; diagonal and right-hand side: ascending neighbour id), so the CSR
 // pattern, values and right-hand side are bit-identical to the reference's
 // Sparse::to_csr(2 nf) (sparse.rs:69-84) of the same chart.
+#include <functional>
+
 #include "fp64rn.cuh"
 #include "system.cuh"
 
@@ -564,8 +566,23 @@ static void build_tiles(const std::vector<int64_t>& off, int64_t tile, std::vect
   beg.push_back(off[nc]);
 }
 
+namespace {
+// Per-iteration hook of the driver loop: run before the iteration's partials with the
+// iteration index, the per-chart driver states and the active-chart counter (KeepMetric
+// forms that iteration's solution there).
+using DriverHook = std::function<void(int, DriverState*, int*)>;
+}  // namespace
+
+static void driver_loop_dev(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x, int max_iter, double* uv,
+                            std::vector<int32_t>& iters, std::vector<double>& err_accum, const DriverHook* hook);
+
 void driver_update(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x, int max_iter, double* uv,
                    std::vector<int32_t>& iters, std::vector<double>& err_accum) {
+  driver_loop_dev(ctx, bt, sys, x, max_iter, uv, iters, err_accum, nullptr);
+}
+
+static void driver_loop_dev(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x, int max_iter, double* uv,
+                            std::vector<int32_t>& iters, std::vector<double>& err_accum, const DriverHook* hook) {
   cudaStream_t s = ctx.stream;
   Workspace& ws = ctx.ws;
   const int64_t NC = bt.n_charts, NV = bt.n_verts;
@@ -600,6 +617,7 @@ void driver_update(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x
   RUV_LAUNCH_CHECK();
   int* h_active = static_cast<int*>(ctx.pinned.get(sizeof(int)));
   for (int it = 0; it < max_iter; ++it) {
+    if (hook) (*hook)(it, st, n_active);
     if (NTL > 0) {
       k_driver_partials<<<(unsigned)NTL, 256, 0, s>>>(d_tab, d_tchart, NTL, st, bt.pinned, bt.pin_uv, bt.row_of, x, uv,
                                                       part);
@@ -630,6 +648,304 @@ void driver_update(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x
     iters[c] = hs[c].iters;
     err_accum[c] = hs[c].err_accum;
   }
+}
+
+namespace {
+// ---------------------------------------------------------------- KeepMetric (lscm.rs:544-568, :642-676)
+// The slack row of the system becomes the area row: with K the conformal free block, u the
+// slack column (flip * normalised vertex area weight, both rows of a free vertex), g(uv) the
+// area gradient and a(uv) the signed UV area,
+//     [ K   u          ] [x  ]   [ b          ]
+//     [ g^T a - target ] [aux] = [ 2 target   ].
+// Only g and a change between driver iterations, so the SPD block is solved once for the two
+// right-hand sides (y_b = K^-1 b, y_u = K^-1 u, the batched PCG) and every iteration is the
+// Schur complement aux = (2 target - g.y_b) / ((a - target) - g.y_u), x = y_b - aux y_u.  The
+// reference factors the bordered matrix every iteration (lscm.rs:672-680); a singular one
+// ends its loop, which here is a zero area row (every free gradient component and a - target
+// exactly zero) or a non-finite aux.
+
+// 3-D area per triangle (segment.rs:61-70)
+__global__ void k_km_face_area(const double* __restrict__ p3, const int32_t* __restrict__ tri_g, int64_t nt,
+                               double* __restrict__ A) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const P3 p0 = ld3(p3, tri_g[3 * t]), p1 = ld3(p3, tri_g[3 * t + 1]), p2 = ld3(p3, tri_g[3 * t + 2]);
+  A[t] = dmul(0.5, plen(pcross(psub(p1, p0), psub(p2, p0))));
+}
+
+// Each triangle at a free vertex once, in the vertex's sorted record order: the record
+// (t[m+1], corner m+2) of the pair that triangle t's corner m contributes.  Calls f(t, m).
+template <class F>
+__device__ __forceinline__ void km_vertex_tris(int64_t v, const int64_t* rec_off, const int2* rec,
+                                               const int32_t* tri_g, F&& f) {
+  for (int64_t r = rec_off[v]; r < rec_off[v + 1]; ++r) {
+    const int2 q = rec[r];
+    const int64_t t = q.y / 3;
+    const int j = q.y - 3 * (int)t;
+    if (q.x == tri_g[3 * t + (j + 2) % 3]) f(t, (j + 1) % 3);
+  }
+}
+
+// area weight of every free vertex (the areas of its triangles)
+__global__ void k_km_area_w(int64_t nv, const uint8_t* __restrict__ pinned, const int64_t* __restrict__ rec_off,
+                            const int2* __restrict__ rec, const int32_t* __restrict__ tri_g,
+                            const double* __restrict__ A, double* __restrict__ aw) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  double w = 0.0;
+  if (!pinned[v]) km_vertex_tris(v, rec_off, rec, tri_g, [&](int64_t t, int) { w = dadd(w, A[t]); });
+  aw[v] = w;
+}
+
+// the signed-area term of a triangle (lscm.rs:120-129) from per-vertex (u, v) pairs
+__device__ __forceinline__ double km_area_term(const double* uv, int32_t a, int32_t b, int32_t c) {
+  const double x0 = uv[2 * a], y0 = uv[2 * a + 1], x1 = uv[2 * b], y1 = uv[2 * b + 1], x2 = uv[2 * c],
+               y2 = uv[2 * c + 1];
+  return dsub(dmul(dsub(x1, x0), dsub(y2, y0)), dmul(dsub(x2, x0), dsub(y1, y0)));
+}
+
+// per triangle tile: the sum of 3 A_t (the total of the vertex area weights)
+__global__ void k_km_setup_part(const int64_t* __restrict__ ttab, const double* __restrict__ A,
+                                double* __restrict__ part) {
+  __shared__ double sh[64];
+  const int64_t tl = blockIdx.x;
+  double acc[2] = {0.0, 0.0};
+  for (int64_t t = ttab[2 * tl] + threadIdx.x; t < ttab[2 * tl + 1]; t += blockDim.x) acc[0] += 3.0 * A[t];
+  block_sum<2>(acc, sh);
+  if (threadIdx.x == 0) {
+    part[2 * tl] = acc[0];
+    part[2 * tl + 1] = acc[1];
+  }
+}
+
+__global__ void k_km_setup_chart(const int64_t* __restrict__ chart_ttile, const double* __restrict__ part,
+                                 double* __restrict__ wsum) {
+  __shared__ double sh[64];
+  const int64_t c = blockIdx.x;
+  double acc[2] = {0.0, 0.0};
+  for (int64_t t = chart_ttile[c] + threadIdx.x; t < chart_ttile[c + 1]; t += blockDim.x) {
+    acc[0] += part[2 * t];
+    acc[1] += part[2 * t + 1];
+  }
+  block_sum<2>(acc, sh);
+  if (threadIdx.x == 0) {
+    wsum[c] = rs_max(acc[0], 1e-30);
+  }
+}
+
+// slack column: flip * area_w / wsum on both rows of every free vertex
+__global__ void k_km_u(const int64_t* __restrict__ tab, const int32_t* __restrict__ tchart,
+                       const uint8_t* __restrict__ pinned, const int64_t* __restrict__ row_of,
+                       const double* __restrict__ aw, const double* __restrict__ wsum, const double* __restrict__ flip,
+                       double* __restrict__ u) {
+  const int64_t tl = blockIdx.x;
+  const int c = tchart[tl];
+  for (int64_t v = tab[2 * tl] + threadIdx.x; v < tab[2 * tl + 1]; v += blockDim.x) {
+    if (pinned[v]) continue;
+    const int64_t r = row_of[v];
+    const double w = flip[c] * ddiv(aw[v], wsum[c]);
+    u[2 * r] = w;
+    u[2 * r + 1] = w;
+  }
+}
+
+// per triangle tile of an active chart: the sum of the area terms of uv
+__global__ void k_km_area(const int64_t* __restrict__ ttab, const int32_t* __restrict__ ttchart,
+                          const DriverState* __restrict__ st, const int32_t* __restrict__ tri_g,
+                          const double* __restrict__ uv, double* __restrict__ part) {
+  __shared__ double sh[32];
+  const int64_t tl = blockIdx.x;
+  if (!st[ttchart[tl]].active) return;
+  double acc[1] = {0.0};
+  for (int64_t t = ttab[2 * tl] + threadIdx.x; t < ttab[2 * tl + 1]; t += blockDim.x)
+    acc[0] += km_area_term(uv, tri_g[3 * t], tri_g[3 * t + 1], tri_g[3 * t + 2]);
+  block_sum<1>(acc, sh);
+  if (threadIdx.x == 0) part[tl] = acc[0];
+}
+
+// per vertex tile of an active chart: the area gradient of every free vertex (lscm.rs:133-155,
+// its triangles in record order) dotted with y_b and y_u, and the count of its nonzero
+// components
+__global__ void k_km_grad(const int64_t* __restrict__ tab, const int32_t* __restrict__ tchart,
+                          const DriverState* __restrict__ st, const uint8_t* __restrict__ pinned,
+                          const int64_t* __restrict__ row_of, const int64_t* __restrict__ rec_off,
+                          const int2* __restrict__ rec, const int32_t* __restrict__ tri_g, const double* __restrict__ uv,
+                          const double* __restrict__ yb, const double* __restrict__ yu, double* __restrict__ part) {
+  __shared__ double sh[96];
+  const int64_t tl = blockIdx.x;
+  if (!st[tchart[tl]].active) return;
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int64_t v = tab[2 * tl] + threadIdx.x; v < tab[2 * tl + 1]; v += blockDim.x) {
+    if (pinned[v]) continue;
+    double gu = 0.0, gv = 0.0;
+    km_vertex_tris(v, rec_off, rec, tri_g, [&](int64_t t, int m) {
+      const int32_t a = tri_g[3 * t], b = tri_g[3 * t + 1], c = tri_g[3 * t + 2];
+      const double x0 = uv[2 * a], y0 = uv[2 * a + 1], x1 = uv[2 * b], y1 = uv[2 * b + 1], x2 = uv[2 * c],
+                   y2 = uv[2 * c + 1];
+      const double sgd = dmul(0.5, dadd(dadd(dmul(x0, dsub(y2, y1)), dmul(x1, dsub(y0, y2))), dmul(x2, dsub(y1, y0))));
+      const double h = sgd > 0.0 ? 0.5 : -0.5;
+      if (m == 0) {
+        gu = dadd(gu, dmul(dsub(y2, y1), h));
+        gv = dadd(gv, dmul(dsub(x1, x2), h));
+      } else if (m == 1) {
+        gu = dadd(gu, dmul(dsub(y0, y2), h));
+        gv = dadd(gv, dmul(dsub(x2, x0), h));
+      } else {
+        gu = dadd(gu, dmul(dsub(y1, y0), h));
+        gv = dadd(gv, dmul(dsub(x0, x1), h));
+      }
+    });
+    const int64_t r = row_of[v];
+    acc[0] += gu * yb[2 * r] + gv * yb[2 * r + 1];
+    acc[1] += gu * yu[2 * r] + gv * yu[2 * r + 1];
+    acc[2] += (gu != 0.0 ? 1.0 : 0.0) + (gv != 0.0 ? 1.0 : 0.0);
+  }
+  block_sum<3>(acc, sh);
+  if (threadIdx.x == 0) {
+    part[3 * tl] = acc[0];
+    part[3 * tl + 1] = acc[1];
+    part[3 * tl + 2] = acc[2];
+  }
+}
+
+// per chart: aux of this iteration; a singular bordered system ends the chart's loop
+__global__ void k_km_aux(const int64_t* __restrict__ chart_ttile, const int64_t* __restrict__ chart_vtile,
+                         DriverState* __restrict__ st, const double* __restrict__ apart, const double* __restrict__ gpart,
+                         const double* __restrict__ target, int it, double* __restrict__ aux, int* __restrict__ n_active) {
+  __shared__ double sh[128];
+  const int64_t c = blockIdx.x;
+  if (!st[c].active) return;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int64_t t = chart_ttile[c] + threadIdx.x; t < chart_ttile[c + 1]; t += blockDim.x) acc[0] += apart[t];
+  for (int64_t t = chart_vtile[c] + threadIdx.x; t < chart_vtile[c + 1]; t += blockDim.x) {
+    acc[1] += gpart[3 * t];
+    acc[2] += gpart[3 * t + 1];
+    acc[3] += gpart[3 * t + 2];
+  }
+  block_sum<4>(acc, sh);
+  if (threadIdx.x != 0) return;
+  const double area = 0.5 * acc[0], diag = area - target[c];
+  const double a = (2.0 * target[c] - acc[1]) / (diag - acc[2]);
+  if ((acc[3] == 0.0 && diag == 0.0) || !isfinite(a)) {
+    st[c].active = 0;  // the reference's LU fails: the loop ends before this iteration's update
+    st[c].iters = it + 1;
+    atomicSub(n_active, 1);
+    return;
+  }
+  aux[c] = a;
+}
+
+// x = y_b - aux y_u on the rows of active charts
+__global__ void k_km_x(const int64_t* __restrict__ tab, const int32_t* __restrict__ tchart,
+                       const DriverState* __restrict__ st, const uint8_t* __restrict__ pinned,
+                       const int64_t* __restrict__ row_of, const double* __restrict__ yb, const double* __restrict__ yu,
+                       const double* __restrict__ aux, double* __restrict__ x) {
+  const int64_t tl = blockIdx.x;
+  const int c = tchart[tl];
+  if (!st[c].active) return;
+  const double a = aux[c];
+  for (int64_t v = tab[2 * tl] + threadIdx.x; v < tab[2 * tl + 1]; v += blockDim.x) {
+    if (pinned[v]) continue;
+    const int64_t r = row_of[v];
+    x[2 * r] = yb[2 * r] - a * yu[2 * r];
+    x[2 * r + 1] = yb[2 * r + 1] - a * yu[2 * r + 1];
+  }
+}
+}  // namespace
+
+// The slack column u of the KeepMetric system (2 * n_rows, device) after assemble_lscm.
+void keep_metric_rhs(Ctx& ctx, DevBatch& bt, DevSystem& sys, const double* d_flip, double* u) {
+  cudaStream_t s = ctx.stream;
+  Workspace& ws = ctx.ws;
+  const int64_t NV = bt.n_verts, NT = bt.n_tris, NC = bt.n_charts;
+  if (sys.n_rows > 0) RUV_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * 2 * sys.n_rows, s));
+  if (NC == 0 || NT == 0) return;
+  double* A = ws.get<double>("km.A", NT);
+  double* aw = ws.get<double>("km.aw", NV);
+  k_km_face_area<<<div_up(NT, 256), 256, 0, s>>>(bt.p3, bt.tri_g, NT, A);
+  k_km_area_w<<<div_up(NV, 256), 256, 0, s>>>(NV, bt.pinned, bt.rec_off, bt.rec, bt.tri_g, A, aw);
+  count_launches(2);
+  std::vector<int64_t> tbeg, tctile, vbeg, vctile;
+  std::vector<int32_t> tchart, vchart;
+  build_tiles(bt.h_tri_off, 2048, tbeg, tchart, tctile);
+  build_tiles(bt.h_vert_off, 2048, vbeg, vchart, vctile);
+  const int64_t NTT = (int64_t)tchart.size(), NTL = (int64_t)vchart.size();
+  std::vector<int64_t> ttab(2 * NTT), vtab(2 * NTL);
+  for (int64_t t = 0; t < NTT; ++t) {
+    ttab[2 * t] = tbeg[t];
+    ttab[2 * t + 1] = std::min(tbeg[t] + 2048, bt.h_tri_off[tchart[t] + 1]);
+  }
+  for (int64_t t = 0; t < NTL; ++t) {
+    vtab[2 * t] = vbeg[t];
+    vtab[2 * t + 1] = std::min(vbeg[t] + 2048, bt.h_vert_off[vchart[t] + 1]);
+  }
+  int64_t* d_ttab = ws.get<int64_t>("km.ttab", std::max<int64_t>(2 * NTT, 1));
+  int64_t* d_tct = ws.get<int64_t>("km.tctile", NC + 1);
+  int64_t* d_vtab = ws.get<int64_t>("km.vtab", std::max<int64_t>(2 * NTL, 1));
+  int32_t* d_vch = ws.get<int32_t>("km.vchart", std::max<int64_t>(NTL, 1));
+  RUV_CUDA(cudaMemcpyAsync(d_ttab, ttab.data(), sizeof(int64_t) * 2 * NTT, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_tct, tctile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_vtab, vtab.data(), sizeof(int64_t) * 2 * NTL, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_vch, vchart.data(), sizeof(int32_t) * NTL, cudaMemcpyHostToDevice, s));
+  double* part = ws.get<double>("km.spart", 2 * std::max<int64_t>(NTT, 1));
+  double* wsum = ws.get<double>("km.wsum", NC);
+  if (NTT > 0) k_km_setup_part<<<(unsigned)NTT, 256, 0, s>>>(d_ttab, A, part);
+  k_km_setup_chart<<<(unsigned)NC, 128, 0, s>>>(d_tct, part, wsum);
+  if (NTL > 0) k_km_u<<<(unsigned)NTL, 256, 0, s>>>(d_vtab, d_vch, bt.pinned, bt.row_of, aw, wsum, d_flip, u);
+  count_launches(3);
+  RUV_LAUNCH_CHECK();
+  (void)sys;
+}
+
+// The KeepMetric driver: every iteration forms x = y_b - aux y_u from the current uv, then
+// takes the damped driver step (the same kernels as the default path).
+void driver_keep_metric(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* yb, const double* yu,
+                        const double* d_target, int max_iter, double* uv, std::vector<int32_t>& iters,
+                        std::vector<double>& err_accum) {
+  cudaStream_t s = ctx.stream;
+  Workspace& ws = ctx.ws;
+  const int64_t NC = bt.n_charts;
+  std::vector<int64_t> tbeg, tctile, vbeg, vctile;
+  std::vector<int32_t> tchart, vchart;
+  build_tiles(bt.h_tri_off, 2048, tbeg, tchart, tctile);
+  build_tiles(bt.h_vert_off, 2048, vbeg, vchart, vctile);
+  const int64_t NTT = (int64_t)tchart.size(), NTL = (int64_t)vchart.size();
+  std::vector<int64_t> ttab(2 * NTT), vtab(2 * NTL);
+  for (int64_t t = 0; t < NTT; ++t) {
+    ttab[2 * t] = tbeg[t];
+    ttab[2 * t + 1] = std::min(tbeg[t] + 2048, bt.h_tri_off[tchart[t] + 1]);
+  }
+  for (int64_t t = 0; t < NTL; ++t) {
+    vtab[2 * t] = vbeg[t];
+    vtab[2 * t + 1] = std::min(vbeg[t] + 2048, bt.h_vert_off[vchart[t] + 1]);
+  }
+  int64_t* d_ttab = ws.get<int64_t>("kmd.ttab", std::max<int64_t>(2 * NTT, 1));
+  int32_t* d_tch = ws.get<int32_t>("kmd.tchart", std::max<int64_t>(NTT, 1));
+  int64_t* d_tct = ws.get<int64_t>("kmd.tctile", NC + 1);
+  int64_t* d_vtab = ws.get<int64_t>("kmd.vtab", std::max<int64_t>(2 * NTL, 1));
+  int32_t* d_vch = ws.get<int32_t>("kmd.vchart", std::max<int64_t>(NTL, 1));
+  int64_t* d_vct = ws.get<int64_t>("kmd.vctile", NC + 1);
+  RUV_CUDA(cudaMemcpyAsync(d_ttab, ttab.data(), sizeof(int64_t) * 2 * NTT, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_tch, tchart.data(), sizeof(int32_t) * NTT, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_tct, tctile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_vtab, vtab.data(), sizeof(int64_t) * 2 * NTL, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_vch, vchart.data(), sizeof(int32_t) * NTL, cudaMemcpyHostToDevice, s));
+  RUV_CUDA(cudaMemcpyAsync(d_vct, vctile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
+  double* apart = ws.get<double>("kmd.apart", std::max<int64_t>(NTT, 1));
+  double* gpart = ws.get<double>("kmd.gpart", 3 * std::max<int64_t>(NTL, 1));
+  double* aux = ws.get<double>("kmd.aux", std::max<int64_t>(NC, 1));
+  double* x = ws.get<double>("kmd.x", 2 * std::max<int64_t>(sys.n_rows, 1));
+  DriverHook hook = [&](int it, DriverState* st, int* n_active) {
+    if (NTT > 0) k_km_area<<<(unsigned)NTT, 256, 0, s>>>(d_ttab, d_tch, st, bt.tri_g, uv, apart);
+    if (NTL > 0)
+      k_km_grad<<<(unsigned)NTL, 256, 0, s>>>(d_vtab, d_vch, st, bt.pinned, bt.row_of, bt.rec_off, bt.rec, bt.tri_g, uv,
+                                              yb, yu, gpart);
+    k_km_aux<<<(unsigned)NC, 128, 0, s>>>(d_tct, d_vct, st, apart, gpart, d_target, it, aux, n_active);
+    if (NTL > 0) k_km_x<<<(unsigned)NTL, 256, 0, s>>>(d_vtab, d_vch, st, bt.pinned, bt.row_of, yb, yu, aux, x);
+    count_launches(4);
+    RUV_LAUNCH_CHECK();
+  };
+  driver_loop_dev(ctx, bt, sys, x, max_iter, uv, iters, err_accum, &hook);
 }
 
 namespace {

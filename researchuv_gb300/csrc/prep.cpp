@@ -853,6 +853,17 @@ ruv_status prepare_mesh_topology(std::vector<double>&& wpos3, std::vector<int32_
   return finish_mesh(wpos, F, ef, cut, threads, sets, clk, P, err);
 }
 
+double uv_signed_area(const double* uv, const int32_t* tris, int64_t nt) {  // lscm.rs:120-129
+  double a = 0.0;
+  for (int64_t t = 0; t < nt; ++t) {
+    const double* p0 = uv + 2 * (int64_t)tris[3 * t];
+    const double* p1 = uv + 2 * (int64_t)tris[3 * t + 1];
+    const double* p2 = uv + 2 * (int64_t)tris[3 * t + 2];
+    a += (p1[0] - p0[0]) * (p2[1] - p0[1]) - (p2[0] - p0[0]) * (p1[1] - p0[1]);
+  }
+  return a * 0.5;
+}
+
 double acos_cut_threshold(double angle_min_deg) {
   // acos(d) > th  <=>  d < d*: the smallest d in [-1, 1] with acos(d) <= th, by bisection over
   // the doubles in value order (acos is non-increasing); NaN when no such d exists or when

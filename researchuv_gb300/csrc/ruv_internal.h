@@ -54,6 +54,11 @@ ruv_status prepare_mesh_topology(std::vector<double>&& wpos3, std::vector<int32_
 // libm's acos (so both sides decide alike); NaN when acos is not monotone around d*.
 double acos_cut_threshold(double angle_min_deg);
 
+// compute_area (lscm.rs:120-129): the signed area of a chart's UVs, triangles in order (host,
+// no FMA contraction) -- KeepMetric's orientation flip is its sign, a decision that must be
+// the reference's even when the area is at rounding level
+double uv_signed_area(const double* uv, const int32_t* tris, int64_t nt);
+
 // prepare_mesh with the weld, edge-face lists, cut flags and chart vertex sets on the device
 // of `ctx` (prep_gpu.cu): the same Prepared, bit for bit.
 struct Ctx;

@@ -128,6 +128,13 @@ int64_t fp64_selftest(Ctx& ctx, int mode, uint64_t seed, int64_t n, double* firs
 // (2 * n_verts) and per-chart driver iterations / err_accum.
 void driver_update(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* x, int max_iter, double* uv,
                    std::vector<int32_t>& iters, std::vector<double>& err_accum);
+// KeepMetric (lscm.rs:544-568, :642-676): the slack column u (2 * n_rows) of the bordered
+// system (d_flip: per chart, the sign of the UV area of p2), and the driver whose every iteration forms x = y_b - aux y_u from the current uv
+// (y_b = K^-1 b, y_u = K^-1 u; d_target per chart).
+void keep_metric_rhs(Ctx& ctx, DevBatch& bt, DevSystem& sys, const double* d_flip, double* u);
+void driver_keep_metric(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const double* yb, const double* yu,
+                        const double* d_target, int max_iter, double* uv, std::vector<int32_t>& iters,
+                        std::vector<double>& err_accum);
 
 struct Ctx {
   int device = 0;

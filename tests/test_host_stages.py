@@ -102,5 +102,6 @@ def test_bad_inputs_are_rejected():
         R.prepare_mesh(p, np.array([[0, 1, 5]]))
     with pytest.raises(R.RuvError):
         R.prepare_patches([0, 3], [0, 1], p, np.array([[0, 1, 3]]))
-    with pytest.raises(R.RuvError):
-        R.UnfoldOptions(keep_metric=True).to_c()
+    with pytest.raises(R.RuvError):  # the library implements SolverBackend::Gpu only
+        R.UnfoldOptions(solver=R.SolverBackend.CPU).to_c()
+    R.UnfoldOptions(keep_metric=True).to_c()  # KeepMetric runs on the GPU path (Schur complement)
