@@ -286,6 +286,33 @@ ruv_status ruv_prepare_mesh(const double* pos, int64_t n_verts, const int32_t* f
 ruv_status ruv_prepare_mesh_gpu(ruv_ctx* ctx, const double* pos, int64_t n_verts, const int32_t* faces, int64_t n_faces,
                                 double weld_tol, double angle_min_deg, int32_t threads, ruv_prepared** out);
 
+/* Seam cut of closed charts (seam.rs SeamCutOptions, :286-305) and distortion-driven
+ * re-cutting of folding charts (recut.rs RecutOptions, :98-146), run after the segmentation
+ * as pipeline::run does (pipeline.rs:149-167).  Both are off by default, as in the reference. */
+typedef struct ruv_cut_opts {
+  int32_t seam_enable;         /* open borderless charts along a seam tree, default 0     */
+  int32_t seam_min_faces;      /* only charts with at least this many faces, default 8    */
+  int32_t seam_branch_count;   /* branches beyond the geodesic-diameter trunk, default 1  */
+  int32_t recut_enable;        /* re-cut charts that fold, default 0                       */
+  int32_t recut_max_rounds;    /* controller rounds, default 6                             */
+  int32_t recut_max_splits;    /* total new cut edges, default 48                          */
+  double recut_fold_fraction;  /* re-cut when more triangles than this fraction fold, 0.02 */
+  int32_t recut_max_charts;    /* stop when the chart count exceeds this, default 64      */
+} ruv_cut_opts;
+
+void ruv_cut_opts_default(ruv_cut_opts* o);
+
+/* ruv_prepare_mesh followed by the seam cut and / or the re-cutting controller.  Every
+ * controller round unfolds all charts in one batched solve on ctx (unfold: the options of
+ * that solve; the reference unfolds chart by chart, recut.rs:71-79) and counts each chart's
+ * winding-inconsistent triangles (metrics.rs:33-56); every folding chart gets its separating
+ * cut (seam tree when closed, border-crossing chord when open, seam.rs:167-283) and the
+ * charts are rebuilt over the grown cut set.  *added_out = the cut edges the controller added.
+ * ctx may be NULL when re-cutting is off (the seam cut alone runs on the host). */
+ruv_status ruv_prepare_mesh_cut(ruv_ctx* ctx, const double* pos, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                                double weld_tol, double angle_min_deg, const ruv_cut_opts* cut,
+                                const ruv_unfold_opts* unfold, int32_t threads, ruv_prepared** out, int64_t* added_out);
+
 /* Charts given directly (one chart per patch, no weld / segmentation): patch c owns
  * vertices [vert_off[c], vert_off[c+1]) and triangles [tri_off[c], tri_off[c+1]) with
  * patch-local indices.  Border loops are walked over each patch's boundary edges. */

@@ -42,6 +42,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <queue>
 #include <set>
 #include <string>
 #include <tuple>
@@ -272,8 +273,11 @@ std::vector<std::vector<uint32_t>> chart_border_loops(const Mesh& mesh,
   return loops;
 }
 
-std::vector<Chart> segment(const Mesh& mesh, double angle_min_deg, size_t* n_cut_out) {
-  // segment.rs:85-102 (dihedrals), :130-140 (segment), :143-223 (build_charts)
+std::vector<Chart> build_charts(const Mesh& mesh, const std::set<EdgeKey>& cut);
+
+// segment.rs:85-102 (dihedrals), :130-140 (segment); the charts by build_charts below
+std::vector<Chart> segment(const Mesh& mesh, double angle_min_deg, size_t* n_cut_out,
+                           std::set<EdgeKey>* cut_out = nullptr) {
   double th = angle_min_deg * (PI / 180.0);
   auto ef = edge_faces(mesh);
   std::set<EdgeKey> cut, mbnd;
@@ -295,6 +299,17 @@ std::vector<Chart> segment(const Mesh& mesh, double angle_min_deg, size_t* n_cut
     if (ang > th) cut.insert(kv.first);
   }
   if (n_cut_out) *n_cut_out = cut.size();
+  if (cut_out) *cut_out = cut;
+  return build_charts(mesh, cut);
+}
+
+// segment.rs:143-223: face components over non-cut edges (DFS stack order), vertex sets,
+// local triangles, border (cut or mesh-boundary edges), loops, area
+std::vector<Chart> build_charts(const Mesh& mesh, const std::set<EdgeKey>& cut) {
+  auto ef = edge_faces(mesh);
+  std::set<EdgeKey> mbnd;
+  for (auto& kv : ef)
+    if (kv.second.size() == 1) mbnd.insert(kv.first);
   auto areas = face_areas3d(mesh);
   size_t nf = mesh.faces.size();
   std::vector<char> seen(nf, 0);
@@ -1005,6 +1020,254 @@ bool keep_metric_loop(const Mesh& mesh, const Chart& ch, const ChartSystem& S, i
   return ok;
 }
 
+// ---------------------------------------------------------------- seam.rs / recut.rs
+// seam.rs:145-165: undirected adjacency over the chart's faces (edges ascending), 3-D lengths
+std::map<uint32_t, std::vector<std::pair<uint32_t, double>>> chart_adjacency(const Mesh& mesh, const Chart& ch) {
+  std::set<EdgeKey> edges;
+  for (size_t fi : ch.face_ids) {
+    auto& t = mesh.faces[fi];
+    edges.insert(edge_key(t[0], t[1]));
+    edges.insert(edge_key(t[1], t[2]));
+    edges.insert(edge_key(t[2], t[0]));
+  }
+  std::map<uint32_t, std::vector<std::pair<uint32_t, double>>> adj;
+  for (auto& e : edges) {
+    double len = len3(sub(mesh.pos[e.first], mesh.pos[e.second]));
+    adj[e.first].push_back({e.second, len});
+    adj[e.second].push_back({e.first, len});
+  }
+  return adj;
+}
+
+// seam.rs:54-109: multi-source Dijkstra; the heap pops the smallest distance, ties the
+// larger vertex id (HeapItem's ordering); relaxations need a 1e-12 improvement
+void dijkstra(const std::map<uint32_t, std::vector<std::pair<uint32_t, double>>>& adj, const std::vector<uint32_t>& seeds,
+              std::map<uint32_t, double>& dist, std::map<uint32_t, uint32_t>& prev) {
+  struct Item {
+    double d;
+    uint32_t v;
+  };
+  auto less = [](const Item& x, const Item& y) { return x.d > y.d || (x.d == y.d && x.v < y.v); };
+  std::priority_queue<Item, std::vector<Item>, decltype(less)> heap(less);
+  dist.clear();
+  prev.clear();
+  for (uint32_t s : seeds) {
+    dist[s] = 0.0;
+    heap.push({0.0, s});
+  }
+  while (!heap.empty()) {
+    Item it = heap.top();
+    heap.pop();
+    auto f = dist.find(it.v);
+    if (f != dist.end() && f->second < it.d - 1e-12) continue;
+    auto a = adj.find(it.v);
+    if (a == adj.end()) continue;
+    for (auto& wl : a->second) {
+      double nd = it.d + wl.second;
+      auto g = dist.find(wl.first);
+      bool better = g == dist.end() ? true : nd < g->second - 1e-12;
+      if (better) {
+        dist[wl.first] = nd;
+        prev[wl.first] = it.v;
+        heap.push({nd, wl.first});
+      }
+    }
+  }
+}
+
+// seam.rs:111-131
+bool farthest_excluding(const std::map<uint32_t, double>& dist, const std::set<uint32_t>& skip, uint32_t* out) {
+  bool have = false;
+  uint32_t bv = 0;
+  double bd = 0.0;
+  for (auto& kv : dist) {
+    if (!std::isfinite(kv.second) || skip.count(kv.first)) continue;
+    if (!have || kv.second > bd || (kv.second == bd && kv.first < bv)) {
+      have = true;
+      bv = kv.first;
+      bd = kv.second;
+    }
+  }
+  *out = bv;
+  return have;
+}
+
+std::vector<uint32_t> reconstruct(const std::map<uint32_t, uint32_t>& prev, uint32_t target) {  // seam.rs:133-143
+  std::vector<uint32_t> path{target};
+  uint32_t cur = target;
+  for (auto p = prev.find(cur); p != prev.end(); p = prev.find(cur)) {
+    path.push_back(p->second);
+    cur = p->second;
+  }
+  std::reverse(path.begin(), path.end());
+  return path;
+}
+
+// min over ids by (x, id): the first minimum (seam.rs:177-187, :253-262)
+template <class It>
+uint32_t min_x_vertex(const Mesh& mesh, It b, It e) {
+  uint32_t best = *b;
+  for (It i = b; i != e; ++i) {
+    double px = mesh.pos[*i].x, pb = mesh.pos[best].x;
+    if (px < pb || (!(px > pb) && !(px < pb) && *i < best)) best = *i;
+  }
+  return best;
+}
+
+std::vector<std::vector<uint32_t>> seam_paths(const Mesh& mesh, const Chart& ch, size_t branch_count) {  // seam.rs:167-220
+  std::vector<std::vector<uint32_t>> paths;
+  if (ch.face_ids.size() < 2 || ch.vertex_ids.empty()) return paths;
+  auto adj = chart_adjacency(mesh, ch);
+  uint32_t start = min_x_vertex(mesh, ch.vertex_ids.begin(), ch.vertex_ids.end());
+  std::set<uint32_t> tree;
+  std::map<uint32_t, double> dist0, dist1;
+  std::map<uint32_t, uint32_t> prev0, prev;
+  dijkstra(adj, {start}, dist0, prev0);
+  uint32_t a, b;
+  if (!farthest_excluding(dist0, tree, &a)) return paths;
+  dijkstra(adj, {a}, dist1, prev);
+  if (!farthest_excluding(dist1, tree, &b)) return paths;
+  if (a == b) return paths;
+  auto trunk = reconstruct(prev, b);
+  tree.insert(trunk.begin(), trunk.end());
+  paths.push_back(trunk);
+  for (size_t k = 0; k < branch_count; ++k) {
+    std::vector<uint32_t> seeds(tree.begin(), tree.end());
+    std::map<uint32_t, double> dt;
+    std::map<uint32_t, uint32_t> pt;
+    dijkstra(adj, seeds, dt, pt);
+    uint32_t f;
+    if (!farthest_excluding(dt, tree, &f)) break;
+    auto branch = reconstruct(pt, f);
+    if (branch.size() < 2) break;
+    tree.insert(branch.begin(), branch.end());
+    paths.push_back(branch);
+  }
+  return paths;
+}
+
+std::set<EdgeKey> seam_cut_edges(const Mesh& mesh, const Chart& ch, size_t branch_count) {  // seam.rs:222-231
+  std::set<EdgeKey> cut;
+  for (auto& path : seam_paths(mesh, ch, branch_count))
+    for (size_t k = 0; k + 1 < path.size(); ++k) cut.insert(edge_key(path[k], path[k + 1]));
+  return cut;
+}
+
+std::vector<uint32_t> border_crossing_path(const Mesh& mesh, const Chart& ch) {  // seam.rs:246-283
+  if (ch.border.empty() || ch.face_ids.size() < 2) return {};
+  auto adj = chart_adjacency(mesh, ch);
+  uint32_t a = min_x_vertex(mesh, ch.border.begin(), ch.border.end());
+  std::map<uint32_t, double> dist;
+  std::map<uint32_t, uint32_t> prev;
+  dijkstra(adj, {a}, dist, prev);
+  bool have = false;
+  uint32_t bv = 0;
+  double bd = 0.0;
+  for (uint32_t v : ch.border) {
+    if (v == a) continue;
+    auto f = dist.find(v);
+    if (f == dist.end() || !std::isfinite(f->second)) continue;
+    double d = f->second;
+    if (have && d < bd) continue;
+    if (have && d == bd) {
+      bv = std::min(bv, v);
+    } else {
+      have = true;
+      bv = v;
+      bd = d;
+    }
+  }
+  if (have && bd > 1e-12) return reconstruct(prev, bv);
+  return {};
+}
+
+// metrics.rs:33-56
+size_t winding_flips(const std::vector<V2>& uv, const std::vector<std::array<uint32_t, 3>>& tris) {
+  if (tris.empty()) return 0;
+  auto ts = [&](const std::array<uint32_t, 3>& t) {
+    V2 u = uv[t[0]], v = uv[t[1]], w = uv[t[2]];
+    return (v.u - u.u) * (w.v - u.v) - (w.u - u.u) * (v.v - u.v);
+  };
+  double sum = 0.0;
+  for (auto& t : tris) sum += ts(t);
+  double dom = sum < 0.0 ? -1.0 : 1.0;
+  size_t n = 0;
+  for (auto& t : tris)
+    if (ts(t) * dom <= 0.0) ++n;
+  return n;
+}
+
+struct CutOptions {
+  bool seam_enable = false;
+  size_t seam_min_faces = 8, seam_branch = 1;
+  bool recut_enable = false;
+  size_t max_rounds = 6, max_splits = 48, max_charts = 64;
+  double fold_fraction = 0.02;
+};
+
+// seam.rs:286-305
+std::vector<Chart> cut_closed_charts(const Mesh& mesh, const std::vector<Chart>& charts, std::set<EdgeKey>& all,
+                                     const CutOptions& o) {
+  size_t before = all.size();
+  for (auto& ch : charts) {
+    if (!ch.border_loops.empty() || ch.face_ids.size() < o.seam_min_faces) continue;
+    for (auto& e : seam_cut_edges(mesh, ch, o.seam_branch)) all.insert(e);
+  }
+  if (all.size() == before) return charts;
+  return build_charts(mesh, all);
+}
+
+// recut.rs:98-146, with each round's unfolds by the reference LU path (unfold_chart with the
+// default options: angle_mix 1, mix_w 1)
+std::vector<Chart> recut_folding_charts(const Mesh& mesh, std::vector<Chart> charts, std::set<EdgeKey>& all,
+                                        const CutOptions& o, int max_iter, size_t* added_out,
+                                        std::vector<std::vector<size_t>>* folds_log) {
+  size_t added = 0;
+  for (size_t round = 0; round < o.max_rounds; ++round) {
+    if (added >= o.max_splits) break;
+    std::vector<size_t> folds(charts.size());
+    for (size_t i = 0; i < charts.size(); ++i) {
+      ChartSystem S = build_system(mesh, charts[i], 1.0, 1.0);
+      LU Fc = factorize(S.M);
+      std::vector<double> sol;
+      std::vector<V2> uv = S.p2;
+      if (lu_solve(Fc, S.M.n, S.rhs, sol)) {
+        int64_t iters;
+        double ea;
+        driver_loop(S, sol, max_iter, uv, &iters, &ea);
+      }
+      folds[i] = winding_flips(uv, charts[i].tris);
+    }
+    if (folds_log) folds_log->push_back(folds);
+    std::vector<size_t> folding;
+    for (size_t i = 0; i < charts.size(); ++i)
+      if ((double)folds[i] / (double)std::max<size_t>(charts[i].tris.size(), 1) > o.fold_fraction) folding.push_back(i);
+    if (folding.empty()) break;
+    std::stable_sort(folding.begin(), folding.end(), [&](size_t x, size_t y) { return folds[x] > folds[y]; });
+    bool grew = false;
+    for (size_t i : folding) {
+      if (added >= o.max_splits) break;
+      std::set<EdgeKey> cut;
+      if (charts[i].border_loops.empty()) {
+        cut = seam_cut_edges(mesh, charts[i], std::max<size_t>(o.seam_branch, 1));
+      } else {
+        auto path = border_crossing_path(mesh, charts[i]);
+        for (size_t k = 0; k + 1 < path.size(); ++k) cut.insert(edge_key(path[k], path[k + 1]));
+      }
+      for (auto& e : cut)
+        if (all.insert(e).second) {
+          ++added;
+          grew = true;
+        }
+    }
+    if (!grew) break;
+    charts = build_charts(mesh, all);
+    if (charts.size() > o.max_charts) break;
+  }
+  *added_out = added;
+  return charts;
+}
+
 // metrics.rs:59-70
 void svd2(const double m[2][2], double* s1, double* s2) {
   double a = m[0][0] * m[0][0] + m[1][0] * m[1][0];
@@ -1570,7 +1833,42 @@ int orc_pipeline(void* h, double weld_tol, double angle_deg, double angle_mix, d
       for (uint32_t v : t) mf.push_back(v);
   }
   size_t n_cut = 0;
-  auto charts = segment(mesh, angle_deg, &n_cut);
+  std::set<EdgeKey> cut0;
+  auto charts = segment(mesh, angle_deg, &n_cut, &cut0);
+  // pipeline.rs:149-167: optional seam cut of closed charts, then optional re-cutting of
+  // folding charts (which starts again from the segmentation's cut set, as the reference does)
+  CutOptions co;
+  if (b->f.count("opt.seam") && b->f["opt.seam"].size() == 3 && b->f["opt.seam"][0] != 0.0) {
+    co.seam_enable = true;
+    co.seam_min_faces = (size_t)b->f["opt.seam"][1];
+    co.seam_branch = (size_t)b->f["opt.seam"][2];
+  }
+  if (b->f.count("opt.seam_branch") && !b->f["opt.seam_branch"].empty())
+    co.seam_branch = (size_t)b->f["opt.seam_branch"][0];
+  if (b->f.count("opt.recut") && b->f["opt.recut"].size() == 5 && b->f["opt.recut"][0] != 0.0) {
+    co.recut_enable = true;
+    co.max_rounds = (size_t)b->f["opt.recut"][1];
+    co.max_splits = (size_t)b->f["opt.recut"][2];
+    co.fold_fraction = b->f["opt.recut"][3];
+    co.max_charts = (size_t)b->f["opt.recut"][4];
+  }
+  if (co.seam_enable) {
+    std::set<EdgeKey> all = cut0;
+    charts = cut_closed_charts(mesh, charts, all, co);
+  }
+  if (co.recut_enable) {
+    std::set<EdgeKey> all = cut0;
+    size_t added = 0;
+    std::vector<std::vector<size_t>> log;
+    charts = recut_folding_charts(mesh, charts, all, co, (int)max_iter, &added, &log);
+    b->i["recut.added"] = {(int64_t)added};
+    auto& lf = b->i["recut.folds"];
+    lf.clear();
+    for (auto& r : log) {
+      lf.push_back((int64_t)r.size());
+      for (size_t x : r) lf.push_back((int64_t)x);
+    }
+  }
   b->i["n_charts"] = {(int64_t)charts.size()};
   b->i["n_cut"] = {(int64_t)n_cut};
   for (size_t ci = 0; ci < charts.size(); ++ci) {

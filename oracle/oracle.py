@@ -180,10 +180,14 @@ class Pipeline:
     """
 
     def __init__(self, pos, faces, weld_tol=1e-12, angle_deg=30.0, angle_mix=1.0, mix_w=1.0,
-                 lu_limit=4000, max_iter=100, keep_metric=False, target_area=0.0):
+                 lu_limit=4000, max_iter=100, keep_metric=False, target_area=0.0, seam_cut=None, recut=None):
         self.bag = Bag()
         self.bag.put_f64("pos", np.asarray(pos, np.float64))
         self.bag.put_i64("faces", np.asarray(faces, np.int64))
+        if seam_cut is not None:  # (enable, min_faces, branch_count): seam.rs SeamCutOptions
+            self.bag.put_f64("opt.seam", np.array(seam_cut, np.float64))
+        if recut is not None:  # (enable, max_rounds, max_splits, fold_fraction, max_charts): recut.rs
+            self.bag.put_f64("opt.recut", np.array(recut, np.float64))
         if keep_metric:  # KeepMetric's area row, solved by the reference LU every iteration
             self.bag.put_f64("opt.keep_metric", np.array([1.0]))
             self.bag.put_f64("opt.target_area", np.array([float(target_area)]))

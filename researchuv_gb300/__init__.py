@@ -68,6 +68,9 @@ SIGNATURES = {
     "ruv_prepare_patches": (ctypes.c_int, [_i64, _P(_i64), _P(_i64), _P(_f64), _P(_i32), _i32, _P(_vp)]),
     "ruv_lscm_solve_batch_keep_metric": (ctypes.c_int, [_vp, _P(RuvBatch), _P(RuvUnfoldOpts), _P(_f64), _P(_f64),
                                                         _P(RuvChartStat)]),
+    "ruv_cut_opts_default": (None, [_vp]),
+    "ruv_prepare_mesh_cut": (ctypes.c_int, [_vp, _P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _vp, _P(RuvUnfoldOpts), _i32,
+                                            _P(_vp), _P(_i64)]),
     "ruv_prepare_mesh_gpu": (ctypes.c_int, [_vp, _P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _i32, _P(_vp)]),
     "ruv_prepared_free": (None, [_vp]),
     "ruv_prepared_batch": (ctypes.c_int, [_vp, _P(RuvBatch)]),
@@ -411,6 +414,56 @@ def prepare_mesh(positions, faces, weld_tol: float = 1e-12, angle_min_deg: float
     if st != 0:
         raise RuvError(st, "ruv_prepare_mesh")
     return Charts(h)
+
+
+class RuvCutOpts(ctypes.Structure):
+    _fields_ = [("seam_enable", _i32), ("seam_min_faces", _i32), ("seam_branch_count", _i32), ("recut_enable", _i32),
+                ("recut_max_rounds", _i32), ("recut_max_splits", _i32), ("recut_fold_fraction", _f64),
+                ("recut_max_charts", _i32)]
+
+
+@dataclasses.dataclass
+class SeamCutOptions:
+    """unwrap/src/seam.rs:30-49."""
+    enable: bool = False
+    min_faces: int = 8
+    branch_count: int = 1
+
+
+@dataclasses.dataclass
+class RecutOptions:
+    """unwrap/src/recut.rs:33-59."""
+    enable: bool = False
+    max_rounds: int = 6
+    max_splits: int = 48
+    fold_fraction: float = 0.02
+    max_charts: int = 64
+
+
+def prepare_mesh_cut(ctx: Optional["Context"], positions, faces, weld_tol: float = 1e-12, angle_min_deg: float = 30.0,
+                     seam_cut: Optional[SeamCutOptions] = None, recut: Optional[RecutOptions] = None,
+                     unfold: Optional[UnfoldOptions] = None, threads: int = 0):
+    """pipeline::run's chart stages with the optional seam cut and re-cutting controller
+    (pipeline.rs:146-167; every controller round unfolds all charts in one batched solve on
+    ctx).  Returns (Charts, cut edges added by the controller)."""
+    sc, rc = seam_cut or SeamCutOptions(), recut or RecutOptions()
+    o = RuvCutOpts()
+    lib().ruv_cut_opts_default(ctypes.byref(o))
+    o.seam_enable, o.seam_min_faces, o.seam_branch_count = int(sc.enable), sc.min_faces, sc.branch_count
+    o.recut_enable, o.recut_max_rounds, o.recut_max_splits = int(rc.enable), rc.max_rounds, rc.max_splits
+    o.recut_fold_fraction, o.recut_max_charts = rc.fold_fraction, rc.max_charts
+    u = (unfold or UnfoldOptions()).to_c()
+    p = np.ascontiguousarray(positions, np.float64).reshape(-1, 3)
+    f = np.ascontiguousarray(faces, np.int32).reshape(-1, 3)
+    h, added = _vp(), _i64(0)
+    st = lib().ruv_prepare_mesh_cut(ctx.h if ctx is not None else None, _ptr(p, _f64), p.shape[0], _ptr(f, _i32),
+                                    f.shape[0], weld_tol, angle_min_deg, ctypes.byref(o), ctypes.byref(u), threads,
+                                    ctypes.byref(h), ctypes.byref(added))
+    if ctx is not None:
+        ctx.check(st, "ruv_prepare_mesh_cut")
+    elif st != 0:
+        raise RuvError(st, "ruv_prepare_mesh_cut")
+    return Charts(h), added.value
 
 
 def prepare_patches(vert_off, tri_off, p3, tris, threads: int = 0) -> Charts:

@@ -718,6 +718,77 @@ ruv_status ruv_prepare_mesh_gpu(ruv_ctx* ctx, const double* pos, int64_t n_verts
   });
 }
 
+void ruv_cut_opts_default(ruv_cut_opts* o) {
+  if (!o) return;
+  o->seam_enable = 0;
+  o->seam_min_faces = 8;
+  o->seam_branch_count = 1;
+  o->recut_enable = 0;
+  o->recut_max_rounds = 6;
+  o->recut_max_splits = 48;
+  o->recut_fold_fraction = 0.02;
+  o->recut_max_charts = 64;
+}
+
+ruv_status ruv_prepare_mesh_cut(ruv_ctx* ctx, const double* pos, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                                double weld_tol, double angle_min_deg, const ruv_cut_opts* cut,
+                                const ruv_unfold_opts* unfold, int32_t threads, ruv_prepared** out, int64_t* added_out) {
+  if (!out || n_verts < 0 || n_faces < 0 || (n_verts > 0 && !pos) || (n_faces > 0 && !faces))
+    return RUV_ERR_BAD_INPUT;
+  if (n_verts >= (int64_t)INT32_MAX) return RUV_ERR_BAD_INPUT;
+  *out = nullptr;
+  ruv_cut_opts co;
+  ruv_cut_opts_default(&co);
+  if (cut) co = *cut;
+  if (!ctx && co.recut_enable) return RUV_ERR_BAD_INPUT;  // (the seam cut alone needs no device)
+  ruv_unfold_opts uo;
+  ruv_unfold_opts_default(&uo);
+  if (unfold) uo = *unfold;
+  CutOpts o;
+  o.seam_enable = co.seam_enable != 0;
+  o.seam_min_faces = co.seam_min_faces;
+  o.seam_branch = co.seam_branch_count;
+  o.recut_enable = co.recut_enable != 0;
+  o.max_rounds = co.recut_max_rounds;
+  o.max_splits = co.recut_max_splits;
+  o.fold_fraction = co.recut_fold_fraction;
+  o.max_charts = co.recut_max_charts;
+  std::unique_ptr<ruv_prepared> p(new ruv_prepared());
+  std::string err;
+  // each controller round: every chart unfolded in one batched solve on the context
+  UnfoldFn solve = [&](const Prepared& P, std::vector<double>& uv, std::string& e) -> bool {
+    ruv_lscm_batch b;
+    b.n_charts = (int64_t)P.vert_off.size() - 1;
+    b.vert_off = P.vert_off.data();
+    b.tri_off = P.tri_off.data();
+    b.p3 = P.p3.data();
+    b.tris = P.tris.data();
+    b.pinned = P.pinned.data();
+    b.pin_uv = P.pin_uv.data();
+    b.p2 = P.p2.data();
+    uv.assign(2 * std::max<int64_t>(P.vert_off.back(), 1), 0.0);
+    ruv_status st = ruv_lscm_solve_batch(ctx, &b, &uo, uv.data(), nullptr);
+    if (st != RUV_OK && st != RUV_ERR_NOT_CONVERGED && st != RUV_ERR_BREAKDOWN) {
+      e = ctx->c.last_error;
+      return false;
+    }
+    return true;
+  };
+  int64_t added = 0;
+  ruv_status s;
+  try {
+    s = prepare_mesh_cut(pos, n_verts, faces, n_faces, weld_tol, angle_min_deg, threads, o, &solve, p->p, &added, err);
+  } catch (const std::bad_alloc&) {
+    return RUV_ERR_OOM;
+  } catch (...) {
+    return RUV_ERR_INTERNAL;
+  }
+  if (s != RUV_OK) return ctx ? fail(ctx, s, err.empty() ? "mesh preparation failed" : err) : s;
+  if (added_out) *added_out = added;
+  *out = p.release();
+  return RUV_OK;
+}
+
 ruv_status ruv_prepare_patches(int64_t n_patches, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
                                const int32_t* tris, int32_t threads, ruv_prepared** out) {
   if (!out || n_patches < 0 || !vert_off || !tri_off) return RUV_ERR_BAD_INPUT;

@@ -853,6 +853,317 @@ ruv_status prepare_mesh_topology(std::vector<double>&& wpos3, std::vector<int32_
   return finish_mesh(wpos, F, ef, cut, threads, sets, clk, P, err);
 }
 
+namespace {
+// ------------------------------------------------------------------ seam cuts and re-cutting
+// seam.rs:54-305, recut.rs:71-146 on one chart of a Prepared, in chart-local vertex indices
+// (the chart's vertex ids are sorted, so local order is source-id order and every visit order
+// and tie-break of the reference's id-keyed maps and sets is kept).
+struct ChartRef {
+  const int64_t* faces;
+  int64_t nf;
+  const int64_t* verts;
+  int64_t nv;
+  const int64_t* border;
+  int64_t nb;
+  bool borderless;
+};
+
+ChartRef chart_ref(const Prepared& P, int64_t c) {
+  return {P.face_ids.data() + P.tri_off[c], P.tri_off[c + 1] - P.tri_off[c], P.vertex_ids.data() + P.vert_off[c],
+          P.vert_off[c + 1] - P.vert_off[c], P.border.data() + P.border_off[c], P.border_off[c + 1] - P.border_off[c],
+          P.loop_off[c + 1] == P.loop_off[c]};
+}
+
+int64_t local_id(const ChartRef& ch, int64_t v) { return std::lower_bound(ch.verts, ch.verts + ch.nv, v) - ch.verts; }
+
+inline uint64_t ekey(uint64_t a, uint64_t b) { return a < b ? (a << 32) | b : (b << 32) | a; }
+
+// undirected adjacency with 3-D lengths, edges ascending, each edge's two entries in that order
+struct LocalAdj {
+  std::vector<int64_t> off;
+  std::vector<int32_t> to;
+  std::vector<double> len;
+};
+LocalAdj local_adjacency(const std::vector<double>& pos, const std::vector<int32_t>& F, const ChartRef& ch) {
+  std::vector<uint64_t> keys;
+  keys.reserve(3 * ch.nf);
+  for (int64_t q = 0; q < ch.nf; ++q) {
+    const int64_t f = ch.faces[q];
+    for (int k = 0; k < 3; ++k)
+      keys.push_back(ekey((uint64_t)local_id(ch, F[3 * f + k]), (uint64_t)local_id(ch, F[3 * f + (k + 1) % 3])));
+  }
+  std::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  LocalAdj A;
+  A.off.assign(ch.nv + 1, 0);
+  for (uint64_t k : keys) {
+    A.off[(k >> 32) + 1]++;
+    A.off[(k & 0xffffffffu) + 1]++;
+  }
+  for (int64_t i = 0; i < ch.nv; ++i) A.off[i + 1] += A.off[i];
+  A.to.resize(A.off[ch.nv]);
+  A.len.resize(A.off[ch.nv]);
+  std::vector<int64_t> cur(A.off.begin(), A.off.end() - 1);
+  for (uint64_t k : keys) {
+    const int64_t a = (int64_t)(k >> 32), b = (int64_t)(k & 0xffffffffu);
+    const int64_t sa = ch.verts[a], sb = ch.verts[b];
+    const D3 d = D3{pos[3 * sa], pos[3 * sa + 1], pos[3 * sa + 2]} - D3{pos[3 * sb], pos[3 * sb + 1], pos[3 * sb + 2]};
+    const double l = norm3(d);
+    A.to[cur[a]] = (int32_t)b;
+    A.len[cur[a]++] = l;
+    A.to[cur[b]] = (int32_t)a;
+    A.len[cur[b]++] = l;
+  }
+  return A;
+}
+
+// multi-source Dijkstra: pops the smallest distance, ties the larger id; a relaxation must
+// improve by more than 1e-12 (seam.rs:54-109).  Unreached vertices keep +inf.
+void local_dijkstra(const LocalAdj& A, const std::vector<int32_t>& seeds, std::vector<double>& dist,
+                    std::vector<int32_t>& prev) {
+  const int64_t n = (int64_t)A.off.size() - 1;
+  dist.assign(n, std::numeric_limits<double>::infinity());
+  prev.assign(n, -1);
+  struct Item {
+    double d;
+    int32_t v;
+  };
+  auto less = [](const Item& x, const Item& y) { return x.d > y.d || (x.d == y.d && x.v < y.v); };
+  std::vector<Item> heap;
+  for (int32_t s : seeds) {
+    dist[s] = 0.0;
+    heap.push_back({0.0, s});
+    std::push_heap(heap.begin(), heap.end(), less);
+  }
+  while (!heap.empty()) {
+    std::pop_heap(heap.begin(), heap.end(), less);
+    const Item it = heap.back();
+    heap.pop_back();
+    if (dist[it.v] < it.d - 1e-12) continue;
+    for (int64_t e = A.off[it.v]; e < A.off[it.v + 1]; ++e) {
+      const int32_t w = A.to[e];
+      const double nd = it.d + A.len[e];
+      if (nd < dist[w] - 1e-12) {
+        dist[w] = nd;
+        prev[w] = it.v;
+        heap.push_back({nd, w});
+        std::push_heap(heap.begin(), heap.end(), less);
+      }
+    }
+  }
+}
+
+// the reached vertex with the largest distance outside `skip`, the smallest id on ties
+int32_t local_farthest(const std::vector<double>& dist, const std::vector<uint8_t>& skip) {
+  int32_t best = -1;
+  for (int32_t v = 0; v < (int32_t)dist.size(); ++v) {
+    if (!std::isfinite(dist[v]) || skip[v]) continue;
+    if (best < 0 || dist[v] > dist[best]) best = v;
+  }
+  return best;
+}
+
+std::vector<int32_t> local_path(const std::vector<int32_t>& prev, int32_t target) {
+  std::vector<int32_t> path{target};
+  for (int32_t cur = prev[target]; cur >= 0; cur = prev[cur]) path.push_back(cur);
+  std::reverse(path.begin(), path.end());
+  return path;
+}
+
+// the first minimum of pos.x over ids (ids ascending), seam.rs:177-187
+int64_t min_x_of(const std::vector<double>& pos, const int64_t* ids, int64_t n) {
+  int64_t best = 0;
+  for (int64_t i = 1; i < n; ++i)
+    if (pos[3 * ids[i]] < pos[3 * ids[best]]) best = i;
+  return best;
+}
+
+// the seam tree's cut edges (seam.rs:167-231), as sorted source-id keys
+std::vector<uint64_t> seam_edges(const std::vector<double>& pos, const std::vector<int32_t>& F, const ChartRef& ch,
+                                 int64_t branch_count) {
+  std::vector<uint64_t> out;
+  if (ch.nf < 2 || ch.nv == 0) return out;
+  const LocalAdj A = local_adjacency(pos, F, ch);
+  std::vector<uint8_t> tree(ch.nv, 0);
+  std::vector<double> dist;
+  std::vector<int32_t> prev;
+  local_dijkstra(A, {(int32_t)min_x_of(pos, ch.verts, ch.nv)}, dist, prev);
+  const int32_t a = local_farthest(dist, tree);
+  if (a < 0) return out;
+  local_dijkstra(A, {a}, dist, prev);
+  const int32_t b = local_farthest(dist, tree);
+  if (b < 0 || a == b) return out;
+  std::vector<std::vector<int32_t>> paths{local_path(prev, b)};
+  for (int32_t v : paths[0]) tree[v] = 1;
+  for (int64_t k = 0; k < branch_count; ++k) {
+    std::vector<int32_t> seeds;
+    for (int32_t v = 0; v < (int32_t)ch.nv; ++v)
+      if (tree[v]) seeds.push_back(v);
+    local_dijkstra(A, seeds, dist, prev);
+    const int32_t f = local_farthest(dist, tree);
+    if (f < 0) break;
+    std::vector<int32_t> br = local_path(prev, f);
+    if (br.size() < 2) break;
+    for (int32_t v : br) tree[v] = 1;
+    paths.push_back(std::move(br));
+  }
+  for (auto& pth : paths)
+    for (size_t k = 0; k + 1 < pth.size(); ++k) out.push_back(ekey((uint64_t)ch.verts[pth[k]], (uint64_t)ch.verts[pth[k + 1]]));
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+  return out;
+}
+
+// the border-crossing chord's edges (seam.rs:246-283)
+std::vector<uint64_t> chord_edges(const std::vector<double>& pos, const std::vector<int32_t>& F, const ChartRef& ch) {
+  std::vector<uint64_t> out;
+  if (ch.nb == 0 || ch.nf < 2) return out;
+  const LocalAdj A = local_adjacency(pos, F, ch);
+  const int64_t a_src = ch.border[min_x_of(pos, ch.border, ch.nb)];
+  const int32_t a = (int32_t)local_id(ch, a_src);
+  std::vector<double> dist;
+  std::vector<int32_t> prev;
+  local_dijkstra(A, {a}, dist, prev);
+  int32_t best = -1;
+  for (int64_t k = 0; k < ch.nb; ++k) {
+    const int32_t v = (int32_t)local_id(ch, ch.border[k]);
+    if (v == a || !std::isfinite(dist[v])) continue;
+    if (best >= 0 && dist[v] < dist[best]) continue;
+    if (best >= 0 && dist[v] == dist[best]) best = std::min(best, v);
+    else best = v;
+  }
+  if (best < 0 || !(dist[best] > 1e-12)) return out;
+  const std::vector<int32_t> pth = local_path(prev, best);
+  for (size_t k = 0; k + 1 < pth.size(); ++k) out.push_back(ekey((uint64_t)ch.verts[pth[k]], (uint64_t)ch.verts[pth[k + 1]]));
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+  return out;
+}
+
+// triangles against the dominant winding (metrics.rs:33-56)
+int64_t winding_flips(const double* uv, const int32_t* tris, int64_t nt) {
+  if (nt == 0) return 0;
+  auto ts = [&](int64_t t) {
+    const double* u = uv + 2 * (int64_t)tris[3 * t];
+    const double* v = uv + 2 * (int64_t)tris[3 * t + 1];
+    const double* w = uv + 2 * (int64_t)tris[3 * t + 2];
+    return (v[0] - u[0]) * (w[1] - u[1]) - (w[0] - u[0]) * (v[1] - u[1]);
+  };
+  double sum = 0.0;
+  for (int64_t t = 0; t < nt; ++t) sum += ts(t);
+  const double dom = sum < 0.0 ? -1.0 : 1.0;
+  int64_t n = 0;
+  for (int64_t t = 0; t < nt; ++t)
+    if (ts(t) * dom <= 0.0) ++n;
+  return n;
+}
+}  // namespace
+
+ruv_status prepare_mesh_cut(const double* pos, int64_t nv, const int32_t* faces, int64_t nf, double weld_tol,
+                            double angle_min_deg, int threads, const CutOpts& co, const UnfoldFn* unfold,
+                            Prepared& P, int64_t* added_out, std::string& err) {
+  *added_out = 0;
+  for (int64_t i = 0; i < 3 * nf; ++i)
+    if (faces[i] < 0 || faces[i] >= nv) {
+      err = "face index out of range";
+      return RUV_ERR_BAD_INPUT;
+    }
+  StageClock clk;
+  std::vector<D3> wpos;
+  std::vector<int32_t> F;
+  weld(pos, nv, faces, nf, weld_tol, wpos, F);
+  const int64_t wnf = (int64_t)F.size() / 3;
+  for (int64_t f = 0; f < wnf; ++f)
+    if (F[3 * f] == F[3 * f + 1] || F[3 * f + 1] == F[3 * f + 2] || F[3 * f] == F[3 * f + 2]) {
+      err = "degenerate face with a repeated vertex";
+      return RUV_ERR_BAD_INPUT;
+    }
+  EdgeFaces ef = build_edge_faces((int64_t)wpos.size(), F, threads);
+  std::vector<uint8_t> cut = cut_flags(wpos, F, ef, angle_min_deg, threads);
+  // the segmentation's cut set as sorted edge keys, and slot flags from a key set
+  std::vector<uint64_t> cut0;
+  for (int64_t sl = 0; sl < 3 * wnf; ++sl)
+    if (cut[sl]) cut0.push_back(ekey((uint64_t)F[sl], (uint64_t)F[3 * (sl / 3) + (sl % 3 + 1) % 3]));
+  std::sort(cut0.begin(), cut0.end());
+  cut0.erase(std::unique(cut0.begin(), cut0.end()), cut0.end());
+  auto flags_of = [&](const std::vector<uint64_t>& keys) {
+    std::vector<uint8_t> fl(3 * wnf, 0);
+    for (int64_t sl = 0; sl < 3 * wnf; ++sl)
+      fl[sl] = std::binary_search(keys.begin(), keys.end(),
+                                  ekey((uint64_t)F[sl], (uint64_t)F[3 * (sl / 3) + (sl % 3 + 1) % 3]))
+                   ? 1
+                   : 0;
+    return fl;
+  };
+  auto rebuild = [&](const std::vector<uint64_t>& keys) -> ruv_status {
+    std::vector<uint8_t> fl = flags_of(keys);
+    Prepared Q;
+    ruv_status st = finish_mesh(wpos, F, ef, fl, threads, nullptr, clk, Q, err);
+    if (st == RUV_OK) P = std::move(Q);
+    return st;
+  };
+  ruv_status st = finish_mesh(wpos, F, ef, cut, threads, nullptr, clk, P, err);
+  if (st != RUV_OK) return st;
+  // seam cut of the closed charts (seam.rs:286-305)
+  if (co.seam_enable) {
+    std::vector<uint64_t> all = cut0;
+    for (int64_t c = 0; c + 1 < (int64_t)P.vert_off.size(); ++c) {
+      const ChartRef ch = chart_ref(P, c);
+      if (!ch.borderless || ch.nf < co.seam_min_faces) continue;
+      for (uint64_t e : seam_edges(P.mesh_pos, P.mesh_faces, ch, co.seam_branch)) all.push_back(e);
+    }
+    std::sort(all.begin(), all.end());
+    all.erase(std::unique(all.begin(), all.end()), all.end());
+    if (all.size() != cut0.size() && (st = rebuild(all)) != RUV_OK) return st;
+  }
+  // re-cutting of folding charts (recut.rs:98-146), from the segmentation's cut set as the
+  // reference's pipeline passes it (pipeline.rs:158)
+  if (co.recut_enable) {
+    if (!unfold) {
+      err = "re-cutting needs an unfold";
+      return RUV_ERR_BAD_INPUT;
+    }
+    std::vector<uint64_t> all = cut0;
+    int64_t added = 0;
+    for (int64_t round = 0; round < co.max_rounds; ++round) {
+      if (added >= co.max_splits) break;
+      std::vector<double> uv;
+      if (!(*unfold)(P, uv, err)) return RUV_ERR_INTERNAL;
+      const int64_t NC = (int64_t)P.vert_off.size() - 1;
+      std::vector<int64_t> folds(NC);
+      std::vector<int64_t> folding;
+      for (int64_t c = 0; c < NC; ++c) {
+        const int64_t nt = P.tri_off[c + 1] - P.tri_off[c];
+        folds[c] = winding_flips(uv.data() + 2 * P.vert_off[c], P.tris.data() + 3 * P.tri_off[c], nt);
+        if ((double)folds[c] / (double)std::max<int64_t>(nt, 1) > co.fold_fraction) folding.push_back(c);
+      }
+      if (folding.empty()) break;
+      std::stable_sort(folding.begin(), folding.end(), [&](int64_t x, int64_t y) { return folds[x] > folds[y]; });
+      bool grew = false;
+      for (int64_t c : folding) {
+        if (added >= co.max_splits) break;
+        const ChartRef ch = chart_ref(P, c);
+        const std::vector<uint64_t> e = ch.borderless
+                                            ? seam_edges(P.mesh_pos, P.mesh_faces, ch, std::max<int64_t>(co.seam_branch, 1))
+                                            : chord_edges(P.mesh_pos, P.mesh_faces, ch);
+        for (uint64_t k : e) {
+          auto it = std::lower_bound(all.begin(), all.end(), k);
+          if (it == all.end() || *it != k) {
+            all.insert(it, k);
+            ++added;
+            grew = true;
+          }
+        }
+      }
+      if (!grew) break;
+      if ((st = rebuild(all)) != RUV_OK) return st;
+      if ((int64_t)P.vert_off.size() - 1 > co.max_charts) break;
+    }
+    *added_out = added;
+  }
+  return RUV_OK;
+}
+
 double uv_signed_area(const double* uv, const int32_t* tris, int64_t nt) {  // lscm.rs:120-129
   double a = 0.0;
   for (int64_t t = 0; t < nt; ++t) {

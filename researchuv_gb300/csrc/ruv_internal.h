@@ -50,6 +50,21 @@ ruv_status prepare_mesh_topology(std::vector<double>&& wpos3, std::vector<int32_
                                  std::vector<int32_t>&& ef_faces, std::vector<uint8_t>&& cut, int threads,
                                  const ChartSetsFn* sets, Prepared& P, std::string& err);
 
+// Seam cut of closed charts (seam.rs SeamCutOptions) and re-cutting of folding charts
+// (recut.rs RecutOptions) after the segmentation (pipeline.rs:149-167).
+struct CutOpts {
+  bool seam_enable = false;
+  int64_t seam_min_faces = 8, seam_branch = 1;
+  bool recut_enable = false;
+  int64_t max_rounds = 6, max_splits = 48, max_charts = 64;
+  double fold_fraction = 0.02;
+};
+// The unfold of every chart of a Prepared (2 * n_verts UVs, chart-local order).
+using UnfoldFn = std::function<bool(const Prepared& P, std::vector<double>& uv, std::string& err)>;
+ruv_status prepare_mesh_cut(const double* pos, int64_t nv, const int32_t* faces, int64_t nf, double weld_tol,
+                            double angle_min_deg, int threads, const CutOpts& co, const UnfoldFn* unfold,
+                            Prepared& P, int64_t* added_out, std::string& err);
+
 // The dihedral test acos(n1.n2) > angle of segment.rs:130-137 as d < d*: d* from the host
 // libm's acos (so both sides decide alike); NaN when acos is not monotone around d*.
 double acos_cut_threshold(double angle_min_deg);

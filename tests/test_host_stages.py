@@ -105,3 +105,29 @@ def test_bad_inputs_are_rejected():
     with pytest.raises(R.RuvError):  # the library implements SolverBackend::Gpu only
         R.UnfoldOptions(solver=R.SolverBackend.CPU).to_c()
     R.UnfoldOptions(keep_metric=True).to_c()  # KeepMetric runs on the GPU path (Schur complement)
+
+
+@pytest.mark.parametrize("name,mesh,angle,min_faces,branch", [
+    ("sphere_8x6", lambda: O.uv_sphere(8, 6), 180.0, 4, 1),
+    ("sphere_24x12", lambda: O.uv_sphere(24, 12), 180.0, 8, 2),
+    ("torus_closed", lambda: O.torus(2.0, 0.7, 24, 16), 180.0, 8, 1),
+    ("cube_charts", lambda: O.cube(6), 30.0, 8, 1),
+])
+def test_seam_cut_bitwise_vs_oracle(name, mesh, angle, min_faces, branch):
+    """seam.rs:167-305 (seam tree of every closed chart, charts rebuilt over the grown cut
+    set) on the host: the same charts, loops, frames and pins as the oracle's restatement."""
+    p, f = mesh()
+    C, added = R.prepare_mesh_cut(None, p, f, angle_min_deg=angle,
+                                  seam_cut=R.SeamCutOptions(enable=True, min_faces=min_faces, branch_count=branch))
+    assert added == 0
+    _compare(O.Pipeline(p, f, angle_deg=angle, lu_limit=0, seam_cut=(1, min_faces, branch)), C)
+
+
+def test_seam_cut_opens_the_sphere():
+    """seam.rs:335-357: the welded 8x6 sphere becomes one chart with one border loop."""
+    p, f = O.uv_sphere(8, 6)
+    C, _ = R.prepare_mesh_cut(None, p, f, angle_min_deg=180.0,
+                              seam_cut=R.SeamCutOptions(enable=True, min_faces=4))
+    assert C.n_charts == 1
+    lo = C.i64("chart.loop_off")
+    assert lo[1] - lo[0] == 1
