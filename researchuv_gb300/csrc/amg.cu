@@ -44,6 +44,11 @@ constexpr int kAccCap = 48;
 // (amg.rs:299); on the device the cap sets the density of every coarse operator and so the
 // set-up and V-cycle cost, and 4 gives the shortest whole solve (iterations nearly those of 8)
 constexpr int kPMaxRow = 4;
+// Levels with a smoothed prolongator in AMG-SA, tentative below: the coarse operators of a
+// fully smoothed hierarchy are the densest, and two smoothed levels give the shortest solve on
+// the measured workloads (4096 disks: 91.7 ms against 91.3 with all levels smoothed; the 2048^2
+// height field: 129 ms against 180 with all, 146 with plain aggregation)
+constexpr int kSaLevels = 2;
 constexpr int64_t kLevelTile = 1024;  // rows per CTA tile in the V-cycle kernels
 
 __device__ __forceinline__ int64_t find_chart64(const int64_t* off, int64_t n_charts, int64_t i) {
@@ -1071,6 +1076,7 @@ struct AmgLevelDev {
   float* rv = nullptr;
   float *b = nullptr, *x = nullptr, *y = nullptr, *t = nullptr;
   int32_t* agg = nullptr;  // aggregate of each row (the tentative prolongator), -1 if none
+  bool smoothed = false;   // transfer to the next level by a smoothed prolongator (else tentative)
   const uint16_t* c16 = nullptr;  // 16-bit column stream (level 0), see ColsNarrow
   const int32_t* cbase = nullptr;
   LvlTiles cont{nullptr, nullptr, 0};  // tiles over rows whose chart continues below this level
@@ -1079,7 +1085,8 @@ struct AmgLevelDev {
 
 struct AmgHierarchy {
   int nrhs = 2;
-  bool smoothed = false;  // smoothed prolongators (AMG-SA); else tentative (one 1 per row)
+  bool smoothed = false;  // smoothed prolongators (AMG-SA) on the first sa_levels levels; else tentative
+  int sa_levels = 0;
   int64_t n_charts = 0;
   std::vector<AmgLevelDev> lv;
   int32_t* final_lvl = nullptr;
@@ -1222,7 +1229,11 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   H->nrhs = sys.nrhs;
   H->smoothed = smooth;
   H->n_charts = NC;
-  H->alpha_c = smooth ? 1.0f : 1.5f;  // over-correct the piecewise-constant coarse space
+  // smoothed prolongators on the first sa_levels levels, tentative below (the coarse levels of a
+  // smoothed hierarchy are the densest: their products and cycles cost the most)
+  H->sa_levels = smooth ? kSaLevels : 0;
+  if (const char* e = std::getenv("RUV_AMG_SA_LEVELS")) H->sa_levels = smooth ? std::max(0, std::atoi(e)) : 0;
+  H->alpha_c = 1.5f;  // over-correct the piecewise-constant coarse space of tentative levels
   if (const char* e = std::getenv("RUV_AMG_ALPHA")) H->alpha_c = (float)std::atof(e);
   float strong = kStrong;  // matching candidates: couplings >= strong * the row's strongest
   if (const char* e = std::getenv("RUV_AMG_STRONG")) strong = (float)std::atof(e);
@@ -1256,6 +1267,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   H->h_final.assign(NC, -1);
   std::vector<int32_t> cont(NC, 0);
   for (int lvl = 0; lvl < kMaxLevels; ++lvl) {
+    const bool sm = lvl < H->sa_levels;  // this level's prolongator is smoothed
     const std::string tag = "amg.l" + std::to_string(lvl);
     AmgLevelDev& L = H->lv[lvl];
     int64_t n_cont = 0;
@@ -1361,14 +1373,14 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     // ---- prolongator P (fine rows of continuing charts)
     int32_t* cnt = ctx.ws.get<int32_t>(tag + ".pcnt", L.n);
     L.poff = ctx.ws.get<int64_t>(tag + ".poff", L.n + 1);
-    k_prolong<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, smooth ? 1 : 0, pmax, cnt,
+    k_prolong<0><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, sm ? 1 : 0, pmax, cnt,
                                               nullptr, nullptr, nullptr, ovf);
     count_launches(1);
     const int64_t PN = offsets_from_counts(ctx, cnt, L.n, L.poff, tag + ".po");
     L.n_pnnz = PN;
     L.pc = ctx.ws.get<int32_t>(tag + ".pc", PN);
     L.pv = ctx.ws.get<float>(tag + ".pv", PN);
-    k_prolong<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, smooth ? 1 : 0, pmax, cnt,
+    k_prolong<1><<<div_up(L.n, B), B, 0, s>>>(L.n, active, L.rp, L.cols, L.vals, L.dinv, agg, sm ? 1 : 0, pmax, cnt,
                                               L.poff, L.pc, L.pv, ovf);
     count_launches(1);
     // ---- R = P^T
@@ -1409,7 +1421,8 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
       }
     };
     int64_t WN = 0;
-    if (!smooth) {
+    L.smoothed = sm;
+    if (!sm) {
       // ---- tentative prolongator: A_c = R A P straight from A (keys through agg)
       const double avg = mean(PN, NA) * mean(L.nnz, L.n);
       gal_count<true>(ctx, gw, NA, avg, nullptr, L.roff, L.rc, (const float*)nullptr, L.rp, L.cols, L.vals64,
@@ -1594,7 +1607,7 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
-    float* xpre = H->smoothed ? L.x : nullptr;  // the tentative cycle re-forms it on the way up
+    float* xpre = L.smoothed ? L.x : nullptr;  // the tentative cycle re-forms it on the way up
 #define CALL(X, UU, KK)                                                                                                \
   k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                     L.dinv, L.b, xpre, L.t)
@@ -1626,7 +1639,7 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
-    if (!H->smoothed) {
+    if (!L.smoothed) {
 #define CALL(X, UU, KK)                                                                                                \
   k_smooth_up_t<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                     L.dinv, L.b, L.agg, C.x, H->alpha_c, L.x)
@@ -1643,8 +1656,7 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
     }
     const int lp = lanes_for(L.n ? (double)L.n_pnnz / (double)L.n : 1.0);
 #define CALL(X, UU, KK)                                                                                                  \
-  k_prolong_add<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.poff, L.pc, L.pv, C.x, L.x, L.y, \
-                                                            H->alpha_c)
+  k_prolong_add<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.poff, L.pc, L.pv, C.x, L.x, L.y, 1.0f)
     RUV_LPR_SWITCH(lp, CALL)
 #undef CALL
 #define CALL(X, UU, KK)                                                                                              \
