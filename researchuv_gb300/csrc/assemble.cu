@@ -664,6 +664,10 @@ namespace {
 // ends its loop, which here is a zero area row (every free gradient component and a - target
 // exactly zero) or a non-finite aux.
 
+// Vertices (triangles) per KeepMetric tile, one per thread of a 256-thread CTA: the gradient
+// is a few dozen FP64 operations per vertex, so a large chart wants many CTAs in flight.
+constexpr int64_t kKmTile = 256;
+
 // 3-D area per triangle (segment.rs:61-70)
 __global__ void k_km_face_area(const double* __restrict__ p3, const int32_t* __restrict__ tri_g, int64_t nt,
                                double* __restrict__ A) {
@@ -867,17 +871,17 @@ void keep_metric_rhs(Ctx& ctx, DevBatch& bt, DevSystem& sys, const double* d_fli
   count_launches(2);
   std::vector<int64_t> tbeg, tctile, vbeg, vctile;
   std::vector<int32_t> tchart, vchart;
-  build_tiles(bt.h_tri_off, 2048, tbeg, tchart, tctile);
-  build_tiles(bt.h_vert_off, 2048, vbeg, vchart, vctile);
+  build_tiles(bt.h_tri_off, kKmTile, tbeg, tchart, tctile);
+  build_tiles(bt.h_vert_off, kKmTile, vbeg, vchart, vctile);
   const int64_t NTT = (int64_t)tchart.size(), NTL = (int64_t)vchart.size();
   std::vector<int64_t> ttab(2 * NTT), vtab(2 * NTL);
   for (int64_t t = 0; t < NTT; ++t) {
     ttab[2 * t] = tbeg[t];
-    ttab[2 * t + 1] = std::min(tbeg[t] + 2048, bt.h_tri_off[tchart[t] + 1]);
+    ttab[2 * t + 1] = std::min(tbeg[t] + kKmTile, bt.h_tri_off[tchart[t] + 1]);
   }
   for (int64_t t = 0; t < NTL; ++t) {
     vtab[2 * t] = vbeg[t];
-    vtab[2 * t + 1] = std::min(vbeg[t] + 2048, bt.h_vert_off[vchart[t] + 1]);
+    vtab[2 * t + 1] = std::min(vbeg[t] + kKmTile, bt.h_vert_off[vchart[t] + 1]);
   }
   int64_t* d_ttab = ws.get<int64_t>("km.ttab", std::max<int64_t>(2 * NTT, 1));
   int64_t* d_tct = ws.get<int64_t>("km.tctile", NC + 1);
@@ -907,17 +911,17 @@ void driver_keep_metric(Ctx& ctx, DevBatch& bt, const DevSystem& sys, const doub
   const int64_t NC = bt.n_charts;
   std::vector<int64_t> tbeg, tctile, vbeg, vctile;
   std::vector<int32_t> tchart, vchart;
-  build_tiles(bt.h_tri_off, 2048, tbeg, tchart, tctile);
-  build_tiles(bt.h_vert_off, 2048, vbeg, vchart, vctile);
+  build_tiles(bt.h_tri_off, kKmTile, tbeg, tchart, tctile);
+  build_tiles(bt.h_vert_off, kKmTile, vbeg, vchart, vctile);
   const int64_t NTT = (int64_t)tchart.size(), NTL = (int64_t)vchart.size();
   std::vector<int64_t> ttab(2 * NTT), vtab(2 * NTL);
   for (int64_t t = 0; t < NTT; ++t) {
     ttab[2 * t] = tbeg[t];
-    ttab[2 * t + 1] = std::min(tbeg[t] + 2048, bt.h_tri_off[tchart[t] + 1]);
+    ttab[2 * t + 1] = std::min(tbeg[t] + kKmTile, bt.h_tri_off[tchart[t] + 1]);
   }
   for (int64_t t = 0; t < NTL; ++t) {
     vtab[2 * t] = vbeg[t];
-    vtab[2 * t + 1] = std::min(vbeg[t] + 2048, bt.h_vert_off[vchart[t] + 1]);
+    vtab[2 * t + 1] = std::min(vbeg[t] + kKmTile, bt.h_vert_off[vchart[t] + 1]);
   }
   int64_t* d_ttab = ws.get<int64_t>("kmd.ttab", std::max<int64_t>(2 * NTT, 1));
   int32_t* d_tch = ws.get<int32_t>("kmd.tchart", std::max<int64_t>(NTT, 1));
