@@ -46,10 +46,11 @@ METRIC = "batched LSCM unknowns/s at <=1e-6 UV err vs FP64 LU"
 UNIT = "unknowns/s"
 L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (read + write) per algorithmic byte of the batched SpMV kernel, from one ncu
-# capture of its first launch on the 1024-disk operator (247.9 MB of traffic for 257 MB of
-# algorithmic bytes; profiles/kernels_disks1024_dram.md).  The disk workloads scale by count,
-# so the traffic of a launch on the 4096-disk operator is this ratio times its algorithmic bytes.
-SPMV_DRAM_PER_ALG_BYTE = 0.965
+# capture of its first launch on the 1024-disk operator with the 16-bit column stream
+# (199.0 MB of traffic for 256.9 MB of algorithmic bytes; profiles/kernels_disks1024_dram.md).
+# The disk workloads scale by count, so the traffic of a launch on the 4096-disk operator is
+# this ratio times its algorithmic bytes.
+SPMV_DRAM_PER_ALG_BYTE = 0.775
 
 
 def parse():
@@ -284,14 +285,17 @@ def run_reference(args, rank):
     print(json.dumps(line))
 
 
-def single_chart_baseline(ctx, vo, unknowns, batched_ms, n_sample):
+def single_chart_baseline(ctx, vo, unknowns, batched_ms, n_sample, precond_name="JACOBI"):
     """The measuring stick of the batched solve: plain single-chart FP64 GPU PCG, i.e. one
-    GpuSolver::cg_solve_precond call (FP64, Jacobi, tol 1e-12, the reference's defaults,
-    lscm.rs:492-501) per chart on that chart's interleaved CSR, sequentially, as the
-    reference's per-chart unfold would.  Timed on a size-stratified sample of charts and
-    scaled to the whole workload by unknowns (larger charts need more iterations per
-    unknown, so the scaling understates the full sequential time)."""
+    GpuSolver::cg_solve_precond call (FP64, tol 1e-12; Jacobi is the reference's default,
+    lscm.rs:492-501, IC(0) its strongest single-level preconditioner) per chart on that
+    chart's interleaved CSR, sequentially, as the reference's per-chart unfold would.  Timed
+    on a size-stratified sample of charts and scaled to the whole workload by unknowns
+    (larger charts need more iterations per unknown, so the scaling understates the full
+    sequential time)."""
     import researchuv_gb300 as R
+
+    pc = getattr(R.Precond, precond_name)
 
     sizes = np.diff(vo)
     order = np.argsort(sizes)
@@ -303,11 +307,11 @@ def single_chart_baseline(ctx, vo, unknowns, batched_ms, n_sample):
             systems.append((R.CsrMatrix(vals, cols, rp), rhs))
     solver = R.GpuSolver.new()
     for a, rhs in systems[:4]:  # warm-up
-        solver.cg_solve_precond(a, rhs, 16384, 1e-12, R.Precond.JACOBI)
+        solver.cg_solve_precond(a, rhs, 16384, 1e-12, pc)
     t0 = time.perf_counter()
     unk, iters, fails = 0, 0, 0
     for a, rhs in systems:
-        r = solver.cg_solve_precond(a, rhs, 16384, 1e-12, R.Precond.JACOBI)
+        r = solver.cg_solve_precond(a, rhs, 16384, 1e-12, pc)
         unk += a.rows()
         if r is None:
             fails += 1
@@ -318,7 +322,7 @@ def single_chart_baseline(ctx, vo, unknowns, batched_ms, n_sample):
     return {"ms_per_step_extrapolated": full_ms, "sample_charts": len(systems), "sample_unknowns": unk,
             "sample_s": round(dt, 3), "sample_iters": iters, "failed": fails,
             "batched_speedup": full_ms / batched_ms,
-            "what": "sequential ruv_cg_solve per chart (FP64 Jacobi PCG, host CSR in / x out), "
+            "what": f"sequential ruv_cg_solve per chart (FP64 {precond_name.lower()} PCG, host CSR in / x out), "
                     "size-stratified sample scaled by unknowns"}
 
 
@@ -513,9 +517,10 @@ def main():
     phases /= max(args.steps, 1)
 
     # dominant kernel (batched SpMV) timed alone on the same operator
-    spmv_ms, spmv_bytes = R.bench_spmv(ctx, prec, reps=30, n_buffers=2)
+    spmv_ms, spmv_bytes, spmv_stream = R.bench_spmv(ctx, prec, reps=30, n_buffers=2)
     peak, peak_src = peaks()
     achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9 if spmv_ms > 0 else 0.0
+    streamed = spmv_stream / (spmv_ms * 1e-3) / 1e9 if spmv_ms > 0 else 0.0
 
     h2d = sum(int(x) for x in [
         8 * (batch.n_charts + 1) * 2, 3 * 8 * nv, 3 * 4 * int(charts.i64("chart.tri_off")[-1]), nv, 2 * 8 * nv,
@@ -543,12 +548,19 @@ def main():
                      "traffic": (SPMV_DRAM_PER_ALG_BYTE * spmv_bytes if args.workload.startswith("disks") else None),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the "
                                        "1024-disk operator, scaled by algorithmic bytes",
-                     "ms_per_launch": spmv_ms, "algorithmic_bytes": spmv_bytes},
+                     "ms_per_launch": spmv_ms, "algorithmic_bytes": spmv_bytes,
+                     "algorithmic_bytes_what": "FP32 values + 32-bit columns per entry, row pointers, p read once, "
+                                               "q written (the canonical scalar-pattern SpMV)",
+                     "stream_bytes": spmv_stream, "stream_gbs": streamed, "stream_frac": streamed / peak,
+                     "stream_bytes_what": "the same with the 16-bit column stream the kernel reads for charts "
+                                          "of <= 65536 rows"},
         "gpu_launches": int(launches),
         "clocks": clock_info,
     }
     if rank == 0 and not args.no_single_chart:
         line["single_chart_fp64_pcg"] = single_chart_baseline(ctx, vo, unknowns, ms, args.single_chart_sample)
+        line["single_chart_fp64_pcg_ic0"] = single_chart_baseline(ctx, vo, unknowns, ms,
+                                                                  max(args.single_chart_sample // 4, 1), "IC0")
     if rank == 0 and not args.no_cpu_baseline and src[0] == "patches":
         base, err, n_err = cpu_baseline(src, uv, args.cpu_budget)
         line["cpu_baseline"] = base

@@ -256,10 +256,12 @@ int64_t ruv_kernel_launches(const ruv_ctx* ctx);
 /* Kernel benchmark on the last assembled batch: `reps` launches of the batched SpMV kernel
  * (q = A p over every row, FP32 values when precision is MIXED, FP64 otherwise), rotating
  * between `n_buffers` vector sets so the timed launches read their vectors from HBM.
- * Writes the mean device time per launch (ms, CUDA events) and the algorithmic bytes of
- * one launch (values + columns + row pointers + p read once + q written). */
+ * Writes the mean device time per launch (ms, CUDA events), the algorithmic bytes of one
+ * launch (values + 32-bit columns + row pointers + p read once + q written) and the bytes
+ * its streams actually hold (the same with 16-bit columns where the operator has them).
+ * Any output may be NULL. */
 ruv_status ruv_bench_spmv(ruv_ctx* ctx, ruv_precision precision, int32_t reps, int32_t n_buffers,
-                          double* ms_per_launch, double* bytes_per_launch);
+                          double* ms_per_launch, double* bytes_per_launch, double* stream_bytes_per_launch);
 
 /* Autotuner: on the last assembled batch, time the batched SpMV for each instantiated
  * launch shape (lanes per row x rows in flight per sub-warp) and tile height (rows per CTA),

@@ -94,7 +94,7 @@ SIGNATURES = {
     "ruv_cg_solve_noalloc": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _i64, _f64, ctypes.c_int, _P(_i64), _vp,
                                             ctypes.c_char_p, _i32]),
     "ruv_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _P(_i32), _P(_i32), _P(_i32), _P(_f64)]),
-    "ruv_bench_spmv": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _i32, _P(_f64), _P(_f64)]),
+    "ruv_bench_spmv": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _i32, _P(_f64), _P(_f64), _P(_f64)]),
 }
 
 _lib = None
@@ -669,11 +669,13 @@ def last_timings(ctx: Context):
 
 
 def bench_spmv(ctx: Context, precision: Precision = Precision.MIXED, reps: int = 20, n_buffers: int = 2):
-    """(ms per launch, algorithmic bytes per launch) of the batched SpMV on the last assembled batch."""
-    ms, by = _f64(0), _f64(0)
-    ctx.check(lib().ruv_bench_spmv(ctx.h, int(precision), reps, n_buffers, ctypes.byref(ms), ctypes.byref(by)),
-              "ruv_bench_spmv")
-    return ms.value, by.value
+    """(ms per launch, algorithmic bytes per launch, stream bytes per launch) of the batched SpMV
+    on the last assembled batch: algorithmic bytes count 32-bit column indices, stream bytes
+    the 16-bit ones the kernel reads where the operator has them."""
+    ms, by, sb = _f64(0), _f64(0), _f64(0)
+    ctx.check(lib().ruv_bench_spmv(ctx.h, int(precision), reps, n_buffers, ctypes.byref(ms), ctypes.byref(by),
+                                   ctypes.byref(sb)), "ruv_bench_spmv")
+    return ms.value, by.value, sb.value
 
 
 def autotune(ctx: Context, precision: Precision = Precision.MIXED, reps: int = 10):

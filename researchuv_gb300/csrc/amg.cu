@@ -1077,7 +1077,7 @@ struct AmgLevelDev {
   float *b = nullptr, *x = nullptr, *y = nullptr, *t = nullptr;
   int32_t* agg = nullptr;  // aggregate of each row (the tentative prolongator), -1 if none
   bool smoothed = false;   // transfer to the next level by a smoothed prolongator (else tentative)
-  const uint16_t* c16 = nullptr;  // 16-bit column stream (level 0), see ColsNarrow
+  const uint16_t* c16 = nullptr;  // 16-bit column stream (every chart of the level <= 65536 rows), see ColsNarrow
   const int32_t* cbase = nullptr;
   LvlTiles cont{nullptr, nullptr, 0};  // tiles over rows whose chart continues below this level
   LvlTiles all{nullptr, nullptr, 0};   // tiles over every row of this level
@@ -1245,6 +1245,8 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   int* ovf = ctx.ws.get<int>("amg.overflow", 8);
   RUV_CUDA(cudaMemsetAsync(ovf, 0, 8 * sizeof(int), s));
   const bool debug = std::getenv("RUV_AMG_DEBUG") != nullptr;
+  const char* narrow_env = std::getenv("RUV_NARROW_COLS");
+  const bool narrow = !(narrow_env && narrow_env[0] == '0');
   {
     AmgLevelDev L0;
     L0.n = sys.n_rows;
@@ -1461,6 +1463,13 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     C.h_chart_row.resize(NC + 1);
     RUV_CUDA(cudaMemcpyAsync(C.h_chart_row.data(), C.chart_row, sizeof(int64_t) * (NC + 1), cudaMemcpyDeviceToHost, s));
     RUV_CUDA(cudaStreamSynchronize(s));
+    if (narrow) {  // 16-bit columns for the smoothers when every chart of this level allows them
+      uint16_t* c16 = nullptr;
+      int32_t* cbase = nullptr;
+      narrow_operator(ctx, NA, C.nnz, NC, C.h_chart_row, C.chart_row, C.rp, C.cols, ntag, &c16, &cbase);
+      C.c16 = c16;
+      C.cbase = cbase;
+    }
     H->lv.push_back(C);
   }
   int h_ovf[8] = {0, 0, 0, 0, 0, 0, 0, 0};

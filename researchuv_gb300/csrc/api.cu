@@ -611,15 +611,16 @@ int32_t ruv_last_timings(const ruv_ctx* ctx, double* ms, int32_t n) {
 }
 
 ruv_status ruv_bench_spmv(ruv_ctx* ctx, ruv_precision precision, int32_t reps, int32_t n_buffers, double* ms_per_launch,
-                          double* bytes_per_launch) {
+                          double* bytes_per_launch, double* stream_bytes_per_launch) {
   if (!ctx || reps <= 0 || n_buffers <= 0) return RUV_ERR_BAD_INPUT;
   return guarded(ctx, [&]() -> ruv_status {
     Ctx& c = ctx->c;
     if (!c.have_last) return fail(ctx, RUV_ERR_BAD_INPUT, "no assembled batch on this context");
-    double bytes = 0.0;
-    double ms = bench_spmv(c, c.last_sys, precision == RUV_PREC_MIXED, reps, n_buffers, &bytes);
+    double bytes = 0.0, stream = 0.0;
+    double ms = bench_spmv(c, c.last_sys, precision == RUV_PREC_MIXED, reps, n_buffers, &bytes, &stream);
     if (ms_per_launch) *ms_per_launch = ms;
     if (bytes_per_launch) *bytes_per_launch = bytes;
+    if (stream_bytes_per_launch) *stream_bytes_per_launch = stream;
     return RUV_OK;
   });
 }

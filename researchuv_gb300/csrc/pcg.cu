@@ -1232,38 +1232,46 @@ __global__ void k_chart_base(int64_t n_charts, const int64_t* __restrict__ chart
 
 }  // namespace
 
-// Off unless RUV_NARROW_COLS=1: on the 4096-disk operator the 16-bit stream cuts the SpMV's
-// bytes by 18% and its time by 8% (0.215 -> 0.187 ms), the AMG solve by 1.7%; the kernel then
-// moves fewer bytes at a lower fraction of the HBM bandwidth.
+// The 16-bit column stream of a chart-blocked CSR operator (all charts of at most 65536
+// rows, else none: the narrow kernels take every tile's base from cbase).  Returns false
+// and leaves both pointers null when some chart is larger.
+bool narrow_operator(Ctx& ctx, int64_t n, int64_t nnz, int64_t n_charts, const std::vector<int64_t>& h_chart_row,
+                     const int64_t* chart_row, const int32_t* row_ptr, const int32_t* cols, const std::string& tag,
+                     uint16_t** c16, int32_t** cbase) {
+  *c16 = nullptr;
+  *cbase = nullptr;
+  for (int64_t c = 0; c < n_charts; ++c)
+    if (h_chart_row[c + 1] - h_chart_row[c] > kNarrowRows) return false;
+  cudaStream_t s = ctx.stream;
+  *c16 = ctx.ws.get<uint16_t>(tag + ".c16", std::max<int64_t>(nnz, 1));
+  *cbase = ctx.ws.get<int32_t>(tag + ".cbase", std::max<int64_t>(n_charts, 1));
+  if (n > 0) {
+    k_narrow_cols<<<div_up(n, 256), 256, 0, s>>>(n, chart_row, n_charts, row_ptr, cols, *c16);
+    count_launches(1);
+  }
+  if (n_charts > 0) {
+    k_chart_base<<<div_up(n_charts, 256), 256, 0, s>>>(n_charts, chart_row, *cbase);
+    count_launches(1);
+  }
+  RUV_LAUNCH_CHECK();
+  return true;
+}
+
+// On unless RUV_NARROW_COLS=0: on the 4096-disk operator the 16-bit stream cuts the SpMV's
+// bytes by 18% and its time by 13% (0.215 -> 0.187 ms).
 void narrow_columns(Ctx& ctx, DevSystem& sys) {
   const char* e = std::getenv("RUV_NARROW_COLS");
-  if (!e || e[0] != '1') {  // 32-bit columns only
+  if (e && e[0] == '0') {  // 32-bit columns only
     sys.cols16 = nullptr;
     sys.cbase = nullptr;
     return;
   }
-  cudaStream_t s = ctx.stream;
-  const int64_t N = sys.n_rows, NC = sys.n_charts;
-  for (int64_t c = 0; c < NC; ++c)
-    if (sys.h_chart_row[c + 1] - sys.h_chart_row[c] > kNarrowRows) {  // a large chart: 32-bit columns
-      sys.cols16 = nullptr;
-      sys.cbase = nullptr;
-      return;
-    }
-  sys.cols16 = ctx.ws.get<uint16_t>("sys.cols16", std::max<int64_t>(sys.nnz, 1));
-  sys.cbase = ctx.ws.get<int32_t>("sys.cbase", std::max<int64_t>(NC, 1));
-  if (N > 0) {
-    k_narrow_cols<<<div_up(N, 256), 256, 0, s>>>(N, sys.chart_row, NC, sys.row_ptr, sys.cols, sys.cols16);
-    count_launches(1);
-  }
-  if (NC > 0) {
-    k_chart_base<<<div_up(NC, 256), 256, 0, s>>>(NC, sys.chart_row, sys.cbase);
-    count_launches(1);
-  }
-  RUV_LAUNCH_CHECK();
+  narrow_operator(ctx, sys.n_rows, sys.nnz, sys.n_charts, sys.h_chart_row, sys.chart_row, sys.row_ptr, sys.cols,
+                  "sys", &sys.cols16, &sys.cbase);
 }
 
-double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes) {
+double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes,
+                  double* stream_bytes) {
   narrow_columns(ctx, sys);
   Tiles T = upload_tiles(ctx, sys, "bench");
   const Shape sh = pick_shape(ctx, sys);
@@ -1283,7 +1291,10 @@ double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers,
       if (sys.h_chart_row[c + 1] - sys.h_chart_row[c] <= kNarrowRows) narrow_nnz += (double)(rp[c + 1] - rp[c]);
     cb = NNZ > 0 ? (2.0 * narrow_nnz + 4.0 * (NNZ - narrow_nnz)) / NNZ : 4.0;
   }
-  if (bytes) *bytes = NNZ * (vb + cb) + (N + 1.0) * 4.0 + 2.0 * N * nr * vb;
+  // algorithmic bytes: values, 32-bit columns, row pointers, p read once, q written; the
+  // stream bytes count the columns the kernel actually reads (16-bit where narrowed)
+  if (bytes) *bytes = NNZ * (vb + 4.0) + (N + 1.0) * 4.0 + 2.0 * N * nr * vb;
+  if (stream_bytes) *stream_bytes = NNZ * (vb + cb) + (N + 1.0) * 4.0 + 2.0 * N * nr * vb;
   if (T.n == 0) return 0.0;
   if (sys.nrhs == 2)
     return mixed ? dispatch_time<float, 2>(sh, ctx, sys, T, reps, n_buffers)

@@ -77,6 +77,11 @@ void ic0_export(Ctx& ctx, const DevSystem& sys, bool colored, std::vector<int64_
 
 // The 16-bit column stream of `sys` (cols16, cbase), built on the device.
 void narrow_columns(Ctx& ctx, DevSystem& sys);
+// The same for any chart-blocked CSR operator (an AMG level); false (null pointers) when a
+// chart has more than 65536 rows.
+bool narrow_operator(Ctx& ctx, int64_t n, int64_t nnz, int64_t n_charts, const std::vector<int64_t>& h_chart_row,
+                     const int64_t* chart_row, const int32_t* row_ptr, const int32_t* cols, const std::string& tag,
+                     uint16_t** c16, int32_t** cbase);
 
 // x (nrhs * n_rows, device) <- A^-1 b per chart.  Returns per-chart results (host).
 std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o);
@@ -158,7 +163,8 @@ struct Ctx {
 };
 
 // Standalone timing of the batched SpMV kernel on an assembled system (see ruv_bench_spmv).
-double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes);
+double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes,
+                  double* stream_bytes);
 
 struct TuneResult {
   int lpr, unroll, tile_rows;
