@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only. Never linked into, loaded by, or called from the
 // product library (researchuv_gb300 / libruv). Only tests/, __graft_entry__.smoke() and
-// bench.py's cpu_baseline / reference legs use it, and only as the checker.
+// bench.py's cpu_baseline / reference legs use it, and only to check or time against.
 //
 // A CPU restatement of ResearchUV's per-chart LSCM unfold path, written from the
 // reference's Rust source semantics (paths relative to crates/, `researchuv-` dropped):

@@ -1,4 +1,4 @@
-"""ORACLE — test infrastructure only (the checker, never the thing measured or shipped).
+"""ORACLE — test infrastructure only (it checks results; it is never the thing measured or shipped).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline / reference
 legs may import this module.  It wraps ``oracle.cpp`` — a CPU restatement of ResearchUV's

@@ -19,7 +19,7 @@
 // the SpMV, preconditioner and CG recurrence in FP32 and keeps an extended-precision
 // solution accumulator and true residual r = b - A x, recomputed per chart whenever the
 // FP32 residual has dropped by `kDelta` (100x) since the last true residual ("reliable
-// updates"); convergence is judged on the true residual only.  The extended precision is
+// updates"); convergence is decided on the true residual only.  The extended precision is
 // double-float (a value is an unevaluated FP32 pair hi + lo, ~48 significant bits, FP32
 // instructions only: GB300's FP64 pipe is a small fraction of its FP32 rate).  The true
 // residual is formed as r_i = b_i - rs_i x_i - sum_j a_ij (x_j - x_i), rs_i the FP64 row
