@@ -47,10 +47,10 @@ UNIT = "unknowns/s"
 L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (read + write) per algorithmic byte of the batched SpMV kernel, from one ncu
 # capture of its first launch on the 1024-disk operator with the 16-bit column stream
-# (199.0 MB of traffic for 256.9 MB of algorithmic bytes; profiles/kernels_disks1024_dram.md).
+# (198.6 MB of traffic for 256.9 MB of algorithmic bytes; profiles/kernels_disks1024_dram.md).
 # The disk workloads scale by count, so the traffic of a launch on the 4096-disk operator is
 # this ratio times its algorithmic bytes.
-SPMV_DRAM_PER_ALG_BYTE = 0.775
+SPMV_DRAM_PER_ALG_BYTE = 0.773
 
 
 def parse():

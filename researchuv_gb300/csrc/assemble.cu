@@ -193,6 +193,27 @@ __global__ void k_scatter_records(const int32_t* __restrict__ tri_g, const uint8
 
 __device__ __forceinline__ bool rec_less(int2 a, int2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
 
+// Ascending bitonic sorting network over 16 keys held in registers (every index is a
+// compile-time constant once unrolled).  A record (neighbour, corner) packs into one 64-bit
+// key, both fields non-negative, so the key order is rec_less; keys are distinct (a corner
+// appears once), so the result equals the insertion sort's.
+__device__ __forceinline__ void sort16(unsigned long long (&k)[16]) {
+#pragma unroll
+  for (int size = 2; size <= 16; size <<= 1)
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1)
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int l = i ^ stride;
+        if (l > i) {
+          const unsigned long long a = k[i], b = k[l];
+          const bool sw = (i & size) == 0 ? b < a : a < b;
+          k[i] = sw ? b : a;
+          k[l] = sw ? a : b;
+        }
+      }
+}
+
 // One row (free vertex v).  MODE 0: sort the bucket, form each kept edge's coefficient
 // c = w / max(|p_nb - p_v|^2, EPS) once (stored at the neighbour's first record; -1 marks a
 // dropped edge) and count entries; MODE 1: fill from the stored coefficients.
@@ -207,10 +228,21 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
   int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n_verts || pinned[v]) return;
   const int64_t r0 = rec_off[v], r1 = rec_off[v + 1];
-  if (MODE == 0) {  // insertion sort by (neighbour, corner) — buckets hold ~2x valence records
+  if (MODE == 0) {  // sort by (neighbour, corner) — buckets hold ~2x valence records
     constexpr int kLocal = 48;  // sorted in thread-local memory, written back once
     const int64_t nrec = r1 - r0;
-    if (nrec <= kLocal) {
+    if (nrec <= 16) {  // the common case (valence <= 8): a sorting network in registers
+      unsigned long long key[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int2 q = i < nrec ? rec[r0 + i] : make_int2(-1, -1);
+        key[i] = i < nrec ? ((unsigned long long)(uint32_t)q.x << 32) | (uint32_t)q.y : ~0ull;
+      }
+      sort16(key);
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        if (i < nrec) rec[r0 + i] = make_int2((int32_t)(key[i] >> 32), (int32_t)(uint32_t)key[i]);
+    } else if (nrec <= kLocal) {
       int2 b[kLocal];
       for (int64_t i = 0; i < nrec; ++i) {
         const int2 key = rec[r0 + i];
@@ -254,26 +286,31 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
     coef[i] = c;
     return c;
   };
-  // pass A: diagonal (sum of c over kept edges, ascending neighbour) and entry count
+  // pass A (MODE 0): diagonal (sum of c over kept edges, ascending neighbour) and entry
+  // count.  Every kept c is > 0, so a row has a diagonal entry iff that sum is nonzero, and
+  // MODE 1 takes both from the stored diagonal instead of walking the records again.
   double dg = 0.0;
   bool has_diag = false;
-  int32_t n_off = 0;
-  for (int64_t i = r0; i < r1;) {
-    int32_t nb = rec[i].x;
-    int64_t j;
-    const double c = group(i, j);
-    i = j;
-    if (lt0(c)) continue;  // dropped: w <= EPS
-    if (ne0(c)) {  // Sparse::add skips zeros (sparse.rs:47-52)
-      dg = dadd(dg, c);
-      has_diag = true;
-      if (!pinned[nb]) ++n_off;
-    }
-  }
   if (MODE == 0) {
+    int32_t n_off = 0;
+    for (int64_t i = r0; i < r1;) {
+      int32_t nb = rec[i].x;
+      int64_t j;
+      const double c = group(i, j);
+      i = j;
+      if (lt0(c)) continue;  // dropped: w <= EPS
+      if (ne0(c)) {  // Sparse::add skips zeros (sparse.rs:47-52)
+        dg = dadd(dg, c);
+        has_diag = true;
+        if (!pinned[nb]) ++n_off;
+      }
+    }
     row_len[row] = n_off + (has_diag ? 1 : 0);
+    diag_out[row] = dg;
     return;
   }
+  dg = diag_out[row];
+  has_diag = ne0(dg);
   // pass B: entries in column order (diagonal between the lower and upper neighbours) and
   // the right-hand side (pinned neighbours eliminated; mix_b pull term, lscm.rs:630-638)
   int64_t at = row_ptr[row];
@@ -510,9 +547,11 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   }
   const double mix_b = 1.0 - angle_mix;
   int32_t* row_len = ws.get<int32_t>("asm.row_len", NR);
+  sys.diag = ws.get<double>("sys.diag", NR);  // written by the counting pass, read by the fill
   if (NV > 0) {
     k_rows<0><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, bt.p3, bt.p2, bt.pin_uv, mix_b,
-                                             row_len, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, coef);
+                                             row_len, nullptr, nullptr, nullptr, nullptr, sys.diag, nullptr, nullptr,
+                                             coef);
     count_launches(1);
   }
   RUV_LAUNCH_CHECK();
@@ -530,7 +569,6 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   sys.cols = ws.get<int32_t>("sys.cols", NNZ);
   sys.vals = ws.get<double>("sys.vals", NNZ);
   sys.vals32 = ws.get<float>("sys.vals32", NNZ);
-  sys.diag = ws.get<double>("sys.diag", NR);
   sys.b = ws.get<double>("sys.b", 2 * NR);
   bt.row_vert = ws.get<int32_t>("sys.row_vert", NR);
   k_i64_to_i32<<<div_up(NR + 1, B), B, 0, s>>>(rp64, NR + 1, sys.row_ptr);
