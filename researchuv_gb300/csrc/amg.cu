@@ -97,6 +97,13 @@ struct Acc {
   }
 };
 
+// max of v over the active lanes, one atomic per warp (a statistic, read in debug output)
+__device__ __forceinline__ void warp_atomic_max(int* p, int v) {
+  const unsigned m = __activemask();
+  const int w = __reduce_max_sync(m, v);
+  if ((int)(threadIdx.x & 31) == __ffs(m) - 1) atomicMax(p, w);
+}
+
 // ---------------------------------------------------------------- setup kernels
 // Row -> chart and whether the chart keeps coarsening at this level.
 __global__ void k_row_chart(int64_t n, const int64_t* __restrict__ chart_row, int64_t n_charts,
@@ -253,7 +260,7 @@ __global__ void k_propose2(int64_t ng, const int64_t* __restrict__ goff, const i
   if (gmate[g] < 0) {
     Acc<kAccCap> acc;
     group_strengths(g, goff, mem, rp, cols, vals, grp_of, acc, [&](int32_t h) { return gmate[h] < 0; });
-    atomicMax(stats + 2, acc.n);
+    warp_atomic_max(stats + 2, acc.n);
     float mx = 0.0f;
     for (int t = 0; t < acc.n; ++t) mx = fmaxf(mx, acc.val[t]);
     uint32_t bp = 0;
@@ -351,7 +358,7 @@ __global__ void k_prolong(int64_t n, const uint8_t* __restrict__ active, const i
     acc.sort();
   }
   if (acc.overflow) atomicExch(overflow, 1);
-  atomicMax(overflow + 3, acc.n);
+  warp_atomic_max(overflow + 3, acc.n);
   if (MODE == 0) {
     cnt[i] = acc.n;
   } else {

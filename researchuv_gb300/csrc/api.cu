@@ -53,9 +53,9 @@ ruv_status guarded(ruv_ctx* ctx, F&& body) {
 }
 
 template <class T>
-T* upload(Ctx& c, const std::string& name, const T* host, int64_t n) {
+T* upload(Ctx& c, const std::string& name, const T* host, int64_t n, cudaStream_t st = nullptr) {
   T* d = c.ws.get<T>(name, n);
-  if (n > 0) RUV_CUDA(cudaMemcpyAsync(d, host, sizeof(T) * n, cudaMemcpyHostToDevice, c.stream));
+  if (n > 0) RUV_CUDA(cudaMemcpyAsync(d, host, sizeof(T) * n, cudaMemcpyHostToDevice, st ? st : c.stream));
   return d;
 }
 
@@ -109,6 +109,14 @@ ruv_status ruv_ctx_create(ruv_ctx** out, int32_t device) {
   if (const char* e = std::getenv("RUV_TILE_ROWS")) ctx->c.tile_rows = std::max(32, std::atoi(e));
   if (cudaSetDevice(device) != cudaSuccess) return RUV_ERR_NO_DEVICE;
   if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) return RUV_ERR_LAUNCH;
+  if (cudaStreamCreateWithFlags(&ctx->c.side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->c.ev_core, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->c.ev_rest, cudaEventDisableTiming) != cudaSuccess) {
+    cudaStreamDestroy(ctx->c.stream);
+    if (ctx->c.side) cudaStreamDestroy(ctx->c.side);
+    if (ctx->c.ev_core) cudaEventDestroy(ctx->c.ev_core);
+    return RUV_ERR_LAUNCH;
+  }
   *out = ctx.release();
   return RUV_OK;
 }
@@ -117,8 +125,12 @@ void ruv_ctx_destroy(ruv_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->c.device);
   cudaStreamSynchronize(ctx->c.stream);
+  cudaStreamSynchronize(ctx->c.side);
   ctx->c.ws.release();
   cudaStreamDestroy(ctx->c.stream);
+  cudaStreamDestroy(ctx->c.side);
+  cudaEventDestroy(ctx->c.ev_core);
+  cudaEventDestroy(ctx->c.ev_rest);
   delete ctx;
 }
 
@@ -254,7 +266,18 @@ ruv_status ruv_ic0_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const
   });
 }
 
-ruv_status ruv_lscm_upload(ruv_ctx* ctx, const ruv_lscm_batch* in) {
+namespace {
+// The batch upload.  With `overlap` (the one-call solve) the arrays the assembly reads only
+// after its cotangent pass (pin flags, pin targets, tangent-frame positions) are copied on
+// the side stream once the others are in, so those copies run under the first kernels;
+// bt.rest_ready orders them before their first use.
+ruv_status upload_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, bool overlap);
+}  // namespace
+
+ruv_status ruv_lscm_upload(ruv_ctx* ctx, const ruv_lscm_batch* in) { return upload_batch(ctx, in, false); }
+
+namespace {
+ruv_status upload_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, bool overlap) {
   if (!ctx || !in) return RUV_ERR_BAD_INPUT;
   return guarded(ctx, [&]() -> ruv_status {
     const int64_t NC = in->n_charts;
@@ -280,13 +303,30 @@ ruv_status ruv_lscm_upload(ruv_ctx* ctx, const ruv_lscm_batch* in) {
     bt.tri_off = upload(c, "in.tri_off", in->tri_off, NC + 1);
     bt.p3 = upload(c, "in.p3", in->p3, 3 * NV);
     bt.tris = upload(c, "in.tris", in->tris, 3 * NT);
-    bt.pinned = upload(c, "in.pinned", in->pinned, NV);
-    bt.pin_uv = upload(c, "in.pin_uv", in->pin_uv, 2 * NV);
-    bt.p2 = upload(c, "in.p2", in->p2, 2 * NV);
+    cudaStream_t rest = c.stream;
+    if (overlap) {  // after everything already on the main stream, then in parallel with it
+      RUV_CUDA(cudaEventRecord(c.ev_core, c.stream));
+      RUV_CUDA(cudaStreamWaitEvent(c.side, c.ev_core, 0));
+      rest = c.side;
+    }
+    struct RestGuard {  // on every exit: the side-stream copies are ordered by rest_ready
+      Ctx& c;
+      DevBatch& bt;
+      bool on;
+      ~RestGuard() {
+        if (!on) return;
+        cudaEventRecord(c.ev_rest, c.side);
+        bt.rest_ready = c.ev_rest;
+      }
+    } guard{c, bt, overlap};
+    bt.pinned = upload(c, "in.pinned", in->pinned, NV, rest);
+    bt.pin_uv = upload(c, "in.pin_uv", in->pin_uv, 2 * NV, rest);
+    bt.p2 = upload(c, "in.p2", in->p2, 2 * NV, rest);
     c.have_batch = true;
     return RUV_OK;
   });
 }
+}  // namespace
 
 ruv_status ruv_lscm_solve_resident(ruv_ctx* ctx, const ruv_unfold_opts* opts, ruv_chart_stat* stats) {
   if (!ctx) return RUV_ERR_BAD_INPUT;
@@ -374,10 +414,15 @@ ruv_status ruv_lscm_download_uv(ruv_ctx* ctx, double* uv_out) {
 
 ruv_status ruv_lscm_solve_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, const ruv_unfold_opts* opts, double* uv_out,
                                 ruv_chart_stat* stats) {
-  ruv_status s = ruv_lscm_upload(ctx, in);
+  ruv_status s = upload_batch(ctx, in, true);
   if (s != RUV_OK) return s;
-  if (in->vert_off[in->n_charts] > 0 && !uv_out) return fail(ctx, RUV_ERR_BAD_INPUT, "null uv_out");
-  ruv_status solved = ruv_lscm_solve_resident(ctx, opts, stats);
+  ruv_status solved = RUV_OK;
+  if (in->vert_off[in->n_charts] > 0 && !uv_out) solved = fail(ctx, RUV_ERR_BAD_INPUT, "null uv_out");
+  else solved = ruv_lscm_solve_resident(ctx, opts, stats);
+  if (ctx->c.resident.rest_ready) {  // a path that never reached the assembly: order the copies here
+    cudaStreamWaitEvent(ctx->c.stream, ctx->c.resident.rest_ready, 0);
+    ctx->c.resident.rest_ready = nullptr;
+  }
   if (solved != RUV_OK && solved != RUV_ERR_NOT_CONVERGED && solved != RUV_ERR_BREAKDOWN) return solved;
   std::string msg = ctx->c.last_error;
   if (!ctx->c.have_uv) return solved;

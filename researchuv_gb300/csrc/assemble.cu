@@ -501,7 +501,11 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
     count_launches(1);
     RUV_LAUNCH_CHECK();
   }
-  // free-row numbering
+  // free-row numbering (the first use of the pin flags, pin targets and frame positions)
+  if (bt.rest_ready) {
+    RUV_CUDA(cudaStreamWaitEvent(s, bt.rest_ready, 0));
+    bt.rest_ready = nullptr;
+  }
   uint8_t* fr = ws.get<uint8_t>("asm.free", NV);
   bt.row_of = ws.get<int64_t>("asm.row_of", NV + 1);
   if (NV > 0) {

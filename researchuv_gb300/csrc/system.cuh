@@ -96,6 +96,9 @@ struct DevBatch {
   uint8_t* pinned = nullptr;
   double* pin_uv = nullptr;     // 2 * n_verts
   double* p2 = nullptr;         // 2 * n_verts
+  // set when pinned / pin_uv / p2 are still being copied on Ctx::side: the assembly waits
+  // for it before its first use of them
+  cudaEvent_t rest_ready = nullptr;
   // produced by assembly
   int64_t* row_of = nullptr;    // n_verts + 1: exclusive count of free vertices (row id if free)
   int32_t* row_vert = nullptr;  // n_rows: packed vertex of each row
@@ -145,6 +148,10 @@ struct Ctx {
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
+  // a second stream for host-to-device copies that overlap the first assembly kernels, and
+  // the events ordering it against `stream`
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_core = nullptr, ev_rest = nullptr;
   Workspace ws;
   PinnedHost pinned;
   std::string last_error;
