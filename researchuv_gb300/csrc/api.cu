@@ -111,10 +111,12 @@ ruv_status ruv_ctx_create(ruv_ctx** out, int32_t device) {
   if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) return RUV_ERR_LAUNCH;
   if (cudaStreamCreateWithFlags(&ctx->c.side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->c.ev_core, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->c.ev_second, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->c.ev_rest, cudaEventDisableTiming) != cudaSuccess) {
     cudaStreamDestroy(ctx->c.stream);
     if (ctx->c.side) cudaStreamDestroy(ctx->c.side);
     if (ctx->c.ev_core) cudaEventDestroy(ctx->c.ev_core);
+    if (ctx->c.ev_second) cudaEventDestroy(ctx->c.ev_second);
     return RUV_ERR_LAUNCH;
   }
   *out = ctx.release();
@@ -130,6 +132,7 @@ void ruv_ctx_destroy(ruv_ctx* ctx) {
   cudaStreamDestroy(ctx->c.stream);
   cudaStreamDestroy(ctx->c.side);
   cudaEventDestroy(ctx->c.ev_core);
+  cudaEventDestroy(ctx->c.ev_second);
   cudaEventDestroy(ctx->c.ev_rest);
   delete ctx;
 }
@@ -267,10 +270,11 @@ ruv_status ruv_ic0_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const
 }
 
 namespace {
-// The batch upload.  With `overlap` (the one-call solve) the arrays the assembly reads only
-// after its cotangent pass (pin flags, pin targets, tangent-frame positions) are copied on
-// the side stream once the others are in, so those copies run under the first kernels;
-// bt.rest_ready orders them before their first use.
+// The batch upload.  With `overlap` (the one-call solve) only the triangles and positions of
+// the charts holding the first half of the triangles go on the main stream; the other half
+// and then the arrays the assembly reads only after its cotangent pass (pin flags, pin
+// targets, tangent-frame positions) follow on the side stream, under the first kernels.
+// bt.second_ready and bt.rest_ready order them before their first use.
 ruv_status upload_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, bool overlap);
 }  // namespace
 
@@ -301,24 +305,48 @@ ruv_status upload_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, bool overlap) {
     bt.h_tri_off.assign(in->tri_off, in->tri_off + NC + 1);
     bt.vert_off = upload(c, "in.vert_off", in->vert_off, NC + 1);
     bt.tri_off = upload(c, "in.tri_off", in->tri_off, NC + 1);
-    bt.p3 = upload(c, "in.p3", in->p3, 3 * NV);
-    bt.tris = upload(c, "in.tris", in->tris, 3 * NT);
+    // the split: the first chart boundary at or past half of the triangles
+    const int64_t cs = overlap && NC > 1
+                           ? std::min<int64_t>(NC - 1, (int64_t)(std::lower_bound(in->tri_off, in->tri_off + NC + 1,
+                                                                                  NT / 2) - in->tri_off))
+                           : NC;
+    const int64_t vs = in->vert_off[cs], ts = in->tri_off[cs];
+    bt.p3 = c.ws.get<double>("in.p3", 3 * NV);
+    bt.tris = c.ws.get<int32_t>("in.tris", 3 * NT);
+    if (vs > 0) RUV_CUDA(cudaMemcpyAsync(bt.p3, in->p3, sizeof(double) * 3 * vs, cudaMemcpyHostToDevice, c.stream));
+    if (ts > 0) RUV_CUDA(cudaMemcpyAsync(bt.tris, in->tris, sizeof(int32_t) * 3 * ts, cudaMemcpyHostToDevice, c.stream));
     cudaStream_t rest = c.stream;
     if (overlap) {  // after everything already on the main stream, then in parallel with it
       RUV_CUDA(cudaEventRecord(c.ev_core, c.stream));
       RUV_CUDA(cudaStreamWaitEvent(c.side, c.ev_core, 0));
       rest = c.side;
     }
-    struct RestGuard {  // on every exit: the side-stream copies are ordered by rest_ready
+    struct SideGuard {  // on every exit: the side-stream copies are ordered by the events
       Ctx& c;
       DevBatch& bt;
-      bool on;
-      ~RestGuard() {
+      bool on, second;
+      ~SideGuard() {
         if (!on) return;
+        if (!second) {  // (an exit before the second half was enqueued)
+          cudaEventRecord(c.ev_second, c.side);
+          bt.second_ready = c.ev_second;
+        }
         cudaEventRecord(c.ev_rest, c.side);
         bt.rest_ready = c.ev_rest;
       }
-    } guard{c, bt, overlap};
+    } guard{c, bt, overlap, false};
+    if (NV > vs)
+      RUV_CUDA(cudaMemcpyAsync(bt.p3 + 3 * vs, in->p3 + 3 * vs, sizeof(double) * 3 * (NV - vs), cudaMemcpyHostToDevice,
+                               rest));
+    if (NT > ts)
+      RUV_CUDA(cudaMemcpyAsync(bt.tris + 3 * ts, in->tris + 3 * ts, sizeof(int32_t) * 3 * (NT - ts),
+                               cudaMemcpyHostToDevice, rest));
+    if (overlap) {
+      RUV_CUDA(cudaEventRecord(c.ev_second, c.side));
+      bt.second_ready = c.ev_second;
+      bt.split_tri = ts;
+      guard.second = true;
+    }
     bt.pinned = upload(c, "in.pinned", in->pinned, NV, rest);
     bt.pin_uv = upload(c, "in.pin_uv", in->pin_uv, 2 * NV, rest);
     bt.p2 = upload(c, "in.p2", in->p2, 2 * NV, rest);
@@ -419,10 +447,11 @@ ruv_status ruv_lscm_solve_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, const ru
   ruv_status solved = RUV_OK;
   if (in->vert_off[in->n_charts] > 0 && !uv_out) solved = fail(ctx, RUV_ERR_BAD_INPUT, "null uv_out");
   else solved = ruv_lscm_solve_resident(ctx, opts, stats);
-  if (ctx->c.resident.rest_ready) {  // a path that never reached the assembly: order the copies here
-    cudaStreamWaitEvent(ctx->c.stream, ctx->c.resident.rest_ready, 0);
-    ctx->c.resident.rest_ready = nullptr;
-  }
+  for (cudaEvent_t* e : {&ctx->c.resident.second_ready, &ctx->c.resident.rest_ready})
+    if (*e) {  // a path that never reached the assembly: order the copies here
+      cudaStreamWaitEvent(ctx->c.stream, *e, 0);
+      *e = nullptr;
+    }
   if (solved != RUV_OK && solved != RUV_ERR_NOT_CONVERGED && solved != RUV_ERR_BREAKDOWN) return solved;
   std::string msg = ctx->c.last_error;
   if (!ctx->c.have_uv) return solved;

@@ -101,10 +101,10 @@ __device__ __forceinline__ int64_t find_chart(const int64_t* off, int64_t n_char
 
 // chart-local triangle indices -> packed vertex ids (validated)
 __global__ void k_globalize(const int32_t* __restrict__ tris, const int64_t* __restrict__ tri_off,
-                            const int64_t* __restrict__ vert_off, int64_t n_charts, int64_t n_tris,
-                            int32_t* __restrict__ tri_g, int* __restrict__ bad) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_tris) return;
+                            const int64_t* __restrict__ vert_off, int64_t n_charts, int64_t t_begin,
+                            int64_t t_end, int32_t* __restrict__ tri_g, int* __restrict__ bad) {
+  int64_t t = t_begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= t_end) return;
   int64_t c = find_chart(tri_off, n_charts, t);
   int64_t v0 = vert_off[c], nv = vert_off[c + 1] - v0;
   int32_t a = tris[3 * t], b = tris[3 * t + 1], d = tris[3 * t + 2];
@@ -119,10 +119,10 @@ __global__ void k_globalize(const int32_t* __restrict__ tris, const int64_t* __r
 
 // Clamped cotangent at each triangle corner m (angle at t[m], opposite edge t[m+1]-t[m+2]),
 // lscm.rs:256-268; 0.0 where the reference skips the corner (degenerate guard).
-__global__ void k_corner_cot(const double* __restrict__ p3, const int32_t* __restrict__ tri_g, int64_t n_tris,
-                             double* __restrict__ cot) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_tris) return;
+__global__ void k_corner_cot(const double* __restrict__ p3, const int32_t* __restrict__ tri_g, int64_t t_begin,
+                             int64_t t_end, double* __restrict__ cot) {
+  int64_t t = t_begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= t_end) return;
   int32_t v[3] = {tri_g[3 * t], tri_g[3 * t + 1], tri_g[3 * t + 2]};
   P3 p[3] = {ld3(p3, v[0]), ld3(p3, v[1]), ld3(p3, v[2])};
   // edge vectors e_k = p[k+1] - p[k] and their lengths, each once: the corner vectors are
@@ -493,11 +493,20 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   double* cot = ws.get<double>("asm.cot", 3 * NT);
   bt.tri_g = tri_g;
   bt.cot = cot;
-  if (NT > 0) {
-    k_globalize<<<div_up(NT, B), B, 0, s>>>(bt.tris, bt.tri_off, bt.vert_off, NC, NT, tri_g, bad);
+  // triangles [0, split) first; with a split upload the rest of the triangles and positions
+  // are still being copied on the side stream until bt.second_ready
+  const int64_t split = bt.second_ready ? std::min<int64_t>(std::max<int64_t>(bt.split_tri, 0), NT) : NT;
+  for (int part = 0; part < 2; ++part) {
+    const int64_t t0 = part == 0 ? 0 : split, t1 = part == 0 ? split : NT;
+    if (part == 1 && bt.second_ready) {
+      RUV_CUDA(cudaStreamWaitEvent(s, bt.second_ready, 0));
+      bt.second_ready = nullptr;
+    }
+    if (t1 <= t0) continue;
+    k_globalize<<<div_up(t1 - t0, B), B, 0, s>>>(bt.tris, bt.tri_off, bt.vert_off, NC, t0, t1, tri_g, bad);
     count_launches(1);
     RUV_LAUNCH_CHECK();
-    k_corner_cot<<<div_up(NT, B), B, 0, s>>>(bt.p3, tri_g, NT, cot);
+    k_corner_cot<<<div_up(t1 - t0, B), B, 0, s>>>(bt.p3, tri_g, t0, t1, cot);
     count_launches(1);
     RUV_LAUNCH_CHECK();
   }

@@ -99,6 +99,10 @@ struct DevBatch {
   // set when pinned / pin_uv / p2 are still being copied on Ctx::side: the assembly waits
   // for it before its first use of them
   cudaEvent_t rest_ready = nullptr;
+  // set when the triangles from split_tri on (and their charts' positions) are still being
+  // copied on Ctx::side: the assembly's first passes run on [0, split_tri) meanwhile
+  cudaEvent_t second_ready = nullptr;
+  int64_t split_tri = 0;
   // produced by assembly
   int64_t* row_of = nullptr;    // n_verts + 1: exclusive count of free vertices (row id if free)
   int32_t* row_vert = nullptr;  // n_rows: packed vertex of each row
@@ -151,7 +155,7 @@ struct Ctx {
   // a second stream for host-to-device copies that overlap the first assembly kernels, and
   // the events ordering it against `stream`
   cudaStream_t side = nullptr;
-  cudaEvent_t ev_core = nullptr, ev_rest = nullptr;
+  cudaEvent_t ev_core = nullptr, ev_second = nullptr, ev_rest = nullptr;
   Workspace ws;
   PinnedHost pinned;
   std::string last_error;
