@@ -546,7 +546,8 @@ def main():
                    "spmv_shape": {"lanes_per_row": tuned[0], "rows_in_flight": tuned[1], "tile_rows": tuned[2]},
                    "charts_not_ok": int((statuses != 0).sum())},
         "e2e": {"value": world * unknowns / (ems / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": ems},
+                "d2h_bytes_per_step": d2h, "ms_per_step": ems,
+                "ms_median": statistics.median(e2e_ms), "ms_min": min(e2e_ms)},
         "roofline": {"bound": "hbm", "kernel": "k_spmv_pq (batched CSR-vector SpMV + p.q)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src,
