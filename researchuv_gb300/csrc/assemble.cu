@@ -14,6 +14,7 @@
 // triangle order; diagonal and right-hand side: ascending neighbour id), so the CSR
 // pattern, values and right-hand side are bit-identical to the reference's
 // Sparse::to_csr(2 nf) (sparse.rs:69-84) of the same chart.
+#include <cstdlib>
 #include <functional>
 
 #include "fp64rn.cuh"
@@ -224,7 +225,7 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
                        double mix_b, int32_t* __restrict__ row_len, const int64_t* __restrict__ row_ptr,
                        int32_t* __restrict__ cols, double* __restrict__ vals, float* __restrict__ vals32,
                        double* __restrict__ diag_out, double* __restrict__ b, int32_t* __restrict__ row_vert,
-                       double* __restrict__ coef) {
+                       double* __restrict__ coef, float* __restrict__ vals_lo, float2* __restrict__ rsum) {
   int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n_verts || pinned[v]) return;
   const int64_t r0 = rec_off[v], r1 = rec_off[v + 1];
@@ -315,6 +316,20 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
   // the right-hand side (pinned neighbours eliminated; mix_b pull term, lscm.rs:630-638)
   int64_t at = row_ptr[row];
   bool diag_done = !has_diag;
+  // one entry, in storage order; with vals_lo / rsum also the mixed solver's low FP32 halves
+  // and the FP64 row sum as a double-float pair (the rounding split_f64 does, so the same bits)
+  double rs = 0.0;
+  auto put = [&](int32_t col, double val) {
+    cols[at] = col;
+    vals[at] = val;
+    const float h = f32_rn(val);
+    vals32[at] = h;
+    if (vals_lo) {
+      vals_lo[at] = f32_rn(dsub(val, (double)h));
+      rs = dadd(rs, val);
+    }
+    ++at;
+  };
   double bu = 0.0, bv = 0.0;
   const double p2u = p2[2 * v], p2v = p2[2 * v + 1];
   for (int64_t i = r0; i < r1;) {
@@ -338,26 +353,20 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
       bv = dadd(bv, dmul(mc, dw));
       if (ne0(c)) {
         if (!diag_done && nb > v) {
-          cols[at] = (int32_t)row;
-          vals[at] = dg;
-          vals32[at] = f32_rn(dg);
-          ++at;
+          put((int32_t)row, dg);
           diag_done = true;
         }
-        cols[at] = (int32_t)row_of[nb];
-        vals[at] = dneg(c);
-        vals32[at] = f32_rn(dneg(c));
-        ++at;
+        put((int32_t)row_of[nb], dneg(c));
       }
     } else {
       bu = dadd(bu, dadd(dmul(mc, du), dmul(c, pin_uv[2 * nb])));
       bv = dadd(bv, dadd(dmul(mc, dw), dmul(c, pin_uv[2 * nb + 1])));
     }
   }
-  if (!diag_done) {
-    cols[at] = (int32_t)row;
-    vals[at] = dg;
-    vals32[at] = f32_rn(dg);
+  if (!diag_done) put((int32_t)row, dg);
+  if (rsum) {
+    const float h = f32_rn(rs);
+    rsum[row] = make_float2(h, f32_rn(dsub(rs, (double)h)));
   }
   diag_out[row] = dg;
   b[2 * row] = bu;
@@ -564,7 +573,7 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   if (NV > 0) {
     k_rows<0><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, bt.p3, bt.p2, bt.pin_uv, mix_b,
                                              row_len, nullptr, nullptr, nullptr, nullptr, sys.diag, nullptr, nullptr,
-                                             coef);
+                                             coef, nullptr, nullptr);
     count_launches(1);
   }
   RUV_LAUNCH_CHECK();
@@ -583,6 +592,11 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   sys.vals = ws.get<double>("sys.vals", NNZ);
   sys.vals32 = ws.get<float>("sys.vals32", NNZ);
   sys.b = ws.get<double>("sys.b", 2 * NR);
+  // the mixed solver's split, formed by the fill (RUV_SPLIT_IN_FILL=0: by the solver instead)
+  const char* split_env = std::getenv("RUV_SPLIT_IN_FILL");
+  const bool split_in_fill = !(split_env && split_env[0] == '0');
+  sys.vals_lo = split_in_fill ? ws.get<float>("asm.vals_lo", NNZ) : nullptr;
+  sys.rsum = split_in_fill ? ws.get<float2>("asm.rsum", NR) : nullptr;
   bt.row_vert = ws.get<int32_t>("sys.row_vert", NR);
   k_i64_to_i32<<<div_up(NR + 1, B), B, 0, s>>>(rp64, NR + 1, sys.row_ptr);
   count_launches(1);
@@ -590,7 +604,7 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   if (NV > 0) {
     k_rows<1><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, bt.p3, bt.p2, bt.pin_uv, mix_b,
                                              nullptr, rp64, sys.cols, sys.vals, sys.vals32, sys.diag, sys.b,
-                                             bt.row_vert, coef);
+                                             bt.row_vert, coef, sys.vals_lo, sys.rsum);
     count_launches(1);
   }
   RUV_LAUNCH_CHECK();

@@ -840,6 +840,11 @@ MixedExtras mixed_extras(Ctx& ctx, DevSystem& sys, int nr) {
   const int64_t N = sys.n_rows;
   m.xdf = ctx.ws.get<float>("pcg.xdf", 2 * nr * N);
   m.bdf = ctx.ws.get<float>("pcg.bdf", 2 * nr * N);
+  if (sys.vals_lo && sys.rsum) {  // formed by the assembly's fill pass
+    m.vals_lo = sys.vals_lo;
+    m.rsum = sys.rsum;
+    return m;
+  }
   m.vals_lo = ctx.ws.get<float>("pcg.vals_lo", sys.nnz);
   m.rsum = ctx.ws.get<float2>("pcg.rsum", N);
   if (N > 0) {
@@ -1129,9 +1134,12 @@ Tiles upload_tiles(Ctx& ctx, const DevSystem& sys, const std::string& tag) {
 // SpMV shape: explicit (RUV_LPR / RUV_UNROLL via the context) or from the row-length
 // profile: enough lanes to cover a typical row once, then as many rows in flight as keep
 // 8 independent loads per lane.
+// The launch shape without the autotuner: for mesh Laplacians (at most 8 entries per row) two
+// lanes per row and two rows in flight, which the autotuner picked on every such operator
+// measured (4096 disks, 1024^2 and 2048^2 height fields); wider sub-warps for denser rows.
 Shape pick_shape(const Ctx& ctx, const DevSystem& sys) {
   double avg = sys.n_rows > 0 ? (double)sys.nnz / (double)sys.n_rows : 1.0;
-  int lpr = ctx.lanes_per_row > 0 ? ctx.lanes_per_row : (avg <= 5 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32);
+  int lpr = ctx.lanes_per_row > 0 ? ctx.lanes_per_row : (avg <= 8 ? 2 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32);
   int u = ctx.unroll > 0 ? ctx.unroll : (lpr <= 4 ? 2 : lpr == 8 ? 4 : 1);
   return Shape{lpr, u};
 }

@@ -27,6 +27,10 @@ struct DevSystem {
   int32_t* cbase = nullptr;      // n_charts: first row of a chart with cols16, -1 otherwise
   double* diag = nullptr;        // n_rows
   double* b = nullptr;           // nrhs * n_rows
+  // the mixed solver's low FP32 halves of vals and FP64 row sums as double-float pairs, when
+  // the assembly formed them (else the solver forms them)
+  float* vals_lo = nullptr;      // nnz
+  float2* rsum = nullptr;        // n_rows
 };
 
 // Solver controls and per-chart outcome.
@@ -164,7 +168,7 @@ struct Ctx {
   bool have_last = false;
   int lanes_per_row = 0;   // SpMV sub-warp width (0 = from the row-length profile)
   int unroll = 0;          // SpMV rows in flight per sub-warp (0 = from the shape)
-  int tile_rows = 256;     // rows per CTA tile
+  int tile_rows = 512;     // rows per CTA tile (the autotuner's pick on the height fields)
   // the batch resident on the device (ruv_lscm_upload)
   DevBatch resident;
   bool have_batch = false;

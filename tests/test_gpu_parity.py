@@ -219,15 +219,34 @@ def test_cg_amg_poisson_and_elongated(known):
 
 
 def test_batched_disks_16bit_columns(monkeypatch):
-    """The 16-bit column stream (RUV_NARROW_COLS=1) gives bitwise the same UVs as the 32-bit one."""
+    """The 16-bit column streams (the default; RUV_NARROW_COLS=0 turns them off) give bitwise
+    the same UVs as 32-bit columns, for the CG operator and for every AMG level."""
     vo, to, p3, tr = W.disks(16, t_min=200, t_max=6000, seed=17)
     C = R.prepare_patches(vo, to, p3, tr)
     ctx = R.Context(0)
-    for pc in (R.Precond.JACOBI, R.Precond.AMG):
-        monkeypatch.delenv("RUV_NARROW_COLS", raising=False)
+    for pc in (R.Precond.JACOBI, R.Precond.AMG, R.Precond.AMG_SA):
+        monkeypatch.setenv("RUV_NARROW_COLS", "0")
         wide = R.unfold_charts(ctx, C, R.UnfoldOptions(precond=pc))
-        monkeypatch.setenv("RUV_NARROW_COLS", "1")
+        monkeypatch.delenv("RUV_NARROW_COLS", raising=False)
         narrow = R.unfold_charts(ctx, C, R.UnfoldOptions(precond=pc))
         for a, b in zip(wide, narrow):
+            assert a.status == b.status == R.Status.OK
+            assert np.array_equal(a.uv, b.uv)
+
+
+def test_mixed_split_formed_in_fill(monkeypatch):
+    """The assembly's fill pass forms the mixed solver's low FP32 halves and double-float row
+    sums with the solver's own rounding: bitwise the same UVs as when the solver forms them
+    (RUV_SPLIT_IN_FILL=0)."""
+    vo, to, p3, tr = W.disks(16, t_min=200, t_max=6000, seed=19)
+    C = R.prepare_patches(vo, to, p3, tr)
+    ctx = R.Context(0)
+    for pc in (R.Precond.JACOBI, R.Precond.AMG_SA):
+        opts = R.UnfoldOptions(precond=pc, precision=R.Precision.MIXED)
+        monkeypatch.setenv("RUV_SPLIT_IN_FILL", "0")
+        solver = R.unfold_charts(ctx, C, opts)
+        monkeypatch.delenv("RUV_SPLIT_IN_FILL", raising=False)
+        fill = R.unfold_charts(ctx, C, opts)
+        for a, b in zip(solver, fill):
             assert a.status == b.status == R.Status.OK
             assert np.array_equal(a.uv, b.uv)
