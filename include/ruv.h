@@ -93,6 +93,20 @@ ruv_status ruv_apply_ic0(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const 
  * nonzeros, *levels_out the dependency-level count (the larger of the two sweeps),
  * *colours_out the colour count (0 without colouring).  BAD_INPUT when nnz exceeds cap
  * (counts are still written); BREAKDOWN where factor_ic0 returns None. */
+/* One level of the aggregation AMG hierarchy the preconditioner builds for A (smoothed != 0:
+ * AMG-SA, else plain aggregation), copied out for inspection: what the reference's own AMG
+ * tests read from its hierarchy (gpu/src/amg.rs:800-942).  sizes[6] receives the level count,
+ * whether this level's prolongator is smoothed, the level's rows, the next level's rows (0 on
+ * the last level), and the nonzeros of the level operator and of its prolongator.  With
+ * cap > 0 the arrays (capacity cap each, cap >= rows + 1) receive the level operator in FP64
+ * CSR (a_ptr, a_cols, a_vals), the prolongator to the next level (p_ptr, p_cols, p_vals; rows
+ * of this level, columns of the next) and the aggregate of each row (-1 on the last level).
+ * BAD_INPUT for a level out of range or a capacity too small (sizes are still written). */
+ruv_status ruv_amg_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols,
+                          const double* vals, int32_t smoothed, int32_t level, int64_t cap, int64_t* sizes,
+                          int64_t* a_ptr, int32_t* a_cols, double* a_vals, int64_t* p_ptr, int32_t* p_cols,
+                          float* p_vals, int32_t* agg);
+
 ruv_status ruv_ic0_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols,
                           const double* vals, int32_t colored, int64_t cap, int64_t* l_ptr,
                           int32_t* l_cols, double* l_vals, int32_t* to_orig, int64_t* nnz_out,

@@ -62,6 +62,9 @@ SIGNATURES = {
     "ruv_apply_ic0": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _P(_f64), _P(_f64)]),
     "ruv_ic0_export": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _i32, _i64, _P(_i64), _P(_i32),
                                       _P(_f64), _P(_i32), _P(_i64), _P(_i32), _P(_i32)]),
+    "ruv_amg_export": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _i32, _i32, _i64, _P(_i64),
+                                      _P(_i64), _P(_i32), _P(_f64), _P(_i64), _P(_i32), _P(ctypes.c_float),
+                                      _P(_i32)]),
     "ruv_unfold_opts_default": (None, [_P(RuvUnfoldOpts)]),
     "ruv_lscm_solve_batch": (ctypes.c_int, [_vp, _P(RuvBatch), _P(RuvUnfoldOpts), _P(_f64), _P(RuvChartStat)]),
     "ruv_prepare_mesh": (ctypes.c_int, [_P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _i32, _P(_vp)]),
@@ -290,6 +293,27 @@ class GpuSolver:
         k = nnz.value
         return {"ptr": ptr, "cols": cols[:k], "vals": vals[:k], "to_orig": perm, "levels": lev.value,
                 "colours": col.value}
+
+    def amg_level(self, a: CsrMatrix, level: int, smoothed: bool = True) -> dict:
+        """Level ``level`` of the device AMG hierarchy of ``a`` (AMG-SA when ``smoothed``): the
+        level operator (FP64 CSR), the prolongator to the next level and the aggregates."""
+        n = a.rows()
+        sizes = np.zeros(6, np.int64)
+        args = (self.ctx.h, n, _ptr(a.row_ptr, _i32), _ptr(a.cols, _i32), _ptr(a.vals, _f64), 1 if smoothed else 0,
+                int(level))
+        nul = (None,) * 7
+        self.ctx.check(lib().ruv_amg_export(*args, 0, _ptr(sizes, _i64), *nul), "ruv_amg_export")
+        levels, sm, rows, nxt, annz, pnnz = (int(x) for x in sizes)
+        cap = max(rows + 1, annz, pnnz, 1)
+        ap, ac, av = np.zeros(cap, np.int64), np.zeros(cap, np.int32), np.zeros(cap, np.float64)
+        pp, pc, pv = np.zeros(cap, np.int64), np.zeros(cap, np.int32), np.zeros(cap, np.float32)
+        ag = np.zeros(cap, np.int32)
+        self.ctx.check(lib().ruv_amg_export(*args, cap, _ptr(sizes, _i64), _ptr(ap, _i64), _ptr(ac, _i32),
+                                            _ptr(av, _f64), _ptr(pp, _i64), _ptr(pc, _i32),
+                                            _ptr(pv, ctypes.c_float), _ptr(ag, _i32)), "ruv_amg_export")
+        return {"levels": levels, "smoothed": bool(sm), "rows": rows, "next_rows": nxt,
+                "A": (ap[:rows + 1], ac[:annz], av[:annz]), "P": (pp[:rows + 1], pc[:pnnz], pv[:pnnz]),
+                "agg": ag[:rows]}
 
 
 # ------------------------------------------------------------------ unfold driver

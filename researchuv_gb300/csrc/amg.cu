@@ -1581,6 +1581,46 @@ void amg_free(AmgHierarchy* H) { delete H; }
 
 int amg_levels(const AmgHierarchy* H) { return (int)H->lv.size(); }
 
+void amg_export_level(Ctx& ctx, const DevSystem& sys, bool smooth, int level, AmgLevelHost& out) {
+  struct Free {
+    void operator()(AmgHierarchy* h) const { amg_free(h); }
+  };
+  std::string info;
+  std::unique_ptr<AmgHierarchy, Free> H(amg_setup(ctx, sys, smooth, info));
+  const int K = (int)H->lv.size();
+  out = AmgLevelHost();
+  out.n_levels = K;
+  if (level < 0 || level >= K) throw Error{RUV_ERR_BAD_INPUT, "level out of range"};
+  const AmgLevelDev& L = H->lv[level];
+  cudaStream_t s = ctx.stream;
+  out.n = L.n;
+  out.nnz = L.nnz;
+  out.rp.resize(L.n + 1);
+  out.cols.resize(L.nnz);
+  out.vals.resize(L.nnz);
+  RUV_CUDA(cudaMemcpyAsync(out.rp.data(), L.rp, sizeof(int32_t) * (L.n + 1), cudaMemcpyDeviceToHost, s));
+  if (L.nnz > 0) {
+    RUV_CUDA(cudaMemcpyAsync(out.cols.data(), L.cols, sizeof(int32_t) * L.nnz, cudaMemcpyDeviceToHost, s));
+    RUV_CUDA(cudaMemcpyAsync(out.vals.data(), L.vals64, sizeof(double) * L.nnz, cudaMemcpyDeviceToHost, s));
+  }
+  if (level + 1 < K && L.poff && L.agg) {
+    out.smoothed = L.smoothed;
+    out.n_next = H->lv[level + 1].n;
+    out.pnnz = L.n_pnnz;
+    out.poff.resize(L.n + 1);
+    out.pc.resize(L.n_pnnz);
+    out.pv.resize(L.n_pnnz);
+    out.agg.resize(L.n);
+    RUV_CUDA(cudaMemcpyAsync(out.poff.data(), L.poff, sizeof(int64_t) * (L.n + 1), cudaMemcpyDeviceToHost, s));
+    if (L.n_pnnz > 0) {
+      RUV_CUDA(cudaMemcpyAsync(out.pc.data(), L.pc, sizeof(int32_t) * L.n_pnnz, cudaMemcpyDeviceToHost, s));
+      RUV_CUDA(cudaMemcpyAsync(out.pv.data(), L.pv, sizeof(float) * L.n_pnnz, cudaMemcpyDeviceToHost, s));
+    }
+    if (L.n > 0) RUV_CUDA(cudaMemcpyAsync(out.agg.data(), L.agg, sizeof(int32_t) * L.n, cudaMemcpyDeviceToHost, s));
+  }
+  RUV_CUDA(cudaStreamSynchronize(s));
+}
+
 // Bind the level-0 right-hand side / output vectors (the CG's r and z) before capture.
 void amg_bind(Ctx& ctx, AmgHierarchy* H, float* r0, float* z0) {
   const int K = (int)H->lv.size();

@@ -269,6 +269,45 @@ ruv_status ruv_ic0_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const
   });
 }
 
+ruv_status ruv_amg_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                          int32_t smoothed, int32_t level, int64_t cap, int64_t* sizes, int64_t* a_ptr, int32_t* a_cols,
+                          double* a_vals, int64_t* p_ptr, int32_t* p_cols, float* p_vals, int32_t* agg) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  return guarded(ctx, [&]() -> ruv_status {
+    if (!sizes || cap < 0) return fail(ctx, RUV_ERR_BAD_INPUT, "null sizes or negative capacity");
+    if (cap > 0 && (!a_ptr || !a_cols || !a_vals || !p_ptr || !p_cols || !p_vals || !agg))
+      return fail(ctx, RUV_ERR_BAD_INPUT, "null output buffer");
+    Ctx& c = ctx->c;
+    DevSystem sys;
+    std::vector<double> diag, zero(n > 0 ? n : 0, 0.0);
+    const ruv_status hs = host_system(ctx, n, row_ptr, cols, vals, zero.data(), sys, diag);
+    if (hs != RUV_OK) return hs;
+    AmgLevelHost h;
+    amg_export_level(c, sys, smoothed != 0, level, h);
+    sizes[0] = h.n_levels;
+    sizes[1] = h.smoothed ? 1 : 0;
+    sizes[2] = h.n;
+    sizes[3] = h.n_next;
+    sizes[4] = h.nnz;
+    sizes[5] = h.pnnz;
+    if (cap == 0) return RUV_OK;
+    if (std::max({h.n + 1, h.nnz, h.pnnz}) > cap) return fail(ctx, RUV_ERR_BAD_INPUT, "level larger than the output capacity");
+    for (int64_t i = 0; i <= h.n; ++i) a_ptr[i] = h.rp[i];
+    std::copy(h.cols.begin(), h.cols.end(), a_cols);
+    std::copy(h.vals.begin(), h.vals.end(), a_vals);
+    if (h.n_next > 0) {
+      std::copy(h.poff.begin(), h.poff.end(), p_ptr);
+      std::copy(h.pc.begin(), h.pc.end(), p_cols);
+      std::copy(h.pv.begin(), h.pv.end(), p_vals);
+      std::copy(h.agg.begin(), h.agg.end(), agg);
+    } else {
+      std::fill(p_ptr, p_ptr + h.n + 1, 0);
+      std::fill(agg, agg + h.n, -1);
+    }
+    return RUV_OK;
+  });
+}
+
 namespace {
 // The batch upload.  With `overlap` (the one-call solve) only the triangles and positions of
 // the charts holding the first half of the triangles go on the main stream; the other half

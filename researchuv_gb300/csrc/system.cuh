@@ -67,6 +67,19 @@ struct AmgHierarchy;
 AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string& info);
 void amg_free(AmgHierarchy* H);
 int amg_levels(const AmgHierarchy* H);
+// One level of the hierarchy amg_setup builds for `sys`, copied to the host: its operator
+// (FP64), and when a coarser level follows, the prolongator to it and the aggregate of each row.
+struct AmgLevelHost {
+  int n_levels = 0;
+  bool smoothed = false;  // this level's prolongator is smoothed
+  int64_t n = 0, nnz = 0, n_next = 0, pnnz = 0;
+  std::vector<int32_t> rp, cols;
+  std::vector<double> vals;
+  std::vector<int64_t> poff;
+  std::vector<int32_t> pc, agg;
+  std::vector<float> pv;
+};
+void amg_export_level(Ctx& ctx, const DevSystem& sys, bool smooth, int level, AmgLevelHost& out);
 void amg_bind(Ctx& ctx, AmgHierarchy* H, float* r0, float* z0);
 int amg_apply(Ctx& ctx, AmgHierarchy* H, const int32_t* done);
 std::unique_ptr<SepPrecond> make_amg(Ctx& ctx, const DevSystem& sys, bool smooth);
