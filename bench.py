@@ -19,11 +19,20 @@ mixed-precision AMG-PCG over the packed block-diagonal operator to rel-res 1e-12
            the same operator: algorithmic bytes per launch / mean launch time vs the
            measured HBM copy bandwidth.
 * cpu_baseline — the reference CPU algorithm (the oracle port of unfold_chart + the BTreeMap
-           sparse LU) on a bounded sample of the same charts, 1 core; its UVs also give the
-           UV error of the GPU result on those charts (plus FP64 SuperLU on a few large charts).
+           sparse LU) on a bounded size-stratified sample of the same charts, 1 core,
+           extrapolated by chart to the whole workload; its UVs also give the UV error of the
+           GPU result on those charts (plus FP64 SuperLU on the six largest charts).
+* cpu_superlu_whole_workload — every chart through the oracle and FP64 SuperLU, all cores.
 
---impl reference times that CPU port on all host cores (process pool over charts, like the
-reference's par_map) as the reference arm.
+--impl reference runs that CPU port on all host cores for the whole workload (a per-chart
+cost model calibrated on a stratified sample, the reference's par_map schedule; see
+run_reference).  `config` holds only the keys that describe the workload and is the same in
+both arms.
+
+--workload hf1024 / hf2048 (the single-large-chart workloads) add the UV error of every chart
+against FP64 SuperLU; --compare ic0_color,amg solves the resident workload once per named
+preconditioner.  --workload sphere512 is the differentiation workload (gradient against the
+CPU LU adjoint and FP64 central differences on 64 vertices of the full sphere).
 """
 from __future__ import annotations
 
@@ -45,6 +54,7 @@ import numpy as np  # noqa: E402
 METRIC = "batched LSCM unknowns/s at <=1e-6 UV err vs FP64 LU"
 UNIT = "unknowns/s"
 L2_BYTES = 129 * 1024 * 1024
+L2_NOTE = "inputs larger than L2 (operator and vectors of a step ~1 GB or more)"
 # DRAM bytes (read + write) per algorithmic byte of the batched SpMV kernel, from one ncu
 # capture of its first launch on the 1024-disk operator with the 16-bit column stream
 # (198.6 MB of traffic for 256.9 MB of algorithmic bytes; profiles/kernels_disks1024_dram.md).
@@ -68,6 +78,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-single-chart", action="store_true")
     ap.add_argument("--single-chart-sample", type=int, default=192)
+    ap.add_argument("--no-superlu-baseline", action="store_true",
+                    help="skip the whole-workload FP64 SuperLU leg of the disks workloads")
+    ap.add_argument("--compare", default="",
+                    help="comma-separated preconditioners (ic0, ic0_color, amg, amg_sa, jacobi) solved once each "
+                         "on the resident workload after the timed steps, for iterations and time")
     ap.add_argument("--ncu-step", action="store_true",
                     help="for profiler launch lists: upload, one warm-up solve, then one solve of the workload "
                          "(launch shape from RUV_LPR / RUV_UNROLL / RUV_TILE_ROWS); prints the kernel count "
@@ -104,29 +119,59 @@ def allmax(pg, x: float) -> float:
     return float(t.item())
 
 
-def make_workload(name):
-    import researchuv_gb300 as R
+def workload_config(name):
+    """Generate a workload (numpy only, no library call) and its config: the keys that
+    describe the workload, identical in both arms.  Returns (cfg, src)."""
     from researchuv_gb300 import workloads as W
 
-    t0 = time.time()
     if name.startswith("disks"):
         n = int(name[5:])
         vo, to, p3, tr = W.disks(n, 50, 50_000, seed=3)
-        gen = time.time() - t0
-        charts = R.prepare_patches(vo, to, p3, tr)
         cfg = {"workload": f"{n} displaced polar-disk charts, triangles log-uniform [50, 50000], seed 3",
-               "charts": n, "triangles": int(to[-1]), "vertices": int(vo[-1])}
-        src = ("patches", vo, to, p3, tr)
+               "charts": n, "triangles": int(to[-1]), "vertices": int(vo[-1]),
+               "unknowns": W.disk_unknowns(vo, to, tr), "l2": L2_NOTE}
+        return cfg, ("patches", vo, to, p3, tr)
+    n, ns, amp = (1024, 8, 0.15) if name == "hf1024" else (2048, 16, 0.3)
+    p, f = W.height_field(n, ns, amp, seed=2)
+    cfg = {"workload": f"{n}x{n} height field, {ns} sines, amplitude {amp}, seed 2",
+           "triangles": int(f.shape[0]), "vertices": int(p.shape[0]), "l2": L2_NOTE}
+    return cfg, ("mesh", p, f)
+
+
+def prepare(src):
+    """The chart stages on the host (weld + segment + frames + pins), timed."""
+    import researchuv_gb300 as R
+
+    t0 = time.time()
+    if src[0] == "patches":
+        charts = R.prepare_patches(*src[1:])
     else:
-        n, ns, amp = (1024, 8, 0.15) if name == "hf1024" else (2048, 16, 0.3)
-        p, f = W.height_field(n, ns, amp, seed=2)
-        gen = time.time() - t0
-        charts = R.prepare_mesh(p, f)
-        cfg = {"workload": f"{n}x{n} height field, {ns} sines, amplitude {amp}, seed 2",
-               "charts": charts.n_charts, "triangles": int(f.shape[0]), "vertices": int(p.shape[0])}
-        src = ("mesh", p, f)
-    cfg["host_prep_s"] = round(time.time() - t0 - gen, 3)
-    return charts, cfg, src
+        charts = R.prepare_mesh(*src[1:])
+    return charts, round(time.time() - t0, 3)
+
+
+def host_info():
+    """nproc, uname -m and the CPU model of the host the CPU legs run on."""
+    import platform
+
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not model:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    return {"nproc": os.cpu_count(), "uname_m": platform.machine(), "cpu_model": model or "unknown"}
 
 
 class Clocks:
@@ -191,7 +236,7 @@ def peaks():
 # ------------------------------------------------------------------ CPU (oracle) legs
 def _oracle_chart(args):
     """One chart through the reference CPU algorithm (oracle port): weld(0) + segment +
-    unfold_chart with the BTreeMap LU.  Returns (uv, unknowns, seconds)."""
+    unfold_chart with the BTreeMap LU.  Returns (uv, unknowns, seconds, charts found)."""
     p, f = args
     from oracle import oracle as O
 
@@ -202,85 +247,233 @@ def _oracle_chart(args):
     return ch.get("uv"), 2 * int((ch["free_pos"] >= 0).sum()), dt, P.n_charts
 
 
-def _sample(src, budget_unknowns_cap=3000, n_max=400, seed=7):
-    """Chart ids of a bounded sample: charts whose reference LU is feasible (2 nf + 1 <= cap),
-    random order (seeded) so the sample spans the feasible part of the size distribution."""
-    _, vo, to, _, _ = src
-    nv = np.diff(vo)
-    ok = np.nonzero(nv <= budget_unknowns_cap // 2)[0]
-    rng = np.random.Generator(np.random.PCG64(seed))
-    rng.shuffle(ok)
-    return ok[:n_max]
+def _oracle_chart_timed(args):
+    """(chart id, seconds) of one chart through the reference CPU algorithm."""
+    c, p, f = args
+    _, _, dt, _ = _oracle_chart((p, f))
+    return c, dt
 
 
-def cpu_baseline(src, uv_gpu, budget_s):
-    """1-core timing of the oracle port on a bounded sample + UV error of the GPU result."""
+def _superlu_chart(args):
+    """One chart through the oracle's chart stages and the FP64 SuperLU direct solve (the
+    practical CPU direct solve): (chart id, unknowns, seconds, UVs)."""
+    c, p, f = args
     from oracle import oracle as O
 
-    kind, vo, to, p3, tr = src
-    ids = _sample(src)
-    t_total, unk, errs, used = 0.0, 0, [], 0
+    t0 = time.perf_counter()
+    P = O.Pipeline(p, f, weld_tol=0.0, lu_limit=0)
+    uv = P.superlu_uv(0) if P.n_charts == 1 else None
+    dt = time.perf_counter() - t0
+    return c, 2 * int((P.chart(0)["free_pos"] >= 0).sum()), dt, uv
+
+
+def parmap_wall(t, workers):
+    """Wall time of core::exec::par_map (core/src/exec.rs:28-60) over items costing t, in
+    order: contiguous chunks of ceil(n / workers) items, one per worker thread."""
+    t = np.asarray(t, np.float64)
+    if workers <= 1 or len(t) <= 1:
+        return float(t.sum())
+    workers = min(workers, len(t))
+    chunk = -(-len(t) // workers)
+    return float(max(t[i:i + chunk].sum() for i in range(0, len(t), chunk)))
+
+
+def stratified_charts(nv, cap, per_stratum=2, strata=24, seed=13):
+    """Chart ids of a sample stratified by size: `strata` log-spaced vertex-count bins over the
+    whole range, up to `per_stratum` seeded picks from each bin, charts above `cap` vertices
+    left out (the reference LU is Theta(n^2) per chart)."""
+    nv = np.asarray(nv)
+    edges = np.geomspace(nv.min(), nv.max() + 1, strata + 1)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for s in range(strata):
+        idx = np.nonzero((nv >= edges[s]) & (nv < edges[s + 1]) & (nv <= cap))[0]
+        if len(idx):
+            out.extend(int(i) for i in rng.choice(idx, min(per_stratum, len(idx)), replace=False))
+    return sorted(out, key=lambda c: nv[c])
+
+
+class ChartCostModel:
+    """Seconds of the reference CPU algorithm per chart, from timed charts of a stratified
+    sample: each chart costs its nearest timed chart's time (in log vertex count) scaled by
+    (nv / nv_timed)^beta, beta fitted over the timed charts of at least 400 vertices.  Charts
+    larger than the largest timed one scale from the mean of the four largest timed charts
+    with the exponent min(beta, 2): the reference LU's triangular solves are Theta(n^2), and
+    a fit over small charts can be steeper than the large charts' growth (measured on one
+    host: 6k -> 12k vertices grew as n^1.84), so the cap keeps the extrapolation in the CPU's
+    favour."""
+
+    def __init__(self, nv_timed, t_timed):
+        self.nv = np.asarray(nv_timed, np.float64)
+        self.t = np.asarray(t_timed, np.float64)
+        big = self.nv >= 400
+        if big.sum() >= 3:
+            self.beta = float(np.polyfit(np.log(self.nv[big]), np.log(self.t[big]), 1)[0])
+        else:
+            self.beta = 2.0
+        order = np.argsort(self.nv)
+        self.nv, self.t = self.nv[order], self.t[order]
+
+    def __call__(self, nv):
+        nv = np.asarray(nv, np.float64)
+        ln, lt = np.log(self.nv), np.log(nv)
+        near = np.abs(lt[:, None] - ln[None, :]).argmin(1)
+        est = self.t[near] * (nv / self.nv[near]) ** self.beta
+        top = slice(max(0, len(self.nv) - 4), len(self.nv))
+        beyond = nv > self.nv[-1]
+        if beyond.any():
+            b = min(self.beta, 2.0)
+            est[beyond] = np.mean(self.t[top][None, :] * (nv[beyond][:, None] / self.nv[top][None, :]) ** b, 1)
+        return est
+
+
+def _time_charts(pool, src, ids):
+    _, vo, to, p3, tr = src
+    tasks = [(int(c), p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]]) for c in sorted(ids, key=lambda c: -(vo[c + 1] - vo[c]))]
+    out = dict(pool.imap_unordered(_oracle_chart_timed, tasks, chunksize=1))
+    return np.array([out[c] for c in ids])
+
+
+def reference_model(src, cores, cap):
+    """Calibrate the per-chart cost model on `cores` processes: a stratified sample of charts
+    up to `cap` vertices, each timed once through the reference CPU algorithm."""
+    import multiprocessing as mp
+
+    _, vo, to, _, _ = src
+    nv = np.diff(vo)
+    ids = stratified_charts(nv, cap)
+    with mp.get_context("spawn").Pool(cores) as pool:
+        t0 = time.perf_counter()
+        t = _time_charts(pool, src, ids)
+        wall = time.perf_counter() - t0
+    return ChartCostModel(nv[ids], t), ids, t, wall
+
+
+def cpu_baseline(src, uv_gpu, budget_s, unknowns):
+    """1-core baseline: the reference CPU algorithm (oracle port) timed on a stratified sample
+    of charts of at most 1500 vertices (a bounded ~10-30 s of work), extrapolated by chart over
+    the whole workload with the fitted per-chart cost model; its UVs also give the GPU
+    result's error on those charts, plus FP64 SuperLU on the six largest charts."""
+    from oracle import oracle as O
+
+    _, vo, to, p3, tr = src
+    nv = np.diff(vo)
+    ids = stratified_charts(nv, 1500, per_stratum=3)
+    t_used, errs, used, ts = 0.0, [], [], []
     for c in ids:
-        if t_total > budget_s:
+        if t_used > budget_s:
             break
-        uv, u, dt, nch = _oracle_chart((p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]]))
-        t_total += dt
-        unk += u
-        used += 1
+        uv, _, dt, nch = _oracle_chart((p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]]))
+        t_used += dt
+        used.append(c)
+        ts.append(dt)
         if uv is not None and nch == 1:
             errs.append(O.uv_error(uv_gpu[vo[c]:vo[c + 1]], uv))
-    # a few of the largest charts against the FP64 SuperLU oracle
-    big = np.argsort(-np.diff(vo))[:6]
+    model = ChartCostModel(nv[used], ts)
+    total = float(model(nv).sum())
+    big = np.argsort(-nv)[:6]
     for c in big:
         P = O.Pipeline(p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]], weld_tol=0.0, lu_limit=0)
         if P.n_charts == 1:
             errs.append(O.uv_error(uv_gpu[vo[c]:vo[c + 1]], P.superlu_uv(0)))
-    return {"value": unk / max(t_total, 1e-9), "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{used} charts with 2nf+1 <= 3000 (reference LU feasible), {unk} unknowns, "
-                      f"{t_total:.1f} s on 1 core; weld+segment+unfold_chart+BTreeMap LU per chart"}, \
-        (max(errs) if errs else None), len(errs)
+    return {"value": unknowns / total, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{len(used)} charts of <= 1500 vertices, stratified by size over the whole range, "
+                      f"{t_used:.1f} s on 1 core (weld + segment + unfold_chart + BTreeMap LU per chart); "
+                      f"extrapolated by chart to all {len(nv)} charts ({total:.0f} s) with a per-chart cost "
+                      f"~ nv^{model.beta:.2f}",
+            "host": host_info()}, (max(errs) if errs else None), len(errs)
+
+
+def superlu_baseline(src, cores):
+    """The practical FP64 CPU direct solve over the WHOLE workload: every chart through the
+    oracle's chart stages and SuperLU (scipy splu, COLAMD) on the scalar Laplacian with the u
+    and v right-hand sides, one process per core."""
+    import multiprocessing as mp
+
+    _, vo, to, p3, tr = src
+    n = len(vo) - 1
+    order = np.argsort(-np.diff(vo))
+    tasks = [(int(c), p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]]) for c in order]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = list(pool.imap_unordered(_superlu_chart, tasks, chunksize=4))
+        wall = time.perf_counter() - t0
+    unk = sum(r[1] for r in res)
+    cpu_s = sum(r[2] for r in res)
+    return {"value": unk / wall, "unit": UNIT, "cores": cores, "wall_s": round(wall, 2),
+            "cpu_s_sum": round(cpu_s, 2), "single_core_value": unk / cpu_s, "charts": n,
+            "what": "every chart: oracle chart stages + FP64 SuperLU (scipy splu, COLAMD) on the scalar Laplacian, "
+                    "2 right-hand sides; process pool over charts, largest first"}
 
 
 def run_reference(args, rank):
-    """Reference arm: the reference CPU algorithm (oracle port) on all host cores."""
+    """Reference arm: the reference CPU algorithm (oracle port of weld + segment +
+    unfold_chart with the BTreeMap LU) over the whole workload on all host cores, as the
+    reference's par_map runs it (pipeline.rs:192-194).  The Theta(n^2) LU of the largest
+    charts runs for many minutes each, so a run calibrates a per-chart cost model once (a
+    stratified sample up to 4000 vertices, timed on all cores); each step then times a
+    bounded stratified sample again and scales the model's whole-workload par_map wall time
+    by the ratio of measured to modelled time on that sample.  No GPU and no part of this
+    repository's library is used."""
     if rank != 0:
         return
     import multiprocessing as mp
 
-    _, cfg, src = make_workload(args.workload)
+    cfg, src = workload_config(args.workload)
     if src[0] != "patches":
         print(json.dumps({"impl": "reference", "metric": METRIC, "value": None, "unit": UNIT,
                           "unavailable": "the reference LU is Theta(n^2) per chart: a single 1M-vertex chart is "
-                                         "infeasible (extrapolated hours); run the disks workload"}))
+                                         "infeasible (extrapolated days); run the disks workload"}))
         return
-    kind, vo, to, p3, tr = src
-    ids = _sample(src, n_max=100000)
+    _, vo, to, p3, tr = src
+    nv = np.diff(vo)
     cores = os.cpu_count() or 1
-    # size one step to ~8 s of all-core work: calibrate on the first charts
-    tasks = [(p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]]) for c in ids]
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        t0 = time.perf_counter()
-        probe = pool.map(_oracle_chart, tasks[:cores * 4])
-        per = (time.perf_counter() - t0) / max(len(probe), 1)
-        n_step = max(cores, min(len(tasks), int(8.0 / max(per, 1e-6))))
-        step_tasks = tasks[:n_step]
+    model, cal_ids, cal_t, cal_wall = reference_model(src, cores, cap=4000)
+    t_model = model(nv)
+    wall_model = parmap_wall(t_model, cores)
+    # the per-step sample: calibration charts in ascending size while the sample's modelled
+    # work stays within ~6 s on all cores and no chart exceeds ~4 s
+    step_ids = []
+    acc = 0.0
+    for c in cal_ids:
+        tc = float(model(np.array([nv[c]]))[0])
+        if tc > 4.0 or (acc + tc) / cores > 6.0:
+            break
+        step_ids.append(c)
+        acc += tc
+    step_pred = float(model(nv[step_ids]).sum())
+    with mp.get_context("spawn").Pool(cores) as pool:
         for _ in range(args.warmup):
-            pool.map(_oracle_chart, step_tasks[: max(cores, n_step // 4)])
-        times, unks = [], 0
+            _time_charts(pool, src, step_ids)
+        walls, extrap = [], []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            out = pool.map(_oracle_chart, step_tasks)
-            times.append(time.perf_counter() - t0)
-            unks = sum(o[1] for o in out)
-    ms = 1000.0 * statistics.mean(times)
-    value = unks / (ms / 1000.0)
+            ts = _time_charts(pool, src, step_ids)
+            walls.append(time.perf_counter() - t0)
+            extrap.append(wall_model * float(ts.sum()) / step_pred)
+    unknowns = cfg["unknowns"]
+    whole_s = statistics.mean(extrap)
+    value = unknowns / whole_s
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {**cfg, "sample": f"{len(step_tasks)} charts per step (2nf+1 <= 3000)"},
+            "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.mean(walls), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{len(step_tasks)} charts/step, {unks} unknowns, process pool over charts"},
+                             "sample": f"whole workload ({len(nv)} charts, {unknowns} unknowns) by chart: "
+                                       f"per-chart cost model calibrated on {len(cal_ids)} size-stratified charts "
+                                       f"up to 4000 vertices ({cal_wall:.0f} s on {cores} cores, cost ~ nv^"
+                                       f"{model.beta:.2f}); each step times {len(step_ids)} of them again and scales "
+                                       "the modelled whole-workload wall time by measured / modelled",
+                             "host": host_info()},
+            "value_from": "unknowns of the whole workload / its extrapolated wall time under the reference's par_map "
+                          "(contiguous chunks, one per core, core/src/exec.rs:28-60); ms_per_step is the wall time of "
+                          "each step's timed sample",
+            "extrapolated_s_per_workload": whole_s,
+            "modelled_cpu_s_per_workload": float(t_model.sum()),
+            "calibration": {"charts": len(cal_ids), "max_vertices": int(nv[cal_ids].max()),
+                            "max_chart_s": float(cal_t.max()), "beta": model.beta,
+                            "largest_chart_vertices": int(nv.max()),
+                            "largest_chart_modelled_s": float(model(np.array([nv.max()]))[0])},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -326,14 +519,92 @@ def single_chart_baseline(ctx, vo, unknowns, batched_ms, n_sample, precond_name=
                     "size-stratified sample scaled by unknowns"}
 
 
+def field_parity(src, uv_gpu, charts):
+    """UV error of the GPU result on EVERY chart of a height field against the FP64 sparse-LU
+    oracle (oracle chart stages, SuperLU on the scalar Laplacian with both right-hand sides,
+    the reference's damped driver), normalised as unwrap/src/lscm.rs:749-758; the oracle's
+    time is the practical 1-core FP64 direct solve of the same workload."""
+    from oracle import oracle as O
+
+    _, p, f = src
+    t0 = time.perf_counter()
+    P = O.Pipeline(p, f, lu_limit=0)
+    t_prep = time.perf_counter() - t0
+    vo = charts.i64("chart.vert_off")
+    assert P.n_charts == len(vo) - 1, (P.n_charts, len(vo) - 1)
+    worst, worst_chart, checked, unk, t_lu = 0.0, -1, 0, 0, 0.0
+    for c in range(P.n_charts):
+        ch = P.chart(c)
+        nf = int((ch["free_pos"] >= 0).sum())
+        t1 = time.perf_counter()
+        uv_lu = P.superlu_uv(c)
+        t_lu += time.perf_counter() - t1
+        unk += 2 * nf
+        err = O.uv_error(uv_gpu[vo[c]:vo[c + 1]], uv_lu)
+        checked += 1
+        if err > worst:
+            worst, worst_chart = err, c
+    return {"uv_err_max_vs_lu": worst, "uv_err_charts_checked": checked,
+            "uv_err_worst_chart": {"chart": worst_chart, "vertices": int(vo[worst_chart + 1] - vo[worst_chart])},
+            "cpu_direct": {"value": unk / (t_prep + t_lu), "unit": UNIT, "cores": 1, "kind": "port",
+                           "oracle_prep_s": round(t_prep, 2), "superlu_s": round(t_lu, 2), "host": host_info(),
+                           "what": "whole workload, 1 core: oracle weld + segment + assembly, then FP64 SuperLU "
+                                   "(scipy splu, COLAMD) per chart with 2 right-hand sides and the damped driver"}}
+
+
+def compare_preconds(ctx, args, stats, names):
+    """One solve of the resident workload per preconditioner: device time of the phases and
+    CG iterations (the AMG-against-IC(0) comparison of the large-chart workload)."""
+    import ctypes
+
+    import researchuv_gb300 as R
+
+    L = R.lib()
+    prec = R.Precision.MIXED if args.precision == "mixed" else R.Precision.FP64
+    out = {}
+    for name in names:
+        pc = {"jacobi": R.Precond.JACOBI, "amg": R.Precond.AMG, "amg_sa": R.Precond.AMG_SA, "ic0": R.Precond.IC0,
+              "ic0_color": R.Precond.IC0_COLOR}[name]
+        copts = R.UnfoldOptions(precision=prec, precond=pc).to_c()
+        st = L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(copts), stats)
+        t = R.last_timings(ctx)
+        it = [stats[i].cg_iters for i in range(len(stats))]
+        out[name] = {"status": R.Status(st).name, "ms": round(sum(t[:3]), 3), "pcg_ms": round(t[1], 3),
+                     "setup_ms": round(t[3], 3), "cg_iters_max": int(max(it)),
+                     "charts_not_ok": int(sum(1 for i in range(len(stats)) if stats[i].status != 0))}
+    return out
+
+
+def _fd_worker(args):
+    from oracle import oracle as O
+
+    p3, tris, pinned, pin_uv, lam, target, picks = args
+    return O.fd_gradient(p3, tris, pinned, pin_uv, lam, target, picks, h=1e-6, reuse_base=True)
+
+
+def fd_parallel(p3, tris, pinned, pin_uv, lam, target, picks, workers):
+    """oracle.fd_gradient over `picks` split across `workers` spawned processes (each factors
+    the unperturbed system once)."""
+    import multiprocessing as mp
+
+    chunks = [picks[i::workers] for i in range(workers)]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        parts = pool.map(_fd_worker, [(p3, tris, pinned, pin_uv, lam, target, c) for c in chunks if c])
+    out = {}
+    for c, part in zip([c for c in chunks if c], parts):
+        for pk, v in zip(c, part):
+            out[pk] = v
+    return np.array([out[pk] for pk in picks])
+
+
 # ------------------------------------------------------------------ GPU arm
 def run_adjoint(args, rank, world, local, pg):
     """Differentiation workload: an n_lat x 2 n_lat spherical-harmonic sphere cut into one disk
     chart; a step = forward solve + distortion loss with gradients + backward (adjoint solve
     and the assembly's reverse pass) through the host-buffer API, giving d(loss)/d(positions)
     for loss = sum_t area_t (s1/s2 - 1)^2 + lam |uv - target|^2.  Checks the gradient
-    against the CPU LU adjoint at full size and against FP64 central differences (h = 1e-6)
-    on 64 random vertices of a 64 x 128 instance."""
+    against the CPU LU adjoint and against FP64 central differences (h = 1e-6) on 64 random
+    vertices, both on the full-size sphere."""
     import researchuv_gb300 as R
     from oracle import oracle as O
     from researchuv_gb300 import workloads as W
@@ -404,23 +675,24 @@ def run_adjoint(args, rank, world, local, pg):
                                 "sample": "the whole workload once: oracle fixed-pin assembly, SuperLU factor, "
                                           "forward + adjoint solves, reverse pass (FP64)"}
         line["grad_rel_err_vs_lu_adjoint"] = float(np.linalg.norm(grad - ref) / np.linalg.norm(ref))
-        # central differences on a smaller instance of the same family
-        p2, f2 = W.sh_sphere(64, 128, seed=4)
-        C2 = R.prepare_patches(np.array([0, len(p2)]), np.array([0, len(f2)]), p2, f2)
-        c2 = C2.chart(0)
-        tg2 = c2["p2"] + 0.01 * rng.standard_normal(c2["p2"].shape)
-        lam2 = 1.0 / len(p2)
-        uv2, _ = R.lscm_forward(ctx, C2.batch(), opts, len(p2))
-        _, duv2, dpd2 = R.distortion_loss(ctx, uv2, 1)
-        dps2, _ = R.lscm_backward(ctx, duv2 + 2.0 * lam2 * (uv2 - tg2), opts, 1)
-        g2 = dpd2 + dps2
-        picks = [(int(v), k) for v in np.random.Generator(np.random.PCG64(5)).choice(len(p2), 64, replace=False)
+        # central differences on 64 random vertices of the same sphere, 3 coordinates each
+        picks = [(int(v), k) for v in np.random.Generator(np.random.PCG64(5)).choice(n, 64, replace=False)
                  for k in range(3)]
-        fd = O.fd_gradient(p2, c2["tris"], c2["pinned"].astype(np.int64), c2["pin_uv"], lam2, tg2, picks, h=1e-6)
-        ad = np.array([g2[v, k] for v, k in picks])
-        line["fd_check"] = {"instance": "64x128 sphere of the same family", "picks": len(picks), "h": 1e-6,
+        t1 = time.time()
+        fd = fd_parallel(p, ch["tris"], ch["pinned"].astype(np.int64), ch["pin_uv"], lam, target, picks,
+                         min(os.cpu_count() or 1, 16))
+        ad = np.array([grad[v, k] for v, k in picks])
+        err = np.abs(ad - fd)
+        floor = 1e-3 * np.abs(fd).max()
+        line["fd_check"] = {"instance": f"the {n_lat}x{2 * n_lat} sphere itself", "picks": len(picks), "h": 1e-6,
+                            "what": "FP64 central differences of the loss through the fixed-pin SuperLU solve "
+                                    "(perturbed systems solved by refinement on the unperturbed factors)",
                             "rel_err_norm": float(np.linalg.norm(ad - fd) / np.linalg.norm(fd)),
-                            "max_abs_err_over_max_abs": float(np.abs(ad - fd).max() / np.abs(fd).max())}
+                            "max_abs_err_over_max_abs": float(err.max() / np.abs(fd).max()),
+                            "per_component_rel_err_max": float((err / np.maximum(np.abs(fd), floor)).max()),
+                            "per_component_floor": "|fd| floored at 1e-3 max|fd|",
+                            "components_below_floor": int((np.abs(fd) < floor).sum()),
+                            "cpu_s": round(time.time() - t1, 1)}
     if rank == 0:
         print(json.dumps(line))
     barrier(pg)
@@ -441,7 +713,7 @@ def main():
 
         import researchuv_gb300 as R
 
-        charts, _, _ = make_workload(args.workload)
+        charts, _ = prepare(workload_config(args.workload)[1])
         ctx = R.Context(local)
         L = R.lib()
         pc = {"jacobi": R.Precond.JACOBI, "amg": R.Precond.AMG, "amg_sa": R.Precond.AMG_SA,
@@ -460,7 +732,8 @@ def main():
 
     import researchuv_gb300 as R
 
-    charts, cfg, src = make_workload(args.workload)
+    cfg, src = workload_config(args.workload)
+    charts, prep_s = prepare(src)
     ctx = R.Context(local)
     L = R.lib()
     batch = charts.batch()
@@ -478,6 +751,10 @@ def main():
         uv, st, status = R.solve_batch(ctx, batch, opts, nv)
     n_free = np.array([s.n_free for s in st])
     unknowns = int(2 * n_free.sum())
+    if "unknowns" in cfg:
+        assert unknowns == cfg["unknowns"], (unknowns, cfg["unknowns"])
+    else:
+        cfg = {**cfg, "charts": int(batch.n_charts), "unknowns": unknowns}
     statuses = np.array([s.status for s in st])
     cg_iters = np.array([s.cg_iters for s in st])
 
@@ -537,8 +814,8 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if prec == R.Precision.MIXED else "f64",
         "data": "synthetic",
-        "config": {**cfg, "unknowns": unknowns, "precision": args.precision, "precond": args.precond,
-                   "tol": 1e-12, "l2": "inputs larger than L2 (operator + vectors ~1 GB)",
+        "config": cfg,
+        "solver": {"precision": args.precision, "precond": args.precond, "tol": 1e-12, "host_prep_s": prep_s,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "phase_ms": {"assembly": round(phases[0], 3), "pcg": round(phases[1], 3),
                                 "driver": round(phases[2], 3), "precond_setup_in_pcg": round(phases[3], 3)},
@@ -567,11 +844,17 @@ def main():
         line["single_chart_fp64_pcg"] = single_chart_baseline(ctx, vo, unknowns, ms, args.single_chart_sample)
         line["single_chart_fp64_pcg_ic0"] = single_chart_baseline(ctx, vo, unknowns, ms,
                                                                   max(args.single_chart_sample // 4, 1), "IC0")
+    if rank == 0 and args.compare:
+        line["compare"] = compare_preconds(ctx, args, stats, [x for x in args.compare.split(",") if x])
     if rank == 0 and not args.no_cpu_baseline and src[0] == "patches":
-        base, err, n_err = cpu_baseline(src, uv, args.cpu_budget)
+        base, err, n_err = cpu_baseline(src, uv, args.cpu_budget, unknowns)
         line["cpu_baseline"] = base
         line["uv_err_max_vs_lu"] = err
         line["uv_err_charts_checked"] = n_err
+        if not args.no_superlu_baseline:
+            line["cpu_superlu_whole_workload"] = superlu_baseline(src, os.cpu_count() or 1)
+    if rank == 0 and not args.no_cpu_baseline and src[0] == "mesh":
+        line.update(field_parity(src, np.array(uv), charts))
     if rank == 0:
         print(json.dumps(line))
     barrier(pg)

@@ -68,6 +68,12 @@ ruv_status ruv_ctx_create(ruv_ctx** out, int32_t device);
 void ruv_ctx_destroy(ruv_ctx* ctx);
 /* Message of the last failing call on this context ("" if none). */
 const char* ruv_last_error(const ruv_ctx* ctx);
+/* Fault injection for tests of the out-of-memory paths (no counterpart in the reference,
+ * whose DeviceMem::alloc failure is an Option::None, gpu/src/solver.rs:671-729): with
+ * nth > 0 the nth device allocation this context makes from now on fails as if the device
+ * were out of memory (no cudaMalloc is made; the call returns OOM), nth <= 0 turns it off.
+ * The context stays usable after the failure. */
+ruv_status ruv_debug_fail_alloc(ruv_ctx* ctx, int64_t nth);
 
 /* GpuSolver::cg_solve_precond (gpu/src/solver.rs:284-565).
  * A: n x n SPD CSR (row_ptr[n+1], cols[nnz], vals[nnz]); b[n]; x_out[n] (written on OK).
@@ -121,12 +127,17 @@ ruv_status ruv_ic0_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const
  * The caller passes DEVICE pointers for the system (row_ptr[n+1], cols[nnz], vals[nnz]),
  * the right-hand side b[n] and the solution x[n]; the solver's own scratch (CG vectors,
  * inverse diagonal, partial sums, solver state) lives in one fixed array compiled into the
- * library, about 12.6 MB, which every GPU that loads the library holds until exit.  Systems
- * with n > RUV_NOALLOC_MAX_ROWS are rejected with BAD_INPUT.  PRECOND_NONE or _JACOBI.
- * Same stopping rule and statuses as ruv_cg_solve; work is enqueued on `stream` (a
- * cudaStream_t, NULL = the legacy default stream) and the call returns after it finished.
- * The first call on each device resolves the array's device address for that device: make
- * that first call before any stream capture.  All calls share the one array, so calls that
+ * library, about 12.6 MB.  Each CUDA context that runs this entry holds its own copy of the
+ * array until the context ends: CUDA loads the library's solver module into a context lazily,
+ * on its first use there, and the array is reserved by the driver at that moment.  So the
+ * FIRST call in each context (each device's primary context, or any context the caller
+ * makes current) does allocate device memory through the driver and may synchronise: make
+ * it at start-up, before any stream capture and outside the frame loop; later calls in that
+ * context allocate nothing.  Every call resolves the array's address in the current
+ * context.  Systems with n > RUV_NOALLOC_MAX_ROWS are rejected with BAD_INPUT.
+ * PRECOND_NONE or _JACOBI.  Same stopping rule and statuses as ruv_cg_solve; work is
+ * enqueued on `stream` (a cudaStream_t, NULL = the legacy default stream) and the call
+ * returns after it finished.  All calls in a context share the one array, so calls that
  * overlap on the GPU (other threads or streams at the same time) race and must be
  * serialised by the caller.  An explanation of a non-OK status is written to msg
  * (msg_len bytes, may be NULL). */

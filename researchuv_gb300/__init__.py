@@ -57,6 +57,7 @@ SIGNATURES = {
     "ruv_ctx_create": (ctypes.c_int, [_P(_vp), _i32]),
     "ruv_ctx_destroy": (None, [_vp]),
     "ruv_last_error": (_cp, [_vp]),
+    "ruv_debug_fail_alloc": (ctypes.c_int, [_vp, _i64]),
     "ruv_cg_solve": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _P(_f64), _P(_f64), _i64, _f64,
                                     ctypes.c_int, _P(_i64)]),
     "ruv_apply_ic0": (ctypes.c_int, [_vp, _i32, _P(_i32), _P(_i32), _P(_f64), _P(_f64), _P(_f64)]),

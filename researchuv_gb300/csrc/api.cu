@@ -40,7 +40,19 @@ ruv_status guarded(ruv_ctx* ctx, F&& body) {
     }
     return body();
   } catch (const Error& e) {
-    if (ctx) cudaStreamSynchronize(ctx->c.stream);
+    if (ctx) {
+      // an error thrown while the stream was being captured leaves the capture open: close it
+      // so that the context's stream stays usable for the next call
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(ctx->c.stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(ctx->c.stream, &g);
+        if (g) cudaGraphDestroy(g);
+      }
+      cudaGetLastError();
+      cudaStreamSynchronize(ctx->c.stream);
+      cudaStreamSynchronize(ctx->c.side);
+    }
     cudaGetLastError();
     return fail(ctx, e.status, e.msg);
   } catch (const std::bad_alloc&) {
@@ -138,6 +150,12 @@ void ruv_ctx_destroy(ruv_ctx* ctx) {
 }
 
 const char* ruv_last_error(const ruv_ctx* ctx) { return ctx ? ctx->c.last_error.c_str() : ""; }
+
+ruv_status ruv_debug_fail_alloc(ruv_ctx* ctx, int64_t nth) {
+  if (!ctx) return RUV_ERR_BAD_INPUT;
+  ctx->c.ws.fail_countdown = nth > 0 ? nth : 0;
+  return RUV_OK;
+}
 
 void ruv_unfold_opts_default(ruv_unfold_opts* o) {
   if (!o) return;

@@ -56,6 +56,8 @@ class Workspace {
       b.ptr = nullptr;
       b.bytes = 0;
       size_t want = bytes + bytes / 8 + 256;
+      if (fail_countdown > 0 && --fail_countdown == 0)  // host-side fault injection (ruv_debug_fail_alloc)
+        throw Error{RUV_ERR_OOM, "injected allocation failure: cudaMalloc(" + std::to_string(want) + ") for " + name};
       cudaError_t e = cudaMalloc(&b.ptr, want);
       if (e != cudaSuccess) {
         b.ptr = nullptr;
@@ -81,6 +83,9 @@ class Workspace {
     for (auto& kv : bufs_) s += kv.second.bytes;
     return s;
   }
+  // > 0: the fail_countdown-th device allocation from now on fails as if the device were out
+  // of memory (no cudaMalloc is made); 0: off.
+  int64_t fail_countdown = 0;
 
  private:
   struct Buf {

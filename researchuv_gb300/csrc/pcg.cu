@@ -32,7 +32,6 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
-#include <mutex>
 
 namespace ruv {
 namespace {
@@ -1433,14 +1432,15 @@ struct NoAllocScratch {
   int32_t nonfinite;
 };
 
-// Every GPU that loads the library holds this array (about 12.6 MB) until the process exits.
+// The allocation-free solve's scratch (about 12.6 MB).  A __device__ array belongs to the
+// module instance of this file, and every CUDA context that loads the module gets its own
+// copy, mapped when the module loads (under CUDA's default lazy loading: the first launch or
+// symbol query in that context) and held until the context ends.  Host code may not use the
+// symbol's name as a device pointer; the entry point resolves the address in the current
+// context on every call (a host-side lookup once the module is loaded), so a context other
+// than the device's primary one, or a context created again after cudaDeviceReset, never
+// sees an address of another context.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
-
-// Device addresses of g_noalloc_scratch, resolved once per device (host code may not use
-// the symbol's name as a device pointer).
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kNoAllocMaxDevices] = {};
 
 __global__ void k_na_check_ptr(int32_t n, const int32_t* __restrict__ row_ptr, int32_t* __restrict__ bad) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1524,25 +1524,22 @@ extern "C" ruv_status ruv_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, co
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+  if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
     na_message(msg, msg_len, "no current CUDA device");
     return RUV_ERR_NO_DEVICE;
   }
+  // The scratch's address in the current context (see g_noalloc_scratch).
   NoAllocScratch* S = nullptr;
   {
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-      void* ptr = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-      if (e != cudaSuccess || !ptr) {
-        cudaGetLastError();
-        na_message(msg, msg_len, "cudaGetSymbolAddress of the no-alloc scratch failed");
-        return RUV_ERR_NO_DEVICE;
-      }
-      g_noalloc_addr[dev] = ptr;
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) {
+      cudaGetLastError();
+      na_message(msg, msg_len, "cudaGetSymbolAddress of the no-alloc scratch failed");
+      return RUV_ERR_NO_DEVICE;
     }
-    S = static_cast<NoAllocScratch*>(g_noalloc_addr[dev]);
+    S = static_cast<NoAllocScratch*>(ptr);
   }
   auto launch_fail = [&](const char* what) {
     cudaGetLastError();

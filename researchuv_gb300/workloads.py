@@ -181,3 +181,24 @@ def sh_sphere(n_lat: int = 512, n_lon: int = 1024, n_sh: int = 8, amp: float = 0
     pos = np.stack([(r * st * np.cos(Ph)).ravel(), (r * st * np.sin(Ph)).ravel(), (r * ct).ravel()], 1)
     return pos.astype(np.float32).astype(np.float64), grid_faces(n_lon, n_lat)
 
+
+def disk_unknowns(vert_off, tri_off, tris) -> int:
+    """Unknowns (2 x free vertices) of a batch of open disk patches, from topology alone: the
+    reference pins every vertex of a border loop (unwrap/src/lscm.rs:524-529), and a disk's
+    border loop is the set of vertices on an edge that only one triangle uses."""
+    vo = np.asarray(vert_off, np.int64)
+    to = np.asarray(tri_off, np.int64)
+    t = np.asarray(tris, np.int64).reshape(-1, 3)
+    # global vertex ids (patch-local + the patch's first vertex)
+    base = np.repeat(vo[:-1], np.diff(to))
+    g = t + base[:, None]
+    e = np.concatenate([g[:, [0, 1]], g[:, [1, 2]], g[:, [2, 0]]])
+    e.sort(axis=1)
+    key = e[:, 0] * (int(vo[-1]) + 1) + e[:, 1]
+    uniq, cnt = np.unique(key, return_counts=True)
+    border = uniq[cnt == 1]
+    on_border = np.zeros(int(vo[-1]), bool)
+    on_border[border // (int(vo[-1]) + 1)] = True
+    on_border[border % (int(vo[-1]) + 1)] = True
+    return int(2 * (int(vo[-1]) - int(on_border.sum())))
+

@@ -47,7 +47,9 @@ def _poisson(side):
     return R.CsrMatrix(vals[order], cols[order], rp), (np.arange(n) % 97) * 0.01 + 1.0
 
 
-def _noalloc(a: R.CsrMatrix, b, max_iter, tol, pc):
+def _noalloc(a: R.CsrMatrix, b, max_iter, tol, pc, stream=None):
+    """One call through the C ABI; returns (status, x, iters, message, free device bytes
+    before the call, free device bytes after it)."""
     n = a.rows()
     dev = torch.device("cuda", 0)
     d_rp = torch.from_numpy(a.row_ptr).to(dev)
@@ -58,30 +60,36 @@ def _noalloc(a: R.CsrMatrix, b, max_iter, tol, pc):
     torch.cuda.synchronize()
     msg = ctypes.create_string_buffer(256)
     iters = ctypes.c_int64(-1)
+    free_before = torch.cuda.mem_get_info(dev)[0]
     st = R.lib().ruv_cg_solve_noalloc(n, d_rp.data_ptr(), d_c.data_ptr(), d_v.data_ptr(), d_b.data_ptr(),
-                                      d_x.data_ptr(), max_iter, tol, int(pc), ctypes.byref(iters), None, msg, 256)
+                                      d_x.data_ptr(), max_iter, tol, int(pc), ctypes.byref(iters),
+                                      None if stream is None else stream.cuda_stream, msg, 256)
     torch.cuda.synchronize()
-    return st, d_x.cpu().numpy(), iters.value, msg.value.decode()
+    free_after = torch.cuda.mem_get_info(dev)[0]
+    return st, d_x.cpu().numpy(), iters.value, msg.value.decode(), free_before, free_after
 
 
-@pytest.mark.parametrize("case", ["lap1d_jacobi", "poisson_none"])
+@pytest.mark.parametrize("case", ["lap1d_jacobi", "poisson_none", "lap1d_jacobi_stream"])
 def test_noalloc_matches_cg_solve_on_two_calls(case):
-    if case == "lap1d_jacobi":
+    if case.startswith("lap1d_jacobi"):
         a, b = _lap1d(4096)
         pc, max_iter, tol = R.Precond.JACOBI, 20_000, 1e-12
     else:
         a, b = _poisson(400)
         pc, max_iter, tol = R.Precond.NONE, 100_000, 1e-10
+    stream = torch.cuda.Stream() if case.endswith("_stream") else None
     ref = R.GpuSolver.new().cg_solve_precond(a, b, max_iter, tol, pc)
     assert ref is not None
     x_ref, it_ref = ref
     scale = max(1.0, np.abs(x_ref).max())
     for call in range(2):  # the shared scratch keeps the previous call's contents
-        st, x, iters, msg = _noalloc(a, b, max_iter, tol, pc)
+        st, x, iters, msg, free_before, free_after = _noalloc(a, b, max_iter, tol, pc, stream)
         assert st == R.Status.OK, f"call {call}: {R.Status(st).name}: {msg}"
         assert np.abs(x - x_ref).max() <= TOL * scale, f"call {call}: differs from ruv_cg_solve"
         assert iters == it_ref
-    if case == "lap1d_jacobi":
+        if call == 1:  # warm: the module (and its scratch array) is loaded; nothing is allocated
+            assert free_after == free_before, f"a warm call changed free device memory by {free_before - free_after} B"
+    if case.startswith("lap1d_jacobi"):
         assert np.abs(x - 1.0).max() < 1e-8  # gpu/src/solver.rs:768-779 known answer
 
 
