@@ -81,8 +81,11 @@ def parse():
     ap.add_argument("--no-superlu-baseline", action="store_true",
                     help="skip the whole-workload FP64 SuperLU leg of the disks workloads")
     ap.add_argument("--compare", default="",
-                    help="comma-separated preconditioners (ic0, ic0_color, amg, amg_sa, jacobi) solved once each "
-                         "on the resident workload after the timed steps, for iterations and time")
+                    help="comma-separated preconditioners (ic0, ic0_color, amg, amg_sa, jacobi; amg+k2 / amg_sa+k2: "
+                         "with the K-cycle on the top 2 levels) solved once each on the resident workload after the "
+                         "timed steps, for iterations and time")
+    ap.add_argument("--kcycle", type=int, default=0,
+                    help="AMG levels in the K-form for the timed steps (0: V(1,1) cycle)")
     ap.add_argument("--ncu-step", action="store_true",
                     help="for profiler launch lists: upload, one warm-up solve, then one solve of the workload "
                          "(launch shape from RUV_LPR / RUV_UNROLL / RUV_TILE_ROWS); prints the kernel count "
@@ -138,15 +141,16 @@ def workload_config(name):
     return cfg, ("mesh", p, f)
 
 
-def prepare(src):
-    """The chart stages on the host (weld + segment + frames + pins), timed."""
+def prepare(src, ctx=None):
+    """The chart stages (weld + segment + frames + pins), timed; with a context their
+    data-parallel parts run on its device (the same charts bit for bit)."""
     import researchuv_gb300 as R
 
     t0 = time.time()
     if src[0] == "patches":
-        charts = R.prepare_patches(*src[1:])
+        charts = R.prepare_patches(*src[1:], ctx=ctx)
     else:
-        charts = R.prepare_mesh(*src[1:])
+        charts = R.prepare_mesh(*src[1:], ctx=ctx)
     return charts, round(time.time() - t0, 3)
 
 
@@ -563,16 +567,66 @@ def compare_preconds(ctx, args, stats, names):
     prec = R.Precision.MIXED if args.precision == "mixed" else R.Precision.FP64
     out = {}
     for name in names:
+        base, _, kc = name.partition("+k")  # "amg_sa+k2": the K-cycle on the top 2 levels
         pc = {"jacobi": R.Precond.JACOBI, "amg": R.Precond.AMG, "amg_sa": R.Precond.AMG_SA, "ic0": R.Precond.IC0,
-              "ic0_color": R.Precond.IC0_COLOR}[name]
+              "ic0_color": R.Precond.IC0_COLOR}[base]
         copts = R.UnfoldOptions(precision=prec, precond=pc).to_c()
+        old_k = os.environ.get("RUV_AMG_KCYCLE")
+        if kc:
+            os.environ["RUV_AMG_KCYCLE"] = kc
         st = L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(copts), stats)
+        if kc:
+            if old_k is None:
+                del os.environ["RUV_AMG_KCYCLE"]
+            else:
+                os.environ["RUV_AMG_KCYCLE"] = old_k
         t = R.last_timings(ctx)
         it = [stats[i].cg_iters for i in range(len(stats))]
         out[name] = {"status": R.Status(st).name, "ms": round(sum(t[:3]), 3), "pcg_ms": round(t[1], 3),
                      "setup_ms": round(t[3], 3), "cg_iters_max": int(max(it)),
                      "charts_not_ok": int(sum(1 for i in range(len(stats)) if stats[i].status != 0))}
     return out
+
+
+def single_chart_reference(ctx, vo, unknowns, batched_ms, n_sample):
+    """The measuring stick of the >= 5x target as the reference builds it: its own CG kernels
+    (gpu/src/kernels.cu, compute_80 PTX JIT-loaded) under the oracle's restatement of its host
+    loop (gpu/src/solver.rs:284-565: per-call uploads, a host-summed dot product after every
+    kernel that needs one), FP64 Jacobi PCG (the reference's default, lscm.rs:492-501), tol
+    1e-12, 16384 iterations, one chart after another on its interleaved CSR.  Timed on the
+    size-stratified sample of single_chart_baseline, scaled to the workload by unknowns."""
+    import researchuv_gb300 as R
+    from oracle import oracle as O
+
+    try:
+        ref = O.RefGpuCG()
+    except Exception as e:  # no PTX (built only where the reference's source is present)
+        return {"unavailable": str(e)}
+    sizes = np.diff(vo)
+    order = np.argsort(sizes)
+    idx = order[np.linspace(0, len(order) - 1, min(n_sample, len(order))).astype(int)]
+    systems = []
+    for c in idx:
+        rp, cols, vals, rhs = R.export_chart_system(ctx, int(c))
+        if len(rp) > 1:
+            systems.append((rp, cols, vals, rhs))
+    for rp, cols, vals, rhs in systems[:4]:  # warm-up (module JIT, first allocations)
+        ref.solve(rp, cols, vals, rhs, 16384, 1e-12, jacobi=True)
+    t0 = time.perf_counter()
+    unk, iters, fails = 0, 0, 0
+    for rp, cols, vals, rhs in systems:
+        r = ref.solve(rp, cols, vals, rhs, 16384, 1e-12, jacobi=True)
+        unk += len(rp) - 1
+        if r is None:
+            fails += 1
+        else:
+            iters += r[1]
+    dt = time.perf_counter() - t0
+    full_ms = 1000.0 * dt * unknowns / max(unk, 1)
+    return {"ms_per_step_extrapolated": full_ms, "sample_charts": len(systems), "sample_unknowns": unk,
+            "sample_s": round(dt, 3), "sample_iters": iters, "failed": fails, "batched_speedup": full_ms / batched_ms,
+            "what": "the reference's CG kernels (kernels.cu, compute_80 PTX) under the restated host loop of "
+                    "solver.rs:284-565, FP64 Jacobi PCG per chart, size-stratified sample scaled by unknowns"}
 
 
 def _fd_worker(args):
@@ -700,6 +754,8 @@ def run_adjoint(args, rank, world, local, pg):
 
 def main():
     args = parse()
+    if args.kcycle > 0:
+        os.environ["RUV_AMG_KCYCLE"] = str(args.kcycle)
     rank, world, local, pg = dist()
     if args.impl == "reference":
         run_reference(args, rank)
@@ -733,8 +789,9 @@ def main():
     import researchuv_gb300 as R
 
     cfg, src = workload_config(args.workload)
-    charts, prep_s = prepare(src)
     ctx = R.Context(local)
+    prepare(src, ctx)  # warm (the first device preparation allocates its workspace)
+    charts, prep_s = prepare(src, ctx)
     L = R.lib()
     batch = charts.batch()
     vo = charts.i64("chart.vert_off")
@@ -815,7 +872,9 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if prec == R.Precision.MIXED else "f64",
         "data": "synthetic",
         "config": cfg,
-        "solver": {"precision": args.precision, "precond": args.precond, "tol": 1e-12, "host_prep_s": prep_s,
+        "solver": {"precision": args.precision, "precond": args.precond, "tol": 1e-12,
+                   "prep_s": prep_s, "prep": "chart stages with their data-parallel parts on the device "
+                                             "(ruv_prepare_patches_gpu / ruv_prepare_mesh_gpu), untimed",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "phase_ms": {"assembly": round(phases[0], 3), "pcg": round(phases[1], 3),
                                 "driver": round(phases[2], 3), "precond_setup_in_pcg": round(phases[3], 3)},
@@ -841,6 +900,8 @@ def main():
         "clocks": clock_info,
     }
     if rank == 0 and not args.no_single_chart:
+        line["single_chart_reference_kernels"] = single_chart_reference(ctx, vo, unknowns, ms,
+                                                                        args.single_chart_sample)
         line["single_chart_fp64_pcg"] = single_chart_baseline(ctx, vo, unknowns, ms, args.single_chart_sample)
         line["single_chart_fp64_pcg_ic0"] = single_chart_baseline(ctx, vo, unknowns, ms,
                                                                   max(args.single_chart_sample // 4, 1), "IC0")

@@ -345,6 +345,16 @@ ruv_status ruv_prepare_mesh_cut(ruv_ctx* ctx, const double* pos, int64_t n_verts
  * patch-local indices.  Border loops are walked over each patch's boundary edges. */
 ruv_status ruv_prepare_patches(int64_t n_patches, const int64_t* vert_off, const int64_t* tri_off,
                                const double* p3, const int32_t* tris, int32_t threads, ruv_prepared** out);
+/* ruv_prepare_patches with its data-parallel stages on the device of ctx: the patch faces
+ * and their checks, the edge-face lists (a stable radix sort of the edge keys), every
+ * patch's faces in the reference's DFS pop order (segment.rs:150-175, one thread per patch),
+ * face areas and chart areas, the centroid and covariance of each chart's vertices and the
+ * projection on the chart's frame (lscm.rs:152-183), the boundary edges.  The border-loop
+ * walk (segment.rs:227-331), the 3 x 3 eig3 of each frame (host libm) and the pins
+ * (lscm.rs:187-413) run on the host per chart.  The result equals ruv_prepare_patches's bit
+ * for bit. */
+ruv_status ruv_prepare_patches_gpu(ruv_ctx* ctx, int64_t n_patches, const int64_t* vert_off, const int64_t* tri_off,
+                                   const double* p3, const int32_t* tris, int32_t threads, ruv_prepared** out);
 void ruv_prepared_free(ruv_prepared* p);
 /* Read-only view of the prepared charts as the batched-solve input (valid while p lives). */
 ruv_status ruv_prepared_batch(const ruv_prepared* p, ruv_lscm_batch* view);

@@ -26,13 +26,93 @@ _CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC"
 
 
 def build(force: bool = False) -> str:
-    """Compile the restatement into oracle/_build/liboracle.so (plain g++, no build system)."""
+    """Compile the restatement into oracle/_build/liboracle.so (plain g++, no build system),
+    and the reference-kernel harness (build_ref_ptx, build_ref_cg) where it can be built."""
     os.makedirs(os.path.dirname(_LIB), exist_ok=True)
     if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
         tmp = _LIB + ".tmp"
         subprocess.check_call(["g++", *_CXXFLAGS, "-o", tmp, _SRC])
         os.replace(tmp, _LIB)
+    build_ref_ptx()
+    build_ref_cg()
     return _LIB
+
+
+# ------------------------------------------------------------------ the reference's own GPU CG
+# The reference's CG kernels (gpu/src/kernels.cu, compute_80 PTX as gpu/build.rs:41-49 builds
+# them) compiled from the reference's source tree into oracle/_ref/ (not committed; built here
+# where the reference is present, carried as a file elsewhere), and ref_gpu_cg.cpp, the C++
+# restatement of the reference's host loop that drives them.
+_REF_KERNELS = "/root/reference/crates/researchuv-gpu/src/kernels.cu"
+REF_PTX = os.path.join(_HERE, "_ref", "kernels_compute80.ptx")
+_REF_CG_SRC = os.path.join(_HERE, "ref_gpu_cg.cpp")
+_REF_CG_LIB = os.path.join(_HERE, "_build", "libref_gpu_cg.so")
+_CUDA = "/usr/local/cuda"
+
+
+def build_ref_ptx() -> str:
+    """nvcc -ptx -arch=compute_80 of the reference's kernels.cu into oracle/_ref/ (only where
+    the reference's source tree is present; elsewhere the file built there is used)."""
+    if os.path.exists(_REF_KERNELS) and (not os.path.exists(REF_PTX)
+                                         or os.path.getmtime(REF_PTX) < os.path.getmtime(_REF_KERNELS)):
+        os.makedirs(os.path.dirname(REF_PTX), exist_ok=True)
+        nvcc = os.path.join(_CUDA, "bin", "nvcc")
+        tmp = REF_PTX + ".tmp"
+        subprocess.check_call([nvcc, "-ptx", "-arch=compute_80", "-o", tmp, _REF_KERNELS])
+        os.replace(tmp, REF_PTX)
+    return REF_PTX
+
+
+def build_ref_cg() -> str | None:
+    """g++ of ref_gpu_cg.cpp against the CUDA driver API (None without cuda.h)."""
+    inc = os.path.join(_CUDA, "include")
+    if not os.path.exists(os.path.join(inc, "cuda.h")):
+        return None
+    if not os.path.exists(_REF_CG_LIB) or os.path.getmtime(_REF_CG_LIB) < os.path.getmtime(_REF_CG_SRC):
+        os.makedirs(os.path.dirname(_REF_CG_LIB), exist_ok=True)
+        tmp = _REF_CG_LIB + ".tmp"
+        libdirs = [d for d in (os.path.join(_CUDA, "lib64"), os.path.join(_CUDA, "lib64", "stubs"),
+                               os.path.join(_CUDA, "targets", "sbsa-linux", "lib", "stubs"),
+                               os.path.join(_CUDA, "targets", "x86_64-linux", "lib", "stubs")) if os.path.isdir(d)]
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", inc, "-o", tmp, _REF_CG_SRC,
+                               *[f"-L{d}" for d in libdirs], "-lcuda"])
+        os.replace(tmp, _REF_CG_LIB)
+    return _REF_CG_LIB
+
+
+class RefGpuCG:
+    """GpuSolver::cg_solve_precond of the reference (None / Jacobi) on its own kernels."""
+
+    def __init__(self):
+        path = build_ref_cg()
+        if path is None or not os.path.exists(REF_PTX):
+            raise RuntimeError("reference GPU CG harness not built (needs cuda.h and oracle/_ref PTX)")
+        L = ctypes.CDLL(path)
+        L.rcg_init.argtypes = [ctypes.c_char_p]
+        L.rcg_last_error.restype = ctypes.c_char_p
+        P = ctypes.POINTER
+        L.rcg_solve.argtypes = [ctypes.c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_double),
+                                P(ctypes.c_double), P(ctypes.c_double), ctypes.c_int64, ctypes.c_double, ctypes.c_int,
+                                P(ctypes.c_int64)]
+        if L.rcg_init(REF_PTX.encode()) != 0:
+            raise RuntimeError("rcg_init: " + L.rcg_last_error().decode())
+        self.L = L
+
+    def solve(self, row_ptr, cols, vals, b, max_iter, tol, jacobi=True):
+        """(x, iterations) or None, as the reference returns."""
+        rp = np.ascontiguousarray(row_ptr, np.int32)
+        c = np.ascontiguousarray(cols, np.int32)
+        v = np.ascontiguousarray(vals, np.float64)
+        bb = np.ascontiguousarray(b, np.float64)
+        n = len(rp) - 1
+        x = np.empty(n)
+        it = ctypes.c_int64(0)
+        P = ctypes.POINTER
+        st = self.L.rcg_solve(n, rp.ctypes.data_as(P(ctypes.c_int32)), c.ctypes.data_as(P(ctypes.c_int32)),
+                              v.ctypes.data_as(P(ctypes.c_double)), bb.ctypes.data_as(P(ctypes.c_double)),
+                              x.ctypes.data_as(P(ctypes.c_double)), int(max_iter), float(tol), 1 if jacobi else 0,
+                              ctypes.byref(it))
+        return None if st != 0 else (x, int(it.value))
 
 
 _lib = None

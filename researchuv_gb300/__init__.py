@@ -76,6 +76,7 @@ SIGNATURES = {
     "ruv_prepare_mesh_cut": (ctypes.c_int, [_vp, _P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _vp, _P(RuvUnfoldOpts), _i32,
                                             _P(_vp), _P(_i64)]),
     "ruv_prepare_mesh_gpu": (ctypes.c_int, [_vp, _P(_f64), _i64, _P(_i32), _i64, _f64, _f64, _i32, _P(_vp)]),
+    "ruv_prepare_patches_gpu": (ctypes.c_int, [_vp, _i64, _P(_i64), _P(_i64), _P(_f64), _P(_i32), _i32, _P(_vp)]),
     "ruv_prepared_free": (None, [_vp]),
     "ruv_prepared_batch": (ctypes.c_int, [_vp, _P(RuvBatch)]),
     "ruv_prepared_get_i64": (_i64, [_vp, _cp, _P(_i64)]),
@@ -491,13 +492,18 @@ def prepare_mesh_cut(ctx: Optional["Context"], positions, faces, weld_tol: float
     return Charts(h), added.value
 
 
-def prepare_patches(vert_off, tri_off, p3, tris, threads: int = 0) -> Charts:
-    """One chart per given patch (no weld / segmentation)."""
+def prepare_patches(vert_off, tri_off, p3, tris, threads: int = 0, ctx: Optional["Context"] = None) -> Charts:
+    """One chart per given patch (no weld / segmentation).  With a Context, the data-parallel
+    stages run on its device (ruv_prepare_patches_gpu); the result is the same bit for bit."""
     vo = np.ascontiguousarray(vert_off, np.int64)
     to = np.ascontiguousarray(tri_off, np.int64)
     p = np.ascontiguousarray(p3, np.float64).reshape(-1)
     t = np.ascontiguousarray(tris, np.int32).reshape(-1)
     h = _vp()
+    if ctx is not None:
+        ctx.check(lib().ruv_prepare_patches_gpu(ctx.h, len(vo) - 1, _ptr(vo, _i64), _ptr(to, _i64), _ptr(p, _f64),
+                                                _ptr(t, _i32), threads, ctypes.byref(h)), "ruv_prepare_patches_gpu")
+        return Charts(h)
     st = lib().ruv_prepare_patches(len(vo) - 1, _ptr(vo, _i64), _ptr(to, _i64), _ptr(p, _f64), _ptr(t, _i32),
                                    threads, ctypes.byref(h))
     if st != 0:

@@ -942,11 +942,100 @@ __global__ void __launch_bounds__(kAmgThreads) k_prolong_add(LvlTiles T, const i
       T.tab[2 * tl], T.tab[2 * tl + 1], poff, nullptr, ColsWide{pc}, [&](int64_t e) { return alpha_c * pv[e]; },
       [&](int32_t j) { return ldf<NR>(xc, j); },
       [&](int64_t i, const F<NR>& s) {
-        F<NR> xi = ldf<NR>(x, i);
+        F<NR> xi;
+        if (x) {
+          xi = ldf<NR>(x, i);
+        } else {
+#pragma unroll
+          for (int c = 0; c < NR; ++c) xi.c[c] = 0.0f;
+        }
 #pragma unroll
         for (int c = 0; c < NR; ++c) xi.c[c] += s.c[c];
         stf<NR>(y, i, xi);
       });
+}
+
+// K-cycle coarse correction (the K-form of gpu/src/amg.rs:468-639): w = A y over the rows of
+// the level's continuing charts, with per-tile partial sums t.t and t.w (FP32 per row, FP64
+// per tile, fixed combine order) for the steplength beta = (t.t) / (t.A y).
+template <int NR, int LPR, int U, int K, bool NARROW>
+__global__ void __launch_bounds__(kAmgThreads) k_kspmv(LvlTiles T, const int32_t* __restrict__ done,
+                                                       const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                                       const uint16_t* __restrict__ c16, const int32_t* __restrict__ cbase,
+                                                       const float* __restrict__ vals, const float* __restrict__ y,
+                                                       const float* __restrict__ t, float* __restrict__ w,
+                                                       double* __restrict__ part) {
+  __shared__ double sh[2 * 32];
+  const int64_t tl = blockIdx.x;
+  const int32_t ch = T.chart[tl];
+  if (done[ch]) return;
+  double acc[2] = {0.0, 0.0};
+  auto run = [&](auto colf) {
+    tile_rows<NR, LPR, U, K>(
+        T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, colf, [&](int64_t e) { return vals[e]; },
+        [&](int32_t j) { return ldf<NR>(y, j); },
+        [&](int64_t i, const F<NR>& sv) {
+          stf<NR>(w, i, sv);
+          const F<NR> ti = ldf<NR>(t, i);
+          float tt = 0.0f, tw = 0.0f;
+#pragma unroll
+          for (int c = 0; c < NR; ++c) {
+            tt += ti.c[c] * ti.c[c];
+            tw += ti.c[c] * sv.c[c];
+          }
+          acc[0] += (double)tt;
+          acc[1] += (double)tw;
+        });
+  };
+  if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
+  else run(ColsWide{cols});
+  block_sum<2>(acc, sh);
+  if (threadIdx.x == 0) {
+    part[2 * tl] = acc[0];
+    part[2 * tl + 1] = acc[1];
+  }
+}
+
+// beta per chart from its tiles' partial sums (one CTA per chart, fixed combine order); a
+// non-positive or tiny t.A y skips the correction (beta = 0), as the reference guards it.
+__global__ void __launch_bounds__(128) k_kbeta(const int32_t* __restrict__ done, const int64_t* __restrict__ chart_tile,
+                                               const double* __restrict__ part, float* __restrict__ beta) {
+  __shared__ double sh[2 * 32];
+  const int64_t c = blockIdx.x;
+  if (done[c]) return;
+  double acc[2] = {0.0, 0.0};
+  for (int64_t t = chart_tile[c] + threadIdx.x; t < chart_tile[c + 1]; t += blockDim.x) {
+    acc[0] += part[2 * t];
+    acc[1] += part[2 * t + 1];
+  }
+  block_sum<2>(acc, sh);
+  if (threadIdx.x == 0) beta[c] = acc[1] > 1e-300 ? (float)(acc[0] / acc[1]) : 0.0f;
+}
+
+// x += beta y; t -= beta w (t may be null: the last correction of the level).
+template <int NR>
+__global__ void __launch_bounds__(kAmgThreads) k_kupdate(LvlTiles T, const int32_t* __restrict__ done,
+                                                         const float* __restrict__ beta, const float* __restrict__ y,
+                                                         const float* __restrict__ w, float* __restrict__ x,
+                                                         float* __restrict__ t) {
+  const int64_t tl = blockIdx.x;
+  const int32_t ch = T.chart[tl];
+  if (done[ch]) return;
+  const float b = beta[ch];
+  for (int64_t i = T.tab[2 * tl] + threadIdx.x; i < T.tab[2 * tl + 1]; i += blockDim.x) {
+    F<NR> xi = ldf<NR>(x, i);
+    const F<NR> yi = ldf<NR>(y, i);
+#pragma unroll
+    for (int c = 0; c < NR; ++c) xi.c[c] += b * yi.c[c];
+    stf<NR>(x, i, xi);
+    if (t) {
+      F<NR> ti = ldf<NR>(t, i);
+      const F<NR> wi = ldf<NR>(w, i);
+#pragma unroll
+      for (int c = 0; c < NR; ++c) ti.c[c] -= b * wi.c[c];
+      stf<NR>(t, i, ti);
+    }
+  }
 }
 
 // Up 2: x = y + w D^-1 (b - A y).
@@ -1027,11 +1116,12 @@ __global__ void __launch_bounds__(kDirect) k_direct_solve(const int32_t* __restr
                                                           const int64_t* const* __restrict__ lvl_chart_row,
                                                           float* const* __restrict__ lvl_b, float* const* __restrict__ lvl_x,
                                                           const float* const* __restrict__ lvl_dinv,
-                                                          const int64_t* __restrict__ fac_off, const float* __restrict__ fac) {
+                                                          const int64_t* __restrict__ fac_off, const float* __restrict__ fac,
+                                                          int lo, int hi) {
   __shared__ float bs[NR][kDirect];
   const int c = blockIdx.x;
   const int f = final_lvl[c];
-  if (f < 0 || done[c]) return;
+  if (f < lo || f > hi || done[c]) return;  // only charts whose last level is in [lo, hi]
   const int64_t r0 = lvl_chart_row[f][c];
   const int m = (int)(lvl_chart_row[f][c + 1] - r0);
   if (m <= 0) return;
@@ -1088,6 +1178,12 @@ struct AmgLevelDev {
   const int32_t* cbase = nullptr;
   LvlTiles cont{nullptr, nullptr, 0};  // tiles over rows whose chart continues below this level
   LvlTiles all{nullptr, nullptr, 0};   // tiles over every row of this level
+  // K-cycle levels: chart c's continuing tiles are [cont_chart_tile[c], cont_chart_tile[c + 1]);
+  // w = A y, the tiles' partial sums and the per-chart steplength
+  const int64_t* cont_chart_tile = nullptr;
+  float* w = nullptr;
+  double* kpart = nullptr;
+  float* kbeta = nullptr;
 };
 
 struct AmgHierarchy {
@@ -1106,6 +1202,7 @@ struct AmgHierarchy {
   std::vector<int32_t> h_final;
   int64_t total_rows = 0, total_nnz = 0;
   float alpha_c = 1.0f;
+  int k_levels = 0;  // top levels applied in the K-form (two coarse corrections with steplengths)
 };
 
 namespace {
@@ -1242,6 +1339,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   if (const char* e = std::getenv("RUV_AMG_SA_LEVELS")) H->sa_levels = smooth ? std::max(0, std::atoi(e)) : 0;
   H->alpha_c = 1.5f;  // over-correct the piecewise-constant coarse space of tentative levels
   if (const char* e = std::getenv("RUV_AMG_ALPHA")) H->alpha_c = (float)std::atof(e);
+  if (const char* e = std::getenv("RUV_AMG_KCYCLE")) H->k_levels = std::max(0, std::atoi(e));
   float strong = kStrong;  // matching candidates: couplings >= strong * the row's strongest
   if (const char* e = std::getenv("RUV_AMG_STRONG")) strong = (float)std::atof(e);
   int pmax = kPMaxRow;
@@ -1490,9 +1588,10 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     AmgLevelDev& L = H->lv[k];
     const std::string tag = "amg.v" + std::to_string(k);
     for (int which = 0; which < 2; ++which) {
-      std::vector<int64_t> tab;
+      std::vector<int64_t> tab, ctile(NC + 1, 0);
       std::vector<int32_t> tch;
       for (int64_t c = 0; c < NC; ++c) {
+        ctile[c] = (int64_t)tch.size();
         if (which == 0 && !(H->h_final[c] > k)) continue;
         for (int64_t a0 = L.h_chart_row[c]; a0 < L.h_chart_row[c + 1]; a0 += kLevelTile) {
           tab.push_back(a0);
@@ -1500,7 +1599,17 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
           tch.push_back((int32_t)c);
         }
       }
+      ctile[NC] = (int64_t)tch.size();
       const int64_t nt = (int64_t)tch.size();
+      if (which == 0 && k < H->k_levels && nt > 0) {
+        int64_t* dct = ctx.ws.get<int64_t>(tag + ".kct", NC + 1);
+        RUV_CUDA(cudaMemcpyAsync(dct, ctile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
+        RUV_CUDA(cudaStreamSynchronize(s));
+        L.cont_chart_tile = dct;
+        L.w = ctx.ws.get<float>(tag + ".kw", NR * L.n);
+        L.kpart = ctx.ws.get<double>(tag + ".kpart", 2 * nt);
+        L.kbeta = ctx.ws.get<float>(tag + ".kbeta", NC);
+      }
       int64_t* dtab = ctx.ws.get<int64_t>(tag + (which ? ".atab" : ".ctab"), 2 * nt);
       int32_t* dch = ctx.ws.get<int32_t>(tag + (which ? ".ach" : ".cch"), nt);
       if (nt > 0) {
@@ -1652,13 +1761,14 @@ int lanes_for(double avg) { return avg <= 1.5 ? 1 : avg <= 8 ? 2 : avg <= 16 ? 4
     default: CALL(16, 1, 4); break; \
   }
 
+// The V(1,1) cycle from level k0 down: x_k0 = M^-1 b_k0 for every chart with rows at k0.
 template <int NR>
-int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
+int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
   cudaStream_t s = ctx.stream;
   const int K = (int)H->lv.size();
   const int B = kAmgThreads;
   int launches = 0;
-  for (int k = 0; k + 1 < K; ++k) {
+  for (int k = k0; k + 1 < K; ++k) {
     AmgLevelDev& L = H->lv[k];
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
@@ -1683,14 +1793,10 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
 #undef CALL
     ++launches;
   }
-  if (NR == 2)
-    k_direct_solve<2><<<(unsigned)H->n_charts, kDirect, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b, H->d_lvl_x,
-                                                           H->d_lvl_dinv, H->fac_off, H->fac);
-  else
-    k_direct_solve<1><<<(unsigned)H->n_charts, kDirect, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b, H->d_lvl_x,
-                                                           H->d_lvl_dinv, H->fac_off, H->fac);
+  k_direct_solve<NR><<<(unsigned)H->n_charts, kDirect, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b,
+                                                               H->d_lvl_x, H->d_lvl_dinv, H->fac_off, H->fac, k0, kMaxLevels);
   ++launches;
-  for (int k = K - 2; k >= 0; --k) {
+  for (int k = K - 2; k >= k0; --k) {
     AmgLevelDev& L = H->lv[k];
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
@@ -1731,11 +1837,79 @@ int apply_impl(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
   return launches;
 }
 
+template <int NR>
+int cycle(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k);
+
+// Level k in the K-form (gpu/src/amg.rs:468-639), for the charts that continue below it:
+// pre-smoothing from zero (x = w D^-1 b, t = b - A x), then two coarse corrections
+// y = P (cycle of level k + 1 on R t), each scaled by its CG steplength
+// beta = (t.t) / (t.A y) per chart (x += beta y; the first also t -= beta A y), no
+// post-smoothing.  Charts whose last level is k get their direct solve.
+template <int NR>
+int kform(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k) {
+  cudaStream_t s = ctx.stream;
+  const int B = kAmgThreads;
+  AmgLevelDev& L = H->lv[k];
+  AmgLevelDev& C = H->lv[k + 1];
+  int launches = 0;
+  const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
+#define CALL(X, UU, KK)                                                                                                \
+  k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
+                                                                    L.dinv, L.b, L.x, L.t)
+  if (L.c16) {
+    constexpr bool NW = true;
+    RUV_LPR_SWITCH(la, CALL)
+  } else {
+    constexpr bool NW = false;
+    RUV_LPR_SWITCH(la, CALL)
+  }
+#undef CALL
+  ++launches;
+  const int lr = lanes_for(C.n ? (double)L.n_pnnz / (double)C.n : 1.0);
+  const int lp = lanes_for(L.n ? (double)L.n_pnnz / (double)L.n : 1.0);
+  for (int step = 0; step < 2; ++step) {
+#define CALL(X, UU, KK) k_restrict<NR, X, UU, KK><<<(unsigned)C.all.n, B, 0, s>>>(C.all, done, L.roff, L.rc, L.rv, L.t, C.b)
+    RUV_LPR_SWITCH(lr, CALL)
+#undef CALL
+    ++launches;
+    launches += cycle<NR>(ctx, H, done, k + 1);
+#define CALL(X, UU, KK)                                                                                                  \
+  k_prolong_add<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.poff, L.pc, L.pv, C.x, nullptr, L.y, 1.0f)
+    RUV_LPR_SWITCH(lp, CALL)
+#undef CALL
+#define CALL(X, UU, KK)                                                                                           \
+  k_kspmv<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, L.y, \
+                                                              L.t, L.w, L.kpart)
+    if (L.c16) {
+      constexpr bool NW = true;
+      RUV_LPR_SWITCH(la, CALL)
+    } else {
+      constexpr bool NW = false;
+      RUV_LPR_SWITCH(la, CALL)
+    }
+#undef CALL
+    k_kbeta<<<(unsigned)H->n_charts, 128, 0, s>>>(done, L.cont_chart_tile, L.kpart, L.kbeta);
+    k_kupdate<NR><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.kbeta, L.y, L.w, L.x, step == 0 ? L.t : nullptr);
+    launches += 4;
+  }
+  k_direct_solve<NR><<<(unsigned)H->n_charts, kDirect, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b,
+                                                               H->d_lvl_x, H->d_lvl_dinv, H->fac_off, H->fac, k, k);
+  return launches + 1;
+}
+
+template <int NR>
+int cycle(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k) {
+  const int K = (int)H->lv.size();
+  if (k < H->k_levels && k + 1 < K && H->lv[k].cont.n > 0 && H->lv[k].kbeta) return kform<NR>(ctx, H, done, k);
+  return vtail<NR>(ctx, H, done, k);
+}
+
 }  // namespace
 
-// One V(1,1) cycle: z0 = M^-1 r0 for every chart not marked done (launches only; capturable).
+// One cycle (V(1,1), or the K-form on the top RUV_AMG_KCYCLE levels): z0 = M^-1 r0 for every
+// chart not marked done (launches only; capturable).
 int amg_apply(Ctx& ctx, AmgHierarchy* H, const int32_t* done) {
-  return H->nrhs == 2 ? apply_impl<2>(ctx, H, done) : apply_impl<1>(ctx, H, done);
+  return H->nrhs == 2 ? cycle<2>(ctx, H, done, 0) : cycle<1>(ctx, H, done, 0);
 }
 
 namespace {

@@ -941,6 +941,22 @@ ruv_status ruv_prepare_patches(int64_t n_patches, const int64_t* vert_off, const
   }
 }
 
+ruv_status ruv_prepare_patches_gpu(ruv_ctx* ctx, int64_t n_patches, const int64_t* vert_off, const int64_t* tri_off,
+                                   const double* p3, const int32_t* tris, int32_t threads, ruv_prepared** out) {
+  if (!ctx || !out || n_patches < 0 || !vert_off || !tri_off) return RUV_ERR_BAD_INPUT;
+  if ((vert_off[n_patches] > 0 && !p3) || (tri_off[n_patches] > 0 && !tris)) return RUV_ERR_BAD_INPUT;
+  if (vert_off[n_patches] >= (int64_t)INT32_MAX || tri_off[n_patches] >= (int64_t)INT32_MAX / 3) return RUV_ERR_BAD_INPUT;
+  *out = nullptr;
+  return guarded(ctx, [&]() -> ruv_status {
+    std::unique_ptr<ruv_prepared> p(new ruv_prepared());
+    std::string err;
+    ruv_status s = prepare_patches_gpu(ctx->c, n_patches, vert_off, tri_off, p3, tris, threads, p->p, err);
+    if (s != RUV_OK) return fail(ctx, s, err.empty() ? "patch preparation failed" : err);
+    *out = p.release();
+    return RUV_OK;
+  });
+}
+
 void ruv_prepared_free(ruv_prepared* p) { delete p; }
 
 ruv_status ruv_prepared_batch(const ruv_prepared* p, ruv_lscm_batch* v) {

@@ -15,6 +15,19 @@
 // 1e-12 * max(|a_ii|, 1e-30), FP64 with each operation rounded on its own (no FMA
 // contraction).  The mixed-precision solver applies an FP32 copy of it.
 //
+// Large charts with many levels (natural ordering of a big grid-like chart: thousands of
+// levels, ~1000 rows each) would leave one CTA per chart walking its levels serially.  There
+// the factorization and both sweeps run sync-free over the whole GPU instead ("tickets"):
+// rows are numbered in global level order, persistent warps take 32 consecutive numbers at a
+// time from an atomic counter, and each thread waits on the done-flags of its row's
+// dependencies (acquire loads) before computing the row and publishing it (release store).
+// A row only waits on rows with smaller numbers, which were taken earlier by warps that are
+// running, so the scheme needs no co-residency of the grid.  Every wait is bounded (a spin
+// limit, RUV_SPIN_LIMIT iterations of a short sleep, about a second by default); a wait that
+// runs out sets an error flag that ends every other wait at once, and the call reports
+// RUV_ERR_TIMEOUT with the context still usable.  Each row's arithmetic is the same as in
+// the per-chart path, so the results are bit-identical to it.
+//
 // Multi-colour ordering: the greedy colouring (smallest colour not taken by a lower-numbered
 // neighbour, vertices in index order) depends on lower neighbours only, so it is computed on
 // the same forward levels and equals the reference's sequential result.  The colour-major
@@ -22,6 +35,7 @@
 // the host; P A P^T is formed on the device and factored as above.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <memory>
 
 #include "system.cuh"
@@ -400,6 +414,130 @@ __global__ void k_permute(int64_t n, const int32_t* __restrict__ to_orig, const 
   else stvec<S, NR>(out, o, ldvec<S, NR>(in, p));
 }
 
+// ---------------------------------------------------------------- sync-free (ticket) kernels
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Wait until flag == ep; false (and the error flag set) when the spin limit runs out or
+// another wait has already failed.
+__device__ __forceinline__ bool wait_ready(const int* flag, int ep, int* err, int64_t limit) {
+  for (int64_t it = 0;; ++it) {
+    if (ld_acquire(flag) == ep) return true;
+    if (it >= limit || ld_relaxed(err) != 0) {
+      atomicOr(err, 1);
+      return false;
+    }
+    __nanosleep(64);
+  }
+}
+
+// Per sweep: the next epoch (the value a finished row's flag takes) and a fresh ticket counter.
+__global__ void k_ticket_begin(int* __restrict__ epoch, int* __restrict__ ticket) {
+  *epoch += 1;
+  *ticket = 0;
+}
+
+// 32 consecutive tickets for the calling warp; n or more when none are left.
+__device__ __forceinline__ int64_t take_tickets(int* ticket) {
+  int t0 = 0;
+  if ((threadIdx.x & 31) == 0) t0 = atomicAdd(ticket, 32);
+  return (int64_t)__shfl_sync(0xffffffffu, t0, 0);
+}
+
+// The factorization of k_factor over the rows in ticket order (forward dependencies).
+__global__ void __launch_bounds__(kIcThreads) k_factor_ticket(const int32_t* __restrict__ order, int64_t n,
+                                                              const int64_t* __restrict__ lptr, const int32_t* __restrict__ lc,
+                                                              double* lv, int* __restrict__ ready, const int* __restrict__ epoch,
+                                                              int* __restrict__ ticket, int* __restrict__ err, int64_t limit,
+                                                              int* __restrict__ flags) {
+  const int ep = *epoch;
+  for (;;) {
+    const int64_t t0 = take_tickets(ticket);
+    if (t0 >= n) return;
+    const int64_t t = t0 + (threadIdx.x & 31);
+    if (t >= n) continue;
+    const int32_t i = order[t];
+    const int64_t b = lptr[i], d = lptr[i + 1] - 1;
+    bool ok = true;
+    for (int64_t e = b; e < d && ok; ++e) {
+      const int32_t k = lc[e];
+      if (!wait_ready(ready + k, ep, err, limit)) {
+        ok = false;
+        break;
+      }
+      double s = lv[e];
+      const int64_t kb = lptr[k], kd = lptr[k + 1] - 1;
+      int64_t q = kb;
+      for (int64_t p = b; p < e; ++p) {
+        const int32_t j = lc[p];
+        while (q < kd && lc[q] < j) ++q;
+        if (q < kd && lc[q] == j) s = __dsub_rn(s, __dmul_rn(lv[p], __ldcg(lv + q)));
+      }
+      const double l_kk = __ldcg(lv + kd);
+      if (!(fabs(l_kk) >= 1e-300)) atomicOr(flags, 8);
+      lv[e] = __ddiv_rn(s, l_kk);
+    }
+    if (!ok) continue;
+    const double a_ii = lv[d];
+    double sum = a_ii;
+    for (int64_t e = b; e < d; ++e) sum = __dsub_rn(sum, __dmul_rn(lv[e], lv[e]));
+    const double fl = 1e-12 * fmax(fabs(a_ii), 1e-30);
+    if (sum < fl) sum = fl;
+    lv[d] = __dsqrt_rn(sum);
+    st_release(ready + i, ep);  // the row's entries are visible to every later acquire of its flag
+  }
+}
+
+// One triangular sweep of k_sweep over the rows in ticket order (rows of charts marked done
+// are skipped; their dependents are in the same chart).
+template <class S, int NR>
+__global__ void __launch_bounds__(kIcThreads) k_sweep_ticket(const int32_t* __restrict__ order, int64_t n,
+                                                             const int32_t* __restrict__ row_chart,
+                                                             const int32_t* __restrict__ done, const int64_t* __restrict__ ptr,
+                                                             const int32_t* __restrict__ col, const S* __restrict__ val,
+                                                             const S* __restrict__ in, S* out, int* __restrict__ ready,
+                                                             const int* __restrict__ epoch, int* __restrict__ ticket,
+                                                             int* __restrict__ err, int64_t limit) {
+  const int ep = *epoch;
+  for (;;) {
+    const int64_t t0 = take_tickets(ticket);
+    if (t0 >= n) return;
+    const int64_t t = t0 + (threadIdx.x & 31);
+    if (t >= n) continue;
+    const int32_t i = order[t];
+    if (done && done[row_chart[i]]) continue;
+    const int64_t b = ptr[i], d = ptr[i + 1] - 1;
+    Vec<S, NR> s = ldvec<S, NR>(in, i);
+    bool ok = true;
+    for (int64_t e = b; e < d; ++e) {
+      const int32_t j = col[e];
+      if (!wait_ready(ready + j, ep, err, limit)) {
+        ok = false;
+        break;
+      }
+      const S a = val[e];
+#pragma unroll
+      for (int k = 0; k < NR; ++k) s.c[k] -= a * __ldcg(out + (int64_t)NR * j + k);
+    }
+    if (!ok) continue;
+    const S dg = val[d];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) __stcg(out + (int64_t)NR * i + k, s.c[k] / dg);
+    st_release(ready + i, ep);
+  }
+}
+
 // ---------------------------------------------------------------- host side
 struct Factor {
   int64_t n = 0, nnz = 0;
@@ -414,12 +552,26 @@ struct Factor {
   // global levels (when chosen): rows by level, host offsets per level
   int32_t *fgrows = nullptr, *bgrows = nullptr, *row_chart = nullptr;
   std::vector<int32_t> foff, boff;
+  // sync-free ticket kernels (when chosen): rows in global level order are fgrows / bgrows
+  bool tickets = false;
+  int* ready = nullptr;  // per row: the epoch of the sweep that finished it
+  int* tick = nullptr;   // [0] epoch, [1] ticket counter, [2] error (a wait ran out)
+  int64_t spin_limit = 0;
+  unsigned ticket_grid = 0;
 };
 
-// Few, wide levels run as one launch per level over all charts; otherwise one CTA per chart
-// walks its own levels.
+// Few, wide levels run as one launch per level over all charts; many levels on a large chart
+// run sync-free over the whole GPU (tickets); otherwise one CTA per chart walks its own levels.
 constexpr int kGlobalMaxLevels = 64;
 constexpr int64_t kGlobalMinRows = 32768;
+constexpr int kTicketMinLevels = 256;
+// iterations of a ~64 ns sleep before a dependency wait gives up (about a second)
+constexpr int64_t kSpinLimit = int64_t(1) << 24;
+
+int64_t spin_limit() {
+  const char* e = std::getenv("RUV_SPIN_LIMIT");
+  return e ? std::max<int64_t>(1, std::atoll(e)) : kSpinLimit;
+}
 
 // Pattern, transpose and both level tables of the IC(0) factor of `sys` (values not yet
 // factored).  Buffers are workspace entries under `tag`.
@@ -483,7 +635,9 @@ Factor factor_pattern(Ctx& ctx, const DevSystem& sys, const std::string& tag, in
     }
   }
   RUV_LAUNCH_CHECK();
-  if (F.max_levels > 0 && F.max_levels <= kGlobalMaxLevels && F.max_chart_rows >= kGlobalMinRows) {
+  const char* te = std::getenv("RUV_IC0_TICKETS");
+  F.tickets = te ? te[0] == '1' : (F.max_levels > kTicketMinLevels && F.max_chart_rows >= kGlobalMinRows);
+  if (F.tickets || (F.max_levels > 0 && F.max_levels <= kGlobalMaxLevels && F.max_chart_rows >= kGlobalMinRows)) {
     int32_t* row_level = ws.get<int32_t>(tag + ".rlev", N);
     int32_t* hist = ws.get<int32_t>(tag + ".hist", F.max_levels);
     F.row_chart = ws.get<int32_t>(tag + ".rchart", N);
@@ -511,12 +665,47 @@ Factor factor_pattern(Ctx& ctx, const DevSystem& sys, const std::string& tag, in
     }
     RUV_LAUNCH_CHECK();
   }
+  if (F.tickets && N > 0) {
+    F.ready = ws.get<int>(tag + ".ready", N);
+    F.tick = ws.get<int>(tag + ".tick", 4);
+    RUV_CUDA(cudaMemsetAsync(F.ready, 0, sizeof(int) * N, s));
+    RUV_CUDA(cudaMemsetAsync(F.tick, 0, sizeof(int) * 4, s));
+    F.spin_limit = spin_limit();
+    // enough warps for a few levels in flight (the widest level's rows, 4 times over), at
+    // least one CTA per SM, at most 8
+    int32_t widest = 0;
+    for (size_t l = 0; l + 1 < F.foff.size(); ++l) widest = std::max(widest, F.foff[l + 1] - F.foff[l]);
+    for (size_t l = 0; l + 1 < F.boff.size(); ++l) widest = std::max(widest, F.boff[l + 1] - F.boff[l]);
+    const int64_t want = div_up(4 * (int64_t)widest, kIcThreads);
+    F.ticket_grid = (unsigned)std::min<int64_t>(8 * (int64_t)ctx.sm_count, std::max<int64_t>(ctx.sm_count, want));
+  } else {
+    F.tickets = false;
+  }
   return F;
+}
+
+// Throws RUV_ERR_TIMEOUT when a ticket kernel's dependency wait ran out.
+void check_ticket_error(Ctx& ctx, const Factor& F) {
+  if (!F.tickets) return;
+  int h = 0;
+  RUV_CUDA(cudaMemcpyAsync(&h, F.tick + 2, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+  RUV_CUDA(cudaStreamSynchronize(ctx.stream));
+  if (h) {
+    RUV_CUDA(cudaMemsetAsync(F.tick + 2, 0, sizeof(int), ctx.stream));
+    throw Error{RUV_ERR_TIMEOUT, "IC(0): a dependency wait of the sync-free sweep ran out (RUV_SPIN_LIMIT)"};
+  }
 }
 
 void factor_values(Ctx& ctx, const DevSystem& sys, Factor& F, int* flags) {
   cudaStream_t s = ctx.stream;
-  if (sys.n_charts > 0) {
+  if (F.tickets) {
+    k_ticket_begin<<<1, 1, 0, s>>>(F.tick, F.tick + 1);
+    k_factor_ticket<<<F.ticket_grid, kIcThreads, 0, s>>>(F.fgrows, F.n, F.lptr, F.lc, F.lv, F.ready, F.tick, F.tick + 1,
+                                                           F.tick + 2, F.spin_limit, flags);
+    count_launches(2);
+    RUV_LAUNCH_CHECK();
+    check_ticket_error(ctx, F);
+  } else if (sys.n_charts > 0) {
     k_factor<<<(unsigned)sys.n_charts, kIcThreads, 0, s>>>(sys.chart_row, F.frows, F.flev, F.fnl, F.lptr, F.lc, F.lv, flags);
     count_launches(1);
   }
@@ -623,6 +812,7 @@ class Ic0Precond final : public SepPrecond {
     if (fp64_) return nrhs_ == 2 ? run<double, 2>(ctx, done) : run<double, 1>(ctx, done);
     return nrhs_ == 2 ? run<float, 2>(ctx, done) : run<float, 1>(ctx, done);
   }
+  const int* error_flag() const override { return F_.tickets ? F_.tick + 2 : nullptr; }
   int levels() const { return F_.max_levels; }
   int colours() const { return n_colours_; }
   const Factor& factor() const { return F_; }
@@ -648,7 +838,17 @@ class Ic0Precond final : public SepPrecond {
       k_permute<S, NR, true><<<g, 256, 0, s>>>(n_, to_orig_, r, rin);
       ++launches;
     }
-    if (F_.fgrows) {
+    if (F_.tickets) {
+      k_ticket_begin<<<1, 1, 0, s>>>(F_.tick, F_.tick + 1);
+      k_sweep_ticket<S, NR><<<F_.ticket_grid, kIcThreads, 0, s>>>(F_.fgrows, n_, F_.row_chart, done, F_.lptr, F_.lc, lv,
+                                                                  rin, y, F_.ready, F_.tick, F_.tick + 1, F_.tick + 2,
+                                                                  F_.spin_limit);
+      k_ticket_begin<<<1, 1, 0, s>>>(F_.tick, F_.tick + 1);
+      k_sweep_ticket<S, NR><<<F_.ticket_grid, kIcThreads, 0, s>>>(F_.bgrows, n_, F_.row_chart, done, F_.tptr, F_.tc, tv,
+                                                                  y, zout, F_.ready, F_.tick, F_.tick + 1, F_.tick + 2,
+                                                                  F_.spin_limit);
+      launches += 4;
+    } else if (F_.fgrows) {
       for (int l = 0; l + 1 < (int)F_.foff.size(); ++l) {
         const int32_t cnt = F_.foff[l + 1] - F_.foff[l];
         if (cnt == 0) continue;
@@ -708,6 +908,7 @@ void ic0_apply_once(Ctx& ctx, const DevSystem& sys, const double* d_r, double* d
   count_launches(P.apply(ctx, nullptr));
   RUV_LAUNCH_CHECK();
   RUV_CUDA(cudaStreamSynchronize(ctx.stream));
+  check_ticket_error(ctx, P.factor());
   if (fwd_levels) *fwd_levels = P.levels();
 }
 

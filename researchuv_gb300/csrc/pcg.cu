@@ -1006,7 +1006,7 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
   k_chart_init<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, o.tol, 0, n_active);  // (rz replaced below)
   count_launches(1);
   RUV_LAUNCH_CHECK();
-  int* h_active = static_cast<int*>(ctx.pinned.get(sizeof(int)));
+  int* h_active = static_cast<int*>(ctx.pinned.get(2 * sizeof(int)));
   RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   RUV_CUDA(cudaStreamSynchronize(s));
   if (*h_active > 0 && NTL > 0) {
@@ -1067,13 +1067,19 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
       throw Error{RUV_ERR_LAUNCH, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
     }
     int64_t launched = 0;
+    const int* perr = P.error_flag();
     try {
       while (launched < o.max_iter + kRep) {
         RUV_CUDA(cudaGraphLaunch(exec, s));
         count_launches((int64_t)kRep * per_iter);
         launched += kRep;
         RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+        if (perr) RUV_CUDA(cudaMemcpyAsync(h_active + 1, perr, sizeof(int), cudaMemcpyDeviceToHost, s));
         RUV_CUDA(cudaStreamSynchronize(s));
+        if (perr && h_active[1] != 0) {
+          RUV_CUDA(cudaMemsetAsync(const_cast<int*>(perr), 0, sizeof(int), s));
+          throw Error{RUV_ERR_TIMEOUT, "preconditioner: a bounded device-side wait ran out"};
+        }
         if (*h_active <= 0) break;
       }
     } catch (...) {

@@ -245,6 +245,17 @@ void jacobi_eig3(double a[3][3], double w[3], double v[3][3]) {
   w[2] = a[2][2];
 }
 
+// lscm.rs:165-178 — the two dominant principal directions of a covariance matrix (eig3, then
+// the eigenvalues in descending total order, ties in index order).
+void frame_axes(double cm[3][3], D3& e1, D3& e2) {
+  double w[3], v[3][3];
+  jacobi_eig3(cm, w, v);
+  int idx[3] = {0, 1, 2};
+  std::stable_sort(idx, idx + 3, [&](int a, int b) { return total_order_key(w[b]) < total_order_key(w[a]); });
+  e1 = D3{v[0][idx[0]], v[1][idx[0]], v[2][idx[0]]};
+  e2 = D3{v[0][idx[1]], v[1][idx[1]], v[2][idx[1]]};
+}
+
 // lscm.rs:152-183 — projection on the two dominant principal directions.
 template <class Get>
 void pca_project(int64_t n, Get get, double* out_uv) {
@@ -259,12 +270,8 @@ void pca_project(int64_t n, Get get, double* out_uv) {
     for (int r = 0; r < 3; ++r)
       for (int s = 0; s < 3; ++s) cm[r][s] += e[r] * e[s];
   }
-  double w[3], v[3][3];
-  jacobi_eig3(cm, w, v);
-  int idx[3] = {0, 1, 2};
-  std::stable_sort(idx, idx + 3, [&](int a, int b) { return total_order_key(w[b]) < total_order_key(w[a]); });
-  D3 e1{v[0][idx[0]], v[1][idx[0]], v[2][idx[0]]};
-  D3 e2{v[0][idx[1]], v[1][idx[1]], v[2][idx[1]]};
+  D3 e1, e2;
+  frame_axes(cm, e1, e2);
   for (int64_t i = 0; i < n; ++i) {
     D3 d = get(i) - c;
     out_uv[2 * i] = dot3(d, e1);
@@ -339,33 +346,42 @@ void chart_sets(const MeshView& m, ChartOut& ch) {
           (int32_t)(std::lower_bound(ch.verts.begin(), ch.verts.end(), F[3 * ch.faces[t] + k]) - ch.verts.begin());
 }
 
-// everything after the vertex set: border, area, loops, frame, pins
-void chart_finish(const MeshView& m, ChartOut& ch) {
-  const auto& F = m.F;
-  auto local = [&](int32_t v) -> int32_t {
-    return (int32_t)(std::lower_bound(ch.verts.begin(), ch.verts.end(), v) - ch.verts.begin());
-  };
-  // border vertices and boundary edge set (segment.rs:198-209, :235-244)
-  std::vector<uint64_t> bedges;
+// The border vertices (sorted, unique) and boundary edges (key min << 32 | max, sorted, unique)
+// of a chart from its border face slots' edges (x, y) in chart face order
+// (segment.rs:198-209, :235-244).
+void chart_border_set(ChartOut& ch, std::vector<uint64_t>& bedges) {
   ch.border.clear();
-  for (int32_t f : ch.faces)
-    for (int k = 0; k < 3; ++k)
-      if (slot_is_border(m, 3 * (int64_t)f + k)) {
-        uint32_t x = (uint32_t)F[3 * f + k], y = (uint32_t)F[3 * f + (k + 1) % 3];
-        ch.border.push_back((int32_t)x);
-        ch.border.push_back((int32_t)y);
-        uint32_t a = std::min(x, y), b = std::max(x, y);
-        bedges.push_back(((uint64_t)a << 32) | b);
-      }
+  for (uint64_t e : bedges) {
+    ch.border.push_back((int32_t)(uint32_t)(e >> 32));
+    ch.border.push_back((int32_t)(uint32_t)e);
+  }
   std::sort(ch.border.begin(), ch.border.end());
   ch.border.erase(std::unique(ch.border.begin(), ch.border.end()), ch.border.end());
   std::sort(bedges.begin(), bedges.end());
   bedges.erase(std::unique(bedges.begin(), bedges.end()), bedges.end());
+}
+
+// border vertices and boundary edges of a chart, and its area (segment.rs:198-212)
+void chart_border(const MeshView& m, ChartOut& ch, std::vector<uint64_t>& bedges) {
+  const auto& F = m.F;
+  bedges.clear();
+  for (int32_t f : ch.faces)
+    for (int k = 0; k < 3; ++k)
+      if (slot_is_border(m, 3 * (int64_t)f + k)) {
+        uint32_t x = (uint32_t)F[3 * f + k], y = (uint32_t)F[3 * f + (k + 1) % 3];
+        uint32_t a = std::min(x, y), b = std::max(x, y);
+        bedges.push_back(((uint64_t)a << 32) | b);
+      }
+  chart_border_set(ch, bedges);
   // area (segment.rs:212): sum in chart face order
   double area = 0.0;
   for (int32_t f : ch.faces) area += m.farea[f];
   ch.area3d = area;
-  // border loops: keep-going-straight walk (segment.rs:245-330)
+}
+
+// border loops: keep-going-straight walk (segment.rs:245-330) over the boundary edges;
+// positions by source vertex id
+void chart_loops(const D3* pos, ChartOut& ch, const std::vector<uint64_t>& bedges) {
   ch.loop_len.clear();
   ch.loop_ids.clear();
   if (!bedges.empty()) {
@@ -415,7 +431,7 @@ void chart_finish(const MeshView& m, ChartOut& ch) {
           if (n != prev && !used[eidx(now, n)]) nxts.push_back((int32_t)n);
         }
         if (nxts.empty()) break;
-        D3 din = m.pos[now] - m.pos[prev];
+        D3 din = pos[now] - pos[prev];
         double ln = norm3(din);
         uint32_t next = (uint32_t)nxts[0];
         if (!(ln < 1e-30)) {
@@ -423,7 +439,7 @@ void chart_finish(const MeshView& m, ChartOut& ch) {
           bool have = false;
           double best = 0.0;
           for (int32_t n : nxts) {
-            double d = dot3(m.pos[n] - m.pos[now], din);
+            double d = dot3(pos[n] - pos[now], din);
             if (!have || !(d <= best)) {  // the first maximum wins (segment.rs:307-310)
               have = true;
               best = d;
@@ -443,17 +459,29 @@ void chart_finish(const MeshView& m, ChartOut& ch) {
       }
     }
   }
-  // positions and tangent frame (lscm.rs:513-516)
+}
+
+// positions and tangent frame of a chart (lscm.rs:513-516)
+void chart_frame(const D3* pos, ChartOut& ch) {
   int64_t nv = (int64_t)ch.verts.size();
   ch.p3.resize(3 * nv);
   for (int64_t i = 0; i < nv; ++i) {
-    D3 p = m.pos[ch.verts[i]];
+    D3 p = pos[ch.verts[i]];
     ch.p3[3 * i] = p.x;
     ch.p3[3 * i + 1] = p.y;
     ch.p3[3 * i + 2] = p.z;
   }
   ch.p2.resize(2 * nv);
-  pca_project(nv, [&](int64_t i) { return m.pos[ch.verts[i]]; }, ch.p2.data());
+  pca_project(nv, [&](int64_t i) { return pos[ch.verts[i]]; }, ch.p2.data());
+}
+
+// pins of a chart (lscm.rs:524-542): 4 anchors of a closed chart (needs ch.p3, ch.p2) or
+// the border rectangle pass over its loops; positions by source vertex id
+void chart_pins(const D3* pos, ChartOut& ch) {
+  auto local = [&](int32_t v) -> int32_t {
+    return (int32_t)(std::lower_bound(ch.verts.begin(), ch.verts.end(), v) - ch.verts.begin());
+  };
+  const int64_t nv = (int64_t)ch.verts.size();
   // pins (lscm.rs:524-542)
   ch.pinned.assign(nv, 0);
   ch.pin_uv.assign(2 * nv, 0.0);
@@ -510,7 +538,7 @@ void chart_finish(const MeshView& m, ChartOut& ch) {
     const int32_t* L = ch.loop_ids.data() + loff[l];
     int64_t len = ch.loop_len[l];
     std::vector<double> seg(len > 0 ? len - 1 : 0);
-    for (int64_t w = 0; w + 1 < len; ++w) seg[w] = norm3(m.pos[L[w + 1]] - m.pos[L[w]]);
+    for (int64_t w = 0; w + 1 < len; ++w) seg[w] = norm3(pos[L[w + 1]] - pos[L[w]]);
     double total = 0.0;
     for (double s : seg) total += s;
     perim[l] = total;
@@ -543,11 +571,11 @@ void chart_finish(const MeshView& m, ChartOut& ch) {
       // pins is a map (later inserts overwrite): emulate by writing in reference order
       for (int64_t k = 0; k < n0; ++k) set_pin(L0[k], -w / 2.0 + w * fracs[0][k], h / 2.0);
       for (int64_t k1 = 0; k1 < n1; ++k1) {
-        D3 p1 = m.pos[L1[k1]];
+        D3 p1 = pos[L1[k1]];
         int64_t best = 0;
         double bd = std::numeric_limits<double>::infinity();
         for (int64_t k0 = 0; k0 < n0; ++k0) {
-          double d = norm3(m.pos[L0[k0]] - p1);
+          double d = norm3(pos[L0[k0]] - p1);
           if (d < bd) {
             bd = d;
             best = k0;
@@ -572,12 +600,12 @@ void chart_finish(const MeshView& m, ChartOut& ch) {
   } else {
     // multi-loop similarity scale (lscm.rs:351-384)
     D3 c{0.0, 0.0, 0.0};
-    for (int32_t v : ch.verts) c = c + m.pos[v];
+    for (int32_t v : ch.verts) c = c + pos[v];
     c = c / (double)std::max<int64_t>(nv, 1);
     std::vector<double> dist(nl);
     for (size_t l = 0; l < nl; ++l) {
       double s = 0.0;
-      for (int64_t k = 0; k < ch.loop_len[l]; ++k) s += norm3(m.pos[ch.loop_ids[loff[l] + k]] - c);
+      for (int64_t k = 0; k < ch.loop_len[l]; ++k) s += norm3(pos[ch.loop_ids[loff[l] + k]] - c);
       dist[l] = s / (double)std::max<int64_t>(ch.loop_len[l], 1);
     }
     std::vector<size_t> order(nl);
@@ -600,7 +628,7 @@ void chart_finish(const MeshView& m, ChartOut& ch) {
     int64_t nverts = closed ? len - 1 : len;
     // winding of the 3-D walk in its own tangent frame (lscm.rs:394-406)
     lp2.assign(2 * len, 0.0);
-    pca_project(len, [&](int64_t i) { return m.pos[L[i]]; }, lp2.data());
+    pca_project(len, [&](int64_t i) { return pos[L[i]]; }, lp2.data());
     double sa3 = 0.0;
     for (int64_t i = 0; i < len; ++i) {
       int64_t j = (i + 1) % len;
@@ -614,6 +642,15 @@ void chart_finish(const MeshView& m, ChartOut& ch) {
       set_pin(L[k], uv[0], uv[1]);
     }
   }
+}
+
+// everything after the vertex set: border, area, loops, frame, pins
+void chart_finish(const MeshView& m, ChartOut& ch) {
+  std::vector<uint64_t> bedges;
+  chart_border(m, ch, bedges);
+  chart_loops(m.pos.data(), ch, bedges);
+  chart_frame(m.pos.data(), ch);
+  chart_pins(m.pos.data(), ch);
 }
 
 void pack_charts(std::vector<ChartOut>& charts, Prepared& P) {
@@ -1216,6 +1253,7 @@ ruv_status prepare_patches(int64_t np, const int64_t* vert_off, const int64_t* t
       err = "offsets must be non-decreasing";
       return RUV_ERR_BAD_INPUT;
     }
+  StageClock clk;
   int64_t NV = vert_off[np], NT = tri_off[np];
   std::vector<D3> pos(NV);
   for (int64_t i = 0; i < NV; ++i) pos[i] = {p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]};
@@ -1239,7 +1277,9 @@ ruv_status prepare_patches(int64_t np, const int64_t* vert_off, const int64_t* t
   }
   P.mesh_pos.assign(p3, p3 + 3 * NV);
   P.mesh_faces.assign(F.begin(), F.end());
+  clk.mark("patch copy/validate");
   EdgeFaces ef = build_edge_faces(NV, F, threads);
+  clk.mark("edge faces");
   std::vector<uint8_t> cut(3 * NT, 0);  // no segmentation: only mesh-boundary edges are border
   P.n_cut_slots = 0;
   // faces of each patch in the reference's DFS pop order (segment.rs:150-175), so a
@@ -1271,7 +1311,9 @@ ruv_status prepare_patches(int64_t np, const int64_t* vert_off, const int64_t* t
       }
     }
   });
+  clk.mark("dfs");
   std::vector<double> farea = face_areas(pos, F, threads);
+  clk.mark("face areas");
   MeshView mv{pos, F, ef, cut, farea};
   std::vector<int64_t> order(np);
   for (int64_t i = 0; i < np; ++i) order[i] = i;
@@ -1281,7 +1323,9 @@ ruv_status prepare_patches(int64_t np, const int64_t* vert_off, const int64_t* t
     chart_sets(mv, charts[order[i]]);
     chart_finish(mv, charts[order[i]]);
   });
+  clk.mark("sets + finish");
   pack_charts(charts, P);
+  clk.mark("pack");
   // a patch's vertices that no triangle uses would be dropped by the vertex set; require
   // every patch vertex to be used so the packed layout equals the caller's
   for (int64_t c = 0; c < np; ++c)
@@ -1289,6 +1333,127 @@ ruv_status prepare_patches(int64_t np, const int64_t* vert_off, const int64_t* t
       err = "patch " + std::to_string(c) + " has vertices no triangle uses";
       return RUV_ERR_BAD_INPUT;
     }
+  return RUV_OK;
+}
+
+ruv_status prepare_patches_device(int64_t np, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
+                                  const int32_t* tris, int threads, const PatchDeviceFn& dev, const PatchProjectFn& proj,
+                                  Prepared& P, std::string& err) {
+  if (np < 0 || vert_off[0] != 0 || tri_off[0] != 0) {
+    err = "offsets must start at 0";
+    return RUV_ERR_BAD_INPUT;
+  }
+  for (int64_t c = 0; c < np; ++c)
+    if (vert_off[c + 1] < vert_off[c] || tri_off[c + 1] < tri_off[c]) {
+      err = "offsets must be non-decreasing";
+      return RUV_ERR_BAD_INPUT;
+    }
+  StageClock clk;
+  const int64_t NV = vert_off[np], NT = tri_off[np];
+  PatchDevice D;
+  ruv_status st = dev(D, err);
+  if (st != RUV_OK) return st;
+  clk.mark("device stages");
+  const D3* pos = reinterpret_cast<const D3*>(p3);
+  std::vector<ChartOut> charts(np);
+  std::vector<double> frames(9 * np, 0.0);
+  std::vector<int64_t> order(np);
+  for (int64_t i = 0; i < np; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+    return D.boff[a + 1] - D.boff[a] > D.boff[b + 1] - D.boff[b];
+  });
+  parallel_for(np, threads, [&](int64_t i) {
+    const int64_t c = order[i];
+    ChartOut& ch = charts[c];
+    std::vector<uint64_t> bedges(D.bkeys.begin() + D.boff[c], D.bkeys.begin() + D.boff[c + 1]);
+    chart_border_set(ch, bedges);
+    ch.area3d = D.area3d[c];
+    chart_loops(pos, ch, bedges);
+    double cm[3][3];
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) cm[r][q] = D.cov[12 * c + 3 + 3 * r + q];
+    D3 e1, e2;
+    if (vert_off[c + 1] > vert_off[c]) frame_axes(cm, e1, e2);
+    else e1 = e2 = D3{0.0, 0.0, 0.0};
+    double* fr = frames.data() + 9 * c;
+    fr[0] = D.cov[12 * c];
+    fr[1] = D.cov[12 * c + 1];
+    fr[2] = D.cov[12 * c + 2];
+    fr[3] = e1.x;
+    fr[4] = e1.y;
+    fr[5] = e1.z;
+    fr[6] = e2.x;
+    fr[7] = e2.y;
+    fr[8] = e2.z;
+  });
+  clk.mark("borders + loops + axes");
+  P.p2.resize(2 * NV);
+  st = proj(frames, P.p2, err);
+  if (st != RUV_OK) return st;
+  clk.mark("projection");
+  // pins (the closed charts' anchors read the chart's p3 and p2)
+  P.pinned.resize(NV);
+  P.pin_uv.resize(2 * NV);
+  parallel_for(np, threads, [&](int64_t i) {
+    const int64_t c = order[i];
+    ChartOut& ch = charts[c];
+    const int64_t v0 = vert_off[c], nv = vert_off[c + 1] - v0;
+    ch.verts.resize(nv);
+    for (int64_t k = 0; k < nv; ++k) ch.verts[k] = (int32_t)(v0 + k);
+    if (ch.loop_len.empty()) {
+      ch.p3.assign(p3 + 3 * v0, p3 + 3 * (v0 + nv));
+      ch.p2.assign(P.p2.begin() + 2 * v0, P.p2.begin() + 2 * (v0 + nv));
+    }
+    chart_pins(pos, ch);
+    std::copy(ch.pinned.begin(), ch.pinned.end(), P.pinned.begin() + v0);
+    std::copy(ch.pin_uv.begin(), ch.pin_uv.end(), P.pin_uv.begin() + 2 * v0);
+    std::vector<int32_t>().swap(ch.verts);
+    std::vector<uint8_t>().swap(ch.pinned);
+    std::vector<double>().swap(ch.pin_uv);
+  });
+  clk.mark("pins");
+  // packing: the charts are the patches, in order; their vertices the patch's, ascending
+  P.mesh_pos.assign(p3, p3 + 3 * NV);
+  P.p3 = P.mesh_pos;
+  P.mesh_faces.resize(3 * NT);
+  P.n_cut_slots = 0;
+  P.vert_off.assign(vert_off, vert_off + np + 1);
+  P.tri_off.assign(tri_off, tri_off + np + 1);
+  P.vertex_ids.resize(NV);
+  P.face_ids.resize(NT);
+  P.tris = std::move(D.tris);
+  P.area3d = std::move(D.area3d);
+  parallel_for(np, threads, [&](int64_t c) {
+    const int64_t v0 = vert_off[c];
+    for (int64_t k = v0; k < vert_off[c + 1]; ++k) P.vertex_ids[k] = k;
+    for (int64_t t = tri_off[c]; t < tri_off[c + 1]; ++t) P.face_ids[t] = D.order[t];
+    for (int64_t t = 3 * tri_off[c]; t < 3 * tri_off[c + 1]; ++t) P.mesh_faces[t] = (int32_t)(v0 + tris[t]);
+  });
+  P.border_off.assign(np + 1, 0);
+  P.loop_off.assign(np + 1, 0);
+  int64_t nloops = 0;
+  for (int64_t c = 0; c < np; ++c) {
+    P.border_off[c + 1] = P.border_off[c] + (int64_t)charts[c].border.size();
+    nloops += (int64_t)charts[c].loop_len.size();
+    P.loop_off[c + 1] = nloops;
+  }
+  P.border.resize(P.border_off[np]);
+  P.loop_seg.assign(nloops + 1, 0);
+  {
+    int64_t li = 0;
+    for (int64_t c = 0; c < np; ++c)
+      for (int64_t len : charts[c].loop_len) {
+        P.loop_seg[li + 1] = P.loop_seg[li] + len;
+        ++li;
+      }
+  }
+  P.loop_ids.resize(P.loop_seg[nloops]);
+  for (int64_t c = 0; c < np; ++c) {
+    std::copy(charts[c].border.begin(), charts[c].border.end(), P.border.begin() + P.border_off[c]);
+    if (!charts[c].loop_ids.empty())
+      std::copy(charts[c].loop_ids.begin(), charts[c].loop_ids.end(), P.loop_ids.begin() + P.loop_seg[P.loop_off[c]]);
+  }
+  clk.mark("pack");
   return RUV_OK;
 }
 

@@ -337,6 +337,224 @@ __global__ void k_chart_local(const uint64_t* __restrict__ keys, const int32_t* 
   tris[vals[j]] = (int32_t)(u - vert_off[keys[j] / nv]);
 }
 
+// ---------------------------------------------------------------- patches (prepare_patches)
+// The last c with off[c] <= t (off[0] = 0 <= t < off[n]): the patch of face or vertex t.
+__device__ __forceinline__ int64_t patch_of(const int64_t* __restrict__ off, int64_t n, int64_t t) {
+  int64_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) / 2;
+    if (off[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Global faces from the patch-local triangles; bad |= 1 for an index outside its patch, 2 for
+// a triangle with a repeated vertex; used[v] = 1 for every vertex a triangle uses.
+__global__ void k_patch_faces(const int64_t* __restrict__ vo, const int64_t* __restrict__ to, int64_t np,
+                              const int32_t* __restrict__ tris, int64_t nt, int32_t* __restrict__ F,
+                              uint8_t* __restrict__ used, int* __restrict__ bad) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const int64_t c = patch_of(to, np, t);
+  const int64_t v0 = vo[c], nvc = vo[c + 1] - v0;
+  int32_t a[3];
+  bool ok = true;
+  for (int k = 0; k < 3; ++k) {
+    a[k] = tris[3 * t + k];
+    if (a[k] < 0 || a[k] >= nvc) ok = false;
+  }
+  if (!ok) {
+    atomicOr(bad, 1);
+    for (int k = 0; k < 3; ++k) F[3 * t + k] = 0;
+    return;
+  }
+  if (a[0] == a[1] || a[1] == a[2] || a[0] == a[2]) atomicOr(bad, 2);
+  for (int k = 0; k < 3; ++k) {
+    F[3 * t + k] = (int32_t)(v0 + a[k]);
+    used[v0 + a[k]] = 1;
+  }
+}
+
+// Faces of each patch in the reference's DFS pop order (segment.rs:150-175: roots in face
+// order, a stack, every edge's faces pushed in ascending order when unseen), one thread per
+// patch; a patch of several components stays one chart, its components one after the other
+// (as on the host); ncomp = the patch's components.  The stack never holds more than the patch's faces
+// (a face is pushed once); bad |= 4 if a list leaves the patch (cannot happen: patches share
+// no vertices).
+__global__ void k_patch_dfs(int64_t np, const int64_t* __restrict__ to, const int64_t* __restrict__ ef_off,
+                            const int32_t* __restrict__ ef_faces, uint8_t* __restrict__ seen, int32_t* __restrict__ stack,
+                            int32_t* __restrict__ order, int32_t* __restrict__ ncomp, int* __restrict__ bad) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= np) return;
+  const int64_t fb = to[c], fe = to[c + 1], n = fe - fb;
+  int64_t out = fb, sp = 0;
+  int32_t comps = 0;
+  for (int64_t f0 = fb; f0 < fe; ++f0) {
+    if (seen[f0]) continue;
+    ++comps;
+    seen[f0] = 1;
+    stack[fb + sp++] = (int32_t)f0;
+    while (sp > 0) {
+      const int32_t f = stack[fb + --sp];
+      order[out++] = f;
+      for (int k = 0; k < 3; ++k) {
+        const int64_t sl = 3 * (int64_t)f + k;
+        for (int64_t q = ef_off[sl]; q < ef_off[sl + 1]; ++q) {
+          const int32_t g = ef_faces[q];
+          if (g < fb || g >= fe) {
+            atomicOr(bad, 4);
+            continue;
+          }
+          if (!seen[g]) {
+            seen[g] = 1;
+            if (sp < n) stack[fb + sp++] = g;
+            else atomicOr(bad, 4);
+          }
+        }
+      }
+    }
+  }
+  ncomp[c] = comps;
+}
+
+// flags |= 1 when a vertex is used by no triangle
+__global__ void k_patch_checks(const uint8_t* __restrict__ used, int64_t nv, int* __restrict__ flags) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nv && !used[i]) atomicOr(flags, 1);
+}
+
+__device__ __forceinline__ double dot3_rn(double ax, double ay, double az, double bx, double by, double bz) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
+}
+
+// Face areas 0.5 |e1 x e2| in the host's operation order (face_areas, segment.rs:61-70).
+__global__ void k_face_area(const double* __restrict__ pos, const int32_t* __restrict__ F, int64_t nt,
+                            double* __restrict__ area) {
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nt) return;
+  const double* p0 = pos + 3 * (int64_t)F[3 * f];
+  const double* p1 = pos + 3 * (int64_t)F[3 * f + 1];
+  const double* p2 = pos + 3 * (int64_t)F[3 * f + 2];
+  const double ax = __dsub_rn(p1[0], p0[0]), ay = __dsub_rn(p1[1], p0[1]), az = __dsub_rn(p1[2], p0[2]);
+  const double bx = __dsub_rn(p2[0], p0[0]), by = __dsub_rn(p2[1], p0[1]), bz = __dsub_rn(p2[2], p0[2]);
+  const double cx = __dsub_rn(__dmul_rn(ay, bz), __dmul_rn(az, by));
+  const double cy = __dsub_rn(__dmul_rn(az, bx), __dmul_rn(ax, bz));
+  const double cz = __dsub_rn(__dmul_rn(ax, by), __dmul_rn(ay, bx));
+  area[f] = __dmul_rn(0.5, __dsqrt_rn(dot3_rn(cx, cy, cz, cx, cy, cz)));
+}
+
+// Per patch (one thread): the area summed in chart face order (segment.rs:212) and the
+// centroid and covariance of its vertices in vertex order (pca_project, lscm.rs:152-170).
+__global__ void k_patch_stats(int64_t np, const int64_t* __restrict__ vo, const int64_t* __restrict__ to,
+                              const double* __restrict__ pos, const int32_t* __restrict__ order,
+                              const double* __restrict__ farea, double* __restrict__ area3d, double* __restrict__ cov) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= np) return;
+  double a = 0.0;
+  for (int64_t k = to[c]; k < to[c + 1]; ++k) a = __dadd_rn(a, farea[order[k]]);
+  area3d[c] = a;
+  double* o = cov + 12 * c;
+  const int64_t v0 = vo[c], n = vo[c + 1] - v0;
+  double m[3] = {0.0, 0.0, 0.0}, cm[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (n > 0) {
+    for (int64_t i = v0; i < v0 + n; ++i)
+      for (int k = 0; k < 3; ++k) m[k] = __dadd_rn(m[k], pos[3 * i + k]);
+    for (int k = 0; k < 3; ++k) m[k] = __ddiv_rn(m[k], (double)n);
+    for (int64_t i = v0; i < v0 + n; ++i) {
+      double e[3];
+      for (int k = 0; k < 3; ++k) e[k] = __dsub_rn(pos[3 * i + k], m[k]);
+      for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) cm[3 * r + q] = __dadd_rn(cm[3 * r + q], __dmul_rn(e[r], e[q]));
+    }
+  }
+  for (int k = 0; k < 3; ++k) o[k] = m[k];
+  for (int k = 0; k < 9; ++k) o[3 + k] = cm[k];
+}
+
+// boundary face slots (an edge carried by one face: segment.rs:198-209 with no cuts)
+__global__ void k_border_flag(const int64_t* __restrict__ ef_off, int64_t ns, uint8_t* __restrict__ flag) {
+  const int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sl < ns) flag[sl] = (ef_off[sl + 1] - ef_off[sl]) == 1 ? 1 : 0;
+}
+__global__ void k_border_keys(const int32_t* __restrict__ F, int64_t ns, const uint8_t* __restrict__ flag,
+                              const int64_t* __restrict__ at, uint64_t* __restrict__ keys) {
+  const int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sl >= ns || !flag[sl]) return;
+  const int64_t f = sl / 3;
+  const int k = (int)(sl % 3);
+  const uint32_t x = (uint32_t)F[3 * f + k], y = (uint32_t)F[3 * f + (k + 1) % 3];
+  const uint32_t a = min(x, y), b = max(x, y);
+  keys[at[sl]] = ((uint64_t)a << 32) | b;
+}
+__global__ void k_border_off(const int64_t* __restrict__ to, int64_t np, const int64_t* __restrict__ at,
+                             int64_t* __restrict__ boff) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c <= np) boff[c] = at[3 * to[c]];
+}
+
+// local triangles in chart (DFS) order
+__global__ void k_tris_order(const int32_t* __restrict__ order, const int32_t* __restrict__ tris, int64_t nt,
+                             const int64_t* __restrict__ to, int64_t np, int32_t* __restrict__ out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  const int64_t f = order[k];
+  for (int j = 0; j < 3; ++j) out[3 * k + j] = tris[3 * f + j];
+}
+
+// p2 of every vertex on its chart's frame (centroid, e1, e2): the projection of pca_project
+__global__ void k_patch_project(const int64_t* __restrict__ vo, int64_t np, const double* __restrict__ pos,
+                                const double* __restrict__ frames, int64_t nv, double* __restrict__ p2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const double* fr = frames + 9 * patch_of(vo, np, i);
+  const double dx = __dsub_rn(pos[3 * i], fr[0]), dy = __dsub_rn(pos[3 * i + 1], fr[1]),
+               dz = __dsub_rn(pos[3 * i + 2], fr[2]);
+  p2[2 * i] = dot3_rn(dx, dy, dz, fr[3], fr[4], fr[5]);
+  p2[2 * i + 1] = dot3_rn(dx, dy, dz, fr[6], fr[7], fr[8]);
+}
+
+int64_t read_i64(Ctx& ctx, const int64_t* d);
+
+// Edge-face lists of the faces F (3 nf vertex ids < nv) on the device: for every face slot,
+// the faces carrying its edge in ascending order (ef_off: 3 nf + 1 offsets, ef_faces).
+// Returns the number of list entries.
+int64_t device_edge_faces(Ctx& ctx, const int32_t* F, int64_t nf, int64_t nv, int64_t*& ef_off, int32_t*& ef_faces) {
+  cudaStream_t s = ctx.stream;
+  constexpr int B = 256;
+  const int64_t ns = 3 * nf;
+  ef_off = ctx.ws.get<int64_t>("prep.ef_off", ns + 1);
+  ef_faces = nullptr;
+  if (ns <= 0) {
+    RUV_CUDA(cudaMemsetAsync(ef_off, 0, sizeof(int64_t), s));
+    return 0;
+  }
+  uint64_t* keys = ctx.ws.get<uint64_t>("prep.ekeys", ns);
+  int32_t* vals = ctx.ws.get<int32_t>("prep.evals", ns);
+  k_edge_keys<<<div_up(ns, B), B, 0, s>>>(F, nf, (uint64_t)nv, keys, vals);
+  count_launches(1);
+  const uint64_t maxk = (uint64_t)nv * (uint64_t)nv;
+  auto sorted = radix_sort(ctx, keys, vals, ns, bits_for(maxk), "prep.esort");
+  uint8_t* start = ctx.ws.get<uint8_t>("prep.estart", ns);
+  int64_t* rid = ctx.ws.get<int64_t>("prep.erid", ns + 1);
+  k_run_start<<<div_up(ns, B), B, 0, s>>>(sorted.first, ns, start);
+  count_launches(1);
+  exclusive_scan_u8(start, rid, ns, ctx.ws, s, "prep.erun");
+  const int64_t nruns = read_i64(ctx, rid + ns);
+  int64_t* rbeg = ctx.ws.get<int64_t>("prep.erbeg", nruns + 1);
+  int32_t* cnt = ctx.ws.get<int32_t>("prep.ecnt", ns);
+  k_run_bounds<<<div_up(ns, B), B, 0, s>>>(start, rid, ns, rbeg);
+  // rid[j + 1] - 1 is j's run for j < ns - 1; the last position reads rid[ns] = the run count
+  k_ef_count<<<div_up(ns, B), B, 0, s>>>(sorted.second, rid, rbeg, ns, cnt);
+  count_launches(2);
+  exclusive_scan(cnt, ef_off, ns, ctx.ws, s, "prep.efoff");
+  const int64_t nef = read_i64(ctx, ef_off + ns);
+  ef_faces = ctx.ws.get<int32_t>("prep.ef_faces", nef);
+  k_ef_fill<<<div_up(ns, B), B, 0, s>>>(sorted.second, rid, rbeg, ef_off, ns, ef_faces);
+  count_launches(1);
+  return nef;
+}
+
 int64_t read_i64(Ctx& ctx, const int64_t* d) {
   int64_t h = 0;
   RUV_CUDA(cudaMemcpyAsync(&h, d, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx.stream));
@@ -414,36 +632,9 @@ ruv_status prepare_mesh_gpu(Ctx& ctx, const double* pos, int64_t nv, const int32
   }
   // ---- edge-face lists
   const int64_t ns = 3 * wnf;
-  int64_t* ef_off = ctx.ws.get<int64_t>("prep.ef_off", ns + 1);
+  int64_t* ef_off = nullptr;
   int32_t* ef_faces = nullptr;
-  int64_t nef = 0;
-  if (ns > 0) {
-    uint64_t* keys = ctx.ws.get<uint64_t>("prep.ekeys", ns);
-    int32_t* vals = ctx.ws.get<int32_t>("prep.evals", ns);
-    k_edge_keys<<<div_up(ns, B), B, 0, s>>>(F, wnf, (uint64_t)wnv, keys, vals);
-    count_launches(1);
-    const uint64_t maxk = (uint64_t)wnv * (uint64_t)wnv;
-    auto sorted = radix_sort(ctx, keys, vals, ns, bits_for(maxk), "prep.esort");
-    uint8_t* start = ctx.ws.get<uint8_t>("prep.estart", ns);
-    int64_t* rid = ctx.ws.get<int64_t>("prep.erid", ns + 1);
-    k_run_start<<<div_up(ns, B), B, 0, s>>>(sorted.first, ns, start);
-    count_launches(1);
-    exclusive_scan_u8(start, rid, ns, ctx.ws, s, "prep.erun");
-    const int64_t nruns = read_i64(ctx, rid + ns);
-    int64_t* rbeg = ctx.ws.get<int64_t>("prep.erbeg", nruns + 1);
-    int32_t* cnt = ctx.ws.get<int32_t>("prep.ecnt", ns);
-    k_run_bounds<<<div_up(ns, B), B, 0, s>>>(start, rid, ns, rbeg);
-    // rid[j + 1] - 1 is j's run for j < ns - 1; the last position reads rid[ns] = the run count
-    k_ef_count<<<div_up(ns, B), B, 0, s>>>(sorted.second, rid, rbeg, ns, cnt);
-    count_launches(2);
-    exclusive_scan(cnt, ef_off, ns, ctx.ws, s, "prep.efoff");
-    nef = read_i64(ctx, ef_off + ns);
-    ef_faces = ctx.ws.get<int32_t>("prep.ef_faces", nef);
-    k_ef_fill<<<div_up(ns, B), B, 0, s>>>(sorted.second, rid, rbeg, ef_off, ns, ef_faces);
-    count_launches(1);
-  } else {
-    RUV_CUDA(cudaMemsetAsync(ef_off, 0, sizeof(int64_t), s));
-  }
+  const int64_t nef = device_edge_faces(ctx, F, wnf, wnv, ef_off, ef_faces);
   // ---- normals and cut flags
   uint8_t* cut = ctx.ws.get<uint8_t>("prep.cut", std::max<int64_t>(ns, 1));
   if (wnf > 0) {
@@ -510,6 +701,129 @@ ruv_status prepare_mesh_gpu(Ctx& ctx, const double* pos, int64_t nv, const int32
   };
   return prepare_mesh_topology(std::move(h_wpos), std::move(h_F), std::move(h_ef_off), std::move(h_ef_faces),
                                std::move(h_cut), threads, &sets, P, err);
+}
+
+// prepare_patches with its data-parallel stages on the device of `ctx` (see
+// prepare_patches_device): the same Prepared as the host path, bit for bit.
+ruv_status prepare_patches_gpu(Ctx& ctx, int64_t np, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
+                               const int32_t* tris, int threads, Prepared& P, std::string& err) {
+  cudaStream_t s = ctx.stream;
+  constexpr int B = 256;
+  int64_t* d_vo = nullptr;
+  double* d_pos = nullptr;
+  PatchDeviceFn dev = [&](PatchDevice& D, std::string& e) -> ruv_status {
+    const int64_t NV = vert_off[np], NT = tri_off[np], ns = 3 * NT;
+    d_vo = ctx.ws.get<int64_t>("pp.vo", np + 1);
+    int64_t* d_to = ctx.ws.get<int64_t>("pp.to", np + 1);
+    d_pos = ctx.ws.get<double>("pp.pos", 3 * std::max<int64_t>(NV, 1));
+    int32_t* d_tris = ctx.ws.get<int32_t>("pp.tris", 3 * std::max<int64_t>(NT, 1));
+    RUV_CUDA(cudaMemcpyAsync(d_vo, vert_off, sizeof(int64_t) * (np + 1), cudaMemcpyHostToDevice, s));
+    RUV_CUDA(cudaMemcpyAsync(d_to, tri_off, sizeof(int64_t) * (np + 1), cudaMemcpyHostToDevice, s));
+    if (NV > 0) RUV_CUDA(cudaMemcpyAsync(d_pos, p3, sizeof(double) * 3 * NV, cudaMemcpyHostToDevice, s));
+    if (NT > 0) RUV_CUDA(cudaMemcpyAsync(d_tris, tris, sizeof(int32_t) * 3 * NT, cudaMemcpyHostToDevice, s));
+    int32_t* F = ctx.ws.get<int32_t>("pp.F", 3 * std::max<int64_t>(NT, 1));
+    uint8_t* used = ctx.ws.get<uint8_t>("pp.used", std::max<int64_t>(NV, 1));
+    int* bad = ctx.ws.get<int>("pp.bad", 4);
+    RUV_CUDA(cudaMemsetAsync(bad, 0, 4 * sizeof(int), s));
+    if (NV > 0) RUV_CUDA(cudaMemsetAsync(used, 0, NV, s));
+    if (NT > 0) {
+      k_patch_faces<<<div_up(NT, B), B, 0, s>>>(d_vo, d_to, np, d_tris, NT, F, used, bad);
+      count_launches(1);
+    }
+    int hb[4] = {0, 0, 0, 0};
+    RUV_CUDA(cudaMemcpyAsync(hb, bad, sizeof(hb), cudaMemcpyDeviceToHost, s));
+    RUV_CUDA(cudaStreamSynchronize(s));
+    if (hb[0] & 1) {
+      e = "patch triangle index out of range";
+      return RUV_ERR_BAD_INPUT;
+    }
+    if (hb[0] & 2) {
+      e = "degenerate patch triangle";
+      return RUV_ERR_BAD_INPUT;
+    }
+    int64_t* ef_off = nullptr;
+    int32_t* ef_faces = nullptr;
+    device_edge_faces(ctx, F, NT, NV, ef_off, ef_faces);
+    uint8_t* seen = ctx.ws.get<uint8_t>("pp.seen", std::max<int64_t>(NT, 1));
+    int32_t* stack = ctx.ws.get<int32_t>("pp.stack", std::max<int64_t>(NT, 1));
+    int32_t* order = ctx.ws.get<int32_t>("pp.order", std::max<int64_t>(NT, 1));
+    int32_t* ncomp = ctx.ws.get<int32_t>("pp.ncomp", std::max<int64_t>(np, 1));
+    if (NT > 0) RUV_CUDA(cudaMemsetAsync(seen, 0, NT, s));
+    if (np > 0) {
+      k_patch_dfs<<<div_up(np, 128), 128, 0, s>>>(np, d_to, ef_off, ef_faces, seen, stack, order, ncomp, bad);
+      count_launches(1);
+    }
+    if (NV > 0) {
+      k_patch_checks<<<div_up(NV, B), B, 0, s>>>(used, NV, bad + 1);
+      count_launches(1);
+    }
+    RUV_CUDA(cudaMemcpyAsync(hb, bad, sizeof(hb), cudaMemcpyDeviceToHost, s));
+    RUV_CUDA(cudaStreamSynchronize(s));
+    if (hb[0] & 4) {
+      e = "patch edge lists leave their patch";
+      return RUV_ERR_INTERNAL;
+    }
+    if (hb[1] & 1) {  // name the first patch with an unused vertex, as the host path does
+      std::vector<uint8_t> hu;
+      download(ctx, hu, (const uint8_t*)used, NV);
+      RUV_CUDA(cudaStreamSynchronize(s));
+      const int64_t v = (int64_t)(std::find(hu.begin(), hu.end(), (uint8_t)0) - hu.begin());
+      const int64_t c = (int64_t)(std::upper_bound(vert_off, vert_off + np + 1, v) - vert_off) - 1;
+      e = "patch " + std::to_string(c) + " has vertices no triangle uses";
+      return RUV_ERR_BAD_INPUT;
+    }
+    double* farea = ctx.ws.get<double>("pp.farea", std::max<int64_t>(NT, 1));
+    double* area3d = ctx.ws.get<double>("pp.area3d", std::max<int64_t>(np, 1));
+    double* cov = ctx.ws.get<double>("pp.cov", 12 * std::max<int64_t>(np, 1));
+    uint8_t* bflag = ctx.ws.get<uint8_t>("pp.bflag", std::max<int64_t>(ns, 1));
+    int64_t* bat = ctx.ws.get<int64_t>("pp.bat", ns + 1);
+    int64_t* boff = ctx.ws.get<int64_t>("pp.boff", np + 1);
+    int32_t* tris_out = ctx.ws.get<int32_t>("pp.tris_out", 3 * std::max<int64_t>(NT, 1));
+    if (NT > 0) {
+      k_face_area<<<div_up(NT, B), B, 0, s>>>(d_pos, F, NT, farea);
+      k_border_flag<<<div_up(ns, B), B, 0, s>>>(ef_off, ns, bflag);
+      k_tris_order<<<div_up(NT, B), B, 0, s>>>(order, d_tris, NT, d_to, np, tris_out);
+      count_launches(3);
+    }
+    if (np > 0) {
+      k_patch_stats<<<div_up(np, 64), 64, 0, s>>>(np, d_vo, d_to, d_pos, order, farea, area3d, cov);
+      count_launches(1);
+    }
+    exclusive_scan_u8(bflag, bat, ns, ctx.ws, s, "pp.bscan");
+    const int64_t nb = read_i64(ctx, bat + ns);
+    uint64_t* bkeys = ctx.ws.get<uint64_t>("pp.bkeys", std::max<int64_t>(nb, 1));
+    if (ns > 0) {
+      k_border_keys<<<div_up(ns, B), B, 0, s>>>(F, ns, bflag, bat, bkeys);
+      count_launches(1);
+    }
+    k_border_off<<<div_up(np + 1, B), B, 0, s>>>(d_to, np, bat, boff);
+    count_launches(1);
+    RUV_LAUNCH_CHECK();
+    download(ctx, D.order, (const int32_t*)order, NT);
+    download(ctx, D.tris, (const int32_t*)tris_out, 3 * NT);
+    download(ctx, D.area3d, (const double*)area3d, np);
+    download(ctx, D.cov, (const double*)cov, 12 * np);
+    download(ctx, D.boff, (const int64_t*)boff, np + 1);
+    download(ctx, D.bkeys, (const uint64_t*)bkeys, nb);
+    RUV_CUDA(cudaStreamSynchronize(s));
+    return RUV_OK;
+  };
+  PatchProjectFn proj = [&](const std::vector<double>& frames, std::vector<double>& p2, std::string& e) -> ruv_status {
+    (void)e;
+    const int64_t NV = vert_off[np];
+    double* d_fr = ctx.ws.get<double>("pp.frames", 9 * std::max<int64_t>(np, 1));
+    double* d_p2 = ctx.ws.get<double>("pp.p2", 2 * std::max<int64_t>(NV, 1));
+    if (np > 0) RUV_CUDA(cudaMemcpyAsync(d_fr, frames.data(), sizeof(double) * 9 * np, cudaMemcpyHostToDevice, s));
+    if (NV > 0) {
+      k_patch_project<<<div_up(NV, B), B, 0, s>>>(d_vo, np, d_pos, d_fr, NV, d_p2);
+      count_launches(1);
+      RUV_LAUNCH_CHECK();
+      RUV_CUDA(cudaMemcpyAsync(p2.data(), d_p2, sizeof(double) * 2 * NV, cudaMemcpyDeviceToHost, s));
+    }
+    RUV_CUDA(cudaStreamSynchronize(s));
+    return RUV_OK;
+  };
+  return prepare_patches_device(np, vert_off, tri_off, p3, tris, threads, dev, proj, P, err);
 }
 
 }  // namespace ruv

@@ -50,6 +50,31 @@ ruv_status prepare_mesh_topology(std::vector<double>&& wpos3, std::vector<int32_
                                  std::vector<int32_t>&& ef_faces, std::vector<uint8_t>&& cut, int threads,
                                  const ChartSetsFn* sets, Prepared& P, std::string& err);
 
+// prepare_patches with its data-parallel stages on a device (prep_gpu.cu supplies the two
+// callbacks): `dev` checks the patches and returns, for patches that are connected, every
+// patch's faces in the reference's DFS pop order with its local triangles in that order, its
+// area, the centroid and covariance of its vertices (tangent frame, lscm.rs:152-183) and
+// its boundary edge keys; `proj` projects every vertex on its chart's frame (9 per chart:
+// centroid, e1, e2).  The border loops, the eig3 of each frame and the pins run on the host
+// (per chart, O(border)), then the packing.  The same Prepared as prepare_patches, bit for bit.
+struct Ctx;
+struct PatchDevice {
+  std::vector<int32_t> order;    // tri_off[np]: source faces, DFS pop order per patch
+  std::vector<int32_t> tris;     // 3 tri_off[np]: patch-local triangles in that order
+  std::vector<double> area3d;    // np
+  std::vector<double> cov;       // 12 np: centroid (3), covariance (3 x 3)
+  std::vector<int64_t> boff;     // np + 1
+  std::vector<uint64_t> bkeys;   // boundary edges (min << 32 | max, source ids), per patch
+};
+using PatchDeviceFn = std::function<ruv_status(PatchDevice& out, std::string& err)>;
+using PatchProjectFn = std::function<ruv_status(const std::vector<double>& frames, std::vector<double>& p2,
+                                                std::string& err)>;
+ruv_status prepare_patches_device(int64_t np, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
+                                  const int32_t* tris, int threads, const PatchDeviceFn& dev, const PatchProjectFn& proj,
+                                  Prepared& P, std::string& err);
+ruv_status prepare_patches_gpu(Ctx& ctx, int64_t np, const int64_t* vert_off, const int64_t* tri_off, const double* p3,
+                               const int32_t* tris, int threads, Prepared& P, std::string& err);
+
 // Seam cut of closed charts (seam.rs SeamCutOptions) and re-cutting of folding charts
 // (recut.rs RecutOptions) after the segmentation (pipeline.rs:149-167).
 struct CutOpts {
@@ -76,7 +101,6 @@ double uv_signed_area(const double* uv, const int32_t* tris, int64_t nt);
 
 // prepare_mesh with the weld, edge-face lists, cut flags and chart vertex sets on the device
 // of `ctx` (prep_gpu.cu): the same Prepared, bit for bit.
-struct Ctx;
 ruv_status prepare_mesh_gpu(Ctx& ctx, const double* pos, int64_t nv, const int32_t* faces, int64_t nf, double weld_tol,
                             double angle_min_deg, int threads, Prepared& P, std::string& err);
 

@@ -60,6 +60,8 @@ struct SepPrecond {
   virtual bool flexible() const = 0;     // varies between applications: flexible-CG beta
   virtual void bind(Ctx& ctx, void* r, void* z, bool fp64) = 0;
   virtual int apply(Ctx& ctx, const int32_t* done) = 0;
+  // device flag set when an application gave up a bounded device-side wait (nullptr: none)
+  virtual const int* error_flag() const { return nullptr; }
 };
 
 // Batched aggregation AMG (amg.cu): hierarchy built on the device, one V(1,1) cycle per apply.

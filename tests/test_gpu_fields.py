@@ -73,12 +73,32 @@ def test_height_field_512_matches_superlu(ctx, precision):
     _check(ctx, (512, 8, 0.15), precision, R.Precond.AMG_SA)
 
 
+@pytest.mark.parametrize("precision", [R.Precision.MIXED, R.Precision.FP64])
+def test_height_field_384_natural_ic0_matches_superlu(ctx, precision):
+    """Natural-order IC(0) on one 146k-vertex chart: about 760 dependency levels, so the
+    factorization and sweeps run sync-free over the whole GPU."""
+    _check(ctx, (384, 8, 0.15), precision, R.Precond.IC0)
+
+
 @pytest.mark.parametrize("precond", [R.Precond.AMG_SA, R.Precond.AMG, R.Precond.IC0_COLOR])
 def test_anisotropic_field_512_matches_superlu(ctx, precond):
     """The 2048^2 / 16-sine / 0.3 family at 512^2: ridges cut at 30 degrees into several
     charts, strongly anisotropic triangles; mixed precision."""
     worst, res = _check(ctx, (512, 16, 0.3), R.Precision.MIXED, precond)
     assert len(res) > 1
+
+
+@pytest.mark.parametrize("precond", [R.Precond.AMG_SA, R.Precond.AMG])
+def test_kcycle_field_matches_superlu(ctx, monkeypatch, precond):
+    """The K-cycle (two coarse corrections with per-chart CG steplengths on the top two
+    levels, gpu/src/amg.rs:468-639) on the anisotropic family: the same UV bar, and no more
+    CG iterations than the V(1,1) cycle on the largest chart."""
+    monkeypatch.setenv("RUV_AMG_KCYCLE", "2")
+    worst, kres = _check(ctx, (512, 16, 0.3), R.Precision.MIXED, precond)
+    monkeypatch.delenv("RUV_AMG_KCYCLE")
+    _, vres = _check(ctx, (512, 16, 0.3), R.Precision.MIXED, precond)
+    big = max(range(len(kres)), key=lambda c: kres[c].n_free)
+    assert kres[big].cg_iters <= vres[big].cg_iters, (kres[big].cg_iters, vres[big].cg_iters)
 
 
 def test_cube_fp64_ic0_matches_cpu_lu(ctx):

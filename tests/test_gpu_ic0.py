@@ -133,3 +133,48 @@ def test_batched_disks_ic0_match_fp64_lu(pc, precision):
         P = O.Pipeline(p3[vo[c]:vo[c + 1]], tr[to[c]:to[c + 1]], weld_tol=0.0, lu_limit=0)
         assert O.uv_error(res[c].uv, P.superlu_uv(0)) <= 1e-6
     assert res[big].cg_iters < jac[big].cg_iters, (res[big].cg_iters, jac[big].cg_iters)
+
+
+def _ic0_pair(gpu, a, r, monkeypatch, tickets):
+    monkeypatch.setenv("RUV_IC0_TICKETS", "1" if tickets else "0")
+    f = gpu.ic0_factor(a)
+    z = gpu.apply_ic0_for_test(a, r)
+    monkeypatch.delenv("RUV_IC0_TICKETS", raising=False)
+    assert z is not None, gpu.last_error
+    return f, z
+
+
+@pytest.mark.parametrize("name", ["poisson300", "lap1d_chain"])
+def test_ic0_sync_free_sweeps_bitwise(gpu, monkeypatch, name):
+    """The sync-free (ticket) factorization and sweeps, used for charts with many dependency
+    levels, against the per-chart level walk: the same factor and the same apply bit for bit,
+    and the factor equal to the oracle's factor_ic0.  A 5-point Poisson grid (599 levels of up
+    to 300 rows) and a pure chain (40000 levels of one row each)."""
+    a = poisson(300)[0] if name == "poisson300" else lap1d(40_000)[0]
+    n = a.rows()
+    r = np.array([((i * 7919) % 101) / 101.0 - 0.5 for i in range(n)])
+    f1, z1 = _ic0_pair(gpu, a, r, monkeypatch, True)
+    f0, z0 = _ic0_pair(gpu, a, r, monkeypatch, False)
+    for k in ("ptr", "cols"):
+        assert np.array_equal(f1[k], f0[k])
+    assert np.array_equal(f1["vals"].view(np.uint64), f0["vals"].view(np.uint64))
+    assert np.array_equal(z1.view(np.uint64), z0.view(np.uint64))
+    _same_factor(f1, O.Ic0(a.row_ptr, a.cols, a.vals))
+
+
+def test_ic0_sync_free_wait_times_out(monkeypatch):
+    """Every device-side dependency wait of the sync-free kernels is bounded: with a spin limit
+    of 1 the waits run out, the call returns TIMEOUT, and the same context solves again once
+    the limit is back to its default."""
+    a, b = poisson(300)
+    g = R.GpuSolver.new()
+    monkeypatch.setenv("RUV_IC0_TICKETS", "1")
+    monkeypatch.setenv("RUV_SPIN_LIMIT", "1")
+    assert g.cg_solve_precond(a, b, 1000, 1e-10, R.Precond.IC0) is None
+    assert "TIMEOUT" in g.last_error, g.last_error
+    assert g.apply_ic0_for_test(a, b) is None and "TIMEOUT" in g.last_error
+    monkeypatch.delenv("RUV_SPIN_LIMIT")
+    r = g.cg_solve_precond(a, b, 100_000, 1e-10, R.Precond.IC0)
+    assert r is not None, g.last_error
+    x_none, _ = g.cg_solve_precond(a, b, 100_000, 1e-10, R.Precond.NONE)
+    assert np.abs(r[0] - x_none).max() < 1e-5

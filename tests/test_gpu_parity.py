@@ -178,8 +178,10 @@ def test_cg_not_converged_and_breakdown():
 
 
 # ------------------------------------------------------------------ AMG preconditioners
+@pytest.mark.parametrize("kcycle", ["0", "2"])
 @pytest.mark.parametrize("pc", [R.Precond.AMG, R.Precond.AMG_SA])
-def test_batched_disks_amg_match_fp64_lu(ctx, pc):
+def test_batched_disks_amg_match_fp64_lu(ctx, pc, kcycle, monkeypatch):
+    monkeypatch.setenv("RUV_AMG_KCYCLE", kcycle)
     vo, to, p3, tr = W.disks(40, t_min=50, t_max=20000, seed=21)
     C = R.prepare_patches(vo, to, p3, tr)
     jac = R.unfold_charts(ctx, C, R.UnfoldOptions(precond=R.Precond.JACOBI))

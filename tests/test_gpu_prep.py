@@ -88,3 +88,74 @@ def test_device_prep_solves_alike():
     ua, _, _ = R.solve_batch(ctx, a.batch(), R.UnfoldOptions(precision=R.Precision.FP64), n)
     ub, _, _ = R.solve_batch(ctx, b.batch(), R.UnfoldOptions(precision=R.Precision.FP64), n)
     assert np.array_equal(ua, ub)
+
+
+def _patch_set(meshes):
+    vo, to, P, T = [0], [0], [], []
+    for p, f in meshes:
+        p = np.asarray(p, np.float64).reshape(-1, 3)
+        f = np.asarray(f, np.int32).reshape(-1, 3)
+        P.append(p)
+        T.append(f)
+        vo.append(vo[-1] + len(p))
+        to.append(to[-1] + len(f))
+    return np.array(vo), np.array(to), np.concatenate(P), np.concatenate(T).astype(np.int32)
+
+
+def _welded(p, f):
+    return O.Pipeline(p, f).mesh()
+
+
+PATCH_CASES = {
+    "disks": lambda: W.disks(96, t_min=50, t_max=20000, seed=31),
+    # closed charts (anchors), two loops (cylinder strip and multi-loop), one loop
+    "fixtures": lambda: _patch_set([_welded(*O.cube(6)), _welded(*O.uv_sphere(32, 16)),
+                                    _welded(*O.torus(2.0, 0.7, 32, 16)), _welded(*O.torus_annulus(2.0, 0.7, 48, 24)),
+                                    _welded(*O.cylinder(1.0, 2.0, 24, 10)), O.grid(17, 11)]),
+}
+
+
+@pytest.mark.parametrize("name", sorted(PATCH_CASES))
+def test_device_patches_match_host(name):
+    """ruv_prepare_patches_gpu against ruv_prepare_patches: every exported array bit for bit."""
+    ctx = R.Context(0)
+    vo, to, p3, tr = PATCH_CASES[name]()
+    _same(R.prepare_patches(vo, to, p3, tr), R.prepare_patches(vo, to, p3, tr, ctx=ctx))
+
+
+def test_device_patches_fallback_and_errors():
+    """A patch of two components stays one chart on both paths (the same result); an index
+    outside its patch and a vertex no triangle uses are errors on both paths."""
+    ctx = R.Context(0)
+    vo, to, p3, tr = W.disks(4, t_min=200, t_max=2000, seed=37)
+    # patches 1 and 2 merged into one patch of two components
+    merged_vo = np.array([vo[0], vo[1], vo[3], vo[4]])
+    shifted = tr.copy().astype(np.int64)
+    shifted[to[2]:to[3]] += vo[2] - vo[1]
+    merged_to = np.array([to[0], to[1], to[3], to[4]])
+    _same(R.prepare_patches(merged_vo, merged_to, p3, shifted),
+          R.prepare_patches(merged_vo, merged_to, p3, shifted, ctx=ctx))
+    bad = tr.copy()
+    bad[to[1]] = [0, 1, vo[2] - vo[1]]  # outside patch 1
+    for c in (None, ctx):
+        with pytest.raises(R.RuvError) as e:
+            R.prepare_patches(vo, to, p3, bad, ctx=c)
+        assert e.value.status == R.Status.BAD_INPUT
+    extra_vo = vo.copy()
+    extra_vo[1:] += 1  # patch 0 gets one vertex no triangle uses
+    extra_p3 = np.concatenate([p3[:vo[1]], [[9.0, 9.0, 9.0]], p3[vo[1]:]])
+    extra_tr = tr.copy()
+    for c in (None, ctx):
+        with pytest.raises(R.RuvError) as e:
+            R.prepare_patches(extra_vo, to, extra_p3, extra_tr, ctx=c)
+        assert e.value.status == R.Status.BAD_INPUT
+
+
+def test_device_patches_solve_alike():
+    ctx = R.Context(0)
+    vo, to, p3, tr = W.disks(64, t_min=50, t_max=20000, seed=41)
+    a, b = R.prepare_patches(vo, to, p3, tr), R.prepare_patches(vo, to, p3, tr, ctx=ctx)
+    n = int(vo[-1])
+    ua, _, _ = R.solve_batch(ctx, a.batch(), R.UnfoldOptions(), n)
+    ub, _, _ = R.solve_batch(ctx, b.batch(), R.UnfoldOptions(), n)
+    assert np.array_equal(ua, ub)
