@@ -276,6 +276,120 @@ __global__ void k_propose2(int64_t ng, const int64_t* __restrict__ goff, const i
   prop[g] = best;
 }
 
+// The group graph of a level, built once for all matching rounds: per group g, its
+// neighbour groups h != g with the summed |a_ij| between their members, the keys in order of
+// first arrival (members in order, entries in order) and each sum in arrival order -- what
+// group_strengths accumulates, for every key.  A round then filters the stored row (the
+// first kAccCap wanted keys in arrival order are exactly the ones the bounded accumulator
+// keeps), so the matching is the same bit for bit.  Row g lives at gcap_off[g] (room for
+// the members' entries) with gn[g] keys.
+__global__ void k_group_nnz(int64_t ng, const int64_t* __restrict__ goff, const int32_t* __restrict__ mem,
+                            const int32_t* __restrict__ rp, int32_t* __restrict__ gcap) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  int32_t c = 0;
+  for (int64_t a = goff[g]; a < goff[g + 1]; ++a) c += rp[mem[a] + 1] - rp[mem[a]];
+  gcap[g] = c;
+}
+__global__ void k_group_graph(int64_t ng, const int64_t* __restrict__ goff, const int32_t* __restrict__ mem,
+                              const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                              const float* __restrict__ vals, const int32_t* __restrict__ grp_of,
+                              const int64_t* __restrict__ gcap_off, int32_t* __restrict__ gn, int32_t* __restrict__ gkey,
+                              float* __restrict__ gval) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  int32_t* K = gkey + gcap_off[g];
+  float* V = gval + gcap_off[g];
+  int n = 0;
+  for (int64_t a = goff[g]; a < goff[g + 1]; ++a) {
+    const int32_t i = mem[a];
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+      const int32_t h = grp_of[cols[e]];
+      if (h == (int32_t)g) continue;
+      const float v = fabsf(vals[e]);
+      int t = 0;
+      while (t < n && K[t] != h) ++t;
+      if (t < n) {
+        V[t] += v;
+      } else {
+        K[n] = h;
+        V[n] = v;
+        ++n;
+      }
+    }
+  }
+  gn[g] = n;
+}
+
+// k_propose2 over the stored group graph.
+__global__ void k_propose2_graph(int64_t ng, const int64_t* __restrict__ gcap_off, const int32_t* __restrict__ gn,
+                                 const int32_t* __restrict__ gkey, const float* __restrict__ gval,
+                                 const int32_t* __restrict__ gmate, int32_t* __restrict__ prop, int* __restrict__ stats,
+                                 float strong) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  int32_t best = -1;
+  if (gmate[g] < 0) {
+    const int32_t* K = gkey + gcap_off[g];
+    const float* V = gval + gcap_off[g];
+    const int n = gn[g];
+    float mx = 0.0f;
+    int kept = 0, t_end = n;
+    for (int t = 0; t < n; ++t) {
+      if (gmate[K[t]] >= 0) continue;
+      if (kept == kAccCap) {
+        t_end = t;
+        break;
+      }
+      ++kept;
+      mx = fmaxf(mx, V[t]);
+    }
+    warp_atomic_max(stats + 2, kept);
+    uint32_t bp = 0;
+    for (int t = 0; t < t_end; ++t) {
+      if (gmate[K[t]] >= 0) continue;
+      if (!(V[t] >= strong * mx) || mx == 0.0f) continue;
+      const uint32_t pr = pair_priority((int32_t)g, K[t]);
+      if (best < 0 || pr > bp || (pr == bp && K[t] < best)) {
+        bp = pr;
+        best = K[t];
+      }
+    }
+  }
+  prop[g] = best;
+}
+
+// k_group_lead over the stored group graph.
+__global__ void k_group_lead_graph(int64_t ng, const int64_t* __restrict__ gcap_off, const int32_t* __restrict__ gn,
+                                   const int32_t* __restrict__ gkey, const float* __restrict__ gval,
+                                   const int32_t* __restrict__ gmate, int32_t* __restrict__ glead_of,
+                                   uint8_t* __restrict__ glead) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  int32_t L;
+  if (gmate[g] >= 0) {
+    L = min((int32_t)g, gmate[g]);
+  } else {
+    const int32_t* K = gkey + gcap_off[g];
+    const float* V = gval + gcap_off[g];
+    const int n = gn[g];
+    int32_t best = -1;
+    float bs = -1.0f;
+    int kept = 0;
+    for (int t = 0; t < n && kept < kAccCap; ++t) {
+      if (gmate[K[t]] < 0) continue;
+      ++kept;
+      if (V[t] > bs || (V[t] == bs && K[t] < best)) {
+        bs = V[t];
+        best = K[t];
+      }
+    }
+    L = best >= 0 ? min(best, gmate[best]) : (int32_t)g;
+  }
+  glead_of[g] = L;
+  glead[g] = L == (int32_t)g ? 1 : 0;
+}
+
 // Lead group of each group after pairing groups (unmatched groups join the pair of their
 // strongest matched neighbour group).
 __global__ void k_group_lead(int64_t ng, const int64_t* __restrict__ goff, const int32_t* __restrict__ mem,
@@ -652,6 +766,93 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
     }
     __syncwarp(smask);
   }
+}
+
+// Rows of a sparse product whose inner rows hold ascending, distinct keys (the prolongator's
+// rows, the rows of W = A P) by a k-way merge instead of a hash table: G lanes per row, lane l
+// holding the inner rows of outer entries ob + l and ob + G + l; each step takes the row's
+// smallest head key, sums that key's products in outer-entry order starting from 0.0 (the
+// arrival order in which k_gal_hash accumulates them, so the sums are the same bits) and
+// advances the lanes that contributed.  Keys come out ascending.  Rows with more than 2 G
+// outer entries are listed for the large-table hash kernel.
+//   MODE 0: counts (cnt[row]); lists the long rows.  MODE 1: writes at off[row] (DIAG: also
+//   the inverse of the diagonal entry); skips the long rows.
+template <int MODE, int G, bool DIAG, class OP, class OV, class IP, class IV>
+__global__ void __launch_bounds__(256) k_gal_merge(int64_t nrows, const uint8_t* __restrict__ active,
+                                                   const OP* __restrict__ o_ptr, const int32_t* __restrict__ o_idx,
+                                                   const OV* __restrict__ o_val, const IP* __restrict__ i_ptr,
+                                                   const int32_t* __restrict__ i_idx, const IV* __restrict__ i_val,
+                                                   int32_t* __restrict__ cnt, const int64_t* __restrict__ off,
+                                                   int32_t* __restrict__ oc, double* __restrict__ ov,
+                                                   float* __restrict__ adinv, int32_t* __restrict__ list,
+                                                   int32_t* __restrict__ list_n) {
+  const int lane = threadIdx.x & 31, sl = lane & (G - 1), gb = lane & ~(G - 1);
+  const unsigned smask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gb);
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;  // uniform within the lane group
+  if (row >= nrows) return;
+  if (active && !active[row]) {
+    if (MODE == 0 && sl == 0) cnt[row] = 0;
+    return;
+  }
+  const int64_t ob = (int64_t)o_ptr[row], oe = (int64_t)o_ptr[row + 1];
+  if (oe - ob > 2 * G) {
+    if (MODE == 0 && sl == 0) {
+      cnt[row] = 0;
+      list[atomicAdd(list_n, 1)] = (int32_t)row;
+    }
+    return;
+  }
+  int64_t c[2] = {0, 0}, ce[2] = {0, 0};
+  double sc[2] = {0.0, 0.0};
+  int32_t key[2] = {INT_MAX, INT_MAX};
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int64_t q = ob + h * G + sl;
+    if (q < oe) {
+      const int32_t j = o_idx[q];
+      sc[h] = o_val ? (double)o_val[q] : 1.0;
+      c[h] = (int64_t)i_ptr[j];
+      ce[h] = (int64_t)i_ptr[j + 1];
+      if (c[h] < ce[h]) key[h] = i_idx[c[h]];
+    }
+  }
+  const int64_t o = MODE == 1 ? off[row] : 0;
+  int d = 0;
+  bool has_d = false;
+  double dval = 0.0;
+  for (;;) {
+    int32_t kmin = min(key[0], key[1]);
+#pragma unroll
+    for (int x = G / 2; x > 0; x >>= 1) kmin = min(kmin, __shfl_xor_sync(smask, kmin, x, G));
+    if (kmin == INT_MAX) break;
+    const bool mine0 = key[0] == kmin, mine1 = key[1] == kmin;
+    if (MODE == 1) {
+      const double v0 = mine0 ? sc[0] * (double)i_val[c[0]] : 0.0;
+      const double v1 = mine1 ? sc[1] * (double)i_val[c[1]] : 0.0;
+      double sum = 0.0;
+      for (unsigned m = __ballot_sync(smask, mine0); m != 0u; m &= m - 1u)
+        sum += __shfl_sync(smask, v0, (__ffs(m) - 1) - gb, G);
+      for (unsigned m = __ballot_sync(smask, mine1); m != 0u; m &= m - 1u)
+        sum += __shfl_sync(smask, v1, (__ffs(m) - 1) - gb, G);
+      if (sl == 0) {
+        oc[o + d] = kmin;
+        ov[o + d] = sum;
+      }
+      if (DIAG && kmin == (int32_t)row) {
+        has_d = true;
+        dval = sum;
+      }
+    }
+    ++d;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      if (key[h] == kmin) {
+        ++c[h];
+        key[h] = c[h] < ce[h] ? i_idx[c[h]] : INT_MAX;
+      }
+  }
+  if (MODE == 0 && sl == 0) cnt[row] = d;
+  if (MODE == 1 && DIAG && sl == 0) adinv[row] = has_d && dval > 0.0 ? (float)(1.0 / dval) : 0.0f;
 }
 
 // Staged rows to their place in the product (8 lanes per row); listed rows (sn < 0) are
@@ -1323,6 +1524,75 @@ void gal_fill(Ctx& ctx, GalWork& g, int64_t nrows, const OP* o_ptr, const int32_
   }
 }
 
+// The merge formulation of gal_count / gal_fill (k_gal_merge) for products whose inner rows
+// hold ascending, distinct keys; `avg_outer` (the mean outer row length) picks 8, 16 or 32
+// lanes per row.  RUV_GAL_MERGE=0 keeps the hash formulation (the same bits).
+inline bool gal_merge_on() {
+  const char* e = std::getenv("RUV_GAL_MERGE");
+  return !(e && e[0] == '0');
+}
+
+template <int MODE, int G, bool DIAG, class OP, class OV, class IP, class IV>
+void launch_merge(cudaStream_t s, int64_t nrows, const uint8_t* active, const OP* o_ptr, const int32_t* o_idx,
+                  const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, int32_t* cnt,
+                  const int64_t* off, int32_t* oc, double* ov, float* adinv, int32_t* list, int32_t* list_n) {
+  k_gal_merge<MODE, G, DIAG><<<div_up(nrows * G, 256), 256, 0, s>>>(nrows, active, o_ptr, o_idx, o_val, i_ptr, i_idx,
+                                                                     i_val, cnt, off, oc, ov, adinv, list, list_n);
+  count_launches(1);
+  RUV_LAUNCH_CHECK();
+}
+
+template <bool DIAG, class OP, class OV, class IP, class IV>
+void gal_merge_count(Ctx& ctx, GalWork& g, int64_t nrows, double avg_outer, const uint8_t* active, const OP* o_ptr,
+                     const int32_t* o_idx, const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val,
+                     int32_t* cnt) {
+  cudaStream_t s = ctx.stream;
+  g.h1 = 0;
+  if (nrows <= 0) return;
+  if (g.debug) {
+    RUV_CUDA(cudaStreamSynchronize(s));
+    g.t0 = std::chrono::steady_clock::now();
+  }
+  g.lanes = avg_outer <= 6.0 ? 8 : avg_outer <= 14.0 ? 16 : 32;
+  RUV_CUDA(cudaMemsetAsync(g.list_n, 0, sizeof(int32_t), s));
+#define M(GG) launch_merge<0, GG, DIAG>(s, nrows, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, cnt, nullptr, nullptr, \
+                                        nullptr, nullptr, g.list, g.list_n)
+  if (g.lanes == 8) M(8);
+  else if (g.lanes == 16) M(16);
+  else M(32);
+#undef M
+  RUV_CUDA(cudaMemcpyAsync(&g.h1, g.list_n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  if (g.h1 > 0) {
+    GalOut o0{cnt, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, g.ovf};
+    launch_gal<0, 32, kGalBigH, 1, DIAG>(s, g.h1, g.list, nullptr, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, KeyId{}, o0);
+  }
+}
+
+template <bool DIAG, class OP, class OV, class IP, class IV>
+void gal_merge_fill(Ctx& ctx, GalWork& g, int64_t nrows, const uint8_t* active, const OP* o_ptr, const int32_t* o_idx,
+                    const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, const int64_t* off,
+                    int32_t* oc, double* ov, float* adinv) {
+  cudaStream_t s = ctx.stream;
+  if (nrows <= 0) return;
+#define M(GG) launch_merge<1, GG, DIAG>(s, nrows, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, nullptr, off, oc, ov, \
+                                        adinv, nullptr, nullptr)
+  if (g.lanes == 8) M(8);
+  else if (g.lanes == 16) M(16);
+  else M(32);
+#undef M
+  if (g.h1 > 0) {
+    GalOut o1{nullptr, nullptr, nullptr, nullptr, off, oc, ov, adinv, nullptr, nullptr, g.ovf};
+    launch_gal<1, 32, kGalBigH, 1, DIAG>(s, g.h1, g.list, nullptr, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, KeyId{}, o1);
+  }
+  if (g.debug) {
+    RUV_CUDA(cudaStreamSynchronize(s));
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - g.t0).count();
+    std::fprintf(stderr, "  merge product rows %lld: %d lanes per row, large-table rows %d, %.3f ms\n",
+                 (long long)nrows, g.lanes, g.h1, ms);
+  }
+}
+
 }  // namespace
 
 AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string& info) {
@@ -1344,6 +1614,12 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   if (const char* e = std::getenv("RUV_AMG_STRONG")) strong = (float)std::atof(e);
   int pmax = kPMaxRow;
   if (const char* e = std::getenv("RUV_AMG_PMAX")) pmax = std::max(1, std::min(kAccCap, std::atoi(e)));
+  int rounds = kPairRounds;  // proposal rounds of each matching pass
+  if (const char* e = std::getenv("RUV_AMG_ROUNDS")) rounds = std::max(1, std::atoi(e));
+  // group matching over a group graph built once per level (RUV_AMG_GROUP_GRAPH=0: strengths
+  // accumulated again in every round; the same aggregates)
+  const char* gg_env = std::getenv("RUV_AMG_GROUP_GRAPH");
+  const bool graph = !(gg_env && gg_env[0] == '0');
   cudaEvent_t t_setup0;
   RUV_CUDA(cudaEventCreate(&t_setup0));
   RUV_CUDA(cudaEventRecord(t_setup0, s));
@@ -1412,7 +1688,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     int32_t* mate = ctx.ws.get<int32_t>(tag + ".mate", L.n);
     int32_t* prop = ctx.ws.get<int32_t>(tag + ".prop", L.n);
     RUV_CUDA(cudaMemsetAsync(mate, 0xff, sizeof(int32_t) * L.n, s));
-    for (int r = 0; r < kPairRounds; ++r) {
+    for (int r = 0; r < rounds; ++r) {
       k_propose<<<div_up(L.n, B), B, 0, s>>>(L.n, L.rp, L.cols, L.vals, active, mate, prop, strong);
       k_accept<<<div_up(L.n, B), B, 0, s>>>(L.n, prop, mate);
       count_launches(2);
@@ -1450,13 +1726,34 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     if (NG > 0) {
       k_sort_members<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem);
       count_launches(1);
-      for (int r = 0; r < kPairRounds; ++r) {
-        k_propose2<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, L.cols, L.vals, grp_of, gmate, gprop, ovf, strong);
-        k_accept<<<div_up(NG, B), B, 0, s>>>(NG, gprop, gmate);
-        count_launches(2);
+      if (graph) {  // the group graph once, then every round and the lead pass filter it
+        int32_t* gcap = ctx.ws.get<int32_t>(tag + ".gcap", NG);
+        int64_t* gcap_off = ctx.ws.get<int64_t>(tag + ".gcapoff", NG + 1);
+        int32_t* gn = ctx.ws.get<int32_t>(tag + ".gn", NG);
+        k_group_nnz<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, gcap);
+        count_launches(1);
+        exclusive_scan(gcap, gcap_off, NG, ctx.ws, s, tag + ".gcs");
+        const int64_t GE = read_i64(ctx, gcap_off + NG);
+        int32_t* gkey = ctx.ws.get<int32_t>("amg.gkey", std::max<int64_t>(GE, 1));
+        float* gval = ctx.ws.get<float>("amg.gval", std::max<int64_t>(GE, 1));
+        k_group_graph<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, L.cols, L.vals, grp_of, gcap_off, gn, gkey, gval);
+        count_launches(1);
+        for (int r = 0; r < rounds; ++r) {
+          k_propose2_graph<<<div_up(NG, B), B, 0, s>>>(NG, gcap_off, gn, gkey, gval, gmate, gprop, ovf, strong);
+          k_accept<<<div_up(NG, B), B, 0, s>>>(NG, gprop, gmate);
+          count_launches(2);
+        }
+        k_group_lead_graph<<<div_up(NG, B), B, 0, s>>>(NG, gcap_off, gn, gkey, gval, gmate, glead_of, glead);
+        count_launches(1);
+      } else {
+        for (int r = 0; r < rounds; ++r) {
+          k_propose2<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, L.cols, L.vals, grp_of, gmate, gprop, ovf, strong);
+          k_accept<<<div_up(NG, B), B, 0, s>>>(NG, gprop, gmate);
+          count_launches(2);
+        }
+        k_group_lead<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, L.cols, L.vals, grp_of, gmate, glead_of, glead);
+        count_launches(1);
       }
-      k_group_lead<<<div_up(NG, B), B, 0, s>>>(NG, goff, mem, L.rp, L.cols, L.vals, grp_of, gmate, glead_of, glead);
-      count_launches(1);
     }
     int64_t* aid = ctx.ws.get<int64_t>(tag + ".aid", NG + 1);
     exclusive_scan_u8(glead, aid, NG, ctx.ws, s, tag + ".as");
@@ -1539,19 +1836,33 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
                      C.vals64, C.dinv);
       finish_coarse();
     } else {
-      // ---- smoothed prolongator: W = A P, then A_c = R W
+      // ---- smoothed prolongator: W = A P, then A_c = R W (the rows of P and of W hold
+      // ascending, distinct keys: merged row by row unless RUV_GAL_MERGE=0)
       int32_t* wcnt = ctx.ws.get<int32_t>(tag + ".wcnt", L.n);
       int64_t* woff = ctx.ws.get<int64_t>(tag + ".woff", L.n + 1);
-      gal_count<false>(ctx, gw, L.n, mean(L.nnz, L.n) * mean(PN, L.n), active, L.rp, L.cols, L.vals64, L.poff, L.pc,
-                       L.pv, KeyId{}, wcnt);
+      const bool merge = gal_merge_on();
+      if (merge)
+        gal_merge_count<false>(ctx, gw, L.n, mean(L.nnz, L.n), active, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt);
+      else
+        gal_count<false>(ctx, gw, L.n, mean(L.nnz, L.n) * mean(PN, L.n), active, L.rp, L.cols, L.vals64, L.poff, L.pc,
+                         L.pv, KeyId{}, wcnt);
       WN = offsets_from_counts(ctx, wcnt, L.n, woff, tag + ".wo");
       int32_t* wc = ctx.ws.get<int32_t>(tag + ".wc", WN);
       double* wv = ctx.ws.get<double>(tag + ".wv", WN);
-      gal_fill<false>(ctx, gw, L.n, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, KeyId{}, woff, wc, wv, nullptr);
-      gal_count<true>(ctx, gw, NA, mean(PN, NA) * mean(WN, L.n), nullptr, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{},
-                      acnt);
+      if (merge)
+        gal_merge_fill<false>(ctx, gw, L.n, active, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, woff, wc, wv, nullptr);
+      else
+        gal_fill<false>(ctx, gw, L.n, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, KeyId{}, woff, wc, wv, nullptr);
+      if (merge)
+        gal_merge_count<true>(ctx, gw, NA, mean(PN, NA), nullptr, L.roff, L.rc, L.rv, woff, wc, wv, acnt);
+      else
+        gal_count<true>(ctx, gw, NA, mean(PN, NA) * mean(WN, L.n), nullptr, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{},
+                        acnt);
       alloc_coarse(offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao"));
-      gal_fill<true>(ctx, gw, NA, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{}, aoff, C.cols, C.vals64, C.dinv);
+      if (merge)
+        gal_merge_fill<true>(ctx, gw, NA, nullptr, L.roff, L.rc, L.rv, woff, wc, wv, aoff, C.cols, C.vals64, C.dinv);
+      else
+        gal_fill<true>(ctx, gw, NA, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{}, aoff, C.cols, C.vals64, C.dinv);
       finish_coarse();
     }
     L.n_next = NA;
