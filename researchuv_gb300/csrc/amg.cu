@@ -300,6 +300,10 @@ __global__ void k_group_graph(int64_t ng, const int64_t* __restrict__ goff, cons
   if (g >= ng) return;
   int32_t* K = gkey + gcap_off[g];
   float* V = gval + gcap_off[g];
+  // the first kLocal keys in a thread-local array (L1), the rest in the row's global area
+  constexpr int kLocal = 64;
+  int32_t lk[kLocal];
+  float lv[kLocal];
   int n = 0;
   for (int64_t a = goff[g]; a < goff[g + 1]; ++a) {
     const int32_t i = mem[a];
@@ -307,16 +311,30 @@ __global__ void k_group_graph(int64_t ng, const int64_t* __restrict__ goff, cons
       const int32_t h = grp_of[cols[e]];
       if (h == (int32_t)g) continue;
       const float v = fabsf(vals[e]);
+      const int nl = min(n, kLocal);
       int t = 0;
+      while (t < nl && lk[t] != h) ++t;
+      if (t < nl) {
+        lv[t] += v;
+        continue;
+      }
       while (t < n && K[t] != h) ++t;
       if (t < n) {
         V[t] += v;
+      } else if (n < kLocal) {
+        lk[n] = h;
+        lv[n] = v;
+        ++n;
       } else {
         K[n] = h;
         V[n] = v;
         ++n;
       }
     }
+  }
+  for (int t = 0; t < min(n, kLocal); ++t) {
+    K[t] = lk[t];
+    V[t] = lv[t];
   }
   gn[g] = n;
 }
@@ -769,15 +787,17 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
 }
 
 // Rows of a sparse product whose inner rows hold ascending, distinct keys (the prolongator's
-// rows, the rows of W = A P) by a k-way merge instead of a hash table: G lanes per row, lane l
-// holding the inner rows of outer entries ob + l and ob + G + l; each step takes the row's
-// smallest head key, sums that key's products in outer-entry order starting from 0.0 (the
-// arrival order in which k_gal_hash accumulates them, so the sums are the same bits) and
-// advances the lanes that contributed.  Keys come out ascending.  Rows with more than 2 G
-// outer entries are listed for the large-table hash kernel.
+// rows, the rows of W = A P) by a k-way merge instead of a hash table.  G lanes per row; lane
+// l owns the inner rows of outer entries ob + l and ob + G + l.  The group first copies the
+// row's products (key, scale * value) into its shared-memory area, every lane its own inner
+// rows with independent loads, then merges there: each step takes the smallest head key,
+// sums that key's products in outer-entry order starting from 0.0 (the arrival order in which
+// k_gal_hash accumulates them, so the sums are the same bits) and advances the lanes that
+// contributed.  Keys come out ascending.  Rows with more than 2 G outer entries or more than
+// CAP products are listed for the large-table hash kernel.
 //   MODE 0: counts (cnt[row]); lists the long rows.  MODE 1: writes at off[row] (DIAG: also
 //   the inverse of the diagonal entry); skips the long rows.
-template <int MODE, int G, bool DIAG, class OP, class OV, class IP, class IV>
+template <int MODE, int G, int CAP, bool DIAG, class OP, class OV, class IP, class IV>
 __global__ void __launch_bounds__(256) k_gal_merge(int64_t nrows, const uint8_t* __restrict__ active,
                                                    const OP* __restrict__ o_ptr, const int32_t* __restrict__ o_idx,
                                                    const OV* __restrict__ o_val, const IP* __restrict__ i_ptr,
@@ -786,7 +806,11 @@ __global__ void __launch_bounds__(256) k_gal_merge(int64_t nrows, const uint8_t*
                                                    int32_t* __restrict__ oc, double* __restrict__ ov,
                                                    float* __restrict__ adinv, int32_t* __restrict__ list,
                                                    int32_t* __restrict__ list_n) {
+  constexpr int GROUPS = 256 / G;
+  __shared__ int32_t skey[GROUPS][CAP];
+  __shared__ double sval[MODE == 1 ? GROUPS : 1][MODE == 1 ? CAP : 1];
   const int lane = threadIdx.x & 31, sl = lane & (G - 1), gb = lane & ~(G - 1);
+  const int grp = threadIdx.x / G;
   const unsigned smask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gb);
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;  // uniform within the lane group
   if (row >= nrows) return;
@@ -795,27 +819,53 @@ __global__ void __launch_bounds__(256) k_gal_merge(int64_t nrows, const uint8_t*
     return;
   }
   const int64_t ob = (int64_t)o_ptr[row], oe = (int64_t)o_ptr[row + 1];
-  if (oe - ob > 2 * G) {
-    if (MODE == 0 && sl == 0) {
-      cnt[row] = 0;
-      list[atomicAdd(list_n, 1)] = (int32_t)row;
-    }
-    return;
-  }
-  int64_t c[2] = {0, 0}, ce[2] = {0, 0};
+  int64_t ib[2] = {0, 0};
+  int len[2] = {0, 0};
   double sc[2] = {0.0, 0.0};
-  int32_t key[2] = {INT_MAX, INT_MAX};
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int64_t q = ob + h * G + sl;
     if (q < oe) {
       const int32_t j = o_idx[q];
       sc[h] = o_val ? (double)o_val[q] : 1.0;
-      c[h] = (int64_t)i_ptr[j];
-      ce[h] = (int64_t)i_ptr[j + 1];
-      if (c[h] < ce[h]) key[h] = i_idx[c[h]];
+      ib[h] = (int64_t)i_ptr[j];
+      len[h] = (int)((int64_t)i_ptr[j + 1] - ib[h]);
     }
   }
+  // segment starts: lane l's first inner row after every lower lane's first, then the second
+  // inner rows in the same way (outer-entry order)
+  int x0 = len[0], x1 = len[1];
+#pragma unroll
+  for (int o = 1; o < G; o <<= 1) {
+    const int y0 = __shfl_up_sync(smask, x0, o, G), y1 = __shfl_up_sync(smask, x1, o, G);
+    if (sl >= o) {
+      x0 += y0;
+      x1 += y1;
+    }
+  }
+  const int tot0 = __shfl_sync(smask, x0, G - 1, G), tot1 = __shfl_sync(smask, x1, G - 1, G);
+  if (oe - ob > 2 * G || tot0 + tot1 > CAP) {
+    if (MODE == 0 && sl == 0) {
+      cnt[row] = 0;
+      list[atomicAdd(list_n, 1)] = (int32_t)row;
+    }
+    return;
+  }
+  int beg[2] = {x0 - len[0], tot0 + x1 - len[1]};
+  int32_t* K = skey[grp];
+  double* Vs = sval[MODE == 1 ? grp : 0];
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+    for (int t = 0; t < len[h]; ++t) {
+      K[beg[h] + t] = i_idx[ib[h] + t];
+      if (MODE == 1) Vs[beg[h] + t] = sc[h] * (double)i_val[ib[h] + t];
+    }
+  __syncwarp(smask);
+  int pos[2] = {beg[0], beg[1]};
+  const int end[2] = {beg[0] + len[0], beg[1] + len[1]};
+  int32_t key[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) key[h] = pos[h] < end[h] ? K[pos[h]] : INT_MAX;
   const int64_t o = MODE == 1 ? off[row] : 0;
   int d = 0;
   bool has_d = false;
@@ -823,12 +873,12 @@ __global__ void __launch_bounds__(256) k_gal_merge(int64_t nrows, const uint8_t*
   for (;;) {
     int32_t kmin = min(key[0], key[1]);
 #pragma unroll
-    for (int x = G / 2; x > 0; x >>= 1) kmin = min(kmin, __shfl_xor_sync(smask, kmin, x, G));
+    for (int xx = G / 2; xx > 0; xx >>= 1) kmin = min(kmin, __shfl_xor_sync(smask, kmin, xx, G));
     if (kmin == INT_MAX) break;
     const bool mine0 = key[0] == kmin, mine1 = key[1] == kmin;
     if (MODE == 1) {
-      const double v0 = mine0 ? sc[0] * (double)i_val[c[0]] : 0.0;
-      const double v1 = mine1 ? sc[1] * (double)i_val[c[1]] : 0.0;
+      const double v0 = mine0 ? Vs[pos[0]] : 0.0;
+      const double v1 = mine1 ? Vs[pos[1]] : 0.0;
       double sum = 0.0;
       for (unsigned m = __ballot_sync(smask, mine0); m != 0u; m &= m - 1u)
         sum += __shfl_sync(smask, v0, (__ffs(m) - 1) - gb, G);
@@ -847,8 +897,8 @@ __global__ void __launch_bounds__(256) k_gal_merge(int64_t nrows, const uint8_t*
 #pragma unroll
     for (int h = 0; h < 2; ++h)
       if (key[h] == kmin) {
-        ++c[h];
-        key[h] = c[h] < ce[h] ? i_idx[c[h]] : INT_MAX;
+        ++pos[h];
+        key[h] = pos[h] < end[h] ? K[pos[h]] : INT_MAX;
       }
   }
   if (MODE == 0 && sl == 0) cnt[row] = d;
@@ -1157,8 +1207,12 @@ __global__ void __launch_bounds__(kAmgThreads) k_prolong_add(LvlTiles T, const i
 }
 
 // K-cycle coarse correction (the K-form of gpu/src/amg.rs:468-639): w = A y over the rows of
-// the level's continuing charts, with per-tile partial sums t.t and t.w (FP32 per row, FP64
-// per tile, fixed combine order) for the steplength beta = (t.t) / (t.A y).
+// the level's continuing charts, with per-tile partial sums y.t and y.w (FP32 per row, FP64
+// per tile, fixed combine order) for the steplength beta = (y.t) / (y.A y), the step along y
+// that minimises the A-norm of the error (the K-cycle's published form, Notay and
+// Vassilevski).  The reference divides t.t by t.A y instead; with the FP32 cycle that
+// quotient is not energy-decreasing, and the outer flexible CG stalled with it (16384
+// iterations without converging on charts the V-cycle solves in a few dozen).
 template <int NR, int LPR, int U, int K, bool NARROW>
 __global__ void __launch_bounds__(kAmgThreads) k_kspmv(LvlTiles T, const int32_t* __restrict__ done,
                                                        const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
@@ -1177,15 +1231,15 @@ __global__ void __launch_bounds__(kAmgThreads) k_kspmv(LvlTiles T, const int32_t
         [&](int32_t j) { return ldf<NR>(y, j); },
         [&](int64_t i, const F<NR>& sv) {
           stf<NR>(w, i, sv);
-          const F<NR> ti = ldf<NR>(t, i);
-          float tt = 0.0f, tw = 0.0f;
+          const F<NR> ti = ldf<NR>(t, i), yi = ldf<NR>(y, i);
+          float yt = 0.0f, yw = 0.0f;
 #pragma unroll
           for (int c = 0; c < NR; ++c) {
-            tt += ti.c[c] * ti.c[c];
-            tw += ti.c[c] * sv.c[c];
+            yt += yi.c[c] * ti.c[c];
+            yw += yi.c[c] * sv.c[c];
           }
-          acc[0] += (double)tt;
-          acc[1] += (double)tw;
+          acc[0] += (double)yt;
+          acc[1] += (double)yw;
         });
   };
   if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
@@ -1198,7 +1252,8 @@ __global__ void __launch_bounds__(kAmgThreads) k_kspmv(LvlTiles T, const int32_t
 }
 
 // beta per chart from its tiles' partial sums (one CTA per chart, fixed combine order); a
-// non-positive or tiny t.A y skips the correction (beta = 0), as the reference guards it.
+// non-positive or tiny y.A y skips the correction (beta = 0), as the reference guards its
+// denominator.
 __global__ void __launch_bounds__(128) k_kbeta(const int32_t* __restrict__ done, const int64_t* __restrict__ chart_tile,
                                                const double* __restrict__ part, float* __restrict__ beta) {
   __shared__ double sh[2 * 32];
@@ -1532,12 +1587,19 @@ inline bool gal_merge_on() {
   return !(e && e[0] == '0');
 }
 
+// products a row may stage in shared memory (per lane group): 8 lanes 64, 16 lanes 128,
+// 32 lanes 512 (MODE 1 stages the values too: 24, 24 and 48 KB per 256-thread block)
+template <int G>
+constexpr int merge_cap() {
+  return G == 32 ? 512 : 8 * G;
+}
+
 template <int MODE, int G, bool DIAG, class OP, class OV, class IP, class IV>
 void launch_merge(cudaStream_t s, int64_t nrows, const uint8_t* active, const OP* o_ptr, const int32_t* o_idx,
                   const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, int32_t* cnt,
                   const int64_t* off, int32_t* oc, double* ov, float* adinv, int32_t* list, int32_t* list_n) {
-  k_gal_merge<MODE, G, DIAG><<<div_up(nrows * G, 256), 256, 0, s>>>(nrows, active, o_ptr, o_idx, o_val, i_ptr, i_idx,
-                                                                     i_val, cnt, off, oc, ov, adinv, list, list_n);
+  k_gal_merge<MODE, G, merge_cap<G>(), DIAG><<<div_up(nrows * G, 256), 256, 0, s>>>(
+      nrows, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, cnt, off, oc, ov, adinv, list, list_n);
   count_launches(1);
   RUV_LAUNCH_CHECK();
 }
@@ -2154,7 +2216,7 @@ int cycle(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k);
 // Level k in the K-form (gpu/src/amg.rs:468-639), for the charts that continue below it:
 // pre-smoothing from zero (x = w D^-1 b, t = b - A x), then two coarse corrections
 // y = P (cycle of level k + 1 on R t), each scaled by its CG steplength
-// beta = (t.t) / (t.A y) per chart (x += beta y; the first also t -= beta A y), no
+// beta = (y.t) / (y.A y) per chart (x += beta y; the first also t -= beta A y), no
 // post-smoothing.  Charts whose last level is k get their direct solve.
 template <int NR>
 int kform(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k) {
