@@ -152,6 +152,11 @@ struct Tiles {
   const int32_t* chart;    // chart of each tile
   const int64_t* chart_tile;
   int64_t n;
+  // bulk-copy SpMV (k_spmv_tma): the largest tile's rows and nonzeros (0: not set up), the
+  // flag a timed-out staging wait sets, and the wait's iteration limit
+  int64_t max_rows = 0, max_nnz = 0;
+  int* err = nullptr;
+  int64_t spin_limit = 0;
 };
 
 // ---------------------------------------------------------------- tile kernels
@@ -313,14 +318,218 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_pq_k(Tiles T, const Chart
   if (threadIdx.x == 0) part[t] = (double)acc[0];
 }
 
+// ---------------------------------------------------------------- bulk-copy SpMV
+// the largest tile's nonzeros and rows (for the bulk-copy SpMV's staging size)
+__global__ void k_tile_max(Tiles T, const int32_t* __restrict__ row_ptr, unsigned long long* __restrict__ mx) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T.n) return;
+  const int64_t b = T.tab[2 * t], e = T.tab[2 * t + 1];
+  atomicMax(mx, (unsigned long long)(row_ptr[e] - row_ptr[b]));
+  atomicMax(mx + 1, (unsigned long long)(e - b));
+}
+
+
+// The same q = A p with the fused p.q as k_spmv_pq_k, but each CTA first stages its tile's
+// row pointers, FP32 values and column stream into shared memory with 1-D bulk asynchronous
+// copies (cp.async.bulk, completing on an mbarrier) and then runs the row loop from shared
+// memory: the per-row chain of dependent global loads (row pointers, then values and
+// columns, then the gathers of p) loses its first two links, and the copy engine keeps a
+// whole tile of bytes in flight per CTA.  Windows are widened to 16-byte boundaries (the
+// bulk copy's alignment rule); the workspace allocations carry the slack that the widened
+// end may read.  The staging wait is bounded: past its iteration limit the CTA sets T.err,
+// waits once more (bounded) for its own copies and returns.
+struct Win {
+  const char* src;   // 16-byte aligned start in global memory
+  int64_t first;     // element index of the first staged element
+  uint32_t bytes;    // multiple of 16
+};
+__device__ __forceinline__ Win stage_window(const void* base, int64_t e0, int64_t e1, int es) {
+  const uint64_t b0 = (uint64_t)e0 * es, b1 = (uint64_t)e1 * es;
+  const uint64_t a0 = b0 & ~(uint64_t)15, a1 = (b1 + 15) & ~(uint64_t)15;
+  return Win{static_cast<const char*>(base) + a0, (int64_t)(a0 / es), (uint32_t)(a1 - a0)};
+}
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  if (bytes == 0) return;
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, int64_t limit) {
+  const uint32_t a = smem_addr(bar);
+  for (int64_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// bytes of dynamic shared memory the bulk-copy SpMV needs for the largest tile
+template <class S, bool NARROW>
+inline size_t spmv_tma_smem(const Tiles& T) {
+  auto up16 = [](int64_t b) { return (size_t)((b + 15) & ~(int64_t)15); };
+  return 16 + up16(4 * (T.max_rows + 1) + 16) + up16((int64_t)sizeof(S) * T.max_nnz + 16) +
+         up16((NARROW ? 2 : 4) * T.max_nnz + 16);
+}
+constexpr size_t kSpmvTmaMaxSmem = 100 * 1024;  // two CTAs per SM at least
+
+template <class S, int NR, int LPR, int U, bool NARROW>
+__global__ void __launch_bounds__(kTileThreads) k_spmv_tma(Tiles T, const ChartState* __restrict__ st,
+                                                           const int32_t* __restrict__ row_ptr,
+                                                           const int32_t* __restrict__ cols,
+                                                           const uint16_t* __restrict__ c16,
+                                                           const int32_t* __restrict__ cbase, const S* __restrict__ vals,
+                                                           const S* __restrict__ p, S* __restrict__ q,
+                                                           double* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char stage[];
+  __shared__ S sh[32];
+  const int64_t t = blockIdx.x;
+  const int32_t ch = T.chart[t];
+  if (st[ch].state != kActive) return;
+  const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
+  const int64_t e0 = row_ptr[beg], e1 = row_ptr[end];
+  const Win wr = stage_window(row_ptr, beg, end + 1, 4);
+  const Win wv = stage_window(vals, e0, e1, (int)sizeof(S));
+  const Win wc = NARROW ? stage_window(c16, e0, e1, 2) : stage_window(cols, e0, e1, 4);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(stage);
+  unsigned char* sr = stage + 16;
+  unsigned char* sv = sr + wr.bytes;
+  unsigned char* sc = sv + wv.bytes;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(wr.bytes + wv.bytes + wc.bytes)
+                 : "memory");
+    bulk_g2s(sr, wr.src, wr.bytes, bar);
+    bulk_g2s(sv, wv.src, wv.bytes, bar);
+    bulk_g2s(sc, wc.src, wc.bytes, bar);
+  }
+  __syncthreads();  // the barrier is initialised before anyone waits on it
+  if (!mbar_wait(bar, 0, T.spin_limit)) {
+    if (threadIdx.x == 0) atomicOr(T.err, 1);
+    mbar_wait(bar, 0, T.spin_limit);  // (bounded) let this CTA's own copies land before it exits
+    return;
+  }
+  const int32_t* rs = reinterpret_cast<const int32_t*>(sr);
+  const S* vs = reinterpret_cast<const S*>(sv);
+  const int32_t cb = NARROW ? cbase[ch] : 0;
+  auto col = [&](int64_t e) -> int32_t {
+    if constexpr (NARROW) return cb + (int32_t)(reinterpret_cast<const uint16_t*>(sc)[e - wc.first]);
+    else return reinterpret_cast<const int32_t*>(sc)[e - wc.first];
+  };
+  // the row loop of spmv_pq_tile, reading row pointers, values and columns from the stage
+  constexpr int K = (8 + LPR - 1) / LPR;
+  const int sub = threadIdx.x % LPR;
+  const int rpp = kTileThreads / LPR;
+  S acc = S(0);
+  for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
+    int lo[U], hi[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      const bool valid = i < end;
+      lo[u] = valid ? rs[i - wr.first] : 0;
+      hi[u] = valid ? rs[i + 1 - wr.first] : 0;
+    }
+    S av[U][K];
+    int cv[U][K];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int e = lo[u] + sub + k * LPR;
+        const bool in = e < hi[u];
+        av[u][k] = in ? vs[e - wv.first] : S(0);
+        cv[u][k] = in ? col(e) : -1;
+      }
+    V<S, NR> sm[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int c = 0; c < NR; ++c) sm[u].c[c] = S(0);
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (cv[u][k] >= 0) {
+          const V<S, NR> pv = ldv<S, NR>(p, cv[u][k]);
+#pragma unroll
+          for (int c = 0; c < NR; ++c) sm[u].c[c] += av[u][k] * pv.c[c];
+        }
+      for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {  // rows longer than K * LPR
+        const S a = vs[e - wv.first];
+        const V<S, NR> pv = ldv<S, NR>(p, col(e));
+#pragma unroll
+        for (int c = 0; c < NR; ++c) sm[u].c[c] += a * pv.c[c];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int o = LPR / 2; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < NR; ++c) sm[u].c[c] += __shfl_xor_sync(0xffffffffu, sm[u].c[c], o, LPR);
+    if (sub == 0) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+        if (i < end) {
+          stv<S, NR>(q, i, sm[u]);
+          const V<S, NR> pi = ldv<S, NR>(p, i);
+#pragma unroll
+          for (int c = 0; c < NR; ++c) acc += pi.c[c] * sm[u].c[c];
+        }
+      }
+    }
+  }
+  S accv[1] = {acc};
+  block_sum_t<1, S>(accv, sh);
+  if (threadIdx.x == 0) part[t] = (double)accv[0];
+}
+
 // One launch of the SpMV: the 16-bit column instance when the system has that stream (every
 // chart of at most 65536 rows), the 32-bit one otherwise.
 template <class S, int NR, int LPR, int U>
 void launch_spmv(cudaStream_t s, unsigned grid, Tiles T, const ChartState* st, const int32_t* row_ptr,
                  const int32_t* cols, const uint16_t* c16, const int32_t* cbase, const S* vals, const S* p, S* q,
                  double* part) {
+  if constexpr (std::is_same<S, float>::value && NR == 2) {
+    if (T.max_rows > 0) {  // the bulk-copy kernel where the context set it up (spmv_tma_prepare)
+      if (c16) {
+        const size_t sm = spmv_tma_smem<S, true>(T);
+        if (sm <= kSpmvTmaMaxSmem) {
+          k_spmv_tma<S, NR, LPR, U, true><<<grid, kTileThreads, sm, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q,
+                                                                         part);
+          return;
+        }
+      } else {
+        const size_t sm = spmv_tma_smem<S, false>(T);
+        if (sm <= kSpmvTmaMaxSmem) {
+          k_spmv_tma<S, NR, LPR, U, false><<<grid, kTileThreads, sm, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q,
+                                                                          part);
+          return;
+        }
+      }
+    }
+  }
   if (c16) k_spmv_pq_k<S, NR, LPR, U, true><<<grid, kTileThreads, 0, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q, part);
   else k_spmv_pq_k<S, NR, LPR, U, false><<<grid, kTileThreads, 0, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q, part);
+}
+
+// Allows the bulk-copy kernels the dynamic shared memory they need (outside any capture).
+template <class S, int NR, int LPR, int U>
+void spmv_tma_attributes() {
+  if constexpr (std::is_same<S, float>::value && NR == 2) {
+    RUV_CUDA(cudaFuncSetAttribute(k_spmv_tma<S, NR, LPR, U, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kSpmvTmaMaxSmem));
+    RUV_CUDA(cudaFuncSetAttribute(k_spmv_tma<S, NR, LPR, U, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kSpmvTmaMaxSmem));
+  }
 }
 
 // x += alpha p; r -= alpha q; z = M^-1 r.  Partials: r.r, r.z.  precond: 0 = none (z = r),
@@ -889,7 +1098,8 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
   k_chart_init<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, o.tol, none, n_active);
   count_launches(1);
   RUV_LAUNCH_CHECK();
-  int* h_active = static_cast<int*>(ctx.pinned.get(sizeof(int)));
+  int* h_active = static_cast<int*>(ctx.pinned.get(3 * sizeof(int)));
+  spmv_tma_attributes<S, NR, LPR, U>();
   RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   RUV_CUDA(cudaStreamSynchronize(s));
   if (*h_active > 0 && NTL > 0) {
@@ -934,7 +1144,12 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
         count_launches((int64_t)kCheckEvery * (mixed ? 8 : 5));
         launched += kCheckEvery;
         RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+        if (T.err) RUV_CUDA(cudaMemcpyAsync(h_active + 2, T.err, sizeof(int), cudaMemcpyDeviceToHost, s));
         RUV_CUDA(cudaStreamSynchronize(s));
+        if (T.err && h_active[2] != 0) {
+          RUV_CUDA(cudaMemsetAsync(T.err, 0, sizeof(int), s));
+          throw Error{RUV_ERR_TIMEOUT, "SpMV: a bounded wait for the staged tile ran out"};
+        }
         if (*h_active <= 0) break;
       }
     } catch (...) {
@@ -1006,7 +1221,8 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
   k_chart_init<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, o.tol, 0, n_active);  // (rz replaced below)
   count_launches(1);
   RUV_LAUNCH_CHECK();
-  int* h_active = static_cast<int*>(ctx.pinned.get(2 * sizeof(int)));
+  int* h_active = static_cast<int*>(ctx.pinned.get(3 * sizeof(int)));
+  spmv_tma_attributes<S, NR, LPR, U>();
   RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   RUV_CUDA(cudaStreamSynchronize(s));
   if (*h_active > 0 && NTL > 0) {
@@ -1075,7 +1291,12 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
         launched += kRep;
         RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
         if (perr) RUV_CUDA(cudaMemcpyAsync(h_active + 1, perr, sizeof(int), cudaMemcpyDeviceToHost, s));
+        if (T.err) RUV_CUDA(cudaMemcpyAsync(h_active + 2, T.err, sizeof(int), cudaMemcpyDeviceToHost, s));
         RUV_CUDA(cudaStreamSynchronize(s));
+        if (T.err && h_active[2] != 0) {
+          RUV_CUDA(cudaMemsetAsync(T.err, 0, sizeof(int), s));
+          throw Error{RUV_ERR_TIMEOUT, "SpMV: a bounded wait for the staged tile ran out"};
+        }
         if (perr && h_active[1] != 0) {
           RUV_CUDA(cudaMemsetAsync(const_cast<int*>(perr), 0, sizeof(int), s));
           throw Error{RUV_ERR_TIMEOUT, "preconditioner: a bounded device-side wait ran out"};
@@ -1132,8 +1353,27 @@ Tiles upload_tiles(Ctx& ctx, const DevSystem& sys, const std::string& tag) {
     RUV_CUDA(cudaMemcpyAsync(d_chart, TT.chart.data(), sizeof(int32_t) * NTL, cudaMemcpyHostToDevice, s));
   }
   RUV_CUDA(cudaMemcpyAsync(d_ctile, TT.chart_tile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
+  Tiles T{d_tab, d_chart, d_ctile, NTL};
+  // the bulk-copy SpMV: its staging size from the largest tile (RUV_SPMV_TMA=0: not used)
+  const char* te = std::getenv("RUV_SPMV_TMA");
+  if (NTL > 0 && sys.row_ptr && !(te && te[0] == '0')) {
+    unsigned long long* mx = ctx.ws.get<unsigned long long>(tag + ".tmax", 2);
+    int* err = ctx.ws.get<int>(tag + ".terr", 1);
+    RUV_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), s));
+    RUV_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    k_tile_max<<<div_up(NTL, 256), 256, 0, s>>>(T, sys.row_ptr, mx);
+    count_launches(1);
+    unsigned long long h[2] = {0, 0};
+    RUV_CUDA(cudaMemcpyAsync(h, mx, sizeof(h), cudaMemcpyDeviceToHost, s));
+    RUV_CUDA(cudaStreamSynchronize(s));
+    T.max_nnz = (int64_t)h[0];
+    T.max_rows = (int64_t)h[1];
+    T.err = err;
+    const char* le = std::getenv("RUV_SPIN_LIMIT");
+    T.spin_limit = le ? std::max<int64_t>(1, std::atoll(le)) : (int64_t(1) << 22);
+  }
   RUV_CUDA(cudaStreamSynchronize(s));  // the host tables go out of scope
-  return Tiles{d_tab, d_chart, d_ctile, NTL};
+  return T;
 }
 
 // SpMV shape: explicit (RUV_LPR / RUV_UNROLL via the context) or from the row-length
@@ -1152,6 +1392,7 @@ Shape pick_shape(const Ctx& ctx, const DevSystem& sys) {
 template <class S, int NR, int LPR, int U>
 double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
   cudaStream_t s = ctx.stream;
+  spmv_tma_attributes<S, NR, LPR, U>();
   const int64_t N = sys.n_rows, NC = sys.n_charts;
   ChartState* st = ctx.ws.get<ChartState>("bench.state", NC);
   RUV_CUDA(cudaMemsetAsync(st, 0, sizeof(ChartState) * NC, s));  // every chart active

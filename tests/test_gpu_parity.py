@@ -274,3 +274,44 @@ def test_galerkin_merge_and_group_graph_bitwise(monkeypatch):
         assert a.status == b.status == R.Status.OK
         assert a.cg_iters == b.cg_iters
         assert np.array_equal(a.uv, b.uv)
+
+
+@pytest.mark.parametrize("case", ["disks_16bit_columns", "field_32bit_columns"])
+def test_bulk_copy_spmv_bitwise(monkeypatch, case):
+    """The SpMV that stages each tile's row pointers, values and columns into shared memory
+    by bulk asynchronous copies (the default; RUV_SPMV_TMA=0 keeps the CSR-vector kernel
+    reading them from global memory) runs the same row loop: bitwise the same UVs and
+    iterations, with the 16-bit column stream (charts of <= 65536 rows) and with 32-bit
+    columns (a 258k-row chart)."""
+    if case == "disks_16bit_columns":
+        vo, to, p3, tr = W.disks(24, t_min=200, t_max=20000, seed=53)
+        C = R.prepare_patches(vo, to, p3, tr)
+    else:
+        p, f = W.height_field(512, 8, 0.15, seed=2)
+        C = R.prepare_mesh(p, f)
+    ctx = R.Context(0)
+    for pc in (R.Precond.JACOBI, R.Precond.AMG_SA):
+        opts = R.UnfoldOptions(precond=pc, precision=R.Precision.MIXED)
+        monkeypatch.setenv("RUV_SPMV_TMA", "0")
+        plain = R.unfold_charts(ctx, C, opts)
+        monkeypatch.delenv("RUV_SPMV_TMA", raising=False)
+        staged = R.unfold_charts(ctx, C, opts)
+        for a, b in zip(plain, staged):
+            assert a.status == b.status == R.Status.OK
+            assert a.cg_iters == b.cg_iters
+            assert np.array_equal(a.uv, b.uv)
+
+
+def test_bulk_copy_spmv_wait_is_bounded(monkeypatch):
+    """The staging wait is bounded: with a spin limit of 1 a solve either finishes (the copies
+    landed within the first try) or returns TIMEOUT, and the context then solves normally."""
+    vo, to, p3, tr = W.disks(8, t_min=2000, t_max=20000, seed=59)
+    C = R.prepare_patches(vo, to, p3, tr)
+    nv = int(C.i64("chart.vert_off")[-1])
+    ctx = R.Context(0)
+    monkeypatch.setenv("RUV_SPIN_LIMIT", "1")
+    _, _, st = R.solve_batch(ctx, C.batch(), R.UnfoldOptions(precond=R.Precond.JACOBI), nv, check=False)
+    assert st in (R.Status.OK, R.Status.TIMEOUT), R.Status(st).name
+    monkeypatch.delenv("RUV_SPIN_LIMIT")
+    _, stats, st = R.solve_batch(ctx, C.batch(), R.UnfoldOptions(precond=R.Precond.JACOBI), nv)
+    assert st == R.Status.OK
