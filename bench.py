@@ -844,14 +844,16 @@ def main():
     for _ in range(max(args.warmup, 1)):  # untimed, as for the device-timed loop
         ctx.check(L.ruv_lscm_solve_batch(ctx.h, ctypes.byref(pbatch), ctypes.byref(copts),
                                          uv.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), stats), "e2e warm-up")
-    e2e_dev = []
+    e2e_dev, e2e_asm = [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         st_ = L.ruv_lscm_solve_batch(ctx.h, ctypes.byref(pbatch), ctypes.byref(copts),
                                      uv.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), stats)
         e2e_ms.append(1000.0 * (time.perf_counter() - t0))
         ctx.check(st_, "e2e")
-        e2e_dev.append(sum(R.last_timings(ctx)[:3]))
+        tt = R.last_timings(ctx)
+        e2e_dev.append(sum(tt[:3]))
+        e2e_asm.append(tt[0])
     barrier(pg)
     ms = allmax(pg, statistics.mean(dev_ms))
     ems = allmax(pg, statistics.mean(e2e_ms))
@@ -887,7 +889,8 @@ def main():
                 "d2h_bytes_per_step": d2h, "ms_per_step": ems,
                 "ms_median": statistics.median(e2e_ms), "ms_min": min(e2e_ms),
                 "per_call_ms": [round(x, 2) for x in e2e_ms],
-                "per_call_device_ms": [round(x, 2) for x in e2e_dev]},
+                "per_call_device_ms": [round(x, 2) for x in e2e_dev],
+                "per_call_assembly_ms": [round(x, 2) for x in e2e_asm]},
         "roofline": {"bound": "hbm", "kernel": "k_spmv_pq (batched CSR-vector SpMV + p.q)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src,
