@@ -1128,6 +1128,62 @@ __device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_
   }
 }
 
+// tile_rows with the row pointers read through a functor (a staged tile in shared memory).
+template <int NR, int LPR, int U, int K, class RP, class Col, class W, class G, class Fin>
+__device__ __forceinline__ void tile_rows_rp(int64_t beg, int64_t end, RP rpf, Col cols, W w, G g, Fin fin) {
+  const int sub = threadIdx.x % LPR;
+  const int rpp = kAmgThreads / LPR;
+  for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
+    int64_t lo[U], hi[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      const bool valid = i < end;
+      lo[u] = valid ? rpf(i) : 0;
+      hi[u] = valid ? rpf(i + 1) : 0;
+    }
+    float av[U][K];
+    int cv[U][K];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int64_t e = lo[u] + sub + k * LPR;
+        const bool in = e < hi[u];
+        av[u][k] = in ? w(e) : 0.0f;
+        cv[u][k] = in ? cols(e) : -1;
+      }
+    F<NR> s[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int c = 0; c < NR; ++c) s[u].c[c] = 0.0f;
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (cv[u][k] >= 0) {
+          const F<NR> v = g(cv[u][k]);
+#pragma unroll
+          for (int c = 0; c < NR; ++c) s[u].c[c] += av[u][k] * v.c[c];
+        }
+      for (int64_t e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {
+        const float a = w(e);
+        const F<NR> v = g(cols(e));
+#pragma unroll
+        for (int c = 0; c < NR; ++c) s[u].c[c] += a * v.c[c];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int o = LPR / 2; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < NR; ++c) s[u].c[c] += __shfl_xor_sync(0xffffffffu, s[u].c[c], o, LPR);
+      const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      if (sub == 0 && i < end) fin(i, s[u]);
+    }
+  }
+}
+
 // Down 1: x = w D^-1 b;  t = b - A x  (x of neighbours formed on the fly).
 template <int NR, int LPR, int U, int K, bool NARROW>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const int32_t* __restrict__ done,
@@ -1165,6 +1221,108 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const i
   };
   if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
   else run(ColsWide{cols});
+}
+
+// Staged forms of the level-0 smoothers: each CTA first stages its tile's row pointers, FP32
+// values and column stream into shared memory by bulk asynchronous copies (stage_rows, a
+// bounded wait that sets *err) and then runs the same row loop from there; the same
+// arithmetic in the same order, so the same results.
+template <class ColsT, bool NARROW>
+struct StagedOp {
+  StagedRows S;
+  int32_t cb;
+  __device__ __forceinline__ int64_t rp(int64_t i) const { return (int64_t)S.rp[i - S.fr]; }
+  __device__ __forceinline__ float w(int64_t e) const { return reinterpret_cast<const float*>(S.v)[e - S.fv]; }
+  __device__ __forceinline__ int32_t col(int64_t e) const {
+    if constexpr (NARROW) return cb + (int32_t)(reinterpret_cast<const uint16_t*>(S.c)[e - S.fc]);
+    else return reinterpret_cast<const int32_t*>(S.c)[e - S.fc];
+  }
+};
+
+template <int NR, int LPR, int U, int K, bool NARROW>
+__global__ void __launch_bounds__(kAmgThreads) k_smooth_down_st(LvlTiles T, const int32_t* __restrict__ done,
+                                                                const int32_t* __restrict__ rp,
+                                                                const int32_t* __restrict__ cols,
+                                                                const uint16_t* __restrict__ c16,
+                                                                const int32_t* __restrict__ cbase,
+                                                                const float* __restrict__ vals,
+                                                                const float* __restrict__ dinv,
+                                                                const float* __restrict__ b, float* __restrict__ x,
+                                                                float* __restrict__ t, int64_t limit, int* err) {
+  extern __shared__ __align__(16) unsigned char stage[];
+  const int64_t tl = blockIdx.x;
+  const int32_t ch = T.chart[tl];
+  if (done[ch]) return;
+  const int64_t beg = T.tab[2 * tl], end = T.tab[2 * tl + 1];
+  StagedOp<int, NARROW> op;
+  if (!stage_rows(stage, rp, beg, end, vals, 4, NARROW ? (const void*)c16 : (const void*)cols, NARROW ? 2 : 4, limit,
+                  err, op.S))
+    return;
+  op.cb = NARROW ? cbase[ch] : 0;
+  tile_rows_rp<NR, LPR, U, K>(
+      beg, end, [&](int64_t i) { return op.rp(i); }, [&](int64_t e) { return op.col(e); },
+      [&](int64_t e) { return op.w(e); },
+      [&](int32_t j) {
+        F<NR> v = ldf<NR>(b, j);
+        const float wd = kOmega * dinv[j];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) v.c[c] *= wd;
+        return v;
+      },
+      [&](int64_t i, const F<NR>& sv) {
+        const F<NR> bi = ldf<NR>(b, i);
+        F<NR> xi, ti;
+        const float wd = kOmega * dinv[i];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+          xi.c[c] = wd * bi.c[c];
+          ti.c[c] = bi.c[c] - sv.c[c];
+        }
+        if (x) stf<NR>(x, i, xi);
+        stf<NR>(t, i, ti);
+      });
+}
+
+template <int NR, int LPR, int U, int K, bool NARROW>
+__global__ void __launch_bounds__(kAmgThreads) k_smooth_up_st(LvlTiles T, const int32_t* __restrict__ done,
+                                                              const int32_t* __restrict__ rp,
+                                                              const int32_t* __restrict__ cols,
+                                                              const uint16_t* __restrict__ c16,
+                                                              const int32_t* __restrict__ cbase,
+                                                              const float* __restrict__ vals,
+                                                              const float* __restrict__ dinv,
+                                                              const float* __restrict__ b, const float* __restrict__ y,
+                                                              float* __restrict__ x, int64_t limit, int* err) {
+  extern __shared__ __align__(16) unsigned char stage[];
+  const int64_t tl = blockIdx.x;
+  const int32_t ch = T.chart[tl];
+  if (done[ch]) return;
+  const int64_t beg = T.tab[2 * tl], end = T.tab[2 * tl + 1];
+  StagedOp<int, NARROW> op;
+  if (!stage_rows(stage, rp, beg, end, vals, 4, NARROW ? (const void*)c16 : (const void*)cols, NARROW ? 2 : 4, limit,
+                  err, op.S))
+    return;
+  op.cb = NARROW ? cbase[ch] : 0;
+  tile_rows_rp<NR, LPR, U, K>(
+      beg, end, [&](int64_t i) { return op.rp(i); }, [&](int64_t e) { return op.col(e); },
+      [&](int64_t e) { return op.w(e); }, [&](int32_t j) { return ldf<NR>(y, j); },
+      [&](int64_t i, const F<NR>& sv) {
+        const F<NR> bi = ldf<NR>(b, i), yi = ldf<NR>(y, i);
+        F<NR> xi;
+        const float wd = kOmega * dinv[i];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) xi.c[c] = yi.c[c] + wd * (bi.c[c] - sv.c[c]);
+        stf<NR>(x, i, xi);
+      });
+}
+
+// the largest tile's nonzeros and rows of a level operator
+__global__ void k_lvl_tile_max(LvlTiles T, const int32_t* __restrict__ rp, unsigned long long* __restrict__ mx) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T.n) return;
+  const int64_t b = T.tab[2 * t], e = T.tab[2 * t + 1];
+  atomicMax(mx, (unsigned long long)(rp[e] - rp[b]));
+  atomicMax(mx + 1, (unsigned long long)(e - b));
 }
 
 // Restrict: b_c = R t over the coarse rows (tiles of the coarse level).
@@ -1440,6 +1598,7 @@ struct AmgLevelDev {
   float* w = nullptr;
   double* kpart = nullptr;
   float* kbeta = nullptr;
+  size_t stage_smem = 0;  // > 0: the smoothers stage their tiles (bytes of shared memory)
 };
 
 struct AmgHierarchy {
@@ -1459,6 +1618,8 @@ struct AmgHierarchy {
   int64_t total_rows = 0, total_nnz = 0;
   float alpha_c = 1.0f;
   int k_levels = 0;  // top levels applied in the K-form (two coarse corrections with steplengths)
+  int* err = nullptr;  // a staged tile's bounded wait ran out
+  int64_t spin_limit = 0;
 };
 
 namespace {
@@ -1656,6 +1817,50 @@ void gal_merge_fill(Ctx& ctx, GalWork& g, int64_t nrows, const uint8_t* active, 
 }
 
 }  // namespace
+
+constexpr size_t kStageMaxSmem = 100 * 1024;
+
+template <int NR, bool NW>
+void stage_attributes_nw() {
+#define A(X, UU, KK)                                                                                            \
+  RUV_CUDA(cudaFuncSetAttribute(k_smooth_down_st<NR, X, UU, KK, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                (int)kStageMaxSmem));                                                            \
+  RUV_CUDA(cudaFuncSetAttribute(k_smooth_up_st<NR, X, UU, KK, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                (int)kStageMaxSmem));
+  A(1, 4, 2) A(2, 2, 4) A(4, 2, 4) A(8, 2, 4) A(16, 1, 4)
+#undef A
+}
+
+// Level 0's smoothers stage their tiles into shared memory when RUV_AMG_STAGE=1 and the
+// largest tile fits in kStageMaxSmem.
+void stage_setup(Ctx& ctx, AmgHierarchy* H) {
+  const char* e = std::getenv("RUV_AMG_STAGE");
+  if (!(e && e[0] == '1') || H->lv.empty()) return;
+  AmgLevelDev& L = H->lv[0];
+  if (L.cont.n == 0) return;
+  cudaStream_t s = ctx.stream;
+  unsigned long long* mx = ctx.ws.get<unsigned long long>("amg.stmax", 2);
+  RUV_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), s));
+  k_lvl_tile_max<<<div_up(L.cont.n, 256), 256, 0, s>>>(L.cont, L.rp, mx);
+  count_launches(1);
+  unsigned long long h[2] = {0, 0};
+  RUV_CUDA(cudaMemcpyAsync(h, mx, sizeof(h), cudaMemcpyDeviceToHost, s));
+  RUV_CUDA(cudaStreamSynchronize(s));
+  const size_t bytes = stage_bytes((int64_t)h[1], (int64_t)h[0], 4, L.c16 ? 2 : 4);
+  if (bytes > kStageMaxSmem) return;
+  if (H->nrhs == 2) {
+    stage_attributes_nw<2, true>();
+    stage_attributes_nw<2, false>();
+  } else {
+    stage_attributes_nw<1, true>();
+    stage_attributes_nw<1, false>();
+  }
+  H->err = ctx.ws.get<int>("amg.err", 1);
+  RUV_CUDA(cudaMemsetAsync(H->err, 0, sizeof(int), s));
+  const char* le = std::getenv("RUV_SPIN_LIMIT");
+  H->spin_limit = le ? std::max<int64_t>(1, std::atoll(le)) : (int64_t(1) << 22);
+  L.stage_smem = bytes;
+}
 
 AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string& info) {
   cudaStream_t s = ctx.stream;
@@ -2056,6 +2261,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
                             sys.nnz > 0 ? (double)H->total_nnz / (double)sys.nnz : 0.0);
   }
   cudaEventDestroy(t_setup0);
+  stage_setup(ctx, H.get());
   return H.release();
 }
 
@@ -2148,8 +2354,12 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
     float* xpre = L.smoothed ? L.x : nullptr;  // the tentative cycle re-forms it on the way up
 #define CALL(X, UU, KK)                                                                                                \
-  k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
-                                                                    L.dinv, L.b, xpre, L.t)
+  if (L.stage_smem)                                                                                                    \
+    k_smooth_down_st<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, L.stage_smem, s>>>(                                   \
+        L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, L.dinv, L.b, xpre, L.t, H->spin_limit, H->err);            \
+  else                                                                                                                 \
+    k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
+                                                                      L.dinv, L.b, xpre, L.t)
     if (L.c16) {
       constexpr bool NW = true;
       RUV_LPR_SWITCH(la, CALL)
@@ -2195,8 +2405,12 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
     RUV_LPR_SWITCH(lp, CALL)
 #undef CALL
 #define CALL(X, UU, KK)                                                                                              \
-  k_smooth_up<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
-                                                                  L.dinv, L.b, L.y, L.x)
+  if (L.stage_smem)                                                                                                  \
+    k_smooth_up_st<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, L.stage_smem, s>>>(                                   \
+        L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, L.dinv, L.b, L.y, L.x, H->spin_limit, H->err);           \
+  else                                                                                                               \
+    k_smooth_up<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
+                                                                    L.dinv, L.b, L.y, L.x)
     if (L.c16) {
       constexpr bool NW = true;
       RUV_LPR_SWITCH(la, CALL)
@@ -2299,6 +2513,7 @@ class AmgPrecond final : public SepPrecond {
   bool flexible() const override { return true; }
   void bind(Ctx& ctx, void* r, void* z, bool) override { amg_bind(ctx, H_, static_cast<float*>(r), static_cast<float*>(z)); }
   int apply(Ctx& ctx, const int32_t* done) override { return amg_apply(ctx, H_, done); }
+  const int* error_flag() const override { return H_->err; }
 
  private:
   AmgHierarchy* H_ = nullptr;

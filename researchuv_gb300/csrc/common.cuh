@@ -183,6 +183,89 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
   __syncthreads();
 }
 
+// ------------------------------------------------------------------ bulk-copy staging
+// A window of a global array staged into shared memory by cp.async.bulk: the element range
+// [e0, e1) widened to 16-byte boundaries (the copy's alignment rule; callers allocate the
+// slack the widened end may read).
+struct Win {
+  const char* src;   // 16-byte aligned start in global memory
+  int64_t first;     // element index of the first staged element
+  uint32_t bytes;    // multiple of 16
+};
+__device__ __forceinline__ Win stage_window(const void* base, int64_t e0, int64_t e1, int es) {
+  const uint64_t b0 = (uint64_t)e0 * es, b1 = (uint64_t)e1 * es;
+  const uint64_t a0 = b0 & ~(uint64_t)15, a1 = (b1 + 15) & ~(uint64_t)15;
+  return Win{static_cast<const char*>(base) + a0, (int64_t)(a0 / es), (uint32_t)(a1 - a0)};
+}
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  if (bytes == 0) return;
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, int64_t limit) {
+  const uint32_t a = smem_addr(bar);
+  for (int64_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+
+// A tile's rows [beg, end) of a CSR operator staged into `stage` (dynamic shared memory, 16
+// bytes of mbarrier first): its row pointers (int32), values (es_v bytes each) and columns
+// (es_c bytes each).  Every thread of the CTA calls it.  The wait is bounded: past `limit`
+// tries the CTA sets *err, waits once more (bounded) for its own copies and gets false.
+struct StagedRows {
+  const int32_t* rp;
+  const unsigned char* v;
+  const unsigned char* c;
+  int64_t fr, fv, fc;  // first staged element of each window
+};
+__device__ __forceinline__ bool stage_rows(unsigned char* stage, const int32_t* rp, int64_t beg, int64_t end,
+                                           const void* vals, int es_v, const void* cols, int es_c, int64_t limit,
+                                           int* err, StagedRows& out) {
+  const int64_t e0 = rp[beg], e1 = rp[end];
+  const Win wr = stage_window(rp, beg, end + 1, 4);
+  const Win wv = stage_window(vals, e0, e1, es_v);
+  const Win wc = stage_window(cols, e0, e1, es_c);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(stage);
+  unsigned char* sr = stage + 16;
+  unsigned char* sv = sr + wr.bytes;
+  unsigned char* sc = sv + wv.bytes;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(wr.bytes + wv.bytes + wc.bytes)
+                 : "memory");
+    bulk_g2s(sr, wr.src, wr.bytes, bar);
+    bulk_g2s(sv, wv.src, wv.bytes, bar);
+    bulk_g2s(sc, wc.src, wc.bytes, bar);
+  }
+  __syncthreads();
+  if (!mbar_wait(bar, 0, limit)) {
+    if (threadIdx.x == 0) atomicOr(err, 1);
+    mbar_wait(bar, 0, limit);
+    return false;
+  }
+  out = StagedRows{reinterpret_cast<const int32_t*>(sr), sv, sc, wr.first, wv.first, wc.first};
+  return true;
+}
+// bytes of stage a tile of `rows` rows and `nnz` entries needs
+inline size_t stage_bytes(int64_t rows, int64_t nnz, int es_v, int es_c) {
+  auto up16 = [](int64_t b) { return (size_t)((b + 15) & ~(int64_t)15); };
+  return 16 + up16(4 * (rows + 1) + 16) + up16((int64_t)es_v * nnz + 16) + up16((int64_t)es_c * nnz + 16);
+}
+
 // ------------------------------------------------------------------ scan
 // Exclusive scan of int32 counts into int64 offsets (out has n + 1 entries; out[n] = total).
 void exclusive_scan(const int32_t* in, int64_t* out, int64_t n, Workspace& ws, cudaStream_t s,

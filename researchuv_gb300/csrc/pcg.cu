@@ -338,38 +338,6 @@ __global__ void k_tile_max(Tiles T, const int32_t* __restrict__ row_ptr, unsigne
 // bulk copy's alignment rule); the workspace allocations carry the slack that the widened
 // end may read.  The staging wait is bounded: past its iteration limit the CTA sets T.err,
 // waits once more (bounded) for its own copies and returns.
-struct Win {
-  const char* src;   // 16-byte aligned start in global memory
-  int64_t first;     // element index of the first staged element
-  uint32_t bytes;    // multiple of 16
-};
-__device__ __forceinline__ Win stage_window(const void* base, int64_t e0, int64_t e1, int es) {
-  const uint64_t b0 = (uint64_t)e0 * es, b1 = (uint64_t)e1 * es;
-  const uint64_t a0 = b0 & ~(uint64_t)15, a1 = (b1 + 15) & ~(uint64_t)15;
-  return Win{static_cast<const char*>(base) + a0, (int64_t)(a0 / es), (uint32_t)(a1 - a0)};
-}
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  if (bytes == 0) return;
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(dst)),
-               "l"(src), "r"(bytes), "r"(smem_addr(bar))
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, int64_t limit) {
-  const uint32_t a = smem_addr(bar);
-  for (int64_t it = 0; it < limit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(a), "r"(phase)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
 // bytes of dynamic shared memory the bulk-copy SpMV needs for the largest tile
 template <class S, bool NARROW>
 inline size_t spmv_tma_smem(const Tiles& T) {

@@ -315,3 +315,20 @@ def test_bulk_copy_spmv_wait_is_bounded(monkeypatch):
     monkeypatch.delenv("RUV_SPIN_LIMIT")
     _, stats, st = R.solve_batch(ctx, C.batch(), R.UnfoldOptions(precond=R.Precond.JACOBI), nv)
     assert st == R.Status.OK
+
+
+def test_staged_smoothers_bitwise(monkeypatch):
+    """Level 0's AMG smoothers with their tiles staged into shared memory by bulk copies
+    (RUV_AMG_STAGE=1) run the same row loop: bitwise the same UVs and iterations."""
+    vo, to, p3, tr = W.disks(24, t_min=200, t_max=20000, seed=61)
+    C = R.prepare_patches(vo, to, p3, tr)
+    ctx = R.Context(0)
+    opts = R.UnfoldOptions(precond=R.Precond.AMG_SA, precision=R.Precision.MIXED)
+    monkeypatch.setenv("RUV_AMG_STAGE", "0")
+    plain = R.unfold_charts(ctx, C, opts)
+    monkeypatch.setenv("RUV_AMG_STAGE", "1")
+    staged = R.unfold_charts(ctx, C, opts)
+    for a, b in zip(plain, staged):
+        assert a.status == b.status == R.Status.OK
+        assert a.cg_iters == b.cg_iters
+        assert np.array_equal(a.uv, b.uv)
