@@ -481,18 +481,45 @@ def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float
     the loss difference term by term, so neither the solve's rounding nor the cancellation
     of two large loss totals reaches the difference quotient.
 
-    ``reuse_base``: solve A' dx = rhs by iterative refinement on the unperturbed matrix's LU
-    factors (A' - A is O(h) and confined to the rows next to v, so each sweep gains about
-    ten digits; it stops at a residual of 1e-15 |rhs|), instead of factoring every
-    perturbed matrix: what makes the check affordable on a half-million-row chart."""
+    ``reuse_base``: solve A' dx = rhs exactly with the unperturbed matrix's LU factors and a
+    low-rank (Woodbury) update instead of factoring every perturbed matrix -- what makes the
+    check affordable on a half-million-row chart.  A' - A is confined to the rows and
+    columns S of v's neighbourhood (the coefficients of the triangles around v), so with
+    M = (A' - A)[S, S] and Z = A^-1 E_S (one solve per row of S, kept per vertex),
+    A'^-1 y = A^-1 y - Z M (I + Z[S] M)^-1 (A^-1 y)[S].  (Iterative refinement on the
+    unperturbed factors diverges where |A^-1 (A' - A)| > 1, which an ill-conditioned chart
+    reaches.)"""
     p3 = np.ascontiguousarray(p3, np.float64).reshape(-1, 3)
     base = FixedPinChart(p3, tris, pinned, pin_uv)
     x = base.solve()
     uv = base.uv(x)
     _, _, _, lt = base.distortion(uv)
     free = base.row_of >= 0
+    zcache = {}  # row -> column of A^-1 (solves shared by the perturbations of one vertex)
+
+    def woodbury(dA, rhs):
+        rows = np.unique(dA.tocoo().row[dA.tocoo().data != 0.0])
+        y = base.solve(rhs)
+        if len(rows) == 0:
+            return y
+        need = [r for r in rows if r not in zcache]
+        if need:
+            E = np.zeros((base.nf, len(need)))
+            E[need, np.arange(len(need))] = 1.0
+            Zn = base.solve(E)
+            for t, r in enumerate(need):
+                zcache[r] = Zn[:, t]
+        Z = np.stack([zcache[r] for r in rows], axis=1)
+        M = dA[rows][:, rows].toarray()
+        K = np.eye(len(rows)) + Z[rows] @ M
+        return y - Z @ (M @ np.linalg.solve(K, y[rows]))
+
     out = []
+    last_v = None
     for v, k in picks:
+        if v != last_v:
+            zcache.clear()
+            last_v = v
         diffs = []
         for sgn in (1.0, -1.0):
             q = p3.copy()
@@ -502,16 +529,7 @@ def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float
                 dA = ch.A.copy()
                 dA.data = ch.A.data - base.A.data
                 rhs = (ch.b - base.b) - dA @ x
-                if reuse_base:
-                    dx = base.solve(rhs)
-                    scale = max(float(np.abs(rhs).max()), 1e-300)
-                    for _ in range(12):
-                        res = rhs - ch.A @ dx
-                        if float(np.abs(res).max()) <= 1e-15 * scale:
-                            break
-                        dx = dx + base.solve(res)
-                else:
-                    dx = ch.solve(rhs)
+                dx = woodbury(dA, rhs) if reuse_base else ch.solve(rhs)
                 for _ in range(refine):  # iterative refinement of the small correction
                     dx = dx + (base if reuse_base else ch).solve(rhs - ch.A @ dx)
             else:  # an edge weight crossed the drop threshold (a clamped cotangent at 0)

@@ -786,125 +786,6 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
   }
 }
 
-// Rows of a sparse product whose inner rows hold ascending, distinct keys (the prolongator's
-// rows, the rows of W = A P) by a k-way merge instead of a hash table.  G lanes per row; lane
-// l owns the inner rows of outer entries ob + l and ob + G + l.  The group first copies the
-// row's products (key, scale * value) into its shared-memory area, every lane its own inner
-// rows with independent loads, then merges there: each step takes the smallest head key,
-// sums that key's products in outer-entry order starting from 0.0 (the arrival order in which
-// k_gal_hash accumulates them, so the sums are the same bits) and advances the lanes that
-// contributed.  Keys come out ascending.  Rows with more than 2 G outer entries or more than
-// CAP products are listed for the large-table hash kernel.
-//   MODE 0: counts (cnt[row]); lists the long rows.  MODE 1: writes at off[row] (DIAG: also
-//   the inverse of the diagonal entry); skips the long rows.
-template <int MODE, int G, int CAP, bool DIAG, class OP, class OV, class IP, class IV>
-__global__ void __launch_bounds__(256) k_gal_merge(int64_t nrows, const uint8_t* __restrict__ active,
-                                                   const OP* __restrict__ o_ptr, const int32_t* __restrict__ o_idx,
-                                                   const OV* __restrict__ o_val, const IP* __restrict__ i_ptr,
-                                                   const int32_t* __restrict__ i_idx, const IV* __restrict__ i_val,
-                                                   int32_t* __restrict__ cnt, const int64_t* __restrict__ off,
-                                                   int32_t* __restrict__ oc, double* __restrict__ ov,
-                                                   float* __restrict__ adinv, int32_t* __restrict__ list,
-                                                   int32_t* __restrict__ list_n) {
-  constexpr int GROUPS = 256 / G;
-  __shared__ int32_t skey[GROUPS][CAP];
-  __shared__ double sval[MODE == 1 ? GROUPS : 1][MODE == 1 ? CAP : 1];
-  const int lane = threadIdx.x & 31, sl = lane & (G - 1), gb = lane & ~(G - 1);
-  const int grp = threadIdx.x / G;
-  const unsigned smask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gb);
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;  // uniform within the lane group
-  if (row >= nrows) return;
-  if (active && !active[row]) {
-    if (MODE == 0 && sl == 0) cnt[row] = 0;
-    return;
-  }
-  const int64_t ob = (int64_t)o_ptr[row], oe = (int64_t)o_ptr[row + 1];
-  int64_t ib[2] = {0, 0};
-  int len[2] = {0, 0};
-  double sc[2] = {0.0, 0.0};
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int64_t q = ob + h * G + sl;
-    if (q < oe) {
-      const int32_t j = o_idx[q];
-      sc[h] = o_val ? (double)o_val[q] : 1.0;
-      ib[h] = (int64_t)i_ptr[j];
-      len[h] = (int)((int64_t)i_ptr[j + 1] - ib[h]);
-    }
-  }
-  // segment starts: lane l's first inner row after every lower lane's first, then the second
-  // inner rows in the same way (outer-entry order)
-  int x0 = len[0], x1 = len[1];
-#pragma unroll
-  for (int o = 1; o < G; o <<= 1) {
-    const int y0 = __shfl_up_sync(smask, x0, o, G), y1 = __shfl_up_sync(smask, x1, o, G);
-    if (sl >= o) {
-      x0 += y0;
-      x1 += y1;
-    }
-  }
-  const int tot0 = __shfl_sync(smask, x0, G - 1, G), tot1 = __shfl_sync(smask, x1, G - 1, G);
-  if (oe - ob > 2 * G || tot0 + tot1 > CAP) {
-    if (MODE == 0 && sl == 0) {
-      cnt[row] = 0;
-      list[atomicAdd(list_n, 1)] = (int32_t)row;
-    }
-    return;
-  }
-  int beg[2] = {x0 - len[0], tot0 + x1 - len[1]};
-  int32_t* K = skey[grp];
-  double* Vs = sval[MODE == 1 ? grp : 0];
-#pragma unroll
-  for (int h = 0; h < 2; ++h)
-    for (int t = 0; t < len[h]; ++t) {
-      K[beg[h] + t] = i_idx[ib[h] + t];
-      if (MODE == 1) Vs[beg[h] + t] = sc[h] * (double)i_val[ib[h] + t];
-    }
-  __syncwarp(smask);
-  int pos[2] = {beg[0], beg[1]};
-  const int end[2] = {beg[0] + len[0], beg[1] + len[1]};
-  int32_t key[2];
-#pragma unroll
-  for (int h = 0; h < 2; ++h) key[h] = pos[h] < end[h] ? K[pos[h]] : INT_MAX;
-  const int64_t o = MODE == 1 ? off[row] : 0;
-  int d = 0;
-  bool has_d = false;
-  double dval = 0.0;
-  for (;;) {
-    int32_t kmin = min(key[0], key[1]);
-#pragma unroll
-    for (int xx = G / 2; xx > 0; xx >>= 1) kmin = min(kmin, __shfl_xor_sync(smask, kmin, xx, G));
-    if (kmin == INT_MAX) break;
-    const bool mine0 = key[0] == kmin, mine1 = key[1] == kmin;
-    if (MODE == 1) {
-      const double v0 = mine0 ? Vs[pos[0]] : 0.0;
-      const double v1 = mine1 ? Vs[pos[1]] : 0.0;
-      double sum = 0.0;
-      for (unsigned m = __ballot_sync(smask, mine0); m != 0u; m &= m - 1u)
-        sum += __shfl_sync(smask, v0, (__ffs(m) - 1) - gb, G);
-      for (unsigned m = __ballot_sync(smask, mine1); m != 0u; m &= m - 1u)
-        sum += __shfl_sync(smask, v1, (__ffs(m) - 1) - gb, G);
-      if (sl == 0) {
-        oc[o + d] = kmin;
-        ov[o + d] = sum;
-      }
-      if (DIAG && kmin == (int32_t)row) {
-        has_d = true;
-        dval = sum;
-      }
-    }
-    ++d;
-#pragma unroll
-    for (int h = 0; h < 2; ++h)
-      if (key[h] == kmin) {
-        ++pos[h];
-        key[h] = pos[h] < end[h] ? K[pos[h]] : INT_MAX;
-      }
-  }
-  if (MODE == 0 && sl == 0) cnt[row] = d;
-  if (MODE == 1 && DIAG && sl == 0) adinv[row] = has_d && dval > 0.0 ? (float)(1.0 / dval) : 0.0f;
-}
-
 // Staged rows to their place in the product (8 lanes per row); listed rows (sn < 0) are
 // written by the large-table kernel.
 __global__ void k_gal_copy(int64_t nrows, int hs, const int32_t* __restrict__ sn, const int32_t* __restrict__ st_key,
@@ -1740,82 +1621,6 @@ void gal_fill(Ctx& ctx, GalWork& g, int64_t nrows, const OP* o_ptr, const int32_
   }
 }
 
-// The merge formulation of gal_count / gal_fill (k_gal_merge) for products whose inner rows
-// hold ascending, distinct keys; `avg_outer` (the mean outer row length) picks 8, 16 or 32
-// lanes per row.  RUV_GAL_MERGE=0 keeps the hash formulation (the same bits).
-inline bool gal_merge_on() {
-  const char* e = std::getenv("RUV_GAL_MERGE");
-  return !(e && e[0] == '0');
-}
-
-// products a row may stage in shared memory (per lane group): 8 lanes 64, 16 lanes 128,
-// 32 lanes 512 (MODE 1 stages the values too: 24, 24 and 48 KB per 256-thread block)
-template <int G>
-constexpr int merge_cap() {
-  return G == 32 ? 512 : 8 * G;
-}
-
-template <int MODE, int G, bool DIAG, class OP, class OV, class IP, class IV>
-void launch_merge(cudaStream_t s, int64_t nrows, const uint8_t* active, const OP* o_ptr, const int32_t* o_idx,
-                  const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, int32_t* cnt,
-                  const int64_t* off, int32_t* oc, double* ov, float* adinv, int32_t* list, int32_t* list_n) {
-  k_gal_merge<MODE, G, merge_cap<G>(), DIAG><<<div_up(nrows * G, 256), 256, 0, s>>>(
-      nrows, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, cnt, off, oc, ov, adinv, list, list_n);
-  count_launches(1);
-  RUV_LAUNCH_CHECK();
-}
-
-template <bool DIAG, class OP, class OV, class IP, class IV>
-void gal_merge_count(Ctx& ctx, GalWork& g, int64_t nrows, double avg_outer, const uint8_t* active, const OP* o_ptr,
-                     const int32_t* o_idx, const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val,
-                     int32_t* cnt) {
-  cudaStream_t s = ctx.stream;
-  g.h1 = 0;
-  if (nrows <= 0) return;
-  if (g.debug) {
-    RUV_CUDA(cudaStreamSynchronize(s));
-    g.t0 = std::chrono::steady_clock::now();
-  }
-  g.lanes = avg_outer <= 6.0 ? 8 : avg_outer <= 14.0 ? 16 : 32;
-  RUV_CUDA(cudaMemsetAsync(g.list_n, 0, sizeof(int32_t), s));
-#define M(GG) launch_merge<0, GG, DIAG>(s, nrows, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, cnt, nullptr, nullptr, \
-                                        nullptr, nullptr, g.list, g.list_n)
-  if (g.lanes == 8) M(8);
-  else if (g.lanes == 16) M(16);
-  else M(32);
-#undef M
-  RUV_CUDA(cudaMemcpyAsync(&g.h1, g.list_n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-  RUV_CUDA(cudaStreamSynchronize(s));
-  if (g.h1 > 0) {
-    GalOut o0{cnt, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, g.ovf};
-    launch_gal<0, 32, kGalBigH, 1, DIAG>(s, g.h1, g.list, nullptr, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, KeyId{}, o0);
-  }
-}
-
-template <bool DIAG, class OP, class OV, class IP, class IV>
-void gal_merge_fill(Ctx& ctx, GalWork& g, int64_t nrows, const uint8_t* active, const OP* o_ptr, const int32_t* o_idx,
-                    const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, const int64_t* off,
-                    int32_t* oc, double* ov, float* adinv) {
-  cudaStream_t s = ctx.stream;
-  if (nrows <= 0) return;
-#define M(GG) launch_merge<1, GG, DIAG>(s, nrows, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, nullptr, off, oc, ov, \
-                                        adinv, nullptr, nullptr)
-  if (g.lanes == 8) M(8);
-  else if (g.lanes == 16) M(16);
-  else M(32);
-#undef M
-  if (g.h1 > 0) {
-    GalOut o1{nullptr, nullptr, nullptr, nullptr, off, oc, ov, adinv, nullptr, nullptr, g.ovf};
-    launch_gal<1, 32, kGalBigH, 1, DIAG>(s, g.h1, g.list, nullptr, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, KeyId{}, o1);
-  }
-  if (g.debug) {
-    RUV_CUDA(cudaStreamSynchronize(s));
-    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - g.t0).count();
-    std::fprintf(stderr, "  merge product rows %lld: %d lanes per row, large-table rows %d, %.3f ms\n",
-                 (long long)nrows, g.lanes, g.h1, ms);
-  }
-}
-
 }  // namespace
 
 constexpr size_t kStageMaxSmem = 100 * 1024;
@@ -2103,33 +1908,19 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
                      C.vals64, C.dinv);
       finish_coarse();
     } else {
-      // ---- smoothed prolongator: W = A P, then A_c = R W (the rows of P and of W hold
-      // ascending, distinct keys: merged row by row unless RUV_GAL_MERGE=0)
+      // ---- smoothed prolongator: W = A P, then A_c = R W
       int32_t* wcnt = ctx.ws.get<int32_t>(tag + ".wcnt", L.n);
       int64_t* woff = ctx.ws.get<int64_t>(tag + ".woff", L.n + 1);
-      const bool merge = gal_merge_on();
-      if (merge)
-        gal_merge_count<false>(ctx, gw, L.n, mean(L.nnz, L.n), active, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, wcnt);
-      else
-        gal_count<false>(ctx, gw, L.n, mean(L.nnz, L.n) * mean(PN, L.n), active, L.rp, L.cols, L.vals64, L.poff, L.pc,
-                         L.pv, KeyId{}, wcnt);
+      gal_count<false>(ctx, gw, L.n, mean(L.nnz, L.n) * mean(PN, L.n), active, L.rp, L.cols, L.vals64, L.poff, L.pc,
+                       L.pv, KeyId{}, wcnt);
       WN = offsets_from_counts(ctx, wcnt, L.n, woff, tag + ".wo");
       int32_t* wc = ctx.ws.get<int32_t>(tag + ".wc", WN);
       double* wv = ctx.ws.get<double>(tag + ".wv", WN);
-      if (merge)
-        gal_merge_fill<false>(ctx, gw, L.n, active, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, woff, wc, wv, nullptr);
-      else
-        gal_fill<false>(ctx, gw, L.n, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, KeyId{}, woff, wc, wv, nullptr);
-      if (merge)
-        gal_merge_count<true>(ctx, gw, NA, mean(PN, NA), nullptr, L.roff, L.rc, L.rv, woff, wc, wv, acnt);
-      else
-        gal_count<true>(ctx, gw, NA, mean(PN, NA) * mean(WN, L.n), nullptr, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{},
-                        acnt);
+      gal_fill<false>(ctx, gw, L.n, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, KeyId{}, woff, wc, wv, nullptr);
+      gal_count<true>(ctx, gw, NA, mean(PN, NA) * mean(WN, L.n), nullptr, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{},
+                      acnt);
       alloc_coarse(offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao"));
-      if (merge)
-        gal_merge_fill<true>(ctx, gw, NA, nullptr, L.roff, L.rc, L.rv, woff, wc, wv, aoff, C.cols, C.vals64, C.dinv);
-      else
-        gal_fill<true>(ctx, gw, NA, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{}, aoff, C.cols, C.vals64, C.dinv);
+      gal_fill<true>(ctx, gw, NA, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{}, aoff, C.cols, C.vals64, C.dinv);
       finish_coarse();
     }
     L.n_next = NA;

@@ -254,20 +254,16 @@ def test_mixed_split_formed_in_fill(monkeypatch):
             assert np.array_equal(a.uv, b.uv)
 
 
-def test_galerkin_merge_and_group_graph_bitwise(monkeypatch):
-    """Two set-up reformulations that must not change a bit: the smoothed levels' Galerkin
-    products by a row merge (default; RUV_GAL_MERGE=0 keeps the shared-memory hash tables) sum
-    every coarse entry in the same arrival order, and the group matching over a group graph
-    built once per level (default; RUV_AMG_GROUP_GRAPH=0 accumulates the strengths in every
-    round) sees the same strengths.  The same hierarchy: the same iterations and UVs."""
+def test_group_graph_bitwise(monkeypatch):
+    """The group matching over a group graph built once per level (the default;
+    RUV_AMG_GROUP_GRAPH=0 accumulates the group strengths again in every round) sees the same
+    strengths in the same order: the same hierarchy, so the same iterations and UVs."""
     vo, to, p3, tr = W.disks(24, t_min=200, t_max=20000, seed=47)
     C = R.prepare_patches(vo, to, p3, tr)
     ctx = R.Context(0)
     opts = R.UnfoldOptions(precond=R.Precond.AMG_SA, precision=R.Precision.MIXED)
-    monkeypatch.setenv("RUV_GAL_MERGE", "0")
     monkeypatch.setenv("RUV_AMG_GROUP_GRAPH", "0")
     old = R.unfold_charts(ctx, C, opts)
-    monkeypatch.delenv("RUV_GAL_MERGE", raising=False)
     monkeypatch.delenv("RUV_AMG_GROUP_GRAPH", raising=False)
     new = R.unfold_charts(ctx, C, opts)
     for a, b in zip(old, new):
