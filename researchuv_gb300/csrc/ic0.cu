@@ -500,16 +500,66 @@ __global__ void __launch_bounds__(kIcThreads) k_factor_ticket(const int32_t* __r
 }
 
 // One triangular sweep of k_sweep over the rows in ticket order (rows of charts marked done
-// are skipped; their dependents are in the same chart).
+// are skipped; their dependents are in the same chart).  The output is its own message: the
+// sweep's output starts filled with all-one bits (a NaN that arithmetic never produces), a
+// row's solved value replaces it, and a thread waiting on a dependency polls that value's
+// components (aligned 4- or 8-byte words: each is read whole, old or new) until none holds
+// the fill -- one load per component and no fences on either side.
+template <class S>
+struct Bits;
+template <>
+struct Bits<float> {
+  using U = uint32_t;
+  static __device__ __forceinline__ U load(const float* p) {
+    U v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+  }
+  static __device__ __forceinline__ void store(float* p, float x) {
+    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(__float_as_uint(x)) : "memory");
+  }
+  static __device__ __forceinline__ float value(U v) { return __uint_as_float(v); }
+};
+template <>
+struct Bits<double> {
+  using U = unsigned long long;
+  static __device__ __forceinline__ U load(const double* p) {
+    U v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+  }
+  static __device__ __forceinline__ void store(double* p, double x) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(x)) : "memory");
+  }
+  static __device__ __forceinline__ double value(U v) { return __longlong_as_double((long long)v); }
+};
+
+// A component of a solved row: spins (bounded, ending at once when another wait failed)
+// until it no longer holds the fill.
+template <class S>
+__device__ __forceinline__ bool wait_value(const S* p, int* err, int64_t limit, S& out) {
+  using B = Bits<S>;
+  for (int64_t it = 0;; ++it) {
+    const typename B::U v = B::load(p);
+    if (v != (typename B::U)(~(typename B::U)0)) {
+      out = B::value(v);
+      return true;
+    }
+    if (it >= limit || ld_relaxed(err) != 0) {
+      atomicOr(err, 1);
+      return false;
+    }
+    if (it >= 32) __nanosleep(32);
+  }
+}
+
 template <class S, int NR>
 __global__ void __launch_bounds__(kIcThreads) k_sweep_ticket(const int32_t* __restrict__ order, int64_t n,
                                                              const int32_t* __restrict__ row_chart,
                                                              const int32_t* __restrict__ done, const int64_t* __restrict__ ptr,
                                                              const int32_t* __restrict__ col, const S* __restrict__ val,
-                                                             const S* __restrict__ in, S* out, int* __restrict__ ready,
-                                                             const int* __restrict__ epoch, int* __restrict__ ticket,
+                                                             const S* __restrict__ in, S* out, int* __restrict__ ticket,
                                                              int* __restrict__ err, int64_t limit) {
-  const int ep = *epoch;
   for (;;) {
     const int64_t t0 = take_tickets(ticket);
     if (t0 >= n) return;
@@ -520,23 +570,28 @@ __global__ void __launch_bounds__(kIcThreads) k_sweep_ticket(const int32_t* __re
     const int64_t b = ptr[i], d = ptr[i + 1] - 1;
     Vec<S, NR> s = ldvec<S, NR>(in, i);
     bool ok = true;
-    for (int64_t e = b; e < d; ++e) {
+    for (int64_t e = b; e < d && ok; ++e) {
       const int32_t j = col[e];
-      if (!wait_ready(ready + j, ep, err, limit)) {
-        ok = false;
-        break;
-      }
       const S a = val[e];
 #pragma unroll
-      for (int k = 0; k < NR; ++k) s.c[k] -= a * __ldcg(out + (int64_t)NR * j + k);
+      for (int k = 0; k < NR; ++k) {
+        S o;
+        if (!wait_value<S>(out + (int64_t)NR * j + k, err, limit, o)) {
+          ok = false;
+          break;
+        }
+        s.c[k] -= a * o;
+      }
     }
     if (!ok) continue;
     const S dg = val[d];
 #pragma unroll
-    for (int k = 0; k < NR; ++k) __stcg(out + (int64_t)NR * i + k, s.c[k] / dg);
-    st_release(ready + i, ep);
+    for (int k = 0; k < NR; ++k) Bits<S>::store(out + (int64_t)NR * i + k, s.c[k] / dg);
   }
 }
+
+// a fresh ticket counter for a sweep
+__global__ void k_ticket_reset(int* __restrict__ ticket) { *ticket = 0; }
 
 // ---------------------------------------------------------------- host side
 struct Factor {
@@ -839,14 +894,15 @@ class Ic0Precond final : public SepPrecond {
       ++launches;
     }
     if (F_.tickets) {
-      k_ticket_begin<<<1, 1, 0, s>>>(F_.tick, F_.tick + 1);
+      const size_t bytes = sizeof(S) * NR * (size_t)n_;
+      RUV_CUDA(cudaMemsetAsync(y, 0xff, bytes, s));  // the fill every output starts as (see k_sweep_ticket)
+      k_ticket_reset<<<1, 1, 0, s>>>(F_.tick + 1);
       k_sweep_ticket<S, NR><<<F_.ticket_grid, kIcThreads, 0, s>>>(F_.fgrows, n_, F_.row_chart, done, F_.lptr, F_.lc, lv,
-                                                                  rin, y, F_.ready, F_.tick, F_.tick + 1, F_.tick + 2,
-                                                                  F_.spin_limit);
-      k_ticket_begin<<<1, 1, 0, s>>>(F_.tick, F_.tick + 1);
+                                                                  rin, y, F_.tick + 1, F_.tick + 2, F_.spin_limit);
+      RUV_CUDA(cudaMemsetAsync(zout, 0xff, bytes, s));
+      k_ticket_reset<<<1, 1, 0, s>>>(F_.tick + 1);
       k_sweep_ticket<S, NR><<<F_.ticket_grid, kIcThreads, 0, s>>>(F_.bgrows, n_, F_.row_chart, done, F_.tptr, F_.tc, tv,
-                                                                  y, zout, F_.ready, F_.tick, F_.tick + 1, F_.tick + 2,
-                                                                  F_.spin_limit);
+                                                                  y, zout, F_.tick + 1, F_.tick + 2, F_.spin_limit);
       launches += 4;
     } else if (F_.fgrows) {
       for (int l = 0; l + 1 < (int)F_.foff.size(); ++l) {
