@@ -288,9 +288,11 @@ int64_t ruv_kernel_launches(const ruv_ctx* ctx);
 ruv_status ruv_bench_spmv(ruv_ctx* ctx, ruv_precision precision, int32_t reps, int32_t n_buffers,
                           double* ms_per_launch, double* bytes_per_launch, double* stream_bytes_per_launch);
 
-/* Autotuner: on the last assembled batch, time the batched SpMV for each instantiated
- * launch shape (lanes per row x rows in flight per sub-warp) and tile height (rows per CTA),
- * keep the fastest for this context's later solves, and report it.  Any output may be NULL. */
+/* Autotuner: on the last assembled batch, time the batched SpMV together with the CG
+ * iteration's other kernels over the same row tiles (update, dots, direction) for each
+ * instantiated launch shape (lanes per row x rows in flight per sub-warp) and tile height
+ * (rows per CTA), keep the fastest for this context's later solves, and report it
+ * (ms_per_launch: that SpMV plus those three kernels).  Any output may be NULL. */
 ruv_status ruv_autotune(ruv_ctx* ctx, ruv_precision precision, int32_t reps, int32_t* lanes_per_row,
                         int32_t* rows_in_flight, int32_t* tile_rows, double* ms_per_launch);
 

@@ -474,7 +474,7 @@ def lu_adjoint_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target):
 
 
 def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float = 1e-6, refine: int = 0,
-                reuse_base: bool = False):
+                reuse_base: bool = False, smooth_steps=None):
     """Central differences of config4_loss with respect to p3[v, k] for (v, k) in picks,
     through the fixed-pin solve.  The perturbed solution is formed as x + dx with
     A' dx = (b' - b) - (A' - A) x (a right-hand side that is exactly zero away from v), and
@@ -488,14 +488,26 @@ def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float
     M = (A' - A)[S, S] and Z = A^-1 E_S (one solve per row of S, kept per vertex),
     A'^-1 y = A^-1 y - Z M (I + Z[S] M)^-1 (A^-1 y)[S].  (Iterative refinement on the
     unperturbed factors diverges where |A^-1 (A' - A)| > 1, which an ill-conditioned chart
-    reaches.)"""
+    reaches.)
+
+    ``smooth_steps`` (a decreasing sequence of h): the loss is only piecewise smooth -- the
+    assembly clamps every corner cotangent at 0 (lscm.rs:256-268) and drops an edge whose
+    weight is <= EPS (lscm.rs:606) -- so a difference quotient across one of those kinks
+    averages two one-sided derivatives.  For each pick the first h of the sequence at which
+    neither v + h nor v - h moves a clamp of the triangles around v (no corner cotangent of
+    them changes sign, the sparsity pattern is unchanged) is used; a pick with no such h gets
+    NaN.  Returns (values, h used per pick) in that case, the values alone otherwise."""
     p3 = np.ascontiguousarray(p3, np.float64).reshape(-1, 3)
+    tris = np.ascontiguousarray(tris, np.int64).reshape(-1, 3)
     base = FixedPinChart(p3, tris, pinned, pin_uv)
     x = base.solve()
     uv = base.uv(x)
     _, _, _, lt = base.distortion(uv)
     free = base.row_of >= 0
     zcache = {}  # row -> column of A^-1 (solves shared by the perturbations of one vertex)
+    if smooth_steps is not None:
+        order = np.argsort(tris.ravel(), kind="stable")
+        starts = np.searchsorted(tris.ravel()[order], np.arange(len(p3) + 1))
 
     def woodbury(dA, rhs):
         rows = np.unique(dA.tocoo().row[dA.tocoo().data != 0.0])
@@ -514,33 +526,71 @@ def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float
         K = np.eye(len(rows)) + Z[rows] @ M
         return y - Z @ (M @ np.linalg.solve(K, y[rows]))
 
-    out = []
+    def cot_signs(q, tv):
+        a, b, c = q[tv[:, 0]], q[tv[:, 1]], q[tv[:, 2]]
+        out = []
+        for o, u, w in ((a, b, c), (b, c, a), (c, a, b)):
+            e1, e2 = u - o, w - o
+            out.append(np.sign(np.einsum("ij,ij->i", e1, e2)))
+        return np.stack(out, axis=1)
+
+    def one_side(q):
+        ch = FixedPinChart(q, tris, pinned, pin_uv)
+        same = np.array_equal(ch.A.indptr, base.A.indptr) and np.array_equal(ch.A.indices, base.A.indices)
+        return ch, same
+
+    def diff(ch, same):
+        if same:
+            dA = ch.A.copy()
+            dA.data = ch.A.data - base.A.data
+            rhs = (ch.b - base.b) - dA @ x
+            dx = woodbury(dA, rhs) if reuse_base else ch.solve(rhs)
+            for _ in range(refine):  # iterative refinement of the small correction
+                dx = dx + (base if reuse_base else ch).solve(rhs - ch.A @ dx)
+        else:  # an edge weight crossed the drop threshold (a clamped cotangent at 0)
+            dx = ch.solve() - x
+        uv2 = uv.copy()
+        uv2[free] = uv[free] + dx[base.row_of[free]]
+        _, _, _, lt2 = ch.distortion(uv2)
+        du = uv2 - uv
+        return float((lt2 - lt).sum()) + lam_l2 * float((du * (uv2 + uv - 2.0 * target)).sum())
+
+    out, used = [], []
     last_v = None
     for v, k in picks:
         if v != last_v:
             zcache.clear()
             last_v = v
-        diffs = []
-        for sgn in (1.0, -1.0):
-            q = p3.copy()
-            q[v, k] += sgn * h
-            ch = FixedPinChart(q, tris, pinned, pin_uv)
-            if np.array_equal(ch.A.indptr, base.A.indptr) and np.array_equal(ch.A.indices, base.A.indices):
-                dA = ch.A.copy()
-                dA.data = ch.A.data - base.A.data
-                rhs = (ch.b - base.b) - dA @ x
-                dx = woodbury(dA, rhs) if reuse_base else ch.solve(rhs)
-                for _ in range(refine):  # iterative refinement of the small correction
-                    dx = dx + (base if reuse_base else ch).solve(rhs - ch.A @ dx)
-            else:  # an edge weight crossed the drop threshold (a clamped cotangent at 0)
-                dx = ch.solve() - x
-            uv2 = uv.copy()
-            uv2[free] = uv[free] + dx[base.row_of[free]]
-            _, _, _, lt2 = ch.distortion(uv2)
-            du = uv2 - uv
-            diffs.append(float((lt2 - lt).sum()) + lam_l2 * float((du * (uv2 + uv - 2.0 * target)).sum()))
-        out.append((diffs[0] - diffs[1]) / (2.0 * h))
-    return np.array(out)
+        if smooth_steps is None:
+            diffs = []
+            for sgn in (1.0, -1.0):
+                q = p3.copy()
+                q[v, k] += sgn * h
+                diffs.append(diff(*one_side(q)))
+            out.append((diffs[0] - diffs[1]) / (2.0 * h))
+            continue
+        tv = tris[order[starts[v]:starts[v + 1]] // 3]
+        s0 = cot_signs(p3, tv)
+        val, hv = float("nan"), float("nan")
+        for hh in smooth_steps:
+            sides, ok = [], True
+            for sgn in (1.0, -1.0):
+                q = p3.copy()
+                q[v, k] += sgn * hh
+                ch, same = one_side(q)
+                if not same or not np.array_equal(cot_signs(q, tv), s0):
+                    ok = False
+                    break
+                sides.append((ch, same))
+            if ok:
+                val = (diff(*sides[0]) - diff(*sides[1])) / (2.0 * hh)
+                hv = hh
+                break
+        out.append(val)
+        used.append(hv)
+    if smooth_steps is None:
+        return np.array(out)
+    return np.array(out), np.array(used)
 
 
 def rectangularize(uv, border):

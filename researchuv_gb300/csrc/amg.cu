@@ -960,9 +960,11 @@ __device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_
   const int rpp = kAmgThreads / LPR;
   for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
     int64_t lo[U], hi[U];
+    int32_t rb[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      rb[u] = cols.row_base(i);
       const bool valid = i < end;
       lo[u] = valid ? (ptr64 ? ptr64[i] : (int64_t)ptr32[i]) : 0;
       hi[u] = valid ? (ptr64 ? ptr64[i + 1] : (int64_t)ptr32[i + 1]) : 0;
@@ -976,7 +978,7 @@ __device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_
         const int64_t e = lo[u] + sub + k * LPR;
         const bool in = e < hi[u];
         av[u][k] = in ? w(e) : 0.0f;
-        cv[u][k] = in ? cols(e) : -1;
+        cv[u][k] = in ? cols(e, rb[u]) : -1;
       }
     F<NR> s[U];
 #pragma unroll
@@ -992,7 +994,7 @@ __device__ __forceinline__ void tile_rows(int64_t beg, int64_t end, const int64_
         }
       for (int64_t e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {
         const float a = w(e);
-        const F<NR> v = g(cols(e));
+        const F<NR> v = g(cols(e, rb[u]));
 #pragma unroll
         for (int c = 0; c < NR; ++c) s[u].c[c] += a * v.c[c];
       }
@@ -1016,9 +1018,11 @@ __device__ __forceinline__ void tile_rows_rp(int64_t beg, int64_t end, RP rpf, C
   const int rpp = kAmgThreads / LPR;
   for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
     int64_t lo[U], hi[U];
+    int32_t rb[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      rb[u] = cols.row_base(i);
       const bool valid = i < end;
       lo[u] = valid ? rpf(i) : 0;
       hi[u] = valid ? rpf(i + 1) : 0;
@@ -1032,7 +1036,7 @@ __device__ __forceinline__ void tile_rows_rp(int64_t beg, int64_t end, RP rpf, C
         const int64_t e = lo[u] + sub + k * LPR;
         const bool in = e < hi[u];
         av[u][k] = in ? w(e) : 0.0f;
-        cv[u][k] = in ? cols(e) : -1;
+        cv[u][k] = in ? cols(e, rb[u]) : -1;
       }
     F<NR> s[U];
 #pragma unroll
@@ -1048,7 +1052,7 @@ __device__ __forceinline__ void tile_rows_rp(int64_t beg, int64_t end, RP rpf, C
         }
       for (int64_t e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {
         const float a = w(e);
-        const F<NR> v = g(cols(e));
+        const F<NR> v = g(cols(e, rb[u]));
 #pragma unroll
         for (int c = 0; c < NR; ++c) s[u].c[c] += a * v.c[c];
       }
@@ -1066,7 +1070,7 @@ __device__ __forceinline__ void tile_rows_rp(int64_t beg, int64_t end, RP rpf, C
 }
 
 // Down 1: x = w D^-1 b;  t = b - A x  (x of neighbours formed on the fly).
-template <int NR, int LPR, int U, int K, bool NARROW>
+template <int NR, int LPR, int U, int K, int NW>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const int32_t* __restrict__ done,
                                                              const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                                                              const uint16_t* __restrict__ c16,
@@ -1100,7 +1104,8 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const i
         stf<NR>(t, i, ti);
       });
   };
-  if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
+  if constexpr (NW == 1) run(ColsNarrow{c16, cbase[ch]});
+  else if constexpr (NW == 2) run(ColsRowRel{c16});
   else run(ColsWide{cols});
 }
 
@@ -1108,19 +1113,20 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_down(LvlTiles T, const i
 // values and column stream into shared memory by bulk asynchronous copies (stage_rows, a
 // bounded wait that sets *err) and then runs the same row loop from there; the same
 // arithmetic in the same order, so the same results.
-template <class ColsT, bool NARROW>
+template <class ColsT, int NW>
 struct StagedOp {
   StagedRows S;
   int32_t cb;
   __device__ __forceinline__ int64_t rp(int64_t i) const { return (int64_t)S.rp[i - S.fr]; }
   __device__ __forceinline__ float w(int64_t e) const { return reinterpret_cast<const float*>(S.v)[e - S.fv]; }
-  __device__ __forceinline__ int32_t col(int64_t e) const {
-    if constexpr (NARROW) return cb + (int32_t)(reinterpret_cast<const uint16_t*>(S.c)[e - S.fc]);
+  __device__ __forceinline__ int32_t row_base(int64_t i) const { return narrow_row_base<NW>(cb, i); }
+  __device__ __forceinline__ int32_t operator()(int64_t e, int32_t rb) const {
+    if constexpr (NW != 0) return rb + (int32_t)(reinterpret_cast<const uint16_t*>(S.c)[e - S.fc]);
     else return reinterpret_cast<const int32_t*>(S.c)[e - S.fc];
   }
 };
 
-template <int NR, int LPR, int U, int K, bool NARROW>
+template <int NR, int LPR, int U, int K, int NW>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_down_st(LvlTiles T, const int32_t* __restrict__ done,
                                                                 const int32_t* __restrict__ rp,
                                                                 const int32_t* __restrict__ cols,
@@ -1135,13 +1141,13 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_down_st(LvlTiles T, cons
   const int32_t ch = T.chart[tl];
   if (done[ch]) return;
   const int64_t beg = T.tab[2 * tl], end = T.tab[2 * tl + 1];
-  StagedOp<int, NARROW> op;
-  if (!stage_rows(stage, rp, beg, end, vals, 4, NARROW ? (const void*)c16 : (const void*)cols, NARROW ? 2 : 4, limit,
+  StagedOp<int, NW> op;
+  if (!stage_rows(stage, rp, beg, end, vals, 4, NW ? (const void*)c16 : (const void*)cols, NW ? 2 : 4, limit,
                   err, op.S))
     return;
-  op.cb = NARROW ? cbase[ch] : 0;
+  op.cb = NW == 1 ? cbase[ch] : 0;
   tile_rows_rp<NR, LPR, U, K>(
-      beg, end, [&](int64_t i) { return op.rp(i); }, [&](int64_t e) { return op.col(e); },
+      beg, end, [&](int64_t i) { return op.rp(i); }, op,
       [&](int64_t e) { return op.w(e); },
       [&](int32_t j) {
         F<NR> v = ldf<NR>(b, j);
@@ -1164,7 +1170,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_down_st(LvlTiles T, cons
       });
 }
 
-template <int NR, int LPR, int U, int K, bool NARROW>
+template <int NR, int LPR, int U, int K, int NW>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_up_st(LvlTiles T, const int32_t* __restrict__ done,
                                                               const int32_t* __restrict__ rp,
                                                               const int32_t* __restrict__ cols,
@@ -1179,13 +1185,13 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up_st(LvlTiles T, const 
   const int32_t ch = T.chart[tl];
   if (done[ch]) return;
   const int64_t beg = T.tab[2 * tl], end = T.tab[2 * tl + 1];
-  StagedOp<int, NARROW> op;
-  if (!stage_rows(stage, rp, beg, end, vals, 4, NARROW ? (const void*)c16 : (const void*)cols, NARROW ? 2 : 4, limit,
+  StagedOp<int, NW> op;
+  if (!stage_rows(stage, rp, beg, end, vals, 4, NW ? (const void*)c16 : (const void*)cols, NW ? 2 : 4, limit,
                   err, op.S))
     return;
-  op.cb = NARROW ? cbase[ch] : 0;
+  op.cb = NW == 1 ? cbase[ch] : 0;
   tile_rows_rp<NR, LPR, U, K>(
-      beg, end, [&](int64_t i) { return op.rp(i); }, [&](int64_t e) { return op.col(e); },
+      beg, end, [&](int64_t i) { return op.rp(i); }, op,
       [&](int64_t e) { return op.w(e); }, [&](int32_t j) { return ldf<NR>(y, j); },
       [&](int64_t i, const F<NR>& sv) {
         const F<NR> bi = ldf<NR>(b, i), yi = ldf<NR>(y, i);
@@ -1252,7 +1258,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_prolong_add(LvlTiles T, const i
 // Vassilevski).  The reference divides t.t by t.A y instead; with the FP32 cycle that
 // quotient is not energy-decreasing, and the outer flexible CG stalled with it (16384
 // iterations without converging on charts the V-cycle solves in a few dozen).
-template <int NR, int LPR, int U, int K, bool NARROW>
+template <int NR, int LPR, int U, int K, int NW>
 __global__ void __launch_bounds__(kAmgThreads) k_kspmv(LvlTiles T, const int32_t* __restrict__ done,
                                                        const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                                                        const uint16_t* __restrict__ c16, const int32_t* __restrict__ cbase,
@@ -1281,7 +1287,8 @@ __global__ void __launch_bounds__(kAmgThreads) k_kspmv(LvlTiles T, const int32_t
           acc[1] += (double)yw;
         });
   };
-  if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
+  if constexpr (NW == 1) run(ColsNarrow{c16, cbase[ch]});
+  else if constexpr (NW == 2) run(ColsRowRel{c16});
   else run(ColsWide{cols});
   block_sum<2>(acc, sh);
   if (threadIdx.x == 0) {
@@ -1334,7 +1341,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_kupdate(LvlTiles T, const int32
 }
 
 // Up 2: x = y + w D^-1 (b - A y).
-template <int NR, int LPR, int U, int K, bool NARROW>
+template <int NR, int LPR, int U, int K, int NW>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int32_t* __restrict__ done,
                                                            const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                                                            const uint16_t* __restrict__ c16,
@@ -1358,7 +1365,8 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int
         stf<NR>(x, i, xi);
       });
   };
-  if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
+  if constexpr (NW == 1) run(ColsNarrow{c16, cbase[ch]});
+  else if constexpr (NW == 2) run(ColsRowRel{c16});
   else run(ColsWide{cols});
 }
 
@@ -1366,7 +1374,7 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int
 // post-smoothing in one pass, x = y + w D^-1 (b - A y) with y_j = w D^-1_j b_j +
 // alpha_c x_c[agg[j]] formed on the fly for every neighbour (the pre-smoothed x is not
 // stored and y is never written).
-template <int NR, int LPR, int U, int K, bool NARROW>
+template <int NR, int LPR, int U, int K, int NW>
 __global__ void __launch_bounds__(kAmgThreads) k_smooth_up_t(LvlTiles T, const int32_t* __restrict__ done,
                                                              const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                                                              const uint16_t* __restrict__ c16,
@@ -1399,7 +1407,8 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up_t(LvlTiles T, const i
         stf<NR>(x, i, xi);
       });
   };
-  if constexpr (NARROW) run(ColsNarrow{c16, cbase[ch]});
+  if constexpr (NW == 1) run(ColsNarrow{c16, cbase[ch]});
+  else if constexpr (NW == 2) run(ColsRowRel{c16});
   else run(ColsWide{cols});
 }
 
@@ -1469,7 +1478,8 @@ struct AmgLevelDev {
   float *b = nullptr, *x = nullptr, *y = nullptr, *t = nullptr;
   int32_t* agg = nullptr;  // aggregate of each row (the tentative prolongator), -1 if none
   bool smoothed = false;   // transfer to the next level by a smoothed prolongator (else tentative)
-  const uint16_t* c16 = nullptr;  // 16-bit column stream (every chart of the level <= 65536 rows), see ColsNarrow
+  const uint16_t* c16 = nullptr;  // 16-bit column stream (see ColsNarrow, ColsRowRel)
+  bool rowrel = false;            // c16 holds row-relative offsets
   const int32_t* cbase = nullptr;
   LvlTiles cont{nullptr, nullptr, 0};  // tiles over rows whose chart continues below this level
   LvlTiles all{nullptr, nullptr, 0};   // tiles over every row of this level
@@ -1625,7 +1635,7 @@ void gal_fill(Ctx& ctx, GalWork& g, int64_t nrows, const OP* o_ptr, const int32_
 
 constexpr size_t kStageMaxSmem = 100 * 1024;
 
-template <int NR, bool NW>
+template <int NR, int NW>
 void stage_attributes_nw() {
 #define A(X, UU, KK)                                                                                            \
   RUV_CUDA(cudaFuncSetAttribute(k_smooth_down_st<NR, X, UU, KK, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
@@ -1654,11 +1664,13 @@ void stage_setup(Ctx& ctx, AmgHierarchy* H) {
   const size_t bytes = stage_bytes((int64_t)h[1], (int64_t)h[0], 4, L.c16 ? 2 : 4);
   if (bytes > kStageMaxSmem) return;
   if (H->nrhs == 2) {
-    stage_attributes_nw<2, true>();
-    stage_attributes_nw<2, false>();
+    stage_attributes_nw<2, 0>();
+    stage_attributes_nw<2, 1>();
+    stage_attributes_nw<2, 2>();
   } else {
-    stage_attributes_nw<1, true>();
-    stage_attributes_nw<1, false>();
+    stage_attributes_nw<1, 0>();
+    stage_attributes_nw<1, 1>();
+    stage_attributes_nw<1, 2>();
   }
   H->err = ctx.ws.get<int>("amg.err", 1);
   RUV_CUDA(cudaMemsetAsync(H->err, 0, sizeof(int), s));
@@ -1712,6 +1724,7 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     L0.vals64 = sys.vals;
     L0.c16 = sys.cols16;
     L0.cbase = sys.cbase;
+    L0.rowrel = sys.rowrel16;
     L0.dinv = ctx.ws.get<float>("amg.l0.dinv", L0.n);
     if (L0.n > 0) {
       k_f64_f32_inv<<<div_up(L0.n, B), B, 0, s>>>(L0.n, sys.diag, L0.dinv);
@@ -1937,12 +1950,14 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     C.h_chart_row.resize(NC + 1);
     RUV_CUDA(cudaMemcpyAsync(C.h_chart_row.data(), C.chart_row, sizeof(int64_t) * (NC + 1), cudaMemcpyDeviceToHost, s));
     RUV_CUDA(cudaStreamSynchronize(s));
-    if (narrow) {  // 16-bit columns for the smoothers when every chart of this level allows them
+    if (narrow) {  // 16-bit columns for the smoothers when the level allows them
       uint16_t* c16 = nullptr;
       int32_t* cbase = nullptr;
-      narrow_operator(ctx, NA, C.nnz, NC, C.h_chart_row, C.chart_row, C.rp, C.cols, ntag, &c16, &cbase);
+      bool rowrel = false;
+      narrow_operator(ctx, NA, C.nnz, NC, C.h_chart_row, C.chart_row, C.rp, C.cols, ntag, &c16, &cbase, &rowrel);
       C.c16 = c16;
       C.cbase = cbase;
+      C.rowrel = rowrel;
     }
     H->lv.push_back(C);
   }
@@ -2151,11 +2166,14 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
   else                                                                                                                 \
     k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                       L.dinv, L.b, xpre, L.t)
-    if (L.c16) {
-      constexpr bool NW = true;
+    if (L.c16 && L.rowrel) {
+      constexpr int NW = 2;
+      RUV_LPR_SWITCH(la, CALL)
+    } else if (L.c16) {
+      constexpr int NW = 1;
       RUV_LPR_SWITCH(la, CALL)
     } else {
-      constexpr bool NW = false;
+      constexpr int NW = 0;
       RUV_LPR_SWITCH(la, CALL)
     }
 #undef CALL
@@ -2179,11 +2197,14 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
 #define CALL(X, UU, KK)                                                                                                \
   k_smooth_up_t<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                     L.dinv, L.b, L.agg, C.x, H->alpha_c, L.x)
-      if (L.c16) {
-        constexpr bool NW = true;
+      if (L.c16 && L.rowrel) {
+        constexpr int NW = 2;
+        RUV_LPR_SWITCH(la, CALL)
+      } else if (L.c16) {
+        constexpr int NW = 1;
         RUV_LPR_SWITCH(la, CALL)
       } else {
-        constexpr bool NW = false;
+        constexpr int NW = 0;
         RUV_LPR_SWITCH(la, CALL)
       }
 #undef CALL
@@ -2202,11 +2223,14 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
   else                                                                                                               \
     k_smooth_up<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                     L.dinv, L.b, L.y, L.x)
-    if (L.c16) {
-      constexpr bool NW = true;
+    if (L.c16 && L.rowrel) {
+      constexpr int NW = 2;
+      RUV_LPR_SWITCH(la, CALL)
+    } else if (L.c16) {
+      constexpr int NW = 1;
       RUV_LPR_SWITCH(la, CALL)
     } else {
-      constexpr bool NW = false;
+      constexpr int NW = 0;
       RUV_LPR_SWITCH(la, CALL)
     }
 #undef CALL
@@ -2234,11 +2258,14 @@ int kform(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k) {
 #define CALL(X, UU, KK)                                                                                                \
   k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                     L.dinv, L.b, L.x, L.t)
-  if (L.c16) {
-    constexpr bool NW = true;
+  if (L.c16 && L.rowrel) {
+    constexpr int NW = 2;
+    RUV_LPR_SWITCH(la, CALL)
+  } else if (L.c16) {
+    constexpr int NW = 1;
     RUV_LPR_SWITCH(la, CALL)
   } else {
-    constexpr bool NW = false;
+    constexpr int NW = 0;
     RUV_LPR_SWITCH(la, CALL)
   }
 #undef CALL
@@ -2258,11 +2285,14 @@ int kform(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k) {
 #define CALL(X, UU, KK)                                                                                           \
   k_kspmv<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, L.y, \
                                                               L.t, L.w, L.kpart)
-    if (L.c16) {
-      constexpr bool NW = true;
+    if (L.c16 && L.rowrel) {
+      constexpr int NW = 2;
+      RUV_LPR_SWITCH(la, CALL)
+    } else if (L.c16) {
+      constexpr int NW = 1;
       RUV_LPR_SWITCH(la, CALL)
     } else {
-      constexpr bool NW = false;
+      constexpr int NW = 0;
       RUV_LPR_SWITCH(la, CALL)
     }
 #undef CALL

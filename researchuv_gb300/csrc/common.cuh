@@ -133,19 +133,35 @@ __device__ __forceinline__ float warp_sum(float v) {
 // NV * 32 values.  Fixed combine order => bitwise reproducible for a fixed launch shape.
 // (GB300 runs FP64 at a small fraction of the FP32 rate: the per-element loops of the
 // FP32 solver reduce in float and widen once per tile.)
-// Column-index streams of a CSR operator: 32-bit global row ids, or -- for a chart of at most
-// 65536 rows -- 16-bit offsets from the chart's first row, 2 bytes less per non-zero in every
-// pass that streams the operator.  A tile never spans two charts, so a kernel picks the
-// stream once per tile.
+// Column-index streams of a CSR operator: 32-bit global row ids, or 16-bit offsets (2 bytes
+// less per non-zero in every pass that streams the operator) -- from the chart's first row when
+// every chart of the operator has at most 65536 rows (ColsNarrow), or, when a chart is larger,
+// from each row's own index minus 32768 where every entry lies within 32767 rows of its row
+// (ColsRowRel: the natural orders of grids and of locally numbered meshes).  A tile never spans
+// two charts.  Kernels take the stream kind as a template parameter NW (0 wide, 1 chart-
+// relative, 2 row-relative), form a row's base once (row_base) and add one offset per entry.
 struct ColsWide {
   const int32_t* c;
-  __device__ __forceinline__ int32_t operator()(int64_t e) const { return c[e]; }
+  __device__ __forceinline__ int32_t row_base(int64_t) const { return 0; }
+  __device__ __forceinline__ int32_t operator()(int64_t e, int32_t) const { return c[e]; }
 };
 struct ColsNarrow {
   const uint16_t* c;
   int32_t base;
-  __device__ __forceinline__ int32_t operator()(int64_t e) const { return base + (int32_t)c[e]; }
+  __device__ __forceinline__ int32_t row_base(int64_t) const { return base; }
+  __device__ __forceinline__ int32_t operator()(int64_t e, int32_t rb) const { return rb + (int32_t)c[e]; }
 };
+constexpr int32_t kRowRelBias = 32768;
+struct ColsRowRel {
+  const uint16_t* c;
+  __device__ __forceinline__ int32_t row_base(int64_t i) const { return (int32_t)i - kRowRelBias; }
+  __device__ __forceinline__ int32_t operator()(int64_t e, int32_t rb) const { return rb + (int32_t)c[e]; }
+};
+// the base of a row in a 16-bit stream of kind NW (1: the chart's first row cb, 2: the row's own)
+template <int NW>
+__device__ __forceinline__ int32_t narrow_row_base(int32_t cb, int64_t i) {
+  return NW == 2 ? (int32_t)i - kRowRelBias : NW == 1 ? cb : 0;
+}
 
 template <int NV, class A>
 __device__ __forceinline__ void block_sum_t(A (&v)[NV], A* sh) {
@@ -252,7 +268,8 @@ __device__ __forceinline__ bool stage_rows(unsigned char* stage, const int32_t* 
     bulk_g2s(sc, wc.src, wc.bytes, bar);
   }
   __syncthreads();
-  if (!mbar_wait(bar, 0, limit)) {
+  // one decision for the whole CTA: a wait that ran out in any thread sends every thread out
+  if (__syncthreads_or(!mbar_wait(bar, 0, limit))) {
     if (threadIdx.x == 0) atomicOr(err, 1);
     mbar_wait(bar, 0, limit);
     return false;

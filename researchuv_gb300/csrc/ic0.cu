@@ -553,8 +553,12 @@ __device__ __forceinline__ bool wait_value(const S* p, int* err, int64_t limit, 
   }
 }
 
+constexpr int kDeps = 4;  // dependencies a sweep row loads at once
+// (a register cap instead of launch bounds: under __launch_bounds__(256) the FP32 two-column
+// instance was held at 32 registers and spilled)
+
 template <class S, int NR>
-__global__ void __launch_bounds__(kIcThreads) k_sweep_ticket(const int32_t* __restrict__ order, int64_t n,
+__global__ void __maxnreg__(48) k_sweep_ticket(const int32_t* __restrict__ order, int64_t n,
                                                              const int32_t* __restrict__ row_chart,
                                                              const int32_t* __restrict__ done, const int64_t* __restrict__ ptr,
                                                              const int32_t* __restrict__ col, const S* __restrict__ val,
@@ -570,17 +574,34 @@ __global__ void __launch_bounds__(kIcThreads) k_sweep_ticket(const int32_t* __re
     const int64_t b = ptr[i], d = ptr[i + 1] - 1;
     Vec<S, NR> s = ldvec<S, NR>(in, i);
     bool ok = true;
-    for (int64_t e = b; e < d && ok; ++e) {
-      const int32_t j = col[e];
-      const S a = val[e];
+    // The dependencies' components are loaded kDeps entries at a time, all loads in flight
+    // together (one round trip to L2 instead of one per component); only those still holding
+    // the fill are then waited on, and the row sums in entry order as before.
+    for (int64_t e0 = b; e0 < d && ok; e0 += kDeps) {
+      const int m = (int)(d - e0 < kDeps ? d - e0 : kDeps);
+      typename Bits<S>::U raw[kDeps][NR];
+      int32_t jj[kDeps];
 #pragma unroll
-      for (int k = 0; k < NR; ++k) {
-        S o;
-        if (!wait_value<S>(out + (int64_t)NR * j + k, err, limit, o)) {
-          ok = false;
-          break;
+      for (int q = 0; q < kDeps; ++q) {
+        jj[q] = q < m ? col[e0 + q] : 0;
+#pragma unroll
+        for (int k = 0; k < NR; ++k) raw[q][k] = q < m ? Bits<S>::load(out + (int64_t)NR * jj[q] + k) : 0;
+      }
+#pragma unroll
+      for (int q = 0; q < kDeps; ++q) {
+        if (q < m && ok) {
+          const S a = val[e0 + q];
+#pragma unroll
+          for (int k = 0; k < NR; ++k) {
+            S o = Bits<S>::value(raw[q][k]);
+            if (raw[q][k] == (typename Bits<S>::U)(~(typename Bits<S>::U)0) &&
+                !wait_value<S>(out + (int64_t)NR * jj[q] + k, err, limit, o)) {
+              ok = false;
+              break;
+            }
+            s.c[k] -= a * o;
+          }
         }
-        s.c[k] -= a * o;
       }
     }
     if (!ok) continue;

@@ -234,9 +234,11 @@ __device__ __forceinline__ void spmv_pq_tile(int64_t beg, int64_t end, const int
   const int rpp = kTileThreads / LPR;
   for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
     int lo[U], hi[U];
+    int32_t rb[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      rb[u] = col.row_base(i);
       const bool valid = i < end;
       lo[u] = valid ? row_ptr[i] : 0;
       hi[u] = valid ? row_ptr[i + 1] : 0;
@@ -250,7 +252,7 @@ __device__ __forceinline__ void spmv_pq_tile(int64_t beg, int64_t end, const int
         const int e = lo[u] + sub + k * LPR;
         const bool in = e < hi[u];
         av[u][k] = in ? vals[e] : S(0);
-        cv[u][k] = in ? col(e) : -1;
+        cv[u][k] = in ? col(e, rb[u]) : -1;
       }
     V<S, NR> s[U];
 #pragma unroll
@@ -266,7 +268,7 @@ __device__ __forceinline__ void spmv_pq_tile(int64_t beg, int64_t end, const int
         }
       for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {  // rows longer than K * LPR
         const S a = vals[e];
-        const V<S, NR> pv = ldv<S, NR>(p, col(e));
+        const V<S, NR> pv = ldv<S, NR>(p, col(e, rb[u]));
 #pragma unroll
         for (int c = 0; c < NR; ++c) s[u].c[c] += a * pv.c[c];
       }
@@ -296,9 +298,9 @@ __device__ __forceinline__ void spmv_pq_tile(int64_t beg, int64_t end, const int
 // each lane covering K = ceil(8 / LPR) entries in one unrolled sweep (rows of a mesh
 // Laplacian hold <= 8 entries almost always; longer rows finish in a remainder loop), U rows
 // per sub-warp in flight so a warp keeps U * K independent value/column loads and U * K
-// gathers outstanding.  Block-uniform trip counts keep every lane in the shuffles.  The
-// column stream is 16-bit where the tile's chart has one (cbase >= 0).
-template <class S, int NR, int LPR, int U, bool NARROW>
+// gathers outstanding.  Block-uniform trip counts keep every lane in the shuffles.  NW: the
+// column stream's kind (ColsWide, ColsNarrow, ColsRowRel).
+template <class S, int NR, int LPR, int U, int NW>
 __global__ void __launch_bounds__(kTileThreads) k_spmv_pq_k(Tiles T, const ChartState* __restrict__ st,
                                                             const int32_t* __restrict__ row_ptr,
                                                             const int32_t* __restrict__ cols,
@@ -312,7 +314,8 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_pq_k(Tiles T, const Chart
   if (st[ch].state != kActive) return;
   S acc[1] = {S(0)};
   const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
-  if constexpr (NARROW) spmv_pq_tile<S, NR, LPR, U>(beg, end, row_ptr, ColsNarrow{c16, cbase[ch]}, vals, p, q, acc);
+  if constexpr (NW == 1) spmv_pq_tile<S, NR, LPR, U>(beg, end, row_ptr, ColsNarrow{c16, cbase[ch]}, vals, p, q, acc);
+  else if constexpr (NW == 2) spmv_pq_tile<S, NR, LPR, U>(beg, end, row_ptr, ColsRowRel{c16}, vals, p, q, acc);
   else spmv_pq_tile<S, NR, LPR, U>(beg, end, row_ptr, ColsWide{cols}, vals, p, q, acc);
   block_sum_t<1, S>(acc, sh);
   if (threadIdx.x == 0) part[t] = (double)acc[0];
@@ -338,73 +341,72 @@ __global__ void k_tile_max(Tiles T, const int32_t* __restrict__ row_ptr, unsigne
 // bulk copy's alignment rule); the workspace allocations carry the slack that the widened
 // end may read.  The staging wait is bounded: past its iteration limit the CTA sets T.err,
 // waits once more (bounded) for its own copies and returns.
-// bytes of dynamic shared memory the bulk-copy SpMV needs for the largest tile
-template <class S, bool NARROW>
-inline size_t spmv_tma_smem(const Tiles& T) {
+// bytes of one tile's stage (row pointers, values, columns) for the largest tile
+template <class S, int NW>
+inline size_t spmv_stage_bytes(const Tiles& T) {
   auto up16 = [](int64_t b) { return (size_t)((b + 15) & ~(int64_t)15); };
-  return 16 + up16(4 * (T.max_rows + 1) + 16) + up16((int64_t)sizeof(S) * T.max_nnz + 16) +
-         up16((NARROW ? 2 : 4) * T.max_nnz + 16);
+  return up16(4 * (T.max_rows + 1) + 16) + up16((int64_t)sizeof(S) * T.max_nnz + 16) +
+         up16((NW ? 2 : 4) * T.max_nnz + 16);
+}
+template <class S, int NW>
+inline size_t spmv_tma_smem(const Tiles& T) {
+  return 16 + spmv_stage_bytes<S, NW>(T);
 }
 constexpr size_t kSpmvTmaMaxSmem = 100 * 1024;  // two CTAs per SM at least
 
-template <class S, int NR, int LPR, int U, bool NARROW>
-__global__ void __launch_bounds__(kTileThreads) k_spmv_tma(Tiles T, const ChartState* __restrict__ st,
-                                                           const int32_t* __restrict__ row_ptr,
-                                                           const int32_t* __restrict__ cols,
-                                                           const uint16_t* __restrict__ c16,
-                                                           const int32_t* __restrict__ cbase, const S* __restrict__ vals,
-                                                           const S* __restrict__ p, S* __restrict__ q,
-                                                           double* __restrict__ part) {
-  extern __shared__ __align__(16) unsigned char stage[];
-  __shared__ S sh[32];
-  const int64_t t = blockIdx.x;
-  const int32_t ch = T.chart[t];
-  if (st[ch].state != kActive) return;
-  const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
+// One tile's windows and where they sit in a stage buffer.
+struct SpmvWin {
+  Win r, v, c;
+};
+template <class S, int NW>
+__device__ __forceinline__ SpmvWin spmv_windows(const int32_t* row_ptr, const S* vals, const int32_t* cols,
+                                                const uint16_t* c16, int64_t beg, int64_t end) {
   const int64_t e0 = row_ptr[beg], e1 = row_ptr[end];
-  const Win wr = stage_window(row_ptr, beg, end + 1, 4);
-  const Win wv = stage_window(vals, e0, e1, (int)sizeof(S));
-  const Win wc = NARROW ? stage_window(c16, e0, e1, 2) : stage_window(cols, e0, e1, 4);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(stage);
-  unsigned char* sr = stage + 16;
-  unsigned char* sv = sr + wr.bytes;
-  unsigned char* sc = sv + wv.bytes;
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-                 "r"(wr.bytes + wv.bytes + wc.bytes)
-                 : "memory");
-    bulk_g2s(sr, wr.src, wr.bytes, bar);
-    bulk_g2s(sv, wv.src, wv.bytes, bar);
-    bulk_g2s(sc, wc.src, wc.bytes, bar);
-  }
-  __syncthreads();  // the barrier is initialised before anyone waits on it
-  if (!mbar_wait(bar, 0, T.spin_limit)) {
-    if (threadIdx.x == 0) atomicOr(T.err, 1);
-    mbar_wait(bar, 0, T.spin_limit);  // (bounded) let this CTA's own copies land before it exits
-    return;
-  }
-  const int32_t* rs = reinterpret_cast<const int32_t*>(sr);
-  const S* vs = reinterpret_cast<const S*>(sv);
-  const int32_t cb = NARROW ? cbase[ch] : 0;
-  auto col = [&](int64_t e) -> int32_t {
-    if constexpr (NARROW) return cb + (int32_t)(reinterpret_cast<const uint16_t*>(sc)[e - wc.first]);
-    else return reinterpret_cast<const int32_t*>(sc)[e - wc.first];
-  };
-  // the row loop of spmv_pq_tile, reading row pointers, values and columns from the stage
+  return SpmvWin{stage_window(row_ptr, beg, end + 1, 4), stage_window(vals, e0, e1, (int)sizeof(S)),
+                 NW ? stage_window(c16, e0, e1, 2) : stage_window(cols, e0, e1, 4)};
+}
+// thread 0: arm `bar` for the tile's bytes and start its three copies into `buf`
+__device__ __forceinline__ void spmv_issue(const SpmvWin& w, unsigned char* buf, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(w.r.bytes + w.v.bytes + w.c.bytes)
+               : "memory");
+  bulk_g2s(buf, w.r.src, w.r.bytes, bar);
+  bulk_g2s(buf + w.r.bytes, w.v.src, w.v.bytes, bar);
+  bulk_g2s(buf + w.r.bytes + w.v.bytes, w.c.src, w.c.bytes, bar);
+}
+
+// The row loop of spmv_pq_tile over a staged tile: row pointers, values and columns read from
+// the stage buffer (the same arithmetic in the same order, so the same bits).
+template <class S, int NR, int LPR, int U, int NW>
+__device__ __forceinline__ void spmv_staged_tile(int64_t beg, int64_t end, const SpmvWin& w,
+                                                 const unsigned char* buf, int32_t cb, const S* __restrict__ p,
+                                                 S* __restrict__ q, S& acc) {
+  const int32_t* rs = reinterpret_cast<const int32_t*>(buf);
+  const S* vs = reinterpret_cast<const S*>(buf + w.r.bytes);
+  const unsigned char* sc = buf + w.r.bytes + w.v.bytes;
+  struct {
+    const unsigned char* sc;
+    int64_t first;
+    int32_t cb;
+    __device__ __forceinline__ int32_t row_base(int64_t i) const { return narrow_row_base<NW>(cb, i); }
+    __device__ __forceinline__ int32_t operator()(int64_t e, int32_t rb) const {
+      if constexpr (NW != 0) return rb + (int32_t)(reinterpret_cast<const uint16_t*>(sc)[e - first]);
+      else return reinterpret_cast<const int32_t*>(sc)[e - first];
+    }
+  } col{sc, w.c.first, cb};
   constexpr int K = (8 + LPR - 1) / LPR;
   const int sub = threadIdx.x % LPR;
   const int rpp = kTileThreads / LPR;
-  S acc = S(0);
   for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
     int lo[U], hi[U];
+    int32_t rb[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      rb[u] = col.row_base(i);
       const bool valid = i < end;
-      lo[u] = valid ? rs[i - wr.first] : 0;
-      hi[u] = valid ? rs[i + 1 - wr.first] : 0;
+      lo[u] = valid ? rs[i - w.r.first] : 0;
+      hi[u] = valid ? rs[i + 1 - w.r.first] : 0;
     }
     S av[U][K];
     int cv[U][K];
@@ -414,8 +416,8 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_tma(Tiles T, const ChartS
       for (int k = 0; k < K; ++k) {
         const int e = lo[u] + sub + k * LPR;
         const bool in = e < hi[u];
-        av[u][k] = in ? vs[e - wv.first] : S(0);
-        cv[u][k] = in ? col(e) : -1;
+        av[u][k] = in ? vs[e - w.v.first] : S(0);
+        cv[u][k] = in ? col(e, rb[u]) : -1;
       }
     V<S, NR> sm[U];
 #pragma unroll
@@ -430,8 +432,8 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_tma(Tiles T, const ChartS
           for (int c = 0; c < NR; ++c) sm[u].c[c] += av[u][k] * pv.c[c];
         }
       for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) {  // rows longer than K * LPR
-        const S a = vs[e - wv.first];
-        const V<S, NR> pv = ldv<S, NR>(p, col(e));
+        const S a = vs[e - w.v.first];
+        const V<S, NR> pv = ldv<S, NR>(p, col(e, rb[u]));
 #pragma unroll
         for (int c = 0; c < NR; ++c) sm[u].c[c] += a * pv.c[c];
       }
@@ -455,47 +457,81 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_tma(Tiles T, const ChartS
       }
     }
   }
+}
+
+template <class S, int NR, int LPR, int U, int NW>
+__global__ void __launch_bounds__(kTileThreads) k_spmv_tma(Tiles T, const ChartState* __restrict__ st,
+                                                           const int32_t* __restrict__ row_ptr,
+                                                           const int32_t* __restrict__ cols,
+                                                           const uint16_t* __restrict__ c16,
+                                                           const int32_t* __restrict__ cbase, const S* __restrict__ vals,
+                                                           const S* __restrict__ p, S* __restrict__ q,
+                                                           double* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char stage[];
+  __shared__ S sh[32];
+  const int64_t t = blockIdx.x;
+  const int32_t ch = T.chart[t];
+  if (st[ch].state != kActive) return;
+  const int64_t beg = T.tab[2 * t], end = T.tab[2 * t + 1];
+  const SpmvWin w = spmv_windows<S, NW>(row_ptr, vals, cols, c16, beg, end);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(stage);
+  unsigned char* buf = stage + 16;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    spmv_issue(w, buf, bar);
+  }
+  __syncthreads();  // the barrier is initialised before anyone waits on it
+  // one decision for the whole CTA: a wait that ran out in any thread sends every thread out
+  if (__syncthreads_or(!mbar_wait(bar, 0, T.spin_limit))) {
+    if (threadIdx.x == 0) atomicOr(T.err, 1);
+    mbar_wait(bar, 0, T.spin_limit);  // (bounded) let this CTA's own copies land before it exits
+    return;
+  }
+  S acc = S(0);
+  spmv_staged_tile<S, NR, LPR, U, NW>(beg, end, w, buf, NW == 1 ? cbase[ch] : 0, p, q, acc);
   S accv[1] = {acc};
   block_sum_t<1, S>(accv, sh);
   if (threadIdx.x == 0) part[t] = (double)accv[0];
 }
 
-// One launch of the SpMV: the 16-bit column instance when the system has that stream (every
-// chart of at most 65536 rows), the 32-bit one otherwise.
-template <class S, int NR, int LPR, int U>
-void launch_spmv(cudaStream_t s, unsigned grid, Tiles T, const ChartState* st, const int32_t* row_ptr,
-                 const int32_t* cols, const uint16_t* c16, const int32_t* cbase, const S* vals, const S* p, S* q,
-                 double* part) {
+// One launch of the SpMV for a column stream of kind nw (0 wide, 1 chart-relative, 2 row-
+// relative): the bulk-copy kernel when the context set it up (upload_tiles) and its stage fits,
+// else the CSR-vector kernel.
+template <class S, int NR, int LPR, int U, int NW>
+void launch_spmv_nw(cudaStream_t s, unsigned grid, const Tiles& T, const ChartState* st, const int32_t* row_ptr,
+                    const int32_t* cols, const uint16_t* c16, const int32_t* cbase, const S* vals, const S* p, S* q,
+                    double* part) {
   if constexpr (std::is_same<S, float>::value && NR == 2) {
-    if (T.max_rows > 0) {  // the bulk-copy kernel where the context set it up (spmv_tma_prepare)
-      if (c16) {
-        const size_t sm = spmv_tma_smem<S, true>(T);
-        if (sm <= kSpmvTmaMaxSmem) {
-          k_spmv_tma<S, NR, LPR, U, true><<<grid, kTileThreads, sm, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q,
-                                                                         part);
-          return;
-        }
-      } else {
-        const size_t sm = spmv_tma_smem<S, false>(T);
-        if (sm <= kSpmvTmaMaxSmem) {
-          k_spmv_tma<S, NR, LPR, U, false><<<grid, kTileThreads, sm, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q,
-                                                                          part);
-          return;
-        }
-      }
+    const size_t sm = spmv_tma_smem<S, NW>(T);
+    if (T.max_rows > 0 && sm <= kSpmvTmaMaxSmem) {
+      k_spmv_tma<S, NR, LPR, U, NW><<<grid, kTileThreads, sm, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q, part);
+      return;
     }
   }
-  if (c16) k_spmv_pq_k<S, NR, LPR, U, true><<<grid, kTileThreads, 0, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q, part);
-  else k_spmv_pq_k<S, NR, LPR, U, false><<<grid, kTileThreads, 0, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q, part);
+  k_spmv_pq_k<S, NR, LPR, U, NW><<<grid, kTileThreads, 0, s>>>(T, st, row_ptr, cols, c16, cbase, vals, p, q, part);
+}
+template <class S, int NR, int LPR, int U>
+void launch_spmv(cudaStream_t s, unsigned grid, const Tiles& T, const ChartState* st, const DevSystem& sys,
+                 const S* vals, const S* p, S* q, double* part) {
+  if (sys.cols16 && sys.rowrel16)
+    launch_spmv_nw<S, NR, LPR, U, 2>(s, grid, T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, vals, p, q, part);
+  else if (sys.cols16)
+    launch_spmv_nw<S, NR, LPR, U, 1>(s, grid, T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, vals, p, q, part);
+  else
+    launch_spmv_nw<S, NR, LPR, U, 0>(s, grid, T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, vals, p, q, part);
 }
 
 // Allows the bulk-copy kernels the dynamic shared memory they need (outside any capture).
 template <class S, int NR, int LPR, int U>
-void spmv_tma_attributes() {
+void spmv_tma_attributes(const Tiles& T) {
   if constexpr (std::is_same<S, float>::value && NR == 2) {
-    RUV_CUDA(cudaFuncSetAttribute(k_spmv_tma<S, NR, LPR, U, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (T.max_rows <= 0) return;
+    RUV_CUDA(cudaFuncSetAttribute(k_spmv_tma<S, NR, LPR, U, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kSpmvTmaMaxSmem));
-    RUV_CUDA(cudaFuncSetAttribute(k_spmv_tma<S, NR, LPR, U, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    RUV_CUDA(cudaFuncSetAttribute(k_spmv_tma<S, NR, LPR, U, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kSpmvTmaMaxSmem));
+    RUV_CUDA(cudaFuncSetAttribute(k_spmv_tma<S, NR, LPR, U, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kSpmvTmaMaxSmem));
   }
 }
@@ -607,7 +643,7 @@ __global__ void __launch_bounds__(kTileThreads) k_fold(Tiles T, const ChartState
 // r32 = r, z = M^-1 r (precond 0: z = r, 1: Jacobi, 2: applied separately, z not written).
 // Partials: r.r and r.z, summed in FP32 over r * rscale and rescaled per tile.  The CSR-vector
 // shape (LPR lanes, K = ceil(8 / LPR) slots, U rows in flight) is the tuned SpMV's.
-template <int NR, int LPR, int U, bool NARROW>
+template <int NR, int LPR, int U, int NW>
 __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const ChartState* __restrict__ st,
                                                                 const int32_t* __restrict__ row_ptr,
                                                                 const int32_t* __restrict__ cols,
@@ -631,10 +667,12 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
   auto run = [&](auto col) {
   for (int64_t base = beg; base < end; base += (int64_t)rpp * U) {
     int lo[U], hi[U];
+    int32_t rb[U];
     DF<NR> xi[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + threadIdx.x / LPR + (int64_t)u * rpp;
+      rb[u] = col.row_base(i);
       const bool valid = i < end;
       lo[u] = valid ? row_ptr[i] : 0;
       hi[u] = valid ? row_ptr[i + 1] : 0;
@@ -650,7 +688,7 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
         const bool in = e < hi[u];
         ah[u][k] = in ? vh[e] : 0.0f;
         al[u][k] = in ? vl[e] : 0.0f;
-        cv[u][k] = in ? col(e) : -1;
+        cv[u][k] = in ? col(e, rb[u]) : -1;
       }
     float Sh[U][NR], Sl[U][NR];
 #pragma unroll
@@ -670,7 +708,7 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
 #pragma unroll
       for (int k = 0; k < K; ++k)
         if (cv[u][k] >= 0) entry(ah[u][k], al[u][k], cv[u][k]);
-      for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) entry(vh[e], vl[e], col(e));
+      for (int e = lo[u] + sub + K * LPR; e < hi[u]; e += LPR) entry(vh[e], vl[e], col(e, rb[u]));
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -715,7 +753,8 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
     }
   }
   };
-  if constexpr (NARROW) run(ColsNarrow{c16, cbase[T.chart[t]]});
+  if constexpr (NW == 1) run(ColsNarrow{c16, cbase[T.chart[t]]});
+  else if constexpr (NW == 2) run(ColsRowRel{c16});
   else run(ColsWide{cols});
   block_sum_t<2, float>(acc, sh);
   if (threadIdx.x == 0) {
@@ -723,6 +762,20 @@ __global__ void __launch_bounds__(kTileThreads) k_true_residual(Tiles T, const C
     part[2 * t] = (double)acc[0] * inv;
     part[2 * t + 1] = (double)acc[1] * inv;
   }
+}
+
+// One launch of the true residual for the system's column stream kind.
+template <int NR, int LPR, int U, class MX>
+void launch_true_residual(cudaStream_t s, unsigned grid, const Tiles& T, const ChartState* st, const DevSystem& sys,
+                          const MX& mx, const float* dinv32, int precond, float* r, float* z, double* part) {
+#define RUV_TR(NWV)                                                                                                   \
+  k_true_residual<NR, LPR, U, NWV><<<grid, kTileThreads, 0, s>>>(T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, \
+                                                                sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32,      \
+                                                                precond, mx.xdf, r, z, part)
+  if (sys.cols16 && sys.rowrel16) RUV_TR(2);
+  else if (sys.cols16) RUV_TR(1);
+  else RUV_TR(0);
+#undef RUV_TR
 }
 
 // ---------------------------------------------------------------- chart kernels
@@ -1067,7 +1120,7 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
   count_launches(1);
   RUV_LAUNCH_CHECK();
   int* h_active = static_cast<int*>(ctx.pinned.get(3 * sizeof(int)));
-  spmv_tma_attributes<S, NR, LPR, U>();
+  spmv_tma_attributes<S, NR, LPR, U>(T);
   RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   RUV_CUDA(cudaStreamSynchronize(s));
   if (*h_active > 0 && NTL > 0) {
@@ -1076,7 +1129,7 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
     cudaGraphExec_t exec = nullptr;
     RUV_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int rep = 0; rep < kCheckEvery; ++rep) {
-      launch_spmv<S, NR, LPR, U>(s, (unsigned)NTL, T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, vals, p, q, part);
+      launch_spmv<S, NR, LPR, U>(s, (unsigned)NTL, T, st, sys, vals, p, q, part);
       k_chart_alpha<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, n_active);
       k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, dinv, jac, mixed ? xs : reinterpret_cast<S*>(x64), r,
                                                              z, p, q, part);
@@ -1086,14 +1139,8 @@ void run_pcg(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T,
         k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0,
                                                                   refresh_delta());
         k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, mx.xdf, reinterpret_cast<float*>(xs), x64);
-        if (sys.cols16)
-          k_true_residual<NR, LPR, U, true><<<(unsigned)NTL, kTileThreads, 0, s>>>(
-              T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, jac,
-              mx.xdf, reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
-        else
-          k_true_residual<NR, LPR, U, false><<<(unsigned)NTL, kTileThreads, 0, s>>>(
-              T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, jac,
-              mx.xdf, reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
+        launch_true_residual<NR, LPR, U>(s, (unsigned)NTL, T, st, sys, mx, dinv32, jac, reinterpret_cast<float*>(r),
+                                         reinterpret_cast<float*>(z), part);
         k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, none, o.max_iter, n_active, 0);
       }
       k_direction<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
@@ -1190,7 +1237,7 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
   count_launches(1);
   RUV_LAUNCH_CHECK();
   int* h_active = static_cast<int*>(ctx.pinned.get(3 * sizeof(int)));
-  spmv_tma_attributes<S, NR, LPR, U>();
+  spmv_tma_attributes<S, NR, LPR, U>(T);
   RUV_CUDA(cudaMemcpyAsync(h_active, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   RUV_CUDA(cudaStreamSynchronize(s));
   if (*h_active > 0 && NTL > 0) {
@@ -1211,21 +1258,15 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
     RUV_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int rep = 0; rep < kRep; ++rep) {
       int l = 0;
-      launch_spmv<S, NR, LPR, U>(s, (unsigned)NTL, T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, vals, p, q, part);
+      launch_spmv<S, NR, LPR, U>(s, (unsigned)NTL, T, st, sys, vals, p, q, part);
       k_chart_alpha<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, n_active);
       k_update<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, dinv, 2, xiter, r, z, p, q, part);
       if (mixed) {
         k_chart_beta_mixed<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1,
                                                                   refresh_delta());
         k_fold<NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, 0, mx.xdf, reinterpret_cast<float*>(xs), x64);
-        if (sys.cols16)
-          k_true_residual<NR, LPR, U, true><<<(unsigned)NTL, kTileThreads, 0, s>>>(
-              T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, 2,
-              mx.xdf, reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
-        else
-          k_true_residual<NR, LPR, U, false><<<(unsigned)NTL, kTileThreads, 0, s>>>(
-              T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, sys.vals32, mx.vals_lo, mx.rsum, mx.bdf, dinv32, 2,
-              mx.xdf, reinterpret_cast<float*>(r), reinterpret_cast<float*>(z), part);
+        launch_true_residual<NR, LPR, U>(s, (unsigned)NTL, T, st, sys, mx, dinv32, 2, reinterpret_cast<float*>(r),
+                                         reinterpret_cast<float*>(z), part);
         k_chart_after_refresh<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part, 1, o.max_iter, n_active, 1);
         l += 4;
       } else {
@@ -1358,13 +1399,22 @@ Shape pick_shape(const Ctx& ctx, const DevSystem& sys) {
 }
 
 template <class S, int NR, int LPR, int U>
-double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
+double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf, bool iter) {
   cudaStream_t s = ctx.stream;
-  spmv_tma_attributes<S, NR, LPR, U>();
+  spmv_tma_attributes<S, NR, LPR, U>(T);
   const int64_t N = sys.n_rows, NC = sys.n_charts;
   ChartState* st = ctx.ws.get<ChartState>("bench.state", NC);
   RUV_CUDA(cudaMemsetAsync(st, 0, sizeof(ChartState) * NC, s));  // every chart active
   double* part = ctx.ws.get<double>("bench.part", T.n);
+  // iter: also the tile kernels of a CG iteration that run over the same tiles (update, dots,
+  // direction), whose cost depends on the tile height as well
+  S* xv = iter ? ctx.ws.get<S>("bench.x", NR * N) : nullptr;
+  S* rv = iter ? ctx.ws.get<S>("bench.r", NR * N) : nullptr;
+  double* part2 = iter ? ctx.ws.get<double>("bench.part2", 2 * T.n) : nullptr;
+  if (iter) {
+    RUV_CUDA(cudaMemsetAsync(xv, 0, sizeof(S) * NR * N, s));
+    RUV_CUDA(cudaMemsetAsync(rv, 0, sizeof(S) * NR * N, s));
+  }
   std::vector<S*> ps(nbuf), qs(nbuf);
   for (int k = 0; k < nbuf; ++k) {
     ps[k] = ctx.ws.get<S>("bench.p" + std::to_string(k), NR * N);
@@ -1373,9 +1423,16 @@ double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
   }
   const S* vals = std::is_same<S, float>::value ? reinterpret_cast<const S*>(sys.vals32) : reinterpret_cast<const S*>(sys.vals);
   auto launch = [&](int k) {
-    launch_spmv<S, NR, LPR, U>(s, (unsigned)T.n, T, st, sys.row_ptr, sys.cols, sys.cols16, sys.cbase, vals, ps[k % nbuf],
+    launch_spmv<S, NR, LPR, U>(s, (unsigned)T.n, T, st, sys, vals, ps[k % nbuf],
                                qs[k % nbuf], part);
     count_launches(1);
+    if (iter && T.n > 0) {
+      k_update<S, NR><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, nullptr, 2, xv, rv, nullptr, ps[k % nbuf],
+                                                             qs[k % nbuf], part2);
+      k_dots_rz<S, NR><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, rv, rv, qs[k % nbuf], part2);
+      k_direction<S, NR><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, rv, ps[k % nbuf]);
+      count_launches(3);
+    }
   };
   for (int k = 0; k < 3; ++k) launch(k);
   RUV_LAUNCH_CHECK();
@@ -1405,9 +1462,9 @@ void dispatch_pcg_sep(Shape sh, Ctx& ctx, DevSystem& sys, double* x64, const Sol
 }
 
 template <class S, int NR>
-double dispatch_time(Shape sh, Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf) {
+double dispatch_time(Shape sh, Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf, bool iter = false) {
 #define RUV_CASE(L, UU) \
-  if (sh.lpr == L && sh.unroll == UU) return time_spmv<S, NR, L, UU>(ctx, sys, T, reps, nbuf);
+  if (sh.lpr == L && sh.unroll == UU) return time_spmv<S, NR, L, UU>(ctx, sys, T, reps, nbuf, iter);
   RUV_SHAPES(RUV_CASE)
 #undef RUV_CASE
   throw Error{RUV_ERR_BAD_INPUT, "unsupported SpMV shape"};
@@ -1429,71 +1486,97 @@ TileTable make_tiles(const std::vector<int64_t>& chart_row, int64_t tile_rows) {
   return T;
 }
 
-// 16-bit column stream: entries of charts of at most 65536 rows as offsets from the chart's
-// first row (one thread per row); cbase = the first row of such a chart, -1 otherwise.
+// 16-bit column stream, one thread per row: every entry as an offset from its chart's first
+// row (all charts of at most 65536 rows), or with `rowrel` as an offset from its row's index
+// minus 32768, *bad set where an entry lies more than 32767 rows from its row.
 constexpr int64_t kNarrowRows = 65536;
 __global__ void k_narrow_cols(int64_t n, const int64_t* __restrict__ chart_row, int64_t n_charts,
-                              const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
-                              uint16_t* __restrict__ c16) {
+                              const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols, int rowrel,
+                              uint16_t* __restrict__ c16, int* __restrict__ bad) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (rowrel) {
+    for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
+      const int64_t d = (int64_t)cols[e] - i + kRowRelBias;
+      if (d < 0 || d > 65535) {
+        atomicOr(bad, 1);
+        return;
+      }
+      c16[e] = (uint16_t)d;
+    }
+    return;
+  }
   int64_t lo = 0, hi = n_charts;  // the chart of row i: largest c with chart_row[c] <= i
   while (hi - lo > 1) {
     const int64_t mid = (lo + hi) >> 1;
     if (chart_row[mid] <= i) lo = mid; else hi = mid;
   }
   const int64_t r0 = chart_row[lo];
-  if (chart_row[lo + 1] - r0 > kNarrowRows) return;
   for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) c16[e] = (uint16_t)(cols[e] - r0);
-}
-__global__ void k_chart_entry(int64_t n_charts, const int64_t* __restrict__ chart_row, const int32_t* __restrict__ row_ptr,
-                              int32_t* __restrict__ out) {  // the first entry of every chart (and the end)
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c <= n_charts) out[c] = row_ptr[chart_row[c]];
 }
 __global__ void k_chart_base(int64_t n_charts, const int64_t* __restrict__ chart_row, int32_t* __restrict__ cbase) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < n_charts) cbase[c] = chart_row[c + 1] - chart_row[c] <= kNarrowRows ? (int32_t)chart_row[c] : -1;
+  if (c < n_charts) cbase[c] = (int32_t)chart_row[c];
 }
 
 }  // namespace
 
-// The 16-bit column stream of a chart-blocked CSR operator (all charts of at most 65536
-// rows, else none: the narrow kernels take every tile's base from cbase).  Returns false
-// and leaves both pointers null when some chart is larger.
+// The 16-bit column stream of a chart-blocked CSR operator: chart-relative (cbase = each
+// chart's first row) when every chart has at most 65536 rows, else row-relative (*rowrel,
+// cbase null) when every entry lies within 32767 rows of its row.  Returns false and leaves
+// the pointers null otherwise (the one case that reads a flag back: only operators with a
+// chart above 65536 rows pay that synchronisation).  RUV_NARROW_COLS=chart: chart-relative
+// streams only.
 bool narrow_operator(Ctx& ctx, int64_t n, int64_t nnz, int64_t n_charts, const std::vector<int64_t>& h_chart_row,
                      const int64_t* chart_row, const int32_t* row_ptr, const int32_t* cols, const std::string& tag,
-                     uint16_t** c16, int32_t** cbase) {
+                     uint16_t** c16, int32_t** cbase, bool* rowrel) {
   *c16 = nullptr;
   *cbase = nullptr;
+  *rowrel = false;
+  bool large = false;
   for (int64_t c = 0; c < n_charts; ++c)
-    if (h_chart_row[c + 1] - h_chart_row[c] > kNarrowRows) return false;
+    if (h_chart_row[c + 1] - h_chart_row[c] > kNarrowRows) large = true;
+  const char* env = std::getenv("RUV_NARROW_COLS");
+  if (large && env && std::string(env) == "chart") return false;
   cudaStream_t s = ctx.stream;
-  *c16 = ctx.ws.get<uint16_t>(tag + ".c16", std::max<int64_t>(nnz, 1));
-  *cbase = ctx.ws.get<int32_t>(tag + ".cbase", std::max<int64_t>(n_charts, 1));
+  uint16_t* d16 = ctx.ws.get<uint16_t>(tag + ".c16", std::max<int64_t>(nnz, 1));
+  int32_t* dbase = large ? nullptr : ctx.ws.get<int32_t>(tag + ".cbase", std::max<int64_t>(n_charts, 1));
+  int* bad = ctx.ws.get<int>(tag + ".c16bad", 1);
+  RUV_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   if (n > 0) {
-    k_narrow_cols<<<div_up(n, 256), 256, 0, s>>>(n, chart_row, n_charts, row_ptr, cols, *c16);
+    k_narrow_cols<<<div_up(n, 256), 256, 0, s>>>(n, chart_row, n_charts, row_ptr, cols, large ? 1 : 0, d16, bad);
     count_launches(1);
   }
-  if (n_charts > 0) {
-    k_chart_base<<<div_up(n_charts, 256), 256, 0, s>>>(n_charts, chart_row, *cbase);
+  if (!large && n_charts > 0) {
+    k_chart_base<<<div_up(n_charts, 256), 256, 0, s>>>(n_charts, chart_row, dbase);
     count_launches(1);
   }
   RUV_LAUNCH_CHECK();
+  if (large) {
+    int h = 0;
+    RUV_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RUV_CUDA(cudaStreamSynchronize(s));
+    if (h != 0) return false;
+  }
+  *c16 = d16;
+  *cbase = dbase;
+  *rowrel = large;
   return true;
 }
 
 // On unless RUV_NARROW_COLS=0: on the 4096-disk operator the 16-bit stream cuts the SpMV's
-// bytes by 18% and its time by 13% (0.215 -> 0.187 ms).
+// bytes by 18% and its time by 13% (0.215 -> 0.187 ms); RUV_NARROW_COLS=chart keeps it to
+// charts of at most 65536 rows (larger charts then make the whole operator 32-bit).
 void narrow_columns(Ctx& ctx, DevSystem& sys) {
   const char* e = std::getenv("RUV_NARROW_COLS");
   if (e && e[0] == '0') {  // 32-bit columns only
     sys.cols16 = nullptr;
     sys.cbase = nullptr;
+    sys.rowrel16 = false;
     return;
   }
   narrow_operator(ctx, sys.n_rows, sys.nnz, sys.n_charts, sys.h_chart_row, sys.chart_row, sys.row_ptr, sys.cols,
-                  "sys", &sys.cols16, &sys.cbase);
+                  "sys", &sys.cols16, &sys.cbase, &sys.rowrel16);
 }
 
 double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers, double* bytes,
@@ -1503,20 +1586,8 @@ double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers,
   const Shape sh = pick_shape(ctx, sys);
   const double N = (double)sys.n_rows, NNZ = (double)sys.nnz, nr = (double)sys.nrhs;
   const double vb = mixed ? 4.0 : 8.0;
-  // column bytes per entry: 2 for charts with the 16-bit stream, 4 otherwise
-  double cb = 4.0;
-  if (sys.cols16 && sys.n_charts > 0) {
-    double narrow_nnz = 0.0;
-    std::vector<int32_t> rp(sys.n_charts + 1);
-    int32_t* d_rp = ctx.ws.get<int32_t>("bench.chart_nnz", sys.n_charts + 1);
-    k_chart_entry<<<div_up(sys.n_charts + 1, 256), 256, 0, ctx.stream>>>(sys.n_charts, sys.chart_row, sys.row_ptr, d_rp);
-    count_launches(1);
-    RUV_CUDA(cudaMemcpyAsync(rp.data(), d_rp, sizeof(int32_t) * (sys.n_charts + 1), cudaMemcpyDeviceToHost, ctx.stream));
-    RUV_CUDA(cudaStreamSynchronize(ctx.stream));
-    for (int64_t c = 0; c < sys.n_charts; ++c)
-      if (sys.h_chart_row[c + 1] - sys.h_chart_row[c] <= kNarrowRows) narrow_nnz += (double)(rp[c + 1] - rp[c]);
-    cb = NNZ > 0 ? (2.0 * narrow_nnz + 4.0 * (NNZ - narrow_nnz)) / NNZ : 4.0;
-  }
+  // column bytes per entry: 2 with the 16-bit stream (every chart has it then), 4 otherwise
+  const double cb = sys.cols16 ? 2.0 : 4.0;
   // algorithmic bytes: values, 32-bit columns, row pointers, p read once, q written; the
   // stream bytes count the columns the kernel actually reads (16-bit where narrowed)
   if (bytes) *bytes = NNZ * (vb + 4.0) + (N + 1.0) * 4.0 + 2.0 * N * nr * vb;
@@ -1529,7 +1600,9 @@ double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers,
 }
 
 // Autotuner: time the batched SpMV for every instantiated (lanes per row, rows in flight)
-// shape and tile height on the assembled operator; keep the fastest in the context.
+// shape and tile height on the assembled operator, each with the update, dots and direction
+// kernels of a CG iteration over the same tiles (the tile height sets their grid too); keep
+// the fastest in the context.
 TuneResult autotune_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps) {
   narrow_columns(ctx, sys);
   TuneResult best{0, 0, 0, 1e30};
@@ -1545,9 +1618,9 @@ TuneResult autotune_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps) {
     Tiles T = upload_tiles(ctx, sys, "tune");
     if (T.n == 0) break;
     for (const Shape& sh : shapes) {
-      double ms = sys.nrhs == 2 ? (mixed ? dispatch_time<float, 2>(sh, ctx, sys, T, reps, 2)
-                                         : dispatch_time<double, 2>(sh, ctx, sys, T, reps, 2))
-                                : dispatch_time<double, 1>(sh, ctx, sys, T, reps, 2);
+      double ms = sys.nrhs == 2 ? (mixed ? dispatch_time<float, 2>(sh, ctx, sys, T, reps, 2, true)
+                                         : dispatch_time<double, 2>(sh, ctx, sys, T, reps, 2, true))
+                                : dispatch_time<double, 1>(sh, ctx, sys, T, reps, 2, true);
       if (ms < best.ms) best = TuneResult{sh.lpr, sh.unroll, tr, ms};
     }
   }

@@ -23,8 +23,10 @@ struct DevSystem {
   int32_t* cols = nullptr;       // nnz (global row ids)
   double* vals = nullptr;        // nnz, FP64
   float* vals32 = nullptr;       // nnz, FP32 copy for the mixed-precision inner loop
-  uint16_t* cols16 = nullptr;    // nnz: column - first row of the chart (charts of <= 65536 rows)
-  int32_t* cbase = nullptr;      // n_charts: first row of a chart with cols16, -1 otherwise
+  uint16_t* cols16 = nullptr;    // nnz: column - first row of the chart (every chart <= 65536 rows),
+                                 // or column - row + 32768 (rowrel16: some chart is larger)
+  int32_t* cbase = nullptr;      // n_charts: first row of each chart (chart-relative stream)
+  bool rowrel16 = false;
   double* diag = nullptr;        // n_rows
   double* b = nullptr;           // nrhs * n_rows
   // the mixed solver's low FP32 halves of vals and FP64 row sums as double-float pairs, when
@@ -96,11 +98,12 @@ void ic0_export(Ctx& ctx, const DevSystem& sys, bool colored, std::vector<int64_
 
 // The 16-bit column stream of `sys` (cols16, cbase), built on the device.
 void narrow_columns(Ctx& ctx, DevSystem& sys);
-// The same for any chart-blocked CSR operator (an AMG level); false (null pointers) when a
-// chart has more than 65536 rows.
+// The same for any chart-blocked CSR operator (an AMG level): chart-relative when every chart
+// has at most 65536 rows, else row-relative (*rowrel); false (null pointers) when an entry of
+// a row-relative operator lies more than 32767 rows from its row.
 bool narrow_operator(Ctx& ctx, int64_t n, int64_t nnz, int64_t n_charts, const std::vector<int64_t>& h_chart_row,
                      const int64_t* chart_row, const int32_t* row_ptr, const int32_t* cols, const std::string& tag,
-                     uint16_t** c16, int32_t** cbase);
+                     uint16_t** c16, int32_t** cbase, bool* rowrel);
 
 // x (nrhs * n_rows, device) <- A^-1 b per chart.  Returns per-chart results (host).
 std::vector<ChartResult> pcg_solve(Ctx& ctx, DevSystem& sys, double* x, const SolveOpts& o);

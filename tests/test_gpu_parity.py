@@ -272,19 +272,21 @@ def test_group_graph_bitwise(monkeypatch):
         assert np.array_equal(a.uv, b.uv)
 
 
-@pytest.mark.parametrize("case", ["disks_16bit_columns", "field_32bit_columns"])
+@pytest.mark.parametrize("case", ["disks_16bit_columns", "field_row_relative_columns", "field_32bit_columns"])
 def test_bulk_copy_spmv_bitwise(monkeypatch, case):
     """The SpMV that stages each tile's row pointers, values and columns into shared memory
-    by bulk asynchronous copies (the default; RUV_SPMV_TMA=0 keeps the CSR-vector kernel
-    reading them from global memory) runs the same row loop: bitwise the same UVs and
-    iterations, with the 16-bit column stream (charts of <= 65536 rows) and with 32-bit
-    columns (a 258k-row chart)."""
+    by bulk asynchronous copies (the default) runs the same row loop as the CSR-vector kernel
+    reading them from global memory (RUV_SPMV_TMA=0): bitwise the same UVs and iterations,
+    with the chart-relative 16-bit column stream (charts of <= 65536 rows), the row-relative
+    one (a 258k-row chart) and 32-bit columns (the same chart, RUV_NARROW_COLS=chart)."""
     if case == "disks_16bit_columns":
         vo, to, p3, tr = W.disks(24, t_min=200, t_max=20000, seed=53)
         C = R.prepare_patches(vo, to, p3, tr)
     else:
         p, f = W.height_field(512, 8, 0.15, seed=2)
         C = R.prepare_mesh(p, f)
+    if case == "field_32bit_columns":
+        monkeypatch.setenv("RUV_NARROW_COLS", "chart")
     ctx = R.Context(0)
     for pc in (R.Precond.JACOBI, R.Precond.AMG_SA):
         opts = R.UnfoldOptions(precond=pc, precision=R.Precision.MIXED)
@@ -293,6 +295,27 @@ def test_bulk_copy_spmv_bitwise(monkeypatch, case):
         monkeypatch.delenv("RUV_SPMV_TMA", raising=False)
         staged = R.unfold_charts(ctx, C, opts)
         for a, b in zip(plain, staged):
+            assert a.status == b.status == R.Status.OK
+            assert a.cg_iters == b.cg_iters
+            assert np.array_equal(a.uv, b.uv)
+
+
+@pytest.mark.parametrize("precision", [R.Precision.MIXED, R.Precision.FP64])
+def test_row_relative_columns_bitwise(monkeypatch, precision):
+    """A chart of more than 65536 rows (a 512^2 height field, 258k rows) streams its columns
+    as 16-bit offsets from each row (every entry lies within 32767 rows of its row in the
+    grid's order) on the system operator and the AMG levels: bitwise the same UVs and
+    iterations as with 32-bit columns (RUV_NARROW_COLS=chart)."""
+    p, f = W.height_field(512, 8, 0.15, seed=2)
+    C = R.prepare_mesh(p, f)
+    ctx = R.Context(0)
+    for pc in (R.Precond.JACOBI, R.Precond.AMG_SA, R.Precond.AMG):
+        opts = R.UnfoldOptions(precond=pc, precision=precision)
+        monkeypatch.setenv("RUV_NARROW_COLS", "chart")
+        wide = R.unfold_charts(ctx, C, opts)
+        monkeypatch.delenv("RUV_NARROW_COLS", raising=False)
+        rel = R.unfold_charts(ctx, C, opts)
+        for a, b in zip(wide, rel):
             assert a.status == b.status == R.Status.OK
             assert a.cg_iters == b.cg_iters
             assert np.array_equal(a.uv, b.uv)
