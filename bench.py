@@ -630,13 +630,16 @@ def single_chart_reference(ctx, vo, unknowns, batched_ms, n_sample):
 
 
 FD_STEPS = (1e-6, 1e-7, 1e-8, 1e-9)
+FD_EDGE_SCALE = None  # (a cap of h at a multiple of the vertex's shortest edge: off)
+FD_REFINE = 2  # refinement steps of each perturbed solve (its rounding scales with the condition number)
 
 
 def _fd_worker(args):
     from oracle import oracle as O
 
     p3, tris, pinned, pin_uv, lam, target, picks = args
-    return O.fd_gradient(p3, tris, pinned, pin_uv, lam, target, picks, reuse_base=True, smooth_steps=FD_STEPS)
+    return O.fd_gradient(p3, tris, pinned, pin_uv, lam, target, picks, reuse_base=True, smooth_steps=FD_STEPS,
+                         edge_scale=FD_EDGE_SCALE, refine=FD_REFINE)
 
 
 def fd_parallel(p3, tris, pinned, pin_uv, lam, target, picks, workers):
@@ -749,10 +752,13 @@ def run_adjoint(args, rank, world, local, pg):
             "instance": f"the {n_lat}x{2 * n_lat} sphere itself", "picks": len(picks),
             "what": "FP64 central differences of the loss through the fixed-pin SuperLU solve (perturbed systems "
                     "by a low-rank update of the unperturbed factors)",
-            "h": "per pick, the largest of 1e-6, 1e-7, 1e-8, 1e-9 at which neither +h nor -h moves a clamp of the "
-                 "assembly around the vertex (a corner cotangent's clamp at 0, an edge weight's drop threshold): "
-                 "the loss is piecewise smooth, and a quotient across a kink averages two one-sided derivatives",
-            "h_counts": {f"{hh:g}": int((fd_h == hh).sum()) for hh in FD_STEPS},
+            "h": "per pick, the largest of 1e-6, 1e-7, 1e-8, 1e-9 (each capped at 1e-3 x the shortest edge at "
+                 "the vertex: next to the poles edges are ~2e-5 long) at which neither +h nor -h moves a clamp of "
+                 "the assembly around the vertex (a corner cotangent's clamp at 0, an edge weight's drop "
+                 "threshold): the loss is piecewise smooth, and a quotient across a kink averages two one-sided "
+                 "derivatives",
+            "h_counts": {"1e-6": int((fd_h == 1e-6).sum()), "below 1e-6": int((fd_h < 1e-6).sum())},
+            "h_min": float(np.nanmin(fd_h)) if np.isfinite(fd_h).any() else None,
             "picks_without_smooth_h": int((~ok).sum()),
             "components": int(ok.sum()),
             "rel_err_norm": float(np.linalg.norm(a_ - f_) / np.linalg.norm(f_)) if ok.any() else None,
@@ -896,7 +902,8 @@ def main():
                    "phase_ms": {"assembly": round(phases[0], 3), "pcg": round(phases[1], 3),
                                 "driver": round(phases[2], 3), "precond_setup_in_pcg": round(phases[3], 3)},
                    "cg_iters_max": int(cg_iters.max()), "cg_iters_mean": float(cg_iters.mean()),
-                   "spmv_shape": {"lanes_per_row": tuned[0], "rows_in_flight": tuned[1], "tile_rows": tuned[2]},
+                   "spmv_shape": {"lanes_per_row": tuned[0], "rows_in_flight": tuned[1], "tile_rows": tuned[2],
+                                  "bulk_copy_staging": bool(R.spmv_form(ctx))},
                    "charts_not_ok": int((statuses != 0).sum())},
         "e2e": {"value": world * unknowns / (ems / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ems,

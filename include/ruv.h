@@ -296,6 +296,11 @@ ruv_status ruv_bench_spmv(ruv_ctx* ctx, ruv_precision precision, int32_t reps, i
 ruv_status ruv_autotune(ruv_ctx* ctx, ruv_precision precision, int32_t reps, int32_t* lanes_per_row,
                         int32_t* rows_in_flight, int32_t* tile_rows, double* ms_per_launch);
 
+/* The SpMV form this context's solves use: *bulk_copy = 1 for the kernel that stages each
+ * tile by bulk asynchronous copies, 0 for the CSR-vector kernel (the default; the autotuner
+ * picks one; the environment variable RUV_SPMV_TMA=0/1 overrides both). */
+ruv_status ruv_spmv_form(ruv_ctx* ctx, int32_t* bulk_copy);
+
 /* ------------------------------------------------------------------ host chart stages */
 
 typedef struct ruv_prepared ruv_prepared;

@@ -474,7 +474,7 @@ def lu_adjoint_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target):
 
 
 def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float = 1e-6, refine: int = 0,
-                reuse_base: bool = False, smooth_steps=None):
+                reuse_base: bool = False, smooth_steps=None, edge_scale=None):
     """Central differences of config4_loss with respect to p3[v, k] for (v, k) in picks,
     through the fixed-pin solve.  The perturbed solution is formed as x + dx with
     A' dx = (b' - b) - (A' - A) x (a right-hand side that is exactly zero away from v), and
@@ -496,7 +496,10 @@ def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float
     averages two one-sided derivatives.  For each pick the first h of the sequence at which
     neither v + h nor v - h moves a clamp of the triangles around v (no corner cotangent of
     them changes sign, the sparsity pattern is unchanged) is used; a pick with no such h gets
-    NaN.  Returns (values, h used per pick) in that case, the values alone otherwise."""
+    NaN.  ``edge_scale``: each h of the sequence is first capped at edge_scale times the
+    shortest edge at v, so the quotient's truncation error, which grows as (h / edge)^2,
+    stays small on short edges too.  Returns (values, h used per pick) in that case, the
+    values alone otherwise."""
     p3 = np.ascontiguousarray(p3, np.float64).reshape(-1, 3)
     tris = np.ascontiguousarray(tris, np.int64).reshape(-1, 3)
     base = FixedPinChart(p3, tris, pinned, pin_uv)
@@ -545,8 +548,9 @@ def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float
             dA.data = ch.A.data - base.A.data
             rhs = (ch.b - base.b) - dA @ x
             dx = woodbury(dA, rhs) if reuse_base else ch.solve(rhs)
-            for _ in range(refine):  # iterative refinement of the small correction
-                dx = dx + (base if reuse_base else ch).solve(rhs - ch.A @ dx)
+            for _ in range(refine):  # iterative refinement of the small correction on A'
+                res = rhs - ch.A @ dx
+                dx = dx + (woodbury(dA, res) if reuse_base else ch.solve(res))
         else:  # an edge weight crossed the drop threshold (a clamped cotangent at 0)
             dx = ch.solve() - x
         uv2 = uv.copy()
@@ -571,8 +575,13 @@ def fd_gradient(p3, tris, pinned, pin_uv, lam_l2: float, target, picks, h: float
             continue
         tv = tris[order[starts[v]:starts[v + 1]] // 3]
         s0 = cot_signs(p3, tv)
+        cap = float("inf")
+        if edge_scale is not None:
+            for a, b in ((0, 1), (1, 2), (2, 0)):
+                cap = min(cap, edge_scale * float(np.linalg.norm(p3[tv[:, a]] - p3[tv[:, b]], axis=1).min()))
         val, hv = float("nan"), float("nan")
         for hh in smooth_steps:
+            hh = min(hh, cap)
             sides, ok = [], True
             for sgn in (1.0, -1.0):
                 q = p3.copy()

@@ -99,6 +99,7 @@ SIGNATURES = {
     "ruv_cg_solve_noalloc": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _i64, _f64, ctypes.c_int, _P(_i64), _vp,
                                             ctypes.c_char_p, _i32]),
     "ruv_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _P(_i32), _P(_i32), _P(_i32), _P(_f64)]),
+    "ruv_spmv_form": (ctypes.c_int, [_vp, _P(_i32)]),
     "ruv_bench_spmv": (ctypes.c_int, [_vp, ctypes.c_int, _i32, _i32, _P(_f64), _P(_f64), _P(_f64)]),
 }
 
@@ -710,9 +711,17 @@ def bench_spmv(ctx: Context, precision: Precision = Precision.MIXED, reps: int =
 
 
 def autotune(ctx: Context, precision: Precision = Precision.MIXED, reps: int = 10):
-    """Pick the fastest SpMV launch shape on the last assembled batch; returns
-    (lanes_per_row, rows_in_flight, tile_rows, ms_per_launch)."""
+    """Pick the fastest SpMV launch shape and form on the last assembled batch; returns
+    (lanes_per_row, rows_in_flight, tile_rows, ms of that SpMV plus the CG iteration's other
+    tile kernels); the form: spmv_form(ctx)."""
     l, u, t, ms = _i32(0), _i32(0), _i32(0), _f64(0)
     ctx.check(lib().ruv_autotune(ctx.h, int(precision), reps, ctypes.byref(l), ctypes.byref(u), ctypes.byref(t),
                                  ctypes.byref(ms)), "ruv_autotune")
     return l.value, u.value, t.value, ms.value
+
+
+def spmv_form(ctx: Context) -> int:
+    """1 when this context's solves use the bulk-copy staged SpMV, 0 for the CSR-vector one."""
+    b = _i32(0)
+    ctx.check(lib().ruv_spmv_form(ctx.h, ctypes.byref(b)), "ruv_spmv_form")
+    return b.value

@@ -64,10 +64,67 @@ ruv_status guarded(ruv_ctx* ctx, F&& body) {
   }
 }
 
+// Host-to-device copy through the SMs: a page-locked, mapped host buffer read over its device
+// mapping, 16 bytes per load with four loads in flight per thread (head and tail bytewise).
+__global__ void k_h2d(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, size_t head,
+                      size_t n16, size_t tail) {
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (size_t)gridDim.x * blockDim.x;
+  if (tid < head) dst[tid] = src[tid];
+  const uint4* s4 = reinterpret_cast<const uint4*>(src + head);
+  uint4* d4 = reinterpret_cast<uint4*>(dst + head);
+  size_t i = tid;
+  for (; i + 3 * nth < n16; i += 4 * nth) {
+    const uint4 a = s4[i], b = s4[i + nth], c = s4[i + 2 * nth], d = s4[i + 3 * nth];
+    d4[i] = a;
+    d4[i + nth] = b;
+    d4[i + 2 * nth] = c;
+    d4[i + 3 * nth] = d;
+  }
+  for (; i < n16; i += nth) d4[i] = s4[i];
+  if (tid < tail) dst[head + 16 * n16 + tid] = src[head + 16 * n16 + tid];
+}
+
+// n bytes host -> device on stream st.  Where the host buffer is page-locked and mapped (and
+// both ends share their offset from a 16-byte boundary) the copy is k_h2d; otherwise
+// cudaMemcpyAsync.  On GB300 hosts copy-engine transfers of pinned memory ran at 211 GB/s but
+// now and then many times slower right after heavy GPU work, while the SMs pulling the same
+// mapped buffer held 211 GB/s in every repetition.  RUV_H2D_KERNEL=0: always cudaMemcpyAsync.
+void h2d(Ctx& c, void* dev, const void* host, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return;
+  static const bool off = [] {
+    const char* e = std::getenv("RUV_H2D_KERNEL");
+    return e && e[0] == '0';
+  }();
+  cudaPointerAttributes a{};
+  const void* src = nullptr;
+  if (!off) {
+    if (cudaPointerGetAttributes(&a, host) == cudaSuccess) {
+      if (a.type == cudaMemoryTypeHost && a.devicePointer) src = a.devicePointer;
+    } else {
+      cudaGetLastError();  // clear what the query left (the copy below reports its own errors)
+    }
+  }
+  const uintptr_t sa = (uintptr_t)src, da = (uintptr_t)dev;
+  if (!src || (sa & 15) != (da & 15)) {
+    RUV_CUDA(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, st));
+    return;
+  }
+  const size_t head = std::min<size_t>(bytes, (16 - (sa & 15)) & 15);
+  const size_t n16 = (bytes - head) / 16, tail = bytes - head - 16 * n16;
+  int dev_id = 0, sms = 0;
+  RUV_CUDA(cudaGetDevice(&dev_id));
+  RUV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 4, div_up((int64_t)n16, 256)));
+  k_h2d<<<grid, 256, 0, st>>>(static_cast<const unsigned char*>(src), static_cast<unsigned char*>(dev), head, n16,
+                              tail);
+  count_launches(1);
+  RUV_LAUNCH_CHECK();
+}
+
 template <class T>
 T* upload(Ctx& c, const std::string& name, const T* host, int64_t n, cudaStream_t st = nullptr) {
   T* d = c.ws.get<T>(name, n);
-  if (n > 0) RUV_CUDA(cudaMemcpyAsync(d, host, sizeof(T) * n, cudaMemcpyHostToDevice, st ? st : c.stream));
+  if (n > 0) h2d(c, d, host, sizeof(T) * n, st ? st : c.stream);
   return d;
 }
 
@@ -370,8 +427,8 @@ ruv_status upload_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, bool overlap) {
     const int64_t vs = in->vert_off[cs], ts = in->tri_off[cs];
     bt.p3 = c.ws.get<double>("in.p3", 3 * NV);
     bt.tris = c.ws.get<int32_t>("in.tris", 3 * NT);
-    if (vs > 0) RUV_CUDA(cudaMemcpyAsync(bt.p3, in->p3, sizeof(double) * 3 * vs, cudaMemcpyHostToDevice, c.stream));
-    if (ts > 0) RUV_CUDA(cudaMemcpyAsync(bt.tris, in->tris, sizeof(int32_t) * 3 * ts, cudaMemcpyHostToDevice, c.stream));
+    if (vs > 0) h2d(c, bt.p3, in->p3, sizeof(double) * 3 * vs, c.stream);
+    if (ts > 0) h2d(c, bt.tris, in->tris, sizeof(int32_t) * 3 * ts, c.stream);
     cudaStream_t rest = c.stream;
     if (overlap) {  // after everything already on the main stream, then in parallel with it
       RUV_CUDA(cudaEventRecord(c.ev_core, c.stream));
@@ -392,12 +449,8 @@ ruv_status upload_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, bool overlap) {
         bt.rest_ready = c.ev_rest;
       }
     } guard{c, bt, overlap, false};
-    if (NV > vs)
-      RUV_CUDA(cudaMemcpyAsync(bt.p3 + 3 * vs, in->p3 + 3 * vs, sizeof(double) * 3 * (NV - vs), cudaMemcpyHostToDevice,
-                               rest));
-    if (NT > ts)
-      RUV_CUDA(cudaMemcpyAsync(bt.tris + 3 * ts, in->tris + 3 * ts, sizeof(int32_t) * 3 * (NT - ts),
-                               cudaMemcpyHostToDevice, rest));
+    if (NV > vs) h2d(c, bt.p3 + 3 * vs, in->p3 + 3 * vs, sizeof(double) * 3 * (NV - vs), rest);
+    if (NT > ts) h2d(c, bt.tris + 3 * ts, in->tris + 3 * ts, sizeof(int32_t) * 3 * (NT - ts), rest);
     if (overlap) {
       RUV_CUDA(cudaEventRecord(c.ev_second, c.side));
       bt.second_ready = c.ev_second;
@@ -754,6 +807,13 @@ ruv_status ruv_bench_spmv(ruv_ctx* ctx, ruv_precision precision, int32_t reps, i
     if (stream_bytes_per_launch) *stream_bytes_per_launch = stream;
     return RUV_OK;
   });
+}
+
+ruv_status ruv_spmv_form(ruv_ctx* ctx, int32_t* bulk_copy) {
+  if (!ctx || !bulk_copy) return RUV_ERR_BAD_INPUT;
+  const char* te = std::getenv("RUV_SPMV_TMA");
+  *bulk_copy = te ? (te[0] == '1' ? 1 : 0) : ctx->c.spmv_tma;
+  return RUV_OK;
 }
 
 ruv_status ruv_autotune(ruv_ctx* ctx, ruv_precision precision, int32_t reps, int32_t* lanes_per_row,

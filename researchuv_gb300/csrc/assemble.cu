@@ -119,9 +119,10 @@ __global__ void k_globalize(const int32_t* __restrict__ tris, const int64_t* __r
 }
 
 // Clamped cotangent at each triangle corner m (angle at t[m], opposite edge t[m+1]-t[m+2]),
-// lscm.rs:256-268; 0.0 where the reference skips the corner (degenerate guard).
+// lscm.rs:256-268; 0.0 where the reference skips the corner (degenerate guard).  Also the
+// squared length of each corner's opposite edge (sq).
 __global__ void k_corner_cot(const double* __restrict__ p3, const int32_t* __restrict__ tri_g, int64_t t_begin,
-                             int64_t t_end, double* __restrict__ cot) {
+                             int64_t t_end, double* __restrict__ cot, double* __restrict__ sq) {
   int64_t t = t_begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= t_end) return;
   int32_t v[3] = {tri_g[3 * t], tri_g[3 * t + 1], tri_g[3 * t + 2]};
@@ -136,7 +137,11 @@ __global__ void k_corner_cot(const double* __restrict__ p3, const int32_t* __res
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     e[k] = psub(p[(k + 1) % 3], p[k]);
-    len[k] = plen(e[k]);
+    const double d2 = pdot(e[k], e[k]);
+    len[k] = sqrt_rn(d2);  // = plen(e[k])
+    // the squared length of the edge opposite corner (k + 2) % 3, for the rows pass: the same
+    // bits as |p_nb - p_v|^2 from either endpoint (a negated difference squares the same)
+    sq[3 * t + (k + 2) % 3] = d2;
   }
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
@@ -218,9 +223,10 @@ __device__ __forceinline__ void sort16(unsigned long long (&k)[16]) {
 // One row (free vertex v).  MODE 0: sort the bucket, form each kept edge's coefficient
 // c = w / max(|p_nb - p_v|^2, EPS) once (stored at the neighbour's first record; -1 marks a
 // dropped edge) and count entries; MODE 1: fill from the stored coefficients.
-template <int MODE>
+template <int MODE, bool MIXB>
 __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, const int64_t* __restrict__ row_of,
                        const int64_t* __restrict__ rec_off, int2* __restrict__ rec, const double* __restrict__ cot,
+                       const double* __restrict__ sq,
                        const double* __restrict__ p3, const double* __restrict__ p2, const double* __restrict__ pin_uv,
                        double mix_b, int32_t* __restrict__ row_len, const int64_t* __restrict__ row_ptr,
                        int32_t* __restrict__ cols, double* __restrict__ vals, float* __restrict__ vals32,
@@ -267,7 +273,6 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
       }
     }
   }
-  const P3 pv = ld3(p3, v);
   const int64_t row = row_of[v];
   // the coefficient of the neighbour group starting at record i (its end returned in j)
   auto group = [&](int64_t i, int64_t& j) -> double {
@@ -277,13 +282,12 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
       while (j < r1 && rec[j].x == nb) ++j;
       return coef[i];
     }
-    double w = 0.0;
-    for (; j < r1 && rec[j].x == nb; ++j) w = dadd(w, cot[rec[j].y]);
+    // w = 0 + cot_1 + cot_2 + ... in record order; every cotangent is +0 or positive, so the
+    // first addition returns cot_1 itself
+    double w = cot[rec[j].y];
+    for (++j; j < r1 && rec[j].x == nb; ++j) w = dadd(w, cot[rec[j].y]);
     double c = -1.0;
-    if (!le_pos(w, kEpsDegenerate)) {  // lscm.rs:606
-      P3 d3 = psub(ld3(p3, nb), pv);
-      c = ddiv(w, max_pos(pdot(d3, d3), kEpsDegenerate));
-    }
+    if (!le_pos(w, kEpsDegenerate)) c = ddiv(w, max_pos(sq[rec[i].y], kEpsDegenerate));  // lscm.rs:606
     coef[i] = c;
     return c;
   };
@@ -331,7 +335,11 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
     ++at;
   };
   double bu = 0.0, bv = 0.0;
-  const double p2u = p2[2 * v], p2v = p2[2 * v + 1];
+  // MIXB false (mix_b == 0, the default angle_mix = 1): every pull term mix_b * c * d is a
+  // signed zero and b starts at +0, so adding it changes no bit of b (x + (+-0) = x for
+  // x != 0, +0 + (+-0) = +0, and b never becomes -0); those FP64 operations and the p2
+  // gathers are skipped.  A pinned neighbour's term reduces to c * pin_uv exactly.
+  const double p2u = MIXB ? p2[2 * v] : 0.0, p2v = MIXB ? p2[2 * v + 1] : 0.0;
   for (int64_t i = r0; i < r1;) {
     int32_t nb = rec[i].x;
     int64_t j;
@@ -339,18 +347,22 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
     i = j;
     if (lt0(c)) continue;
     // dv as the reference forms it: d = p2[hi] - p2[lo], negated for the higher endpoint
-    double du, dw;
-    if (v < nb) {
-      du = dsub(p2[2 * nb], p2u);
-      dw = dsub(p2[2 * nb + 1], p2v);
-    } else {
-      du = dneg(dsub(p2u, p2[2 * nb]));
-      dw = dneg(dsub(p2v, p2[2 * nb + 1]));
+    double du = 0.0, dw = 0.0, mc = 0.0;
+    if (MIXB) {
+      if (v < nb) {
+        du = dsub(p2[2 * nb], p2u);
+        dw = dsub(p2[2 * nb + 1], p2v);
+      } else {
+        du = dneg(dsub(p2u, p2[2 * nb]));
+        dw = dneg(dsub(p2v, p2[2 * nb + 1]));
+      }
+      mc = dmul(mix_b, c);
     }
-    double mc = dmul(mix_b, c);
     if (!pinned[nb]) {
-      bu = dadd(bu, dmul(mc, du));
-      bv = dadd(bv, dmul(mc, dw));
+      if (MIXB) {
+        bu = dadd(bu, dmul(mc, du));
+        bv = dadd(bv, dmul(mc, dw));
+      }
       if (ne0(c)) {
         if (!diag_done && nb > v) {
           put((int32_t)row, dg);
@@ -358,9 +370,12 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
         }
         put((int32_t)row_of[nb], dneg(c));
       }
-    } else {
+    } else if (MIXB) {
       bu = dadd(bu, dadd(dmul(mc, du), dmul(c, pin_uv[2 * nb])));
       bv = dadd(bv, dadd(dmul(mc, dw), dmul(c, pin_uv[2 * nb + 1])));
+    } else {
+      bu = dadd(bu, dmul(c, pin_uv[2 * nb]));
+      bv = dadd(bv, dmul(c, pin_uv[2 * nb + 1]));
     }
   }
   if (!diag_done) put((int32_t)row, dg);
@@ -500,6 +515,7 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   RUV_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   int32_t* tri_g = ws.get<int32_t>("asm.tri_g", 3 * NT);
   double* cot = ws.get<double>("asm.cot", 3 * NT);
+  double* sq = ws.get<double>("asm.sq", 3 * NT);
   bt.tri_g = tri_g;
   bt.cot = cot;
   // triangles [0, split) first; with a split upload the rest of the triangles and positions
@@ -515,7 +531,7 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
     k_globalize<<<div_up(t1 - t0, B), B, 0, s>>>(bt.tris, bt.tri_off, bt.vert_off, NC, t0, t1, tri_g, bad);
     count_launches(1);
     RUV_LAUNCH_CHECK();
-    k_corner_cot<<<div_up(t1 - t0, B), B, 0, s>>>(bt.p3, tri_g, t0, t1, cot);
+    k_corner_cot<<<div_up(t1 - t0, B), B, 0, s>>>(bt.p3, tri_g, t0, t1, cot, sq);
     count_launches(1);
     RUV_LAUNCH_CHECK();
   }
@@ -571,7 +587,7 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   int32_t* row_len = ws.get<int32_t>("asm.row_len", NR);
   sys.diag = ws.get<double>("sys.diag", NR);  // written by the counting pass, read by the fill
   if (NV > 0) {
-    k_rows<0><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, bt.p3, bt.p2, bt.pin_uv, mix_b,
+    k_rows<0, false><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, sq, bt.p3, bt.p2, bt.pin_uv, mix_b,
                                              row_len, nullptr, nullptr, nullptr, nullptr, sys.diag, nullptr, nullptr,
                                              coef, nullptr, nullptr);
     count_launches(1);
@@ -602,9 +618,14 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   count_launches(1);
   RUV_LAUNCH_CHECK();
   if (NV > 0) {
-    k_rows<1><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, bt.p3, bt.p2, bt.pin_uv, mix_b,
-                                             nullptr, rp64, sys.cols, sys.vals, sys.vals32, sys.diag, sys.b,
-                                             bt.row_vert, coef, sys.vals_lo, sys.rsum);
+    if (mix_b != 0.0)
+      k_rows<1, true><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, sq, bt.p3, bt.p2,
+                                                      bt.pin_uv, mix_b, nullptr, rp64, sys.cols, sys.vals, sys.vals32,
+                                                      sys.diag, sys.b, bt.row_vert, coef, sys.vals_lo, sys.rsum);
+    else
+      k_rows<1, false><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, sq, bt.p3, bt.p2,
+                                                       bt.pin_uv, mix_b, nullptr, rp64, sys.cols, sys.vals, sys.vals32,
+                                                       sys.diag, sys.b, bt.row_vert, coef, sys.vals_lo, sys.rsum);
     count_launches(1);
   }
   RUV_LAUNCH_CHECK();

@@ -1363,9 +1363,11 @@ Tiles upload_tiles(Ctx& ctx, const DevSystem& sys, const std::string& tag) {
   }
   RUV_CUDA(cudaMemcpyAsync(d_ctile, TT.chart_tile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
   Tiles T{d_tab, d_chart, d_ctile, NTL};
-  // the bulk-copy SpMV: its staging size from the largest tile (RUV_SPMV_TMA=0: not used)
+  // the bulk-copy SpMV (when the context chose it, or RUV_SPMV_TMA=1 / =0 says so): its
+  // staging size from the largest tile
   const char* te = std::getenv("RUV_SPMV_TMA");
-  if (NTL > 0 && sys.row_ptr && !(te && te[0] == '0')) {
+  const bool tma = te ? te[0] == '1' : ctx.spmv_tma == 1;
+  if (NTL > 0 && sys.row_ptr && tma) {
     unsigned long long* mx = ctx.ws.get<unsigned long long>(tag + ".tmax", 2);
     int* err = ctx.ws.get<int>(tag + ".terr", 1);
     RUV_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), s));
@@ -1600,36 +1602,43 @@ double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers,
 }
 
 // Autotuner: time the batched SpMV for every instantiated (lanes per row, rows in flight)
-// shape and tile height on the assembled operator, each with the update, dots and direction
-// kernels of a CG iteration over the same tiles (the tile height sets their grid too); keep
-// the fastest in the context.
+// shape, tile height and SpMV form (CSR-vector or bulk-copy staged) on the assembled operator,
+// each with the update, dots and direction kernels of a CG iteration over the same tiles (the
+// tile height sets their grid too); keep the fastest in the context.
 TuneResult autotune_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps) {
   narrow_columns(ctx, sys);
-  TuneResult best{0, 0, 0, 1e30};
+  TuneResult best{0, 0, 0, 0, 1e30};
   const int tiles[] = {128, 256, 512, 1024};
   const Shape shapes[] = {
 #define RUV_SH(L, UU) Shape{L, UU},
       RUV_SHAPES(RUV_SH)
 #undef RUV_SH
   };
-  const int saved_tile = ctx.tile_rows;
+  const int saved_tile = ctx.tile_rows, saved_tma = ctx.spmv_tma;
+  // the bulk-copy kernel exists for the mixed solver's two-column SpMV only
+  const int n_tma = mixed && sys.nrhs == 2 ? 2 : 1;
   for (int tr : tiles) {
     ctx.tile_rows = tr;
-    Tiles T = upload_tiles(ctx, sys, "tune");
-    if (T.n == 0) break;
-    for (const Shape& sh : shapes) {
-      double ms = sys.nrhs == 2 ? (mixed ? dispatch_time<float, 2>(sh, ctx, sys, T, reps, 2, true)
-                                         : dispatch_time<double, 2>(sh, ctx, sys, T, reps, 2, true))
-                                : dispatch_time<double, 1>(sh, ctx, sys, T, reps, 2, true);
-      if (ms < best.ms) best = TuneResult{sh.lpr, sh.unroll, tr, ms};
+    for (int tma = 0; tma < n_tma; ++tma) {
+      ctx.spmv_tma = tma;
+      Tiles T = upload_tiles(ctx, sys, "tune");
+      if (T.n == 0) break;
+      for (const Shape& sh : shapes) {
+        double ms = sys.nrhs == 2 ? (mixed ? dispatch_time<float, 2>(sh, ctx, sys, T, reps, 2, true)
+                                           : dispatch_time<double, 2>(sh, ctx, sys, T, reps, 2, true))
+                                  : dispatch_time<double, 1>(sh, ctx, sys, T, reps, 2, true);
+        if (ms < best.ms) best = TuneResult{sh.lpr, sh.unroll, tr, tma, ms};
+      }
     }
   }
   if (best.lpr > 0) {
     ctx.lanes_per_row = best.lpr;
     ctx.unroll = best.unroll;
     ctx.tile_rows = best.tile_rows;
+    ctx.spmv_tma = best.tma;
   } else {
     ctx.tile_rows = saved_tile;
+    ctx.spmv_tma = saved_tma;
   }
   return best;
 }

@@ -187,6 +187,9 @@ struct Ctx {
   int lanes_per_row = 0;   // SpMV sub-warp width (0 = from the row-length profile)
   int unroll = 0;          // SpMV rows in flight per sub-warp (0 = from the shape)
   int tile_rows = 512;     // rows per CTA tile (the autotuner's pick on the height fields)
+  // the bulk-copy SpMV (k_spmv_tma): 0 off (the default: on the 4096-disk step the CSR-vector
+  // kernel's iteration ran faster), 1 on; the autotuner chooses it, RUV_SPMV_TMA=0/1 overrides
+  int spmv_tma = 0;
   // the batch resident on the device (ruv_lscm_upload)
   DevBatch resident;
   bool have_batch = false;
@@ -200,7 +203,7 @@ double bench_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps, int n_buffers,
                   double* stream_bytes);
 
 struct TuneResult {
-  int lpr, unroll, tile_rows;
+  int lpr, unroll, tile_rows, tma;
   double ms;
 };
 TuneResult autotune_spmv(Ctx& ctx, DevSystem& sys, bool mixed, int reps);

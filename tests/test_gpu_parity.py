@@ -8,6 +8,8 @@ Bars (from the reference and the workload definitions):
 * Driver iterations and err_accum as the reference driver computes them.
 * GpuSolver::cg_solve known answers (gpu/src/solver.rs:767-1109).
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -55,6 +57,27 @@ def test_cube_fp64_matches_cpu_lu(ctx):
         assert O.uv_error(res[c].uv, ref["uv"]) <= FP64_TOL
         assert res[c].iters == ref["iters"] == 2
         assert abs(res[c].err_accum - ref["err_accum"]) <= 1e-9 * abs(ref["err_accum"])
+
+
+@pytest.mark.parametrize("angle_mix", [0.0, 0.5])
+def test_angle_mix_matches_cpu_lu(ctx, angle_mix):
+    """#AngleDistanceMix below 1 (mix_b = 1 - angle_mix > 0: the pull towards the frame
+    positions enters the right-hand side, lscm.rs:630-638): the same CSR systems and
+    right-hand sides bit for bit, and the UVs of the FP64 solve within 1e-10 of the reference
+    LU with its damped driver (the default angle_mix = 1 skips those zero terms)."""
+    for p, f in (O.cube(6), O.uv_sphere(48, 24)):
+        P = O.Pipeline(p, f, angle_mix=angle_mix, lu_limit=6000)
+        C = R.prepare_mesh(p, f)
+        assert C.n_charts == P.n_charts
+        res = R.unfold_charts(ctx, C, R.UnfoldOptions(precision=R.Precision.FP64, precond=R.Precond.JACOBI,
+                                                      angle_mix=angle_mix))
+        for c in range(P.n_charts):
+            _check_system(ctx, P, c)
+            ref = P.chart(c)
+            assert res[c].status == R.Status.OK
+            if "uv" in ref:
+                assert O.uv_error(res[c].uv, ref["uv"]) <= FP64_TOL
+                assert res[c].iters == ref["iters"]
 
 
 @pytest.mark.parametrize("precision", [R.Precision.FP64, R.Precision.MIXED])
@@ -275,8 +298,8 @@ def test_group_graph_bitwise(monkeypatch):
 @pytest.mark.parametrize("case", ["disks_16bit_columns", "field_row_relative_columns", "field_32bit_columns"])
 def test_bulk_copy_spmv_bitwise(monkeypatch, case):
     """The SpMV that stages each tile's row pointers, values and columns into shared memory
-    by bulk asynchronous copies (the default) runs the same row loop as the CSR-vector kernel
-    reading them from global memory (RUV_SPMV_TMA=0): bitwise the same UVs and iterations,
+    by bulk asynchronous copies (RUV_SPMV_TMA=1) runs the same row loop as the CSR-vector
+    kernel reading them from global memory (RUV_SPMV_TMA=0): bitwise the same UVs and iterations,
     with the chart-relative 16-bit column stream (charts of <= 65536 rows), the row-relative
     one (a 258k-row chart) and 32-bit columns (the same chart, RUV_NARROW_COLS=chart)."""
     if case == "disks_16bit_columns":
@@ -292,8 +315,9 @@ def test_bulk_copy_spmv_bitwise(monkeypatch, case):
         opts = R.UnfoldOptions(precond=pc, precision=R.Precision.MIXED)
         monkeypatch.setenv("RUV_SPMV_TMA", "0")
         plain = R.unfold_charts(ctx, C, opts)
-        monkeypatch.delenv("RUV_SPMV_TMA", raising=False)
+        monkeypatch.setenv("RUV_SPMV_TMA", "1")
         staged = R.unfold_charts(ctx, C, opts)
+        monkeypatch.delenv("RUV_SPMV_TMA", raising=False)
         for a, b in zip(plain, staged):
             assert a.status == b.status == R.Status.OK
             assert a.cg_iters == b.cg_iters
@@ -328,12 +352,36 @@ def test_bulk_copy_spmv_wait_is_bounded(monkeypatch):
     C = R.prepare_patches(vo, to, p3, tr)
     nv = int(C.i64("chart.vert_off")[-1])
     ctx = R.Context(0)
+    monkeypatch.setenv("RUV_SPMV_TMA", "1")
     monkeypatch.setenv("RUV_SPIN_LIMIT", "1")
     _, _, st = R.solve_batch(ctx, C.batch(), R.UnfoldOptions(precond=R.Precond.JACOBI), nv, check=False)
     assert st in (R.Status.OK, R.Status.TIMEOUT), R.Status(st).name
     monkeypatch.delenv("RUV_SPIN_LIMIT")
     _, stats, st = R.solve_batch(ctx, C.batch(), R.UnfoldOptions(precond=R.Precond.JACOBI), nv)
     assert st == R.Status.OK
+
+
+@pytest.mark.parametrize("kernel", ["1", "0"])
+def test_pinned_inputs_bitwise(monkeypatch, kernel):
+    """The one-call entry with its inputs in page-locked host memory (copied by the SMs over
+    the buffers' device mapping; RUV_H2D_KERNEL=0: by cudaMemcpyAsync) gives bitwise the UVs
+    and statistics of the same batch from pageable memory, split upload included."""
+    monkeypatch.setenv("RUV_H2D_KERNEL", kernel)
+    vo, to, p3, tr = W.disks(12, t_min=200, t_max=20000, seed=67)
+    C = R.prepare_patches(vo, to, p3, tr)
+    nv = int(C.i64("chart.vert_off")[-1])
+    ctx = R.Context(0)
+    opts = R.UnfoldOptions(precond=R.Precond.AMG_SA, precision=R.Precision.MIXED)
+    uv_a, st_a, s_a = R.solve_batch(ctx, C.batch(), opts, nv)
+    pb, keep = R.pinned_batch(ctx, C)
+    out = R.pinned_empty(ctx, (nv, 2), np.float64)
+    stats = (R.RuvChartStat * max(pb.n_charts, 1))()
+    L = R.lib()
+    ctx.check(L.ruv_lscm_solve_batch(ctx.h, ctypes.byref(pb), ctypes.byref(opts.to_c()),
+                                     out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), stats), "pinned solve")
+    assert s_a == R.Status.OK
+    assert np.array_equal(uv_a, out)
+    assert [s.cg_iters for s in st_a] == [stats[c].cg_iters for c in range(pb.n_charts)]
 
 
 def test_staged_smoothers_bitwise(monkeypatch):
