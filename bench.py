@@ -584,6 +584,8 @@ def compare_preconds(ctx, args, stats, names):
         it = [stats[i].cg_iters for i in range(len(stats))]
         out[name] = {"status": R.Status(st).name, "ms": round(sum(t[:3]), 3), "pcg_ms": round(t[1], 3),
                      "setup_ms": round(t[3], 3), "cg_iters_max": int(max(it)),
+                     # the iterations of the slowest chart set the batch's pace
+                     "ms_per_iteration": round((t[1] - t[3]) / max(max(it), 1), 4),
                      "charts_not_ok": int(sum(1 for i in range(len(stats)) if stats[i].status != 0))}
     return out
 

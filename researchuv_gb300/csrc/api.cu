@@ -64,8 +64,9 @@ ruv_status guarded(ruv_ctx* ctx, F&& body) {
   }
 }
 
-// Host-to-device copy through the SMs: a page-locked, mapped host buffer read over its device
-// mapping, 16 bytes per load with four loads in flight per thread (head and tail bytewise).
+// Copy through the SMs between device memory and a page-locked, mapped host buffer (read or
+// written over its device mapping), 16 bytes per access with four loads in flight per thread
+// (head and tail bytewise).
 __global__ void k_h2d(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, size_t head,
                       size_t n16, size_t tail) {
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (size_t)gridDim.x * blockDim.x;
@@ -116,6 +117,40 @@ void h2d(Ctx& c, void* dev, const void* host, size_t bytes, cudaStream_t st) {
   RUV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
   const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 4, div_up((int64_t)n16, 256)));
   k_h2d<<<grid, 256, 0, st>>>(static_cast<const unsigned char*>(src), static_cast<unsigned char*>(dev), head, n16,
+                              tail);
+  count_launches(1);
+  RUV_LAUNCH_CHECK();
+}
+
+// n bytes device -> host on stream st: the same choice as h2d (k_h2d writing through the
+// host buffer's device mapping where it is page-locked and mapped, else cudaMemcpyAsync).
+void d2h(Ctx& c, void* host, const void* dev, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return;
+  static const bool off = [] {
+    const char* e = std::getenv("RUV_H2D_KERNEL");
+    return e && e[0] == '0';
+  }();
+  cudaPointerAttributes a{};
+  void* dst = nullptr;
+  if (!off) {
+    if (cudaPointerGetAttributes(&a, host) == cudaSuccess) {
+      if (a.type == cudaMemoryTypeHost && a.devicePointer) dst = a.devicePointer;
+    } else {
+      cudaGetLastError();
+    }
+  }
+  const uintptr_t sa = (uintptr_t)dev, da = (uintptr_t)dst;
+  if (!dst || (sa & 15) != (da & 15)) {
+    RUV_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, st));
+    return;
+  }
+  const size_t head = std::min<size_t>(bytes, (16 - (sa & 15)) & 15);
+  const size_t n16 = (bytes - head) / 16, tail = bytes - head - 16 * n16;
+  int dev_id = 0, sms = 0;
+  RUV_CUDA(cudaGetDevice(&dev_id));
+  RUV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 4, div_up((int64_t)n16, 256)));
+  k_h2d<<<grid, 256, 0, st>>>(static_cast<const unsigned char*>(dev), static_cast<unsigned char*>(dst), head, n16,
                               tail);
   count_launches(1);
   RUV_LAUNCH_CHECK();
@@ -544,7 +579,7 @@ ruv_status ruv_lscm_download_uv(ruv_ctx* ctx, double* uv_out) {
     const int64_t NV = c.resident.n_verts;
     if (NV > 0 && !uv_out) return fail(ctx, RUV_ERR_BAD_INPUT, "null uv_out");
     double* uv = c.ws.get<double>("lscm.uv", 2 * NV);
-    if (NV > 0) RUV_CUDA(cudaMemcpyAsync(uv_out, uv, sizeof(double) * 2 * NV, cudaMemcpyDeviceToHost, c.stream));
+    if (NV > 0) d2h(c, uv_out, uv, sizeof(double) * 2 * NV, c.stream);
     RUV_CUDA(cudaStreamSynchronize(c.stream));
     return RUV_OK;
   });
