@@ -567,8 +567,51 @@ __global__ void k_sort_rows(int64_t n, const int64_t* __restrict__ off, const in
 //   MODE 2 (one evaluation): writes the row to a staging area of H/2 entries per row, or, if
 //          it has more distinct keys, lists it (sn = -1) for the large-table kernel;
 //   MODE 0 / 1: counts / writes at off[row] (the large-table kernel, rows from the list).
+//
+// Arithmetic: every operand and sum is a double-float pair (hi, lo: FP32 values whose sum
+// carries about 48 significant bits), formed by error-free FP32 transformations on the FMA
+// pipe.  GB300 issues FP64 at a small fraction of its FP32 rate, and with FP64 products and
+// sums these kernels were bound by the FP64 pipe (78% busy); the products' relative error
+// stays near 1e-14, far below what the FP32 V-cycle can see.  Operands come through loaders:
+// FP32 values (P, R), (hi, lo) array pairs (a level's operator) or pair arrays (W).
 struct KeyId {
   __device__ __forceinline__ int32_t operator()(int32_t k) const { return k; }
+};
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  const float s = a.x + b.x;
+  const float bb = s - a.x;
+  const float err = (a.x - (s - bb)) + (b.x - bb);
+  const float lo = err + a.y + b.y;
+  const float h = s + lo;
+  return make_float2(h, lo - (h - s));
+}
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float h = p + e;
+  return make_float2(h, e - (h - p));
+}
+struct LdOne {  // no values: every entry 1
+  static constexpr bool kHas = false;
+  __device__ __forceinline__ float2 operator()(int64_t) const { return make_float2(1.0f, 0.0f); }
+};
+struct LdF {  // FP32 values
+  const float* v;
+  static constexpr bool kHas = true;
+  __device__ __forceinline__ float2 operator()(int64_t e) const { return make_float2(v[e], 0.0f); }
+};
+struct LdHL {  // a level operator: hi and lo halves in two arrays
+  const float* h;
+  const float* l;
+  static constexpr bool kHas = true;
+  __device__ __forceinline__ float2 operator()(int64_t e) const { return make_float2(h[e], l[e]); }
+};
+struct LdDF {  // pairs
+  const float2* v;
+  static constexpr bool kHas = true;
+  __device__ __forceinline__ float2 operator()(int64_t e) const { return v[e]; }
 };
 struct KeyAgg {
   const int32_t* agg;
@@ -578,29 +621,29 @@ struct KeyAgg {
 template <int G, int H>
 struct GalSmem {
   static constexpr int HS = H / 2;  // distinct keys a row may hold
-  static constexpr size_t bytes = sizeof(double) * (H + G) + sizeof(int32_t) * (H + 2 * HS);
+  static constexpr size_t bytes = sizeof(float2) * (H + G) + sizeof(int32_t) * (H + 2 * HS);
 };
 
 struct GalOut {
   int32_t* cnt;         // distinct keys per row (MODE 0, 2)
   int32_t* sn;          // MODE 2: staged count, or -1 when listed
   int32_t* st_key;      // MODE 2: staging, H/2 entries per row
-  double* st_val;
+  float2* st_val;
   const int64_t* off;   // MODE 1: output offsets
   int32_t* oc;
-  double* ov;
+  float2* ov;
   float* adinv;         // DIAG
   int32_t* next;        // MODE 2: listed rows
   int32_t* next_n;
   int* overflow;        // MODE 0 / 1: a row above the large table's capacity
 };
 
-template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
+template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OL, class IP, class IL, class KeyF>
 __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const int32_t* __restrict__ list,
                                                          const uint8_t* __restrict__ active, const OP* __restrict__ o_ptr,
-                                                         const int32_t* __restrict__ o_idx, const OV* __restrict__ o_val,
+                                                         const int32_t* __restrict__ o_idx, OL o_val,
                                                          const IP* __restrict__ i_ptr, const int32_t* __restrict__ i_idx,
-                                                         const IV* __restrict__ i_val, KeyF keyf, GalOut out) {
+                                                         IL i_val, KeyF keyf, GalOut out) {
   using S = GalSmem<G, H>;
   constexpr int HS = S::HS;
   constexpr int SUB = 32 / G;
@@ -611,8 +654,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
   const unsigned smask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gb);
   const int sw = (threadIdx.x >> 5) * SUB + (lane / G);
   unsigned char* base = gal_smem + S::bytes * (size_t)sw;
-  double* tval = reinterpret_cast<double*>(base);
-  double* stage = tval + H;
+  float2* tval = reinterpret_cast<float2*>(base);
+  float2* stage = tval + H;
   int32_t* tkey = reinterpret_cast<int32_t*>(stage + G);
   int32_t* ckey = tkey + H;
   int32_t* cslot = ckey + HS;
@@ -621,7 +664,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
   auto clear_all = [&]() {
     for (int t = sl; t < H; t += G) {
       tkey[t] = -1;
-      tval[t] = 0.0;
+      tval[t] = make_float2(0.0f, 0.0f);
     }
     __syncwarp(smask);
   };
@@ -642,10 +685,10 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
       const int64_t q = q0 + sl;
       int64_t ib = 0;
       int len = 0;
-      double sc = 0.0;
+      float2 sc = make_float2(0.0f, 0.0f);
       if (q < oe) {
         const int32_t j = o_idx[q];
-        sc = o_val ? (double)o_val[q] : 1.0;
+        if (MODE != 0) sc = o_val(q);
         ib = (int64_t)i_ptr[j];
         len = (int)((int64_t)i_ptr[j + 1] - ib);
       }
@@ -666,17 +709,17 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
           if (xv <= pl) own += st;
         }
         own = min(own, G - 1);
-        const double sco = __shfl_sync(smask, sc, own, G);
+        const float2 sco = make_float2(__shfl_sync(smask, sc.x, own, G), __shfl_sync(smask, sc.y, own, G));
         const long long ibo = __shfl_sync(smask, (long long)ib, own, G);
         const int sto = __shfl_sync(smask, x - len, own, G);
         int32_t key = 0;
-        double v = 0.0;
+        float2 v = make_float2(0.0f, 0.0f);
         int slot = -1;
         bool fresh = false;
         if (valid) {
           const int64_t e = (int64_t)ibo + (pl - sto);
           key = keyf(i_idx[e]);
-          if (MODE != 0) v = sco * (double)i_val[e];
+          if (MODE != 0) v = df_mul(sco, i_val(e));
           unsigned h = ((uint32_t)key * 0x9E3779B1u) >> (32 - LOGH);
           for (int pr = 0; pr < H; ++pr) {
             const int32_t k = reinterpret_cast<volatile int32_t*>(tkey)[h];
@@ -713,8 +756,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
           __syncwarp(smask);
           const unsigned gm = __match_any_sync(smask, valid ? slot : -1);
           if (valid && (__ffs(gm) - 1) == lane) {
-            double s = tval[slot];
-            for (unsigned m = gm; m != 0u; m &= m - 1u) s += stage[(__ffs(m) - 1) - gb];
+            float2 s = tval[slot];
+            for (unsigned m = gm; m != 0u; m &= m - 1u) s = df_add(s, stage[(__ffs(m) - 1) - gb]);
             tval[slot] = s;
           }
         }
@@ -745,7 +788,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
     }
     // rank each key by counting smaller ones
     int32_t* dk;
-    double* dv;
+    float2* dv;
     if (MODE == 2) {
       dk = out.st_key + row * HS;
       dv = out.st_val + row * HS;
@@ -754,25 +797,25 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
       dv = out.ov + out.off[row];
     }
     bool has_d = false;
-    double dval = 0.0;
+    float dval = 0.0f;
     for (int c = sl; c < d; c += G) {
       const int32_t k = ckey[c];
       int rank = 0;
       for (int u = 0; u < d; ++u) rank += ckey[u] < k;
       const int slot = cslot[c];
-      const double val = tval[slot];
+      const float2 val = tval[slot];
       dk[rank] = k;
       dv[rank] = val;
       if (DIAG && k == (int32_t)row) {
         has_d = true;
-        dval = val;
+        dval = val.x;
       }
     }
     if (DIAG) {
       if (__ballot_sync(smask, has_d) == 0u) {
         if (sl == 0) out.adinv[row] = 0.0f;
       } else if (has_d) {
-        out.adinv[row] = dval > 0.0 ? (float)(1.0 / dval) : 0.0f;
+        out.adinv[row] = dval > 0.0f ? 1.0f / dval : 0.0f;  // (hi of a normalised pair: lo changes no FP32 bit)
       }
     }
     if (MODE == 2 && sl == 0) {  // (MODE 1 leaves the counts alone)
@@ -783,7 +826,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
     for (int c = sl; c < d; c += G) {
       const int slot = cslot[c];
       tkey[slot] = -1;
-      tval[slot] = 0.0;
+      tval[slot] = make_float2(0.0f, 0.0f);
     }
     __syncwarp(smask);
   }
@@ -792,8 +835,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const in
 // Staged rows to their place in the product (8 lanes per row); listed rows (sn < 0) are
 // written by the large-table kernel.
 __global__ void k_gal_copy(int64_t nrows, int hs, const int32_t* __restrict__ sn, const int32_t* __restrict__ st_key,
-                           const double* __restrict__ st_val, const int64_t* __restrict__ off, int32_t* __restrict__ oc,
-                           double* __restrict__ ov) {
+                           const float2* __restrict__ st_val, const int64_t* __restrict__ off, int32_t* __restrict__ oc,
+                           float2* __restrict__ ov) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t row = t >> 3;
   const int sl = (int)(t & 7);
@@ -811,10 +854,23 @@ __global__ void k_i64_i32(int64_t n, const int64_t* __restrict__ a, int32_t* __r
   if (i < n) b[i] = (int32_t)a[i];
 }
 
-__global__ void k_f64_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+// A coarse operator's pairs into its FP32 values (hi), their low halves and FP64 values.
+__global__ void k_df_unpack(int64_t n, const float2* __restrict__ v, float* __restrict__ hi, float* __restrict__ lo,
+                            double* __restrict__ v64) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = (float)a[i];
+  if (i >= n) return;
+  const float2 a = v[i];
+  hi[i] = a.x;
+  lo[i] = a.y;
+  v64[i] = (double)a.x + (double)a.y;
 }
+
+// lo = (float)(v - hi) for an operator whose FP32 values hi = (float)v are given
+__global__ void k_lo_half(int64_t n, const double* __restrict__ v, const float* __restrict__ hi, float* __restrict__ lo) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) lo[i] = (float)(v[i] - (double)hi[i]);
+}
+
 
 __global__ void k_f64_f32_inv(int64_t n, const double* __restrict__ d, float* __restrict__ inv) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1470,7 +1526,9 @@ struct AmgLevelDev {
   int32_t* row_chart = nullptr;
   int32_t *rp = nullptr, *cols = nullptr;
   float *vals = nullptr, *dinv = nullptr;
-  double* vals64 = nullptr;  // the operator in FP64 (the Galerkin products' input)
+  double* vals64 = nullptr;  // the operator in FP64 (the coarsest level's dense factors)
+  float* vals_lo = nullptr;  // (vals, vals_lo): the operator as double-float pairs (the Galerkin products' input)
+  float2* vdf = nullptr;     // a coarse level's pairs as its Galerkin product wrote them
   // transfer to the next level (rows of charts that continue below this level)
   int64_t* poff = nullptr;
   int32_t* pc = nullptr;
@@ -1539,7 +1597,7 @@ struct GalWork {
   int* ovf = nullptr;
   int32_t* sn = nullptr;
   int32_t* st_key = nullptr;
-  double* st_val = nullptr;
+  float2* st_val = nullptr;
   float* st_dinv = nullptr;
   int hs = 0;     // staged entries per row
   int lanes = 0;  // lanes per row of the first pass
@@ -1550,13 +1608,13 @@ struct GalWork {
 constexpr int kGalWarps = 8;
 constexpr int kGalBigH = 8192;  // large table: 4096 distinct keys, 128 KB of shared memory
 
-template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
+template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OL, class IP, class IL, class KeyF>
 void launch_gal(cudaStream_t s, int64_t nrows, const int32_t* list, const uint8_t* active, const OP* o_ptr,
-                const int32_t* o_idx, const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, KeyF keyf,
+                const int32_t* o_idx, OL o_val, const IP* i_ptr, const int32_t* i_idx, IL i_val, KeyF keyf,
                 const GalOut& out) {
   constexpr int SUB = 32 / G;
   constexpr size_t smem = GalSmem<G, H>::bytes * WARPS * SUB;
-  auto k = k_gal_hash<MODE, G, H, WARPS, DIAG, OP, OV, IP, IV, KeyF>;
+  auto k = k_gal_hash<MODE, G, H, WARPS, DIAG, OP, OL, IP, IL, KeyF>;
   if (smem > 48 * 1024) RUV_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k<<<div_up(nrows, (int64_t)WARPS * SUB), 32 * WARPS, smem, s>>>(nrows, list, active, o_ptr, o_idx, o_val, i_ptr, i_idx,
                                                                  i_val, keyf, out);
@@ -1574,9 +1632,9 @@ inline double env_or(const char* name, double dflt) {
 // for short rows).  Every row is evaluated once into the staging area; rows with more distinct
 // keys than the table holds are counted by the large-table kernel.  cnt holds every row's
 // count on return.
-template <bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
+template <bool DIAG, class OP, class OL, class IP, class IL, class KeyF>
 void gal_count(Ctx& ctx, GalWork& g, int64_t nrows, double avg, const uint8_t* active, const OP* o_ptr,
-               const int32_t* o_idx, const OV* o_val, const IP* i_ptr, const int32_t* i_idx, const IV* i_val, KeyF keyf,
+               const int32_t* o_idx, OL o_val, const IP* i_ptr, const int32_t* i_idx, IL i_val, KeyF keyf,
                int32_t* cnt) {
   cudaStream_t s = ctx.stream;
   g.h1 = 0;
@@ -1590,7 +1648,7 @@ void gal_count(Ctx& ctx, GalWork& g, int64_t nrows, double avg, const uint8_t* a
   g.hs = g.lanes == 8 ? GalSmem<8, 64>::HS : g.lanes == 16 ? GalSmem<16, 128>::HS : GalSmem<32, 256>::HS;
   g.sn = ctx.ws.get<int32_t>("amg.gal_sn", nrows);
   g.st_key = ctx.ws.get<int32_t>("amg.gal_key", nrows * g.hs);
-  g.st_val = ctx.ws.get<double>("amg.gal_val", nrows * g.hs);
+  g.st_val = ctx.ws.get<float2>("amg.gal_val", nrows * g.hs);
   g.st_dinv = DIAG ? ctx.ws.get<float>("amg.gal_dinv", nrows) : nullptr;
   RUV_CUDA(cudaMemsetAsync(g.list_n, 0, sizeof(int32_t), s));
   GalOut out{cnt, g.sn, g.st_key, g.st_val, nullptr, nullptr, nullptr, g.st_dinv, g.list, g.list_n, g.ovf};
@@ -1610,10 +1668,10 @@ void gal_count(Ctx& ctx, GalWork& g, int64_t nrows, double avg, const uint8_t* a
 
 // Second half: staged rows copied to their offsets, listed rows evaluated again by the
 // large-table kernel straight into place.
-template <bool DIAG, class OP, class OV, class IP, class IV, class KeyF>
-void gal_fill(Ctx& ctx, GalWork& g, int64_t nrows, const OP* o_ptr, const int32_t* o_idx, const OV* o_val,
-              const IP* i_ptr, const int32_t* i_idx, const IV* i_val, KeyF keyf, const int64_t* off, int32_t* oc,
-              double* ov, float* adinv) {
+template <bool DIAG, class OP, class OL, class IP, class IL, class KeyF>
+void gal_fill(Ctx& ctx, GalWork& g, int64_t nrows, const OP* o_ptr, const int32_t* o_idx, OL o_val,
+              const IP* i_ptr, const int32_t* i_idx, IL i_val, KeyF keyf, const int64_t* off, int32_t* oc,
+              float2* ov, float* adinv) {
   cudaStream_t s = ctx.stream;
   if (nrows <= 0) return;
   k_gal_copy<<<div_up(nrows * 8, 256), 256, 0, s>>>(nrows, g.hs, g.sn, g.st_key, g.st_val, off, oc, ov);
@@ -1725,6 +1783,12 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     L0.cols = sys.cols;
     L0.vals = sys.vals32;
     L0.vals64 = sys.vals;
+    L0.vals_lo = sys.vals_lo;
+    if (!L0.vals_lo && L0.nnz > 0) {  // (the assembly formed no split: form it here)
+      L0.vals_lo = ctx.ws.get<float>("amg.l0.lo", L0.nnz);
+      k_lo_half<<<div_up(L0.nnz, B), B, 0, s>>>(L0.nnz, sys.vals, sys.vals32, L0.vals_lo);
+      count_launches(1);
+    }
     L0.c16 = sys.cols16;
     L0.cbase = sys.cbase;
     L0.rowrel = sys.rowrel16;
@@ -1902,13 +1966,15 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
       C.cols = ctx.ws.get<int32_t>(ntag + ".cols", AN);
       C.vals = ctx.ws.get<float>(ntag + ".vals", AN);
       C.vals64 = ctx.ws.get<double>(ntag + ".vals64", AN);
+      C.vals_lo = ctx.ws.get<float>(ntag + ".lo", AN);
+      C.vdf = ctx.ws.get<float2>(ntag + ".vdf", AN);
       C.dinv = ctx.ws.get<float>(ntag + ".dinv", NA);
       C.nnz = AN;
     };
     auto finish_coarse = [&]() {
       if (NA > 0) {
         k_i64_i32<<<div_up(NA + 1, B), B, 0, s>>>(NA + 1, aoff, C.rp);
-        if (C.nnz > 0) k_f64_f32<<<div_up(C.nnz, B), B, 0, s>>>(C.nnz, C.vals64, C.vals);
+        if (C.nnz > 0) k_df_unpack<<<div_up(C.nnz, B), B, 0, s>>>(C.nnz, C.vdf, C.vals, C.vals_lo, C.vals64);
         count_launches(2);
       }
     };
@@ -1917,26 +1983,27 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
     if (!sm) {
       // ---- tentative prolongator: A_c = R A P straight from A (keys through agg)
       const double avg = mean(PN, NA) * mean(L.nnz, L.n);
-      gal_count<true>(ctx, gw, NA, avg, nullptr, L.roff, L.rc, (const float*)nullptr, L.rp, L.cols, L.vals64,
+      gal_count<true>(ctx, gw, NA, avg, nullptr, L.roff, L.rc, LdOne{}, L.rp, L.cols, LdHL{L.vals, L.vals_lo},
                       KeyAgg{agg}, acnt);
       alloc_coarse(offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao"));
-      gal_fill<true>(ctx, gw, NA, L.roff, L.rc, (const float*)nullptr, L.rp, L.cols, L.vals64, KeyAgg{agg}, aoff, C.cols,
-                     C.vals64, C.dinv);
+      gal_fill<true>(ctx, gw, NA, L.roff, L.rc, LdOne{}, L.rp, L.cols, LdHL{L.vals, L.vals_lo}, KeyAgg{agg}, aoff,
+                     C.cols, C.vdf, C.dinv);
       finish_coarse();
     } else {
       // ---- smoothed prolongator: W = A P, then A_c = R W
       int32_t* wcnt = ctx.ws.get<int32_t>(tag + ".wcnt", L.n);
       int64_t* woff = ctx.ws.get<int64_t>(tag + ".woff", L.n + 1);
-      gal_count<false>(ctx, gw, L.n, mean(L.nnz, L.n) * mean(PN, L.n), active, L.rp, L.cols, L.vals64, L.poff, L.pc,
-                       L.pv, KeyId{}, wcnt);
+      gal_count<false>(ctx, gw, L.n, mean(L.nnz, L.n) * mean(PN, L.n), active, L.rp, L.cols, LdHL{L.vals, L.vals_lo},
+                       L.poff, L.pc, LdF{L.pv}, KeyId{}, wcnt);
       WN = offsets_from_counts(ctx, wcnt, L.n, woff, tag + ".wo");
       int32_t* wc = ctx.ws.get<int32_t>(tag + ".wc", WN);
-      double* wv = ctx.ws.get<double>(tag + ".wv", WN);
-      gal_fill<false>(ctx, gw, L.n, L.rp, L.cols, L.vals64, L.poff, L.pc, L.pv, KeyId{}, woff, wc, wv, nullptr);
-      gal_count<true>(ctx, gw, NA, mean(PN, NA) * mean(WN, L.n), nullptr, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{},
-                      acnt);
+      float2* wv = ctx.ws.get<float2>(tag + ".wv", WN);
+      gal_fill<false>(ctx, gw, L.n, L.rp, L.cols, LdHL{L.vals, L.vals_lo}, L.poff, L.pc, LdF{L.pv}, KeyId{}, woff, wc,
+                      wv, nullptr);
+      gal_count<true>(ctx, gw, NA, mean(PN, NA) * mean(WN, L.n), nullptr, L.roff, L.rc, LdF{L.rv}, woff, wc, LdDF{wv},
+                      KeyId{}, acnt);
       alloc_coarse(offsets_from_counts(ctx, acnt, NA, aoff, ntag + ".ao"));
-      gal_fill<true>(ctx, gw, NA, L.roff, L.rc, L.rv, woff, wc, wv, KeyId{}, aoff, C.cols, C.vals64, C.dinv);
+      gal_fill<true>(ctx, gw, NA, L.roff, L.rc, LdF{L.rv}, woff, wc, LdDF{wv}, KeyId{}, aoff, C.cols, C.vdf, C.dinv);
       finish_coarse();
     }
     L.n_next = NA;

@@ -85,6 +85,20 @@ __global__ void k_h2d(const unsigned char* __restrict__ src, unsigned char* __re
   if (tid < tail) dst[head + 16 * n16 + tid] = src[head + 16 * n16 + tid];
 }
 
+// The copy kernel's grid: RUV_H2D_CTAS (default 1) CTAs of 256 threads per SM -- four 16-byte
+// loads in flight per thread already cover the host link's latency, and the fewer SMs the
+// copy holds the more the assembly kernels it overlaps keep.
+unsigned h2d_grid(size_t n16) {
+  static const int per_sm = [] {
+    const char* e = std::getenv("RUV_H2D_CTAS");
+    return e ? std::max(1, std::atoi(e)) : 1;
+  }();
+  int dev_id = 0, sms = 0;
+  RUV_CUDA(cudaGetDevice(&dev_id));
+  RUV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, div_up((int64_t)n16, 256)));
+}
+
 // n bytes host -> device on stream st.  Where the host buffer is page-locked and mapped (and
 // both ends share their offset from a 16-byte boundary) the copy is k_h2d; otherwise
 // cudaMemcpyAsync.  On GB300 hosts copy-engine transfers of pinned memory ran at 211 GB/s but
@@ -112,10 +126,7 @@ void h2d(Ctx& c, void* dev, const void* host, size_t bytes, cudaStream_t st) {
   }
   const size_t head = std::min<size_t>(bytes, (16 - (sa & 15)) & 15);
   const size_t n16 = (bytes - head) / 16, tail = bytes - head - 16 * n16;
-  int dev_id = 0, sms = 0;
-  RUV_CUDA(cudaGetDevice(&dev_id));
-  RUV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
-  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 4, div_up((int64_t)n16, 256)));
+  const unsigned grid = h2d_grid(n16);
   k_h2d<<<grid, 256, 0, st>>>(static_cast<const unsigned char*>(src), static_cast<unsigned char*>(dev), head, n16,
                               tail);
   count_launches(1);
@@ -146,10 +157,7 @@ void d2h(Ctx& c, void* host, const void* dev, size_t bytes, cudaStream_t st) {
   }
   const size_t head = std::min<size_t>(bytes, (16 - (sa & 15)) & 15);
   const size_t n16 = (bytes - head) / 16, tail = bytes - head - 16 * n16;
-  int dev_id = 0, sms = 0;
-  RUV_CUDA(cudaGetDevice(&dev_id));
-  RUV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
-  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 4, div_up((int64_t)n16, 256)));
+  const unsigned grid = h2d_grid(n16);
   k_h2d<<<grid, 256, 0, st>>>(static_cast<const unsigned char*>(dev), static_cast<unsigned char*>(dst), head, n16,
                               tail);
   count_launches(1);
