@@ -641,7 +641,7 @@ def _fd_worker(args):
 
     p3, tris, pinned, pin_uv, lam, target, picks = args
     return O.fd_gradient(p3, tris, pinned, pin_uv, lam, target, picks, reuse_base=True, smooth_steps=FD_STEPS,
-                         edge_scale=FD_EDGE_SCALE, refine=FD_REFINE, richardson=True)
+                         edge_scale=FD_EDGE_SCALE, refine=FD_REFINE)
 
 
 def fd_parallel(p3, tris, pinned, pin_uv, lam, target, picks, workers):
@@ -757,8 +757,7 @@ def run_adjoint(args, rank, world, local, pg):
             "h": "per pick, the largest of 1e-6, 1e-7, 1e-8, 1e-9 at which neither +h nor -h moves a clamp of "
                  "the assembly around the vertex (a corner cotangent's clamp at 0, an edge weight's drop "
                  "threshold): the loss is piecewise smooth, and a quotient across a kink averages two one-sided "
-                 "derivatives; each quotient Richardson-combined with its h/2 quotient, (4 D(h/2) - D(h)) / 3, "
-                 "which cancels the h^2 truncation term (next to the poles edges are ~2e-5 long)",
+                 "derivatives",
             "h_counts": {"1e-6": int((fd_h == 1e-6).sum()), "below 1e-6": int((fd_h < 1e-6).sum())},
             "h_min": float(np.nanmin(fd_h)) if np.isfinite(fd_h).any() else None,
             "picks_without_smooth_h": int((~ok).sum()),
@@ -768,6 +767,24 @@ def run_adjoint(args, rank, world, local, pg):
             "per_component_floor": "|fd| floored at 1e-3 max|fd|",
             "components_below_floor": int((np.abs(f_) < floor).sum()),
             "cpu_s": round(time.time() - t1, 1)}
+        # the same split by the vertex's shortest incident edge: next to the poles (edges down to
+        # ~2e-5) no step gives a clean quotient -- h = 1e-6 is 5% of an edge (truncation), and the
+        # smaller steps that avoid the clamps leave differences of entries ~1e9 (rounding)
+        tri = np.asarray(ch["tris"], np.int64)
+        emin = np.full(n, np.inf)
+        for a, b in ((0, 1), (1, 2), (2, 0)):
+            el = np.linalg.norm(p[tri[:, a]] - p[tri[:, b]], axis=1)
+            np.minimum.at(emin, tri[:, a], el)
+            np.minimum.at(emin, tri[:, b], el)
+        far = np.array([emin[v] >= 1e-3 for v, _ in picks]) & ok
+        if far.any():
+            a2, f2 = ad[far], fd[far]
+            fl2 = 1e-3 * np.abs(f2).max()
+            line["fd_check"]["away_from_poles"] = {
+                "criterion": "shortest incident edge >= 1e-3 (h <= 1e-3 x the edge)", "components": int(far.sum()),
+                "rel_err_norm": float(np.linalg.norm(a2 - f2) / np.linalg.norm(f2)),
+                "per_component_rel_err_max": float((np.abs(a2 - f2) / np.maximum(np.abs(f2), fl2)).max())}
+            line["fd_check"]["next_to_poles_vertices"] = sorted({int(v) for (v, _), r in zip(picks, far) if not r})
     if rank == 0:
         print(json.dumps(line))
     barrier(pg)
