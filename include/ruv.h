@@ -269,11 +269,9 @@ void ruv_host_free(void* p);
 /* Self-test of the assembly's FP64 division and square root (computed on the integer and
  * FP32 pipes, bit-identical to the IEEE operations by design): n seeded inputs of class
  * `mode` (0-2: quotients -- moderate exponents, arbitrary bit patterns, near midpoints;
- * 3-5: square roots -- moderate exponents, arbitrary bit patterns, near perfect squares;
- * 6-7: the FP32 low half (float)(a - (double)(float)a) -- moderate exponents with rounding
- * ties, arbitrary bit patterns) compared bit for bit with the hardware operations.
- * *mismatches = the count; first4 = (a, b, got, want) of the first mismatch.  No reference
- * counterpart: a diagnostic. */
+ * 3-5: square roots -- moderate exponents, arbitrary bit patterns, near perfect squares)
+ * compared bit for bit with the hardware operations.  *mismatches = the count; first4 =
+ * (a, b, got, want) of the first mismatch.  No reference counterpart: a diagnostic. */
 ruv_status ruv_selftest_fp64(ruv_ctx* ctx, int mode, uint64_t seed, int64_t n, int64_t* mismatches, double* first4);
 
 /* Number of kernels this context has enqueued so far (each node of a replayed CUDA graph

@@ -804,7 +804,7 @@ ruv_status ruv_rectangularize(ruv_ctx* ctx, const double* uv, const uint8_t* bor
 }
 
 ruv_status ruv_selftest_fp64(ruv_ctx* ctx, int mode, uint64_t seed, int64_t n, int64_t* mismatches, double* first4) {
-  if (!ctx || !mismatches || !first4 || mode < 0 || mode > 7 || n < 0) return RUV_ERR_BAD_INPUT;
+  if (!ctx || !mismatches || !first4 || mode < 0 || mode > 5 || n < 0) return RUV_ERR_BAD_INPUT;
   return guarded(ctx, [&]() -> ruv_status {
     *mismatches = fp64_selftest(ctx->c, mode, seed, n, first4);
     return RUV_OK;

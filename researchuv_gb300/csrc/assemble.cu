@@ -85,27 +85,6 @@ __device__ __forceinline__ float f32_rn(double x) {
   if ((fb >> 23) >= 255u) return __double2float_rn(x);
   return __uint_as_float(fb | ((uint32_t)(u >> 32) & 0x80000000u));
 }
-// (float)(x - (double)h) for h = f32_rn(x), on the integer pipe: with x = M 2^(e-52) (M the
-// 53-bit significand) and h its rounding to 24 bits, x - h is exactly +-r 2^(e-52) with r the
-// low 29 bits of M (rounded down) or 2^29 minus them (rounded up), so its FP32 rounding is the
-// 32-bit conversion of r scaled by a power of two (exact while the result stays a normal
-// float).  Inputs outside that range go to the FP64 pipe.
-__device__ __forceinline__ float lo_half_rn(double x, float h) {
-  const uint64_t u = (uint64_t)__double_as_longlong(x);
-  const int ex = (int)((u >> 52) & 0x7ff);
-  const int ef = ex - 1023 + 127;
-  if (ef <= 0 || ef >= 254) return __double2float_rn(x - (double)h);  // (and h = inf: the top binade)
-  const uint32_t mf = (uint32_t)((u >> 29) & 0x7fffffu);
-  const uint32_t rest = (uint32_t)(u & ((1ull << 29) - 1)), half = 1u << 28;
-  const bool up = rest > half || (rest == half && (mf & 1u));  // f32_rn's rounding
-  const uint32_t r = up ? (1u << 29) - rest : rest;
-  if (r == 0) return 0.0f;
-  const float fr = __uint2float_rn(r);  // rn24(r), exact scaling below
-  const int er = (int)((__float_as_uint(fr) >> 23) & 0xff) + (ex - 1023 - 52);
-  if (er <= 0 || er >= 255) return __double2float_rn(x - (double)h);
-  const uint32_t neg = (uint32_t)(u >> 63) ^ (up ? 1u : 0u);
-  return __uint_as_float((neg << 31) | ((uint32_t)er << 23) | (__float_as_uint(fr) & 0x7fffffu));
-}
 __device__ __forceinline__ double rs_max(double a, double b) {  // Rust f64::max
   if (a != a) return b;
   if (b != b) return a;
@@ -350,7 +329,7 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
     const float h = f32_rn(val);
     vals32[at] = h;
     if (vals_lo) {
-      vals_lo[at] = lo_half_rn(val, h);  // = f32_rn(dsub(val, (double)h))
+      vals_lo[at] = f32_rn(dsub(val, (double)h));
       rs = dadd(rs, val);
     }
     ++at;
@@ -402,7 +381,7 @@ __global__ void k_rows(int64_t n_verts, const uint8_t* __restrict__ pinned, cons
   if (!diag_done) put((int32_t)row, dg);
   if (rsum) {
     const float h = f32_rn(rs);
-    rsum[row] = make_float2(h, lo_half_rn(rs, h));
+    rsum[row] = make_float2(h, f32_rn(dsub(rs, (double)h)));
   }
   diag_out[row] = dg;
   b[2 * row] = bu;
@@ -1085,17 +1064,7 @@ __global__ void k_fp64_selftest(int mode, uint64_t seed, int64_t n, unsigned lon
   const uint64_t r0 = splitmix64(seed + 3 * (uint64_t)i), r1 = splitmix64(seed + 3 * (uint64_t)i + 1),
                  r2 = splitmix64(seed + 3 * (uint64_t)i + 2);
   double a = 0.0, b = 0.0, got, want;
-  if (mode >= 6) {  // the fill pass's low halves: (float)(a - (double)(float)a)
-    if (mode == 6) {
-      uint64_t m = r0 & 0x800FFFFFFFFFFFFFull;
-      if ((r2 >> 20) % 4 == 0) m = (m & ~((1ull << 29) - 1)) | (1ull << 28);  // a rounding tie
-      a = bits_d(m | ((uint64_t)(1023 - 60 + (int)(r2 % 121)) << 52));
-    } else {
-      a = bits_d(r0);
-    }
-    got = (double)lo_half_rn(a, f32_rn(a));
-    want = (double)__double2float_rn(a - (double)__double2float_rn(a));
-  } else if (mode <= 2) {
+  if (mode <= 2) {
     if (mode == 0) {
       a = bits_d((r0 & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 60 + (int)(r2 % 121)) << 52));
       b = bits_d((r1 & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 60 + (int)((r2 >> 8) % 121)) << 52));

@@ -3,9 +3,7 @@ FP32 pipes, Newton corrections with an exact 128-bit residual, remainder-based r
 give the IEEE round-to-nearest bits of the hardware operations for every input: checked bit
 for bit on 2^26 seeded inputs per class -- moderate exponents, arbitrary bit patterns
 (zeros, subnormals, infinities, NaNs, out-of-range quotients through the hardware path),
-quotients near midpoints, square roots near perfect squares.  The same for the fill pass's
-FP32 low halves (float)(x - (double)(float)x) formed on the integer pipe (assemble.cu
-lo_half_rn), rounding ties included."""
+quotients near midpoints, square roots near perfect squares."""
 import pytest
 
 import researchuv_gb300 as R
@@ -14,9 +12,7 @@ pytestmark = pytest.mark.gpu
 
 CLASSES = {0: "quotients, exponents within +-60", 1: "quotients of arbitrary bit patterns",
            2: "quotients near a midpoint", 3: "square roots, exponents within +-60",
-           4: "square roots of arbitrary bit patterns", 5: "square roots near perfect squares",
-           6: "FP32 low halves, exponents within +-60 and rounding ties",
-           7: "FP32 low halves of arbitrary bit patterns"}
+           4: "square roots of arbitrary bit patterns", 5: "square roots near perfect squares"}
 
 
 @pytest.mark.parametrize("mode", sorted(CLASSES))
