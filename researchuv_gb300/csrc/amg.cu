@@ -659,8 +659,8 @@ struct GalOut {
   int* overflow;        // MODE 0 / 1: a row above the large table's capacity
 };
 
-template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OL, class IP, class IL, class KeyF, int KP>
-__global__ void __launch_bounds__(32 * WARPS, KP == 1 ? 1 : 4) k_gal_hash(int64_t nrows, const int32_t* __restrict__ list,
+template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OL, class IP, class IL, class KeyF>
+__global__ void __launch_bounds__(32 * WARPS) k_gal_hash(int64_t nrows, const int32_t* __restrict__ list,
                                                          const uint8_t* __restrict__ active, const OP* __restrict__ o_ptr,
                                                          const int32_t* __restrict__ o_idx, OL o_val,
                                                          const IP* __restrict__ i_ptr, const int32_t* __restrict__ i_idx,
@@ -720,86 +720,69 @@ __global__ void __launch_bounds__(32 * WARPS, KP == 1 ? 1 : 4) k_gal_hash(int64_
         if (sl >= o) x += y;
       }
       const int total = __shfl_sync(smask, x, G - 1, G);
-      // KP steps of G products at a time: first every step's inner loads (independent, all in
-      // flight together), then the steps' table updates in order -- the same sums in the same
-      // order as one step at a time, with one dependent load round per KP steps
-      for (int p0 = 0; p0 < total && !over; p0 += G * KP) {
-        int32_t kk[KP];
-        float2 vv[KP];
+      for (int p0 = 0; p0 < total; p0 += G) {
+        const int pl = p0 + sl;
+        const bool valid = pl < total;
+        int own = 0;  // lanes whose inclusive end is <= pl
 #pragma unroll
-        for (int u = 0; u < KP; ++u) {
-          const int pl = p0 + u * G + sl;
-          int own = 0;  // lanes whose inclusive end is <= pl
-#pragma unroll
-          for (int st = G / 2; st >= 1; st >>= 1) {
-            const int xv = __shfl_sync(smask, x, own + st - 1, G);
-            if (xv <= pl) own += st;
-          }
-          own = min(own, G - 1);
-          const float2 sco = make_float2(__shfl_sync(smask, sc.x, own, G), __shfl_sync(smask, sc.y, own, G));
-          const long long ibo = __shfl_sync(smask, (long long)ib, own, G);
-          const int sto = __shfl_sync(smask, x - len, own, G);
-          kk[u] = 0;
-          vv[u] = make_float2(0.0f, 0.0f);
-          if (pl < total) {
-            const int64_t e = (int64_t)ibo + (pl - sto);
-            kk[u] = keyf(i_idx[e]);
-            if (MODE != 0) vv[u] = df_mul(sco, i_val(e));
-          }
+        for (int st = G / 2; st >= 1; st >>= 1) {
+          const int xv = __shfl_sync(smask, x, own + st - 1, G);
+          if (xv <= pl) own += st;
         }
-#pragma unroll
-        for (int u = 0; u < KP; ++u) {
-          if (p0 + u * G >= total) break;  // (uniform across the sub-warp)
-          const int pl = p0 + u * G + sl;
-          const bool valid = pl < total;
-          const int32_t key = kk[u];
-          const float2 v = vv[u];
-          int slot = -1;
-          bool fresh = false;
-          if (valid) {
-            unsigned h = ((uint32_t)key * 0x9E3779B1u) >> (32 - LOGH);
-            for (int pr = 0; pr < H; ++pr) {
-              const int32_t k = reinterpret_cast<volatile int32_t*>(tkey)[h];
-              if (k == key) {
+        own = min(own, G - 1);
+        const float2 sco = make_float2(__shfl_sync(smask, sc.x, own, G), __shfl_sync(smask, sc.y, own, G));
+        const long long ibo = __shfl_sync(smask, (long long)ib, own, G);
+        const int sto = __shfl_sync(smask, x - len, own, G);
+        int32_t key = 0;
+        float2 v = make_float2(0.0f, 0.0f);
+        int slot = -1;
+        bool fresh = false;
+        if (valid) {
+          const int64_t e = (int64_t)ibo + (pl - sto);
+          key = keyf(i_idx[e]);
+          if (MODE != 0) v = df_mul(sco, i_val(e));
+          unsigned h = ((uint32_t)key * 0x9E3779B1u) >> (32 - LOGH);
+          for (int pr = 0; pr < H; ++pr) {
+            const int32_t k = reinterpret_cast<volatile int32_t*>(tkey)[h];
+            if (k == key) {
+              slot = (int)h;
+              break;
+            }
+            if (k == -1) {
+              const int32_t old = atomicCAS(&tkey[h], -1, key);
+              if (old == -1 || old == key) {
                 slot = (int)h;
+                fresh = old == -1;
                 break;
               }
-              if (k == -1) {
-                const int32_t old = atomicCAS(&tkey[h], -1, key);
-                if (old == -1 || old == key) {
-                  slot = (int)h;
-                  fresh = old == -1;
-                  break;
-                }
-              }
-              h = (h + 1) & (H - 1);
             }
+            h = (h + 1) & (H - 1);
           }
-          const unsigned fm = __ballot_sync(smask, fresh);
-          if (fresh) {  // the occupied slots in insertion order
-            const int pos = d + __popc(fm & ((1u << lane) - 1u));
-            if (pos < HS) {
-              ckey[pos] = key;
-              cslot[pos] = slot;
-            }
-          }
-          d += __popc(fm);
-          if (__ballot_sync(smask, valid && slot < 0) != 0u || d > HS) {
-            over = true;
-            break;
-          }
-          if (MODE != 0) {
-            stage[sl] = v;
-            __syncwarp(smask);
-            const unsigned gm = __match_any_sync(smask, valid ? slot : -1);
-            if (valid && (__ffs(gm) - 1) == lane) {
-              float2 s = tval[slot];
-              for (unsigned m = gm; m != 0u; m &= m - 1u) s = df_add(s, stage[(__ffs(m) - 1) - gb]);
-              tval[slot] = s;
-            }
-          }
-          __syncwarp(smask);
         }
+        const unsigned fm = __ballot_sync(smask, fresh);
+        if (fresh) {  // the occupied slots in insertion order
+          const int pos = d + __popc(fm & ((1u << lane) - 1u));
+          if (pos < HS) {
+            ckey[pos] = key;
+            cslot[pos] = slot;
+          }
+        }
+        d += __popc(fm);
+        if (__ballot_sync(smask, valid && slot < 0) != 0u || d > HS) {
+          over = true;
+          break;
+        }
+        if (MODE != 0) {
+          stage[sl] = v;
+          __syncwarp(smask);
+          const unsigned gm = __match_any_sync(smask, valid ? slot : -1);
+          if (valid && (__ffs(gm) - 1) == lane) {
+            float2 s = tval[slot];
+            for (unsigned m = gm; m != 0u; m &= m - 1u) s = df_add(s, stage[(__ffs(m) - 1) - gb]);
+            tval[slot] = s;
+          }
+        }
+        __syncwarp(smask);
       }
     }
     if (over) {
@@ -1644,40 +1627,20 @@ struct GalWork {
   std::chrono::steady_clock::time_point t0;
 };
 constexpr int kGalWarps = 8;
-constexpr int kGalPrefetch = 2;
 constexpr int kGalBigH = 8192;  // large table: 4096 distinct keys, 128 KB of shared memory
 
-// steps of inner loads a product kernel keeps in flight (RUV_GAL_PREFETCH: 1, 2 or 4)
-inline int gal_prefetch() {
-  const char* e = std::getenv("RUV_GAL_PREFETCH");
-  const int v = e ? std::atoi(e) : kGalPrefetch;
-  return v >= 4 ? 4 : v >= 2 ? 2 : 1;
-}
-
-template <int MODE, int G, int H, int WARPS, bool DIAG, int KP, class OP, class OL, class IP, class IL, class KeyF>
-void launch_gal_kp(cudaStream_t s, int64_t nrows, const int32_t* list, const uint8_t* active, const OP* o_ptr,
-                   const int32_t* o_idx, OL o_val, const IP* i_ptr, const int32_t* i_idx, IL i_val, KeyF keyf,
-                   const GalOut& out) {
+template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OL, class IP, class IL, class KeyF>
+void launch_gal(cudaStream_t s, int64_t nrows, const int32_t* list, const uint8_t* active, const OP* o_ptr,
+                const int32_t* o_idx, OL o_val, const IP* i_ptr, const int32_t* i_idx, IL i_val, KeyF keyf,
+                const GalOut& out) {
   constexpr int SUB = 32 / G;
   constexpr size_t smem = GalSmem<G, H>::bytes * WARPS * SUB;
-  auto k = k_gal_hash<MODE, G, H, WARPS, DIAG, OP, OL, IP, IL, KeyF, KP>;
+  auto k = k_gal_hash<MODE, G, H, WARPS, DIAG, OP, OL, IP, IL, KeyF>;
   if (smem > 48 * 1024) RUV_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k<<<div_up(nrows, (int64_t)WARPS * SUB), 32 * WARPS, smem, s>>>(nrows, list, active, o_ptr, o_idx, o_val, i_ptr, i_idx,
                                                                  i_val, keyf, out);
   count_launches(1);
   RUV_LAUNCH_CHECK();
-}
-template <int MODE, int G, int H, int WARPS, bool DIAG, class OP, class OL, class IP, class IL, class KeyF>
-void launch_gal(cudaStream_t s, int64_t nrows, const int32_t* list, const uint8_t* active, const OP* o_ptr,
-                const int32_t* o_idx, OL o_val, const IP* i_ptr, const int32_t* i_idx, IL i_val, KeyF keyf,
-                const GalOut& out) {
-  const int kp = MODE == 2 ? gal_prefetch() : 1;  // (the one-warp large-table rows: one step at a time)
-  if (kp == 4)
-    launch_gal_kp<MODE, G, H, WARPS, DIAG, 4>(s, nrows, list, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, out);
-  else if (kp == 2)
-    launch_gal_kp<MODE, G, H, WARPS, DIAG, 2>(s, nrows, list, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, out);
-  else
-    launch_gal_kp<MODE, G, H, WARPS, DIAG, 1>(s, nrows, list, active, o_ptr, o_idx, o_val, i_ptr, i_idx, i_val, keyf, out);
 }
 
 inline double env_or(const char* name, double dflt) {

@@ -295,27 +295,6 @@ def test_group_graph_bitwise(monkeypatch):
         assert np.array_equal(a.uv, b.uv)
 
 
-def test_galerkin_prefetch_bitwise(monkeypatch):
-    """The Galerkin products with 1, 2 or 4 steps of inner loads in flight (RUV_GAL_PREFETCH)
-    update their tables in the same order: the same hierarchy, iterations and UVs, bit for
-    bit (smoothed and tentative levels)."""
-    vo, to, p3, tr = W.disks(24, t_min=200, t_max=20000, seed=71)
-    C = R.prepare_patches(vo, to, p3, tr)
-    ctx = R.Context(0)
-    for pc in (R.Precond.AMG_SA, R.Precond.AMG):
-        opts = R.UnfoldOptions(precond=pc, precision=R.Precision.MIXED)
-        runs = []
-        for kp in ("1", "2", "4"):
-            monkeypatch.setenv("RUV_GAL_PREFETCH", kp)
-            runs.append(R.unfold_charts(ctx, C, opts))
-        monkeypatch.delenv("RUV_GAL_PREFETCH", raising=False)
-        for res in runs[1:]:
-            for a, b in zip(runs[0], res):
-                assert a.status == b.status == R.Status.OK
-                assert a.cg_iters == b.cg_iters
-                assert np.array_equal(a.uv, b.uv)
-
-
 @pytest.mark.parametrize("case", ["disks_16bit_columns", "field_row_relative_columns", "field_32bit_columns"])
 def test_bulk_copy_spmv_bitwise(monkeypatch, case):
     """The SpMV that stages each tile's row pointers, values and columns into shared memory
