@@ -983,13 +983,17 @@ __global__ void __launch_bounds__(kFactorThreads) k_direct_factor(const int32_t*
     }
   }
   __syncthreads();
-  // A^-1 = Y^T Y: (A^-1)[i][k] = sum_{j >= max(i,k)} Y[j][i] Y[j][k]
+  // A^-1 = Y^T Y: (A^-1)[i][k] = sum_{j >= max(i,k)} Y[j][i] Y[j][k], formed for i <= k and
+  // written to both halves (the products of (k, i) are those of (i, k) with their factors
+  // swapped, which rounds the same: the same bits for half the FP64 work)
   float* Ainv = fac + fac_off[c];
   for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
     const int i = t / m, k = t % m;
+    if (i > k) continue;
     double s = 0.0;
-    for (int j = i > k ? i : k; j < m; ++j) s += Y[j * m + i] * Y[j * m + k];
-    Ainv[t] = (float)s;
+    for (int j = k; j < m; ++j) s += Y[j * m + i] * Y[j * m + k];
+    Ainv[i * m + k] = (float)s;
+    Ainv[k * m + i] = (float)s;
   }
 }
 
