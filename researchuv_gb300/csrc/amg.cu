@@ -303,10 +303,16 @@ __global__ void k_group_graph(int64_t ng, const int64_t* __restrict__ goff, cons
   if (g >= ng) return;
   int32_t* K = gkey + gcap_off[g];
   float* V = gval + gcap_off[g];
-  // the first kLocal keys in a thread-local array (L1), the rest in the row's global area
-  constexpr int kLocal = 64;
-  int32_t lk[kLocal];
-  float lv[kLocal];
+  // the first kReg keys in registers (every index a compile-time constant once unrolled), the
+  // rest in the row's global area; each key's strength summed in entry order
+  constexpr int kReg = 16;
+  int32_t rk[kReg];
+  float rv[kReg];
+#pragma unroll
+  for (int t = 0; t < kReg; ++t) {
+    rk[t] = -1;
+    rv[t] = 0.0f;
+  }
   int n = 0;
   for (int64_t a = goff[g]; a < goff[g + 1]; ++a) {
     const int32_t i = mem[a];
@@ -314,19 +320,25 @@ __global__ void k_group_graph(int64_t ng, const int64_t* __restrict__ goff, cons
       const int32_t h = grp_of[cols[e]];
       if (h == (int32_t)g) continue;
       const float v = fabsf(vals[e]);
-      const int nl = min(n, kLocal);
-      int t = 0;
-      while (t < nl && lk[t] != h) ++t;
-      if (t < nl) {
-        lv[t] += v;
-        continue;
-      }
+      bool hit = false;
+#pragma unroll
+      for (int t = 0; t < kReg; ++t)
+        if (rk[t] == h) {  // (unused slots hold -1, never a group)
+          rv[t] += v;
+          hit = true;
+        }
+      if (hit) continue;
+      int t = kReg;
       while (t < n && K[t] != h) ++t;
       if (t < n) {
         V[t] += v;
-      } else if (n < kLocal) {
-        lk[n] = h;
-        lv[n] = v;
+      } else if (n < kReg) {
+#pragma unroll
+        for (int q = 0; q < kReg; ++q)
+          if (q == n) {
+            rk[q] = h;
+            rv[q] = v;
+          }
         ++n;
       } else {
         K[n] = h;
@@ -335,10 +347,12 @@ __global__ void k_group_graph(int64_t ng, const int64_t* __restrict__ goff, cons
       }
     }
   }
-  for (int t = 0; t < min(n, kLocal); ++t) {
-    K[t] = lk[t];
-    V[t] = lv[t];
-  }
+#pragma unroll
+  for (int t = 0; t < kReg; ++t)
+    if (t < n) {
+      K[t] = rk[t];
+      V[t] = rv[t];
+    }
   gn[g] = n;
 }
 
