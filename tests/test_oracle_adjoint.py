@@ -39,3 +39,22 @@ def test_fixed_system_matches_unfold_solution():
     P = O.Pipeline(p, tris, weld_tol=0.0, lu_limit=0)
     assert P.n_charts == 1
     assert O.uv_error(uv, P.superlu_uv(0)) < 1e-12
+
+
+def test_fd_steps_avoid_the_clamps_and_low_rank_solves_agree():
+    """The FD check's step selection (the largest of 1e-6 ... 1e-9 at which +-h moves no clamp
+    of the assembly around the vertex) and its low-rank (Woodbury) perturbed solves: on a
+    smooth instance every pick keeps h = 1e-6, and the quotients equal those of refactoring
+    every perturbed system and agree with the LU adjoint."""
+    p, tris, pinned, pin_uv, target = _instance()
+    lam_l2 = 1.0 / len(p)
+    g, _ = O.lu_adjoint_gradient(p, tris, pinned, pin_uv, lam_l2, target)
+    rng = np.random.Generator(np.random.PCG64(9))
+    picks = [(int(v), k) for v in rng.choice(len(p), 12, replace=False) for k in range(3)]
+    fd, hs = O.fd_gradient(p, tris, pinned, pin_uv, lam_l2, target, picks, reuse_base=True,
+                           smooth_steps=(1e-6, 1e-7, 1e-8, 1e-9))
+    assert np.all(hs == 1e-6)
+    plain = O.fd_gradient(p, tris, pinned, pin_uv, lam_l2, target, picks, h=1e-6)
+    assert np.abs(fd - plain).max() <= 1e-9 * np.abs(plain).max()
+    ad = np.array([g[v, k] for v, k in picks])
+    assert np.linalg.norm(ad - fd) / np.linalg.norm(fd) <= 1e-5
