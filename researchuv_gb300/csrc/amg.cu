@@ -928,13 +928,36 @@ __global__ void k_agg_lead_rows(int64_t n, const uint8_t* __restrict__ lead, con
   if (i < n) arow[i] = (lead[i] && glead[grp_of[i]]) ? 1 : 0;
 }
 
-// Dense inverse of each final chart block (<= kDirect rows), one CTA per chart, FP64 in
-// shared memory: Cholesky A = L L^T, then Y = L^-1 (one column per thread), then
-// A^-1 = Y^T Y, stored as FP32 (symmetric, row-major m x m).  The V-cycle's coarse solve is
-// then one dense mat-vec per chart instead of two serial triangular sweeps.
+// Dense inverse of each final chart block (<= kDirect rows), one CTA per chart, in shared
+// memory: Cholesky A = L L^T, then Y = L^-1, then A^-1 = Y^T Y, stored as FP32 (symmetric,
+// row-major m x m).  The V-cycle's coarse solve is then one dense mat-vec per chart instead
+// of two serial triangular sweeps.
 constexpr int kFactorThreads = 128;
-constexpr size_t kFactorSmem = 2 * sizeof(double) * kDirect * kDirect;
+constexpr size_t kFactorSmem = 2 * sizeof(float2) * kDirect * kDirect;
 
+// df helpers of the dense factors: a - b, a / b and sqrt(a) on (hi, lo) pairs (one Newton
+// correction each on the FP32 quotient / root, the residual formed with error-free products)
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 df_div(float2 a, float2 b) {
+  const float q1 = a.x / b.x;
+  const float2 r = df_add(a, df_neg(df_mul(make_float2(q1, 0.0f), b)));
+  const float q2 = r.x / b.x;
+  return df_add(make_float2(q1, 0.0f), make_float2(q2, 0.0f));
+}
+__device__ __forceinline__ float2 df_sqrt(float2 a) {
+  if (!(a.x > 0.0f)) return make_float2(0.0f, 0.0f);
+  const float x = sqrtf(a.x);
+  const float2 r = df_add(a, df_neg(df_mul(make_float2(x, 0.0f), make_float2(x, 0.0f))));
+  return df_add(make_float2(x, 0.0f), make_float2(r.x / (2.0f * x), 0.0f));
+}
+
+// Per chart: the dense inverse of its last block (m <= kDirect rows), by a right-looking
+// Cholesky factorisation and a right-looking forward substitution of L Y = I, then
+// A^-1 = Y^T Y, all in double-float pairs (FP32 FMA pipe; GB300's FP64 pipe made the FP64
+// form of this kernel throughput-bound).  Pivot floor: on a nearly singular chart (kappa ~
+// 1e10: a long chain pinned at its ends) the smallest eigenvalue of the coarse block is below
+// the rounding of its entries; the floor 1e-6 |a_jj| keeps the factor real and leaves that
+// one mode to the outer Krylov iteration.  A zero or non-finite pivot sets *bad.
 __global__ void __launch_bounds__(kFactorThreads) k_direct_factor(const int32_t* __restrict__ final_lvl,
                                                                   const int64_t* const* __restrict__ lvl_chart_row,
                                                                   const int32_t* const* __restrict__ lvl_rp,
@@ -942,72 +965,80 @@ __global__ void __launch_bounds__(kFactorThreads) k_direct_factor(const int32_t*
                                                                   const double* const* __restrict__ lvl_vals,
                                                                   const int64_t* __restrict__ fac_off, float* __restrict__ fac,
                                                                   int* __restrict__ bad) {
-  extern __shared__ double smem[];
-  double* M = smem;                        // m x m, row-major; L in the lower triangle
-  double* Y = smem + kDirect * kDirect;    // Y[k * m + j] = (L^-1)[k][j]
+  extern __shared__ float2 dsm[];
+  float2* M = dsm;                      // m x m, row-major: the lower triangle becomes L
+  float2* Y = dsm + kDirect * kDirect;  // starts as I; row i becomes (L^-1)[i] at step i
+  __shared__ float dg0[kDirect];        // |a_jj| before the factorisation (the pivot floor)
   const int c = blockIdx.x;
   const int f = final_lvl[c];
   if (f < 0) return;
   const int64_t r0 = lvl_chart_row[f][c];
   const int m = (int)(lvl_chart_row[f][c + 1] - r0);
   if (m <= 0 || m > kDirect) return;
-  for (int t = threadIdx.x; t < m * m; t += blockDim.x) M[t] = 0.0;
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+    M[t] = make_float2(0.0f, 0.0f);
+    Y[t] = make_float2((t / m) == (t % m) ? 1.0f : 0.0f, 0.0f);
+  }
+  for (int t = threadIdx.x; t < m; t += blockDim.x) dg0[t] = 0.0f;
   __syncthreads();
   for (int r = threadIdx.x; r < m; r += blockDim.x) {
     const int64_t row = r0 + r;
     for (int e = lvl_rp[f][row]; e < lvl_rp[f][row + 1]; ++e) {
-      int64_t col = lvl_cols[f][e] - r0;
-      if (col >= 0 && col < m) M[r * m + col] = lvl_vals[f][e];
+      const int64_t col = lvl_cols[f][e] - r0;
+      if (col >= 0 && col < m) {
+        const double v = lvl_vals[f][e];
+        const float hi = (float)v;
+        M[r * m + col] = make_float2(hi, (float)(v - (double)hi));
+        if (col == r) dg0[r] = fabsf(hi);
+      }
     }
   }
   __syncthreads();
+  // L: column j scaled by its pivot, then the trailing block updated (entries in parallel)
   for (int j = 0; j < m; ++j) {
     if (threadIdx.x == 0) {
-      // pivot floor: the coarse operator comes from FP32 Galerkin products, so on a nearly
-      // singular chart (kappa ~ 1e10: a long chain pinned at its ends) its smallest
-      // eigenvalue is below the rounding of its entries; the floor keeps the factor real
-      // and leaves that one mode to the outer Krylov iteration
-      const double a_jj = M[j * m + j];
-      double d = a_jj;
-      for (int k = 0; k < j; ++k) d -= M[j * m + k] * M[j * m + k];
-      const double fl = 1e-6 * fabs(a_jj);
-      if (!(d > fl)) d = fl;
-      if (!(d > 0.0)) {  // a zero or non-finite diagonal
+      float2 d = M[j * m + j];
+      const float fl = 1e-6f * dg0[j];
+      if (!(d.x > fl)) d = make_float2(fl, 0.0f);
+      if (!(d.x > 0.0f) || !isfinite(d.x)) {  // a zero or non-finite diagonal
         atomicExch(bad, 1);
-        d = 1e-30;
+        d = make_float2(1e-30f, 0.0f);
       }
-      M[j * m + j] = sqrt(d);
+      M[j * m + j] = df_sqrt(d);
     }
     __syncthreads();
-    const double piv = M[j * m + j];
-    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
-      double s = M[i * m + j];
-      for (int k = 0; k < j; ++k) s -= M[i * m + k] * M[j * m + k];
-      M[i * m + j] = s / piv;
+    const float2 piv = M[j * m + j];
+    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) M[i * m + j] = df_div(M[i * m + j], piv);
+    __syncthreads();
+    const int w = m - j - 1;  // trailing block: rows and columns j+1 .. m-1, lower triangle
+    for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
+      const int i = j + 1 + t / w, k = j + 1 + t % w;
+      if (k > i) continue;
+      M[i * m + k] = df_add(M[i * m + k], df_neg(df_mul(M[i * m + j], M[k * m + j])));
     }
     __syncthreads();
   }
-  // Y = L^-1: column j solves L y = e_j by forward substitution (rows above j are zero).
-  for (int j = threadIdx.x; j < m; j += blockDim.x) {
-    for (int i = 0; i < j; ++i) Y[i * m + j] = 0.0;
-    for (int i = j; i < m; ++i) {
-      double s = i == j ? 1.0 : 0.0;
-      for (int k = j; k < i; ++k) s -= M[i * m + k] * Y[k * m + j];
-      Y[i * m + j] = s / M[i * m + i];
+  // Y = L^-1: row i scaled by L_ii, then the rows below updated
+  for (int i = 0; i < m; ++i) {
+    const float2 lii = M[i * m + i];
+    for (int j = threadIdx.x; j <= i; j += blockDim.x) Y[i * m + j] = df_div(Y[i * m + j], lii);
+    __syncthreads();
+    const int rows = m - i - 1;
+    for (int t = threadIdx.x; t < rows * (i + 1); t += blockDim.x) {
+      const int k = i + 1 + t / (i + 1), j = t % (i + 1);
+      Y[k * m + j] = df_add(Y[k * m + j], df_neg(df_mul(M[k * m + i], Y[i * m + j])));
     }
+    __syncthreads();
   }
-  __syncthreads();
-  // A^-1 = Y^T Y: (A^-1)[i][k] = sum_{j >= max(i,k)} Y[j][i] Y[j][k], formed for i <= k and
-  // written to both halves (the products of (k, i) are those of (i, k) with their factors
-  // swapped, which rounds the same: the same bits for half the FP64 work)
+  // A^-1 = Y^T Y: (A^-1)[i][k] = sum_{j >= max(i,k)} Y[j][i] Y[j][k], for i <= k and mirrored
   float* Ainv = fac + fac_off[c];
   for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
     const int i = t / m, k = t % m;
     if (i > k) continue;
-    double s = 0.0;
-    for (int j = k; j < m; ++j) s += Y[j * m + i] * Y[j * m + k];
-    Ainv[i * m + k] = (float)s;
-    Ainv[k * m + i] = (float)s;
+    float2 s = make_float2(0.0f, 0.0f);
+    for (int j = k; j < m; ++j) s = df_add(s, df_mul(Y[j * m + i], Y[j * m + k]));
+    Ainv[i * m + k] = s.x;
+    Ainv[k * m + i] = s.x;
   }
 }
 
