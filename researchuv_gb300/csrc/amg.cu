@@ -1065,33 +1065,6 @@ __device__ __forceinline__ void stf(float* p, int64_t i, const F<NR>& v) {
   else p[i] = v.c[0];
 }
 
-// Level 0's post-smoother can also form the CG's per-tile partials r.z and z.q of the z it
-// writes (b = r at level 0), sparing the CG a pass over r, z and q: map[t] is the CG tile of
-// level tile t (every continuing tile has one when this is on); the sums run in FP32 per row
-// and are combined per tile, as the CG's own dots kernel does.
-struct DotsOut {
-  const float* q = nullptr;
-  double* part = nullptr;
-  const int32_t* map = nullptr;
-  template <int NR>
-  __device__ __forceinline__ void add(int64_t i, const F<NR>& r, const F<NR>& z, float (&acc)[2]) const {
-    const F<NR> qi = ldf<NR>(q, i);
-#pragma unroll
-    for (int c = 0; c < NR; ++c) {
-      acc[0] += r.c[c] * z.c[c];
-      acc[1] += z.c[c] * qi.c[c];
-    }
-  }
-  __device__ __forceinline__ void finish(int64_t tl, float (&acc)[2], float* sh) const {
-    block_sum_t<2, float>(acc, sh);
-    if (threadIdx.x == 0) {
-      const int32_t t = map[tl];
-      part[2 * t] = (double)acc[0];
-      part[2 * t + 1] = (double)acc[1];
-    }
-  }
-};
-
 // The level kernels run over chart-aligned row tiles (one CTA per tile, one chart-state
 // check per CTA) as CSR-vector: LPR lanes per row, each lane covering K entries in one
 // unrolled sweep (longer rows finish in a remainder loop), U rows in flight per sub-warp,
@@ -1504,12 +1477,10 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int
                                                            const int32_t* __restrict__ cbase,
                                                            const float* __restrict__ vals, const float* __restrict__ dinv,
                                                            const float* __restrict__ b, const float* __restrict__ y,
-                                                           float* __restrict__ x, DotsOut dots) {
-  __shared__ float sh[2 * 32];
+                                                           float* __restrict__ x) {
   const int64_t tl = blockIdx.x;
   const int32_t ch = T.chart[tl];
   if (done[ch]) return;
-  float acc[2] = {0.0f, 0.0f};
   auto run = [&](auto colf) {
   tile_rows<NR, LPR, U, K>(
       T.tab[2 * tl], T.tab[2 * tl + 1], nullptr, rp, colf, [&](int64_t e) { return vals[e]; },
@@ -1521,13 +1492,11 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up(LvlTiles T, const int
 #pragma unroll
         for (int c = 0; c < NR; ++c) xi.c[c] = yi.c[c] + wd * (bi.c[c] - s.c[c]);
         stf<NR>(x, i, xi);
-        if (dots.map) dots.add(i, bi, xi, acc);
       });
   };
   if constexpr (NW == 1) run(ColsNarrow{c16, cbase[ch]});
   else if constexpr (NW == 2) run(ColsRowRel{c16});
   else run(ColsWide{cols});
-  if (dots.map) dots.finish(tl, acc, sh);
 }
 
 // Up, tentative prolongator (one 1 per row at agg[i]): the prolongation and the
@@ -1542,12 +1511,10 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up_t(LvlTiles T, const i
                                                              const float* __restrict__ vals, const float* __restrict__ dinv,
                                                              const float* __restrict__ b, const int32_t* __restrict__ agg,
                                                              const float* __restrict__ xc, float alpha_c,
-                                                             float* __restrict__ x, DotsOut dots) {
-  __shared__ float sh[2 * 32];
+                                                             float* __restrict__ x) {
   const int64_t tl = blockIdx.x;
   const int32_t ch = T.chart[tl];
   if (done[ch]) return;
-  float acc[2] = {0.0f, 0.0f};
   auto yval = [&](int64_t j) {
     F<NR> v = ldf<NR>(b, j);
     const float wd = kOmega * dinv[j];
@@ -1567,13 +1534,11 @@ __global__ void __launch_bounds__(kAmgThreads) k_smooth_up_t(LvlTiles T, const i
 #pragma unroll
         for (int c = 0; c < NR; ++c) xi.c[c] = yi.c[c] + wd * (bi.c[c] - s.c[c]);
         stf<NR>(x, i, xi);
-        if (dots.map) dots.add(i, bi, xi, acc);
       });
   };
   if constexpr (NW == 1) run(ColsNarrow{c16, cbase[ch]});
   else if constexpr (NW == 2) run(ColsRowRel{c16});
   else run(ColsWide{cols});
-  if (dots.map) dots.finish(tl, acc, sh);
 }
 
 // Direct solve of every chart at its last level: x = A^-1 b with the dense inverse (one CTA
@@ -1677,12 +1642,6 @@ struct AmgHierarchy {
   int k_levels = 0;  // top levels applied in the K-form (two coarse corrections with steplengths)
   int* err = nullptr;  // a staged tile's bounded wait ran out
   int64_t spin_limit = 0;
-  std::vector<int64_t> h_l0_cont_tab;  // level 0's continuing tiles, [begin, end) pairs (host)
-  // the CG's r.z and z.q partials formed by level 0's post-smoother (amg_fuse_dots): q, the
-  // partials array and each continuing tile's CG tile (null: not fused)
-  const float* dots_q = nullptr;
-  double* dots_part = nullptr;
-  int32_t* dots_map = nullptr;
 };
 
 namespace {
@@ -2171,7 +2130,6 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
       }
       ctile[NC] = (int64_t)tch.size();
       const int64_t nt = (int64_t)tch.size();
-      if (k == 0 && which == 0) H->h_l0_cont_tab = tab;
       if (which == 0 && k < H->k_levels && nt > 0) {
         int64_t* dct = ctx.ws.get<int64_t>(tag + ".kct", NC + 1);
         RUV_CUDA(cudaMemcpyAsync(dct, ctile.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, s));
@@ -2317,39 +2275,6 @@ void amg_bind(Ctx& ctx, AmgHierarchy* H, float* r0, float* z0) {
   RUV_CUDA(cudaStreamSynchronize(ctx.stream));
 }
 
-// Level 0's post-smoother forms the CG's r.z and z.q tile partials (see DotsOut) when every
-// continuing tile of level 0 is also one of the CG's tiles (cg_tab: the CG's [begin, end)
-// pairs), the cycle is the V-cycle at level 0 and its smoothers are not staged.  covered[t]
-// (device, one per CG tile) then marks the tiles whose partials the cycle writes.
-bool amg_fuse_dots(Ctx& ctx, AmgHierarchy* H, const std::vector<int64_t>& cg_tab, const float* q, double* part,
-                   uint8_t* covered) {
-  H->dots_q = nullptr;
-  H->dots_part = nullptr;
-  H->dots_map = nullptr;
-  const char* e = std::getenv("RUV_FUSE_DOTS");
-  if ((e && e[0] == '0') || H->lv.size() < 2 || H->k_levels > 0 || H->lv[0].stage_smem) return false;
-  const int64_t ncg = (int64_t)cg_tab.size() / 2, nl = (int64_t)H->h_l0_cont_tab.size() / 2;
-  std::vector<int32_t> map(nl, -1);
-  std::vector<uint8_t> cov(ncg, 0);
-  int64_t t = 0;  // both tables ascend by row
-  for (int64_t l = 0; l < nl; ++l) {
-    const int64_t b = H->h_l0_cont_tab[2 * l], en = H->h_l0_cont_tab[2 * l + 1];
-    while (t < ncg && cg_tab[2 * t] < b) ++t;
-    if (t >= ncg || cg_tab[2 * t] != b || cg_tab[2 * t + 1] != en) return false;
-    map[l] = (int32_t)t;
-    cov[t] = 1;
-  }
-  cudaStream_t s = ctx.stream;
-  int32_t* dmap = ctx.ws.get<int32_t>("amg.dots_map", std::max<int64_t>(nl, 1));
-  if (nl > 0) RUV_CUDA(cudaMemcpyAsync(dmap, map.data(), sizeof(int32_t) * nl, cudaMemcpyHostToDevice, s));
-  if (ncg > 0) RUV_CUDA(cudaMemcpyAsync(covered, cov.data(), ncg, cudaMemcpyHostToDevice, s));
-  RUV_CUDA(cudaStreamSynchronize(s));  // the host tables go out of scope
-  H->dots_q = q;
-  H->dots_part = part;
-  H->dots_map = dmap;
-  return true;
-}
-
 namespace {
 
 // Lanes per row from the operator's mean row length: one lane per row for the tentative
@@ -2413,11 +2338,10 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
-    const DotsOut dots = k == 0 && H->dots_map ? DotsOut{H->dots_q, H->dots_part, H->dots_map} : DotsOut{};
     if (!L.smoothed) {
 #define CALL(X, UU, KK)                                                                                                \
   k_smooth_up_t<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
-                                                                    L.dinv, L.b, L.agg, C.x, H->alpha_c, L.x, dots)
+                                                                    L.dinv, L.b, L.agg, C.x, H->alpha_c, L.x)
       if (L.c16 && L.rowrel) {
         constexpr int NW = 2;
         RUV_LPR_SWITCH(la, CALL)
@@ -2443,7 +2367,7 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
         L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, L.dinv, L.b, L.y, L.x, H->spin_limit, H->err);           \
   else                                                                                                               \
     k_smooth_up<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
-                                                                    L.dinv, L.b, L.y, L.x, dots)
+                                                                    L.dinv, L.b, L.y, L.x)
     if (L.c16 && L.rowrel) {
       constexpr int NW = 2;
       RUV_LPR_SWITCH(la, CALL)
@@ -2556,10 +2480,6 @@ class AmgPrecond final : public SepPrecond {
   void bind(Ctx& ctx, void* r, void* z, bool) override { amg_bind(ctx, H_, static_cast<float*>(r), static_cast<float*>(z)); }
   int apply(Ctx& ctx, const int32_t* done) override { return amg_apply(ctx, H_, done); }
   const int* error_flag() const override { return H_->err; }
-  bool fuse_dots(Ctx& ctx, const std::vector<int64_t>& cg_tab, const float* q, double* part,
-                 uint8_t* covered) override {
-    return amg_fuse_dots(ctx, H_, cg_tab, q, part, covered);
-  }
 
  private:
   AmgHierarchy* H_ = nullptr;

@@ -950,14 +950,13 @@ __global__ void k_mark_done(const ChartState* __restrict__ st, int64_t n, int32_
   if (c < n) done[c] = st[c].state != kActive ? 1 : 0;
 }
 
-// r.z and z.q per tile (tiles marked in `skip` have theirs from the preconditioner)
 template <class S, int NR>
 __global__ void __launch_bounds__(kTileThreads) k_dots_rz(Tiles T, const ChartState* __restrict__ st, const S* __restrict__ r,
                                                           const S* __restrict__ z, const S* __restrict__ q,
-                                                          double* __restrict__ part, const uint8_t* __restrict__ skip) {
+                                                          double* __restrict__ part) {
   __shared__ S sh[2 * 32];
   int64_t t = blockIdx.x;
-  if (st[T.chart[t]].state != kActive || (skip && skip[t])) return;
+  if (st[T.chart[t]].state != kActive) return;
   S acc[2] = {S(0), S(0)};
   for (int64_t i = T.tab[2 * t] + threadIdx.x; i < T.tab[2 * t + 1]; i += blockDim.x) {
     const V<S, NR> rv = ldv<S, NR>(r, i), zv = ldv<S, NR>(z, i), qv = ldv<S, NR>(q, i);
@@ -1215,15 +1214,6 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
   int32_t* done = ws.get<int32_t>("pcg.done", NC);
   if (copies) P.bind(ctx, r32, z32, false);
   else P.bind(ctx, r, z, !mixed);
-  // the FP32 loop: the preconditioner may form the r.z / z.q partials of the tiles it covers
-  const uint8_t* dskip = nullptr;
-  if (mixed && NTL > 0) {
-    std::vector<int64_t> htab(2 * NTL);
-    RUV_CUDA(cudaMemcpyAsync(htab.data(), T.tab, sizeof(int64_t) * 2 * NTL, cudaMemcpyDeviceToHost, s));
-    RUV_CUDA(cudaStreamSynchronize(s));
-    uint8_t* cov = ws.get<uint8_t>("pcg.dots_cov", NTL);
-    if (P.fuse_dots(ctx, htab, reinterpret_cast<const float*>(q), part2, cov)) dskip = cov;
-  }
   const int flex = P.flexible() ? 1 : 0;
   const unsigned gv = div_up(NR * NR_, 256);
   auto to32 = [&]() {
@@ -1256,7 +1246,7 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
     to32();
     count_launches(1 + conv + P.apply(ctx, done));
     to64();
-    k_dots_rz<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, r, z, q, part2, dskip);
+    k_dots_rz<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, r, z, q, part2);
     k_chart_rz0<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part2);
     k_copy_dir<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
     count_launches(3);
@@ -1288,7 +1278,7 @@ void run_pcg_sep(Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tile
       l += 4 + conv;
       l += P.apply(ctx, done);
       to64();
-      k_dots_rz<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, r, z, q, part2, dskip);
+      k_dots_rz<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, r, z, q, part2);
       k_chart_beta_pc<<<(unsigned)NC, kChartThreads, 0, s>>>(T, st, part2, flex);
       k_direction<S, NR><<<(unsigned)NTL, kTileThreads, 0, s>>>(T, st, z, p);
       l += 3;
@@ -1441,7 +1431,7 @@ double time_spmv(Ctx& ctx, DevSystem& sys, Tiles T, int reps, int nbuf, bool ite
     if (iter && T.n > 0) {
       k_update<S, NR><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, nullptr, 2, xv, rv, nullptr, ps[k % nbuf],
                                                              qs[k % nbuf], part2);
-      k_dots_rz<S, NR><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, rv, rv, qs[k % nbuf], part2, nullptr);
+      k_dots_rz<S, NR><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, rv, rv, qs[k % nbuf], part2);
       k_direction<S, NR><<<(unsigned)T.n, kTileThreads, 0, s>>>(T, st, rv, ps[k % nbuf]);
       count_launches(3);
     }

@@ -64,12 +64,6 @@ struct SepPrecond {
   virtual int apply(Ctx& ctx, const int32_t* done) = 0;
   // device flag set when an application gave up a bounded device-side wait (nullptr: none)
   virtual const int* error_flag() const { return nullptr; }
-  // the FP32 CG's r.z and z.q tile partials formed inside the application (the AMG's level-0
-  // post-smoother) for the CG tiles it marks in `covered`; false: not offered
-  virtual bool fuse_dots(Ctx&, const std::vector<int64_t>& /*cg_tab*/, const float* /*q*/, double* /*part*/,
-                         uint8_t* /*covered*/) {
-    return false;
-  }
 };
 
 // Batched aggregation AMG (amg.cu): hierarchy built on the device, one V(1,1) cycle per apply.
@@ -192,8 +186,7 @@ struct Ctx {
   bool have_last = false;
   int lanes_per_row = 0;   // SpMV sub-warp width (0 = from the row-length profile)
   int unroll = 0;          // SpMV rows in flight per sub-warp (0 = from the shape)
-  int tile_rows = 1024;    // rows per CTA tile (the autotuner's pick on the disks and the height
-                           // fields; the AMG's level tiles have the same height, see amg_fuse_dots)
+  int tile_rows = 512;     // rows per CTA tile (the autotuner's pick on the height fields)
   // the bulk-copy SpMV (k_spmv_tma): 0 off (the default: on the 4096-disk step the CSR-vector
   // kernel's iteration ran faster), 1 on; the autotuner chooses it, RUV_SPMV_TMA=0/1 overrides
   int spmv_tma = 0;

@@ -384,27 +384,6 @@ def test_pinned_inputs_bitwise(monkeypatch, kernel):
     assert [s.cg_iters for s in st_a] == [stats[c].cg_iters for c in range(pb.n_charts)]
 
 
-@pytest.mark.parametrize("precond", [R.Precond.AMG_SA, R.Precond.AMG])
-def test_fused_dots_match_separate_pass(monkeypatch, precond):
-    """The CG's r.z and z.q partials formed by the AMG's level-0 post-smoother (the default in
-    mixed precision) against the CG's own dots pass (RUV_FUSE_DOTS=0): the same per-tile sums
-    in another FP32 order, so every chart converges in about the same iterations to the same
-    UVs (both within the bar against FP64 LU)."""
-    vo, to, p3, tr = W.disks(24, t_min=200, t_max=20000, seed=73)
-    C = R.prepare_patches(vo, to, p3, tr)
-    monkeypatch.setenv("RUV_TILE_ROWS", "1024")  # the CG's tiles are the AMG's level tiles
-    ctx = R.Context(0)
-    opts = R.UnfoldOptions(precond=precond, precision=R.Precision.MIXED)
-    monkeypatch.setenv("RUV_FUSE_DOTS", "0")
-    sep = R.unfold_charts(ctx, C, opts)
-    monkeypatch.delenv("RUV_FUSE_DOTS", raising=False)
-    fused = R.unfold_charts(ctx, C, opts)
-    for a, b in zip(sep, fused):
-        assert a.status == b.status == R.Status.OK
-        assert abs(a.cg_iters - b.cg_iters) <= 2
-        assert O.uv_error(a.uv, b.uv) <= 1e-9
-
-
 def test_staged_smoothers_bitwise(monkeypatch):
     """Level 0's AMG smoothers with their tiles staged into shared memory by bulk copies
     (RUV_AMG_STAGE=1) run the same row loop: bitwise the same UVs and iterations."""
@@ -412,7 +391,6 @@ def test_staged_smoothers_bitwise(monkeypatch):
     C = R.prepare_patches(vo, to, p3, tr)
     ctx = R.Context(0)
     opts = R.UnfoldOptions(precond=R.Precond.AMG_SA, precision=R.Precision.MIXED)
-    monkeypatch.setenv("RUV_FUSE_DOTS", "0")  # (the staged smoothers do not form the CG's dots)
     monkeypatch.setenv("RUV_AMG_STAGE", "0")
     plain = R.unfold_charts(ctx, C, opts)
     monkeypatch.setenv("RUV_AMG_STAGE", "1")
