@@ -186,7 +186,7 @@ struct Ctx {
   bool have_last = false;
   int lanes_per_row = 0;   // SpMV sub-warp width (0 = from the row-length profile)
   int unroll = 0;          // SpMV rows in flight per sub-warp (0 = from the shape)
-  int tile_rows = 512;     // rows per CTA tile (the autotuner's pick on the height fields)
+  int tile_rows = 1024;    // rows per CTA tile (the autotuner's pick on the disks and the height fields)
   // the bulk-copy SpMV (k_spmv_tma): 0 off (the default: on the 4096-disk step the CSR-vector
   // kernel's iteration ran faster), 1 on; the autotuner chooses it, RUV_SPMV_TMA=0/1 overrides
   int spmv_tma = 0;
