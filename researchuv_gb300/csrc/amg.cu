@@ -1586,148 +1586,6 @@ __global__ void __launch_bounds__(kDirect) k_direct_solve(const int32_t* __restr
   for (int k = 0; k < NR; ++k) x[NR * (r0 + i) + k] = s[k];
 }
 
-// The coarse tail of the V(1,1) cycle for one small chart (one CTA per chart): from level kt
-// (tentative prolongators only) down to the chart's last level and back, every step over the
-// chart's own rows with a block barrier between steps, instead of a launch per level and step
-// for the whole batch (levels below kt hold a few hundred rows per chart or fewer, and their
-// batch-wide launches ran at a fraction of their bytes' time).  The same formulas as
-// k_smooth_down (x not stored), k_restrict, k_direct_solve and k_smooth_up_t, one thread per
-// row, sums in entry order.
-struct TailArgs {
-  const int64_t* const* chart_row;
-  const int32_t* const* rp;
-  const int32_t* const* cols;
-  const float* const* vals;
-  const float* const* dinv;
-  float* const* b;
-  float* const* x;
-  float* const* t;
-  const int32_t* const* agg;
-  const int64_t* const* roff;
-  const int32_t* const* rc;
-  const float* const* rv;
-  const int32_t* final_lvl;
-  const int64_t* fac_off;
-  const float* fac;
-  float alpha_c;
-};
-
-template <int NR>
-__global__ void __launch_bounds__(kAmgThreads) k_vtail_chart(TailArgs A, const int32_t* __restrict__ done,
-                                                             const uint8_t* __restrict__ small, int kt) {
-  const int c = blockIdx.x;
-  if (done[c] || !small[c]) return;
-  const int f = A.final_lvl[c];
-  for (int k = kt; k < f; ++k) {  // down: t = b - A (w D^-1 b), then b_(k+1) = R t
-    const int64_t r0 = A.chart_row[k][c], r1 = A.chart_row[k][c + 1];
-    const int32_t* rp = A.rp[k];
-    const int32_t* cl = A.cols[k];
-    const float* va = A.vals[k];
-    const float* dv = A.dinv[k];
-    const float* b = A.b[k];
-    float* t = A.t[k];
-    for (int64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-      float sacc[NR];
-#pragma unroll
-      for (int q = 0; q < NR; ++q) sacc[q] = 0.0f;
-      for (int e = rp[i]; e < rp[i + 1]; ++e) {
-        const int32_t jn = cl[e];
-        const float w = va[e] * (kOmega * dv[jn]);
-#pragma unroll
-        for (int q = 0; q < NR; ++q) sacc[q] += w * b[NR * jn + q];
-      }
-#pragma unroll
-      for (int q = 0; q < NR; ++q) t[NR * i + q] = b[NR * i + q] - sacc[q];
-    }
-    __syncthreads();
-    const int64_t R0 = A.chart_row[k + 1][c], R1 = A.chart_row[k + 1][c + 1];
-    const int64_t* ro = A.roff[k];
-    const int32_t* rc = A.rc[k];
-    const float* rv = A.rv[k];
-    float* bc = A.b[k + 1];
-    for (int64_t I = R0 + threadIdx.x; I < R1; I += blockDim.x) {
-      float sacc[NR];
-#pragma unroll
-      for (int q = 0; q < NR; ++q) sacc[q] = 0.0f;
-      for (int64_t e = ro[I]; e < ro[I + 1]; ++e) {
-        const int32_t jn = rc[e];
-#pragma unroll
-        for (int q = 0; q < NR; ++q) sacc[q] += rv[e] * t[NR * jn + q];
-      }
-#pragma unroll
-      for (int q = 0; q < NR; ++q) bc[NR * I + q] = sacc[q];
-    }
-    __syncthreads();
-  }
-  {  // the last level: the dense inverse, or x = D^-1 b where the aggregation stalled
-    const int64_t r0 = A.chart_row[f][c];
-    const int m = (int)(A.chart_row[f][c + 1] - r0);
-    const float* b = A.b[f];
-    float* x = A.x[f];
-    if (m > kDirect) {
-      const float* dv = A.dinv[f];
-      for (int r = threadIdx.x; r < m; r += blockDim.x)
-#pragma unroll
-        for (int q = 0; q < NR; ++q) x[NR * (r0 + r) + q] = dv[r0 + r] * b[NR * (r0 + r) + q];
-    } else {
-      const float* Ainv = A.fac + A.fac_off[c];
-      for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        float sacc[NR];
-#pragma unroll
-        for (int q = 0; q < NR; ++q) sacc[q] = 0.0f;
-        for (int jn = 0; jn < m; ++jn) {
-          const float a = Ainv[jn * m + i];
-#pragma unroll
-          for (int q = 0; q < NR; ++q) sacc[q] += a * b[NR * (r0 + jn) + q];
-        }
-#pragma unroll
-        for (int q = 0; q < NR; ++q) x[NR * (r0 + i) + q] = sacc[q];
-      }
-    }
-    __syncthreads();
-  }
-  for (int k = f - 1; k >= kt; --k) {  // up: y = w D^-1 b + alpha_c x_c[agg]; x = y + w D^-1 (b - A y)
-    const int64_t r0 = A.chart_row[k][c], r1 = A.chart_row[k][c + 1];
-    const int32_t* rp = A.rp[k];
-    const int32_t* cl = A.cols[k];
-    const float* va = A.vals[k];
-    const float* dv = A.dinv[k];
-    const float* b = A.b[k];
-    const int32_t* ag = A.agg[k];
-    const float* xc = A.x[k + 1];
-    float* x = A.x[k];
-    const float ac = A.alpha_c;
-    for (int64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-      float sacc[NR];
-#pragma unroll
-      for (int q = 0; q < NR; ++q) sacc[q] = 0.0f;
-      for (int e = rp[i]; e < rp[i + 1]; ++e) {
-        const int32_t jn = cl[e];
-        const float wd = kOmega * dv[jn];
-        const int32_t aj = ag[jn];
-#pragma unroll
-        for (int q = 0; q < NR; ++q) sacc[q] += va[e] * (wd * b[NR * jn + q] + ac * xc[NR * aj + q]);
-      }
-      const float wi = kOmega * dv[i];
-      const int32_t ai = ag[i];
-#pragma unroll
-      for (int q = 0; q < NR; ++q) {
-        const float yi = wi * b[NR * i + q] + ac * xc[NR * ai + q];
-        x[NR * i + q] = yi + wi * (b[NR * i + q] - sacc[q]);
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// done2[c] = done[c] or c takes the per-chart coarse tail (the batch-wide kernels of the
-// tail's levels skip it)
-__global__ void k_done_or_small(int64_t n, const int32_t* __restrict__ done, const uint8_t* __restrict__ small,
-                                int32_t* __restrict__ done2) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < n) done2[c] = (done[c] || small[c]) ? 1 : 0;
-}
-
 }  // namespace
 
 // ---------------------------------------------------------------- host side
@@ -1784,11 +1642,6 @@ struct AmgHierarchy {
   int k_levels = 0;  // top levels applied in the K-form (two coarse corrections with steplengths)
   int* err = nullptr;  // a staged tile's bounded wait ran out
   int64_t spin_limit = 0;
-  // the per-chart coarse tail (k_vtail_chart): from level tail_kt down for the charts small[c]
-  int tail_kt = -1;
-  uint8_t* small = nullptr;
-  int32_t* done2 = nullptr;
-  TailArgs tail{};
 };
 
 namespace {
@@ -1955,74 +1808,6 @@ void stage_setup(Ctx& ctx, AmgHierarchy* H) {
   const char* le = std::getenv("RUV_SPIN_LIMIT");
   H->spin_limit = le ? std::max<int64_t>(1, std::atoll(le)) : (int64_t(1) << 22);
   L.stage_smem = bytes;
-}
-
-// The per-chart coarse tail (k_vtail_chart) from the first tentative level below level 0,
-// for every chart that continues below that level with at most kTailRows rows there (all of
-// the disk workload's charts; a height field's large chart keeps the batch-wide kernels).
-// RUV_AMG_TAIL=0: batch-wide kernels for every level.  Not with the K-cycle.
-constexpr int64_t kTailRows = 4096;
-void tail_setup(Ctx& ctx, AmgHierarchy* H) {
-  H->tail_kt = -1;
-  const char* e = std::getenv("RUV_AMG_TAIL");
-  const int K = (int)H->lv.size();
-  const int kt = std::max(H->sa_levels, 1);
-  if ((e && e[0] == '0') || H->k_levels > 0 || kt >= K - 1) return;
-  const int64_t NC = H->n_charts;
-  std::vector<uint8_t> small(NC, 0);
-  int64_t n_small = 0;
-  for (int64_t c = 0; c < NC; ++c) {
-    const int64_t rows = H->lv[kt].h_chart_row[c + 1] - H->lv[kt].h_chart_row[c];
-    if (H->h_final[c] > kt && rows <= kTailRows) {
-      small[c] = 1;
-      ++n_small;
-    }
-  }
-  if (n_small == 0) return;
-  cudaStream_t s = ctx.stream;
-  H->small = ctx.ws.get<uint8_t>("amg.tail.small", NC);
-  H->done2 = ctx.ws.get<int32_t>("amg.tail.done2", NC);
-  RUV_CUDA(cudaMemcpyAsync(H->small, small.data(), NC, cudaMemcpyHostToDevice, s));
-  std::vector<const int32_t*> rp(K), cl(K), ag(K), rc(K);
-  std::vector<const float*> va(K), rv(K);
-  std::vector<float*> t(K);
-  std::vector<const int64_t*> ro(K);
-  for (int k = 0; k < K; ++k) {
-    const AmgLevelDev& L = H->lv[k];
-    rp[k] = L.rp;
-    cl[k] = L.cols;
-    va[k] = L.vals;
-    t[k] = L.t;
-    ag[k] = L.agg;
-    ro[k] = L.roff;
-    rc[k] = L.rc;
-    rv[k] = L.rv;
-  }
-  auto up = [&](const char* name, const auto& v) {
-    using T = typename std::remove_reference<decltype(v)>::type::value_type;
-    T* d = ctx.ws.get<T>(std::string("amg.tail.") + name, K);
-    RUV_CUDA(cudaMemcpyAsync(d, v.data(), sizeof(T) * K, cudaMemcpyHostToDevice, s));
-    return d;
-  };
-  TailArgs& A = H->tail;
-  A.chart_row = H->d_lvl_chart_row;
-  A.rp = up("rp", rp);
-  A.cols = up("cols", cl);
-  A.vals = up("vals", va);
-  A.dinv = H->d_lvl_dinv;
-  A.b = H->d_lvl_b;
-  A.x = H->d_lvl_x;
-  A.t = up("t", t);
-  A.agg = up("agg", ag);
-  A.roff = up("roff", ro);
-  A.rc = up("rc", rc);
-  A.rv = up("rv", rv);
-  A.final_lvl = H->final_lvl;
-  A.fac_off = H->fac_off;
-  A.fac = H->fac;
-  A.alpha_c = H->alpha_c;
-  RUV_CUDA(cudaStreamSynchronize(s));  // the host tables go out of scope
-  H->tail_kt = kt;
 }
 
 AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string& info) {
@@ -2428,7 +2213,6 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   }
   cudaEventDestroy(t_setup0);
   stage_setup(ctx, H.get());
-  tail_setup(ctx, H.get());
   return H.release();
 }
 
@@ -2514,27 +2298,18 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
   const int K = (int)H->lv.size();
   const int B = kAmgThreads;
   int launches = 0;
-  // the small charts' levels from tail_kt down run in k_vtail_chart; the batch-wide kernels of
-  // those levels (and the direct solves) skip them through done2
-  const bool tail = H->tail_kt >= 0 && k0 <= H->tail_kt;
-  if (tail) {
-    k_done_or_small<<<div_up(H->n_charts, 256), 256, 0, s>>>(H->n_charts, done, H->small, H->done2);
-    ++launches;
-  }
-  auto dk = [&](int k) -> const int32_t* { return tail && k >= H->tail_kt ? H->done2 : done; };
   for (int k = k0; k + 1 < K; ++k) {
     AmgLevelDev& L = H->lv[k];
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
     float* xpre = L.smoothed ? L.x : nullptr;  // the tentative cycle re-forms it on the way up
-    const int32_t* done_k = dk(k);
 #define CALL(X, UU, KK)                                                                                                \
   if (L.stage_smem)                                                                                                    \
     k_smooth_down_st<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, L.stage_smem, s>>>(                                   \
-        L.cont, done_k, L.rp, L.cols, L.c16, L.cbase, L.vals, L.dinv, L.b, xpre, L.t, H->spin_limit, H->err);            \
+        L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, L.dinv, L.b, xpre, L.t, H->spin_limit, H->err);            \
   else                                                                                                                 \
-    k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done_k, L.rp, L.cols, L.c16, L.cbase, L.vals, \
+    k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                       L.dinv, L.b, xpre, L.t)
     if (L.c16 && L.rowrel) {
       constexpr int NW = 2;
@@ -2550,28 +2325,22 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
     ++launches;
     if (C.all.n == 0) continue;
     const int lr = lanes_for(C.n ? (double)L.n_pnnz / (double)C.n : 1.0);
-#define CALL(X, UU, KK) k_restrict<NR, X, UU, KK><<<(unsigned)C.all.n, B, 0, s>>>(C.all, done_k, L.roff, L.rc, L.rv, L.t, C.b)
+#define CALL(X, UU, KK) k_restrict<NR, X, UU, KK><<<(unsigned)C.all.n, B, 0, s>>>(C.all, done, L.roff, L.rc, L.rv, L.t, C.b)
     RUV_LPR_SWITCH(lr, CALL)
 #undef CALL
     ++launches;
   }
-  k_direct_solve<NR><<<(unsigned)H->n_charts, kDirect, 0, s>>>(H->final_lvl, tail ? H->done2 : done,
-                                                               H->d_lvl_chart_row, H->d_lvl_b, H->d_lvl_x, H->d_lvl_dinv,
-                                                               H->fac_off, H->fac, k0, kMaxLevels);
+  k_direct_solve<NR><<<(unsigned)H->n_charts, kDirect, 0, s>>>(H->final_lvl, done, H->d_lvl_chart_row, H->d_lvl_b,
+                                                               H->d_lvl_x, H->d_lvl_dinv, H->fac_off, H->fac, k0, kMaxLevels);
   ++launches;
-  if (tail) {
-    k_vtail_chart<NR><<<(unsigned)H->n_charts, kAmgThreads, 0, s>>>(H->tail, done, H->small, H->tail_kt);
-    ++launches;
-  }
   for (int k = K - 2; k >= k0; --k) {
     AmgLevelDev& L = H->lv[k];
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
     const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
-    const int32_t* done_k = dk(k);
     if (!L.smoothed) {
 #define CALL(X, UU, KK)                                                                                                \
-  k_smooth_up_t<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done_k, L.rp, L.cols, L.c16, L.cbase, L.vals, \
+  k_smooth_up_t<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                     L.dinv, L.b, L.agg, C.x, H->alpha_c, L.x)
       if (L.c16 && L.rowrel) {
         constexpr int NW = 2;
@@ -2589,15 +2358,15 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
     }
     const int lp = lanes_for(L.n ? (double)L.n_pnnz / (double)L.n : 1.0);
 #define CALL(X, UU, KK)                                                                                                  \
-  k_prolong_add<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done_k, L.poff, L.pc, L.pv, C.x, L.x, L.y, 1.0f)
+  k_prolong_add<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.poff, L.pc, L.pv, C.x, L.x, L.y, 1.0f)
     RUV_LPR_SWITCH(lp, CALL)
 #undef CALL
 #define CALL(X, UU, KK)                                                                                              \
   if (L.stage_smem)                                                                                                  \
     k_smooth_up_st<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, L.stage_smem, s>>>(                                   \
-        L.cont, done_k, L.rp, L.cols, L.c16, L.cbase, L.vals, L.dinv, L.b, L.y, L.x, H->spin_limit, H->err);           \
+        L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, L.dinv, L.b, L.y, L.x, H->spin_limit, H->err);           \
   else                                                                                                               \
-    k_smooth_up<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done_k, L.rp, L.cols, L.c16, L.cbase, L.vals, \
+    k_smooth_up<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                     L.dinv, L.b, L.y, L.x)
     if (L.c16 && L.rowrel) {
       constexpr int NW = 2;

@@ -384,31 +384,6 @@ def test_pinned_inputs_bitwise(monkeypatch, kernel):
     assert [s.cg_iters for s in st_a] == [stats[c].cg_iters for c in range(pb.n_charts)]
 
 
-@pytest.mark.parametrize("precond", [R.Precond.AMG_SA, R.Precond.AMG])
-def test_coarse_tail_matches_batch_wide_levels(monkeypatch, precond):
-    """The coarse levels of the small charts run in one CTA per chart (the default) against
-    the batch-wide level kernels (RUV_AMG_TAIL=0): the same smoother, restriction, coarse
-    solve and prolongation with row sums in another order, so every chart converges in about
-    the same iterations to the same UVs.  The batches: 24 disks of up to 20k triangles (every
-    chart in the tail), and 16 disks of up to 300k triangles (charts of 90-112k vertices keep
-    the batch-wide kernels beside the small ones in the same cycle)."""
-    vo, to, p3, tr = W.disks(24, t_min=200, t_max=20000, seed=79)
-    C = R.prepare_patches(vo, to, p3, tr)
-    vo, to, p3, tr = W.disks(16, t_min=500, t_max=300000, seed=79)
-    Cm = R.prepare_patches(vo, to, p3, tr)
-    ctx = R.Context(0)
-    opts = R.UnfoldOptions(precond=precond, precision=R.Precision.MIXED)
-    for charts in (C, Cm):
-        monkeypatch.setenv("RUV_AMG_TAIL", "0")
-        wide = R.unfold_charts(ctx, charts, opts)
-        monkeypatch.delenv("RUV_AMG_TAIL", raising=False)
-        tail = R.unfold_charts(ctx, charts, opts)
-        for a, b in zip(wide, tail):
-            assert a.status == b.status == R.Status.OK
-            assert abs(a.cg_iters - b.cg_iters) <= 2
-            assert O.uv_error(a.uv, b.uv) <= 1e-9
-
-
 def test_staged_smoothers_bitwise(monkeypatch):
     """Level 0's AMG smoothers with their tiles staged into shared memory by bulk copies
     (RUV_AMG_STAGE=1) run the same row loop: bitwise the same UVs and iterations."""
