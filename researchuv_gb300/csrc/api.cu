@@ -85,18 +85,25 @@ __global__ void k_h2d(const unsigned char* __restrict__ src, unsigned char* __re
   if (tid < tail) dst[head + 16 * n16 + tid] = src[head + 16 * n16 + tid];
 }
 
-// The copy kernel's grid: RUV_H2D_CTAS (default 1) CTAs of 256 threads per SM -- four 16-byte
-// loads in flight per thread already cover the host link's latency, and the fewer SMs the
-// copy holds the more the assembly kernels it overlaps keep.
+// The copy kernel's grid: RUV_H2D_CTAS (default 1) CTAs of 256 threads per SM, or
+// RUV_H2D_GRID CTAs in all -- four 16-byte loads in flight per thread already cover the host
+// link's latency, and the fewer SMs the copy holds the more the assembly kernels it overlaps
+// keep.
 unsigned h2d_grid(size_t n16) {
-  static const int per_sm = [] {
-    const char* e = std::getenv("RUV_H2D_CTAS");
-    return e ? std::max(1, std::atoi(e)) : 1;
-  }();
+  const char* e = std::getenv("RUV_H2D_CTAS");
+  const char* g = std::getenv("RUV_H2D_GRID");
+  const int per_sm = e ? std::max(1, std::atoi(e)) : 1;
   int dev_id = 0, sms = 0;
   RUV_CUDA(cudaGetDevice(&dev_id));
   RUV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
-  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, div_up((int64_t)n16, 256)));
+  const int64_t want = g ? std::max(1, std::atoi(g)) : (int64_t)sms * per_sm;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, div_up((int64_t)n16, 256)));
+}
+
+// RUV_H2D_KERNEL=0 (read on every copy): host copies through cudaMemcpyAsync only
+bool copies_by_engines() {
+  const char* e = std::getenv("RUV_H2D_KERNEL");
+  return e && e[0] == '0';
 }
 
 // n bytes host -> device on stream st.  Where the host buffer is page-locked and mapped (and
@@ -106,10 +113,7 @@ unsigned h2d_grid(size_t n16) {
 // mapped buffer held 211 GB/s in every repetition.  RUV_H2D_KERNEL=0: always cudaMemcpyAsync.
 void h2d(Ctx& c, void* dev, const void* host, size_t bytes, cudaStream_t st) {
   if (bytes == 0) return;
-  static const bool off = [] {
-    const char* e = std::getenv("RUV_H2D_KERNEL");
-    return e && e[0] == '0';
-  }();
+  const bool off = copies_by_engines();
   cudaPointerAttributes a{};
   const void* src = nullptr;
   if (!off) {
@@ -137,10 +141,7 @@ void h2d(Ctx& c, void* dev, const void* host, size_t bytes, cudaStream_t st) {
 // host buffer's device mapping where it is page-locked and mapped, else cudaMemcpyAsync).
 void d2h(Ctx& c, void* host, const void* dev, size_t bytes, cudaStream_t st) {
   if (bytes == 0) return;
-  static const bool off = [] {
-    const char* e = std::getenv("RUV_H2D_KERNEL");
-    return e && e[0] == '0';
-  }();
+  const bool off = copies_by_engines();
   cudaPointerAttributes a{};
   void* dst = nullptr;
   if (!off) {
@@ -176,6 +177,27 @@ int worst(int a, int b) {
   if (a == RUV_OK) return b;
   if (b == RUV_OK) return a;
   return a > b ? a : b;
+}
+
+// the context's events of the split upload
+std::vector<cudaEvent_t*> copy_events(Ctx& c) {
+  std::vector<cudaEvent_t*> e{&c.ev_core, &c.ev_pins, &c.ev_rest};
+  for (cudaEvent_t& p : c.ev_part) e.push_back(&p);
+  return e;
+}
+
+// Orders the resident batch's side-stream copies that the assembly has not waited for yet
+// before everything enqueued next on the main stream (a path that failed or returned before
+// the assembly, or before its last wait).
+void order_pending_copies(Ctx& c) {
+  DevBatch& bt = c.resident;
+  std::vector<cudaEvent_t*> pending{&bt.pins_ready, &bt.rest_ready};
+  for (cudaEvent_t& p : bt.part_ready) pending.push_back(&p);
+  for (cudaEvent_t* e : pending)
+    if (*e) {
+      cudaStreamWaitEvent(c.stream, *e, 0);
+      *e = nullptr;
+    }
 }
 
 }  // namespace
@@ -221,14 +243,14 @@ ruv_status ruv_ctx_create(ruv_ctx** out, int32_t device) {
   if (const char* e = std::getenv("RUV_TILE_ROWS")) ctx->c.tile_rows = std::max(32, std::atoi(e));
   if (cudaSetDevice(device) != cudaSuccess) return RUV_ERR_NO_DEVICE;
   if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) return RUV_ERR_LAUNCH;
-  if (cudaStreamCreateWithFlags(&ctx->c.side, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->c.ev_core, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->c.ev_second, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->c.ev_rest, cudaEventDisableTiming) != cudaSuccess) {
+  bool ok = cudaStreamCreateWithFlags(&ctx->c.side, cudaStreamNonBlocking) == cudaSuccess;
+  for (cudaEvent_t* e : copy_events(ctx->c))
+    ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
     cudaStreamDestroy(ctx->c.stream);
     if (ctx->c.side) cudaStreamDestroy(ctx->c.side);
-    if (ctx->c.ev_core) cudaEventDestroy(ctx->c.ev_core);
-    if (ctx->c.ev_second) cudaEventDestroy(ctx->c.ev_second);
+    for (cudaEvent_t* e : copy_events(ctx->c))
+      if (*e) cudaEventDestroy(*e);
     return RUV_ERR_LAUNCH;
   }
   *out = ctx.release();
@@ -243,9 +265,7 @@ void ruv_ctx_destroy(ruv_ctx* ctx) {
   ctx->c.ws.release();
   cudaStreamDestroy(ctx->c.stream);
   cudaStreamDestroy(ctx->c.side);
-  cudaEventDestroy(ctx->c.ev_core);
-  cudaEventDestroy(ctx->c.ev_second);
-  cudaEventDestroy(ctx->c.ev_rest);
+  for (cudaEvent_t* e : copy_events(ctx->c)) cudaEventDestroy(*e);
   delete ctx;
 }
 
@@ -427,11 +447,12 @@ ruv_status ruv_amg_export(ruv_ctx* ctx, int32_t n, const int32_t* row_ptr, const
 }
 
 namespace {
-// The batch upload.  With `overlap` (the one-call solve) only the triangles and positions of
-// the charts holding the first half of the triangles go on the main stream; the other half
-// and then the arrays the assembly reads only after its cotangent pass (pin flags, pin
-// targets, tangent-frame positions) follow on the side stream, under the first kernels.
-// bt.second_ready and bt.rest_ready order them before their first use.
+// The batch upload.  With `overlap` (the one-call solve) the triangles and positions go in
+// parts split at chart boundaries (about equal triangle counts; RUV_UPLOAD_PARTS, default 8):
+// the first part on the main stream, the others and then the arrays the assembly reads only
+// after its cotangent pass (pin flags, pin targets, tangent-frame positions) on the side
+// stream, under the kernels of the parts before them.  bt.part_ready, bt.pins_ready and
+// bt.rest_ready order them before their first use.
 ruv_status upload_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, bool overlap);
 }  // namespace
 
@@ -453,6 +474,7 @@ ruv_status upload_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, bool overlap) {
     Ctx& c = ctx->c;
     c.have_batch = false;
     c.have_uv = false;
+    order_pending_copies(c);
     DevBatch& bt = c.resident;
     bt = DevBatch();
     bt.n_charts = NC;
@@ -462,47 +484,63 @@ ruv_status upload_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, bool overlap) {
     bt.h_tri_off.assign(in->tri_off, in->tri_off + NC + 1);
     bt.vert_off = upload(c, "in.vert_off", in->vert_off, NC + 1);
     bt.tri_off = upload(c, "in.tri_off", in->tri_off, NC + 1);
-    // the split: the first chart boundary at or past half of the triangles
-    const int64_t cs = overlap && NC > 1
-                           ? std::min<int64_t>(NC - 1, (int64_t)(std::lower_bound(in->tri_off, in->tri_off + NC + 1,
-                                                                                  NT / 2) - in->tri_off))
-                           : NC;
-    const int64_t vs = in->vert_off[cs], ts = in->tri_off[cs];
     bt.p3 = c.ws.get<double>("in.p3", 3 * NV);
     bt.tris = c.ws.get<int32_t>("in.tris", 3 * NT);
-    if (vs > 0) h2d(c, bt.p3, in->p3, sizeof(double) * 3 * vs, c.stream);
-    if (ts > 0) h2d(c, bt.tris, in->tris, sizeof(int32_t) * 3 * ts, c.stream);
+    // part k: charts [cs[k], cs[k + 1]), cs[k] the first chart boundary at or past k / P of
+    // the triangles
+    const char* parts_env = std::getenv("RUV_UPLOAD_PARTS");
+    const int env_parts = parts_env ? std::atoi(parts_env) : 8;
+    const int P = overlap ? (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)env_parts, DevBatch::kMaxParts, NC}))
+                          : 1;
+    std::vector<int64_t> cs(P + 1, NC);
+    cs[0] = 0;
+    for (int k = 1; k < P; ++k)
+      cs[k] = std::max(cs[k - 1], (int64_t)(std::lower_bound(in->tri_off, in->tri_off + NC + 1, NT * k / P) -
+                                            in->tri_off));
+    auto copy_part = [&](int k, cudaStream_t st) {
+      const int64_t v0 = in->vert_off[cs[k]], v1 = in->vert_off[cs[k + 1]];
+      const int64_t t0 = in->tri_off[cs[k]], t1 = in->tri_off[cs[k + 1]];
+      if (v1 > v0) h2d(c, bt.p3 + 3 * v0, in->p3 + 3 * v0, sizeof(double) * 3 * (v1 - v0), st);
+      if (t1 > t0) h2d(c, bt.tris + 3 * t0, in->tris + 3 * t0, sizeof(int32_t) * 3 * (t1 - t0), st);
+    };
+    copy_part(0, c.stream);
     cudaStream_t rest = c.stream;
     if (overlap) {  // after everything already on the main stream, then in parallel with it
       RUV_CUDA(cudaEventRecord(c.ev_core, c.stream));
       RUV_CUDA(cudaStreamWaitEvent(c.side, c.ev_core, 0));
       rest = c.side;
     }
-    struct SideGuard {  // on every exit: the side-stream copies are ordered by the events
+    struct SideGuard {  // an exit before every side copy was enqueued: the main stream waits
       Ctx& c;
-      DevBatch& bt;
-      bool on, second;
+      bool on;
       ~SideGuard() {
         if (!on) return;
-        if (!second) {  // (an exit before the second half was enqueued)
-          cudaEventRecord(c.ev_second, c.side);
-          bt.second_ready = c.ev_second;
-        }
         cudaEventRecord(c.ev_rest, c.side);
-        bt.rest_ready = c.ev_rest;
+        cudaStreamWaitEvent(c.stream, c.ev_rest, 0);
+        c.resident.n_parts = 0;
+        for (cudaEvent_t& e : c.resident.part_ready) e = nullptr;
+        c.resident.pins_ready = c.resident.rest_ready = nullptr;
       }
-    } guard{c, bt, overlap, false};
-    if (NV > vs) h2d(c, bt.p3 + 3 * vs, in->p3 + 3 * vs, sizeof(double) * 3 * (NV - vs), rest);
-    if (NT > ts) h2d(c, bt.tris + 3 * ts, in->tris + 3 * ts, sizeof(int32_t) * 3 * (NT - ts), rest);
-    if (overlap) {
-      RUV_CUDA(cudaEventRecord(c.ev_second, c.side));
-      bt.second_ready = c.ev_second;
-      bt.split_tri = ts;
-      guard.second = true;
+    } guard{c, overlap};
+    for (int k = 1; k < P; ++k) {
+      copy_part(k, rest);
+      RUV_CUDA(cudaEventRecord(c.ev_part[k], rest));
+      bt.part_ready[k] = c.ev_part[k];
     }
     bt.pinned = upload(c, "in.pinned", in->pinned, NV, rest);
+    if (overlap) {
+      RUV_CUDA(cudaEventRecord(c.ev_pins, rest));
+      bt.pins_ready = c.ev_pins;
+    }
     bt.pin_uv = upload(c, "in.pin_uv", in->pin_uv, 2 * NV, rest);
     bt.p2 = upload(c, "in.p2", in->p2, 2 * NV, rest);
+    if (overlap) {
+      RUV_CUDA(cudaEventRecord(c.ev_rest, rest));
+      bt.rest_ready = c.ev_rest;
+      bt.n_parts = P;
+      for (int k = 0; k <= P; ++k) bt.part_tri[k] = in->tri_off[cs[k]];
+      guard.on = false;
+    }
     c.have_batch = true;
     return RUV_OK;
   });
@@ -600,11 +638,7 @@ ruv_status ruv_lscm_solve_batch(ruv_ctx* ctx, const ruv_lscm_batch* in, const ru
   ruv_status solved = RUV_OK;
   if (in->vert_off[in->n_charts] > 0 && !uv_out) solved = fail(ctx, RUV_ERR_BAD_INPUT, "null uv_out");
   else solved = ruv_lscm_solve_resident(ctx, opts, stats);
-  for (cudaEvent_t* e : {&ctx->c.resident.second_ready, &ctx->c.resident.rest_ready})
-    if (*e) {  // a path that never reached the assembly: order the copies here
-      cudaStreamWaitEvent(ctx->c.stream, *e, 0);
-      *e = nullptr;
-    }
+  order_pending_copies(ctx->c);  // (a path that returned before the assembly's waits)
   if (solved != RUV_OK && solved != RUV_ERR_NOT_CONVERGED && solved != RUV_ERR_BREAKDOWN) return solved;
   std::string msg = ctx->c.last_error;
   if (!ctx->c.have_uv) return solved;

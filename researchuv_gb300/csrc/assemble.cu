@@ -518,14 +518,15 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   double* sq = ws.get<double>("asm.sq", 3 * NT);
   bt.tri_g = tri_g;
   bt.cot = cot;
-  // triangles [0, split) first; with a split upload the rest of the triangles and positions
-  // are still being copied on the side stream until bt.second_ready
-  const int64_t split = bt.second_ready ? std::min<int64_t>(std::max<int64_t>(bt.split_tri, 0), NT) : NT;
-  for (int part = 0; part < 2; ++part) {
-    const int64_t t0 = part == 0 ? 0 : split, t1 = part == 0 ? split : NT;
-    if (part == 1 && bt.second_ready) {
-      RUV_CUDA(cudaStreamWaitEvent(s, bt.second_ready, 0));
-      bt.second_ready = nullptr;
+  // part by part, as a split upload delivers them (one part [0, NT) otherwise): each part's
+  // triangles and positions may still be being copied on the side stream until its event
+  const int n_parts = std::min(std::max(bt.n_parts, 1), DevBatch::kMaxParts);
+  for (int part = 0; part < n_parts; ++part) {
+    const int64_t t0 = bt.n_parts > 0 ? std::min(std::max<int64_t>(bt.part_tri[part], 0), NT) : 0;
+    const int64_t t1 = bt.n_parts > 0 ? std::min(std::max<int64_t>(bt.part_tri[part + 1], 0), NT) : NT;
+    if (bt.part_ready[part]) {
+      RUV_CUDA(cudaStreamWaitEvent(s, bt.part_ready[part], 0));
+      bt.part_ready[part] = nullptr;
     }
     if (t1 <= t0) continue;
     k_globalize<<<div_up(t1 - t0, B), B, 0, s>>>(bt.tris, bt.tri_off, bt.vert_off, NC, t0, t1, tri_g, bad);
@@ -535,10 +536,10 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
     count_launches(1);
     RUV_LAUNCH_CHECK();
   }
-  // free-row numbering (the first use of the pin flags, pin targets and frame positions)
-  if (bt.rest_ready) {
-    RUV_CUDA(cudaStreamWaitEvent(s, bt.rest_ready, 0));
-    bt.rest_ready = nullptr;
+  // free-row numbering (the first use of the pin flags)
+  if (bt.pins_ready) {
+    RUV_CUDA(cudaStreamWaitEvent(s, bt.pins_ready, 0));
+    bt.pins_ready = nullptr;
   }
   uint8_t* fr = ws.get<uint8_t>("asm.free", NV);
   bt.row_of = ws.get<int64_t>("asm.row_of", NV + 1);
@@ -617,6 +618,11 @@ void assemble_lscm(Ctx& ctx, DevBatch& bt, DevSystem& sys, double angle_mix) {
   k_i64_to_i32<<<div_up(NR + 1, B), B, 0, s>>>(rp64, NR + 1, sys.row_ptr);
   count_launches(1);
   RUV_LAUNCH_CHECK();
+  // the fill: the first use of the pin targets and frame positions
+  if (bt.rest_ready) {
+    RUV_CUDA(cudaStreamWaitEvent(s, bt.rest_ready, 0));
+    bt.rest_ready = nullptr;
+  }
   if (NV > 0) {
     if (mix_b != 0.0)
       k_rows<1, true><<<div_up(NV, 128), 128, 0, s>>>(NV, bt.pinned, bt.row_of, rec_off, rec, cot, sq, bt.p3, bt.p2,

@@ -118,13 +118,16 @@ struct DevBatch {
   uint8_t* pinned = nullptr;
   double* pin_uv = nullptr;     // 2 * n_verts
   double* p2 = nullptr;         // 2 * n_verts
-  // set when pinned / pin_uv / p2 are still being copied on Ctx::side: the assembly waits
-  // for it before its first use of them
+  // The one-call entry's split upload (n_parts > 0): triangles [part_tri[k], part_tri[k + 1])
+  // and their charts' positions are still being copied on Ctx::side until part_ready[k]
+  // (nullptr once on the device), the pin flags until pins_ready, the pin targets and frame
+  // positions until rest_ready.  The assembly waits for each before its first use.
+  static constexpr int kMaxParts = 16;
+  int n_parts = 0;
+  int64_t part_tri[kMaxParts + 1] = {};
+  cudaEvent_t part_ready[kMaxParts] = {};
+  cudaEvent_t pins_ready = nullptr;
   cudaEvent_t rest_ready = nullptr;
-  // set when the triangles from split_tri on (and their charts' positions) are still being
-  // copied on Ctx::side: the assembly's first passes run on [0, split_tri) meanwhile
-  cudaEvent_t second_ready = nullptr;
-  int64_t split_tri = 0;
   // produced by assembly
   int64_t* row_of = nullptr;    // n_verts + 1: exclusive count of free vertices (row id if free)
   int32_t* row_vert = nullptr;  // n_rows: packed vertex of each row
@@ -177,7 +180,8 @@ struct Ctx {
   // a second stream for host-to-device copies that overlap the first assembly kernels, and
   // the events ordering it against `stream`
   cudaStream_t side = nullptr;
-  cudaEvent_t ev_core = nullptr, ev_second = nullptr, ev_rest = nullptr;
+  cudaEvent_t ev_core = nullptr, ev_pins = nullptr, ev_rest = nullptr;
+  cudaEvent_t ev_part[DevBatch::kMaxParts] = {};
   Workspace ws;
   PinnedHost pinned;
   std::string last_error;

@@ -361,12 +361,15 @@ def test_bulk_copy_spmv_wait_is_bounded(monkeypatch):
     assert st == R.Status.OK
 
 
-@pytest.mark.parametrize("kernel", ["1", "0"])
-def test_pinned_inputs_bitwise(monkeypatch, kernel):
+@pytest.mark.parametrize("kernel,parts", [("1", None), ("0", None), ("1", "1"), ("1", "5"), ("0", "16")])
+def test_pinned_inputs_bitwise(monkeypatch, kernel, parts):
     """The one-call entry with its inputs in page-locked host memory (copied by the SMs over
     the buffers' device mapping; RUV_H2D_KERNEL=0: by cudaMemcpyAsync) gives bitwise the UVs
-    and statistics of the same batch from pageable memory, split upload included."""
+    and statistics of the same batch from pageable memory and of the resident upload, for
+    any number of upload parts (RUV_UPLOAD_PARTS; 16 is more than the 12 charts)."""
     monkeypatch.setenv("RUV_H2D_KERNEL", kernel)
+    if parts is not None:
+        monkeypatch.setenv("RUV_UPLOAD_PARTS", parts)
     vo, to, p3, tr = W.disks(12, t_min=200, t_max=20000, seed=67)
     C = R.prepare_patches(vo, to, p3, tr)
     nv = int(C.i64("chart.vert_off")[-1])
@@ -382,6 +385,12 @@ def test_pinned_inputs_bitwise(monkeypatch, kernel):
     assert s_a == R.Status.OK
     assert np.array_equal(uv_a, out)
     assert [s.cg_iters for s in st_a] == [stats[c].cg_iters for c in range(pb.n_charts)]
+    # the resident path (one upload on the main stream, no parts)
+    ctx.check(L.ruv_lscm_upload(ctx.h, ctypes.byref(pb)), "upload")
+    ctx.check(L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(opts.to_c()), stats), "resident solve")
+    res = R.pinned_empty(ctx, (nv, 2), np.float64)
+    ctx.check(L.ruv_lscm_download_uv(ctx.h, res.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "download")
+    assert np.array_equal(uv_a, res)
 
 
 def test_staged_smoothers_bitwise(monkeypatch):
