@@ -85,18 +85,18 @@ __global__ void k_h2d(const unsigned char* __restrict__ src, unsigned char* __re
   if (tid < tail) dst[head + 16 * n16 + tid] = src[head + 16 * n16 + tid];
 }
 
-// The copy kernel's grid: RUV_H2D_CTAS (default 1) CTAs of 256 threads per SM, or
-// RUV_H2D_GRID CTAs in all -- four 16-byte loads in flight per thread already cover the host
-// link's latency, and the fewer SMs the copy holds the more the assembly kernels it overlaps
-// keep.
-unsigned h2d_grid(size_t n16) {
-  const char* e = std::getenv("RUV_H2D_CTAS");
-  const char* g = std::getenv("RUV_H2D_GRID");
-  const int per_sm = e ? std::max(1, std::atoi(e)) : 1;
+// The copy kernel's grid: `knob` (RUV_H2D_GRID for host-to-device, RUV_D2H_GRID back) CTAs of
+// 256 threads, default a quarter of the SMs.  Four 16-byte loads in flight per thread over 38
+// CTAs (608 KB) already hold the host link's rate, and the SMs the copy leaves free keep the
+// assembly kernels it overlaps at speed: on the 4096-disk one-call solve 38 CTAs ran 0.9 ms
+// faster per call than one CTA per SM (152), 19 CTAs the same as 38; the copy back of the
+// UVs took the same time with 38, 76 or 152 CTAs.
+unsigned h2d_grid(size_t n16, const char* knob = "RUV_H2D_GRID") {
+  const char* g = std::getenv(knob);
   int dev_id = 0, sms = 0;
   RUV_CUDA(cudaGetDevice(&dev_id));
   RUV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
-  const int64_t want = g ? std::max(1, std::atoi(g)) : (int64_t)sms * per_sm;
+  const int64_t want = g ? std::max(1, std::atoi(g)) : std::max(1, sms / 4);
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, div_up((int64_t)n16, 256)));
 }
 
@@ -158,7 +158,7 @@ void d2h(Ctx& c, void* host, const void* dev, size_t bytes, cudaStream_t st) {
   }
   const size_t head = std::min<size_t>(bytes, (16 - (sa & 15)) & 15);
   const size_t n16 = (bytes - head) / 16, tail = bytes - head - 16 * n16;
-  const unsigned grid = h2d_grid(n16);
+  const unsigned grid = h2d_grid(n16, "RUV_D2H_GRID");
   k_h2d<<<grid, 256, 0, st>>>(static_cast<const unsigned char*>(dev), static_cast<unsigned char*>(dst), head, n16,
                               tail);
   count_launches(1);
