@@ -90,7 +90,78 @@ def parse():
                     help="for profiler launch lists: upload, one warm-up solve, then one solve of the workload "
                          "(launch shape from RUV_LPR / RUV_UNROLL / RUV_TILE_ROWS); prints the kernel count "
                          "before the last solve to stderr and nothing else")
+    ap.add_argument("--e2e-sweep", default="",
+                    help="semicolon-separated settings of the one-call entry's copy knobs, each a comma-separated "
+                         "list of NAME=VALUE environment variables (RUV_UPLOAD_PARTS, RUV_H2D_GRID, RUV_D2H_GRID, "
+                         "RUV_H2D_KERNEL): the e2e call timed --steps times per setting after --warmup untimed "
+                         "calls, one JSON line per setting, then the device-resident solve; nothing else runs")
     return ap.parse_args()
+
+
+def e2e_sweep(args, local):
+    """The one-call entry on page-locked buffers under each setting of its copy knobs (read by
+    the library on every call): wall time per call on the host, the call's device and assembly
+    times from its CUDA events, and whether the UVs equal those of the first setting."""
+    import ctypes
+
+    import researchuv_gb300 as R
+
+    cfg, src = workload_config(args.workload)
+    ctx = R.Context(local)
+    prepare(src, ctx)
+    charts, _ = prepare(src, ctx)
+    L = R.lib()
+    nv = int(charts.i64("chart.vert_off")[-1])
+    prec = R.Precision.MIXED if args.precision == "mixed" else R.Precision.FP64
+    pc = {"jacobi": R.Precond.JACOBI, "amg": R.Precond.AMG, "amg_sa": R.Precond.AMG_SA,
+          "none": R.Precond.NONE}[args.precond]
+    opts = R.UnfoldOptions(precision=prec, precond=pc)
+    copts = opts.to_c()
+    batch = charts.batch()
+    stats = (R.RuvChartStat * max(batch.n_charts, 1))()
+    for _ in range(2):
+        R.solve_batch(ctx, batch, opts, nv)
+    R.autotune(ctx, prec, reps=5)
+    pb, _keep = R.pinned_batch(ctx, charts)
+    uv = R.pinned_empty(ctx, (nv, 2), np.float64)
+    ptr = uv.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    first = None
+    for setting in [x for x in args.e2e_sweep.split(";") if x.strip()]:
+        env = dict(kv.split("=", 1) for kv in setting.split(",") if kv.strip())
+        saved = {k: os.environ.get(k) for k in env}
+        os.environ.update(env)
+        for _ in range(max(args.warmup, 1)):
+            ctx.check(L.ruv_lscm_solve_batch(ctx.h, ctypes.byref(pb), ctypes.byref(copts), ptr, stats), "warm-up")
+        wall, dev, asm = [], [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            st = L.ruv_lscm_solve_batch(ctx.h, ctypes.byref(pb), ctypes.byref(copts), ptr, stats)
+            wall.append(1000.0 * (time.perf_counter() - t0))
+            ctx.check(st, "e2e")
+            t = R.last_timings(ctx)
+            dev.append(sum(t[:3]))
+            asm.append(t[0])
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        if first is None:
+            first = uv.copy()
+        print(json.dumps({"setting": env, "wall_ms_mean": round(statistics.mean(wall), 2),
+                          "wall_ms_median": round(statistics.median(wall), 2), "wall_ms_min": round(min(wall), 2),
+                          "device_ms_median": round(statistics.median(dev), 2),
+                          "assembly_ms_median": round(statistics.median(asm), 2),
+                          "uv_equal_to_first": bool(np.array_equal(first, uv))}), flush=True)
+    ctx.check(L.ruv_lscm_upload(ctx.h, ctypes.byref(batch)), "upload")
+    dev, asm = [], []
+    for _ in range(args.steps):
+        ctx.check(L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(copts), stats), "solve")
+        t = R.last_timings(ctx)
+        dev.append(sum(t[:3]))
+        asm.append(t[0])
+    print(json.dumps({"resident_device_ms_median": round(statistics.median(dev), 2),
+                      "resident_assembly_ms_median": round(statistics.median(asm), 2)}), flush=True)
 
 
 def dist():
@@ -801,6 +872,9 @@ def main():
         return
     if args.workload.startswith("sphere"):
         run_adjoint(args, rank, world, local, pg)
+        return
+    if args.e2e_sweep:
+        e2e_sweep(args, local)
         return
     if args.ncu_step:
         import ctypes
