@@ -95,7 +95,68 @@ def parse():
                          "list of NAME=VALUE environment variables (RUV_UPLOAD_PARTS, RUV_H2D_GRID, RUV_D2H_GRID, "
                          "RUV_H2D_KERNEL): the e2e call timed --steps times per setting after --warmup untimed "
                          "calls, one JSON line per setting, then the device-resident solve; nothing else runs")
+    ap.add_argument("--step-sweep", default="",
+                    help="the same form of settings (any RUV_* variable the library reads per call): the "
+                         "device-resident solve timed --steps times per setting after --warmup untimed solves, one "
+                         "JSON line per setting (step, phases, CG iterations); nothing else runs")
     return ap.parse_args()
+
+
+def step_sweep(args, local):
+    """The device-resident solve under each setting of the library's environment variables:
+    device time per step from the call's CUDA events (median, mean), its phases and the CG
+    iterations, and whether the UVs equal those of the first setting."""
+    import ctypes
+
+    import researchuv_gb300 as R
+
+    cfg, src = workload_config(args.workload)
+    ctx = R.Context(local)
+    prepare(src, ctx)
+    charts, _ = prepare(src, ctx)
+    L = R.lib()
+    nv = int(charts.i64("chart.vert_off")[-1])
+    prec = R.Precision.MIXED if args.precision == "mixed" else R.Precision.FP64
+    pc = {"jacobi": R.Precond.JACOBI, "amg": R.Precond.AMG, "amg_sa": R.Precond.AMG_SA,
+          "none": R.Precond.NONE}[args.precond]
+    opts = R.UnfoldOptions(precision=prec, precond=pc)
+    copts = opts.to_c()
+    batch = charts.batch()
+    stats = (R.RuvChartStat * max(batch.n_charts, 1))()
+    for _ in range(2):
+        R.solve_batch(ctx, batch, opts, nv)
+    R.autotune(ctx, prec, reps=5)
+    ctx.check(L.ruv_lscm_upload(ctx.h, ctypes.byref(batch)), "upload")
+    uv = np.empty((nv, 2), np.float64)
+    first = None
+    for setting in [x for x in args.step_sweep.split(";") if x.strip()]:
+        env = dict(kv.split("=", 1) for kv in setting.split(",") if kv.strip())
+        saved = {k: os.environ.get(k) for k in env}
+        os.environ.update(env)
+        for _ in range(max(args.warmup, 1)):
+            ctx.check(L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(copts), stats), "warm-up")
+        dev, ph = [], np.zeros(4)
+        for _ in range(args.steps):
+            ctx.check(L.ruv_lscm_solve_resident(ctx.h, ctypes.byref(copts), stats), "solve")
+            t = R.last_timings(ctx)
+            dev.append(sum(t[:3]))
+            ph += np.array(t)
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        ctx.check(L.ruv_lscm_download_uv(ctx.h, uv.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "download")
+        if first is None:
+            first = uv.copy()
+        its = np.array([stats[c].cg_iters for c in range(batch.n_charts)])
+        ph /= max(args.steps, 1)
+        print(json.dumps({"setting": env, "step_ms_median": round(statistics.median(dev), 3),
+                          "step_ms_mean": round(statistics.mean(dev), 3),
+                          "phase_ms": {"assembly": round(ph[0], 3), "pcg": round(ph[1], 3), "driver": round(ph[2], 3),
+                                       "precond_setup_in_pcg": round(ph[3], 3)},
+                          "cg_iters_max": int(its.max()), "cg_iters_mean": round(float(its.mean()), 2),
+                          "uv_max_abs_diff_to_first": float(np.abs(uv - first).max())}), flush=True)
 
 
 def e2e_sweep(args, local):
@@ -875,6 +936,9 @@ def main():
         return
     if args.e2e_sweep:
         e2e_sweep(args, local)
+        return
+    if args.step_sweep:
+        step_sweep(args, local)
         return
     if args.ncu_step:
         import ctypes

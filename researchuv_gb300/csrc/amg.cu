@@ -2282,6 +2282,25 @@ namespace {
 // typical row in one sweep with two rows in flight (8 independent gathers per lane).
 int lanes_for(double avg) { return avg <= 1.5 ? 1 : avg <= 8 ? 2 : avg <= 16 ? 4 : avg <= 32 ? 8 : 16; }
 
+// The same with a per-level override: the k-th entry of the list in `knob`, entries separated
+// by ',' or '/' (RUV_AMG_LANES for the smoothers, RUV_AMG_TLANES for restriction and
+// prolongation; 0 or a missing entry: from the row length; only 1, 2, 4, 8 and 16 are taken).
+int lanes_at(const char* knob, int k, double avg) {
+  if (const char* e = std::getenv(knob)) {
+    int i = 0;
+    for (const char* q = e; *q; ++i) {
+      const int v = std::atoi(q);
+      if (i == k) {
+        if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) return v;
+        break;
+      }
+      while (*q && *q != ',' && *q != '/') ++q;
+      if (*q) ++q;
+    }
+  }
+  return lanes_for(avg);
+}
+
 #define RUV_LPR_SWITCH(lpr, CALL) \
   switch (lpr) {                   \
     case 1: CALL(1, 4, 2); break;  \
@@ -2302,7 +2321,7 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
     AmgLevelDev& L = H->lv[k];
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
-    const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
+    const int la = lanes_at("RUV_AMG_LANES", k, L.n ? (double)L.nnz / (double)L.n : 1.0);
     float* xpre = L.smoothed ? L.x : nullptr;  // the tentative cycle re-forms it on the way up
 #define CALL(X, UU, KK)                                                                                                \
   if (L.stage_smem)                                                                                                    \
@@ -2324,7 +2343,7 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
 #undef CALL
     ++launches;
     if (C.all.n == 0) continue;
-    const int lr = lanes_for(C.n ? (double)L.n_pnnz / (double)C.n : 1.0);
+    const int lr = lanes_at("RUV_AMG_TLANES", k, C.n ? (double)L.n_pnnz / (double)C.n : 1.0);
 #define CALL(X, UU, KK) k_restrict<NR, X, UU, KK><<<(unsigned)C.all.n, B, 0, s>>>(C.all, done, L.roff, L.rc, L.rv, L.t, C.b)
     RUV_LPR_SWITCH(lr, CALL)
 #undef CALL
@@ -2337,7 +2356,7 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
     AmgLevelDev& L = H->lv[k];
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
-    const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
+    const int la = lanes_at("RUV_AMG_LANES", k, L.n ? (double)L.nnz / (double)L.n : 1.0);
     if (!L.smoothed) {
 #define CALL(X, UU, KK)                                                                                                \
   k_smooth_up_t<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
@@ -2356,7 +2375,7 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
       ++launches;
       continue;
     }
-    const int lp = lanes_for(L.n ? (double)L.n_pnnz / (double)L.n : 1.0);
+    const int lp = lanes_at("RUV_AMG_TLANES", k, L.n ? (double)L.n_pnnz / (double)L.n : 1.0);
 #define CALL(X, UU, KK)                                                                                                  \
   k_prolong_add<NR, X, UU, KK><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.poff, L.pc, L.pv, C.x, L.x, L.y, 1.0f)
     RUV_LPR_SWITCH(lp, CALL)
