@@ -1773,7 +1773,7 @@ void stage_attributes_nw() {
                                 (int)kStageMaxSmem));                                                            \
   RUV_CUDA(cudaFuncSetAttribute(k_smooth_up_st<NR, X, UU, KK, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                                 (int)kStageMaxSmem));
-  A(1, 4, 2) A(2, 2, 4) A(4, 2, 4) A(8, 2, 4) A(16, 1, 4)
+  A(1, 4, 2) A(1, 2, 8) A(1, 4, 4) A(2, 2, 4) A(4, 2, 4) A(8, 2, 4) A(16, 1, 4)
 #undef A
 }
 
@@ -2282,10 +2282,47 @@ namespace {
 // typical row in one sweep with two rows in flight (8 independent gathers per lane).
 int lanes_for(double avg) { return avg <= 1.5 ? 1 : avg <= 8 ? 2 : avg <= 16 ? 4 : avg <= 32 ? 8 : 16; }
 
+// Lanes per row of the smoothers' operator rows (A's row length): fewer lanes than the transfer
+// rule, more rows per warp.  On the 4096-disk hierarchy (levels of 6.9, 15.8, 24.0 and 10.8
+// entries per row) one lane per row at level 0 ran the step 1.1 ms faster than two, two lanes
+// at levels 1 and 2 each 0.4 ms faster than four and eight, with the same iterations.
+// (RUV_AMG_SMOOTH_LANES=0: the transfer rule instead.)
+int smoother_lanes(double avg) {
+  const char* e = std::getenv("RUV_AMG_SMOOTH_LANES");
+  if (e && e[0] == '0') return lanes_for(avg);
+  return avg <= 8 ? 1 : avg <= 32 ? 2 : avg <= 64 ? 4 : avg <= 128 ? 8 : 16;
+}
+
+// Shape of the one-lane smoothers (RUV_AMG_L1SHAPE): 0 = 4 rows in flight x 2 slots, 1 = 2 x 8,
+// 2 = 4 x 4.
+int lane1_shape() {
+  const char* e = std::getenv("RUV_AMG_L1SHAPE");
+  const int v = e ? std::atoi(e) : 0;
+  return v >= 0 && v <= 2 ? v : 0;
+}
+
+#define RUV_SMOOTH_SWITCH(lpr, CALL) \
+  switch (lpr) {                    \
+    case 1:                         \
+      if (l1s == 1) {               \
+        CALL(1, 2, 8);              \
+      } else if (l1s == 2) {        \
+        CALL(1, 4, 4);              \
+      } else {                      \
+        CALL(1, 4, 2);              \
+      }                             \
+      break;                        \
+    case 2: CALL(2, 2, 4); break;   \
+    case 4: CALL(4, 2, 4); break;   \
+    case 8: CALL(8, 2, 4); break;   \
+    default: CALL(16, 1, 4); break; \
+  }
+
 // The same with a per-level override: the k-th entry of the list in `knob`, entries separated
 // by ',' or '/' (RUV_AMG_LANES for the smoothers, RUV_AMG_TLANES for restriction and
-// prolongation; 0 or a missing entry: from the row length; only 1, 2, 4, 8 and 16 are taken).
-int lanes_at(const char* knob, int k, double avg) {
+// prolongation; 0 or a missing entry: from the row length by `rule`; only 1, 2, 4, 8 and 16
+// are taken).
+int lanes_at(const char* knob, int k, double avg, int (*rule)(double) = lanes_for) {
   if (const char* e = std::getenv(knob)) {
     int i = 0;
     for (const char* q = e; *q; ++i) {
@@ -2298,7 +2335,7 @@ int lanes_at(const char* knob, int k, double avg) {
       if (*q) ++q;
     }
   }
-  return lanes_for(avg);
+  return rule(avg);
 }
 
 #define RUV_LPR_SWITCH(lpr, CALL) \
@@ -2314,6 +2351,7 @@ int lanes_at(const char* knob, int k, double avg) {
 template <int NR>
 int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
   cudaStream_t s = ctx.stream;
+  const int l1s = lane1_shape();
   const int K = (int)H->lv.size();
   const int B = kAmgThreads;
   int launches = 0;
@@ -2321,7 +2359,7 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
     AmgLevelDev& L = H->lv[k];
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
-    const int la = lanes_at("RUV_AMG_LANES", k, L.n ? (double)L.nnz / (double)L.n : 1.0);
+    const int la = lanes_at("RUV_AMG_LANES", k, L.n ? (double)L.nnz / (double)L.n : 1.0, smoother_lanes);
     float* xpre = L.smoothed ? L.x : nullptr;  // the tentative cycle re-forms it on the way up
 #define CALL(X, UU, KK)                                                                                                \
   if (L.stage_smem)                                                                                                    \
@@ -2332,13 +2370,13 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
                                                                       L.dinv, L.b, xpre, L.t)
     if (L.c16 && L.rowrel) {
       constexpr int NW = 2;
-      RUV_LPR_SWITCH(la, CALL)
+      RUV_SMOOTH_SWITCH(la, CALL)
     } else if (L.c16) {
       constexpr int NW = 1;
-      RUV_LPR_SWITCH(la, CALL)
+      RUV_SMOOTH_SWITCH(la, CALL)
     } else {
       constexpr int NW = 0;
-      RUV_LPR_SWITCH(la, CALL)
+      RUV_SMOOTH_SWITCH(la, CALL)
     }
 #undef CALL
     ++launches;
@@ -2356,20 +2394,20 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
     AmgLevelDev& L = H->lv[k];
     AmgLevelDev& C = H->lv[k + 1];
     if (L.cont.n == 0) continue;
-    const int la = lanes_at("RUV_AMG_LANES", k, L.n ? (double)L.nnz / (double)L.n : 1.0);
+    const int la = lanes_at("RUV_AMG_LANES", k, L.n ? (double)L.nnz / (double)L.n : 1.0, smoother_lanes);
     if (!L.smoothed) {
 #define CALL(X, UU, KK)                                                                                                \
   k_smooth_up_t<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                     L.dinv, L.b, L.agg, C.x, H->alpha_c, L.x)
       if (L.c16 && L.rowrel) {
         constexpr int NW = 2;
-        RUV_LPR_SWITCH(la, CALL)
+        RUV_SMOOTH_SWITCH(la, CALL)
       } else if (L.c16) {
         constexpr int NW = 1;
-        RUV_LPR_SWITCH(la, CALL)
+        RUV_SMOOTH_SWITCH(la, CALL)
       } else {
         constexpr int NW = 0;
-        RUV_LPR_SWITCH(la, CALL)
+        RUV_SMOOTH_SWITCH(la, CALL)
       }
 #undef CALL
       ++launches;
@@ -2389,13 +2427,13 @@ int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
                                                                     L.dinv, L.b, L.y, L.x)
     if (L.c16 && L.rowrel) {
       constexpr int NW = 2;
-      RUV_LPR_SWITCH(la, CALL)
+      RUV_SMOOTH_SWITCH(la, CALL)
     } else if (L.c16) {
       constexpr int NW = 1;
-      RUV_LPR_SWITCH(la, CALL)
+      RUV_SMOOTH_SWITCH(la, CALL)
     } else {
       constexpr int NW = 0;
-      RUV_LPR_SWITCH(la, CALL)
+      RUV_SMOOTH_SWITCH(la, CALL)
     }
 #undef CALL
     launches += 2;
@@ -2418,19 +2456,20 @@ int kform(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k) {
   AmgLevelDev& L = H->lv[k];
   AmgLevelDev& C = H->lv[k + 1];
   int launches = 0;
-  const int la = lanes_for(L.n ? (double)L.nnz / (double)L.n : 1.0);
+  const int l1s = lane1_shape();
+  const int la = lanes_at("RUV_AMG_LANES", k, L.n ? (double)L.nnz / (double)L.n : 1.0, smoother_lanes);
 #define CALL(X, UU, KK)                                                                                                \
   k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \
                                                                     L.dinv, L.b, L.x, L.t)
   if (L.c16 && L.rowrel) {
     constexpr int NW = 2;
-    RUV_LPR_SWITCH(la, CALL)
+    RUV_SMOOTH_SWITCH(la, CALL)
   } else if (L.c16) {
     constexpr int NW = 1;
-    RUV_LPR_SWITCH(la, CALL)
+    RUV_SMOOTH_SWITCH(la, CALL)
   } else {
     constexpr int NW = 0;
-    RUV_LPR_SWITCH(la, CALL)
+    RUV_SMOOTH_SWITCH(la, CALL)
   }
 #undef CALL
   ++launches;
@@ -2451,13 +2490,13 @@ int kform(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k) {
                                                               L.t, L.w, L.kpart)
     if (L.c16 && L.rowrel) {
       constexpr int NW = 2;
-      RUV_LPR_SWITCH(la, CALL)
+      RUV_SMOOTH_SWITCH(la, CALL)
     } else if (L.c16) {
       constexpr int NW = 1;
-      RUV_LPR_SWITCH(la, CALL)
+      RUV_SMOOTH_SWITCH(la, CALL)
     } else {
       constexpr int NW = 0;
-      RUV_LPR_SWITCH(la, CALL)
+      RUV_SMOOTH_SWITCH(la, CALL)
     }
 #undef CALL
     k_kbeta<<<(unsigned)H->n_charts, 128, 0, s>>>(done, L.cont_chart_tile, L.kpart, L.kbeta);
