@@ -95,6 +95,9 @@ def parse():
                          "list of NAME=VALUE environment variables (RUV_UPLOAD_PARTS, RUV_H2D_GRID, RUV_D2H_GRID, "
                          "RUV_H2D_KERNEL): the e2e call timed --steps times per setting after --warmup untimed "
                          "calls, one JSON line per setting, then the device-resident solve; nothing else runs")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="with --step-sweep: keep the context's SpMV shape (RUV_LPR / RUV_UNROLL / RUV_TILE_ROWS or "
+                         "the default) instead of autotuning it first")
     ap.add_argument("--step-sweep", default="",
                     help="the same form of settings (any RUV_* variable the library reads per call): the "
                          "device-resident solve timed --steps times per setting after --warmup untimed solves, one "
@@ -125,7 +128,9 @@ def step_sweep(args, local):
     stats = (R.RuvChartStat * max(batch.n_charts, 1))()
     for _ in range(2):
         R.solve_batch(ctx, batch, opts, nv)
-    R.autotune(ctx, prec, reps=5)
+    tuned = None if args.no_autotune else R.autotune(ctx, prec, reps=5)
+    print(json.dumps({"spmv_shape_autotuned": list(tuned) if tuned else None,
+                      "bulk_copy_staging": bool(R.spmv_form(ctx))}), flush=True)
     ctx.check(L.ruv_lscm_upload(ctx.h, ctypes.byref(batch)), "upload")
     uv = np.empty((nv, 2), np.float64)
     first = None

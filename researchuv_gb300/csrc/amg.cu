@@ -1773,7 +1773,7 @@ void stage_attributes_nw() {
                                 (int)kStageMaxSmem));                                                            \
   RUV_CUDA(cudaFuncSetAttribute(k_smooth_up_st<NR, X, UU, KK, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                                 (int)kStageMaxSmem));
-  A(1, 4, 2) A(1, 2, 8) A(1, 4, 4) A(2, 2, 4) A(4, 2, 4) A(8, 2, 4) A(16, 1, 4)
+  A(1, 4, 2) A(1, 2, 8) A(2, 2, 4) A(4, 2, 4) A(8, 2, 4) A(16, 1, 4)
 #undef A
 }
 
@@ -2285,7 +2285,8 @@ int lanes_for(double avg) { return avg <= 1.5 ? 1 : avg <= 8 ? 2 : avg <= 16 ? 4
 // Lanes per row of the smoothers' operator rows (A's row length): fewer lanes than the transfer
 // rule, more rows per warp.  On the 4096-disk hierarchy (levels of 6.9, 15.8, 24.0 and 10.8
 // entries per row) one lane per row at level 0 ran the step 1.1 ms faster than two, two lanes
-// at levels 1 and 2 each 0.4 ms faster than four and eight, with the same iterations.
+// at levels 1 and 2 each 0.4 ms faster than four and eight, all together 1.6 ms (2048^2 field:
+// 6.4 ms), with the same iterations.
 // (RUV_AMG_SMOOTH_LANES=0: the transfer rule instead.)
 int smoother_lanes(double avg) {
   const char* e = std::getenv("RUV_AMG_SMOOTH_LANES");
@@ -2293,12 +2294,12 @@ int smoother_lanes(double avg) {
   return avg <= 8 ? 1 : avg <= 32 ? 2 : avg <= 64 ? 4 : avg <= 128 ? 8 : 16;
 }
 
-// Shape of the one-lane smoothers (RUV_AMG_L1SHAPE): 0 = 4 rows in flight x 2 slots, 1 = 2 x 8,
-// 2 = 4 x 4.
+// Shape of the one-lane smoothers (RUV_AMG_L1SHAPE): 1 (default) = 2 rows in flight x 8
+// slots, 0 = 4 x 2.  One lane sums its row in entry order whatever the shape, so both give
+// the same bits; on the 4096 disks 2 x 8 ran the step 0.4 ms faster (4 x 4 was 2.5 ms slower).
 int lane1_shape() {
   const char* e = std::getenv("RUV_AMG_L1SHAPE");
-  const int v = e ? std::atoi(e) : 0;
-  return v >= 0 && v <= 2 ? v : 0;
+  return e && e[0] == '0' ? 0 : 1;
 }
 
 #define RUV_SMOOTH_SWITCH(lpr, CALL) \
@@ -2306,8 +2307,6 @@ int lane1_shape() {
     case 1:                         \
       if (l1s == 1) {               \
         CALL(1, 2, 8);              \
-      } else if (l1s == 2) {        \
-        CALL(1, 4, 4);              \
       } else {                      \
         CALL(1, 4, 2);              \
       }                             \

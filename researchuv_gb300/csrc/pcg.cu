@@ -1336,7 +1336,7 @@ struct Shape {
   int lpr, unroll;
 };
 
-#define RUV_SHAPES(X) X(2, 2) X(2, 4) X(4, 1) X(4, 2) X(4, 4) X(8, 1) X(8, 2) X(8, 4) X(16, 1) X(32, 1)
+#define RUV_SHAPES(X) X(1, 2) X(2, 2) X(2, 4) X(4, 1) X(4, 2) X(4, 4) X(8, 1) X(8, 2) X(8, 4) X(16, 1) X(32, 1)
 
 template <class S, int NR>
 void dispatch_pcg(Shape sh, Ctx& ctx, DevSystem& sys, double* x64, const SolveOpts& o, Tiles T, ChartState* st,
