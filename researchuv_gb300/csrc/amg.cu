@@ -54,6 +54,24 @@ constexpr int kPMaxRow = 4;
 constexpr int kSaLevels = 2;
 constexpr int64_t kLevelTile = 1024;  // rows per CTA tile in the V-cycle kernels
 
+// Rows per V-cycle tile of level k: the k-th entry of RUV_AMG_TILE (entries separated by ',' or
+// '/'; 0 or missing: kLevelTile; 64 to 65536 taken).
+int64_t level_tile_rows(int k) {
+  if (const char* e = std::getenv("RUV_AMG_TILE")) {
+    int i = 0;
+    for (const char* q = e; *q; ++i) {
+      const long long v = std::atoll(q);
+      if (i == k) {
+        if (v >= 64 && v <= 65536) return v;
+        break;
+      }
+      while (*q && *q != ',' && *q != '/') ++q;
+      if (*q) ++q;
+    }
+  }
+  return kLevelTile;
+}
+
 __device__ __forceinline__ int64_t find_chart64(const int64_t* off, int64_t n_charts, int64_t i) {
   int64_t lo = 0, hi = n_charts;
   while (hi - lo > 1) {
@@ -2116,15 +2134,16 @@ AmgHierarchy* amg_setup(Ctx& ctx, const DevSystem& sys, bool smooth, std::string
   for (int k = 0; k < K; ++k) {
     AmgLevelDev& L = H->lv[k];
     const std::string tag = "amg.v" + std::to_string(k);
+    const int64_t tile = level_tile_rows(k);
     for (int which = 0; which < 2; ++which) {
       std::vector<int64_t> tab, ctile(NC + 1, 0);
       std::vector<int32_t> tch;
       for (int64_t c = 0; c < NC; ++c) {
         ctile[c] = (int64_t)tch.size();
         if (which == 0 && !(H->h_final[c] > k)) continue;
-        for (int64_t a0 = L.h_chart_row[c]; a0 < L.h_chart_row[c + 1]; a0 += kLevelTile) {
+        for (int64_t a0 = L.h_chart_row[c]; a0 < L.h_chart_row[c + 1]; a0 += tile) {
           tab.push_back(a0);
-          tab.push_back(std::min(a0 + kLevelTile, L.h_chart_row[c + 1]));
+          tab.push_back(std::min(a0 + tile, L.h_chart_row[c + 1]));
           tch.push_back((int32_t)c);
         }
       }
