@@ -52,10 +52,15 @@ constexpr int kPMaxRow = 4;
 // the measured workloads (4096 disks: 91.7 ms against 91.3 with all levels smoothed; the 2048^2
 // height field: 129 ms against 180 with all, 146 with plain aggregation)
 constexpr int kSaLevels = 2;
-constexpr int64_t kLevelTile = 1024;  // rows per CTA tile in the V-cycle kernels
+// Rows per CTA tile in the V-cycle kernels: 2048 on level 0, 512 on the coarser levels.  On
+// the 4096 disks (step, 8 steps per setting, 1024 everywhere = 92.45 ms): level 0 at 2048
+// -0.44 ms, at 512 +1.7 ms; levels 1-3 at 512 -0.88 ms, at 256 -0.58 ms, at 2048 +1.1 ms;
+// level 0 at 2048 with levels 1-3 at 256 -1.02 ms.  Smaller coarse tiles spread the coarse
+// levels' few rows per chart over more SMs; level 0 keeps its rows streaming longer per CTA.
+constexpr int64_t kLevelTile0 = 2048, kLevelTile = 512;
 
 // Rows per V-cycle tile of level k: the k-th entry of RUV_AMG_TILE (entries separated by ',' or
-// '/'; 0 or missing: kLevelTile; 64 to 65536 taken).
+// '/'; 0 or missing: the default above; 64 to 65536 taken).
 int64_t level_tile_rows(int k) {
   if (const char* e = std::getenv("RUV_AMG_TILE")) {
     int i = 0;
@@ -69,7 +74,7 @@ int64_t level_tile_rows(int k) {
       if (*q) ++q;
     }
   }
-  return kLevelTile;
+  return k == 0 ? kLevelTile0 : kLevelTile;
 }
 
 __device__ __forceinline__ int64_t find_chart64(const int64_t* off, int64_t n_charts, int64_t i) {

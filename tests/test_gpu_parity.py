@@ -395,11 +395,14 @@ def test_pinned_inputs_bitwise(monkeypatch, kernel, parts):
 
 def test_staged_smoothers_bitwise(monkeypatch):
     """Level 0's AMG smoothers with their tiles staged into shared memory by bulk copies
-    (RUV_AMG_STAGE=1) run the same row loop: bitwise the same UVs and iterations."""
+    (RUV_AMG_STAGE=1) run the same row loop: bitwise the same UVs and iterations.  Level 0's
+    tiles at 1024 rows, whose staged rows always fit the 100 KB cap (at the default 2048 the
+    largest tiles may not, and the smoothers then stay unstaged)."""
     vo, to, p3, tr = W.disks(24, t_min=200, t_max=20000, seed=61)
     C = R.prepare_patches(vo, to, p3, tr)
     ctx = R.Context(0)
     opts = R.UnfoldOptions(precond=R.Precond.AMG_SA, precision=R.Precision.MIXED)
+    monkeypatch.setenv("RUV_AMG_TILE", "1024")
     monkeypatch.setenv("RUV_AMG_STAGE", "0")
     plain = R.unfold_charts(ctx, C, opts)
     monkeypatch.setenv("RUV_AMG_STAGE", "1")
