@@ -59,21 +59,25 @@ constexpr int kSaLevels = 2;
 // levels' few rows per chart over more SMs; level 0 keeps its rows streaming longer per CTA.
 constexpr int64_t kLevelTile0 = 2048, kLevelTile = 512;
 
-// Rows per V-cycle tile of level k: the k-th entry of RUV_AMG_TILE (entries separated by ',' or
-// '/'; 0 or missing: the default above; 64 to 65536 taken).
-int64_t level_tile_rows(int k) {
-  if (const char* e = std::getenv("RUV_AMG_TILE")) {
-    int i = 0;
-    for (const char* q = e; *q; ++i) {
-      const long long v = std::atoll(q);
-      if (i == k) {
-        if (v >= 64 && v <= 65536) return v;
-        break;
-      }
-      while (*q && *q != ',' && *q != '/') ++q;
-      if (*q) ++q;
-    }
+// The k-th entry of the per-level list in the environment variable `knob` (entries separated
+// by ',' or '/'), or 0 where the variable or its k-th entry is missing.
+long long env_level_entry(const char* knob, int k) {
+  const char* e = std::getenv(knob);
+  if (!e) return 0;
+  int i = 0;
+  for (const char* q = e; *q; ++i) {
+    if (i == k) return std::atoll(q);
+    while (*q && *q != ',' && *q != '/') ++q;
+    if (*q) ++q;
   }
+  return 0;
+}
+
+// Rows per V-cycle tile of level k: the k-th entry of RUV_AMG_TILE (0 or missing: the default
+// above; 64 to 65536 taken).
+int64_t level_tile_rows(int k) {
+  const long long v = env_level_entry("RUV_AMG_TILE", k);
+  if (v >= 64 && v <= 65536) return v;
   return k == 0 ? kLevelTile0 : kLevelTile;
 }
 
@@ -2341,23 +2345,12 @@ int lane1_shape() {
     default: CALL(16, 1, 4); break; \
   }
 
-// The same with a per-level override: the k-th entry of the list in `knob`, entries separated
-// by ',' or '/' (RUV_AMG_LANES for the smoothers, RUV_AMG_TLANES for restriction and
-// prolongation; 0 or a missing entry: from the row length by `rule`; only 1, 2, 4, 8 and 16
-// are taken).
+// The same with a per-level override: the k-th entry of the list in `knob` (RUV_AMG_LANES for
+// the smoothers, RUV_AMG_TLANES for restriction and prolongation; 0 or a missing entry: from
+// the row length by `rule`; only 1, 2, 4, 8 and 16 are taken).
 int lanes_at(const char* knob, int k, double avg, int (*rule)(double) = lanes_for) {
-  if (const char* e = std::getenv(knob)) {
-    int i = 0;
-    for (const char* q = e; *q; ++i) {
-      const int v = std::atoi(q);
-      if (i == k) {
-        if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) return v;
-        break;
-      }
-      while (*q && *q != ',' && *q != '/') ++q;
-      if (*q) ++q;
-    }
-  }
+  const long long v = env_level_entry(knob, k);
+  if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) return (int)v;
   return rule(avg);
 }
 
