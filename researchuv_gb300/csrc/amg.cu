@@ -1800,7 +1800,7 @@ void stage_attributes_nw() {
                                 (int)kStageMaxSmem));                                                            \
   RUV_CUDA(cudaFuncSetAttribute(k_smooth_up_st<NR, X, UU, KK, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                                 (int)kStageMaxSmem));
-  A(1, 4, 2) A(1, 2, 8) A(2, 2, 4) A(4, 2, 4) A(8, 2, 4) A(16, 1, 4)
+  A(1, 4, 2) A(1, 2, 8) A(2, 2, 4) A(2, 2, 8) A(4, 2, 4) A(8, 2, 4) A(16, 1, 4)
 #undef A
 }
 
@@ -2330,6 +2330,14 @@ int lane1_shape() {
   return e && e[0] == '0' ? 0 : 1;
 }
 
+// Shape of the two-lane smoothers (RUV_AMG_L2SHAPE): 0 (default) = 2 rows in flight x 4 slots
+// per lane, 1 = 2 x 8.  A lane sums its entries (every second one of the row) in entry order
+// whatever the slot count, so both give the same bits.
+int lane2_shape() {
+  const char* e = std::getenv("RUV_AMG_L2SHAPE");
+  return e && e[0] == '1' ? 1 : 0;
+}
+
 #define RUV_SMOOTH_SWITCH(lpr, CALL) \
   switch (lpr) {                    \
     case 1:                         \
@@ -2339,7 +2347,13 @@ int lane1_shape() {
         CALL(1, 4, 2);              \
       }                             \
       break;                        \
-    case 2: CALL(2, 2, 4); break;   \
+    case 2:                         \
+      if (l2s == 1) {               \
+        CALL(2, 2, 8);              \
+      } else {                      \
+        CALL(2, 2, 4);              \
+      }                             \
+      break;                        \
     case 4: CALL(4, 2, 4); break;   \
     case 8: CALL(8, 2, 4); break;   \
     default: CALL(16, 1, 4); break; \
@@ -2367,7 +2381,7 @@ int lanes_at(const char* knob, int k, double avg, int (*rule)(double) = lanes_fo
 template <int NR>
 int vtail(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k0) {
   cudaStream_t s = ctx.stream;
-  const int l1s = lane1_shape();
+  const int l1s = lane1_shape(), l2s = lane2_shape();
   const int K = (int)H->lv.size();
   const int B = kAmgThreads;
   int launches = 0;
@@ -2472,7 +2486,7 @@ int kform(Ctx& ctx, AmgHierarchy* H, const int32_t* done, int k) {
   AmgLevelDev& L = H->lv[k];
   AmgLevelDev& C = H->lv[k + 1];
   int launches = 0;
-  const int l1s = lane1_shape();
+  const int l1s = lane1_shape(), l2s = lane2_shape();
   const int la = lanes_at("RUV_AMG_LANES", k, L.n ? (double)L.nnz / (double)L.n : 1.0, smoother_lanes);
 #define CALL(X, UU, KK)                                                                                                \
   k_smooth_down<NR, X, UU, KK, NW><<<(unsigned)L.cont.n, B, 0, s>>>(L.cont, done, L.rp, L.cols, L.c16, L.cbase, L.vals, \

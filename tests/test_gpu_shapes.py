@@ -65,18 +65,20 @@ def test_autotuner_keeps_an_instantiated_shape(disks):
 def test_smoother_lane_rules_and_one_lane_shapes(monkeypatch, disks):
     """The smoothers' lane rule (one lane per row at level 0) against the transfer rule
     (RUV_AMG_SMOOTH_LANES=0) and per-level overrides: all on the LU bar with the same CG
-    iterations; the two one-lane shapes (RUV_AMG_L1SHAPE 1 and 0) bit for bit."""
+    iterations; the two one-lane shapes (RUV_AMG_L1SHAPE 1 and 0) and the two two-lane shapes
+    (RUV_AMG_L2SHAPE 0 and 1) bit for bit."""
     C, ref = disks
     ctx = R.Context(0)
     opts = R.UnfoldOptions(precond=R.Precond.AMG_SA)
     base = R.unfold_charts(ctx, C, opts)
     _check(base, ref)
-    monkeypatch.setenv("RUV_AMG_L1SHAPE", "0")
-    other = R.unfold_charts(ctx, C, opts)
-    for a, b in zip(base, other):
-        assert a.cg_iters == b.cg_iters
-        assert np.array_equal(a.uv, b.uv)
-    monkeypatch.delenv("RUV_AMG_L1SHAPE")
+    for knob, v in (("RUV_AMG_L1SHAPE", "0"), ("RUV_AMG_L2SHAPE", "1")):
+        monkeypatch.setenv(knob, v)
+        other = R.unfold_charts(ctx, C, opts)
+        for a, b in zip(base, other):
+            assert a.cg_iters == b.cg_iters
+            assert np.array_equal(a.uv, b.uv)
+        monkeypatch.delenv(knob)
     for env in ({"RUV_AMG_SMOOTH_LANES": "0"}, {"RUV_AMG_LANES": "2/4/16/1"}, {"RUV_AMG_TLANES": "1,8"}):
         for k, v in env.items():
             monkeypatch.setenv(k, v)
