@@ -2332,7 +2332,8 @@ int lane1_shape() {
 
 // Shape of the two-lane smoothers (RUV_AMG_L2SHAPE): 0 (default) = 2 rows in flight x 4 slots
 // per lane, 1 = 2 x 8.  A lane sums its entries (every second one of the row) in entry order
-// whatever the slot count, so both give the same bits.
+// whatever the slot count, so both give the same bits; 2 x 8 ran the 4096-disk step 0.43 ms
+// slower.
 int lane2_shape() {
   const char* e = std::getenv("RUV_AMG_L2SHAPE");
   return e && e[0] == '1' ? 1 : 0;
