@@ -57,7 +57,7 @@ L2_BYTES = 129 * 1024 * 1024
 L2_NOTE = "inputs larger than L2 (operator and vectors of a step ~1 GB or more)"
 # DRAM bytes (read + write) per algorithmic byte of the batched SpMV kernel, from one ncu
 # capture of its first launch on the 1024-disk operator with the 16-bit column stream
-# (198.6 MB of traffic for 256.9 MB of algorithmic bytes; profiles/kernels_disks1024_dram.md).
+# (198.6 MB of traffic for 256.9 MB of algorithmic bytes).
 # The disk workloads scale by count, so the traffic of a launch on the 4096-disk operator is
 # this ratio times its algorithmic bytes.
 SPMV_DRAM_PER_ALG_BYTE = 0.773
@@ -105,6 +105,25 @@ def parse():
     return ap.parse_args()
 
 
+def sweep_settings(text):
+    """The settings of --e2e-sweep / --step-sweep: settings separated by ';', each a
+    comma-separated list of NAME=VALUE environment variables (values may hold '/', not ',')."""
+    out = []
+    for setting in text.split(";"):
+        if not setting.strip():
+            continue
+        env = {}
+        for kv in setting.split(","):
+            if not kv.strip():
+                continue
+            if "=" not in kv:
+                raise ValueError(f"sweep setting {kv!r} is not NAME=VALUE")
+            k, v = kv.split("=", 1)
+            env[k.strip()] = v.strip()
+        out.append(env)
+    return out
+
+
 def step_sweep(args, local):
     """The device-resident solve under each setting of the library's environment variables:
     device time per step from the call's CUDA events (median, mean), its phases and the CG
@@ -134,8 +153,7 @@ def step_sweep(args, local):
     ctx.check(L.ruv_lscm_upload(ctx.h, ctypes.byref(batch)), "upload")
     uv = np.empty((nv, 2), np.float64)
     first = None
-    for setting in [x for x in args.step_sweep.split(";") if x.strip()]:
-        env = dict(kv.split("=", 1) for kv in setting.split(",") if kv.strip())
+    for env in sweep_settings(args.step_sweep):
         saved = {k: os.environ.get(k) for k in env}
         os.environ.update(env)
         for _ in range(max(args.warmup, 1)):
@@ -192,8 +210,7 @@ def e2e_sweep(args, local):
     uv = R.pinned_empty(ctx, (nv, 2), np.float64)
     ptr = uv.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     first = None
-    for setting in [x for x in args.e2e_sweep.split(";") if x.strip()]:
-        env = dict(kv.split("=", 1) for kv in setting.split(",") if kv.strip())
+    for env in sweep_settings(args.e2e_sweep):
         saved = {k: os.environ.get(k) for k in env}
         os.environ.update(env)
         for _ in range(max(args.warmup, 1)):
